@@ -1,0 +1,190 @@
+"""Python host binding of the GB300 ray-tracing library (libatlas_rt.so).
+
+Mirrors the engine's host interface for the software ray-tracing path:
+
+* :class:`BVH` -- ``Volume::BVH`` (src/engine/volume/BVH.h:114-138): built
+  from triangles or AABBs, exposing ``nodes`` (GPUBVHNode layout), the
+  flattened primitive ``order`` (``BVHTriangle::idx``) and leaf flags, and the
+  ``GPUBVHTriangle`` packing of ``MeshData::BuildBVH``.
+* :class:`Context` -- device context: mesh uploads (``Mesh::BuildBVH``'s
+  buffers) and the batched GPU ray queries ``trace_closest`` / ``trace_any``
+  (shader ``HitClosest`` / ``HitAny``; the GPU form of
+  ``BVH::GetIntersection`` / ``GetIntersectionAny``).
+
+Buffers may be numpy arrays (host memory; copied in and out by the library)
+or CUDA tensors / raw device pointers (asynchronous on the given stream).
+Every call goes through the C ABI; nothing here computes results itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._native import AeRtError, Config, lib
+
+NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
+                       ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
+                       ("leftPtr", "<i4"), ("rightPtr", "<i4"), ("padding", "<i4", 2)])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("triPtr", "<i4"), ("instance", "<i4"), ("flags", "<u4"),
+                      ("u", "<f4"), ("v", "<f4"), ("tSecond", "<f4"), ("reserved", "<i4")])
+assert NODE_DTYPE.itemsize == 64 and HIT_DTYPE.itemsize == 32
+
+HIT_FLAG_HIT = 0x1
+HIT_FLAG_NEAR_TIE = 0x2
+HIT_FLAG_OVERFLOW = 0x4
+HIT_FLAG_ITER_CAP = 0x8
+
+MASK_ALL = 1 << 7
+MASK_SHADOW = 1 << 6
+CFG_COUNT_FETCHES = 0x1
+
+
+def _check(status: int, ctx=None):
+    if status != 0:
+        msg = ""
+        if ctx is not None:
+            raw = lib().ae_rt_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise AeRtError(status, msg)
+
+
+def _ptr(x):
+    """Raw address of a numpy array, a CUDA tensor or an integer pointer."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("buffer must be C-contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_contiguous") and not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(x)!r}")
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class BVH:
+    """Host BVH with the reference builder's output layout (``Volume::BVH``)."""
+
+    def __init__(self, verts=None, aabbs=None, parallel: bool = True, *, boxes_only=None):
+        L = lib()
+        h = C.c_void_p()
+        if boxes_only is not None:
+            b = np.ascontiguousarray(boxes_only, np.float32).reshape(-1, 6)
+            self.n_input = len(b)
+            _check(L.ae_bvh_build_aabbs(_ptr(b) if len(b) else None, len(b), int(parallel), C.byref(h)))
+            self._verts = None
+        else:
+            v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+            a = None if aabbs is None else np.ascontiguousarray(aabbs, np.float32).reshape(-1, 6)
+            self.n_input = len(v)
+            _check(L.ae_bvh_build_triangles(_ptr(v) if len(v) else None, _ptr(a), len(v), int(parallel),
+                                            C.byref(h)))
+            self._verts = v
+        self._h = h
+        nn = L.ae_bvh_node_count(h)
+        npr = L.ae_bvh_primitive_count(h)
+        self.nodes = np.zeros(nn, NODE_DTYPE)
+        _check(L.ae_bvh_get_nodes(h, _ptr(self.nodes) if nn else None))
+        self.order = np.zeros(npr, np.uint32)
+        self.end_of_node = np.zeros(npr, np.uint8)
+        if npr:
+            _check(L.ae_bvh_get_order(h, _ptr(self.order), _ptr(self.end_of_node)))
+
+    def pack_triangles(self, material=None, opacity=None) -> np.ndarray:
+        """GPUBVHTriangle array (n, 12) float32 in BVH order (MeshData.cpp:241-248)."""
+        out = np.zeros((len(self.order), 12), np.float32)
+        m = None if material is None else np.ascontiguousarray(material, np.int32)
+        o = None if opacity is None else np.ascontiguousarray(opacity, np.float32)
+        if len(self.order):
+            _check(lib().ae_bvh_pack_triangles(self._h, _ptr(self._verts), _ptr(m), _ptr(o), _ptr(out)))
+        return out
+
+    @property
+    def nodes_f32(self) -> np.ndarray:
+        return self.nodes.view(np.float32).reshape(-1, 16)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().ae_bvh_destroy(h)
+            self._h = None
+
+
+class Context:
+    """Device context of the library (``ae_rt_ctx``)."""
+
+    def __init__(self, device: int = 0, count_fetches: bool = False, blocks_per_sm: int = 0,
+                 max_steps: int = 0):
+        cfg = Config()
+        cfg.device = device
+        cfg.blocks_per_sm = blocks_per_sm
+        cfg.max_steps = max_steps
+        cfg.reserved[0] = CFG_COUNT_FETCHES if count_fetches else 0
+        h = C.c_void_p()
+        _check(lib().ae_rt_ctx_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ae_rt_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload_mesh(self, nodes, bvh_tris, shading=None) -> int:
+        nodes = np.ascontiguousarray(nodes)
+        bvh_tris = np.ascontiguousarray(bvh_tris, np.float32)
+        n_nodes = nodes.nbytes // 64
+        n_tris = bvh_tris.nbytes // 48
+        mid = C.c_int32(-1)
+        _check(lib().ae_rt_mesh_upload(self._h, _ptr(nodes) if n_nodes else None, n_nodes,
+                                       _ptr(bvh_tris) if n_tris else None,
+                                       _ptr(shading), n_tris, C.byref(mid)), self._h)
+        return mid.value
+
+    def trace_closest(self, mesh: int, rays, tmin: float, tmax: float, out=None, stream=None,
+                      n_rays: int | None = None):
+        """rays: PackedRay buffer (n, 12) float32 / 48-byte records.  Returns the
+        hit buffer (HIT_DTYPE for host input)."""
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, HIT_DTYPE)
+        _check(lib().ae_rt_trace_closest(self._h, mesh, _ptr(rays), n_rays, tmin, tmax, _ptr(out),
+                                         _stream_handle(stream)), self._h)
+        return out
+
+    def trace_any(self, mesh: int, rays, tmin: float, tmax: float, out=None, stream=None,
+                  n_rays: int | None = None):
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, np.uint8)
+        _check(lib().ae_rt_trace_any(self._h, mesh, _ptr(rays), n_rays, tmin, tmax, _ptr(out),
+                                     _stream_handle(stream)), self._h)
+        return out
+
+    def synchronize(self, stream=None):
+        _check(lib().ae_rt_synchronize(self._h, _stream_handle(stream)), self._h)
+
+    def fetch_counts(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib().ae_rt_get_fetch_counts(self._h, C.byref(a), C.byref(b)), self._h)
+        return a.value, b.value

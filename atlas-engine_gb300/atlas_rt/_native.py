@@ -1,0 +1,73 @@
+"""ctypes declarations of libatlas_rt.so (include/atlas_rt.h).
+
+The library is loaded from this directory only; if it is missing, importing
+fails loudly -- there is no Python or CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libatlas_rt.so"
+
+P = C.c_void_p
+U32 = C.c_uint32
+I32 = C.c_int32
+F32 = C.c_float
+
+STATUS_NAMES = {
+    0: "AE_RT_OK", 1: "AE_RT_INVALID_ARG", 2: "AE_RT_BAD_BVH", 3: "AE_RT_OUT_OF_MEMORY",
+    4: "AE_RT_CUDA_ERROR", 5: "AE_RT_TIMEOUT", 6: "AE_RT_STACK_OVERFLOW",
+    7: "AE_RT_ITERATION_LIMIT", 8: "AE_RT_NO_DEVICE", 9: "AE_RT_NOT_BUILT",
+}
+
+
+class AeRtError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class Config(C.Structure):
+    _fields_ = [("device", I32), ("blocks_per_sm", U32), ("threads_per_block", U32),
+                ("max_steps", U32), ("reserved", U32 * 4)]
+
+
+# (name, restype, argtypes)
+_SIGNATURES = [
+    ("ae_bvh_build_triangles", C.c_int, [P, P, U32, C.c_int, C.POINTER(P)]),
+    ("ae_bvh_build_aabbs", C.c_int, [P, U32, C.c_int, C.POINTER(P)]),
+    ("ae_bvh_destroy", None, [P]),
+    ("ae_bvh_node_count", U32, [P]),
+    ("ae_bvh_primitive_count", U32, [P]),
+    ("ae_bvh_get_nodes", C.c_int, [P, P]),
+    ("ae_bvh_get_order", C.c_int, [P, P, P]),
+    ("ae_bvh_pack_triangles", C.c_int, [P, P, P, P, P]),
+    ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
+    ("ae_rt_ctx_destroy", None, [P]),
+    ("ae_rt_last_error", C.c_char_p, [P]),
+    ("ae_rt_mesh_upload", C.c_int, [P, P, U32, P, P, U32, C.POINTER(I32)]),
+    ("ae_rt_trace_closest", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
+    ("ae_rt_trace_any", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
+    ("ae_rt_synchronize", C.c_int, [P, P]),
+    ("ae_rt_get_fetch_counts", C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+]
+
+EXPORTED = [s[0] for s in _SIGNATURES]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build() "
+                              "(the CUDA library is required, there is no fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, res, args in _SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib

@@ -1,0 +1,335 @@
+// Device context, uploads and trace entry points of the C ABI (include/atlas_rt.h).
+#include "atlas_rt.h"
+#include "trace_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+
+using atlas::rt::dev::TraceParams;
+
+constexpr int kWarps = 4;          // 128 threads per CTA
+constexpr int kSmemStack = 32;     // shared-memory stack entries per lane (the shader's STACK_SIZE)
+constexpr int kSpillStack = 32;    // local-memory entries behind them
+constexpr int kMinBlocks = 8;
+
+template <bool ANY, bool COUNT>
+void* KernelFor() {
+    return reinterpret_cast<void*>(
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, kWarps, kSmemStack, kSpillStack, kMinBlocks>);
+}
+
+struct DeviceMesh {
+    float4* nodes = nullptr;
+    float4* tris = nullptr;
+    float4* shading = nullptr;
+    uint32_t n_nodes = 0;
+    uint32_t n_tris = 0;
+};
+
+// Grow-only device scratch buffer.
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace
+
+struct ae_rt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    uint32_t blocks_per_sm = 0;
+    uint32_t max_steps_cfg = 0;
+    bool count_fetches = false;
+    std::vector<DeviceMesh> meshes;
+    uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
+    unsigned long long* d_fetch = nullptr;
+    Scratch rays_in, results_out;
+    std::string last_error;
+    std::mutex upload_mutex;
+};
+
+namespace {
+
+ae_rt_status Fail(ae_rt_ctx* ctx, ae_rt_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+ae_rt_status CudaFail(ae_rt_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return Fail(ctx, AE_RT_OUT_OF_MEMORY, m);
+    return Fail(ctx, AE_RT_CUDA_ERROR, m);
+}
+
+#define AE_CUDA(ctx, call)                                         \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return CudaFail((ctx), e_, #call);  \
+    } while (0)
+
+// True when the GPU can read `p` directly as device memory.
+bool IsDevicePointer(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Host-side BVH validation before upload: child pointers in range, inner
+// children after their parent (pre-order, which rules out cycles), and every
+// referenced leaf terminated by an end-of-node flag inside the buffer.
+ae_rt_status ValidateBlas(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_t n_nodes,
+                          const ae_bvh_triangle* tris, uint32_t n_tris) {
+    // leafEnd[i] = first index >= i carrying the end flag (n_tris if none)
+    std::vector<uint32_t> leafEnd(n_tris + 1, n_tris);
+    for (int64_t i = int64_t(n_tris) - 1; i >= 0; i--)
+        leafEnd[i] = tris[i].v0[3] > 0.0f ? uint32_t(i) : leafEnd[i + 1];
+    for (uint32_t i = 0; i < n_nodes; i++) {
+        const int32_t ptrs[2] = { nodes[i].leftPtr, nodes[i].rightPtr };
+        for (int32_t ptr : ptrs) {
+            if (ptr >= 0) {
+                if (uint32_t(ptr) >= n_nodes || uint32_t(ptr) <= i)
+                    return Fail(ctx, AE_RT_BAD_BVH, "node " + std::to_string(i) + " has child pointer " +
+                                                    std::to_string(ptr) + " out of range or not after its parent");
+            } else {
+                const uint32_t first = uint32_t(~ptr);
+                if (first >= n_tris)
+                    return Fail(ctx, AE_RT_BAD_BVH, "node " + std::to_string(i) + " points at triangle " +
+                                                    std::to_string(first) + " beyond " + std::to_string(n_tris));
+                if (leafEnd[first] >= n_tris)
+                    return Fail(ctx, AE_RT_BAD_BVH, "leaf starting at triangle " + std::to_string(first) +
+                                                    " has no end-of-node flag");
+            }
+        }
+    }
+    return AE_RT_OK;
+}
+
+uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
+    if (ctx->max_steps_cfg) return ctx->max_steps_cfg;
+    return 4u * m.n_nodes + 64u;
+}
+
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, TraceParams& p, cudaStream_t s) {
+    AE_CUDA(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(uint32_t), s));
+    if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
+    void* fn = any ? (ctx->count_fetches ? KernelFor<true, true>() : KernelFor<true, false>())
+                   : (ctx->count_fetches ? KernelFor<false, true>() : KernelFor<false, false>());
+    // Persistent grid: never more CTAs than can be resident, never more warps than rays.
+    uint32_t grid = uint32_t(ctx->sm_count) * ctx->blocks_per_sm;
+    const uint32_t needed = (p.n_rays + kWarps * 32 - 1) / (kWarps * 32);
+    if (needed < grid) grid = needed;
+    if (grid == 0) grid = 1;
+    void* args[] = { &p };
+    AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kWarps * 32), args, 0, s));
+    return AE_RT_OK;
+}
+
+ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
+                   float tmin, float tmax, void* out, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
+        return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
+    if (n_rays == 0) return AE_RT_OK;
+    if (!rays || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray or result buffer");
+    if (n_rays > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one call");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const DeviceMesh& m = ctx->meshes[size_t(mesh_id)];
+
+    const size_t ray_bytes = size_t(n_rays) * sizeof(ae_packed_ray);
+    const size_t out_bytes = size_t(n_rays) * (any ? 1 : sizeof(ae_hit));
+    const bool rays_dev = IsDevicePointer(rays);
+    const bool out_dev = IsDevicePointer(out);
+
+    const void* d_rays = rays;
+    void* d_out = out;
+    if (!rays_dev) {
+        AE_CUDA(ctx, ctx->rays_in.ensure(ray_bytes));
+        AE_CUDA(ctx, cudaMemcpyAsync(ctx->rays_in.ptr, rays, ray_bytes, cudaMemcpyHostToDevice, s));
+        d_rays = ctx->rays_in.ptr;
+    }
+    if (!out_dev) {
+        AE_CUDA(ctx, ctx->results_out.ensure(out_bytes));
+        d_out = ctx->results_out.ptr;
+    }
+
+    TraceParams p{};
+    p.nodes = m.nodes;
+    p.tris = m.tris;
+    p.n_nodes = m.n_nodes;
+    p.n_tris = m.n_tris;
+    p.rays = static_cast<const float4*>(d_rays);
+    p.n_rays = n_rays;
+    p.tmin = tmin;
+    p.tmax = tmax;
+    p.hits = any ? nullptr : static_cast<float4*>(d_out);
+    p.occluded = any ? static_cast<uint8_t*>(d_out) : nullptr;
+    p.work_counter = ctx->d_counter;
+    p.error_word = ctx->d_counter + 1;
+    p.fetch_counts = ctx->d_fetch;
+    p.max_steps = MaxSteps(ctx, m);
+    ae_rt_status st = Launch(ctx, any, p, s);
+    if (st != AE_RT_OK) return st;
+
+    if (!out_dev) {
+        AE_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s));
+    }
+    if (!out_dev || !rays_dev) return ae_rt_synchronize(ctx, stream);
+    return AE_RT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
+    if (!out) return AE_RT_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return AE_RT_NO_DEVICE;
+    }
+    ae_rt_ctx* ctx = new (std::nothrow) ae_rt_ctx;
+    if (!ctx) return AE_RT_OUT_OF_MEMORY;
+    ae_rt_config c{};
+    if (cfg) c = *cfg;
+    if (c.device < 0 || c.device >= count) {
+        delete ctx;
+        return AE_RT_INVALID_ARG;
+    }
+    ctx->device = c.device;
+    ctx->max_steps_cfg = c.max_steps;
+    ctx->count_fetches = (c.reserved[0] & AE_RT_CFG_COUNT_FETCHES) != 0;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_fetch, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_fetch, 0, 2 * sizeof(unsigned long long));
+    int occ = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(KernelFor<false, false>()),
+                                                          kWarps * 32, 0);
+    if (e != cudaSuccess) {
+        ae_rt_ctx_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? AE_RT_OUT_OF_MEMORY : AE_RT_CUDA_ERROR;
+    }
+    ctx->blocks_per_sm = c.blocks_per_sm ? c.blocks_per_sm : uint32_t(occ > 0 ? occ : 1);
+    *out = ctx;
+    return AE_RT_OK;
+}
+
+void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    for (auto& m : ctx->meshes) {
+        cudaFree(m.nodes);
+        cudaFree(m.tris);
+        cudaFree(m.shading);
+    }
+    cudaFree(ctx->d_counter);
+    cudaFree(ctx->d_fetch);
+    ctx->rays_in.release();
+    ctx->results_out.release();
+    delete ctx;
+}
+
+const char* ae_rt_last_error(const ae_rt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_t n_nodes,
+                               const ae_bvh_triangle* tris, const ae_triangle* shading, uint32_t n_tris,
+                               int32_t* mesh_id) {
+    if (!ctx || !mesh_id) return AE_RT_INVALID_ARG;
+    if ((n_nodes && !nodes) || (n_tris && !tris)) return Fail(ctx, AE_RT_INVALID_ARG, "null mesh buffer");
+    if (n_tris >= (1u << 31) - 1 || n_nodes >= (1u << 31) - 1) return Fail(ctx, AE_RT_INVALID_ARG, "mesh too large");
+    ae_rt_status v = ValidateBlas(ctx, nodes, n_nodes, tris, n_tris);
+    if (v != AE_RT_OK) return v;
+    std::lock_guard<std::mutex> g(ctx->upload_mutex);
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    DeviceMesh m;
+    m.n_nodes = n_nodes;
+    m.n_tris = n_tris;
+    auto upload = [&](float4** dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!bytes) return cudaSuccess;
+        cudaError_t e = cudaMalloc(dst, bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+        return e;
+    };
+    cudaError_t e = upload(&m.nodes, nodes, size_t(n_nodes) * sizeof(ae_bvh_node));
+    if (e == cudaSuccess) e = upload(&m.tris, tris, size_t(n_tris) * sizeof(ae_bvh_triangle));
+    if (e == cudaSuccess && shading) e = upload(&m.shading, shading, size_t(n_tris) * sizeof(ae_triangle));
+    if (e != cudaSuccess) {
+        cudaFree(m.nodes);
+        cudaFree(m.tris);
+        cudaFree(m.shading);
+        return CudaFail(ctx, e, "mesh upload");
+    }
+    *mesh_id = int32_t(ctx->meshes.size());
+    ctx->meshes.push_back(m);
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_trace_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
+                                 float tmin, float tmax, ae_hit* hits, void* stream) {
+    return Trace(ctx, false, mesh_id, rays, n_rays, tmin, tmax, hits, stream);
+}
+
+ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
+                             float tmin, float tmax, uint8_t* occluded, void* stream) {
+    return Trace(ctx, true, mesh_id, rays, n_rays, tmin, tmax, occluded, stream);
+}
+
+ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    AE_CUDA(ctx, cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    uint32_t err = 0;
+    AE_CUDA(ctx, cudaMemcpy(&err, ctx->d_counter + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (err) {
+        AE_CUDA(ctx, cudaMemset(ctx->d_counter + 1, 0, sizeof(uint32_t)));
+        if (err & atlas::rt::dev::kErrStackOverflow)
+            return Fail(ctx, AE_RT_STACK_OVERFLOW, "a ray needed more than " +
+                                                   std::to_string(kSmemStack + kSpillStack) + " stack entries");
+        return Fail(ctx, AE_RT_ITERATION_LIMIT, "a ray exceeded the traversal step cap");
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches) {
+    if (!ctx || !node_fetches || !tri_fetches) return AE_RT_INVALID_ARG;
+    if (!ctx->count_fetches) return Fail(ctx, AE_RT_NOT_BUILT, "context created without AE_RT_CFG_COUNT_FETCHES");
+    unsigned long long h[2] = { 0, 0 };
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    AE_CUDA(ctx, cudaMemcpy(h, ctx->d_fetch, sizeof(h), cudaMemcpyDeviceToHost));
+    *node_fetches = h[0];
+    *tri_fetches = h[1];
+    return AE_RT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,275 @@
+// Persistent wavefront BVH traversal kernels for sm_103a.
+//
+// Semantics: the engine's shader traversal on one BLAS --
+//   HitClosest  data/shader/raytracer/bvh.hsh:191-273 (+ CheckLeafClosest :44-72)
+//   HitAny      data/shader/raytracer/bvh.hsh:359-441 (+ CheckLeaf :74-104)
+//   IntersectAABB / IntersectTriangle  data/shader/raytracer/intersections.hsh:18-57
+// reproduced bit for bit: every multiply, add and divide is an explicitly
+// rounded IEEE operation in the shader's order (no FMA contraction), GLSL
+// min/max are min.f32/max.f32 (a NaN operand loses), the descent goes to the
+// nearer child first (hitL <= hitR) and pushes the farther one.
+//
+// Execution model (not the shader's):
+//  * persistent CTAs, a few per SM; each warp pulls rays from a global
+//    counter.  A lane that finishes its ray takes a fresh one at the next
+//    refill point: the idle lanes are found by a warp ballot and served with
+//    one atomic per warp, so live rays stay packed in the warp;
+//  * the traversal stack of each lane lives in shared memory, lane-interleaved
+//    (entry k of lane l at [k][l], conflict-free), with a local-memory spill
+//    area behind it;
+//  * nodes (4 x 16 B) and triangles (3 x 16 B) are fetched with 128-bit
+//    read-only loads;
+//  * every ray carries a step cap and a stack bound; exceeding either sets a
+//    flag on the ray and in the context's error word instead of faulting.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace atlas::rt::dev {
+
+constexpr uint32_t kErrStackOverflow = 0x1u;
+constexpr uint32_t kErrIterationCap = 0x2u;
+
+constexpr uint32_t kHitFlagHit = 0x1u;
+constexpr uint32_t kHitFlagNearTie = 0x2u;
+constexpr uint32_t kHitFlagOverflow = 0x4u;
+constexpr uint32_t kHitFlagIterCap = 0x8u;
+
+struct TraceParams {
+    const float4* nodes;         // 4 float4 per GPUBVHNode
+    const float4* tris;          // 3 float4 per GPUBVHTriangle
+    uint32_t n_nodes;
+    uint32_t n_tris;
+    const float4* rays;          // 3 float4 per PackedRay
+    uint32_t n_rays;
+    float tmin;
+    float tmax;
+    float4* hits;                // 2 float4 per ae_hit (closest)
+    uint8_t* occluded;           // 1 byte per ray (any)
+    uint32_t* work_counter;      // rays handed out so far (zeroed before launch)
+    uint32_t* error_word;        // kErr* bits
+    unsigned long long* fetch_counts;  // [0] nodes, [1] triangles (optional)
+    uint32_t max_steps;
+};
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// IEEE single operations with explicit rounding (no contraction into FMA).
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// IntersectAABB(ray, aabb, tmin, tmax, out dist) -- intersections.hsh:18-34.
+__device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx, float dy, float dz,
+                                         float lx, float ly, float lz, float hx, float hy, float hz,
+                                         float tmin, float tmax, float& dist) {
+    const float t0x = fdiv(fsub(lx, ox), dx), t0y = fdiv(fsub(ly, oy), dy), t0z = fdiv(fsub(lz, oz), dz);
+    const float t1x = fdiv(fsub(hx, ox), dx), t1y = fdiv(fsub(hy, oy), dy), t1z = fdiv(fsub(hz, oz), dz);
+    const float sx = fminf(t0x, t1x), sy = fminf(t0y, t1y), sz = fminf(t0z, t1z);
+    const float bx = fmaxf(t0x, t1x), by = fmaxf(t0y, t1y), bz = fmaxf(t0z, t1z);
+    const float tminf = fmaxf(fmaxf(tmin, sx), fmaxf(sy, sz));
+    const float tmaxf = fminf(fminf(tmax, bx), fminf(by, bz));
+    const bool hit = tminf <= tmaxf;
+    dist = hit ? tminf : tmax;
+    return hit;
+}
+
+// IntersectTriangle -- intersections.hsh:36-57.  Returns the shader's accept
+// test; (t, u, v) = sol.
+__device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
+                                         const float4& a, const float4& b, const float4& c,
+                                         float& t, float& u, float& v) {
+    const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
+    const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
+    const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
+    // p = cross(s, e0), q = cross(d, e1)
+    const float px = fsub(fmul(sy, e0z), fmul(e0y, sz));
+    const float py = fsub(fmul(sz, e0x), fmul(e0z, sx));
+    const float pz = fsub(fmul(sx, e0y), fmul(e0x, sy));
+    const float qx = fsub(fmul(dy, e1z), fmul(e1y, dz));
+    const float qy = fsub(fmul(dz, e1x), fmul(e1z, dx));
+    const float qz = fsub(fmul(dx, e1y), fmul(e1x, dy));
+    const float den = fadd(fadd(fmul(qx, e0x), fmul(qy, e0y)), fmul(qz, e0z));
+    t = fdiv(fadd(fadd(fmul(px, e1x), fmul(py, e1y)), fmul(pz, e1z)), den);
+    u = fdiv(fadd(fadd(fmul(qx, sx), fmul(qy, sy)), fmul(qz, sz)), den);
+    v = fdiv(fadd(fadd(fmul(px, dx), fmul(py, dy)), fmul(pz, dz)), den);
+    return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Per-lane traversal stack: SMEM entries in shared memory (lane-interleaved),
+// then SPILL entries in local memory.
+template <int SMEM, int SPILL>
+struct LaneStack {
+    int32_t* sh;           // &shared[warp][0][lane]; entry k at sh[k * 32]
+    int32_t spill[SPILL];
+    __device__ __forceinline__ void put(uint32_t k, int32_t v) {
+        if (k < SMEM) sh[k * 32] = v;
+        else spill[k - SMEM] = v;
+    }
+    __device__ __forceinline__ int32_t get(uint32_t k) const {
+        return k < SMEM ? sh[k * 32] : spill[k - SMEM];
+    }
+    static constexpr uint32_t capacity = SMEM + SPILL;
+};
+
+template <bool ANY, bool COUNT, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS>
+__global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
+    __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    constexpr unsigned kFull = 0xffffffffu;
+
+    LaneStack<SMEM_STACK, SPILL_STACK> st;
+    st.sh = &s_stack[warp][0][lane];
+
+    bool live = false;
+    bool queueDry = false;          // warp-uniform
+    uint32_t rid = 0;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
+    float hitDist = 0, second = 0, hu = 0, hv = 0;
+    int32_t hitID = -1;
+    int32_t node = 0;
+    uint32_t sp = 0, steps = 0, flags = 0;
+    bool occl = false;
+    unsigned long long nodeCount = 0, triCount = 0;
+    const float tmin = p.tmin, tmax = p.tmax;
+
+    for (;;) {
+        // ---- refill idle lanes (one atomic per warp) ----
+        if (!queueDry) {
+            const uint32_t idle = __ballot_sync(kFull, !live);
+            if (idle) {
+                const uint32_t leader = __ffs(idle) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(p.work_counter, __popc(idle));
+                base = __shfl_sync(kFull, base, leader);
+                if (base + __popc(idle) >= p.n_rays) queueDry = true;
+                if (!live) {
+                    const uint32_t r = base + __popc(idle & lanemask_lt());
+                    if (r < p.n_rays) {
+                        rid = r;
+                        const float4 o4 = ldg4(p.rays + size_t(r) * 3);
+                        const float4 d4 = ldg4(p.rays + size_t(r) * 3 + 1);
+                        ox = o4.x; oy = o4.y; oz = o4.z;
+                        dx = d4.x; dy = d4.y; dz = d4.z;
+                        hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
+                        hitID = -1; node = 0; sp = 0; steps = 0; flags = 0; occl = false;
+                        live = true;
+                        // NaN direction or an empty BVH: miss (bvh.hsh:204, BVH.cpp:107)
+                        if (isnan(dx) || isnan(dy) || isnan(dz) || p.n_nodes == 0) node = INT32_MIN;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(kFull, live)) break;
+
+        // ---- traverse: a bounded number of steps, then refill again ----
+        if (live) {
+            bool done = node == INT32_MIN;
+            for (int k = 0; k < 64 && !done; k++) {
+                if (++steps > p.max_steps) {
+                    flags |= kHitFlagIterCap;
+                    atomicOr(p.error_word, kErrIterationCap);
+                    done = true;
+                    break;
+                }
+                if (node < 0) {
+                    // Leaf: contiguous triangles up to the end-of-node flag.
+                    int32_t tp = ~node;
+                    bool end = false;
+                    do {
+                        const float4 a = ldg4(p.tris + size_t(tp) * 3);
+                        const float4 b = ldg4(p.tris + size_t(tp) * 3 + 1);
+                        const float4 c = ldg4(p.tris + size_t(tp) * 3 + 2);
+                        end = a.w > 0.0f;
+                        if (COUNT) triCount++;
+                        float t, u, v;
+                        const bool hit = tri_test(ox, oy, oz, dx, dy, dz, a, b, c, t, u, v);
+                        if (ANY) {
+                            if (hit && t > tmin && t < tmax) { occl = true; end = true; }
+                        } else if (hit && t > tmin && t < tmax) {
+                            if (t < hitDist) {
+                                second = hitDist;
+                                hitDist = t; hitID = tp; hu = u; hv = v;
+                            } else if (t < second) {
+                                second = t;
+                            }
+                        }
+                        tp++;
+                    } while (!end);
+                    if (ANY && occl) { done = true; break; }
+                    if (sp == 0) { done = true; break; }
+                    node = st.get(--sp);
+                } else {
+                    const float4* np = p.nodes + size_t(node) * 4;
+                    const float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
+                    if (COUNT) nodeCount++;
+                    const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
+                    const float bound = ANY ? tmax : hitDist;
+                    float hl, hr;
+                    const bool il = box_test(ox, oy, oz, dx, dy, dz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y,
+                                             tmin, bound, hl);
+                    const bool ir = box_test(ox, oy, oz, dx, dy, dz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w,
+                                             tmin, bound, hr);
+                    int32_t next, far;
+                    if (ANY) {
+                        next = il ? lptr : rptr;
+                        far = rptr;
+                    } else {
+                        const bool leftFirst = hl <= hr;
+                        next = leftFirst ? lptr : rptr;
+                        far = leftFirst ? rptr : lptr;
+                    }
+                    if (il && ir) {
+                        if (sp >= st.capacity) {
+                            flags |= kHitFlagOverflow;
+                            atomicOr(p.error_word, kErrStackOverflow);
+                            done = true;
+                            break;
+                        }
+                        st.put(sp++, far);
+                    } else if (!il && !ir) {
+                        if (sp == 0) { done = true; break; }
+                        next = st.get(--sp);
+                    }
+                    node = next;
+                }
+            }
+            if (done) {
+                if (ANY) {
+                    p.occluded[rid] = (occl && !(flags & (kHitFlagOverflow | kHitFlagIterCap))) ? 1 : 0;
+                } else {
+                    const bool hit = hitID >= 0;
+                    uint32_t f = flags | (hit ? kHitFlagHit : 0u);
+                    if (hit && fsub(second, hitDist) <= fmul(1e-6f, hitDist)) f |= kHitFlagNearTie;
+                    float4* hp = p.hits + size_t(rid) * 2;
+                    hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(-1), __uint_as_float(f));
+                    hp[1] = make_float4(hu, hv, second, 0.0f);
+                }
+                live = false;
+            }
+        }
+    }
+
+    if (COUNT) {
+        unsigned long long nc = nodeCount, tc = triCount;
+        for (int off = 16; off > 0; off >>= 1) {
+            nc += __shfl_down_sync(kFull, nc, off);
+            tc += __shfl_down_sync(kFull, tc, off);
+        }
+        if (lane == 0) {
+            atomicAdd(p.fetch_counts, nc);
+            atomicAdd(p.fetch_counts + 1, tc);
+        }
+    }
+}
+
+}  // namespace atlas::rt::dev

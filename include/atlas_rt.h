@@ -1,0 +1,261 @@
+/*
+ * atlas_rt.h -- C ABI of the GB300 ray-tracing library for Atlas Engine.
+ *
+ * Drop-in boundary for the engine's software ray-tracing path: the host BVH
+ * builder and ray query (src/engine/volume/BVH.h:114-138), the GPU buffer
+ * layouts the engine uploads (src/engine/raytracing/RTStructures.h:14-110),
+ * and the traversal / path-tracing dispatches that the engine records today
+ * as Vulkan compute shaders (data/shader/raytracer/bvh.hsh,
+ * src/engine/renderer/helper/RayTracingHelper.cpp).
+ *
+ * Conventions
+ *  - Every struct below is byte-identical to the engine's struct of the same
+ *    role; the engine's host arrays can be passed without repacking.
+ *  - Every call returns ae_rt_status; no C++ exception crosses this boundary.
+ *  - Buffer arguments of trace calls may live in host memory (pageable or
+ *    pinned) or in device memory of the context's GPU.  With device buffers a
+ *    call is asynchronous on `stream` (a cudaStream_t, NULL = the legacy
+ *    default stream); with host buffers it returns after the results have
+ *    been copied back.
+ *  - One context is driven by one host thread at a time; independent
+ *    contexts may be used concurrently.
+ */
+#ifndef ATLAS_RT_H
+#define ATLAS_RT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AE_RT_ABI_VERSION 1
+
+typedef enum ae_rt_status {
+    AE_RT_OK = 0,
+    AE_RT_INVALID_ARG = 1,      /* null pointer, bad id, size out of range */
+    AE_RT_BAD_BVH = 2,          /* the BVH validator rejected an upload */
+    AE_RT_OUT_OF_MEMORY = 3,
+    AE_RT_CUDA_ERROR = 4,       /* a CUDA call failed; see ae_rt_last_error */
+    AE_RT_TIMEOUT = 5,          /* a bounded device wait gave up */
+    AE_RT_STACK_OVERFLOW = 6,   /* a ray needed more traversal stack than configured */
+    AE_RT_ITERATION_LIMIT = 7,  /* a ray exceeded the traversal step cap (cyclic BVH?) */
+    AE_RT_NO_DEVICE = 8,
+    AE_RT_NOT_BUILT = 9         /* the library was built without the requested feature */
+} ae_rt_status;
+
+/* ------------------------------------------------------------------------ */
+/* Engine buffer layouts                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* GPUAABB (RTStructures.h:80-83) */
+typedef struct ae_aabb {
+    float min[3];
+    float max[3];
+} ae_aabb;
+
+/* GPUBVHNode (RTStructures.h:95-103).  Pointer >= 0: inner node index;
+ * pointer < 0: leaf, ~pointer = first triangle (BLAS) or instance (TLAS). */
+typedef struct ae_bvh_node {
+    ae_aabb leftAABB;
+    ae_aabb rightAABB;
+    int32_t leftPtr;
+    int32_t rightPtr;
+    int32_t padding0;
+    int32_t padding1;
+} ae_bvh_node;
+
+/* GPUBVHTriangle (RTStructures.h:23-27), packed by MeshData.cpp:241-248:
+ * v0.w > 0 marks the last triangle of a leaf, v1.w = material index bits,
+ * v2.w = opacity (-1: opacity texture). */
+typedef struct ae_bvh_triangle {
+    float v0[4];
+    float v1[4];
+    float v2[4];
+} ae_bvh_triangle;
+
+/* GPUTriangle (RTStructures.h:14-21), packed by MeshData.cpp:172-239:
+ * v*.w = 10:10:10:2 normal bits, d0 = half2 UVs x3 + material index bits,
+ * d1 = tangent, bitangent, endOfNode (+1/-1), 0; d2 = unorm4x8 colours x3 + opacity. */
+typedef struct ae_triangle {
+    float v0[4];
+    float v1[4];
+    float v2[4];
+    float d0[4];
+    float d1[4];
+    float d2[4];
+} ae_triangle;
+
+/* GPUBVHInstance (RTStructures.h:85-93): mat3x4 (three vec4 columns) holding
+ * the transposed inverse model matrix, so that
+ * objectPos[i] = dot(vec4(worldPos, 1), inverseMatrix[i]). */
+typedef struct ae_bvh_instance {
+    float inverseMatrix[12];
+    int32_t meshOffset;
+    int32_t materialOffset;
+    int32_t nextInstance;
+    uint32_t mask;
+} ae_bvh_instance;
+
+/* GPUMaterial (RTStructures.h:51-78) */
+typedef struct ae_material {
+    int32_t ID;
+    float baseColor[3];
+    float emissiveColor[3];
+    float opacity;
+    float roughness;
+    float metalness;
+    float ao;
+    float reflectance;
+    float normalScale;
+    int32_t invertUVs;
+    int32_t twoSided;
+    int32_t cullBackFaces;
+    int32_t useVertexColors;
+    int32_t baseColorTexture;
+    int32_t opacityTexture;
+    int32_t normalTexture;
+    int32_t roughnessTexture;
+    int32_t metalnessTexture;
+    int32_t aoTexture;
+} ae_material;
+
+/* GPULight (RTStructures.h:105-110): data.x = (type << 28) | triangle index
+ * bits, data.y = selection weight, data.z = area, data.w = instance bits. */
+typedef struct ae_light {
+    float P[4];
+    float N[4];
+    float color[4];
+    float data[4];
+} ae_light;
+
+/* PackedRay (data/shader/raytracer/structures.hsh:9-13): origin.w = ray ID
+ * bits; hit = (t, hitID bits, instance bits, unused). */
+typedef struct ae_packed_ray {
+    float origin[4];
+    float direction[4];
+    float hit[4];
+} ae_packed_ray;
+
+/* Instance cull masks (RTStructures.h:9-12, common.hsh:14-15) */
+#define AE_RT_MASK_ALL    (1u << 7)
+#define AE_RT_MASK_SHADOW (1u << 6)
+
+/* Result of a closest-hit query.  triPtr is the BVH-order triangle index the
+ * shader writes as ray.hitID (bvh.hsh:65); u, v are the barycentric weights
+ * of v1 and v2 (surface.hsh:80-88), which the shader re-derives at shading
+ * time.  tSecond is the second-smallest accepted t the traversal met (used to
+ * flag near ties). */
+typedef struct ae_hit {
+    float t;
+    int32_t triPtr;       /* -1: miss */
+    int32_t instance;     /* -1: miss or single-mesh query */
+    uint32_t flags;       /* AE_HIT_* */
+    float u;
+    float v;
+    float tSecond;
+    int32_t reserved;
+} ae_hit;
+
+#define AE_HIT_HIT       0x1u
+#define AE_HIT_NEAR_TIE  0x2u  /* a second hit lies within 1e-6 relative t */
+#define AE_HIT_OVERFLOW  0x4u  /* traversal stack overflowed; result invalid */
+#define AE_HIT_ITER_CAP  0x8u  /* traversal step cap hit; result invalid */
+
+/* ------------------------------------------------------------------------ */
+/* Host BVH builder -- replaces Volume::BVH::BVH (BVH.cpp:14, :58)           */
+/* ------------------------------------------------------------------------ */
+
+typedef struct ae_bvh ae_bvh;
+
+/* Triangle BVH.  verts: n * 9 floats (v0, v1, v2).  aabbs: optional n * 6
+ * floats (min, max); when NULL each is the triangle's vertex bound, as
+ * MeshData::BuildBVH forms it (MeshData.cpp:143-146).  parallel != 0 builds
+ * sub-trees on worker threads (the result is identical).  An empty input gives
+ * an empty BVH (the reference dereferences a missing child there).
+ * Replaces Volume::BVH::BVH(aabbs, data, parallelBuild)  BVH.cpp:14-56. */
+ae_rt_status ae_bvh_build_triangles(const float* verts, const float* aabbs, uint32_t n,
+                                    int parallel, ae_bvh** out);
+
+/* AABB-only BVH (the top level over instances, 64 bins).
+ * Replaces Volume::BVH::BVH(aabbs, parallelBuild)  BVH.cpp:58-100. */
+ae_rt_status ae_bvh_build_aabbs(const float* aabbs, uint32_t n, int parallel, ae_bvh** out);
+
+void ae_bvh_destroy(ae_bvh* bvh);
+
+/* Sizes of BVH::nodes and BVH::data / BVH::refs (BVH.h:133-137). */
+uint32_t ae_bvh_node_count(const ae_bvh* bvh);
+uint32_t ae_bvh_primitive_count(const ae_bvh* bvh);
+
+/* Nodes in the GPUBVHNode layout, as MeshData.cpp:256-268 copies them. */
+ae_rt_status ae_bvh_get_nodes(const ae_bvh* bvh, ae_bvh_node* out);
+
+/* Flattened primitive order: order[i] = input index of primitive i
+ * (BVHTriangle::idx / Ref::idx), end_of_node[i] = leaf terminator flag. */
+ae_rt_status ae_bvh_get_order(const ae_bvh* bvh, uint32_t* order, uint8_t* end_of_node);
+
+/* GPUBVHTriangle packing in BVH order (MeshData.cpp:241-248).  material and
+ * opacity are per input triangle and optional (0 and 1.0). */
+ae_rt_status ae_bvh_pack_triangles(const ae_bvh* bvh, const float* verts, const int32_t* material,
+                                   const float* opacity, ae_bvh_triangle* out);
+
+/* ------------------------------------------------------------------------ */
+/* Device context                                                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct ae_rt_ctx ae_rt_ctx;
+
+typedef struct ae_rt_config {
+    int32_t device;             /* CUDA device ordinal */
+    uint32_t blocks_per_sm;     /* persistent traversal CTAs per SM (0 = tuned default) */
+    uint32_t threads_per_block; /* 0 = tuned default (multiple of 32) */
+    uint32_t max_steps;         /* traversal step cap per ray (0 = 4 x nodes + 64) */
+    uint32_t reserved[4];
+} ae_rt_config;
+
+ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out);
+void ae_rt_ctx_destroy(ae_rt_ctx* ctx);
+
+/* Text of the last error on this context ("" when none). */
+const char* ae_rt_last_error(const ae_rt_ctx* ctx);
+
+/* Uploads one mesh's BLAS: nodes, BVH triangles and (optional) shading
+ * triangles, deep-copied into device memory the context owns.  The host
+ * validator checks pointer ranges, leaf termination and pre-order child
+ * indices (which rules out cycles) and returns AE_RT_BAD_BVH otherwise.
+ * Replaces Mesh::BuildBVH's uploads (src/engine/mesh/Mesh.cpp:97-108). */
+ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_t n_nodes,
+                               const ae_bvh_triangle* tris, const ae_triangle* shading,
+                               uint32_t n_tris, int32_t* mesh_id);
+
+/* Closest hit of every ray against one mesh: HitClosest (bvh.hsh:191-273)
+ * over one BLAS, i.e. the engine's traversal with an identity instance.
+ * tmin/tmax as HitClosest's arguments.  Also the batched GPU form of
+ * Volume::BVH::GetIntersection (BVH.cpp:103). */
+ae_rt_status ae_rt_trace_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                 uint32_t n_rays, float tmin, float tmax, ae_hit* hits,
+                                 void* stream);
+
+/* Occlusion of every ray against one mesh: HitAny (bvh.hsh:359-441); the
+ * batched GPU form of Volume::BVH::GetIntersectionAny (BVH.cpp:176).
+ * occluded[i] = 1 when a triangle is hit with tmin < t < tmax. */
+ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                             uint32_t n_rays, float tmin, float tmax, uint8_t* occluded,
+                             void* stream);
+
+/* Waits for `stream` and reports device-side errors of the context's
+ * preceding asynchronous calls (stack overflow, step cap, timeouts). */
+ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
+
+/* Per-launch statistics of the most recent trace on this context (counted
+ * only when the context was created with AE_RT_CFG_COUNT_FETCHES in
+ * reserved[0]): inner-node fetches and triangle fetches summed over rays. */
+#define AE_RT_CFG_COUNT_FETCHES 0x1u
+ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATLAS_RT_H */

@@ -1,0 +1,397 @@
+/*
+ * CPU restatement of Atlas Engine's BVH ray queries -- the ORACLE.
+ * TEST INFRASTRUCTURE ONLY (see ae_oracle.h).  Compiled with
+ * -ffp-contract=off so every multiply and add rounds separately, in the
+ * order written, on x86-64 and aarch64 alike.
+ */
+#include "ae_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct { float x, y, z; } v3;
+
+static inline v3 mk(float x, float y, float z) { v3 r = { x, y, z }; return r; }
+static inline v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+/* dot as (x + y) + z, cross in the GLSL component formula. */
+static inline float dot3(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline v3 cross3(v3 a, v3 b) {
+    return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+static inline v3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+
+/* glm scalar min/max as the GLSL specification defines them. */
+static inline float gmin(float x, float y) { return (y < x) ? y : x; }
+static inline float gmax(float x, float y) { return (x < y) ? y : x; }
+
+/* ---------------------------------------------------------------------- */
+/* Triangle test shared by both semantics: Ray.cpp:53-76 and               */
+/* intersections.hsh:36-57 are the same formula.  u weights v1, v weights v2. */
+/* ---------------------------------------------------------------------- */
+static inline int tri_test(v3 o, v3 d, const aeo_tri* t, float* st, float* su, float* sv) {
+    v3 v0 = ld3(t->v0), v1 = ld3(t->v1), v2 = ld3(t->v2);
+    v3 e0 = sub(v1, v0);
+    v3 e1 = sub(v2, v0);
+    v3 s = sub(o, v0);
+    v3 p = cross3(s, e0);
+    v3 q = cross3(d, e1);
+    float den = dot3(q, e0);
+    float x = dot3(p, e1) / den;
+    float y = dot3(q, s) / den;
+    float z = dot3(p, d) / den;
+    *st = x; *su = y; *sv = z;
+    return x >= 0.0f && y >= 0.0f && z >= 0.0f && y + z <= 1.0f;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Host semantics (BVH.cpp / Ray.cpp)                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Ray::Intersects(const AABB&, float&) -- Ray.cpp:28-43. */
+static inline int box_cpu(v3 o, v3 inv, float tmin, float tmax, const float* bmin, const float* bmax, float* t) {
+    float t0x = (bmin[0] - o.x) * inv.x, t0y = (bmin[1] - o.y) * inv.y, t0z = (bmin[2] - o.z) * inv.z;
+    float t1x = (bmax[0] - o.x) * inv.x, t1y = (bmax[1] - o.y) * inv.y, t1z = (bmax[2] - o.z) * inv.z;
+    float sx = gmin(t0x, t1x), sy = gmin(t0y, t1y), sz = gmin(t0z, t1z);
+    float bx = gmax(t0x, t1x), by = gmax(t0y, t1y), bz = gmax(t0z, t1z);
+    float tminf = gmax(tmin, gmax(sx, gmax(sy, sz)));
+    float tmaxf = gmin(tmax, gmin(bx, gmin(by, bz)));
+    *t = tminf;
+    return tminf <= tmaxf;
+}
+
+typedef struct { int32_t ptr; float dist; } cpu_entry;
+
+/* BVH::GetIntersection -- BVH.cpp:103-174. */
+static void closest_cpu_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris,
+                            const float* r, cpu_entry* stack, int32_t* out_ptr, float* out_tuv) {
+    v3 o = ld3(r), d = ld3(r + 3);
+    v3 inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float tMin = r[6], tMax = r[7];
+    float ix = tMax, iy = 0.0f, iz = 0.0f;   /* intersection.x starts at tMax */
+    int32_t closest = -1;
+    if (n_nodes) {
+        uint32_t sp = 1;
+        stack[0].ptr = 0; stack[0].dist = 0.0f;
+        float rayTMax = tMax;
+        while (sp != 0) {
+            cpu_entry e = stack[--sp];
+            if (e.dist > ix) continue;
+            if (e.ptr < 0) {
+                int32_t tp = ~e.ptr;
+                int end = 0;
+                while (!end) {
+                    int32_t ptr = tp++;
+                    const aeo_tri* t = &tris[ptr];
+                    end = t->v0[3] > 0.0f;
+                    float st, su, sv;
+                    int hit = tri_test(o, d, t, &st, &su, &sv);
+                    if (hit && st < ix) { closest = ptr; ix = st; iy = su; iz = sv; }
+                }
+            } else {
+                rayTMax = ix;
+                const aeo_node* nd = &nodes[e.ptr];
+                float hl = 0.0f, hr = 0.0f;
+                int il = box_cpu(o, inv, tMin, rayTMax, nd->lmin, nd->lmax, &hl);
+                int ir = box_cpu(o, inv, tMin, rayTMax, nd->rmin, nd->rmax, &hr);
+                if (ir && il) {
+                    if (hl < hr) {
+                        stack[sp].ptr = nd->right; stack[sp++].dist = hr;
+                        stack[sp].ptr = nd->left;  stack[sp++].dist = hl;
+                    } else {
+                        stack[sp].ptr = nd->left;  stack[sp++].dist = hl;
+                        stack[sp].ptr = nd->right; stack[sp++].dist = hr;
+                    }
+                } else if (ir) {
+                    stack[sp].ptr = nd->right; stack[sp++].dist = hr;
+                } else if (il) {
+                    stack[sp].ptr = nd->left;  stack[sp++].dist = hl;
+                }
+            }
+        }
+    }
+    /* Hit predicate: intersection.x < the caller's tMax (the returned bool of
+     * the reference compares against the mutated ray.tMax, BVH.cpp:141/:172). */
+    *out_ptr = (ix < tMax) ? closest : -1;
+    out_tuv[0] = ix; out_tuv[1] = iy; out_tuv[2] = iz;
+}
+
+/* BVH::GetIntersectionAny -- BVH.cpp:176-217. */
+static int any_cpu_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris,
+                       const float* r, int32_t* stack) {
+    if (!n_nodes) return 0;
+    v3 o = ld3(r), d = ld3(r + 3);
+    v3 inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float tMin = r[6], tMax = r[7];
+    uint32_t sp = 1;
+    stack[0] = 0;
+    while (sp != 0) {
+        int32_t ptr = stack[--sp];
+        if (ptr < 0) {
+            int32_t tp = ~ptr;
+            int end = 0;
+            while (!end) {
+                const aeo_tri* t = &tris[tp++];
+                end = t->v0[3] > 0.0f;
+                float st, su, sv;
+                if (tri_test(o, d, t, &st, &su, &sv) && st < tMax) return 1;
+            }
+        } else {
+            const aeo_node* nd = &nodes[ptr];
+            float dummy;
+            int il = box_cpu(o, inv, tMin, tMax, nd->lmin, nd->lmax, &dummy);
+            int ir = box_cpu(o, inv, tMin, tMax, nd->rmin, nd->rmax, &dummy);
+            if (ir) stack[sp++] = nd->right;
+            if (il) stack[sp++] = nd->left;
+        }
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Shader semantics (bvh.hsh / intersections.hsh)                          */
+/* ---------------------------------------------------------------------- */
+
+/* IntersectAABB(ray, aabb, tmin, tmax, out dist) -- intersections.hsh:18-34.
+ * GLSL min/max are taken as IEEE minNum/maxNum (fminf/fmaxf): a NaN operand
+ * loses, as it does for the GPU min/max instructions. */
+static inline int box_glsl(v3 o, v3 d, float tmin, float tmax, const float* bmin, const float* bmax, float* dist) {
+    float t0x = (bmin[0] - o.x) / d.x, t0y = (bmin[1] - o.y) / d.y, t0z = (bmin[2] - o.z) / d.z;
+    float t1x = (bmax[0] - o.x) / d.x, t1y = (bmax[1] - o.y) / d.y, t1z = (bmax[2] - o.z) / d.z;
+    float sx = fminf(t0x, t1x), sy = fminf(t0y, t1y), sz = fminf(t0z, t1z);
+    float bx = fmaxf(t0x, t1x), by = fmaxf(t0y, t1y), bz = fmaxf(t0z, t1z);
+    float tminf = fmaxf(fmaxf(tmin, sx), fmaxf(sy, sz));
+    float tmaxf = fminf(fminf(tmax, bx), fminf(by, bz));
+    int hit = tminf <= tmaxf;
+    *dist = hit ? tminf : tmax;
+    return hit;
+}
+
+static inline int isnan3(v3 d) { return isnan(d.x) || isnan(d.y) || isnan(d.z); }
+
+/* HitClosest -- bvh.hsh:191-273 on one BLAS, CheckLeafClosest :44-72.
+ * The stack is unbounded here (the shader's holds 32 entries with no check). */
+static void closest_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris,
+                             const float* r, int32_t* stack, int32_t* out_ptr, float* out_tuv,
+                             uint32_t* nf, uint32_t* tf) {
+    v3 o = ld3(r), d = ld3(r + 3);
+    float tMin = r[6], tMax = r[7];
+    float hitDist = tMax, hu = 0.0f, hv = 0.0f;
+    int32_t hitID = -1;
+    uint32_t nodeFetches = 0, triFetches = 0;
+    if (n_nodes && !isnan3(d)) {
+        uint32_t sp = 1;
+        int32_t nodePtr = 0;
+        stack[0] = 0;
+        while (sp != 0) {
+            if (nodePtr < 0) {
+                int32_t tp = ~nodePtr;
+                int end = 0;
+                while (!end) {
+                    const aeo_tri* t = &tris[tp];
+                    end = t->v0[3] > 0.0f;
+                    triFetches++;
+                    float st, su, sv;
+                    int hit = tri_test(o, d, t, &st, &su, &sv);
+                    /* tmax of CheckLeafClosest is ray.hitDistance (bvh.hsh:246) */
+                    if (hit && st > tMin && st < hitDist) {
+                        if (st < hitDist) { hitDist = st; hitID = tp; hu = su; hv = sv; }
+                    }
+                    tp++;
+                }
+                nodePtr = stack[--sp];
+            } else {
+                const aeo_node* nd = &nodes[nodePtr];
+                nodeFetches++;
+                float hl = 0.0f, hr = 0.0f;
+                int il = box_glsl(o, d, tMin, hitDist, nd->lmin, nd->lmax, &hl);
+                int ir = box_glsl(o, d, tMin, hitDist, nd->rmin, nd->rmax, &hr);
+                int none = !il && !ir;
+                int32_t next = (hl <= hr) ? nd->left : nd->right;
+                if (none) next = stack[--sp];
+                if (ir && il) stack[sp++] = (hl <= hr) ? nd->right : nd->left;
+                nodePtr = next;
+            }
+        }
+    }
+    *out_ptr = hitID;
+    out_tuv[0] = hitDist; out_tuv[1] = hu; out_tuv[2] = hv;
+    if (nf) *nf = nodeFetches;
+    if (tf) *tf = triFetches;
+}
+
+/* HitAny -- bvh.hsh:359-441 on one BLAS, CheckLeaf :74-104. */
+static int any_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris,
+                        const float* r, int32_t* stack, uint32_t* nf, uint32_t* tf) {
+    v3 o = ld3(r), d = ld3(r + 3);
+    float tMin = r[6], tMax = r[7];
+    uint32_t nodeFetches = 0, triFetches = 0;
+    int hit = 0;
+    if (n_nodes && !isnan3(d)) {
+        uint32_t sp = 1;
+        int32_t nodePtr = 0;
+        stack[0] = 0;
+        while (sp != 0 && !hit) {
+            if (nodePtr < 0) {
+                int32_t tp = ~nodePtr;
+                int end = 0;
+                while (!end && !hit) {
+                    const aeo_tri* t = &tris[tp];
+                    end = t->v0[3] > 0.0f;
+                    triFetches++;
+                    float st, su, sv;
+                    if (tri_test(o, d, t, &st, &su, &sv) && st > tMin && st < tMax) hit = 1;
+                    tp++;
+                }
+                nodePtr = stack[--sp];
+            } else {
+                const aeo_node* nd = &nodes[nodePtr];
+                nodeFetches++;
+                float dl, dr;
+                int il = box_glsl(o, d, tMin, tMax, nd->lmin, nd->lmax, &dl);
+                int ir = box_glsl(o, d, tMin, tMax, nd->rmin, nd->rmax, &dr);
+                int32_t next = il ? nd->left : nd->right;
+                if (!ir && !il) next = stack[--sp];
+                if (ir && il) stack[sp++] = nd->right;
+                nodePtr = next;
+            }
+        }
+    }
+    if (nf) *nf = nodeFetches;
+    if (tf) *tf = triFetches;
+    return hit;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Double-precision brute force                                            */
+/* ---------------------------------------------------------------------- */
+static void closest_f64_one(const aeo_tri* tris, uint32_t n_tris, const float* r,
+                            int32_t* out_ptr, double* out_t, double* out_t2) {
+    double o[3] = { r[0], r[1], r[2] }, d[3] = { r[3], r[4], r[5] };
+    double tMin = r[6], tMax = r[7];
+    double best = INFINITY, second = INFINITY;
+    int32_t bi = -1;
+    for (uint32_t i = 0; i < n_tris; i++) {
+        const aeo_tri* t = &tris[i];
+        double v0[3] = { t->v0[0], t->v0[1], t->v0[2] };
+        double e0[3] = { t->v1[0] - v0[0], t->v1[1] - v0[1], t->v1[2] - v0[2] };
+        double e1[3] = { t->v2[0] - v0[0], t->v2[1] - v0[1], t->v2[2] - v0[2] };
+        double s[3] = { o[0] - v0[0], o[1] - v0[1], o[2] - v0[2] };
+        double p[3] = { s[1] * e0[2] - e0[1] * s[2], s[2] * e0[0] - e0[2] * s[0], s[0] * e0[1] - e0[0] * s[1] };
+        double q[3] = { d[1] * e1[2] - e1[1] * d[2], d[2] * e1[0] - e1[2] * d[0], d[0] * e1[1] - e1[0] * d[1] };
+        double den = q[0] * e0[0] + q[1] * e0[1] + q[2] * e0[2];
+        double x = (p[0] * e1[0] + p[1] * e1[1] + p[2] * e1[2]) / den;
+        double y = (q[0] * s[0] + q[1] * s[1] + q[2] * s[2]) / den;
+        double z = (p[0] * d[0] + p[1] * d[1] + p[2] * d[2]) / den;
+        if (x >= 0.0 && y >= 0.0 && z >= 0.0 && y + z <= 1.0 && x > tMin && x < tMax) {
+            if (x < best) { second = best; best = x; bi = (int32_t)i; }
+            else if (x < second) second = x;
+        }
+    }
+    *out_ptr = bi; *out_t = best; *out_t2 = second;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Batch drivers on pthreads                                               */
+/* ---------------------------------------------------------------------- */
+enum { K_CLOSEST_CPU, K_ANY_CPU, K_CLOSEST_GLSL, K_ANY_GLSL, K_F64 };
+
+typedef struct {
+    int kind;
+    const aeo_node* nodes; uint32_t n_nodes;
+    const aeo_tri* tris; uint32_t n_tris;
+    const float* rays; uint32_t begin, end;
+    int32_t* ptr; float* tuv; uint8_t* occ; uint32_t* nf; uint32_t* tf;
+    double* t64; double* t64b;
+} job_t;
+
+static void* run_job(void* arg) {
+    job_t* j = (job_t*)arg;
+    size_t cap = (size_t)j->n_nodes + 64;
+    void* stack = malloc(cap * sizeof(cpu_entry));
+    for (uint32_t i = j->begin; i < j->end; i++) {
+        const float* r = j->rays + (size_t)i * 8;
+        switch (j->kind) {
+        case K_CLOSEST_CPU:
+            closest_cpu_one(j->nodes, j->n_nodes, j->tris, r, (cpu_entry*)stack, &j->ptr[i], &j->tuv[(size_t)i * 3]);
+            break;
+        case K_ANY_CPU:
+            j->occ[i] = (uint8_t)any_cpu_one(j->nodes, j->n_nodes, j->tris, r, (int32_t*)stack);
+            break;
+        case K_CLOSEST_GLSL:
+            closest_glsl_one(j->nodes, j->n_nodes, j->tris, r, (int32_t*)stack, &j->ptr[i], &j->tuv[(size_t)i * 3],
+                             j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL);
+            break;
+        case K_ANY_GLSL:
+            j->occ[i] = (uint8_t)any_glsl_one(j->nodes, j->n_nodes, j->tris, r, (int32_t*)stack,
+                                              j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL);
+            break;
+        case K_F64:
+            closest_f64_one(j->tris, j->n_tris, r, &j->ptr[i], &j->t64[i], &j->t64b[i]);
+            break;
+        }
+    }
+    free(stack);
+    return NULL;
+}
+
+static void run_batch(job_t proto, uint32_t n, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    job_t jobs[256];
+    uint32_t chunk = (n + (uint32_t)threads - 1) / (uint32_t)threads;
+    int started = 0;
+    for (int t = 0; t < threads; t++) {
+        uint32_t b = (uint32_t)t * chunk;
+        if (b >= n) break;
+        uint32_t e = b + chunk < n ? b + chunk : n;
+        jobs[t] = proto; jobs[t].begin = b; jobs[t].end = e;
+        if (threads == 1) { run_job(&jobs[t]); continue; }
+        pthread_create(&th[t], NULL, run_job, &jobs[t]);
+        started++;
+    }
+    for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+void aeo_closest_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                     const float* rays, uint32_t n_rays, int threads, int32_t* tri_ptr, float* tuv) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_CLOSEST_CPU; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
+    p.rays = rays; p.ptr = tri_ptr; p.tuv = tuv;
+    run_batch(p, n_rays, threads);
+}
+
+void aeo_any_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                 const float* rays, uint32_t n_rays, int threads, uint8_t* occluded) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_ANY_CPU; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
+    p.rays = rays; p.occ = occluded;
+    run_batch(p, n_rays, threads);
+}
+
+void aeo_closest_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                      const float* rays, uint32_t n_rays, int threads,
+                      int32_t* tri_ptr, float* tuv, uint32_t* node_fetches, uint32_t* tri_fetches) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_CLOSEST_GLSL; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
+    p.rays = rays; p.ptr = tri_ptr; p.tuv = tuv; p.nf = node_fetches; p.tf = tri_fetches;
+    run_batch(p, n_rays, threads);
+}
+
+void aeo_any_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                  const float* rays, uint32_t n_rays, int threads, uint8_t* occluded,
+                  uint32_t* node_fetches, uint32_t* tri_fetches) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_ANY_GLSL; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
+    p.rays = rays; p.occ = occluded; p.nf = node_fetches; p.tf = tri_fetches;
+    run_batch(p, n_rays, threads);
+}
+
+void aeo_closest_f64_brute(const aeo_tri* tris, uint32_t n_tris, const float* rays, uint32_t n_rays,
+                           int threads, int32_t* tri_ptr, double* t, double* t2) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_F64; p.tris = tris; p.n_tris = n_tris; p.rays = rays; p.ptr = tri_ptr; p.t64 = t; p.t64b = t2;
+    run_batch(p, n_rays, threads);
+}

@@ -1,0 +1,78 @@
+/*
+ * CPU restatement of Atlas Engine's BVH ray queries -- the ORACLE.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline / reference arm load this library, and only to
+ * check or time against; the product path (libatlas_rt.so) never links it.
+ *
+ * Two traversal semantics are restated, both over the engine's GPU buffer
+ * layouts (64-byte GPUBVHNode, 48-byte GPUBVHTriangle, see
+ * src/engine/raytracing/RTStructures.h:23-27, :95-103):
+ *
+ *   *_cpu   the host query  Volume::BVH::GetIntersection / GetIntersectionAny
+ *           (src/engine/volume/BVH.cpp:103-217, Ray.cpp:28-76): slab test by
+ *           multiplication with 1/dir, triangle accepted for t >= 0, glm
+ *           min/max semantics.
+ *   *_glsl  the shader query HitClosest / HitAny on one BLAS
+ *           (data/shader/raytracer/bvh.hsh:44-104, :191-273, :359-441;
+ *           intersections.hsh:3-57): slab test by division, near-child-first
+ *           descent, triangle accepted for tmin < t < tmax.
+ *
+ * Rays are rows of 8 floats: origin.xyz, direction.xyz, tmin, tmax.
+ */
+#ifndef AE_ORACLE_H
+#define AE_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct aeo_node {
+    float lmin[3], lmax[3];
+    float rmin[3], rmax[3];
+    int32_t left, right, pad0, pad1;
+} aeo_node;
+
+typedef struct aeo_tri {
+    float v0[4];  /* w > 0: last triangle of its leaf */
+    float v1[4];
+    float v2[4];
+} aeo_tri;
+
+/* Host closest-hit query (BVH.cpp:103-174).  tri_ptr = BVH-order index of the
+ * closest triangle or -1; tuv = (t, u, v) of that hit. */
+void aeo_closest_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                     const float* rays, uint32_t n_rays, int threads,
+                     int32_t* tri_ptr, float* tuv);
+
+/* Host any-hit query (BVH.cpp:176-217); occluded[i] = 0/1. */
+void aeo_any_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                 const float* rays, uint32_t n_rays, int threads, uint8_t* occluded);
+
+/* Shader closest-hit query on one BLAS (bvh.hsh:191-273 with the TLAS level
+ * collapsed to a single identity instance).  Outputs as aeo_closest_cpu plus
+ * per-ray counts of inner nodes fetched and triangles tested (any counter
+ * pointer may be NULL). */
+void aeo_closest_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                      const float* rays, uint32_t n_rays, int threads,
+                      int32_t* tri_ptr, float* tuv, uint32_t* node_fetches, uint32_t* tri_fetches);
+
+/* Shader any-hit query on one BLAS (bvh.hsh:359-441). */
+void aeo_any_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                  const float* rays, uint32_t n_rays, int threads, uint8_t* occluded,
+                  uint32_t* node_fetches, uint32_t* tri_fetches);
+
+/* Exact-as-possible nearest hit in double precision by brute force over every
+ * triangle (for small cases and for re-testing near ties): the double-precision
+ * form of the same triangle test, accepting tmin < t < tmax.  t2 = second
+ * smallest accepted t (or +inf). */
+void aeo_closest_f64_brute(const aeo_tri* tris, uint32_t n_tris, const float* rays, uint32_t n_rays,
+                           int threads, int32_t* tri_ptr, double* t, double* t2);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

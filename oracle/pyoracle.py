@@ -1,0 +1,232 @@
+"""Python access to the oracle libraries.  TEST INFRASTRUCTURE ONLY.
+
+* ``libaeoracle.so`` (oracle/_build): the C restatement of the engine's BVH
+  ray queries (ae_oracle.c), host and shader semantics.  Builds with gcc on
+  any host.
+* ``libaeref.so`` (oracle/_ref): the reference's own BVH builder and host
+  queries compiled from the reference tree (oracle/Makefile target ``ref``).
+  Only available where the reference tree is present.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+PORT_LIB = ORACLE_DIR / "_build" / "libaeoracle.so"
+REF_LIB = ORACLE_DIR / "_ref" / "libaeref.so"
+REFERENCE_ROOT = Path(os.environ.get("AE_REFERENCE_ROOT", "/root/reference"))
+
+P = C.c_void_p
+U32 = C.c_uint32
+
+_port = None
+_ref = None
+
+
+def build_port(force: bool = False) -> Path:
+    src = [ORACLE_DIR / "ae_oracle.c", ORACLE_DIR / "ae_oracle.h"]
+    if force or not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in src):
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref(force: bool = False) -> Path | None:
+    """Compiles the reference's own sources, if the reference tree exists here."""
+    if not (REFERENCE_ROOT / "src" / "engine" / "volume" / "BVH.cpp").exists():
+        return None
+    if force or not REF_LIB.exists():
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REFERENCE_ROOT={REFERENCE_ROOT}"],
+                       check=True, capture_output=True)
+    return REF_LIB
+
+
+def port():
+    global _port
+    if _port is None:
+        build_port()
+        L = C.CDLL(str(PORT_LIB))
+        L.aeo_closest_cpu.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P]
+        L.aeo_any_cpu.argtypes = [P, U32, P, U32, P, U32, C.c_int, P]
+        L.aeo_closest_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P, P]
+        L.aeo_any_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P]
+        L.aeo_closest_f64_brute.argtypes = [P, U32, P, U32, C.c_int, P, P, P]
+        for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
+            f.restype = None
+        _port = L
+    return _port
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists() or build_ref() is not None
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if build_ref() is None and not REF_LIB.exists():
+            raise RuntimeError("the reference tree is not available on this host")
+        L = C.CDLL(str(REF_LIB))
+        L.aeref_build.restype = P
+        L.aeref_build.argtypes = [P, U32, C.c_int]
+        L.aeref_build_aabbs.restype = P
+        L.aeref_build_aabbs.argtypes = [P, U32, C.c_int]
+        for f in ("aeref_node_count", "aeref_data_count", "aeref_refs_count"):
+            getattr(L, f).restype = U32
+            getattr(L, f).argtypes = [P]
+        L.aeref_get_nodes.argtypes = [P, P]
+        L.aeref_get_data.argtypes = [P, P, P, P]
+        L.aeref_get_refs.argtypes = [P, P]
+        L.aeref_closest.argtypes = [P, P, U32, C.c_int, P, P, P]
+        L.aeref_any.argtypes = [P, P, U32, C.c_int, P]
+        L.aeref_free.argtypes = [P]
+        L.aeref_jobsystem_init.argtypes = [C.c_int]
+        _ref = L
+    return _ref
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dt)
+
+
+# ---------------------------------------------------------------------------
+# Restatement (port)
+# ---------------------------------------------------------------------------
+
+def closest_cpu(nodes_f32, tris_f32, rays8, threads=os.cpu_count()):
+    n = len(rays8)
+    nodes_f32, tris_f32, rays8 = _c(nodes_f32, np.float32), _c(tris_f32, np.float32), _c(rays8, np.float32)
+    ptr = np.empty(n, np.int32)
+    tuv = np.empty((n, 3), np.float32)
+    port().aeo_closest_cpu(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
+                           rays8.ctypes.data, n, threads, ptr.ctypes.data, tuv.ctypes.data)
+    return ptr, tuv
+
+
+def any_cpu(nodes_f32, tris_f32, rays8, threads=os.cpu_count()):
+    n = len(rays8)
+    nodes_f32, tris_f32, rays8 = _c(nodes_f32, np.float32), _c(tris_f32, np.float32), _c(rays8, np.float32)
+    occ = np.empty(n, np.uint8)
+    port().aeo_any_cpu(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
+                       rays8.ctypes.data, n, threads, occ.ctypes.data)
+    return occ
+
+
+def closest_glsl(nodes_f32, tris_f32, rays8, threads=os.cpu_count(), counters=False):
+    n = len(rays8)
+    nodes_f32, tris_f32, rays8 = _c(nodes_f32, np.float32), _c(tris_f32, np.float32), _c(rays8, np.float32)
+    ptr = np.empty(n, np.int32)
+    tuv = np.empty((n, 3), np.float32)
+    nf = np.empty(n, np.uint32) if counters else None
+    tf = np.empty(n, np.uint32) if counters else None
+    port().aeo_closest_glsl(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
+                            rays8.ctypes.data, n, threads, ptr.ctypes.data, tuv.ctypes.data,
+                            None if nf is None else nf.ctypes.data, None if tf is None else tf.ctypes.data)
+    if counters:
+        return ptr, tuv, nf, tf
+    return ptr, tuv
+
+
+def any_glsl(nodes_f32, tris_f32, rays8, threads=os.cpu_count(), counters=False):
+    n = len(rays8)
+    nodes_f32, tris_f32, rays8 = _c(nodes_f32, np.float32), _c(tris_f32, np.float32), _c(rays8, np.float32)
+    occ = np.empty(n, np.uint8)
+    nf = np.empty(n, np.uint32) if counters else None
+    tf = np.empty(n, np.uint32) if counters else None
+    port().aeo_any_glsl(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
+                        rays8.ctypes.data, n, threads, occ.ctypes.data,
+                        None if nf is None else nf.ctypes.data, None if tf is None else tf.ctypes.data)
+    if counters:
+        return occ, nf, tf
+    return occ
+
+
+def closest_f64_brute(tris_f32, rays8, threads=os.cpu_count()):
+    n = len(rays8)
+    tris_f32, rays8 = _c(tris_f32, np.float32), _c(rays8, np.float32)
+    ptr = np.empty(n, np.int32)
+    t = np.empty(n, np.float64)
+    t2 = np.empty(n, np.float64)
+    port().aeo_closest_f64_brute(tris_f32.ctypes.data, len(tris_f32), rays8.ctypes.data, n, threads,
+                                 ptr.ctypes.data, t.ctypes.data, t2.ctypes.data)
+    return ptr, t, t2
+
+
+# ---------------------------------------------------------------------------
+# Compiled reference
+# ---------------------------------------------------------------------------
+
+class RefBVH:
+    """The reference's Volume::BVH built from triangles, exported to arrays."""
+
+    def __init__(self, verts, parallel=True):
+        L = ref()
+        v = _c(verts, np.float32).reshape(-1, 9)
+        self.h = L.aeref_build(v.ctypes.data if len(v) else None, len(v), int(parallel))
+        nn = L.aeref_node_count(self.h)
+        nd = L.aeref_data_count(self.h)
+        self.nodes_f32 = np.zeros((nn, 16), np.float32)
+        if nn:
+            L.aeref_get_nodes(self.h, self.nodes_f32.ctypes.data)
+        self.data_verts = np.zeros((nd, 9), np.float32)
+        self.order = np.zeros(nd, np.uint32)
+        self.end_of_node = np.zeros(nd, np.uint8)
+        if nd:
+            L.aeref_get_data(self.h, self.data_verts.ctypes.data, self.order.ctypes.data,
+                             self.end_of_node.ctypes.data)
+
+    def gpu_triangles(self):
+        """GPUBVHTriangle packing of the reference data (MeshData.cpp:241-248)."""
+        nd = len(self.order)
+        t = np.zeros((nd, 12), np.float32)
+        t[:, 0:3] = self.data_verts[:, 0:3]
+        t[:, 3] = np.where(self.end_of_node > 0, 1.0, -1.0)
+        t[:, 4:7] = self.data_verts[:, 3:6]
+        t[:, 8:11] = self.data_verts[:, 6:9]
+        t[:, 11] = 1.0
+        return t
+
+    def closest(self, rays8, threads=os.cpu_count()):
+        n = len(rays8)
+        rays8 = _c(rays8, np.float32)
+        idx = np.empty(n, np.int32)
+        tuv = np.empty((n, 3), np.float32)
+        rb = np.empty(n, np.uint8)
+        ref().aeref_closest(self.h, rays8.ctypes.data, n, threads, idx.ctypes.data, tuv.ctypes.data,
+                            rb.ctypes.data)
+        return idx, tuv, rb
+
+    def any(self, rays8, threads=os.cpu_count()):
+        n = len(rays8)
+        rays8 = _c(rays8, np.float32)
+        occ = np.empty(n, np.uint8)
+        ref().aeref_any(self.h, rays8.ctypes.data, n, threads, occ.ctypes.data)
+        return occ
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref().aeref_free(self.h)
+            self.h = None
+
+
+def ref_build_aabbs(boxes, parallel=True):
+    """The reference's AABB-only BVH: (nodes_f32, refs order)."""
+    L = ref()
+    b = _c(boxes, np.float32).reshape(-1, 6)
+    h = L.aeref_build_aabbs(b.ctypes.data, len(b), int(parallel))
+    nn = L.aeref_node_count(h)
+    nr = L.aeref_refs_count(h)
+    nodes = np.zeros((nn, 16), np.float32)
+    if nn:
+        L.aeref_get_nodes(h, nodes.ctypes.data)
+    order = np.zeros(nr, np.uint32)
+    if nr:
+        L.aeref_get_refs(h, order.ctypes.data)
+    L.aeref_free(h)
+    return nodes, order
