@@ -21,7 +21,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import AeRtError, Config, lib
+from ._native import AeRtError, BounceParams, Camera, CastOutputs, Config, lib
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
@@ -181,6 +181,38 @@ class Context:
                                      _stream_handle(stream)), self._h)
         return out
 
+    # ---- wavefront stages (device buffers) ----
+    def raygen(self, cam: "Camera", rays, stream=None):
+        _check(lib().ae_rt_raygen(self._h, C.byref(cam), _ptr(rays), _stream_handle(stream)), self._h)
+
+    def trace_closest_queue(self, mesh, rays, count, capacity, tmin, tmax, hits, stream=None):
+        _check(lib().ae_rt_trace_closest_queue(self._h, mesh, _ptr(rays), _ptr(count), capacity, tmin, tmax,
+                                               _ptr(hits), _stream_handle(stream)), self._h)
+
+    def trace_any_queue(self, mesh, rays, count, capacity, tmin, tmax, occluded, stream=None):
+        _check(lib().ae_rt_trace_any_queue(self._h, mesh, _ptr(rays), _ptr(count), capacity, tmin, tmax,
+                                           _ptr(occluded), _stream_handle(stream)), self._h)
+
+    def spawn_bounce(self, mesh, rays, hits, n, params: "BounceParams", secondary, shadow, counts,
+                     count=None, stream=None):
+        _check(lib().ae_rt_spawn_bounce(self._h, mesh, _ptr(rays), _ptr(hits), _ptr(count), n, C.byref(params),
+                                        _ptr(secondary), _ptr(shadow), _ptr(counts), _stream_handle(stream)),
+               self._h)
+
+    def cast_pass(self, mesh, cam: "Camera", params: "BounceParams", primary_hits=None, secondary_rays=None,
+                  secondary_hits=None, shadow_rays=None, shadow_occluded=None, stream=None):
+        """One camera pass (primary, bounce and shadow rays).  Returns counts
+        (primary, secondary, shadow)."""
+        out = CastOutputs()
+        out.primary_hits = _ptr(primary_hits)
+        out.secondary_rays = _ptr(secondary_rays)
+        out.secondary_hits = _ptr(secondary_hits)
+        out.shadow_rays = _ptr(shadow_rays)
+        out.shadow_occluded = _ptr(shadow_occluded)
+        _check(lib().ae_rt_cast_pass(self._h, mesh, C.byref(cam), C.byref(params), C.byref(out),
+                                     _stream_handle(stream)), self._h)
+        return tuple(out.counts)
+
     def synchronize(self, stream=None):
         _check(lib().ae_rt_synchronize(self._h, _stream_handle(stream)), self._h)
 
@@ -188,3 +220,27 @@ class Context:
         a, b = C.c_uint64(), C.c_uint64()
         _check(lib().ae_rt_get_fetch_counts(self._h, C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
+
+
+def make_camera(cam: dict) -> Camera:
+    """ae_camera from the dict of scenes.pinhole_camera."""
+    c = Camera()
+    for name in ("location", "origin", "right", "bottom"):
+        v = getattr(c, name)
+        for i in range(3):
+            v[i] = float(cam[name][i])
+    c.width, c.height = cam["width"], cam["height"]
+    j = cam.get("jitter", (0.5, 0.5))
+    c.jitter[0], c.jitter[1] = j
+    return c
+
+
+def make_bounce_params(light_dir=(0.4, 1.0, 0.3), epsilon=0.1, seed=1) -> BounceParams:
+    p = BounceParams()
+    L = np.asarray(light_dir, np.float64)
+    L = L / np.linalg.norm(L)
+    for i in range(3):
+        p.light_dir[i] = float(L[i])
+    p.epsilon = epsilon
+    p.seed = seed
+    return p

@@ -33,6 +33,20 @@ class Config(C.Structure):
                 ("max_steps", U32), ("reserved", U32 * 4)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("location", F32 * 4), ("origin", F32 * 4), ("right", F32 * 4), ("bottom", F32 * 4),
+                ("width", U32), ("height", U32), ("jitter", F32 * 2)]
+
+
+class BounceParams(C.Structure):
+    _fields_ = [("light_dir", F32 * 4), ("epsilon", F32), ("seed", U32), ("reserved", U32 * 2)]
+
+
+class CastOutputs(C.Structure):
+    _fields_ = [("primary_hits", P), ("secondary_rays", P), ("secondary_hits", P),
+                ("shadow_rays", P), ("shadow_occluded", P), ("counts", U32 * 3)]
+
+
 # (name, restype, argtypes)
 _SIGNATURES = [
     ("ae_bvh_build_triangles", C.c_int, [P, P, U32, C.c_int, C.POINTER(P)]),
@@ -49,6 +63,11 @@ _SIGNATURES = [
     ("ae_rt_mesh_upload", C.c_int, [P, P, U32, P, P, U32, C.POINTER(I32)]),
     ("ae_rt_trace_closest", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
     ("ae_rt_trace_any", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
+    ("ae_rt_raygen", C.c_int, [P, C.POINTER(Camera), P, P]),
+    ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),
+    ("ae_rt_trace_any_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),
+    ("ae_rt_spawn_bounce", C.c_int, [P, I32, P, P, P, U32, C.POINTER(BounceParams), P, P, P, P]),
+    ("ae_rt_cast_pass", C.c_int, [P, I32, C.POINTER(Camera), C.POINTER(BounceParams), C.POINTER(CastOutputs), P]),
     ("ae_rt_synchronize", C.c_int, [P, P]),
     ("ae_rt_get_fetch_counts", C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 ]

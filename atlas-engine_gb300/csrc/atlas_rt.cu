@@ -1,6 +1,7 @@
 // Device context, uploads and trace entry points of the C ABI (include/atlas_rt.h).
 #include "atlas_rt.h"
 #include "trace_kernels.cuh"
+#include "cast_kernels.cuh"
 
 #include <cuda_runtime.h>
 
@@ -66,6 +67,9 @@ struct ae_rt_ctx {
     uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
     unsigned long long* d_fetch = nullptr;
     Scratch rays_in, results_out;
+    // buffers of ae_rt_cast_pass
+    Scratch cast_primary, cast_primary_hits, cast_secondary, cast_secondary_hits, cast_shadow, cast_occluded;
+    uint32_t* d_cast_counts = nullptr;
     std::string last_error;
     std::mutex upload_mutex;
 };
@@ -150,7 +154,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, TraceParams& p, cudaStream_t s) {
 }
 
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
-                   float tmin, float tmax, void* out, void* stream) {
+                   float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr) {
     if (!ctx) return AE_RT_INVALID_ARG;
     if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
         return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
@@ -185,6 +189,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
     p.n_tris = m.n_tris;
     p.rays = static_cast<const float4*>(d_rays);
     p.n_rays = n_rays;
+    p.n_rays_dev = count_dev;
     p.tmin = tmin;
     p.tmax = tmax;
     p.hits = any ? nullptr : static_cast<float4*>(d_out);
@@ -232,6 +237,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 2 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_fetch, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_fetch, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cast_counts, 4 * sizeof(uint32_t));
     int occ = 0;
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(KernelFor<false, false>()),
@@ -255,8 +261,10 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     }
     cudaFree(ctx->d_counter);
     cudaFree(ctx->d_fetch);
-    ctx->rays_in.release();
-    ctx->results_out.release();
+    cudaFree(ctx->d_cast_counts);
+    for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->cast_primary, &ctx->cast_primary_hits,
+                         &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
+        sc->release();
     delete ctx;
 }
 
@@ -303,6 +311,128 @@ ae_rt_status ae_rt_trace_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packe
 ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                              float tmin, float tmax, uint8_t* occluded, void* stream) {
     return Trace(ctx, true, mesh_id, rays, n_rays, tmin, tmax, occluded, stream);
+}
+
+ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!cam || !rays) return Fail(ctx, AE_RT_INVALID_ARG, "null camera or ray buffer");
+    if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 30))
+        return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
+    if (!IsDevicePointer(rays)) return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_raygen writes device memory only");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    atlas::rt::dev::CameraParams c{};
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+    c.jx = cam->jitter[0]; c.jy = cam->jitter[1];
+    const uint32_t n = cam->width * cam->height;
+    atlas::rt::dev::raygen_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        c, reinterpret_cast<float4*>(rays));
+    AE_CUDA(ctx, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_trace_closest_queue(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                       const uint32_t* count, uint32_t capacity, float tmin, float tmax,
+                                       ae_hit* hits, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!count || !IsDevicePointer(count) || (capacity && (!IsDevicePointer(rays) || !IsDevicePointer(hits))))
+        return Fail(ctx, AE_RT_INVALID_ARG, "queue traces take device buffers");
+    return Trace(ctx, false, mesh_id, rays, capacity, tmin, tmax, hits, stream, count);
+}
+
+ae_rt_status ae_rt_trace_any_queue(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                   const uint32_t* count, uint32_t capacity, float tmin, float tmax,
+                                   uint8_t* occluded, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!count || !IsDevicePointer(count) || (capacity && (!IsDevicePointer(rays) || !IsDevicePointer(occluded))))
+        return Fail(ctx, AE_RT_INVALID_ARG, "queue traces take device buffers");
+    return Trace(ctx, true, mesh_id, rays, capacity, tmin, tmax, occluded, stream, count);
+}
+
+ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, const ae_hit* hits,
+                                const uint32_t* count, uint32_t n, const ae_bounce_params* params,
+                                ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts,
+                                void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
+        return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
+    if (!params || !counts) return Fail(ctx, AE_RT_INVALID_ARG, "null parameters");
+    if (n == 0) return AE_RT_OK;
+    if (!IsDevicePointer(rays) || !IsDevicePointer(hits) || !IsDevicePointer(secondary) ||
+        !IsDevicePointer(shadow) || !IsDevicePointer(counts) || (count && !IsDevicePointer(count)))
+        return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_spawn_bounce takes device buffers");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    atlas::rt::dev::SpawnParams sp{};
+    sp.rays = reinterpret_cast<const float4*>(rays);
+    sp.hits = reinterpret_cast<const float4*>(hits);
+    sp.n_dev = count;
+    sp.n = n;
+    sp.tris = ctx->meshes[size_t(mesh_id)].tris;
+    sp.secondary = reinterpret_cast<float4*>(secondary);
+    sp.shadow = reinterpret_cast<float4*>(shadow);
+    sp.counts = counts;
+    sp.lightx = params->light_dir[0]; sp.lighty = params->light_dir[1]; sp.lightz = params->light_dir[2];
+    sp.epsilon = params->epsilon;
+    sp.seed = params->seed;
+    atlas::rt::dev::spawn_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(sp);
+    AE_CUDA(ctx, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam,
+                             const ae_bounce_params* params, ae_cast_outputs* out, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!cam || !params || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null argument");
+    if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
+        return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
+    if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 30))
+        return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t n = cam->width * cam->height;
+    const size_t rb = size_t(n) * sizeof(ae_packed_ray), hb = size_t(n) * sizeof(ae_hit);
+    AE_CUDA(ctx, ctx->cast_primary.ensure(rb));
+    AE_CUDA(ctx, ctx->cast_primary_hits.ensure(hb));
+    AE_CUDA(ctx, ctx->cast_secondary.ensure(rb));
+    AE_CUDA(ctx, ctx->cast_secondary_hits.ensure(hb));
+    AE_CUDA(ctx, ctx->cast_shadow.ensure(rb));
+    AE_CUDA(ctx, ctx->cast_occluded.ensure(n));
+    auto* prim = static_cast<ae_packed_ray*>(ctx->cast_primary.ptr);
+    auto* primHits = static_cast<ae_hit*>(ctx->cast_primary_hits.ptr);
+    auto* sec = static_cast<ae_packed_ray*>(ctx->cast_secondary.ptr);
+    auto* secHits = static_cast<ae_hit*>(ctx->cast_secondary_hits.ptr);
+    auto* shd = static_cast<ae_packed_ray*>(ctx->cast_shadow.ptr);
+    auto* occ = static_cast<uint8_t*>(ctx->cast_occluded.ptr);
+    uint32_t* counts = ctx->d_cast_counts;
+    const float kInf = 1e12f;   // INF of common.hsh:8
+    ae_rt_status st;
+    if ((st = ae_rt_raygen(ctx, cam, prim, stream)) != AE_RT_OK) return st;
+    if ((st = Trace(ctx, false, mesh_id, prim, n, 0.0f, kInf, primHits, stream)) != AE_RT_OK) return st;
+    AE_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s));
+    if ((st = ae_rt_spawn_bounce(ctx, mesh_id, prim, primHits, nullptr, n, params, sec, shd, counts, stream)) != AE_RT_OK)
+        return st;
+    if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
+    const float shadowMax = kInf - 2.0f * params->epsilon;   // rayHit.csh:333
+    if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, stream, counts + 1)) != AE_RT_OK) return st;
+    uint32_t hc[2] = { 0, 0 };
+    AE_CUDA(ctx, cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    AE_CUDA(ctx, cudaStreamSynchronize(s));
+    out->counts[0] = n;
+    out->counts[1] = hc[0];
+    out->counts[2] = hc[1];
+    auto copy = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!dst || !bytes) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s);
+    };
+    AE_CUDA(ctx, copy(out->primary_hits, primHits, hb));
+    AE_CUDA(ctx, copy(out->secondary_rays, sec, size_t(hc[0]) * sizeof(ae_packed_ray)));
+    AE_CUDA(ctx, copy(out->secondary_hits, secHits, size_t(hc[0]) * sizeof(ae_hit)));
+    AE_CUDA(ctx, copy(out->shadow_rays, shd, size_t(hc[1]) * sizeof(ae_packed_ray)));
+    AE_CUDA(ctx, copy(out->shadow_occluded, occ, hc[1]));
+    return ae_rt_synchronize(ctx, stream);
 }
 
 ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {

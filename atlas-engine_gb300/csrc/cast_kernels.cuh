@@ -1,0 +1,171 @@
+// Wavefront stages around the traversal kernels: primary ray generation and
+// the bounce/shadow ray spawn that follows a closest-hit trace.
+//
+//  * raygen_kernel: pinhole camera rays from the frustum description of the
+//    engine's ray-gen pass (data/shader/pathtracer/rayGen.csh:25-91,
+//    PathTracingRenderer.cpp:157-160): dir = normalize(origin + right*u +
+//    bottom*v - location), u,v = (pixel + jitter) / resolution.  Rays are
+//    written in 8x8 tile order (as rayGen.csh:53-80 orders its queue) so that
+//    neighbouring lanes trace neighbouring pixels; ray.ID = pixel index.
+//    Arithmetic is explicitly rounded in a fixed order, so a host can
+//    regenerate the same rays bit for bit.
+//  * spawn_kernel: for every hit, one cosine-weighted diffuse bounce ray
+//    (origin pushed back along the view direction by EPSILON, as
+//    rayHit.csh:282) and, when the light is above the surface, one shadow
+//    ray towards a directional light (origin lifted along the normal by
+//    EPSILON, rayHit.csh:327-338).  Queue appends are warp-aggregated: one
+//    atomic per warp and queue (the reference takes one per ray,
+//    tracing.hsh:70-77).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace atlas::rt::dev {
+
+struct CameraParams {
+    float lx, ly, lz;       // location
+    float ox, oy, oz;       // top-left corner of the image plane
+    float rx, ry, rz;       // right span
+    float bx, by, bz;       // bottom span
+    uint32_t width, height;
+    float jx, jy;           // sub-pixel jitter
+};
+
+struct SpawnParams {
+    const float4* rays;
+    const float4* hits;        // 2 float4 per ae_hit
+    const uint32_t* n_dev;     // optional device count
+    uint32_t n;
+    const float4* tris;        // GPUBVHTriangle
+    float4* secondary;         // PackedRay queue
+    float4* shadow;            // PackedRay queue
+    uint32_t* counts;          // [0] secondary, [1] shadow
+    float lightx, lighty, lightz;
+    float epsilon;
+    uint32_t seed;
+};
+
+// Pixel index of queue slot i.
+__device__ __forceinline__ uint32_t slot_to_pixel(uint32_t i, uint32_t w, uint32_t h) {
+    if ((w & 7u) == 0 && (h & 7u) == 0) {
+        const uint32_t tile = i >> 6, local = i & 63u;
+        const uint32_t tilesX = w >> 3;
+        const uint32_t tx = tile % tilesX, ty = tile / tilesX;
+        return (ty * 8u + (local >> 3)) * w + tx * 8u + (local & 7u);
+    }
+    return i;
+}
+
+__global__ void raygen_kernel(CameraParams c, float4* rays) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = c.width * c.height;
+    if (i >= n) return;
+    const uint32_t pix = slot_to_pixel(i, c.width, c.height);
+    const float px = float(pix % c.width), py = float(pix / c.width);
+    const float u = __fdiv_rn(__fadd_rn(px, c.jx), float(c.width));
+    const float v = __fdiv_rn(__fadd_rn(py, c.jy), float(c.height));
+    const float qx = __fsub_rn(__fadd_rn(__fadd_rn(c.ox, __fmul_rn(c.rx, u)), __fmul_rn(c.bx, v)), c.lx);
+    const float qy = __fsub_rn(__fadd_rn(__fadd_rn(c.oy, __fmul_rn(c.ry, u)), __fmul_rn(c.by, v)), c.ly);
+    const float qz = __fsub_rn(__fadd_rn(__fadd_rn(c.oz, __fmul_rn(c.rz, u)), __fmul_rn(c.bz, v)), c.lz);
+    const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
+    const float inv = __frcp_rn(__fsqrt_rn(len2));
+    float4* r = rays + size_t(i) * 3;
+    r[0] = make_float4(c.lx, c.ly, c.lz, __int_as_float(int32_t(pix)));
+    r[1] = make_float4(__fmul_rn(qx, inv), __fmul_rn(qy, inv), __fmul_rn(qz, inv), 0.0f);
+    r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+}
+
+// Integer hash of Jarzynski & Olano, "Hash Functions for GPU Rendering"
+// (JCGT 2020), PCG variant.
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
+    const uint32_t state = x * 747796405u + 2891336453u;
+    const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+
+__device__ __forceinline__ float rand01(uint32_t a, uint32_t b, uint32_t c) {
+    const uint32_t h = pcg_hash(a ^ pcg_hash(b ^ pcg_hash(c)));
+    return float(h >> 8) * (1.0f / 16777216.0f);
+}
+
+// Orthonormal basis around a unit normal: Duff et al., "Building an
+// Orthonormal Basis, Revisited" (JCGT 2017).
+__device__ __forceinline__ void onb(float nx, float ny, float nz, float3& t, float3& b) {
+    const float sign = copysignf(1.0f, nz);
+    const float a = -1.0f / (sign + nz);
+    const float bb = nx * ny * a;
+    t = make_float3(1.0f + sign * nx * nx * a, sign * bb, -sign * nx);
+    b = make_float3(bb, sign + ny * ny * a, -ny);
+}
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want, uint32_t lane) {
+    const uint32_t mask = __ballot_sync(0xffffffffu, want);
+    uint32_t base = 0;
+    const uint32_t leader = mask ? (__ffs(mask) - 1) : 0;
+    if (mask && lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    uint32_t lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    return base + __popc(mask & lt);
+}
+
+__global__ void spawn_kernel(SpawnParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
+    bool sec = false, shd = false;
+    float3 P = make_float3(0, 0, 0), N = make_float3(0, 0, 0), D = make_float3(0, 0, 0), S = make_float3(0, 0, 0);
+    int32_t id = 0;
+    if (i < n) {
+        const float4 h0 = p.hits[size_t(i) * 2];
+        const int32_t tp = __float_as_int(h0.y);
+        if (tp >= 0) {
+            const float4 o4 = p.rays[size_t(i) * 3];
+            const float4 d4 = p.rays[size_t(i) * 3 + 1];
+            id = __float_as_int(o4.w);
+            const float t = h0.x;
+            P = make_float3(o4.x + t * d4.x, o4.y + t * d4.y, o4.z + t * d4.z);
+            const float4 a = __ldg(p.tris + size_t(tp) * 3), b = __ldg(p.tris + size_t(tp) * 3 + 1),
+                         c = __ldg(p.tris + size_t(tp) * 3 + 2);
+            const float3 e0 = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+            const float3 e1 = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
+            float3 n = make_float3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x);
+            const float inv = rsqrtf(fmaxf(n.x * n.x + n.y * n.y + n.z * n.z, 1e-30f));
+            n = make_float3(n.x * inv, n.y * inv, n.z * inv);
+            if (n.x * d4.x + n.y * d4.y + n.z * d4.z > 0.0f) n = make_float3(-n.x, -n.y, -n.z);
+            N = n;
+            // cosine-weighted bounce direction
+            const float r1 = rand01(uint32_t(id), p.seed, 0x68bc21ebu);
+            const float r2 = rand01(uint32_t(id), p.seed, 0x02e5be93u);
+            float sp, cp;
+            sincospif(2.0f * r1, &sp, &cp);
+            const float rad = sqrtf(r2);
+            const float lz = sqrtf(fmaxf(0.0f, 1.0f - r2));
+            float3 tg, bt;
+            onb(N.x, N.y, N.z, tg, bt);
+            D = make_float3(rad * cp * tg.x + rad * sp * bt.x + lz * N.x,
+                            rad * cp * tg.y + rad * sp * bt.y + lz * N.y,
+                            rad * cp * tg.z + rad * sp * bt.z + lz * N.z);
+            S = make_float3(P.x - d4.x * p.epsilon, P.y - d4.y * p.epsilon, P.z - d4.z * p.epsilon);
+            sec = true;
+            shd = N.x * p.lightx + N.y * p.lighty + N.z * p.lightz > 0.0f;
+        }
+    }
+    const uint32_t si = warp_append(p.counts, sec, lane);
+    if (sec) {
+        float4* r = p.secondary + size_t(si) * 3;
+        r[0] = make_float4(S.x, S.y, S.z, __int_as_float(id));
+        r[1] = make_float4(D.x, D.y, D.z, 0.0f);
+        r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+    }
+    const uint32_t hi = warp_append(p.counts + 1, shd, lane);
+    if (shd) {
+        float4* r = p.shadow + size_t(hi) * 3;
+        r[0] = make_float4(P.x + N.x * p.epsilon, P.y + N.y * p.epsilon, P.z + N.z * p.epsilon, __int_as_float(id));
+        r[1] = make_float4(p.lightx, p.lighty, p.lightz, 0.0f);
+        r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+    }
+}
+
+}  // namespace atlas::rt::dev

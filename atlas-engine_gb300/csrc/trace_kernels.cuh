@@ -42,7 +42,8 @@ struct TraceParams {
     uint32_t n_nodes;
     uint32_t n_tris;
     const float4* rays;          // 3 float4 per PackedRay
-    uint32_t n_rays;
+    uint32_t n_rays;             // ray count, or the queue capacity when n_rays_dev is set
+    const uint32_t* n_rays_dev;  // optional: ray count written by an earlier kernel
     float tmin;
     float tmax;
     float4* hits;                // 2 float4 per ae_hit (closest)
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     bool occl = false;
     unsigned long long nodeCount = 0, triCount = 0;
     const float tmin = p.tmin, tmax = p.tmax;
+    const uint32_t nRays = p.n_rays_dev ? min(*p.n_rays_dev, p.n_rays) : p.n_rays;
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
@@ -151,10 +153,10 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 uint32_t base = 0;
                 if (lane == leader) base = atomicAdd(p.work_counter, __popc(idle));
                 base = __shfl_sync(kFull, base, leader);
-                if (base + __popc(idle) >= p.n_rays) queueDry = true;
+                if (base + __popc(idle) >= nRays) queueDry = true;
                 if (!live) {
                     const uint32_t r = base + __popc(idle & lanemask_lt());
-                    if (r < p.n_rays) {
+                    if (r < nRays) {
                         rid = r;
                         const float4 o4 = ldg4(p.rays + size_t(r) * 3);
                         const float4 d4 = ldg4(p.rays + size_t(r) * 3 + 1);

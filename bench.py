@@ -1,0 +1,399 @@
+"""Benchmark of the GB300 ray-tracing hot path.
+
+Workload (one "step"): one ray-cast pass of a 1920x1080 pinhole camera over
+the terrain + boxes scene (512x512 value-noise heightfield over [0,100]^2,
+524,288 triangles, plus 200 boxes, 2,400 triangles): primary closest-hit
+rays, then per hit one cosine-weighted bounce ray (closest hit) and one
+shadow ray to a directional light (any hit).  The scene and BVH are built
+once (host builder, byte-identical to the reference builder) and stay in
+HBM; each step regenerates the camera rays on the device.
+
+value   = rays traced per second over the whole pass (primary + bounce +
+          shadow), CUDA events on the launching stream, L2 flushed between
+          steps (a 256 MiB write), max over ranks.
+e2e     = the same pass through the C ABI call ae_rt_cast_pass with pinned
+          host result buffers (results copied back inside the timed region).
+roofline: the primary closest-hit trace kernel; algorithmic bytes = per ray
+          (32 B ray read + 32 B hit write) + node fetches x 64 B + triangle
+          fetches x 48 B (fetch counts from the counting build of the same
+          kernel); bound = L2 (the 59 MB BVH is L2-resident), peak = an L2
+          copy bandwidth measured live on this GPU; the HBM fraction against
+          the measured copy peak is reported beside it.
+cpu_baseline: the oracle's C restatement of the reference's host query
+          (Volume::BVH::GetIntersection / GetIntersectionAny, bit-identical to
+          the compiled reference) on all host cores, over the same pass's rays.
+
+`--impl reference` times that CPU restatement alone (the reference has no
+GPU path usable here: its traversal is Vulkan compute).
+
+Multi-GPU: replicas only (each rank traces its own copy of the pass; no
+collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+
+W, H = 1920, 1080
+TMIN, TINF = 0.0, 1e12
+EPSILON = 0.1
+LIGHT = (0.4, 1.0, 0.3)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs"), "MEASURED_PEAKS.json"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"ae_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def build_scene():
+    from atlas_rt import BVH, scenes
+    tris, obj = scenes.terrain_boxes()
+    bvh = BVH(tris)
+    return tris, bvh, bvh.pack_triangles()
+
+
+def cpu_reference_pass(bvh, gt, prim_rays8, sec_rays8, shd_rays8, threads):
+    """The oracle's restatement of the reference host query over the pass's
+    rays.  Returns (seconds, rays)."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import pyoracle
+    pyoracle.build_port()
+    t0 = time.perf_counter()
+    pyoracle.closest_cpu(bvh.nodes_f32, gt, prim_rays8, threads)
+    pyoracle.closest_cpu(bvh.nodes_f32, gt, sec_rays8, threads)
+    pyoracle.any_cpu(bvh.nodes_f32, gt, shd_rays8, threads)
+    dt = time.perf_counter() - t0
+    return dt, len(prim_rays8) + len(sec_rays8) + len(shd_rays8)
+
+
+def rays8_from_packed(packed, tmin, tmax):
+    r = np.empty((len(packed), 8), np.float32)
+    r[:, 0:3] = packed[:, 0:3]
+    r[:, 3:6] = packed[:, 4:7]
+    r[:, 6] = tmin
+    r[:, 7] = tmax
+    return r
+
+
+def run_reference(args, rank):
+    """CPU arm: the restated reference host query over the full pass's rays
+    (generated once on the GPU-free host path: primary rays by the same
+    camera formula; bounce/shadow rays from the CPU closest hits)."""
+    from atlas_rt import scenes
+    if rank != 0:
+        return
+    tris, bvh, gt = build_scene()
+    cam = scenes.pinhole_camera(W, H)
+    o, d = scenes.pinhole_rays(cam)
+    prim = scenes.rays8(o, d, TMIN, TINF)
+    sys.path.insert(0, str(REPO / "oracle"))
+    import pyoracle
+    threads = os.cpu_count() or 1
+    # bounce / shadow rays: spawned on the host from the CPU hits (same rules
+    # as the GPU spawn stage: view-offset bounce origin, normal-offset shadow)
+    ptr, tuv = pyoracle.closest_cpu(bvh.nodes_f32, gt, prim, threads)
+    hit = ptr >= 0
+    P = o[hit] + tuv[hit, 0:1] * d[hit]
+    t = gt[ptr[hit]]
+    e0, e1 = t[:, 4:7] - t[:, 0:3], t[:, 8:11] - t[:, 0:3]
+    n = np.cross(e0, e1)
+    n /= np.linalg.norm(n, axis=1, keepdims=True) + 1e-30
+    n = np.where((n * d[hit]).sum(1, keepdims=True) > 0, -n, n).astype(np.float32)
+    rng = np.random.Generator(np.random.PCG64(1))
+    r1, r2 = rng.random(len(n)), rng.random(len(n))
+    a = np.cross(n, np.where(np.abs(n[:, :1]) > 0.9, [[0, 1, 0]], [[1, 0, 0]]))
+    a /= np.linalg.norm(a, axis=1, keepdims=True)
+    b = np.cross(n, a)
+    rad = np.sqrt(r2)[:, None]
+    phi = 2 * np.pi * r1[:, None]
+    sd = (rad * np.cos(phi) * a + rad * np.sin(phi) * b + np.sqrt(1 - r2)[:, None] * n).astype(np.float32)
+    sec = scenes.rays8((P - d[hit] * EPSILON).astype(np.float32), sd, TMIN, TINF)
+    L = np.asarray(LIGHT, np.float64)
+    L = (L / np.linalg.norm(L)).astype(np.float32)
+    lit = (n @ L) > 0
+    shd = scenes.rays8((P[lit] + n[lit] * EPSILON).astype(np.float32),
+                       np.broadcast_to(L, (int(lit.sum()), 3)).copy(), TMIN, TINF - 2 * EPSILON)
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, nrays = cpu_reference_pass(bvh, gt, prim, sec, shd, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    sec_per_step = float(np.mean(times))
+    value = nrays / sec_per_step / 1e6
+    line = {
+        "impl": "reference", "metric": "closest-hit Mrays/s at 1 GB300; radiance-cache vs plain PT time to equal rel-MSE",
+        "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec_per_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded terrain + boxes, 1920x1080 camera)",
+        "config": {"workload": "terrain_boxes_cast_1920x1080", "triangles": int(len(tris)),
+                   "rays_per_step": int(nrays), "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"full pass: {len(prim)} primary + {len(sec)} bounce closest-hit, "
+                                   f"{len(shd)} shadow any-hit rays"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def measure_l2_copy_gbs(torch, dev):
+    """Copy bandwidth of a 2 x 24 MiB working set that stays in L2."""
+    a = torch.empty(24 << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(5):
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / 50
+        gbs = 2 * a.numel() / (ms * 1e-3) / 1e9
+        best = gbs if best is None else max(best, gbs)
+    return best
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    import atlas_rt
+    from atlas_rt import scenes
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    tris, bvh, gt = build_scene()
+    ctx = atlas_rt.Context(device=local)
+    mid = ctx.upload_mesh(bvh.nodes, gt)
+    cam_d = scenes.pinhole_camera(W, H)
+    cam = atlas_rt.make_camera(cam_d)
+    bp = atlas_rt.make_bounce_params(LIGHT, EPSILON, seed=1)
+    n = W * H
+    f32 = torch.float32
+    prim = torch.empty((n, 12), dtype=f32, device=dev)
+    prim_hits = torch.empty((n, 8), dtype=f32, device=dev)
+    sec = torch.empty((n, 12), dtype=f32, device=dev)
+    sec_hits = torch.empty((n, 8), dtype=f32, device=dev)
+    shd = torch.empty((n, 12), dtype=f32, device=dev)
+    occ = torch.empty(n, dtype=torch.uint8, device=dev)
+    counts = torch.zeros(4, dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    launches_per_step = 5
+
+    def step(ev_trace=None):
+        ctx.raygen(cam, prim, stream)
+        if ev_trace is not None:
+            ev_trace[0].record(stream)
+        ctx.trace_closest(mid, prim, TMIN, TINF, out=prim_hits, stream=stream, n_rays=n)
+        if ev_trace is not None:
+            ev_trace[1].record(stream)
+        counts.zero_()
+        ctx.spawn_bounce(mid, prim, prim_hits, n, bp, sec, shd, counts, stream=stream)
+        ctx.trace_closest_queue(mid, sec, counts[0:1], n, TMIN, TINF, sec_hits, stream=stream)
+        ctx.trace_any_queue(mid, shd, counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize(stream)
+    n_sec, n_shd = (int(x) for x in counts[:2].cpu())
+    rays_per_step = n + n_sec + n_shd
+
+    # fetch counts of the primary trace (counting build, outside the timed region)
+    cctx = atlas_rt.Context(device=local, count_fetches=True)
+    cmid = cctx.upload_mesh(bvh.nodes, gt)
+    cctx.trace_closest(cmid, prim, TMIN, TINF, out=prim_hits, stream=stream, n_rays=n)
+    cctx.synchronize(stream)
+    node_f, tri_f = cctx.fetch_counts()
+    cctx.close()
+    step()
+    ctx.synchronize(stream)
+
+    l2_gbs = measure_l2_copy_gbs(torch, dev)
+    hbm_peak, hbm_src = load_peaks()
+
+    # ---- timed region: K steps, L2 flushed before each (untimed) ----
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    tev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        evs[k][0].record(stream)
+        step(tev[k])
+        evs[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    ctx.synchronize(stream)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    trace_ms = [a.elapsed_time(b) for a, b in tev]
+
+    # ---- end to end through the C ABI with pinned host result buffers ----
+    h_prim_hits = torch.empty((n, 8), dtype=f32, pin_memory=True)
+    h_sec_hits = torch.empty((n, 8), dtype=f32, pin_memory=True)
+    h_occ = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    for _ in range(2):
+        ctx.cast_pass(mid, cam, bp, primary_hits=h_prim_hits, secondary_hits=h_sec_hits,
+                      shadow_occluded=h_occ, stream=stream)
+    e2e_ms = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        c = ctx.cast_pass(mid, cam, bp, primary_hits=h_prim_hits, secondary_hits=h_sec_hits,
+                          shadow_occluded=h_occ, stream=stream)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    clk = clocks.stop()
+    assert c == (n, n_sec, n_shd), (c, n, n_sec, n_shd)
+    d2h = n * 32 + n_sec * 32 + n_shd
+    h2d = 96  # camera + bounce parameters
+
+    ms = float(np.mean(step_ms))
+    ms_trace = float(np.mean(trace_ms))
+    e2e = float(np.mean(e2e_ms))
+    if world > 1:
+        t = torch.tensor([ms, e2e, ms_trace], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e, ms_trace = (float(x) for x in t.cpu())
+    value = world * rays_per_step / (ms * 1e-3) / 1e6
+    e2e_value = world * rays_per_step / (e2e * 1e-3) / 1e6
+
+    alg_bytes = n * (32 + 32) + node_f * 64 + tri_f * 48
+    achieved = alg_bytes / (ms_trace * 1e-3) / 1e9
+    line = {
+        "metric": "closest-hit Mrays/s at 1 GB300; radiance-cache vs plain PT time to equal rel-MSE",
+        "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded terrain + boxes, 1920x1080 camera)",
+        "config": {"workload": "terrain_boxes_cast_1920x1080", "triangles": int(len(tris)),
+                   "rays_per_step": rays_per_step, "primary": n, "bounce": n_sec, "shadow": n_shd,
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": f"replicas x{world}"},
+        "breakdown": {"primary_closest_ms": ms_trace,
+                      "primary_closest_mrays_s": n / (ms_trace * 1e-3) / 1e6,
+                      "node_fetches_per_ray": node_f / n, "tri_fetches_per_ray": tri_f / n},
+        "roofline": {"bound": "l2", "kernel": "trace_kernel<closest> (primary rays)",
+                     "achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
+                     "peak_source": "L2-resident copy measured live (2 x 24 MiB)",
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "hbm_frac": achieved / hbm_peak, "hbm_peak": hbm_peak, "hbm_peak_source": hbm_src,
+                     "traffic": None},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "ae_rt_cast_pass, pinned host result buffers"},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # bounded sample: the pass's own rays, read back from the device
+        prim_np = prim.cpu().numpy()
+        sec_np = sec[:n_sec].cpu().numpy()
+        shd_np = shd[:n_shd].cpu().numpy()
+        threads = os.cpu_count() or 1
+        dt, nr = cpu_reference_pass(bvh, gt, rays8_from_packed(prim_np, TMIN, TINF),
+                                    rays8_from_packed(sec_np, TMIN, TINF),
+                                    rays8_from_packed(shd_np, TMIN, TINF - 2 * EPSILON), threads)
+        line["cpu_baseline"] = {"value": nr / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                "sample": f"one full pass: {n} primary + {n_sec} bounce closest-hit, "
+                                          f"{n_shd} shadow any-hit rays"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

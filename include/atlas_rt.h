@@ -244,6 +244,76 @@ ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ra
                              uint32_t n_rays, float tmin, float tmax, uint8_t* occluded,
                              void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Wavefront stages (device buffers, asynchronous on `stream`)               */
+/* ------------------------------------------------------------------------ */
+
+/* Pinhole camera in the form of the engine's ray-gen uniforms
+ * (PathTracingRenderer.h:49-57, PathTracingRenderer.cpp:157-160): `origin`
+ * is the image-plane corner of pixel (0,0) at unit distance, `right` and
+ * `bottom` span the image, `location` is the eye. */
+typedef struct ae_camera {
+    float location[4];
+    float origin[4];
+    float right[4];
+    float bottom[4];
+    uint32_t width;
+    uint32_t height;
+    float jitter[2];     /* sub-pixel offset in [0,1) */
+} ae_camera;
+
+/* Bounce / shadow ray spawn after a closest-hit trace. */
+typedef struct ae_bounce_params {
+    float light_dir[4];  /* unit direction towards the directional light */
+    float epsilon;       /* origin offset (the engine's EPSILON = 0.1, common.hsh:9) */
+    uint32_t seed;       /* random stream of the bounce directions */
+    uint32_t reserved[2];
+} ae_bounce_params;
+
+/* Writes width*height primary rays (8x8 tile order, ID = pixel index) into
+ * the device buffer `rays`.  Replaces the ray-gen dispatch
+ * RayTracingHelper::DispatchRayGen (RayTracingHelper.cpp:147-221) running
+ * rayGen.csh. */
+ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream);
+
+/* Queue-driven traces: the ray count is read on the device from `count`
+ * (written by an earlier kernel), at most `capacity`.  These replace the
+ * indirect-dispatch pair traceDispatch.csh + traceClosest.csh
+ * (RayTracingHelper.cpp:224-363) without a host round trip. */
+ae_rt_status ae_rt_trace_closest_queue(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                       const uint32_t* count, uint32_t capacity, float tmin, float tmax,
+                                       ae_hit* hits, void* stream);
+ae_rt_status ae_rt_trace_any_queue(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                   const uint32_t* count, uint32_t capacity, float tmin, float tmax,
+                                   uint8_t* occluded, void* stream);
+
+/* For every hit among the first min(*count, n) rays (count may be NULL):
+ * appends one cosine-weighted bounce ray to `secondary` and, when the light
+ * is above the surface, one shadow ray to `shadow`; counts[0] / counts[1]
+ * are incremented (the caller zeroes them).  Ray IDs are carried over.
+ * The hit-shader step of rayHit.csh:160-338 reduced to ray spawning. */
+ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, const ae_hit* hits,
+                                const uint32_t* count, uint32_t n, const ae_bounce_params* params,
+                                ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts,
+                                void* stream);
+
+/* One ray-cast pass of a camera over a mesh: primary closest-hit, bounce and
+ * shadow spawn, secondary closest-hit, shadow any-hit.  Output buffers may be
+ * host or device memory (any may be NULL); counts receives the number of
+ * primary, secondary and shadow rays.  Returns after the results are in
+ * place. */
+typedef struct ae_cast_outputs {
+    ae_hit* primary_hits;            /* width*height */
+    ae_packed_ray* secondary_rays;   /* up to width*height */
+    ae_hit* secondary_hits;
+    ae_packed_ray* shadow_rays;
+    uint8_t* shadow_occluded;
+    uint32_t counts[3];
+} ae_cast_outputs;
+
+ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam,
+                             const ae_bounce_params* params, ae_cast_outputs* out, void* stream);
+
 /* Waits for `stream` and reports device-side errors of the context's
  * preceding asynchronous calls (stack overflow, step cap, timeouts). */
 ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
