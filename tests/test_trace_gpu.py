@@ -212,17 +212,17 @@ def test_validator_rejects_bad_bvh(ctx):
 
 
 def comb_bvh(depth):
-    """A valid but degenerate BVH: node i has a leaf on the left and node i+1
-    on the right, every box the same.  A ray through the box visits the
-    right child first at every level (equal entry distances go left... the
-    leaf), so the stack grows by one entry per level."""
+    """A valid but degenerate BVH: node i has node i+1 on the left and a leaf
+    on the right, every box the same.  A ray through the box sees equal
+    entry distances, descends left (hitL <= hitR) and pushes the right leaf,
+    so the stack grows by one entry per level."""
     nodes = np.zeros(depth, atlas_rt.NODE_DTYPE)
     box_lo, box_hi = np.zeros(3, np.float32), np.ones(3, np.float32)
     for i in range(depth):
         nodes[i]["leftMin"], nodes[i]["leftMax"] = box_lo, box_hi
         nodes[i]["rightMin"], nodes[i]["rightMax"] = box_lo, box_hi
-        nodes[i]["leftPtr"] = ~i
-        nodes[i]["rightPtr"] = i + 1 if i + 1 < depth else ~depth
+        nodes[i]["leftPtr"] = i + 1 if i + 1 < depth else ~depth
+        nodes[i]["rightPtr"] = ~i
     tris = np.zeros((depth + 1, 12), np.float32)
     tris[:, 0:3] = [5, 5, 5]     # triangles far outside the ray path
     tris[:, 4:7] = [6, 5, 5]
