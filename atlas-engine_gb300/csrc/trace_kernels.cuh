@@ -121,7 +121,10 @@ struct LaneStack {
     static constexpr uint32_t capacity = SMEM + SPILL;
 };
 
-template <bool ANY, bool COUNT, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS>
+// BOUNDS = true adds range checks of every node and triangle index against
+// n_nodes / n_tris (for callers whose BVH did not pass the host validator);
+// an out-of-range index ends the ray with the overflow flag set.
+template <bool ANY, bool COUNT, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS, bool BOUNDS = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
     const uint32_t lane = threadIdx.x & 31u;
@@ -183,11 +186,22 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     done = true;
                     break;
                 }
+                if (BOUNDS && (node < 0 ? uint32_t(~node) >= p.n_tris : uint32_t(node) >= p.n_nodes)) {
+                    flags |= kHitFlagOverflow;
+                    atomicOr(p.error_word, kErrStackOverflow);
+                    done = true;
+                    break;
+                }
                 if (node < 0) {
                     // Leaf: contiguous triangles up to the end-of-node flag.
                     int32_t tp = ~node;
                     bool end = false;
                     do {
+                        if (BOUNDS && uint32_t(tp) >= p.n_tris) {
+                            flags |= kHitFlagOverflow;
+                            atomicOr(p.error_word, kErrStackOverflow);
+                            break;
+                        }
                         const float4 a = ldg4(p.tris + size_t(tp) * 3);
                         const float4 b = ldg4(p.tris + size_t(tp) * 3 + 1);
                         const float4 c = ldg4(p.tris + size_t(tp) * 3 + 2);
@@ -207,6 +221,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         }
                         tp++;
                     } while (!end);
+                    if (BOUNDS && (flags & kHitFlagOverflow)) { done = true; break; }
                     if (ANY && occl) { done = true; break; }
                     if (sp == 0) { done = true; break; }
                     node = st.get(--sp);

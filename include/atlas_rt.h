@@ -244,6 +244,33 @@ ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ra
                              uint32_t n_rays, float tmin, float tmax, uint8_t* occluded,
                              void* stream);
 
+/* Closest hit against one mesh without any device allocation.  This entry
+ * point has no counterpart in the reference.  It is for hosts that own all
+ * device memory and do not let a library call cudaMalloc / cudaFree -- an
+ * engine that carves every GPU buffer out of its own arenas at load time, or
+ * a frame loop that must not hit the implicit device synchronisation those
+ * calls bring -- and so cannot create an ae_rt_ctx.
+ *  - nodes, tris, rays and hits are device pointers the caller owns; the BVH
+ *    need not have passed the upload validator: node and triangle indices are
+ *    range-checked on the device, and a bad one ends that ray with
+ *    AE_HIT_OVERFLOW in its flags.
+ *  - Results and semantics are those of ae_rt_trace_closest.  The call is
+ *    asynchronous on `stream` (NULL = legacy default stream) and reports
+ *    device-side failures per ray in ae_hit.flags (AE_HIT_OVERFLOW,
+ *    AE_HIT_ITER_CAP) rather than through a status.
+ *  - Its only scratch is a 256-byte static device array per GPU (work
+ *    counter and error word), which each call re-zeroes; calls that overlap
+ *    on the GPU race on it, so issue them in one stream or order them.
+ *  - The first call on a device looks up that array's device address and
+ *    the kernel's occupancy; make it before any stream capture.
+ *  - n_rays above AE_RT_NOALLOC_MAX_RAYS is rejected with AE_RT_INVALID_ARG
+ *    (the work counter is 32 bits wide), as are host pointers. */
+#define AE_RT_NOALLOC_MAX_RAYS (1u << 30)
+ae_rt_status ae_rt_trace_closest_noalloc(const ae_bvh_node* nodes, uint32_t n_nodes,
+                                         const ae_bvh_triangle* tris, uint32_t n_tris,
+                                         const ae_packed_ray* rays, uint32_t n_rays, float tmin, float tmax,
+                                         ae_hit* hits, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Wavefront stages (device buffers, asynchronous on `stream`)               */
 /* ------------------------------------------------------------------------ */
