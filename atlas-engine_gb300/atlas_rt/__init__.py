@@ -216,6 +216,11 @@ class Context:
     def synchronize(self, stream=None):
         _check(lib().ae_rt_synchronize(self._h, _stream_handle(stream)), self._h)
 
+    def selftest_division(self, n: int, seed: int = 1) -> int:
+        m = C.c_uint64()
+        _check(lib().ae_rt_selftest_division(self._h, n, seed, C.byref(m)), self._h)
+        return m.value
+
     def fetch_counts(self):
         a, b = C.c_uint64(), C.c_uint64()
         _check(lib().ae_rt_get_fetch_counts(self._h, C.byref(a), C.byref(b)), self._h)

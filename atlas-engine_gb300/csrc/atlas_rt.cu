@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -210,6 +211,46 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
 
 }  // namespace
 
+namespace {
+
+// Random float with |v| in [2^lo, 2^hi] (random sign, mantissa, exponent), or
+// a structured special case (power of two, all-ones mantissa, zero).
+__device__ __forceinline__ float selftest_float(uint32_t h1, uint32_t h2, int lo, int hi, bool allow_zero) {
+    const uint32_t kind = h2 & 15u;
+    if (allow_zero && kind == 0) return (h1 & 1u) ? -0.0f : 0.0f;
+    const int e = lo + int((h2 >> 4) % uint32_t(hi - lo + 1));
+    uint32_t mant = h1 & 0x7fffffu;
+    if (kind == 1) mant = 0;                 // power of two
+    if (kind == 2) mant = 0x7fffffu;         // just below the next power of two
+    if (kind == 3) mant = 1;                 // just above a power of two
+    const uint32_t bits = ((h1 >> 31) << 31) | (uint32_t(e + 127) << 23) | mant;
+    return __uint_as_float(bits);
+}
+
+__global__ void selftest_division_kernel(uint64_t n, uint32_t seed, unsigned long long* mismatches) {
+    using namespace atlas::rt::dev;
+    unsigned long long bad = 0;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t k = uint32_t(i) ^ uint32_t(i >> 32) * 0x9E3779B9u;
+        const uint32_t h0 = pcg_hash(k ^ seed), h1 = pcg_hash(h0), h2 = pcg_hash(h1), h3 = pcg_hash(h2);
+        const uint32_t h4 = pcg_hash(h3), h5 = pcg_hash(h4);
+        // a = c - o with c, o in the coordinate window, d in the direction window
+        const float c = selftest_float(h0, h1, -40, 39, true);
+        float o = selftest_float(h2, h3, -40, 39, true);
+        if ((h5 & 7u) == 0) o = __uint_as_float(__float_as_uint(c) ^ (h5 & 0xffu)); // nearly equal pair
+        const float d = selftest_float(h4, h5, -40, 39, false);
+        const float a = __fsub_rn(c, o);
+        const float ref = __fdiv_rn(a, d);
+        const float got = div_rn_from_rcp(a, d, __frcp_rn(d));
+        if (__float_as_uint(ref) != __float_as_uint(got) && !(ref == 0.0f && got == 0.0f)) bad++;
+    }
+    for (int off = 16; off > 0; off >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, off);
+    if ((threadIdx.x & 31u) == 0 && bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace
+
 extern "C" {
 
 ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
@@ -289,7 +330,20 @@ ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_
         if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
         return e;
     };
-    cudaError_t e = upload(&m.nodes, nodes, size_t(n_nodes) * sizeof(ae_bvh_node));
+    // Device copy of the nodes with padding0 = 1 on nodes holding a coordinate
+    // outside the traversal kernel's fast-division window (0 or 2^-40..2^40).
+    std::vector<ae_bvh_node> flagged(nodes, nodes + n_nodes);
+    for (auto& nd : flagged) {
+        const float* c = nd.leftAABB.min;
+        bool ok = true;
+        for (int k = 0; k < 12; k++) {
+            const float a = std::fabs(c[k]);
+            ok = ok && (a == 0.0f || (a >= 9.094947017729282e-13f && a <= 1.099511627776e12f));
+        }
+        nd.padding0 = ok ? 0 : 1;
+        nd.padding1 = 0;
+    }
+    cudaError_t e = upload(&m.nodes, flagged.data(), size_t(n_nodes) * sizeof(ae_bvh_node));
     if (e == cudaSuccess) e = upload(&m.tris, tris, size_t(n_tris) * sizeof(ae_bvh_triangle));
     if (e == cudaSuccess && shading) e = upload(&m.shading, shading, size_t(n_tris) * sizeof(ae_triangle));
     if (e != cudaSuccess) {
@@ -448,6 +502,18 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
                                                    std::to_string(kSmemStack + kSpillStack) + " stack entries");
         return Fail(ctx, AE_RT_ITERATION_LIMIT, "a ray exceeded the traversal step cap");
     }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_selftest_division(ae_rt_ctx* ctx, uint64_t n, uint32_t seed, uint64_t* mismatches) {
+    if (!ctx || !mismatches) return AE_RT_INVALID_ARG;
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    AE_CUDA(ctx, cudaMemset(ctx->d_fetch, 0, sizeof(unsigned long long)));
+    selftest_division_kernel<<<uint32_t(ctx->sm_count) * 8u, 256>>>(n, seed, ctx->d_fetch);
+    AE_CUDA(ctx, cudaGetLastError());
+    unsigned long long h = 0;
+    AE_CUDA(ctx, cudaMemcpy(&h, ctx->d_fetch, sizeof(h), cudaMemcpyDeviceToHost));
+    *mismatches = h;
     return AE_RT_OK;
 }
 

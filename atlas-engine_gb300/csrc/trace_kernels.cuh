@@ -62,12 +62,52 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
+// Correctly rounded a / b from y = RN(1/b) without a divide instruction:
+// q0 = RN(a*y) is within 1.5 ulp of a/b; one residual correction
+// q1 = RN(q0 + RN(a - b*q0)*y) makes it faithful; with a faithful quotient the
+// residual a - b*q1 is exact (computed by FMA) and Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990) gives RN(q1 + r1*y) = RN(a/b).
+// Valid while no intermediate under- or overflows, which the callers ensure
+// by range (see kFastLo / kFastHi); everything else takes div.rn.
+__device__ __forceinline__ float div_rn_from_rcp(float a, float b, float y) {
+    float q = __fmul_rn(a, y);
+    float r = __fmaf_rn(-q, b, a);
+    q = __fmaf_rn(r, y, q);
+    r = __fmaf_rn(-q, b, a);
+    return __fmaf_rn(r, y, q);
+}
+
+// Exponent window of the fast quotient: every |origin|, |box coordinate| is 0
+// or in [2^-40, 2^40] and every |direction| in [2^-40, 2^40], so |a| = |c - o|
+// is 0 or in [2^-63, 2^41] and all intermediates stay normal.
+constexpr float kFastLo = 9.094947017729282e-13f;   // 2^-40
+constexpr float kFastHi = 1.099511627776e12f;       // 2^40
+
+__device__ __forceinline__ bool in_fast_range(float v, bool zero_ok) {
+    const float m = fabsf(v);
+    return (zero_ok && m == 0.0f) || (m >= kFastLo && m <= kFastHi);
+}
+
 // IntersectAABB(ray, aabb, tmin, tmax, out dist) -- intersections.hsh:18-34.
+// FAST: quotients through div_rn_from_rcp with (yx, yy, yz) = RN(1/d); the
+// result is bit-identical to the div.rn form.
+template <bool FAST>
 __device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx, float dy, float dz,
+                                         float yx, float yy, float yz,
                                          float lx, float ly, float lz, float hx, float hy, float hz,
                                          float tmin, float tmax, float& dist) {
-    const float t0x = fdiv(fsub(lx, ox), dx), t0y = fdiv(fsub(ly, oy), dy), t0z = fdiv(fsub(lz, oz), dz);
-    const float t1x = fdiv(fsub(hx, ox), dx), t1y = fdiv(fsub(hy, oy), dy), t1z = fdiv(fsub(hz, oz), dz);
+    float t0x, t0y, t0z, t1x, t1y, t1z;
+    if (FAST) {
+        t0x = div_rn_from_rcp(fsub(lx, ox), dx, yx);
+        t0y = div_rn_from_rcp(fsub(ly, oy), dy, yy);
+        t0z = div_rn_from_rcp(fsub(lz, oz), dz, yz);
+        t1x = div_rn_from_rcp(fsub(hx, ox), dx, yx);
+        t1y = div_rn_from_rcp(fsub(hy, oy), dy, yy);
+        t1z = div_rn_from_rcp(fsub(hz, oz), dz, yz);
+    } else {
+        t0x = fdiv(fsub(lx, ox), dx); t0y = fdiv(fsub(ly, oy), dy); t0z = fdiv(fsub(lz, oz), dz);
+        t1x = fdiv(fsub(hx, ox), dx); t1y = fdiv(fsub(hy, oy), dy); t1z = fdiv(fsub(hz, oz), dz);
+    }
     const float sx = fminf(t0x, t1x), sy = fminf(t0y, t1y), sz = fminf(t0z, t1z);
     const float bx = fmaxf(t0x, t1x), by = fmaxf(t0y, t1y), bz = fmaxf(t0z, t1z);
     const float tminf = fmaxf(fmaxf(tmin, sx), fmaxf(sy, sz));
@@ -138,6 +178,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     bool queueDry = false;          // warp-uniform
     uint32_t rid = 0;
     float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
+    float yx = 0, yy = 0, yz = 0;   // RN(1/d)
+    bool rayFast = false;
     float hitDist = 0, second = 0, hu = 0, hv = 0;
     int32_t hitID = -1;
     int32_t node = 0;
@@ -165,6 +207,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         const float4 d4 = ldg4(p.rays + size_t(r) * 3 + 1);
                         ox = o4.x; oy = o4.y; oz = o4.z;
                         dx = d4.x; dy = d4.y; dz = d4.z;
+                        yx = __frcp_rn(dx); yy = __frcp_rn(dy); yz = __frcp_rn(dz);
+                        rayFast = in_fast_range(ox, true) && in_fast_range(oy, true) && in_fast_range(oz, true) &&
+                                  in_fast_range(dx, false) && in_fast_range(dy, false) && in_fast_range(dz, false);
                         hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
                         hitID = -1; node = 0; sp = 0; steps = 0; flags = 0; occl = false;
                         live = true;
@@ -232,10 +277,21 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
                     const float bound = ANY ? tmax : hitDist;
                     float hl, hr;
-                    const bool il = box_test(ox, oy, oz, dx, dy, dz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y,
-                                             tmin, bound, hl);
-                    const bool ir = box_test(ox, oy, oz, dx, dy, dz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w,
-                                             tmin, bound, hr);
+                    bool il, ir;
+                    // node.padding0 != 0 marks a node with a coordinate outside the fast window
+                    // (set by the upload); such nodes and out-of-window rays divide with div.rn,
+                    // as does the BOUNDS variant, whose nodes did not go through the upload.
+                    if (!BOUNDS && rayFast && __float_as_int(n3.z) == 0) {
+                        il = box_test<true>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n0.x, n0.y, n0.z, n0.w, n1.x,
+                                            n1.y, tmin, bound, hl);
+                        ir = box_test<true>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n1.z, n1.w, n2.x, n2.y, n2.z,
+                                            n2.w, tmin, bound, hr);
+                    } else {
+                        il = box_test<false>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n0.x, n0.y, n0.z, n0.w, n1.x,
+                                             n1.y, tmin, bound, hl);
+                        ir = box_test<false>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n1.z, n1.w, n2.x, n2.y, n2.z,
+                                             n2.w, tmin, bound, hr);
+                    }
                     int32_t next, far;
                     if (ANY) {
                         next = il ? lptr : rptr;

@@ -351,6 +351,13 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
 #define AE_RT_CFG_COUNT_FETCHES 0x1u
 ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
 
+/* Device self-test of the traversal kernel's divide-free slab arithmetic:
+ * compares it bit for bit with div.rn.f32 on n generated operand pairs from
+ * the kernel's fast window (coordinates 0 or of magnitude 2^-40..2^40, ray
+ * directions of magnitude 2^-40..2^40) and returns the mismatch count
+ * (0 expected).  Diagnostic only; uses the context's fetch-count scratch. */
+ae_rt_status ae_rt_selftest_division(ae_rt_ctx* ctx, uint64_t n, uint32_t seed, uint64_t* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

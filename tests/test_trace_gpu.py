@@ -279,3 +279,11 @@ def test_fetch_counts_match_oracle():
         assert nodes == int(nf.sum()) and trisf == int(tf.sum())
     finally:
         c.close()
+
+
+def test_divide_free_slab_quotient_is_correctly_rounded(ctx):
+    """The traversal kernel's slab quotients come from RN(1/d) and two FMA
+    corrections; on the operand window the kernel uses them for, they must
+    equal div.rn.f32 bit for bit."""
+    assert ctx.selftest_division(1 << 31, seed=12345) == 0
+    assert ctx.selftest_division(1 << 28, seed=777) == 0
