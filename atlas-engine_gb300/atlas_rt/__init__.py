@@ -28,7 +28,9 @@ NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("leftPtr", "<i4"), ("rightPtr", "<i4"), ("padding", "<i4", 2)])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("triPtr", "<i4"), ("instance", "<i4"), ("flags", "<u4"),
                       ("u", "<f4"), ("v", "<f4"), ("tSecond", "<f4"), ("reserved", "<i4")])
-assert NODE_DTYPE.itemsize == 64 and HIT_DTYPE.itemsize == 32
+INSTANCE_DTYPE = np.dtype([("inverseMatrix", "<f4", 12), ("meshOffset", "<i4"), ("materialOffset", "<i4"),
+                           ("nextInstance", "<i4"), ("mask", "<u4")])
+assert NODE_DTYPE.itemsize == 64 and HIT_DTYPE.itemsize == 32 and INSTANCE_DTYPE.itemsize == 64
 
 HIT_FLAG_HIT = 0x1
 HIT_FLAG_NEAR_TIE = 0x2
@@ -181,6 +183,55 @@ class Context:
                                      _stream_handle(stream)), self._h)
         return out
 
+    # ---- two-level scene ----
+    def scene_set(self, tlas_nodes, instances):
+        tlas_nodes = np.ascontiguousarray(tlas_nodes)
+        instances = np.ascontiguousarray(instances, INSTANCE_DTYPE)
+        _check(lib().ae_rt_scene_set(self._h, _ptr(tlas_nodes) if tlas_nodes.size else None,
+                                     tlas_nodes.nbytes // 64, _ptr(instances) if len(instances) else None,
+                                     len(instances)), self._h)
+
+    def scene_build(self, instances, world_aabbs):
+        """RayTracingWorld-style top level; returns the input index of each
+        ordered instance."""
+        instances = np.ascontiguousarray(instances, INSTANCE_DTYPE)
+        boxes = np.ascontiguousarray(world_aabbs, np.float32).reshape(-1, 6)
+        order = np.zeros(len(instances) + 1, np.uint32)
+        n = C.c_uint32()
+        _check(lib().ae_rt_scene_build(self._h, _ptr(instances), _ptr(boxes), len(instances), _ptr(order),
+                                       C.byref(n)), self._h)
+        return order[:n.value]
+
+    def trace_scene_closest(self, rays, tmin, tmax, cull_mask=0xFFFFFFFF, out=None, stream=None,
+                            n_rays: int | None = None):
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, HIT_DTYPE)
+        _check(lib().ae_rt_trace_scene_closest(self._h, _ptr(rays), n_rays, tmin, tmax, cull_mask, _ptr(out),
+                                               _stream_handle(stream)), self._h)
+        return out
+
+    def trace_scene_any(self, rays, tmin, tmax, cull_mask=0xFFFFFFFF, out=None, stream=None,
+                        n_rays: int | None = None):
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, np.uint8)
+        _check(lib().ae_rt_trace_scene_any(self._h, _ptr(rays), n_rays, tmin, tmax, cull_mask, _ptr(out),
+                                           _stream_handle(stream)), self._h)
+        return out
+
+    def trace_scene_closest_queue(self, rays, count, capacity, tmin, tmax, hits, cull_mask=0xFFFFFFFF,
+                                  stream=None):
+        _check(lib().ae_rt_trace_scene_closest_queue(self._h, _ptr(rays), _ptr(count), capacity, tmin, tmax,
+                                                     cull_mask, _ptr(hits), _stream_handle(stream)), self._h)
+
+    def trace_scene_any_queue(self, rays, count, capacity, tmin, tmax, occluded, cull_mask=0xFFFFFFFF,
+                              stream=None):
+        _check(lib().ae_rt_trace_scene_any_queue(self._h, _ptr(rays), _ptr(count), capacity, tmin, tmax,
+                                                 cull_mask, _ptr(occluded), _stream_handle(stream)), self._h)
+
     # ---- wavefront stages (device buffers) ----
     def raygen(self, cam: "Camera", rays, stream=None):
         _check(lib().ae_rt_raygen(self._h, C.byref(cam), _ptr(rays), _stream_handle(stream)), self._h)
@@ -249,3 +300,40 @@ def make_bounce_params(light_dir=(0.4, 1.0, 0.3), epsilon=0.1, seed=1) -> Bounce
     p.epsilon = epsilon
     p.seed = seed
     return p
+
+
+def make_instance(model, mesh_id: int, mask: int = MASK_ALL | MASK_SHADOW, material_offset: int = 0):
+    """GPUBVHInstance for an object-to-world affine `model` (3x4 or 4x4): the
+    mat3x4 columns are the rows of the inverse model matrix
+    (RayTracingWorld.cpp:100), computed in double and stored as float."""
+    M = np.eye(4)
+    m = np.asarray(model, np.float64)
+    M[: m.shape[0], : m.shape[1]] = m
+    inv = np.linalg.inv(M)
+    rec = np.zeros((), INSTANCE_DTYPE)
+    rec["inverseMatrix"] = inv[:3, :4].reshape(-1).astype(np.float32)
+    rec["meshOffset"] = mesh_id
+    rec["materialOffset"] = material_offset
+    rec["nextInstance"] = -1
+    rec["mask"] = mask
+    return rec
+
+
+def transform_aabb(lo, hi, model):
+    """AABB::Transform (AABB.cpp:33-56): the box of the 8 transformed corners."""
+    M = np.asarray(model, np.float64)
+    corners = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])],
+                       np.float64)
+    w = corners @ M[:3, :3].T + M[:3, 3]
+    return np.concatenate([w.min(0), w.max(0)]).astype(np.float32)
+
+
+def mesh_bounds(bvh: "BVH"):
+    """Root box of a mesh BVH: the union of the root's two child boxes."""
+    if len(bvh.nodes) == 0:
+        v = bvh._verts.reshape(-1, 3)
+        return v.min(0), v.max(0)
+    r = bvh.nodes[0]
+    lo = np.minimum(r["leftMin"], r["rightMin"])
+    hi = np.maximum(r["leftMax"], r["rightMax"])
+    return lo, hi

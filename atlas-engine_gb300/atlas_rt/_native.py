@@ -63,6 +63,12 @@ _SIGNATURES = [
     ("ae_rt_mesh_upload", C.c_int, [P, P, U32, P, P, U32, C.POINTER(I32)]),
     ("ae_rt_trace_closest", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
     ("ae_rt_trace_any", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
+    ("ae_rt_scene_set", C.c_int, [P, P, U32, P, U32]),
+    ("ae_rt_scene_build", C.c_int, [P, P, P, U32, P, P]),
+    ("ae_rt_trace_scene_closest", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_scene_any", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_scene_closest_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_scene_any_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_closest_noalloc", C.c_int, [P, U32, P, U32, P, U32, F32, F32, P, P]),
     ("ae_rt_raygen", C.c_int, [P, C.POINTER(Camera), P, P]),
     ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),

@@ -2,6 +2,7 @@
 #include "atlas_rt.h"
 #include "trace_kernels.cuh"
 #include "cast_kernels.cuh"
+#include "bvh_builder.h"
 
 #include <cuda_runtime.h>
 
@@ -22,10 +23,19 @@ constexpr int kSmemStack = 32;     // shared-memory stack entries per lane (the 
 constexpr int kSpillStack = 32;    // local-memory entries behind them
 constexpr int kMinBlocks = 8;
 
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool TLAS>
 void* KernelFor() {
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<ANY, COUNT, kWarps, kSmemStack, kSpillStack, kMinBlocks>);
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, TLAS, kWarps, kSmemStack, kSpillStack, kMinBlocks>);
+}
+
+void* PickKernel(bool any, bool count, bool tlas) {
+    if (tlas) {
+        if (any) return count ? KernelFor<true, true, true>() : KernelFor<true, false, true>();
+        return count ? KernelFor<false, true, true>() : KernelFor<false, false, true>();
+    }
+    if (any) return count ? KernelFor<true, true, false>() : KernelFor<true, false, false>();
+    return count ? KernelFor<false, true, false>() : KernelFor<false, false, false>();
 }
 
 struct DeviceMesh {
@@ -65,6 +75,15 @@ struct ae_rt_ctx {
     uint32_t max_steps_cfg = 0;
     bool count_fetches = false;
     std::vector<DeviceMesh> meshes;
+    // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot
+    float4* d_tlas = nullptr;
+    uint32_t n_tlas = 0;
+    float4* d_instances = nullptr;
+    uint32_t n_instances = 0;
+    atlas::rt::dev::MeshDesc* d_mesh_table = nullptr;
+    uint32_t n_mesh_table = 0;
+    uint32_t scene_steps = 0;
+    bool scene_ready = false;
     uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
     unsigned long long* d_fetch = nullptr;
     Scratch rays_in, results_out;
@@ -104,6 +123,23 @@ bool IsDevicePointer(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Copy of `nodes` with padding0 = 1 on nodes holding a coordinate outside the
+// traversal kernel's fast-division window (0 or 2^-40..2^40), 0 elsewhere.
+std::vector<ae_bvh_node> FlagNodes(const ae_bvh_node* nodes, uint32_t n) {
+    std::vector<ae_bvh_node> out(nodes, nodes + n);
+    for (auto& nd : out) {
+        const float* c = nd.leftAABB.min;
+        bool ok = true;
+        for (int k = 0; k < 12; k++) {
+            const float a = std::fabs(c[k]);
+            ok = ok && (a == 0.0f || (a >= 9.094947017729282e-13f && a <= 1.099511627776e12f));
+        }
+        nd.padding0 = ok ? 0 : 1;
+        nd.padding1 = 0;
+    }
+    return out;
+}
+
 // Host-side BVH validation before upload: child pointers in range, inner
 // children after their parent (pre-order, which rules out cycles), and every
 // referenced leaf terminated by an end-of-node flag inside the buffer.
@@ -139,11 +175,10 @@ uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
     return 4u * m.n_nodes + 64u;
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, TraceParams& p, cudaStream_t s) {
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, bool tlas, TraceParams& p, cudaStream_t s) {
     AE_CUDA(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
-    void* fn = any ? (ctx->count_fetches ? KernelFor<true, true>() : KernelFor<true, false>())
-                   : (ctx->count_fetches ? KernelFor<false, true>() : KernelFor<false, false>());
+    void* fn = PickKernel(any, ctx->count_fetches, tlas);
     // Persistent grid: never more CTAs than can be resident, never more warps than rays.
     uint32_t grid = uint32_t(ctx->sm_count) * ctx->blocks_per_sm;
     const uint32_t needed = (p.n_rays + kWarps * 32 - 1) / (kWarps * 32);
@@ -154,17 +189,23 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, TraceParams& p, cudaStream_t s) {
     return AE_RT_OK;
 }
 
+constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
+
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
-                   float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr) {
+                   float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
+                   uint32_t cull_mask = 0xffffffffu) {
     if (!ctx) return AE_RT_INVALID_ARG;
-    if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
+    const bool scene = mesh_id == kSceneTarget;
+    if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
+    if (!scene && (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size()))
         return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
     if (n_rays == 0) return AE_RT_OK;
     if (!rays || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray or result buffer");
     if (n_rays > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one call");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const DeviceMesh& m = ctx->meshes[size_t(mesh_id)];
+    static const DeviceMesh kNoMesh;
+    const DeviceMesh& m = scene ? kNoMesh : ctx->meshes[size_t(mesh_id)];
 
     const size_t ray_bytes = size_t(n_rays) * sizeof(ae_packed_ray);
     const size_t out_bytes = size_t(n_rays) * (any ? 1 : sizeof(ae_hit));
@@ -198,8 +239,17 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
     p.work_counter = ctx->d_counter;
     p.error_word = ctx->d_counter + 1;
     p.fetch_counts = ctx->d_fetch;
-    p.max_steps = MaxSteps(ctx, m);
-    ae_rt_status st = Launch(ctx, any, p, s);
+    p.max_steps = scene ? (ctx->max_steps_cfg ? ctx->max_steps_cfg : ctx->scene_steps) : MaxSteps(ctx, m);
+    if (scene) {
+        p.tlas = ctx->d_tlas;
+        p.n_tlas = ctx->n_tlas;
+        p.instances = ctx->d_instances;
+        p.n_instances = ctx->n_instances;
+        p.meshes = ctx->d_mesh_table;
+        p.n_meshes = ctx->n_mesh_table;
+        p.cull_mask = cull_mask;
+    }
+    ae_rt_status st = Launch(ctx, any, scene, p, s);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -238,7 +288,8 @@ __global__ void selftest_division_kernel(uint64_t n, uint32_t seed, unsigned lon
         // a = c - o with c, o in the coordinate window, d in the direction window
         const float c = selftest_float(h0, h1, -40, 39, true);
         float o = selftest_float(h2, h3, -40, 39, true);
-        if ((h5 & 7u) == 0) o = __uint_as_float(__float_as_uint(c) ^ (h5 & 0xffu)); // nearly equal pair
+        // nearly equal pair (a tiny difference); c = 0 would make o subnormal, outside the window
+        if ((h5 & 7u) == 0 && c != 0.0f) o = __uint_as_float(__float_as_uint(c) ^ (h5 & 0xffu));
         const float d = selftest_float(h4, h5, -40, 39, false);
         const float a = __fsub_rn(c, o);
         const float ref = __fdiv_rn(a, d);
@@ -281,7 +332,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cast_counts, 4 * sizeof(uint32_t));
     int occ = 0;
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(KernelFor<false, false>()),
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(KernelFor<false, false, false>()),
                                                           kWarps * 32, 0);
     if (e != cudaSuccess) {
         ae_rt_ctx_destroy(ctx);
@@ -303,6 +354,9 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     cudaFree(ctx->d_counter);
     cudaFree(ctx->d_fetch);
     cudaFree(ctx->d_cast_counts);
+    cudaFree(ctx->d_tlas);
+    cudaFree(ctx->d_instances);
+    cudaFree(ctx->d_mesh_table);
     for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
         sc->release();
@@ -330,19 +384,7 @@ ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_
         if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
         return e;
     };
-    // Device copy of the nodes with padding0 = 1 on nodes holding a coordinate
-    // outside the traversal kernel's fast-division window (0 or 2^-40..2^40).
-    std::vector<ae_bvh_node> flagged(nodes, nodes + n_nodes);
-    for (auto& nd : flagged) {
-        const float* c = nd.leftAABB.min;
-        bool ok = true;
-        for (int k = 0; k < 12; k++) {
-            const float a = std::fabs(c[k]);
-            ok = ok && (a == 0.0f || (a >= 9.094947017729282e-13f && a <= 1.099511627776e12f));
-        }
-        nd.padding0 = ok ? 0 : 1;
-        nd.padding1 = 0;
-    }
+    std::vector<ae_bvh_node> flagged = FlagNodes(nodes, n_nodes);
     cudaError_t e = upload(&m.nodes, flagged.data(), size_t(n_nodes) * sizeof(ae_bvh_node));
     if (e == cudaSuccess) e = upload(&m.tris, tris, size_t(n_tris) * sizeof(ae_bvh_triangle));
     if (e == cudaSuccess && shading) e = upload(&m.shading, shading, size_t(n_tris) * sizeof(ae_triangle));
@@ -365,6 +407,119 @@ ae_rt_status ae_rt_trace_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packe
 ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                              float tmin, float tmax, uint8_t* occluded, void* stream) {
     return Trace(ctx, true, mesh_id, rays, n_rays, tmin, tmax, occluded, stream);
+}
+
+ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n_tlas,
+                             const ae_bvh_instance* instances, uint32_t n_instances) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if ((n_tlas && !tlas) || (n_instances && !instances)) return Fail(ctx, AE_RT_INVALID_ARG, "null scene buffer");
+    if (n_tlas >= (1u << 31) - 1 || n_instances >= (1u << 31) - 1) return Fail(ctx, AE_RT_INVALID_ARG, "scene too large");
+    // top-level pointers: inner nodes after their parent, leaves name an instance
+    for (uint32_t i = 0; i < n_tlas; i++) {
+        const int32_t ptrs[2] = { tlas[i].leftPtr, tlas[i].rightPtr };
+        for (int32_t ptr : ptrs) {
+            if (ptr >= 0 ? (uint32_t(ptr) >= n_tlas || uint32_t(ptr) <= i) : uint32_t(~ptr) >= n_instances)
+                return Fail(ctx, AE_RT_BAD_BVH, "top-level node " + std::to_string(i) + " has pointer " +
+                                                std::to_string(ptr) + " out of range");
+        }
+    }
+    uint64_t steps = uint64_t(n_tlas) + n_instances;
+    for (uint32_t i = 0; i < n_instances; i++) {
+        const int32_t m = instances[i].meshOffset;
+        if (m < 0 || size_t(m) >= ctx->meshes.size())
+            return Fail(ctx, AE_RT_INVALID_ARG, "instance " + std::to_string(i) + " names unknown mesh " +
+                                                std::to_string(m));
+        steps += ctx->meshes[size_t(m)].n_nodes + ctx->meshes[size_t(m)].n_tris;
+    }
+    std::lock_guard<std::mutex> g(ctx->upload_mutex);
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<atlas::rt::dev::MeshDesc> table(ctx->meshes.size());
+    for (size_t i = 0; i < table.size(); i++) {
+        table[i].nodes = ctx->meshes[i].nodes;
+        table[i].tris = ctx->meshes[i].tris;
+        table[i].n_nodes = ctx->meshes[i].n_nodes;
+        table[i].n_tris = ctx->meshes[i].n_tris;
+    }
+    std::vector<ae_bvh_node> flagged = FlagNodes(tlas, n_tlas);
+    cudaFree(ctx->d_tlas);
+    cudaFree(ctx->d_instances);
+    cudaFree(ctx->d_mesh_table);
+    ctx->d_tlas = nullptr;
+    ctx->d_instances = nullptr;
+    ctx->d_mesh_table = nullptr;
+    ctx->scene_ready = false;
+    auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!bytes) return cudaSuccess;
+        cudaError_t e = cudaMalloc(dst, bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+        return e;
+    };
+    cudaError_t e = up(reinterpret_cast<void**>(&ctx->d_tlas), flagged.data(), flagged.size() * sizeof(ae_bvh_node));
+    if (e == cudaSuccess)
+        e = up(reinterpret_cast<void**>(&ctx->d_instances), instances, size_t(n_instances) * sizeof(ae_bvh_instance));
+    if (e == cudaSuccess)
+        e = up(reinterpret_cast<void**>(&ctx->d_mesh_table), table.data(), table.size() * sizeof(table[0]));
+    if (e != cudaSuccess) return CudaFail(ctx, e, "scene upload");
+    ctx->n_tlas = n_tlas;
+    ctx->n_instances = n_instances;
+    ctx->n_mesh_table = uint32_t(table.size());
+    steps = 4 * steps + 64;
+    ctx->scene_steps = steps > 0xffffffffull ? 0xffffffffu : uint32_t(steps);
+    ctx->scene_ready = true;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_scene_build(ae_rt_ctx* ctx, const ae_bvh_instance* instances, const ae_aabb* world_aabbs,
+                               uint32_t n_instances, uint32_t* order_out, uint32_t* n_ordered) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (n_instances == 0 || !instances || !world_aabbs)
+        return Fail(ctx, AE_RT_INVALID_ARG, "a scene needs at least one instance");
+    atlas::rt::BuiltBVH b;
+    try {
+        b = atlas::rt::BuildBoxBVH(reinterpret_cast<const float*>(world_aabbs), n_instances, false);
+    } catch (...) {
+        return Fail(ctx, AE_RT_OUT_OF_MEMORY, "top-level build failed");
+    }
+    // instances in reference order, nextInstance linking the members of a leaf
+    std::vector<ae_bvh_instance> ordered(b.order.size());
+    for (size_t i = 0; i < b.order.size(); i++) {
+        ordered[i] = instances[b.order[i]];
+        ordered[i].nextInstance = b.endOfNode[i] ? -1 : int32_t(i) + 1;
+    }
+    if (order_out)
+        for (size_t i = 0; i < b.order.size(); i++) order_out[i] = b.order[i];
+    if (n_ordered) *n_ordered = uint32_t(b.order.size());
+    static_assert(sizeof(atlas::rt::BuiltNode) == sizeof(ae_bvh_node), "node layout");
+    return ae_rt_scene_set(ctx, reinterpret_cast<const ae_bvh_node*>(b.nodes.data()), uint32_t(b.nodes.size()),
+                           ordered.data(), uint32_t(ordered.size()));
+}
+
+ae_rt_status ae_rt_trace_scene_closest(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays, float tmin,
+                                       float tmax, uint32_t cull_mask, ae_hit* hits, void* stream) {
+    return Trace(ctx, false, kSceneTarget, rays, n_rays, tmin, tmax, hits, stream, nullptr, cull_mask);
+}
+
+ae_rt_status ae_rt_trace_scene_any(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays, float tmin,
+                                   float tmax, uint32_t cull_mask, uint8_t* occluded, void* stream) {
+    return Trace(ctx, true, kSceneTarget, rays, n_rays, tmin, tmax, occluded, stream, nullptr, cull_mask);
+}
+
+ae_rt_status ae_rt_trace_scene_closest_queue(ae_rt_ctx* ctx, const ae_packed_ray* rays, const uint32_t* count,
+                                             uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
+                                             ae_hit* hits, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!count || !IsDevicePointer(count) || (capacity && (!IsDevicePointer(rays) || !IsDevicePointer(hits))))
+        return Fail(ctx, AE_RT_INVALID_ARG, "queue traces take device buffers");
+    return Trace(ctx, false, kSceneTarget, rays, capacity, tmin, tmax, hits, stream, count, cull_mask);
+}
+
+ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* rays, const uint32_t* count,
+                                         uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
+                                         uint8_t* occluded, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!count || !IsDevicePointer(count) || (capacity && (!IsDevicePointer(rays) || !IsDevicePointer(occluded))))
+        return Fail(ctx, AE_RT_INVALID_ARG, "queue traces take device buffers");
+    return Trace(ctx, true, kSceneTarget, rays, capacity, tmin, tmax, occluded, stream, count, cull_mask);
 }
 
 ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream) {

@@ -36,6 +36,16 @@ constexpr uint32_t kHitFlagNearTie = 0x2u;
 constexpr uint32_t kHitFlagOverflow = 0x4u;
 constexpr uint32_t kHitFlagIterCap = 0x8u;
 
+// One uploaded mesh (BLAS): the bindless blasNodes[mesh] / bvhTriangles[mesh]
+// pair of the engine (data/shader/raytracer/buffers.hsh:45-57).
+struct MeshDesc {
+    const float4* nodes;
+    const float4* tris;
+    uint32_t n_nodes;
+    uint32_t n_tris;
+    uint32_t pad[2];
+};
+
 struct TraceParams {
     const float4* nodes;         // 4 float4 per GPUBVHNode
     const float4* tris;          // 3 float4 per GPUBVHTriangle
@@ -52,6 +62,14 @@ struct TraceParams {
     uint32_t* error_word;        // kErr* bits
     unsigned long long* fetch_counts;  // [0] nodes, [1] triangles (optional)
     uint32_t max_steps;
+    // two-level scenes (TLAS instantiation only)
+    const float4* tlas;          // TLAS nodes, 4 float4 each
+    uint32_t n_tlas;
+    const float4* instances;     // GPUBVHInstance, 4 float4 each
+    uint32_t n_instances;
+    const MeshDesc* meshes;      // indexed by GPUBVHInstance::meshOffset
+    uint32_t n_meshes;
+    uint32_t cull_mask;
 };
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
@@ -161,10 +179,56 @@ struct LaneStack {
     static constexpr uint32_t capacity = SMEM + SPILL;
 };
 
+// One traversal ray in the space of the structure being traversed, with
+// the reciprocals of its direction and the fast-division window flag.
+struct TRay {
+    float ox, oy, oz, dx, dy, dz, yx, yy, yz;
+    bool fast;
+    __device__ __forceinline__ void prepare() {
+        yx = __frcp_rn(dx); yy = __frcp_rn(dy); yz = __frcp_rn(dz);
+        fast = in_fast_range(ox, true) && in_fast_range(oy, true) && in_fast_range(oz, true) &&
+               in_fast_range(dx, false) && in_fast_range(dy, false) && in_fast_range(dz, false);
+    }
+};
+
+// Both child boxes of a node (IntersectAABB x 2, bvh.hsh:229-232 / :253-256).
+// node.padding0 != 0 marks a node holding a coordinate outside the fast window
+// (set by the upload); such nodes, out-of-window rays and the BOUNDS variant
+// (whose nodes did not go through the upload) divide with div.rn.
+template <bool BOUNDS>
+__device__ __forceinline__ void test_children(const TRay& r, const float4& n0, const float4& n1, const float4& n2,
+                                              const float4& n3, float tmin, float bound, bool& il, bool& ir,
+                                              float& hl, float& hr) {
+    if (!BOUNDS && r.fast && __float_as_int(n3.z) == 0) {
+        il = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y,
+                            tmin, bound, hl);
+        ir = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w,
+                            tmin, bound, hr);
+    } else {
+        il = box_test<false>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n0.x, n0.y, n0.z, n0.w, n1.x,
+                             n1.y, tmin, bound, hl);
+        ir = box_test<false>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z,
+                             n2.w, tmin, bound, hr);
+    }
+}
+
+// vec4(v, w) * inverseMatrix (bvh.hsh:179-180): component i = dot(vec4(v, w),
+// column i), summed left to right with separate roundings.
+__device__ __forceinline__ float xform_row(float x, float y, float z, float w, const float4& c) {
+    return fadd(fadd(fadd(fmul(x, c.x), fmul(y, c.y)), fmul(z, c.z)), fmul(w, c.w));
+}
+
+constexpr uint32_t kTlasInvalid = 0xffffffffu;
+
+// ANY: HitAny instead of HitClosest.  COUNT: per-launch node / triangle fetch
+// totals.  TLAS: two-level traversal over instances (CheckInstance,
+// bvh.hsh:172-189, with the TLAS/BLAS switch keyed on the stack depth at which
+// the instance was entered, bvh.hsh:212-223); otherwise one BLAS.
 // BOUNDS = true adds range checks of every node and triangle index against
 // n_nodes / n_tris (for callers whose BVH did not pass the host validator);
 // an out-of-range index ends the ray with the overflow flag set.
-template <bool ANY, bool COUNT, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS, bool BOUNDS = false>
+template <bool ANY, bool COUNT, bool TLAS, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
+          bool BOUNDS = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
     const uint32_t lane = threadIdx.x & 31u;
@@ -177,17 +241,19 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     bool live = false;
     bool queueDry = false;          // warp-uniform
     uint32_t rid = 0;
-    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
-    float yx = 0, yy = 0, yz = 0;   // RN(1/d)
-    bool rayFast = false;
+    TRay wr{};                      // world-space ray (TLAS level)
+    TRay r{};                       // ray in the space of the current BLAS
     float hitDist = 0, second = 0, hu = 0, hv = 0;
-    int32_t hitID = -1;
+    int32_t hitID = -1, hitInst = -1, curInst = -1;
     int32_t node = 0;
-    uint32_t sp = 0, steps = 0, flags = 0;
+    uint32_t sp = 0, steps = 0, flags = 0, tlasIndex = kTlasInvalid;
+    const float4* blasNodes = p.nodes;
+    const float4* blasTris = p.tris;
     bool occl = false;
     unsigned long long nodeCount = 0, triCount = 0;
     const float tmin = p.tmin, tmax = p.tmax;
     const uint32_t nRays = p.n_rays_dev ? min(*p.n_rays_dev, p.n_rays) : p.n_rays;
+    const uint32_t nTop = TLAS ? p.n_tlas : p.n_nodes;
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
@@ -200,21 +266,23 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 base = __shfl_sync(kFull, base, leader);
                 if (base + __popc(idle) >= nRays) queueDry = true;
                 if (!live) {
-                    const uint32_t r = base + __popc(idle & lanemask_lt());
-                    if (r < nRays) {
-                        rid = r;
-                        const float4 o4 = ldg4(p.rays + size_t(r) * 3);
-                        const float4 d4 = ldg4(p.rays + size_t(r) * 3 + 1);
-                        ox = o4.x; oy = o4.y; oz = o4.z;
-                        dx = d4.x; dy = d4.y; dz = d4.z;
-                        yx = __frcp_rn(dx); yy = __frcp_rn(dy); yz = __frcp_rn(dz);
-                        rayFast = in_fast_range(ox, true) && in_fast_range(oy, true) && in_fast_range(oz, true) &&
-                                  in_fast_range(dx, false) && in_fast_range(dy, false) && in_fast_range(dz, false);
+                    const uint32_t ri = base + __popc(idle & lanemask_lt());
+                    if (ri < nRays) {
+                        rid = ri;
+                        const float4 o4 = ldg4(p.rays + size_t(ri) * 3);
+                        const float4 d4 = ldg4(p.rays + size_t(ri) * 3 + 1);
+                        r.ox = o4.x; r.oy = o4.y; r.oz = o4.z;
+                        r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
+                        r.prepare();
+                        if (TLAS) wr = r;
                         hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
-                        hitID = -1; node = 0; sp = 0; steps = 0; flags = 0; occl = false;
+                        hitID = -1; hitInst = -1; curInst = -1;
+                        node = 0; sp = 0; steps = 0; flags = 0; occl = false;
+                        tlasIndex = kTlasInvalid;
+                        if (!TLAS) { blasNodes = p.nodes; blasTris = p.tris; }
                         live = true;
                         // NaN direction or an empty BVH: miss (bvh.hsh:204, BVH.cpp:107)
-                        if (isnan(dx) || isnan(dy) || isnan(dz) || p.n_nodes == 0) node = INT32_MIN;
+                        if (isnan(r.dx) || isnan(r.dy) || isnan(r.dz) || nTop == 0) node = INT32_MIN;
                     }
                 }
             }
@@ -231,6 +299,42 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     done = true;
                     break;
                 }
+                const bool top = TLAS && sp < tlasIndex;
+                if (top) {
+                    tlasIndex = kTlasInvalid;
+                    if (node < 0) {
+                        // CheckInstance: object-space ray, mesh, cull mask
+                        const uint32_t ii = uint32_t(~node);
+                        const float4* ip = p.instances + size_t(ii) * 4;
+                        const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
+                        curInst = int32_t(ii);
+                        bool enter = (__float_as_uint(c3.w) & p.cull_mask) != 0u;
+                        MeshDesc m{};
+                        if (enter) {
+                            m = p.meshes[__float_as_int(c3.x)];
+                            enter = m.n_nodes > 0;     // an empty BLAS has no root to visit
+                        }
+                        if (enter) {
+                            r.ox = xform_row(wr.ox, wr.oy, wr.oz, 1.0f, c0);
+                            r.oy = xform_row(wr.ox, wr.oy, wr.oz, 1.0f, c1);
+                            r.oz = xform_row(wr.ox, wr.oy, wr.oz, 1.0f, c2);
+                            r.dx = xform_row(wr.dx, wr.dy, wr.dz, 0.0f, c0);
+                            r.dy = xform_row(wr.dx, wr.dy, wr.dz, 0.0f, c1);
+                            r.dz = xform_row(wr.dx, wr.dy, wr.dz, 0.0f, c2);
+                            r.prepare();
+                            blasNodes = m.nodes;
+                            blasTris = m.tris;
+                            node = 0;
+                            tlasIndex = sp;
+                        } else {
+                            if (sp == 0) { done = true; break; }
+                            node = st.get(--sp);
+                        }
+                        continue;
+                    }
+                }
+                const float4* nodesArr = top ? p.tlas : blasNodes;
+                const TRay& cr = top ? wr : r;
                 if (BOUNDS && (node < 0 ? uint32_t(~node) >= p.n_tris : uint32_t(node) >= p.n_nodes)) {
                     flags |= kHitFlagOverflow;
                     atomicOr(p.error_word, kErrStackOverflow);
@@ -247,19 +351,19 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                             atomicOr(p.error_word, kErrStackOverflow);
                             break;
                         }
-                        const float4 a = ldg4(p.tris + size_t(tp) * 3);
-                        const float4 b = ldg4(p.tris + size_t(tp) * 3 + 1);
-                        const float4 c = ldg4(p.tris + size_t(tp) * 3 + 2);
+                        const float4 a = ldg4(blasTris + size_t(tp) * 3);
+                        const float4 b = ldg4(blasTris + size_t(tp) * 3 + 1);
+                        const float4 c = ldg4(blasTris + size_t(tp) * 3 + 2);
                         end = a.w > 0.0f;
                         if (COUNT) triCount++;
                         float t, u, v;
-                        const bool hit = tri_test(ox, oy, oz, dx, dy, dz, a, b, c, t, u, v);
+                        const bool hit = tri_test(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
                         if (ANY) {
                             if (hit && t > tmin && t < tmax) { occl = true; end = true; }
                         } else if (hit && t > tmin && t < tmax) {
                             if (t < hitDist) {
                                 second = hitDist;
-                                hitDist = t; hitID = tp; hu = u; hv = v;
+                                hitDist = t; hitID = tp; hu = u; hv = v; hitInst = curInst;
                             } else if (t < second) {
                                 second = t;
                             }
@@ -271,27 +375,13 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     if (sp == 0) { done = true; break; }
                     node = st.get(--sp);
                 } else {
-                    const float4* np = p.nodes + size_t(node) * 4;
+                    const float4* np = nodesArr + size_t(node) * 4;
                     const float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
                     if (COUNT) nodeCount++;
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
-                    const float bound = ANY ? tmax : hitDist;
                     float hl, hr;
                     bool il, ir;
-                    // node.padding0 != 0 marks a node with a coordinate outside the fast window
-                    // (set by the upload); such nodes and out-of-window rays divide with div.rn,
-                    // as does the BOUNDS variant, whose nodes did not go through the upload.
-                    if (!BOUNDS && rayFast && __float_as_int(n3.z) == 0) {
-                        il = box_test<true>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n0.x, n0.y, n0.z, n0.w, n1.x,
-                                            n1.y, tmin, bound, hl);
-                        ir = box_test<true>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n1.z, n1.w, n2.x, n2.y, n2.z,
-                                            n2.w, tmin, bound, hr);
-                    } else {
-                        il = box_test<false>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n0.x, n0.y, n0.z, n0.w, n1.x,
-                                             n1.y, tmin, bound, hl);
-                        ir = box_test<false>(ox, oy, oz, dx, dy, dz, yx, yy, yz, n1.z, n1.w, n2.x, n2.y, n2.z,
-                                             n2.w, tmin, bound, hr);
-                    }
+                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, hl, hr);
                     int32_t next, far;
                     if (ANY) {
                         next = il ? lptr : rptr;
@@ -324,7 +414,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     uint32_t f = flags | (hit ? kHitFlagHit : 0u);
                     if (hit && fsub(second, hitDist) <= fmul(1e-6f, hitDist)) f |= kHitFlagNearTie;
                     float4* hp = p.hits + size_t(rid) * 2;
-                    hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(-1), __uint_as_float(f));
+                    hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(hitInst), __uint_as_float(f));
                     hp[1] = make_float4(hu, hv, second, 0.0f);
                 }
                 live = false;

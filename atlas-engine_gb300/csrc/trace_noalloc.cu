@@ -46,7 +46,7 @@ DeviceSetup g_setup[kMaxDevices];
 
 void* NoAllocKernel() {
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<false, false, kWarps, kSmemStack, kSpillStack, kMinBlocks, true>);
+        &atlas::rt::dev::trace_kernel<false, false, false, kWarps, kSmemStack, kSpillStack, kMinBlocks, true>);
 }
 
 bool IsDeviceMemory(const void* p) {

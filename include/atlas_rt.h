@@ -244,6 +244,43 @@ ae_rt_status ae_rt_trace_any(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ra
                              uint32_t n_rays, float tmin, float tmax, uint8_t* occluded,
                              void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Two-level scene: top level over instances                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Sets the scene traced by ae_rt_trace_scene_*: the top-level nodes (GPUBVHNode
+ * layout, leaves ~index into `instances`) and the instances in top-level
+ * order (GPUBVHInstance; meshOffset = a mesh id from ae_rt_mesh_upload).
+ * Validated (pointer ranges, pre-order, mesh ids) and deep-copied.  Replaces
+ * the tlasNodeBuffer / bvhInstanceBuffer uploads of RayTracingWorld
+ * (RayTracingWorld.cpp:150-160, :297-301). */
+ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n_tlas,
+                             const ae_bvh_instance* instances, uint32_t n_instances);
+
+/* Builds the top level the way RayTracingWorld::UpdateForSoftwareRayTracing
+ * does (RayTracingWorld.cpp:267-307): an AABB-only BVH over the instances'
+ * world boxes (BVH.cpp:58-100), instances reordered to its reference order
+ * with nextInstance linking each leaf, then ae_rt_scene_set.  order_out
+ * (optional, capacity n_instances + 1) receives the input index of each
+ * ordered instance; n_ordered their count (n_instances, or 2 for a single
+ * instance, which the reference lists twice). */
+ae_rt_status ae_rt_scene_build(ae_rt_ctx* ctx, const ae_bvh_instance* instances, const ae_aabb* world_aabbs,
+                               uint32_t n_instances, uint32_t* order_out, uint32_t* n_ordered);
+
+/* HitClosest / HitAny over the scene (bvh.hsh:191-273, :359-441): instances
+ * whose mask shares no bit with cull_mask are skipped; ae_hit.instance is the
+ * hit instance's top-level index. */
+ae_rt_status ae_rt_trace_scene_closest(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays, float tmin,
+                                       float tmax, uint32_t cull_mask, ae_hit* hits, void* stream);
+ae_rt_status ae_rt_trace_scene_any(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays, float tmin,
+                                   float tmax, uint32_t cull_mask, uint8_t* occluded, void* stream);
+ae_rt_status ae_rt_trace_scene_closest_queue(ae_rt_ctx* ctx, const ae_packed_ray* rays, const uint32_t* count,
+                                             uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
+                                             ae_hit* hits, void* stream);
+ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* rays, const uint32_t* count,
+                                         uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
+                                         uint8_t* occluded, void* stream);
+
 /* Closest hit against one mesh without any device allocation.  This entry
  * point has no counterpart in the reference.  It is for hosts that own all
  * device memory and do not let a library call cudaMalloc / cudaFree -- an

@@ -263,6 +263,236 @@ static int any_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* 
     return hit;
 }
 
+
+/* ---------------------------------------------------------------------- */
+/* Two-level shader traversal (TLAS + instances + BLAS)                    */
+/* ---------------------------------------------------------------------- */
+
+/* vec4(v, w) * inverseMatrix (bvh.hsh:179-180): component i is
+ * dot(vec4(v, w), column i), summed left to right. */
+static inline v3 xform(const aeo_instance* in, v3 v, float w) {
+    const float* m = in->m;
+    v3 r;
+    r.x = ((v.x * m[0] + v.y * m[1]) + v.z * m[2]) + w * m[3];
+    r.y = ((v.x * m[4] + v.y * m[5]) + v.z * m[6]) + w * m[7];
+    r.z = ((v.x * m[8] + v.y * m[9]) + v.z * m[10]) + w * m[11];
+    return r;
+}
+
+#define TLAS_INVALID 0xFFFFFFFFu
+
+typedef struct {
+    const aeo_node* tlas; uint32_t n_tlas;
+    const aeo_instance* inst; uint32_t n_inst;
+    const aeo_mesh* meshes; uint32_t n_meshes;
+} scene_t;
+
+/* HitClosest -- bvh.hsh:191-273.  The TLAS/BLAS switch is keyed on the stack
+ * depth at which the instance was entered (tlasIndex). */
+static void scene_closest_one(const scene_t* sc, const float* r, uint32_t cull, int32_t* stack,
+                              int32_t* out_ptr, int32_t* out_inst, float* out_tuv, uint32_t* nf, uint32_t* tf) {
+    v3 wo = ld3(r), wd = ld3(r + 3);
+    float tMin = r[6], tMax = r[7];
+    float hitDist = tMax, hu = 0.0f, hv = 0.0f;
+    int32_t hitID = -1, hitInst = -1, curInst = -1;
+    uint32_t nodeFetches = 0, triFetches = 0;
+    if (sc->n_tlas && !isnan3(wd)) {
+        v3 o = wo, d = wd;
+        const aeo_mesh* mesh = NULL;
+        uint32_t sp = 1, tlasIndex = TLAS_INVALID;
+        int32_t nodePtr = 0;
+        stack[0] = 0;
+        while (sp != 0) {
+            if (sp < tlasIndex) {
+                o = wo; d = wd;
+                tlasIndex = TLAS_INVALID;
+                if (nodePtr < 0) {
+                    /* CheckInstance -- bvh.hsh:172-189 */
+                    const aeo_instance* in = &sc->inst[~nodePtr];
+                    o = xform(in, wo, 1.0f);
+                    d = xform(in, wd, 0.0f);
+                    curInst = ~nodePtr;
+                    mesh = &sc->meshes[in->meshOffset];
+                    if ((in->mask & cull) > 0 && mesh->n_nodes > 0) {
+                        nodePtr = 0;
+                        tlasIndex = sp;
+                    } else {
+                        nodePtr = stack[--sp];
+                    }
+                } else {
+                    const aeo_node* nd = &sc->tlas[nodePtr];
+                    nodeFetches++;
+                    float hl = 0.0f, hr = 0.0f;
+                    int il = box_glsl(o, d, tMin, hitDist, nd->lmin, nd->lmax, &hl);
+                    int ir = box_glsl(o, d, tMin, hitDist, nd->rmin, nd->rmax, &hr);
+                    int none = !il && !ir;
+                    int32_t next = (hl <= hr) ? nd->left : nd->right;
+                    if (none) next = stack[--sp];
+                    if (ir && il) stack[sp++] = (hl <= hr) ? nd->right : nd->left;
+                    nodePtr = next;
+                }
+            } else {
+                if (nodePtr < 0) {
+                    int32_t tp = ~nodePtr;
+                    int end = 0;
+                    while (!end) {
+                        const aeo_tri* t = &mesh->tris[tp];
+                        end = t->v0[3] > 0.0f;
+                        triFetches++;
+                        float st, su, sv;
+                        int hit = tri_test(o, d, t, &st, &su, &sv);
+                        if (hit && st > tMin && st < hitDist) {
+                            hitDist = st; hitID = tp; hu = su; hv = sv; hitInst = curInst;
+                        }
+                        tp++;
+                    }
+                    nodePtr = stack[--sp];
+                } else {
+                    const aeo_node* nd = &mesh->nodes[nodePtr];
+                    nodeFetches++;
+                    float hl = 0.0f, hr = 0.0f;
+                    int il = box_glsl(o, d, tMin, hitDist, nd->lmin, nd->lmax, &hl);
+                    int ir = box_glsl(o, d, tMin, hitDist, nd->rmin, nd->rmax, &hr);
+                    int none = !il && !ir;
+                    int32_t next = (hl <= hr) ? nd->left : nd->right;
+                    if (none) next = stack[--sp];
+                    if (ir && il) stack[sp++] = (hl <= hr) ? nd->right : nd->left;
+                    nodePtr = next;
+                }
+            }
+        }
+    }
+    *out_ptr = hitID;
+    *out_inst = hitInst;
+    out_tuv[0] = hitDist; out_tuv[1] = hu; out_tuv[2] = hv;
+    if (nf) *nf = nodeFetches;
+    if (tf) *tf = triFetches;
+}
+
+/* HitAny -- bvh.hsh:359-441. */
+static int scene_any_one(const scene_t* sc, const float* r, uint32_t cull, int32_t* stack) {
+    v3 wo = ld3(r), wd = ld3(r + 3);
+    float tMin = r[6], tMax = r[7];
+    if (!sc->n_tlas || isnan3(wd)) return 0;
+    v3 o = wo, d = wd;
+    const aeo_mesh* mesh = NULL;
+    uint32_t sp = 1, tlasIndex = TLAS_INVALID;
+    int32_t nodePtr = 0;
+    int hit = 0;
+    stack[0] = 0;
+    while (sp != 0 && !hit) {
+        if (sp < tlasIndex) {
+            o = wo; d = wd;
+            tlasIndex = TLAS_INVALID;
+            if (nodePtr < 0) {
+                const aeo_instance* in = &sc->inst[~nodePtr];
+                o = xform(in, wo, 1.0f);
+                d = xform(in, wd, 0.0f);
+                mesh = &sc->meshes[in->meshOffset];
+                if ((in->mask & cull) > 0 && mesh->n_nodes > 0) {
+                    nodePtr = 0;
+                    tlasIndex = sp;
+                } else {
+                    nodePtr = stack[--sp];
+                }
+            } else {
+                const aeo_node* nd = &sc->tlas[nodePtr];
+                float dl, dr;
+                int il = box_glsl(o, d, tMin, tMax, nd->lmin, nd->lmax, &dl);
+                int ir = box_glsl(o, d, tMin, tMax, nd->rmin, nd->rmax, &dr);
+                int32_t next = il ? nd->left : nd->right;
+                if (!ir && !il) next = stack[--sp];
+                if (ir && il) stack[sp++] = nd->right;
+                nodePtr = next;
+            }
+        } else {
+            if (nodePtr < 0) {
+                int32_t tp = ~nodePtr;
+                int end = 0;
+                while (!end && !hit) {
+                    const aeo_tri* t = &mesh->tris[tp];
+                    end = t->v0[3] > 0.0f;
+                    float st, su, sv;
+                    if (tri_test(o, d, t, &st, &su, &sv) && st > tMin && st < tMax) hit = 1;
+                    tp++;
+                }
+                nodePtr = stack[--sp];
+            } else {
+                const aeo_node* nd = &mesh->nodes[nodePtr];
+                float dl, dr;
+                int il = box_glsl(o, d, tMin, tMax, nd->lmin, nd->lmax, &dl);
+                int ir = box_glsl(o, d, tMin, tMax, nd->rmin, nd->rmax, &dr);
+                int32_t next = il ? nd->left : nd->right;
+                if (!ir && !il) next = stack[--sp];
+                if (ir && il) stack[sp++] = nd->right;
+                nodePtr = next;
+            }
+        }
+    }
+    return hit;
+}
+
+typedef struct {
+    const scene_t* sc; const float* rays; uint32_t begin, end; uint32_t cull; int any;
+    int32_t* ptr; int32_t* inst; float* tuv; uint8_t* occ; uint32_t* nf; uint32_t* tf; size_t stack_cap;
+} scene_job_t;
+
+static void* run_scene_job(void* arg) {
+    scene_job_t* j = (scene_job_t*)arg;
+    int32_t* stack = (int32_t*)malloc(j->stack_cap * sizeof(int32_t));
+    for (uint32_t i = j->begin; i < j->end; i++) {
+        const float* r = j->rays + (size_t)i * 8;
+        if (j->any) j->occ[i] = (uint8_t)scene_any_one(j->sc, r, j->cull, stack);
+        else scene_closest_one(j->sc, r, j->cull, stack, &j->ptr[i], &j->inst[i], &j->tuv[(size_t)i * 3],
+                               j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL);
+    }
+    free(stack);
+    return NULL;
+}
+
+static void run_scene(scene_job_t proto, uint32_t n, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    scene_job_t jobs[256];
+    uint32_t chunk = (n + (uint32_t)threads - 1) / (uint32_t)threads;
+    int started = 0;
+    for (int t = 0; t < threads; t++) {
+        uint32_t b = (uint32_t)t * chunk;
+        if (b >= n) break;
+        jobs[t] = proto; jobs[t].begin = b; jobs[t].end = b + chunk < n ? b + chunk : n;
+        pthread_create(&th[t], NULL, run_scene_job, &jobs[t]);
+        started++;
+    }
+    for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+static size_t scene_stack_cap(const scene_t* sc) {
+    size_t cap = sc->n_tlas + 64;
+    for (uint32_t i = 0; i < sc->n_meshes; i++) cap += sc->meshes[i].n_nodes;
+    return cap;
+}
+
+void aeo_scene_closest_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
+                            const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
+                            uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out, float* tuv,
+                            uint32_t* node_fetches, uint32_t* tri_fetches) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    scene_job_t p; memset(&p, 0, sizeof(p));
+    p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 0; p.ptr = tri_ptr; p.inst = inst_out; p.tuv = tuv;
+    p.nf = node_fetches; p.tf = tri_fetches; p.stack_cap = scene_stack_cap(&sc);
+    run_scene(p, n_rays, threads);
+}
+
+void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
+                        const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
+                        uint32_t cull_mask, int threads, uint8_t* occluded) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    scene_job_t p; memset(&p, 0, sizeof(p));
+    p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 1; p.occ = occluded; p.stack_cap = scene_stack_cap(&sc);
+    run_scene(p, n_rays, threads);
+}
+
 /* ---------------------------------------------------------------------- */
 /* Double-precision brute force                                            */
 /* ---------------------------------------------------------------------- */

@@ -64,6 +64,34 @@ void aeo_any_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, 
                   const float* rays, uint32_t n_rays, int threads, uint8_t* occluded,
                   uint32_t* node_fetches, uint32_t* tri_fetches);
 
+/* Two-level scene (top level over instances): GPUBVHInstance
+ * (RTStructures.h:85-93): m = mat3x4 columns = rows of the inverse model
+ * matrix, objectPos[i] = dot(vec4(worldPos, 1), m[i]). */
+typedef struct aeo_instance {
+    float m[12];
+    int32_t meshOffset, materialOffset, nextInstance;
+    uint32_t mask;
+} aeo_instance;
+
+typedef struct aeo_mesh {
+    const aeo_node* nodes;
+    uint32_t n_nodes;
+    const aeo_tri* tris;
+    uint32_t n_tris;
+} aeo_mesh;
+
+/* Shader closest-hit over TLAS + BLASes: HitClosest with CheckInstance
+ * (bvh.hsh:172-273).  inst_out = hitInstanceID (-1 on a miss). */
+void aeo_scene_closest_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
+                            const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
+                            uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out, float* tuv,
+                            uint32_t* node_fetches, uint32_t* tri_fetches);
+
+/* Shader any-hit over TLAS + BLASes: HitAny (bvh.hsh:359-441). */
+void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
+                        const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
+                        uint32_t cull_mask, int threads, uint8_t* occluded);
+
 /* Exact-as-possible nearest hit in double precision by brute force over every
  * triangle (for small cases and for re-testing near ties): the double-precision
  * form of the same triangle test, accepting tmin < t < tmax.  t2 = second

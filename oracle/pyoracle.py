@@ -57,6 +57,10 @@ def port():
         L.aeo_closest_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P, P]
         L.aeo_any_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P]
         L.aeo_closest_f64_brute.argtypes = [P, U32, P, U32, C.c_int, P, P, P]
+        L.aeo_scene_closest_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P, P, P, P, P]
+        L.aeo_scene_any_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P]
+        L.aeo_scene_closest_glsl.restype = None
+        L.aeo_scene_any_glsl.restype = None
         for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
             f.restype = None
         _port = L
@@ -156,6 +160,59 @@ def closest_f64_brute(tris_f32, rays8, threads=os.cpu_count()):
     port().aeo_closest_f64_brute(tris_f32.ctypes.data, len(tris_f32), rays8.ctypes.data, n, threads,
                                  ptr.ctypes.data, t.ctypes.data, t2.ctypes.data)
     return ptr, t, t2
+
+
+class _Mesh(C.Structure):
+    _fields_ = [("nodes", P), ("n_nodes", U32), ("tris", P), ("n_tris", U32)]
+
+
+def _mesh_table(meshes):
+    """meshes: list of (nodes_f32 (n,16), tris_f32 (m,12)); keeps the arrays alive."""
+    keep = []
+    table = (_Mesh * max(1, len(meshes)))()
+    for i, (nodes, tris) in enumerate(meshes):
+        nodes = _c(nodes, np.float32)
+        tris = _c(tris, np.float32)
+        keep += [nodes, tris]
+        table[i].nodes = nodes.ctypes.data if nodes.size else None
+        table[i].n_nodes = len(nodes)
+        table[i].tris = tris.ctypes.data if tris.size else None
+        table[i].n_tris = len(tris)
+    return table, keep
+
+
+def scene_closest_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, threads=os.cpu_count(),
+                       counters=False):
+    """HitClosest over TLAS + instances + BLASes.  instances: structured array
+    with the GPUBVHInstance layout (64 bytes each)."""
+    n = len(rays8)
+    tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
+    inst = np.ascontiguousarray(instances)
+    table, keep = _mesh_table(meshes)
+    ptr = np.empty(n, np.int32)
+    ino = np.empty(n, np.int32)
+    tuv = np.empty((n, 3), np.float32)
+    nf = np.empty(n, np.uint32) if counters else None
+    tf = np.empty(n, np.uint32) if counters else None
+    port().aeo_scene_closest_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
+                                  inst.ctypes.data, len(inst), table, len(meshes), rays8.ctypes.data, n,
+                                  cull_mask, threads, ptr.ctypes.data, ino.ctypes.data, tuv.ctypes.data,
+                                  None if nf is None else nf.ctypes.data, None if tf is None else tf.ctypes.data)
+    if counters:
+        return ptr, ino, tuv, nf, tf
+    return ptr, ino, tuv
+
+
+def scene_any_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, threads=os.cpu_count()):
+    n = len(rays8)
+    tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
+    inst = np.ascontiguousarray(instances)
+    table, keep = _mesh_table(meshes)
+    occ = np.empty(n, np.uint8)
+    port().aeo_scene_any_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
+                              inst.ctypes.data, len(inst), table, len(meshes), rays8.ctypes.data, n,
+                              cull_mask, threads, occ.ctypes.data)
+    return occ
 
 
 # ---------------------------------------------------------------------------
