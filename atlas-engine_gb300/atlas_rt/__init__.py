@@ -21,7 +21,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import AeRtError, BounceParams, Camera, CastOutputs, Config, lib
+from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, lib
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
@@ -128,12 +128,16 @@ class Context:
     """Device context of the library (``ae_rt_ctx``)."""
 
     def __init__(self, device: int = 0, count_fetches: bool = False, blocks_per_sm: int = 0,
-                 max_steps: int = 0):
+                 max_steps: int = 0, refill_steps: int = 0, threads_per_block: int = 0,
+                 stack_entries_smem: int = 0):
         cfg = Config()
         cfg.device = device
         cfg.blocks_per_sm = blocks_per_sm
+        cfg.threads_per_block = threads_per_block
+        cfg.stack_entries_smem = stack_entries_smem
         cfg.max_steps = max_steps
-        cfg.reserved[0] = CFG_COUNT_FETCHES if count_fetches else 0
+        cfg.flags = CFG_COUNT_FETCHES if count_fetches else 0
+        cfg.refill_steps = refill_steps
         h = C.c_void_p()
         _check(lib().ae_rt_ctx_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -232,6 +236,28 @@ class Context:
         _check(lib().ae_rt_trace_scene_any_queue(self._h, _ptr(rays), _ptr(count), capacity, tmin, tmax,
                                                  cull_mask, _ptr(occluded), _stream_handle(stream)), self._h)
 
+    # ---- batched multi-mesh launches ----
+    @staticmethod
+    def _batch_table(batches):
+        """batches: list of dicts {mesh, any, rays, out, n_rays, tmin, tmax}."""
+        table = (BatchDesc * len(batches))()
+        for i, b in enumerate(batches):
+            table[i].mesh_id = b["mesh"]
+            table[i].any = 1 if b["any"] else 0
+            table[i].rays = _ptr(b["rays"])
+            table[i].out = _ptr(b["out"])
+            table[i].n_rays = b["n_rays"]
+            table[i].tmin = b["tmin"]
+            table[i].tmax = b["tmax"]
+        return table
+
+    def trace_batched(self, batches, stream=None):
+        table = self._batch_table(batches)
+        _check(lib().ae_rt_trace_batched(self._h, table, len(batches), _stream_handle(stream)), self._h)
+
+    def batch_plan(self, batches) -> "BatchPlan":
+        return BatchPlan(self, batches)
+
     # ---- wavefront stages (device buffers) ----
     def raygen(self, cam: "Camera", rays, stream=None):
         _check(lib().ae_rt_raygen(self._h, C.byref(cam), _ptr(rays), _stream_handle(stream)), self._h)
@@ -276,6 +302,28 @@ class Context:
         a, b = C.c_uint64(), C.c_uint64()
         _check(lib().ae_rt_get_fetch_counts(self._h, C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
+
+
+class BatchPlan:
+    """ae_rt_batch_plan: a batched launch captured once in a CUDA graph."""
+
+    def __init__(self, ctx: Context, batches):
+        self.ctx = ctx
+        table = Context._batch_table(batches)
+        h = C.c_void_p()
+        _check(lib().ae_rt_batch_plan_create(ctx.handle, table, len(batches), C.byref(h)), ctx.handle)
+        self._h = h
+
+    def launch(self, stream=None):
+        _check(lib().ae_rt_batch_plan_launch(self._h, _stream_handle(stream)), self.ctx.handle)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ae_rt_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def make_camera(cam: dict) -> Camera:

@@ -30,7 +30,13 @@ class AeRtError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("device", I32), ("blocks_per_sm", U32), ("threads_per_block", U32),
-                ("max_steps", U32), ("reserved", U32 * 4)]
+                ("max_steps", U32), ("flags", U32), ("refill_steps", U32), ("stack_entries_smem", U32),
+                ("reserved", U32)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("mesh_id", I32), ("any", U32), ("rays", P), ("out", P), ("n_rays", U32),
+                ("tmin", F32), ("tmax", F32), ("reserved", U32)]
 
 
 class Camera(C.Structure):
@@ -69,6 +75,10 @@ _SIGNATURES = [
     ("ae_rt_trace_scene_any", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_scene_closest_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_scene_any_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_batched", C.c_int, [P, P, U32, P]),
+    ("ae_rt_batch_plan_create", C.c_int, [P, P, U32, C.POINTER(P)]),
+    ("ae_rt_batch_plan_launch", C.c_int, [P, P]),
+    ("ae_rt_batch_plan_destroy", None, [P]),
     ("ae_rt_trace_closest_noalloc", C.c_int, [P, U32, P, U32, P, U32, F32, F32, P, P]),
     ("ae_rt_raygen", C.c_int, [P, C.POINTER(Camera), P, P]),
     ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),

@@ -18,24 +18,57 @@ namespace {
 
 using atlas::rt::dev::TraceParams;
 
-constexpr int kWarps = 4;          // 128 threads per CTA
-constexpr int kSmemStack = 32;     // shared-memory stack entries per lane (the shader's STACK_SIZE)
-constexpr int kSpillStack = 32;    // local-memory entries behind them
-constexpr int kMinBlocks = 8;
+// Kernel shapes the context can run (chosen by ae_rt_config, tuned by the
+// project's autotuner): warps per CTA and the shared-memory part of each
+// lane's 64-entry traversal stack (the rest spills to local memory).  The
+// register budget follows from the minimum resident CTAs per SM.
+constexpr int kStackEntries = 64;
+struct Shape {
+    int warps;
+    int smem;
+};
+constexpr Shape kShapes[] = { { 4, 32 }, { 2, 32 }, { 8, 16 }, { 4, 16 } };
+constexpr int kNumShapes = 4;
 
-template <bool ANY, bool COUNT, bool TLAS>
+using atlas::rt::dev::MODE_BATCH;
+using atlas::rt::dev::MODE_MESH;
+using atlas::rt::dev::MODE_SCENE;
+
+template <bool ANY, bool COUNT, int MODE, int W, int S>
 void* KernelFor() {
+    // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
+    // more per-lane state and get ~73
+    constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<ANY, COUNT, TLAS, kWarps, kSmemStack, kSpillStack, kMinBlocks>);
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks>);
 }
 
-void* PickKernel(bool any, bool count, bool tlas) {
-    if (tlas) {
-        if (any) return count ? KernelFor<true, true, true>() : KernelFor<true, false, true>();
-        return count ? KernelFor<false, true, true>() : KernelFor<false, false, true>();
+template <int W, int S>
+void* PickShape(bool any, bool count, int mode) {
+    if (mode == MODE_BATCH) return count ? KernelFor<false, true, MODE_BATCH, W, S>() : KernelFor<false, false, MODE_BATCH, W, S>();
+    if (mode == MODE_SCENE) {
+        if (any) return count ? KernelFor<true, true, MODE_SCENE, W, S>() : KernelFor<true, false, MODE_SCENE, W, S>();
+        return count ? KernelFor<false, true, MODE_SCENE, W, S>() : KernelFor<false, false, MODE_SCENE, W, S>();
     }
-    if (any) return count ? KernelFor<true, true, false>() : KernelFor<true, false, false>();
-    return count ? KernelFor<false, true, false>() : KernelFor<false, false, false>();
+    if (any) return count ? KernelFor<true, true, MODE_MESH, W, S>() : KernelFor<true, false, MODE_MESH, W, S>();
+    return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
+}
+
+void* PickKernelShape(int shape, bool any, bool count, int mode) {
+    switch (shape) {
+    case 1: return PickShape<2, 32>(any, count, mode);
+    case 2: return PickShape<8, 16>(any, count, mode);
+    case 3: return PickShape<4, 16>(any, count, mode);
+    default: return PickShape<4, 32>(any, count, mode);
+    }
+}
+
+int ShapeIndex(uint32_t threads, uint32_t smem) {
+    if (threads == 0) threads = 128;
+    if (smem == 0) smem = 32;
+    for (int i = 0; i < kNumShapes; i++)
+        if (uint32_t(kShapes[i].warps * 32) == threads && uint32_t(kShapes[i].smem) == smem) return i;
+    return -1;
 }
 
 struct DeviceMesh {
@@ -71,8 +104,11 @@ struct Scratch {
 struct ae_rt_ctx {
     int device = 0;
     int sm_count = 0;
-    uint32_t blocks_per_sm = 0;
+    uint32_t blocks_per_sm = 0;         // 0: occupancy of each kernel
+    int shape = 0;                      // index into kShapes
+    uint32_t threads = 128;
     uint32_t max_steps_cfg = 0;
+    uint32_t refill_steps = 0;
     bool count_fetches = false;
     std::vector<DeviceMesh> meshes;
     // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot
@@ -86,7 +122,7 @@ struct ae_rt_ctx {
     bool scene_ready = false;
     uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
     unsigned long long* d_fetch = nullptr;
-    Scratch rays_in, results_out;
+    Scratch rays_in, results_out, batch_table;
     // buffers of ae_rt_cast_pass
     Scratch cast_primary, cast_primary_hits, cast_secondary, cast_secondary_hits, cast_shadow, cast_occluded;
     uint32_t* d_cast_counts = nullptr;
@@ -175,17 +211,32 @@ uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
     return 4u * m.n_nodes + 64u;
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, bool tlas, TraceParams& p, cudaStream_t s) {
+// Persistent grid for `fn`: SMs x resident CTAs (the configured count, or the
+// kernel's occupancy), never more warps than rays.
+uint32_t GridFor(const ae_rt_ctx* ctx, const void* fn, uint32_t n_rays) {
+    uint32_t per_sm = ctx->blocks_per_sm;
+    if (per_sm == 0) {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, int(ctx->threads), 0) != cudaSuccess) {
+            cudaGetLastError();
+            occ = 1;
+        }
+        per_sm = uint32_t(occ > 0 ? occ : 1);
+    }
+    uint32_t grid = uint32_t(ctx->sm_count) * per_sm;
+    const uint32_t needed = (n_rays + ctx->threads - 1) / ctx->threads;
+    if (needed < grid) grid = needed;
+    return grid == 0 ? 1 : grid;
+}
+
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s) {
     AE_CUDA(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
-    void* fn = PickKernel(any, ctx->count_fetches, tlas);
-    // Persistent grid: never more CTAs than can be resident, never more warps than rays.
-    uint32_t grid = uint32_t(ctx->sm_count) * ctx->blocks_per_sm;
-    const uint32_t needed = (p.n_rays + kWarps * 32 - 1) / (kWarps * 32);
-    if (needed < grid) grid = needed;
-    if (grid == 0) grid = 1;
+    p.refill_steps = ctx->refill_steps;
+    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode);
+    const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
-    AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kWarps * 32), args, 0, s));
+    AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
     return AE_RT_OK;
 }
 
@@ -249,7 +300,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.n_meshes = ctx->n_mesh_table;
         p.cull_mask = cull_mask;
     }
-    ae_rt_status st = Launch(ctx, any, scene, p, s);
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -322,7 +373,8 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     }
     ctx->device = c.device;
     ctx->max_steps_cfg = c.max_steps;
-    ctx->count_fetches = (c.reserved[0] & AE_RT_CFG_COUNT_FETCHES) != 0;
+    ctx->count_fetches = (c.flags & AE_RT_CFG_COUNT_FETCHES) != 0;
+    ctx->refill_steps = c.refill_steps;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 2 * sizeof(uint32_t));
@@ -330,15 +382,17 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_fetch, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_fetch, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cast_counts, 4 * sizeof(uint32_t));
-    int occ = 0;
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(KernelFor<false, false, false>()),
-                                                          kWarps * 32, 0);
     if (e != cudaSuccess) {
         ae_rt_ctx_destroy(ctx);
         return e == cudaErrorMemoryAllocation ? AE_RT_OUT_OF_MEMORY : AE_RT_CUDA_ERROR;
     }
-    ctx->blocks_per_sm = c.blocks_per_sm ? c.blocks_per_sm : uint32_t(occ > 0 ? occ : 1);
+    ctx->shape = ShapeIndex(c.threads_per_block, c.stack_entries_smem);
+    if (ctx->shape < 0) {
+        ae_rt_ctx_destroy(ctx);
+        return AE_RT_INVALID_ARG;
+    }
+    ctx->threads = uint32_t(kShapes[ctx->shape].warps * 32);
+    ctx->blocks_per_sm = c.blocks_per_sm;
     *out = ctx;
     return AE_RT_OK;
 }
@@ -357,7 +411,7 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     cudaFree(ctx->d_tlas);
     cudaFree(ctx->d_instances);
     cudaFree(ctx->d_mesh_table);
-    for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->cast_primary, &ctx->cast_primary_hits,
+    for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
         sc->release();
     delete ctx;
@@ -522,6 +576,145 @@ ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* ra
     return Trace(ctx, true, kSceneTarget, rays, capacity, tmin, tmax, occluded, stream, count, cull_mask);
 }
 
+struct ae_rt_batch_plan {
+    ae_rt_ctx* ctx = nullptr;
+    atlas::rt::dev::BatchDesc* d_batches = nullptr;
+    uint32_t* d_counter = nullptr;
+    uint32_t n_batches = 0;
+    uint32_t total = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Device batch table for a launch; returns the total ray count.
+ae_rt_status MakeBatchTable(ae_rt_ctx* ctx, const ae_batch_desc* batches, uint32_t n,
+                            std::vector<atlas::rt::dev::BatchDesc>& table, uint32_t& total) {
+    table.resize(n);
+    uint64_t first = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const ae_batch_desc& b = batches[i];
+        if (b.mesh_id < 0 || size_t(b.mesh_id) >= ctx->meshes.size())
+            return Fail(ctx, AE_RT_INVALID_ARG, "batch " + std::to_string(i) + ": unknown mesh id");
+        if (b.n_rays && (!IsDevicePointer(b.rays) || !IsDevicePointer(b.out)))
+            return Fail(ctx, AE_RT_INVALID_ARG, "batch " + std::to_string(i) + ": batched traces take device buffers");
+        const DeviceMesh& m = ctx->meshes[size_t(b.mesh_id)];
+        atlas::rt::dev::BatchDesc& d = table[i];
+        d.nodes = m.nodes;
+        d.tris = m.tris;
+        d.rays = reinterpret_cast<const float4*>(b.rays);
+        d.out = b.out;
+        d.n_nodes = m.n_nodes;
+        d.n_tris = m.n_tris;
+        d.n_rays = b.n_rays;
+        d.any = b.any ? 1u : 0u;
+        d.tmin = b.tmin;
+        d.tmax = b.tmax;
+        d.first = uint32_t(first);
+        d.max_steps = ctx->max_steps_cfg ? ctx->max_steps_cfg : MaxSteps(ctx, m);
+        first += b.n_rays;
+        if (first > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one batched launch");
+    }
+    total = uint32_t(first);
+    return AE_RT_OK;
+}
+
+TraceParams BatchParams(ae_rt_ctx* ctx, const atlas::rt::dev::BatchDesc* d_batches, uint32_t n, uint32_t total,
+                        uint32_t* counter) {
+    TraceParams p{};
+    p.n_rays = total;
+    p.work_counter = counter;
+    p.error_word = ctx->d_counter + 1;
+    p.fetch_counts = ctx->d_fetch;
+    p.batches = d_batches;
+    p.n_batches = n;
+    p.refill_steps = ctx->refill_steps;
+    p.max_steps = 0xffffffffu;
+    return p;
+}
+
+}  // namespace
+
+ae_rt_status ae_rt_trace_batched(ae_rt_ctx* ctx, const ae_batch_desc* batches, uint32_t n_batches, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (n_batches == 0) return AE_RT_OK;
+    if (!batches) return Fail(ctx, AE_RT_INVALID_ARG, "null batch table");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<atlas::rt::dev::BatchDesc> table;
+    uint32_t total = 0;
+    ae_rt_status st = MakeBatchTable(ctx, batches, n_batches, table, total);
+    if (st != AE_RT_OK) return st;
+    if (total == 0) return AE_RT_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    AE_CUDA(ctx, ctx->batch_table.ensure(table.size() * sizeof(table[0])));
+    AE_CUDA(ctx, cudaMemcpyAsync(ctx->batch_table.ptr, table.data(), table.size() * sizeof(table[0]),
+                                 cudaMemcpyHostToDevice, s));
+    TraceParams p = BatchParams(ctx, static_cast<atlas::rt::dev::BatchDesc*>(ctx->batch_table.ptr), n_batches,
+                                total, ctx->d_counter);
+    return Launch(ctx, false, MODE_BATCH, p, s);
+}
+
+ae_rt_status ae_rt_batch_plan_create(ae_rt_ctx* ctx, const ae_batch_desc* batches, uint32_t n_batches,
+                                     ae_rt_batch_plan** out) {
+    if (!ctx || !out) return AE_RT_INVALID_ARG;
+    *out = nullptr;
+    if (n_batches == 0 || !batches) return Fail(ctx, AE_RT_INVALID_ARG, "a plan needs at least one batch");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<atlas::rt::dev::BatchDesc> table;
+    uint32_t total = 0;
+    ae_rt_status st = MakeBatchTable(ctx, batches, n_batches, table, total);
+    if (st != AE_RT_OK) return st;
+    auto* plan = new (std::nothrow) ae_rt_batch_plan;
+    if (!plan) return AE_RT_OUT_OF_MEMORY;
+    plan->ctx = ctx;
+    plan->n_batches = n_batches;
+    plan->total = total;
+    cudaStream_t cap = nullptr;
+    cudaError_t e = cudaMalloc(&plan->d_batches, table.size() * sizeof(table[0]));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_batches, table.data(), table.size() * sizeof(table[0]), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&plan->d_counter, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        TraceParams p = BatchParams(ctx, plan->d_batches, n_batches, total, plan->d_counter);
+        cudaError_t le = cudaMemsetAsync(plan->d_counter, 0, sizeof(uint32_t), cap);
+        void* args[] = { &p };
+        void* fn = PickKernelShape(ctx->shape, false, false, MODE_BATCH);
+        if (le == cudaSuccess)
+            le = cudaLaunchKernel(fn, dim3(GridFor(ctx, fn, total)), dim3(ctx->threads), args, 0, cap);
+        e = cudaStreamEndCapture(cap, &plan->graph);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+    if (cap) cudaStreamDestroy(cap);
+    if (e != cudaSuccess) {
+        ae_rt_batch_plan_destroy(plan);
+        return CudaFail(ctx, e, "batch plan");
+    }
+    *out = plan;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_batch_plan_launch(ae_rt_batch_plan* plan, void* stream) {
+    if (!plan) return AE_RT_INVALID_ARG;
+    ae_rt_ctx* ctx = plan->ctx;
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    AE_CUDA(ctx, cudaGraphLaunch(plan->exec, static_cast<cudaStream_t>(stream)));
+    return AE_RT_OK;
+}
+
+void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan) {
+    if (!plan) return;
+    cudaSetDevice(plan->ctx->device);
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    cudaFree(plan->d_batches);
+    cudaFree(plan->d_counter);
+    delete plan;
+}
+
 ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
     if (!cam || !rays) return Fail(ctx, AE_RT_INVALID_ARG, "null camera or ray buffer");
@@ -654,7 +847,7 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
         AE_CUDA(ctx, cudaMemset(ctx->d_counter + 1, 0, sizeof(uint32_t)));
         if (err & atlas::rt::dev::kErrStackOverflow)
             return Fail(ctx, AE_RT_STACK_OVERFLOW, "a ray needed more than " +
-                                                   std::to_string(kSmemStack + kSpillStack) + " stack entries");
+                                                   std::to_string(kStackEntries) + " stack entries");
         return Fail(ctx, AE_RT_ITERATION_LIMIT, "a ray exceeded the traversal step cap");
     }
     return AE_RT_OK;

@@ -70,7 +70,33 @@ struct TraceParams {
     const MeshDesc* meshes;      // indexed by GPUBVHInstance::meshOffset
     uint32_t n_meshes;
     uint32_t cull_mask;
+    // batched multi-mesh launches (MODE_BATCH): n_rays = total over batches
+    const struct BatchDesc* batches;
+    uint32_t n_batches;
+    uint32_t refill_steps;       // traversal steps between warp refills
 };
+
+// One ray batch of a batched launch: its mesh, its rays and results, its
+// query kind, and its first index in the launch's global ray numbering.
+struct BatchDesc {
+    const float4* nodes;
+    const float4* tris;
+    const float4* rays;
+    void* out;                   // ae_hit[] (closest) or uint8_t[] (any)
+    uint32_t n_nodes;
+    uint32_t n_tris;
+    uint32_t n_rays;
+    uint32_t any;
+    float tmin;
+    float tmax;
+    uint32_t first;              // global index of the batch's first ray
+    uint32_t max_steps;
+};
+static_assert(sizeof(BatchDesc) == 64, "batch descriptor layout");
+
+constexpr int MODE_MESH = 0;     // one BLAS
+constexpr int MODE_SCENE = 1;    // TLAS over instances
+constexpr int MODE_BATCH = 2;    // many BLASes, one per batch
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
@@ -220,16 +246,31 @@ __device__ __forceinline__ float xform_row(float x, float y, float z, float w, c
 
 constexpr uint32_t kTlasInvalid = 0xffffffffu;
 
+// Batch holding global ray index g: the last descriptor whose first <= g.
+__device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, uint32_t g) {
+    uint32_t lo = 0, hi = n;            // invariant: b[lo].first <= g < b[hi].first
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&b[mid].first) <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // ANY: HitAny instead of HitClosest.  COUNT: per-launch node / triangle fetch
-// totals.  TLAS: two-level traversal over instances (CheckInstance,
+// totals.  MODE_SCENE: two-level traversal over instances (CheckInstance,
 // bvh.hsh:172-189, with the TLAS/BLAS switch keyed on the stack depth at which
-// the instance was entered, bvh.hsh:212-223); otherwise one BLAS.
+// the instance was entered, bvh.hsh:212-223).  MODE_BATCH: every lane finds
+// its ray's batch (mesh, query kind, t range, result buffer) when it takes a
+// ray, so one launch serves many meshes and both query kinds.
 // BOUNDS = true adds range checks of every node and triangle index against
 // n_nodes / n_tris (for callers whose BVH did not pass the host validator);
 // an out-of-range index ends the ray with the overflow flag set.
-template <bool ANY, bool COUNT, bool TLAS, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
+template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
           bool BOUNDS = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
+    constexpr bool TLAS = MODE == MODE_SCENE;
+    constexpr bool BATCH = MODE == MODE_BATCH;
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = threadIdx.x >> 5;
@@ -250,10 +291,14 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     const float4* blasNodes = p.nodes;
     const float4* blasTris = p.tris;
     bool occl = false;
+    bool laneAny = ANY;             // batched: the lane's query kind
+    float tmin = p.tmin, tmax = p.tmax;
+    uint32_t maxSteps = p.max_steps;
+    void* out = nullptr;            // batched: the lane's result array
     unsigned long long nodeCount = 0, triCount = 0;
-    const float tmin = p.tmin, tmax = p.tmax;
     const uint32_t nRays = p.n_rays_dev ? min(*p.n_rays_dev, p.n_rays) : p.n_rays;
     const uint32_t nTop = TLAS ? p.n_tlas : p.n_nodes;
+    const int refill = p.refill_steps ? int(p.refill_steps) : 64;
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
@@ -266,11 +311,27 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 base = __shfl_sync(kFull, base, leader);
                 if (base + __popc(idle) >= nRays) queueDry = true;
                 if (!live) {
-                    const uint32_t ri = base + __popc(idle & lanemask_lt());
-                    if (ri < nRays) {
+                    const uint32_t gi = base + __popc(idle & lanemask_lt());
+                    if (gi < nRays) {
+                        const float4* raySrc = p.rays;
+                        uint32_t ri = gi;
+                        uint32_t nodesHere = nTop;
+                        if (BATCH) {
+                            const BatchDesc& bd = p.batches[find_batch(p.batches, p.n_batches, gi)];
+                            ri = gi - bd.first;
+                            raySrc = bd.rays;
+                            blasNodes = bd.nodes;
+                            blasTris = bd.tris;
+                            nodesHere = bd.n_nodes;
+                            laneAny = bd.any != 0;
+                            tmin = bd.tmin;
+                            tmax = bd.tmax;
+                            maxSteps = bd.max_steps;
+                            out = bd.out;
+                        }
                         rid = ri;
-                        const float4 o4 = ldg4(p.rays + size_t(ri) * 3);
-                        const float4 d4 = ldg4(p.rays + size_t(ri) * 3 + 1);
+                        const float4 o4 = ldg4(raySrc + size_t(ri) * 3);
+                        const float4 d4 = ldg4(raySrc + size_t(ri) * 3 + 1);
                         r.ox = o4.x; r.oy = o4.y; r.oz = o4.z;
                         r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
                         r.prepare();
@@ -279,10 +340,10 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         hitID = -1; hitInst = -1; curInst = -1;
                         node = 0; sp = 0; steps = 0; flags = 0; occl = false;
                         tlasIndex = kTlasInvalid;
-                        if (!TLAS) { blasNodes = p.nodes; blasTris = p.tris; }
+                        if (MODE == MODE_MESH) { blasNodes = p.nodes; blasTris = p.tris; }
                         live = true;
                         // NaN direction or an empty BVH: miss (bvh.hsh:204, BVH.cpp:107)
-                        if (isnan(r.dx) || isnan(r.dy) || isnan(r.dz) || nTop == 0) node = INT32_MIN;
+                        if (isnan(r.dx) || isnan(r.dy) || isnan(r.dz) || nodesHere == 0) node = INT32_MIN;
                     }
                 }
             }
@@ -291,9 +352,10 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
 
         // ---- traverse: a bounded number of steps, then refill again ----
         if (live) {
+            const bool anyQ = ANY || (BATCH && laneAny);
             bool done = node == INT32_MIN;
-            for (int k = 0; k < 64 && !done; k++) {
-                if (++steps > p.max_steps) {
+            for (int k = 0; k < refill && !done; k++) {
+                if (++steps > maxSteps) {
                     flags |= kHitFlagIterCap;
                     atomicOr(p.error_word, kErrIterationCap);
                     done = true;
@@ -358,7 +420,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         if (COUNT) triCount++;
                         float t, u, v;
                         const bool hit = tri_test(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
-                        if (ANY) {
+                        if (anyQ) {
                             if (hit && t > tmin && t < tmax) { occl = true; end = true; }
                         } else if (hit && t > tmin && t < tmax) {
                             if (t < hitDist) {
@@ -371,7 +433,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         tp++;
                     } while (!end);
                     if (BOUNDS && (flags & kHitFlagOverflow)) { done = true; break; }
-                    if (ANY && occl) { done = true; break; }
+                    if (anyQ && occl) { done = true; break; }
                     if (sp == 0) { done = true; break; }
                     node = st.get(--sp);
                 } else {
@@ -381,9 +443,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
                     float hl, hr;
                     bool il, ir;
-                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, hl, hr);
+                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, hl, hr);
                     int32_t next, far;
-                    if (ANY) {
+                    if (anyQ) {
                         next = il ? lptr : rptr;
                         far = rptr;
                     } else {
@@ -407,13 +469,14 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 }
             }
             if (done) {
-                if (ANY) {
-                    p.occluded[rid] = (occl && !(flags & (kHitFlagOverflow | kHitFlagIterCap))) ? 1 : 0;
+                if (anyQ) {
+                    uint8_t* occOut = BATCH ? static_cast<uint8_t*>(out) : p.occluded;
+                    occOut[rid] = (occl && !(flags & (kHitFlagOverflow | kHitFlagIterCap))) ? 1 : 0;
                 } else {
                     const bool hit = hitID >= 0;
                     uint32_t f = flags | (hit ? kHitFlagHit : 0u);
                     if (hit && fsub(second, hitDist) <= fmul(1e-6f, hitDist)) f |= kHitFlagNearTie;
-                    float4* hp = p.hits + size_t(rid) * 2;
+                    float4* hp = (BATCH ? static_cast<float4*>(out) : p.hits) + size_t(rid) * 2;
                     hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(hitInst), __uint_as_float(f));
                     hp[1] = make_float4(hu, hv, second, 0.0f);
                 }

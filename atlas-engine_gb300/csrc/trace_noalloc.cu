@@ -46,7 +46,8 @@ DeviceSetup g_setup[kMaxDevices];
 
 void* NoAllocKernel() {
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<false, false, false, kWarps, kSmemStack, kSpillStack, kMinBlocks, true>);
+        &atlas::rt::dev::trace_kernel<false, false, atlas::rt::dev::MODE_MESH, kWarps, kSmemStack, kSpillStack,
+                                       kMinBlocks, true>);
 }
 
 bool IsDeviceMemory(const void* p) {

@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline pass only (no extra workloads)")
+    ap.add_argument("--autotune", action="store_true", help="re-run the launch-parameter autotuner")
     return ap.parse_args()
 
 
@@ -249,6 +251,119 @@ def measure_l2_copy_gbs(torch, dev):
     return best
 
 
+TUNING = REPO / "atlas-engine_gb300" / "atlas_rt" / "tuning.json"
+
+
+def timed_steps(torch, dev, stream, step, steps, flush):
+    """Per-step CUDA-event times (ms) with an L2 flush before each step."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        evs[k][0].record(stream)
+        step()
+        evs[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def workload_random65536(torch, dev, stream, flush, steps):
+    """65,536 random triangles x 1,048,576 sphere rays: closest and any hit,
+    device-resident, kernel time per launch."""
+    import atlas_rt
+    from atlas_rt import BVH, scenes
+    tris = scenes.random_triangles()
+    o, d = scenes.sphere_rays()
+    b = BVH(tris)
+    gt = b.pack_triangles()
+    ctx = atlas_rt.Context(device=dev.index or 0)
+    mid = ctx.upload_mesh(b.nodes, gt)
+    n = len(o)
+    rays = torch.from_numpy(scenes.pack_rays(o, d)).to(dev)
+    hits = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    occ = torch.empty(n, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, fn in (("closest", lambda: ctx.trace_closest(mid, rays, 1e-4, 10.0, out=hits, stream=stream, n_rays=n)),
+                     ("any", lambda: ctx.trace_any(mid, rays, 1e-4, 10.0, out=occ, stream=stream, n_rays=n))):
+        for _ in range(3):
+            fn()
+        ms = float(np.mean(timed_steps(torch, dev, stream, fn, steps, flush)))
+        out[f"{name}_mrays_s"] = n / (ms * 1e-3) / 1e6
+        out[f"{name}_ms"] = ms
+    ctx.synchronize(stream)
+    ctx.close()
+    out["rays"] = n
+    out["triangles"] = len(tris)
+    return out
+
+
+def workload_batched(torch, dev, stream, flush, steps, autotune=False, log=None):
+    """64 random-triangle meshes (log-uniform 1k..500k triangles, own BVH
+    each) and 64 ray batches (log-uniform 4k..1M rays, alternating
+    closest / any hit): one persistent launch replayed from a CUDA graph,
+    against one launch per batch."""
+    import atlas_rt
+    from atlas_rt import BVH, scenes
+    from atlas_rt import autotune as at
+    specs = scenes.batched_scenes()
+    meshes = []
+    for sp in specs:
+        tris = scenes.random_triangles(sp["n_tris"], seed=sp["seed"])
+        b = BVH(tris)
+        meshes.append((b.nodes.copy(), b.pack_triangles()))
+    rays, outs = [], []
+    for i, sp in enumerate(specs):
+        o, d = scenes.sphere_rays(sp["n_rays"], seed=sp["seed"] + 7)
+        rays.append(torch.from_numpy(scenes.pack_rays(o, d)).to(dev))
+        outs.append(torch.empty(sp["n_rays"], dtype=torch.uint8, device=dev) if sp["any"]
+                    else torch.empty((sp["n_rays"], 8), dtype=torch.float32, device=dev))
+    total = sum(sp["n_rays"] for sp in specs)
+
+    def make_ctx(cfg):
+        ctx = atlas_rt.Context(device=dev.index or 0, threads_per_block=cfg["threads_per_block"],
+                               stack_entries_smem=cfg["stack_entries_smem"], refill_steps=cfg["refill_steps"],
+                               blocks_per_sm=max(cfg.get("blocks_per_sm", 0), 0))
+        mids = [ctx.upload_mesh(n, t) for n, t in meshes]
+        batches = [{"mesh": mids[i], "any": sp["any"], "rays": rays[i], "out": outs[i], "n_rays": sp["n_rays"],
+                    "tmin": 1e-4, "tmax": 10.0} for i, sp in enumerate(specs)]
+        return ctx, batches
+
+    tuned = None if autotune else at.load(TUNING, "batched64")
+    tuning_info = {"source": "tuning.json" if tuned else "autotune"}
+    if tuned is None:
+        def make_run(cfg):
+            ctx, batches = make_ctx(cfg)
+            plan = ctx.batch_plan(batches)
+            return (lambda: plan.launch(stream)), (lambda: (plan.close(), ctx.close()))
+        space = list(at.candidates(refills=[16, 32, 64, 128]))
+        tuned, best_ms, results = at.tune(make_run, torch, space=space, reps=3, log=log)
+        at.save(TUNING, "batched64", tuned, best_ms, results, torch.cuda.get_device_name(dev))
+        tuning_info["candidates"] = len(results)
+    tuning_info["config"] = tuned
+    ctx, batches = make_ctx(tuned)
+    plan = ctx.batch_plan(batches)
+    graph_ms = float(np.mean(timed_steps(torch, dev, stream, lambda: plan.launch(stream), steps, flush)))
+
+    def per_scene():
+        for bt in batches:
+            if bt["any"]:
+                ctx.trace_any(bt["mesh"], bt["rays"], bt["tmin"], bt["tmax"], out=bt["out"], stream=stream,
+                              n_rays=bt["n_rays"])
+            else:
+                ctx.trace_closest(bt["mesh"], bt["rays"], bt["tmin"], bt["tmax"], out=bt["out"], stream=stream,
+                                  n_rays=bt["n_rays"])
+    for _ in range(2):
+        per_scene()
+    per_ms = float(np.mean(timed_steps(torch, dev, stream, per_scene, steps, flush)))
+    ctx.synchronize(stream)
+    plan.close()
+    ctx.close()
+    return {"meshes": len(specs), "triangles": int(sum(sp["n_tris"] for sp in specs)), "rays": total,
+            "graph_launch_ms": graph_ms, "graph_launch_mrays_s": total / (graph_ms * 1e-3) / 1e6,
+            "per_scene_ms": per_ms, "per_scene_mrays_s": total / (per_ms * 1e-3) / 1e6,
+            "speedup_vs_per_scene": per_ms / graph_ms, "tuning": tuning_info}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -388,6 +503,13 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
     }
+    if not args.quick:
+        line["workloads"] = {
+            "random65536": workload_random65536(torch, dev, stream, flush, max(args.steps // 2, 3)),
+            "batched64": workload_batched(torch, dev, stream, flush, max(args.steps // 2, 3),
+                                          autotune=args.autotune,
+                                          log=(lambda m: print(m, file=sys.stderr))),
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # bounded sample: the pass's own rays, read back from the device
         prim_np = prim.cpu().numpy()

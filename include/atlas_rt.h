@@ -206,12 +206,20 @@ ae_rt_status ae_bvh_pack_triangles(const ae_bvh* bvh, const float* verts, const 
 
 typedef struct ae_rt_ctx ae_rt_ctx;
 
+/* Launch shape of the traversal kernels; the project's autotuner
+ * (atlas_rt.autotune) picks these per workload.  Supported
+ * (threads_per_block, stack_entries_smem) pairs: (128, 32) default, (64, 32),
+ * (256, 16), (128, 16); each lane has 64 stack entries in total, the rest in
+ * local memory. */
 typedef struct ae_rt_config {
-    int32_t device;             /* CUDA device ordinal */
-    uint32_t blocks_per_sm;     /* persistent traversal CTAs per SM (0 = tuned default) */
-    uint32_t threads_per_block; /* 0 = tuned default (multiple of 32) */
-    uint32_t max_steps;         /* traversal step cap per ray (0 = 4 x nodes + 64) */
-    uint32_t reserved[4];
+    int32_t device;               /* CUDA device ordinal */
+    uint32_t blocks_per_sm;       /* persistent CTAs per SM (0 = the kernel's occupancy) */
+    uint32_t threads_per_block;   /* 0 = 128 */
+    uint32_t max_steps;           /* traversal step cap per ray (0 = 4 x nodes + 64) */
+    uint32_t flags;               /* AE_RT_CFG_* */
+    uint32_t refill_steps;        /* traversal steps between warp refills (0 = 64) */
+    uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
+    uint32_t reserved;
 } ae_rt_config;
 
 ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out);
@@ -280,6 +288,40 @@ ae_rt_status ae_rt_trace_scene_closest_queue(ae_rt_ctx* ctx, const ae_packed_ray
 ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* rays, const uint32_t* count,
                                          uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
                                          uint8_t* occluded, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Batched multi-mesh traces in one persistent launch                        */
+/* ------------------------------------------------------------------------ */
+
+/* One batch: rays against one uploaded mesh, closest hit (out = ae_hit[n]) or
+ * any hit (out = uint8_t[n]); device buffers.  This is the engine's bindless
+ * per-mesh array indexing (blasNodes[meshIdx], buffers.hsh:3-7, :45-61)
+ * turned into a launch table. */
+typedef struct ae_batch_desc {
+    int32_t mesh_id;
+    uint32_t any;
+    const ae_packed_ray* rays;
+    void* out;
+    uint32_t n_rays;
+    float tmin;
+    float tmax;
+    uint32_t reserved;
+} ae_batch_desc;
+
+/* All batches in one persistent launch: warps pull rays from one global
+ * numbering; each lane looks up its ray's batch.  Asynchronous on `stream`. */
+ae_rt_status ae_rt_trace_batched(ae_rt_ctx* ctx, const ae_batch_desc* batches, uint32_t n_batches, void* stream);
+
+/* A reusable plan of a batched launch: the batch table lives in device
+ * memory and the launch (counter reset + kernel) is captured once in a CUDA
+ * graph; ae_rt_batch_plan_launch replays it.  The plan keeps the buffer
+ * pointers of `batches`, so their contents may change between launches but
+ * not their addresses or sizes. */
+typedef struct ae_rt_batch_plan ae_rt_batch_plan;
+ae_rt_status ae_rt_batch_plan_create(ae_rt_ctx* ctx, const ae_batch_desc* batches, uint32_t n_batches,
+                                     ae_rt_batch_plan** out);
+ae_rt_status ae_rt_batch_plan_launch(ae_rt_batch_plan* plan, void* stream);
+void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan);
 
 /* Closest hit against one mesh without any device allocation.  This entry
  * point has no counterpart in the reference.  It is for hosts that own all
@@ -384,7 +426,8 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
 
 /* Per-launch statistics of the most recent trace on this context (counted
  * only when the context was created with AE_RT_CFG_COUNT_FETCHES in
- * reserved[0]): inner-node fetches and triangle fetches summed over rays. */
+ * ae_rt_config.flags): inner-node fetches and triangle fetches summed over
+ * rays. */
 #define AE_RT_CFG_COUNT_FETCHES 0x1u
 ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
 
