@@ -21,7 +21,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, lib
+from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, PtParams, lib
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
@@ -30,7 +30,14 @@ HIT_DTYPE = np.dtype([("t", "<f4"), ("triPtr", "<i4"), ("instance", "<i4"), ("fl
                       ("u", "<f4"), ("v", "<f4"), ("tSecond", "<f4"), ("reserved", "<i4")])
 INSTANCE_DTYPE = np.dtype([("inverseMatrix", "<f4", 12), ("meshOffset", "<i4"), ("materialOffset", "<i4"),
                            ("nextInstance", "<i4"), ("mask", "<u4")])
+MATERIAL_DTYPE = np.dtype([("ID", "<i4"), ("baseColor", "<f4", 3), ("emissiveColor", "<f4", 3),
+                           ("opacity", "<f4"), ("roughness", "<f4"), ("metalness", "<f4"), ("ao", "<f4"),
+                           ("reflectance", "<f4"), ("normalScale", "<f4"), ("invertUVs", "<i4"),
+                           ("twoSided", "<i4"), ("cullBackFaces", "<i4"), ("useVertexColors", "<i4"),
+                           ("baseColorTexture", "<i4"), ("opacityTexture", "<i4"), ("normalTexture", "<i4"),
+                           ("roughnessTexture", "<i4"), ("metalnessTexture", "<i4"), ("aoTexture", "<i4")])
 assert NODE_DTYPE.itemsize == 64 and HIT_DTYPE.itemsize == 32 and INSTANCE_DTYPE.itemsize == 64
+assert MATERIAL_DTYPE.itemsize == 92
 
 HIT_FLAG_HIT = 0x1
 HIT_FLAG_NEAR_TIE = 0x2
@@ -111,6 +118,16 @@ class BVH:
         o = None if opacity is None else np.ascontiguousarray(opacity, np.float32)
         if len(self.order):
             _check(lib().ae_bvh_pack_triangles(self._h, _ptr(self._verts), _ptr(m), _ptr(o), _ptr(out)))
+        return out
+
+    def pack_shading(self, normals=None, material=None, opacity=None) -> np.ndarray:
+        """GPUTriangle array (n, 24) float32 in BVH order (MeshData.cpp:172-239)."""
+        out = np.zeros((len(self.order), 24), np.float32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        m = None if material is None else np.ascontiguousarray(material, np.int32)
+        o = None if opacity is None else np.ascontiguousarray(opacity, np.float32)
+        if len(self.order):
+            _check(lib().ae_bvh_pack_shading(self._h, _ptr(self._verts), _ptr(nrm), _ptr(m), _ptr(o), _ptr(out)))
         return out
 
     @property
@@ -289,6 +306,24 @@ class Context:
         _check(lib().ae_rt_cast_pass(self._h, mesh, C.byref(cam), C.byref(params), C.byref(out),
                                      _stream_handle(stream)), self._h)
         return tuple(out.counts)
+
+    # ---- path tracer ----
+    def set_materials(self, materials):
+        materials = np.ascontiguousarray(materials, MATERIAL_DTYPE)
+        _check(lib().ae_rt_scene_set_materials(self._h, _ptr(materials) if len(materials) else None,
+                                               len(materials)), self._h)
+
+    def set_lights(self, lights):
+        lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 16)
+        _check(lib().ae_rt_scene_set_lights(self._h, _ptr(lights) if len(lights) else None, len(lights)),
+               self._h)
+
+    def pathtrace(self, cam: "Camera", accum, accum64=None, spp=1, max_bounces=3, sample_offset=0, seed=1,
+                  epsilon=0.1, stream=None):
+        p = PtParams()
+        p.spp, p.max_bounces, p.sample_offset, p.seed, p.epsilon = spp, max_bounces, sample_offset, seed, epsilon
+        _check(lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
+                                     _stream_handle(stream)), self._h)
 
     def synchronize(self, stream=None):
         _check(lib().ae_rt_synchronize(self._h, _stream_handle(stream)), self._h)

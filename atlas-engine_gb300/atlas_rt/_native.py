@@ -53,6 +53,11 @@ class CastOutputs(C.Structure):
                 ("shadow_rays", P), ("shadow_occluded", P), ("counts", U32 * 3)]
 
 
+class PtParams(C.Structure):
+    _fields_ = [("spp", U32), ("max_bounces", U32), ("sample_offset", U32), ("seed", U32),
+                ("epsilon", F32), ("reserved", U32 * 3)]
+
+
 # (name, restype, argtypes)
 _SIGNATURES = [
     ("ae_bvh_build_triangles", C.c_int, [P, P, U32, C.c_int, C.POINTER(P)]),
@@ -63,6 +68,7 @@ _SIGNATURES = [
     ("ae_bvh_get_nodes", C.c_int, [P, P]),
     ("ae_bvh_get_order", C.c_int, [P, P, P]),
     ("ae_bvh_pack_triangles", C.c_int, [P, P, P, P, P]),
+    ("ae_bvh_pack_shading", C.c_int, [P, P, P, P, P, P]),
     ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     ("ae_rt_ctx_destroy", None, [P]),
     ("ae_rt_last_error", C.c_char_p, [P]),
@@ -79,6 +85,9 @@ _SIGNATURES = [
     ("ae_rt_batch_plan_create", C.c_int, [P, P, U32, C.POINTER(P)]),
     ("ae_rt_batch_plan_launch", C.c_int, [P, P]),
     ("ae_rt_batch_plan_destroy", None, [P]),
+    ("ae_rt_scene_set_materials", C.c_int, [P, P, U32]),
+    ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
+    ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
     ("ae_rt_trace_closest_noalloc", C.c_int, [P, U32, P, U32, P, U32, F32, F32, P, P]),
     ("ae_rt_raygen", C.c_int, [P, C.POINTER(Camera), P, P]),
     ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),

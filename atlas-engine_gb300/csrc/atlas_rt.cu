@@ -2,6 +2,7 @@
 #include "atlas_rt.h"
 #include "trace_kernels.cuh"
 #include "cast_kernels.cuh"
+#include "pt_kernels.cuh"
 #include "bvh_builder.h"
 
 #include <cuda_runtime.h>
@@ -120,6 +121,14 @@ struct ae_rt_ctx {
     uint32_t n_mesh_table = 0;
     uint32_t scene_steps = 0;
     bool scene_ready = false;
+    float4* d_inst_model = nullptr;     // object-to-world rows per instance (shading)
+    float* d_materials = nullptr;       // GPUMaterial array
+    uint32_t n_materials = 0;
+    float4* d_lights = nullptr;         // GPULight array
+    uint32_t n_lights = 0;
+    // path tracer queues
+    Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
+    uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2] shadow queue
     uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
     unsigned long long* d_fetch = nullptr;
     Scratch rays_in, results_out, batch_table;
@@ -244,7 +253,7 @@ constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
 
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                    float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
-                   uint32_t cull_mask = 0xffffffffu) {
+                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false) {
     if (!ctx) return AE_RT_INVALID_ARG;
     const bool scene = mesh_id == kSceneTarget;
     if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
@@ -300,6 +309,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.n_meshes = ctx->n_mesh_table;
         p.cull_mask = cull_mask;
     }
+    p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
     ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s);
     if (st != AE_RT_OK) return st;
 
@@ -411,6 +421,13 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     cudaFree(ctx->d_tlas);
     cudaFree(ctx->d_instances);
     cudaFree(ctx->d_mesh_table);
+    cudaFree(ctx->d_inst_model);
+    cudaFree(ctx->d_materials);
+    cudaFree(ctx->d_lights);
+    cudaFree(ctx->d_pt_counts);
+    for (Scratch* sc : { &ctx->pt_rays[0], &ctx->pt_rays[1], &ctx->pt_pay[0], &ctx->pt_pay[1], &ctx->pt_hits,
+                         &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ })
+        sc->release();
     for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
         sc->release();
@@ -491,16 +508,51 @@ ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n
     for (size_t i = 0; i < table.size(); i++) {
         table[i].nodes = ctx->meshes[i].nodes;
         table[i].tris = ctx->meshes[i].tris;
+        table[i].shading = ctx->meshes[i].shading;
         table[i].n_nodes = ctx->meshes[i].n_nodes;
         table[i].n_tris = ctx->meshes[i].n_tris;
     }
     std::vector<ae_bvh_node> flagged = FlagNodes(tlas, n_tlas);
+    // object-to-world matrices: the inverse of each instance's world-to-object
+    // affine map (the engine's TransformTriangle, surface.hsh:46-61)
+    std::vector<float> model(size_t(n_instances) * 12);
+    for (uint32_t i = 0; i < n_instances; i++) {
+        const float* m = instances[i].inverseMatrix;
+        double a[3][4];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) a[r][c] = m[r * 4 + c];
+        const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+                           a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                           a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+        if (det == 0.0 || !std::isfinite(det))
+            return Fail(ctx, AE_RT_INVALID_ARG, "instance " + std::to_string(i) + " has a singular matrix");
+        double inv[3][3];
+        inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+        inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+        inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+        inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+        inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+        inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+        inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+        inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+        inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+        for (int r = 0; r < 3; r++) {
+            double t = 0.0;
+            for (int c = 0; c < 3; c++) {
+                model[size_t(i) * 12 + r * 4 + c] = float(inv[r][c]);
+                t -= inv[r][c] * a[c][3];
+            }
+            model[size_t(i) * 12 + r * 4 + 3] = float(t);
+        }
+    }
     cudaFree(ctx->d_tlas);
     cudaFree(ctx->d_instances);
     cudaFree(ctx->d_mesh_table);
+    cudaFree(ctx->d_inst_model);
     ctx->d_tlas = nullptr;
     ctx->d_instances = nullptr;
     ctx->d_mesh_table = nullptr;
+    ctx->d_inst_model = nullptr;
     ctx->scene_ready = false;
     auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
         if (!bytes) return cudaSuccess;
@@ -513,6 +565,8 @@ ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n
         e = up(reinterpret_cast<void**>(&ctx->d_instances), instances, size_t(n_instances) * sizeof(ae_bvh_instance));
     if (e == cudaSuccess)
         e = up(reinterpret_cast<void**>(&ctx->d_mesh_table), table.data(), table.size() * sizeof(table[0]));
+    if (e == cudaSuccess)
+        e = up(reinterpret_cast<void**>(&ctx->d_inst_model), model.data(), model.size() * sizeof(float));
     if (e != cudaSuccess) return CudaFail(ctx, e, "scene upload");
     ctx->n_tlas = n_tlas;
     ctx->n_instances = n_instances;
@@ -713,6 +767,132 @@ void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan) {
     cudaFree(plan->d_batches);
     cudaFree(plan->d_counter);
     delete plan;
+}
+
+ae_rt_status ae_rt_scene_set_materials(ae_rt_ctx* ctx, const ae_material* materials, uint32_t n) {
+    if (!ctx || (n && !materials)) return AE_RT_INVALID_ARG;
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaFree(ctx->d_materials);
+    ctx->d_materials = nullptr;
+    ctx->n_materials = 0;
+    if (n) {
+        AE_CUDA(ctx, cudaMalloc(&ctx->d_materials, size_t(n) * sizeof(ae_material)));
+        AE_CUDA(ctx, cudaMemcpy(ctx->d_materials, materials, size_t(n) * sizeof(ae_material), cudaMemcpyHostToDevice));
+    }
+    ctx->n_materials = n;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n) {
+    if (!ctx || (n && !lights)) return AE_RT_INVALID_ARG;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t data;
+        std::memcpy(&data, &lights[i].data[0], 4);
+        const uint32_t type = data >> 28;
+        int32_t inst;
+        std::memcpy(&inst, &lights[i].data[3], 4);
+        if (type > 1) return Fail(ctx, AE_RT_INVALID_ARG, "light " + std::to_string(i) + ": unknown type");
+        if (type == 1 && (inst < 0 || uint32_t(inst) >= ctx->n_instances))
+            return Fail(ctx, AE_RT_INVALID_ARG, "light " + std::to_string(i) + ": instance out of range");
+    }
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaFree(ctx->d_lights);
+    ctx->d_lights = nullptr;
+    ctx->n_lights = 0;
+    if (n) {
+        AE_CUDA(ctx, cudaMalloc(&ctx->d_lights, size_t(n) * sizeof(ae_light)));
+        AE_CUDA(ctx, cudaMemcpy(ctx->d_lights, lights, size_t(n) * sizeof(ae_light), cudaMemcpyHostToDevice));
+    }
+    ctx->n_lights = n;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
+                             double* accum64, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!cam || !params || !accum) return Fail(ctx, AE_RT_INVALID_ARG, "null argument");
+    if (!ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
+    if (!ctx->d_materials) return Fail(ctx, AE_RT_INVALID_ARG, "no materials have been set");
+    for (const auto& m : ctx->meshes)
+        if (!m.shading && m.n_tris) return Fail(ctx, AE_RT_INVALID_ARG, "path tracing needs shading triangles");
+    if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 28))
+        return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
+    if (!IsDevicePointer(accum) || (accum64 && !IsDevicePointer(accum64)))
+        return Fail(ctx, AE_RT_INVALID_ARG, "accumulation buffers must be device memory");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t n = cam->width * cam->height;
+    for (int k = 0; k < 2; k++) {
+        AE_CUDA(ctx, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
+        AE_CUDA(ctx, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
+    }
+    AE_CUDA(ctx, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
+    AE_CUDA(ctx, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
+    AE_CUDA(ctx, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
+    AE_CUDA(ctx, ctx->pt_occ.ensure(n));
+    if (!ctx->d_pt_counts) AE_CUDA(ctx, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+
+    atlas::rt::dev::CameraParams c{};
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+
+    atlas::rt::dev::PtParams p{};
+    p.sc.instances = ctx->d_instances;
+    p.sc.inst_model = ctx->d_inst_model;
+    p.sc.meshes = ctx->d_mesh_table;
+    p.sc.materials = ctx->d_materials;
+    p.sc.n_materials = ctx->n_materials;
+    p.sc.lights = ctx->d_lights;
+    p.sc.n_lights = ctx->n_lights;
+    p.width = cam->width;
+    p.height = cam->height;
+    p.max_bounces = params->max_bounces;
+    p.epsilon = params->epsilon;
+    p.seed = params->seed;
+    p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
+    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
+    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
+    p.n_shadow = ctx->d_pt_counts + 2;
+    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
+    p.accum = reinterpret_cast<float4*>(accum);
+    p.accum64 = accum64;
+    const uint32_t blocks = (n + 255) / 256;
+    const float kInf = 1e12f;   // INF of common.hsh:8
+    for (uint32_t smp = 0; smp < params->spp; smp++) {
+        p.sample = params->sample_offset + smp;
+        // ray generation into queue 0
+        p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
+        p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
+        p.n_out = ctx->d_pt_counts + 0;
+        atlas::rt::dev::pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
+        AE_CUDA(ctx, cudaGetLastError());
+        for (uint32_t b = 0; b <= params->max_bounces; b++) {
+            const int in = int(b & 1), out = 1 - in;
+            p.bounce = b;
+            p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
+            p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
+            p.n_in = ctx->d_pt_counts + in;
+            p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
+            p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
+            p.n_out = ctx->d_pt_counts + out;
+            ae_rt_status st = Trace(ctx, false, kSceneTarget, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n,
+                                    0.0f, kInf, ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL);
+            if (st != AE_RT_OK) return st;
+            AE_CUDA(ctx, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
+            AE_CUDA(ctx, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
+            atlas::rt::dev::pt_shade_kernel<<<blocks, 256, 0, s>>>(p);
+            AE_CUDA(ctx, cudaGetLastError());
+            st = Trace(ctx, true, kSceneTarget, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, kInf,
+                       ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
+            if (st != AE_RT_OK) return st;
+            atlas::rt::dev::pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
+            AE_CUDA(ctx, cudaGetLastError());
+        }
+    }
+    return AE_RT_OK;
 }
 
 ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream) {

@@ -2,6 +2,7 @@
 #include "atlas_rt.h"
 #include "bvh_builder.h"
 
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -86,6 +87,79 @@ ae_rt_status ae_bvh_pack_triangles(const ae_bvh* bvh, const float* verts, const 
         std::memcpy(&o.v1[3], &m, 4);
         o.v2[0] = t[6]; o.v2[1] = t[7]; o.v2[2] = t[8];
         o.v2[3] = opacity ? opacity[src] : 1.0f;
+    }
+    return AE_RT_OK;
+}
+
+namespace {
+
+// Common::Packing::PackSignedVector3x10_1x2 (src/engine/common/Packing.cpp:24-35)
+int32_t PackSigned10(float x, float y, float z, float w) {
+    int32_t p = 0;
+    p |= int32_t((x * 0.5f + 0.5f) * 1023.0f) << 0;
+    p |= int32_t((y * 0.5f + 0.5f) * 1023.0f) << 10;
+    p |= int32_t((z * 0.5f + 0.5f) * 1023.0f) << 20;
+    p |= int32_t((w * 0.5f + 0.5f) * 2.0f) << 30;
+    return p;
+}
+
+float Bits(int32_t v) {
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+}
+
+void Normalize3(const float* in, float* out) {
+    const float l = std::sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+    const float s = l > 0.0f ? 1.0f / l : 0.0f;
+    out[0] = in[0] * s;
+    out[1] = in[1] * s;
+    out[2] = in[2] * s;
+}
+
+}  // namespace
+
+// GPUTriangle packing in BVH order (MeshData.cpp:172-239), without texture
+// coordinates and vertex colours (UVs 0, colours white, tangent frame from
+// the face): normals are normalised and stored 10:10:10:2.
+ae_rt_status ae_bvh_pack_shading(const ae_bvh* bvh, const float* verts, const float* normals,
+                                 const int32_t* material, const float* opacity, ae_triangle* out) {
+    if (!bvh || !verts || (!out && bvh->primitives)) return AE_RT_INVALID_ARG;
+    for (uint32_t i = 0; i < bvh->primitives; i++) {
+        const uint32_t src = bvh->built.order[i];
+        const float* t = verts + size_t(src) * 9;
+        float n[3][3];
+        if (normals) {
+            for (int k = 0; k < 3; k++) Normalize3(normals + size_t(src) * 9 + 3 * k, n[k]);
+        } else {
+            const float e0[3] = { t[3] - t[0], t[4] - t[1], t[5] - t[2] };
+            const float e1[3] = { t[6] - t[0], t[7] - t[1], t[8] - t[2] };
+            const float c[3] = { e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0] };
+            Normalize3(c, n[0]);
+            for (int k = 0; k < 3; k++) n[1][k] = n[2][k] = n[0][k];
+        }
+        // tangent frame from the face (there are no texture coordinates)
+        float e0[3] = { t[3] - t[0], t[4] - t[1], t[5] - t[2] };
+        float tan[3], bit[3];
+        Normalize3(e0, tan);
+        const float* nn = n[0];
+        const float b[3] = { nn[1] * tan[2] - nn[2] * tan[1], nn[2] * tan[0] - nn[0] * tan[2], nn[0] * tan[1] - nn[1] * tan[0] };
+        Normalize3(b, bit);
+        ae_triangle& o = out[i];
+        for (int k = 0; k < 3; k++) {
+            float* v = k == 0 ? o.v0 : (k == 1 ? o.v1 : o.v2);
+            v[0] = t[3 * k]; v[1] = t[3 * k + 1]; v[2] = t[3 * k + 2];
+            v[3] = Bits(PackSigned10(n[k][0], n[k][1], n[k][2], 0.0f));
+        }
+        const int32_t m = material ? material[src] : 0;
+        o.d0[0] = 0.0f; o.d0[1] = 0.0f; o.d0[2] = 0.0f; o.d0[3] = Bits(m);
+        o.d1[0] = Bits(PackSigned10(tan[0], tan[1], tan[2], 0.0f));
+        o.d1[1] = Bits(PackSigned10(bit[0], bit[1], bit[2], 0.0f));
+        o.d1[2] = bvh->built.endOfNode[i] ? 1.0f : -1.0f;
+        o.d1[3] = 0.0f;
+        const int32_t white = int32_t(0xFFFFFFFFu);
+        o.d2[0] = Bits(white); o.d2[1] = Bits(white); o.d2[2] = Bits(white);
+        o.d2[3] = opacity ? opacity[src] : 1.0f;
     }
     return AE_RT_OK;
 }

@@ -1,0 +1,486 @@
+// Wavefront path tracer: ray generation, the hit/shade bounce kernel and the
+// shadow-ray resolve, around the traversal kernels.
+//
+// Estimator: the engine's non-real-time path tracer
+// (data/shader/pathtracer/rayGen.csh, rayHit.csh) --
+//   * emission of the first hit only (rayHit.csh:180-183);
+//   * next-event estimation at every vertex: one light picked by streaming
+//     weighted selection (raytracer/direct.hsh:12-49; weight =
+//     brightness*area*cos/d^2 for triangle lights, clamped to [1e-7, 1]), a
+//     uniform point on the light triangle (raytracer/lights.hsh:11-29), the
+//     Disney-diffuse + GGX BRDF (brdf/brdfEval.hsh:8-32, brdf/brdf.hsh), a
+//     shadow ray from P + N*EPSILON to the light (rayHit.csh:327-338);
+//   * the continuation: lobe picked by Fresnel (spec probability clamped to
+//     [0.1, 0.9]), cosine-weighted diffuse or GGX VNDF specular sampling
+//     (brdf/brdfSample.hsh), origin pushed back along V by EPSILON, ambient
+//     occlusion factor, Russian roulette with p = clamp(max(throughput),
+//     0.01, 0.99), tripled before bounce 3, and termination below the
+//     geometric surface (rayHit.csh:237-325);
+//   * no environment light (the scenes here have none), and -- deliberately --
+//     without the engine's clamp of indirect radiance at 10 (rayHit.csh:
+//     196-201), which biases the estimate; this renderer is the unbiased
+//     reference the radiance cache is judged against.
+// Shadow rays are not traced inline: the shade kernel appends them, with the
+// contribution they would add, to a shadow queue that the any-hit kernel
+// traces and the resolve kernel adds into the accumulation buffers (FP32,
+// and FP64 for converged images).
+// Random numbers: the PCG hash of Jarzynski & Olano (JCGT 2020) keyed by
+// (pixel, sample, bounce, dimension).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cast_kernels.cuh"
+
+namespace atlas::rt::dev {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.31830988618379067154f;
+
+struct PtScene {
+    const float4* instances;      // GPUBVHInstance (4 float4)
+    const float4* inst_model;     // object-to-world 3x4 rows per instance (3 float4)
+    const MeshDesc* meshes;
+    const float* materials;       // GPUMaterial, 23 words each
+    uint32_t n_materials;
+    const float4* lights;         // GPULight (4 float4)
+    uint32_t n_lights;
+};
+
+struct PtParams {
+    PtScene sc;
+    uint32_t width, height;
+    uint32_t sample;              // sample index (RNG stream)
+    uint32_t bounce;              // bounce of the rays being shaded
+    uint32_t max_bounces;
+    float epsilon;
+    uint32_t seed;
+    // queues
+    const float4* rays_in;        // PackedRay
+    const float4* hits_in;        // ae_hit
+    const float4* pay_in;         // throughput.xyz, pixel bits
+    const uint32_t* n_in;
+    float4* rays_out;
+    float4* pay_out;
+    uint32_t* n_out;
+    float4* shadow_rays;
+    float4* shadow_pay;           // contribution.rgb, pixel bits
+    uint32_t* n_shadow;
+    const uint8_t* shadow_occ;
+    float4* accum;                // W*H float4 (rgb, sample count in .w from raygen)
+    double* accum64;              // W*H*3 or null
+};
+
+// ---- small vector helpers (fast math is fine here: statistics, not parity) ----
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{ x, y, z }; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ V3 normalize(V3 a) {
+    const float l2 = dot(a, a);
+    return a * (l2 > 0.0f ? rsqrtf(l2) : 0.0f);
+}
+__device__ __forceinline__ float saturate(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+__device__ __forceinline__ V3 ld3(const float4& f) { return v3(f.x, f.y, f.z); }
+
+// 10:10:10:2 signed unit vector (common/packing.hsh unpackUnitVector)
+__device__ __forceinline__ V3 unpack_unit(float bits) {
+    const int32_t c = __float_as_int(bits);
+    return v3(float((c >> 0) & 1023) / 1023.0f * 2.0f - 1.0f, float((c >> 10) & 1023) / 1023.0f * 2.0f - 1.0f,
+              float((c >> 20) & 1023) / 1023.0f * 2.0f - 1.0f);
+}
+
+__device__ __forceinline__ float rng(uint32_t pixel, uint32_t sample, uint32_t bounce, uint32_t dim, uint32_t seed) {
+    return rand01(pixel, sample * 16u + bounce + (seed << 12), dim * 0x9E3779B9u + 0x7F4A7C15u);
+}
+
+struct Mat {
+    V3 base, emissive;
+    float opacity, roughness, metalness, ao, reflectance;
+    int twoSided;
+};
+
+__device__ __forceinline__ Mat load_material(const float* m) {
+    Mat r;
+    r.base = v3(m[1], m[2], m[3]);
+    r.emissive = v3(m[4], m[5], m[6]);
+    r.opacity = m[7];
+    r.roughness = m[8];
+    r.metalness = m[9];
+    r.ao = m[10];
+    r.reflectance = m[11];
+    r.twoSided = __float_as_int(m[14]);
+    return r;
+}
+
+struct Surf {
+    V3 P, V, N, L, H, geoN;
+    float NdotL, LdotH, NdotH, NdotV;
+    V3 F0;
+    float F90;
+    Mat mat;
+};
+
+// UpdateSurface (brdf/surface.hsh:25-41)
+__device__ __forceinline__ void update_surface(Surf& s) {
+    s.L = normalize(s.L);
+    s.V = normalize(s.V);
+    s.N = normalize(s.N);
+    s.H = normalize(s.L + s.V);
+    s.NdotL = saturate(dot(s.N, s.L));
+    s.LdotH = saturate(dot(s.L, s.H));
+    s.NdotH = saturate(dot(s.N, s.H));
+    s.NdotV = saturate(dot(s.N, s.V));
+    const float f0 = 0.16f * s.mat.reflectance * s.mat.reflectance;
+    s.F0 = v3(f0, f0, f0) * (1.0f - s.mat.metalness) + s.mat.base * s.mat.metalness;
+    s.F90 = saturate(50.0f * (s.F0.x * 0.333f + s.F0.y * 0.333f + s.F0.z * 0.333f));
+}
+
+__device__ __forceinline__ float pow5(float x) { return x * x * x * x * x; }
+
+__device__ __forceinline__ V3 fresnel(V3 F0, float F90, float c) {
+    const float k = pow5(1.0f - c);
+    return v3(F0.x + (F90 - F0.x) * k, F0.y + (F90 - F0.y) * k, F0.z + (F90 - F0.z) * k);
+}
+
+// brdf.hsh: RenormalizedDisneyDiffuse, visibility terms, GGX distribution
+__device__ __forceinline__ float disney_diffuse(float NdotV, float NdotL, float LdotH, float lr) {
+    const float energyBias = 0.5f * lr;
+    const float energyFactor = 1.0f + (1.0f / 1.51f - 1.0f) * lr;
+    const float FD90 = energyBias + 2.0f * LdotH * LdotH * lr;
+    const float ls = 1.0f + (FD90 - 1.0f) * pow5(1.0f - NdotL);
+    const float vs = 1.0f + (FD90 - 1.0f) * pow5(1.0f - NdotV);
+    return ls * vs * energyFactor;
+}
+__device__ __forceinline__ float vis_separable(float c, float a) {
+    const float a2 = a * a;
+    return 2.0f * c / (c + sqrtf(a2 + (1.0f - a2) * c * c));
+}
+__device__ __forceinline__ float vis_correlated(float NdotL, float NdotV, float a) {
+    const float a2 = a * a;
+    const float gl = NdotV * sqrtf((-NdotL * a2 + NdotL) * NdotL + a2);
+    const float gv = NdotL * sqrtf((-NdotV * a2 + NdotV) * NdotV + a2);
+    return 0.5f / (gl + gv + 0.0000001f);
+}
+__device__ __forceinline__ float ggx_d(float NdotH, float a) {
+    const float a2 = a * a;
+    const float f = (NdotH * a2 - NdotH) * NdotH + 1.0f;
+    return a2 / (f * f + 0.0000001f) * kInvPi;
+}
+
+// brdfEval.hsh:8-32
+__device__ __forceinline__ V3 eval_diffuse(const Surf& s) {
+    const float r = fmaxf(s.mat.roughness * s.mat.roughness, 0.00001f);
+    return s.mat.base * ((1.0f - s.mat.metalness) * disney_diffuse(s.NdotV, s.NdotL, s.LdotH, r) * kInvPi);
+}
+__device__ __forceinline__ V3 eval_specular(const Surf& s) {
+    const float r = fmaxf(s.mat.roughness * s.mat.roughness, 0.00001f);
+    return fresnel(s.F0, s.F90, s.LdotH) * (ggx_d(s.NdotH, r) * vis_correlated(s.NdotV, s.NdotL, r));
+}
+
+__device__ __forceinline__ void basis_from(V3 N, V3& t, V3& b) {
+    const V3 up = fabsf(N.z) < 0.999f ? v3(0, 0, 1) : v3(1, 0, 0);
+    t = normalize(cross(up, N));
+    b = cross(N, t);
+}
+
+// brdfSample.hsh:8-30 -- returns pdf, sets s.L
+__device__ __forceinline__ float sample_diffuse(Surf& s, float u0, float u1, V3& refl) {
+    const float th = sqrtf(u0);
+    float sp, cp;
+    sincospif(2.0f * u1, &sp, &cp);
+    V3 t, b;
+    basis_from(s.N, t, b);
+    s.L = normalize(t * (th * cp) + b * (th * sp) + s.N * sqrtf(fmaxf(0.0f, 1.0f - u0)));
+    update_surface(s);
+    refl = eval_diffuse(s);
+    return s.NdotL * kInvPi;
+}
+
+// brdfSample.hsh:32-90 (Dupuy & Benyoub spherical-cap VNDF sampling)
+__device__ __forceinline__ float sample_specular(Surf& s, float u0, float u1, V3& refl) {
+    const float alpha = s.mat.roughness * s.mat.roughness;
+    s.V = normalize(s.V);
+    const V3 N = normalize(s.N);
+    const V3 up = fabsf(N.z) < 0.999f ? v3(0, 0, 1) : v3(1, 0, 0);
+    const V3 t = normalize(cross(up, N));
+    const V3 b = normalize(cross(N, t));
+    // V in the tangent frame (V * TBN)
+    V3 Vl = normalize(v3(dot(s.V, t), dot(s.V, b), dot(s.V, N)));
+    Vl = normalize(v3(Vl.x * alpha, Vl.y * alpha, Vl.z));
+    float sp, cp;
+    sincospif(2.0f * u0, &sp, &cp);
+    const float z = (1.0f - u1) * (1.0f + Vl.z) - Vl.z;
+    const float rr = sqrtf(saturate(1.0f - z * z));
+    const V3 c = v3(cp * rr, sp * rr, z);
+    const V3 Hh = c + Vl;
+    const V3 Ml = v3(Hh.x * alpha, Hh.y * alpha, fmaxf(Hh.z, 0.0f));
+    const V3 M = normalize(t * Ml.x + b * Ml.y + N * Ml.z);
+    s.L = M * (2.0f * dot(s.V, M)) - s.V;
+    update_surface(s);
+    refl = v3(0, 0, 0);
+    float pdf = 1.0f;
+    if (s.NdotL > 0.0f && s.LdotH > 0.0f) {
+        const V3 F = fresnel(s.F0, s.F90, s.LdotH);
+        const float Vis = vis_correlated(s.NdotV, s.NdotL, alpha);
+        const float G1 = vis_separable(s.NdotV, alpha);
+        pdf = G1 / (4.0f * fabsf(dot(s.V, s.N)));
+        refl = F * Vis;
+    }
+    return pdf;
+}
+
+__device__ __forceinline__ V3 xform_point(const float4* m, V3 p) {
+    return v3(m[0].x * p.x + m[0].y * p.y + m[0].z * p.z + m[0].w, m[1].x * p.x + m[1].y * p.y + m[1].z * p.z + m[1].w,
+              m[2].x * p.x + m[2].y * p.y + m[2].z * p.z + m[2].w);
+}
+__device__ __forceinline__ V3 xform_dir(const float4* m, V3 p) {
+    return v3(m[0].x * p.x + m[0].y * p.y + m[0].z * p.z, m[1].x * p.x + m[1].y * p.y + m[1].z * p.z,
+              m[2].x * p.x + m[2].y * p.y + m[2].z * p.z);
+}
+
+struct Tri {
+    V3 v0, v1, v2, n0, n1, n2;
+    int material;
+};
+
+// GPUTriangle (common.hsh:17-44) in world space (TransformTriangle, surface.hsh:46-61)
+__device__ __forceinline__ Tri load_triangle(const PtScene& sc, int32_t inst, int32_t tri) {
+    const float4* ip = sc.instances + size_t(inst) * 4;
+    const float4 c3 = __ldg(ip + 3);
+    const MeshDesc m = sc.meshes[__float_as_int(c3.x)];
+    const float4* tp = m.shading + size_t(tri) * 6;
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2), d0 = __ldg(tp + 3);
+    const float4* M = sc.inst_model + size_t(inst) * 3;
+    float4 mm[3] = { __ldg(M), __ldg(M + 1), __ldg(M + 2) };
+    Tri t;
+    t.v0 = xform_point(mm, ld3(a));
+    t.v1 = xform_point(mm, ld3(b));
+    t.v2 = xform_point(mm, ld3(c));
+    t.n0 = normalize(xform_dir(mm, unpack_unit(a.w)));
+    t.n1 = normalize(xform_dir(mm, unpack_unit(b.w)));
+    t.n2 = normalize(xform_dir(mm, unpack_unit(c.w)));
+    t.material = __float_as_int(d0.w) + __float_as_int(c3.y);
+    return t;
+}
+
+struct Light {
+    V3 P, N, radiance;
+    uint32_t type;
+    int32_t tri, inst;
+    float pdf, area, brightness;
+};
+
+__device__ __forceinline__ Light load_light(const float4* l) {
+    const float4 P = __ldg(l), N = __ldg(l + 1), C = __ldg(l + 2), D = __ldg(l + 3);
+    Light r;
+    r.P = ld3(P);
+    r.N = ld3(N);
+    r.radiance = ld3(C);
+    const uint32_t data = __float_as_uint(D.x);
+    r.type = data >> 28;
+    r.tri = int32_t(data & 0x0FFFFFFFu);
+    r.inst = __float_as_int(D.w);
+    r.pdf = D.y;
+    r.area = D.z;
+    r.brightness = (r.radiance.x + r.radiance.y + r.radiance.z) * 0.33333f;
+    return r;
+}
+
+__global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = c.width * c.height;
+    if (i >= n) return;
+    const uint32_t pix = slot_to_pixel(i, c.width, c.height);
+    const float jx = rng(pix, p.sample, 15, 0, p.seed), jy = rng(pix, p.sample, 15, 1, p.seed);
+    const float u = (float(pix % c.width) + jx) / float(c.width);
+    const float v = (float(pix / c.width) + jy) / float(c.height);
+    V3 d = v3(c.ox + c.rx * u + c.bx * v - c.lx, c.oy + c.ry * u + c.by * v - c.ly, c.oz + c.rz * u + c.bz * v - c.lz);
+    d = normalize(d);
+    float4* r = p.rays_out + size_t(i) * 3;
+    r[0] = make_float4(c.lx, c.ly, c.lz, __int_as_float(int32_t(pix)));
+    r[1] = make_float4(d.x, d.y, d.z, 0.0f);
+    r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+    p.pay_out[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pix));
+    if (i == 0) *p.n_out = n;
+}
+
+__device__ __forceinline__ void add_radiance(const PtParams& p, uint32_t pix, V3 L) {
+    float4* a = p.accum + pix;
+    a->x += L.x;
+    a->y += L.y;
+    a->z += L.z;
+    if (p.accum64) {
+        double* d = p.accum64 + size_t(pix) * 3;
+        d[0] += double(L.x);
+        d[1] += double(L.y);
+        d[2] += double(L.z);
+    }
+}
+
+// rayHit.csh:55-325 for one bounce of the wavefront.
+__global__ void pt_shade_kernel(PtParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n = min(*p.n_in, p.width * p.height);
+    bool emitRay = false, emitShadow = false;
+    float4 outRay0{}, outRay1{}, outPay{}, shRay0{}, shRay1{}, shPay{};
+    if (i < n) {
+        const float4 h0 = p.hits_in[size_t(i) * 2];
+        const int32_t triPtr = __float_as_int(h0.y);
+        const float4 pay = p.pay_in[i];
+        const uint32_t pix = __float_as_uint(pay.w);
+        V3 thr = v3(pay.x, pay.y, pay.z);
+        if (triPtr >= 0) {
+            const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
+            const V3 ro = ld3(o4), rd = ld3(d4);
+            const int32_t inst = __float_as_int(h0.z);
+            const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
+            const Tri tri = load_triangle(p.sc, inst, triPtr);
+            const float s = h1.x, t = h1.y, r = 1.0f - s - t;
+            Surf sf;
+            sf.mat = load_material(p.sc.materials + size_t(tri.material) * 23);
+            sf.P = ro + rd * h0.x;
+            V3 N = normalize(tri.n0 * r + tri.n1 * s + tri.n2 * t);
+            V3 triN = normalize(cross(tri.v0 - tri.v1, tri.v0 - tri.v2));
+            const bool flip = dot(triN, rd) > 0.0f;
+            if (flip && sf.mat.twoSided > 0) triN = triN * -1.0f;
+            if (dot(N, triN) < 0.0f && sf.mat.twoSided > 0) N = N * -1.0f;
+            sf.V = rd * -1.0f;
+            sf.N = normalize(N);
+            sf.geoN = triN;
+            sf.L = sf.N;
+            // emission of the first hit (rayHit.csh:180-183)
+            V3 Lo = v3(0, 0, 0);
+            if (p.bounce == 0 && sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f)
+                Lo = sf.mat.emissive;
+            // ---- direct light (EvaluateDirectLight, rayHit.csh:209-235) ----
+            if (p.sc.n_lights > 0) {
+                Light sel{};
+                float selW = 0.0f, total = 0.0f;
+                for (uint32_t li = 0; li < p.sc.n_lights; li++) {
+                    const Light L = load_light(p.sc.lights + size_t(li) * 4);
+                    float w = 1.0f;
+                    if (L.type == 1u) {
+                        const V3 toL = L.P - sf.P;
+                        const float d2 = dot(toL, toL);
+                        const float NdotL = fmaxf(dot(L.N, normalize(toL) * -1.0f), 0.0f);
+                        w = L.brightness * L.area * NdotL / d2;
+                    } else {
+                        w = L.brightness;
+                    }
+                    w = fminf(fmaxf(w, 0.0000001f), 1.0f);
+                    total += w;
+                    if (rng(pix, p.sample, p.bounce, 16u + li, p.seed) < w / total) {
+                        selW = w;
+                        sel = L;
+                    }
+                }
+                const float lightPdf = selW / total * sel.pdf;
+                float solidAngle = 1.0f, dist = 1e12f;
+                if (sel.type == 1u) {
+                    const float r0 = rng(pix, p.sample, p.bounce, 1, p.seed);
+                    const float r1 = rng(pix, p.sample, p.bounce, 2, p.seed);
+                    const Tri lt = load_triangle(p.sc, sel.inst, sel.tri);
+                    const float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
+                    const V3 LP = lt.v0 * lu + lt.v1 * lv + lt.v2 * lw;
+                    const V3 LN = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
+                    const V3 toL = LP - sf.P;
+                    const float d2 = dot(toL, toL);
+                    dist = sqrtf(d2);
+                    sf.L = toL * (1.0f / dist);
+                    update_surface(sf);
+                    const float NdotLl = fmaxf(dot(LN, sf.L * -1.0f), 0.0f);
+                    solidAngle = NdotLl / (d2 * (1.0f / sel.area));
+                } else {
+                    sf.L = normalize(sel.N * -1.0f);
+                    update_surface(sf);
+                }
+                const V3 refl = (eval_diffuse(sf) + eval_specular(sf)) * sf.mat.opacity;
+                const V3 contrib = thr * sf.mat.opacity * (refl * sel.radiance) *
+                                   (solidAngle * sf.NdotL / lightPdf);
+                if (sf.NdotL > 0.0f && lightPdf > 0.0f &&
+                    contrib.x + contrib.y + contrib.z > 0.0f) {   // CheckVisibility, rayHit.csh:327-338
+                    const V3 so = sf.P + sf.N * p.epsilon;
+                    emitShadow = true;
+                    shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
+                    shRay1 = make_float4(sf.L.x, sf.L.y, sf.L.z, dist - 2.0f * p.epsilon);
+                    shPay = make_float4(contrib.x, contrib.y, contrib.z, __uint_as_float(pix));
+                }
+            }
+            if (Lo.x + Lo.y + Lo.z > 0.0f) add_radiance(p, pix, Lo);
+            // ---- continuation (EvaluateIndirectLight, rayHit.csh:237-325) ----
+            if (p.bounce < p.max_bounces) {
+                const Mat& mat = sf.mat;
+                const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
+                const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+                const float rnd = rng(pix, p.sample, p.bounce, 4, p.seed);
+                const float u0 = rng(pix, p.sample, p.bounce, 5, p.seed);
+                const float u1 = rng(pix, p.sample, p.bounce, 6, p.seed);
+                V3 refl;
+                float pdf;
+                if (rnd < specChance) {
+                    pdf = sample_specular(sf, u0, u1, refl);
+                    refl = refl * mat.opacity;
+                    pdf *= specChance;
+                } else {
+                    pdf = sample_diffuse(sf, u0, u1, refl);
+                    refl = refl * ((1.0f - mat.metalness) * mat.opacity);
+                    pdf *= (1.0f - specChance);
+                }
+                const V3 origin = sf.P + sf.V * p.epsilon;
+                if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = thr * refl * (sf.NdotL / pdf);
+                else thr = v3(0, 0, 0);
+                const V3 dir = normalize(sf.L);
+                thr = thr * mat.ao;
+                float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
+                prob = p.bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
+                const bool alive = thr.x + thr.y + thr.z > 0.0f && rng(pix, p.sample, p.bounce, 7, p.seed) <= prob &&
+                                   dot(dir, sf.geoN) > 0.0f;
+                if (alive) {
+                    thr = thr * (1.0f / prob);
+                    emitRay = true;
+                    outRay0 = make_float4(origin.x, origin.y, origin.z, __uint_as_float(pix));
+                    outRay1 = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                    outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
+                }
+            }
+        }
+    }
+    const uint32_t ri = warp_append(p.n_out, emitRay, lane);
+    if (emitRay) {
+        float4* r = p.rays_out + size_t(ri) * 3;
+        r[0] = outRay0;
+        r[1] = outRay1;
+        r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+        p.pay_out[ri] = outPay;
+    }
+    const uint32_t si = warp_append(p.n_shadow, emitShadow, lane);
+    if (emitShadow) {
+        float4* r = p.shadow_rays + size_t(si) * 3;
+        r[0] = shRay0;
+        r[1] = make_float4(shRay1.x, shRay1.y, shRay1.z, 0.0f);
+        r[2] = make_float4(shRay1.w, __int_as_float(-1), __int_as_float(-1), 0.0f);   // hit.x = tmax
+        p.shadow_pay[si] = shPay;
+    }
+}
+
+// Adds the contributions of the unoccluded shadow rays.
+__global__ void pt_resolve_kernel(PtParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = min(*p.n_shadow, p.width * p.height);
+    if (i >= n || p.shadow_occ[i]) return;
+    const float4 c = p.shadow_pay[i];
+    add_radiance(p, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+}
+
+}  // namespace atlas::rt::dev

@@ -41,9 +41,9 @@ constexpr uint32_t kHitFlagIterCap = 0x8u;
 struct MeshDesc {
     const float4* nodes;
     const float4* tris;
+    const float4* shading;       // GPUTriangle (6 float4), may be null
     uint32_t n_nodes;
     uint32_t n_tris;
-    uint32_t pad[2];
 };
 
 struct TraceParams {
@@ -74,6 +74,7 @@ struct TraceParams {
     const struct BatchDesc* batches;
     uint32_t n_batches;
     uint32_t refill_steps;       // traversal steps between warp refills
+    uint32_t per_ray_tmax;       // nonzero: a ray's tmax is its PackedRay hit.x (shadow queues)
 };
 
 // One ray batch of a batched launch: its mesh, its rays and results, its
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
                         r.prepare();
                         if (TLAS) wr = r;
+                        if (p.per_ray_tmax) tmax = ldg4(raySrc + size_t(ri) * 3 + 2).x;
                         hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
                         hitID = -1; hitInst = -1; curInst = -1;
                         node = 0; sp = 0; steps = 0; flags = 0; occl = false;

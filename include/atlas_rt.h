@@ -200,6 +200,14 @@ ae_rt_status ae_bvh_get_order(const ae_bvh* bvh, uint32_t* order, uint8_t* end_o
 ae_rt_status ae_bvh_pack_triangles(const ae_bvh* bvh, const float* verts, const int32_t* material,
                                    const float* opacity, ae_bvh_triangle* out);
 
+/* GPUTriangle packing in BVH order (MeshData.cpp:172-239) for meshes without
+ * texture coordinates or vertex colours: normals (n * 9 floats, per vertex;
+ * NULL = face normals) normalised and packed 10:10:10:2, UVs 0, colours
+ * white, tangent frame from the first edge; material and opacity per input
+ * triangle (optional: 0, 1.0). */
+ae_rt_status ae_bvh_pack_shading(const ae_bvh* bvh, const float* verts, const float* normals,
+                                 const int32_t* material, const float* opacity, ae_triangle* out);
+
 /* ------------------------------------------------------------------------ */
 /* Device context                                                            */
 /* ------------------------------------------------------------------------ */
@@ -419,6 +427,38 @@ typedef struct ae_cast_outputs {
 
 ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam,
                              const ae_bounce_params* params, ae_cast_outputs* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Path tracer                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Materials (GPUMaterial, indexed by GPUTriangle material index +
+ * GPUBVHInstance::materialOffset) and lights (GPULight; type 1 = triangle
+ * light: data.x = (1 << 28) | BVH-order triangle index, data.z = area,
+ * data.w = instance index bits; type 0 = directional: N = direction).
+ * Replaces RayTracingWorld::UpdateMaterials (RayTracingWorld.cpp:171-251)
+ * and RayTracingHelper::UpdateLights (RayTracingHelper.cpp:436-500). */
+ae_rt_status ae_rt_scene_set_materials(ae_rt_ctx* ctx, const ae_material* materials, uint32_t n);
+ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n);
+
+typedef struct ae_pt_params {
+    uint32_t spp;            /* samples per pixel in this call */
+    uint32_t max_bounces;    /* the engine's `bounces`: bounces + 1 hit evaluations */
+    uint32_t sample_offset;  /* index of the first sample (random streams continue across calls) */
+    uint32_t seed;
+    float epsilon;           /* ray origin offset (EPSILON = 0.1, common.hsh:9) */
+    uint32_t reserved[3];
+} ae_pt_params;
+
+/* Path-traces spp samples of every pixel of `cam` over the scene (which needs
+ * shading triangles, materials and lights) and adds the radiance of each
+ * sample into accum (float4 per pixel, rgb) and, if given, accum64 (double x3
+ * per pixel).  Device buffers, asynchronous on `stream`; divide by the
+ * number of samples for the image.  Replaces PathTracingRenderer::Render's
+ * ray-gen + bounce loop (PathTracingRenderer.cpp:29-192) for the
+ * non-real-time mode, without the indirect radiance clamp (rayHit.csh:196-201). */
+ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
+                             double* accum64, void* stream);
 
 /* Waits for `stream` and reports device-side errors of the context's
  * preceding asynchronous calls (stack overflow, step cap, timeouts). */

@@ -625,3 +625,359 @@ void aeo_closest_f64_brute(const aeo_tri* tris, uint32_t n_tris, const float* ra
     p.kind = K_F64; p.tris = tris; p.n_tris = n_tris; p.rays = rays; p.ptr = tri_ptr; p.t64 = t; p.t64b = t2;
     run_batch(p, n_rays, threads);
 }
+
+/* ---------------------------------------------------------------------- */
+/* Path tracer restatement (statistical oracle of the GPU path tracer)     */
+/* ---------------------------------------------------------------------- */
+
+static inline uint32_t pcg_hash(uint32_t x) {
+    uint32_t state = x * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+static inline float rand01(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = pcg_hash(a ^ pcg_hash(b ^ pcg_hash(c)));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+static inline float prng(uint32_t pix, uint32_t sample, uint32_t bounce, uint32_t dim, uint32_t seed) {
+    return rand01(pix, sample * 16u + bounce + (seed << 12), dim * 0x9E3779B9u + 0x7F4A7C15u);
+}
+
+static inline v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vmul(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline v3 vmulv(v3 a, v3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 vcross(v3 a, v3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static inline v3 vnorm(v3 a) {
+    float l2 = vdot(a, a);
+    return vmul(a, l2 > 0.0f ? 1.0f / sqrtf(l2) : 0.0f);
+}
+static inline float sat(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+static inline float p5(float x) { return x * x * x * x * x; }
+
+static v3 unpack10(float bits) {
+    int32_t c;
+    memcpy(&c, &bits, 4);
+    return mk((float)((c >> 0) & 1023) / 1023.0f * 2.0f - 1.0f, (float)((c >> 10) & 1023) / 1023.0f * 2.0f - 1.0f,
+              (float)((c >> 20) & 1023) / 1023.0f * 2.0f - 1.0f);
+}
+
+typedef struct {
+    v3 base, emissive;
+    float opacity, roughness, metalness, ao, reflectance;
+    int twoSided;
+} pt_mat;
+
+typedef struct {
+    v3 P, V, N, L, H, geoN, F0;
+    float NdotL, LdotH, NdotH, NdotV, F90;
+    pt_mat m;
+} pt_surf;
+
+static void pt_update(pt_surf* s) {   /* UpdateSurface, brdf/surface.hsh:25-41 */
+    s->L = vnorm(s->L);
+    s->V = vnorm(s->V);
+    s->N = vnorm(s->N);
+    s->H = vnorm(vadd(s->L, s->V));
+    s->NdotL = sat(vdot(s->N, s->L));
+    s->LdotH = sat(vdot(s->L, s->H));
+    s->NdotH = sat(vdot(s->N, s->H));
+    s->NdotV = sat(vdot(s->N, s->V));
+    float f0 = 0.16f * s->m.reflectance * s->m.reflectance;
+    s->F0 = vadd(vmul(mk(f0, f0, f0), 1.0f - s->m.metalness), vmul(s->m.base, s->m.metalness));
+    s->F90 = sat(50.0f * (s->F0.x * 0.333f + s->F0.y * 0.333f + s->F0.z * 0.333f));
+}
+
+static v3 pt_fresnel(v3 F0, float F90, float c) {
+    float k = p5(1.0f - c);
+    return mk(F0.x + (F90 - F0.x) * k, F0.y + (F90 - F0.y) * k, F0.z + (F90 - F0.z) * k);
+}
+static float pt_disney(float NdotV, float NdotL, float LdotH, float lr) {
+    float bias = 0.5f * lr, factor = 1.0f + (1.0f / 1.51f - 1.0f) * lr;
+    float FD90 = bias + 2.0f * LdotH * LdotH * lr;
+    return (1.0f + (FD90 - 1.0f) * p5(1.0f - NdotL)) * (1.0f + (FD90 - 1.0f) * p5(1.0f - NdotV)) * factor;
+}
+static float pt_vis_sep(float c, float a) { float a2 = a * a; return 2.0f * c / (c + sqrtf(a2 + (1.0f - a2) * c * c)); }
+static float pt_vis_cor(float NdotL, float NdotV, float a) {
+    float a2 = a * a;
+    float gl = NdotV * sqrtf((-NdotL * a2 + NdotL) * NdotL + a2);
+    float gv = NdotL * sqrtf((-NdotV * a2 + NdotV) * NdotV + a2);
+    return 0.5f / (gl + gv + 0.0000001f);
+}
+static float pt_ggx(float NdotH, float a) {
+    float a2 = a * a, f = (NdotH * a2 - NdotH) * NdotH + 1.0f;
+    return a2 / (f * f + 0.0000001f) * 0.31830988618379067154f;
+}
+static v3 pt_eval_diffuse(const pt_surf* s) {
+    float r = fmaxf(s->m.roughness * s->m.roughness, 0.00001f);
+    return vmul(s->m.base, (1.0f - s->m.metalness) * pt_disney(s->NdotV, s->NdotL, s->LdotH, r) * 0.31830988618379067154f);
+}
+static v3 pt_eval_specular(const pt_surf* s) {
+    float r = fmaxf(s->m.roughness * s->m.roughness, 0.00001f);
+    return vmul(pt_fresnel(s->F0, s->F90, s->LdotH), pt_ggx(s->NdotH, r) * pt_vis_cor(s->NdotV, s->NdotL, r));
+}
+static float pt_sample_diffuse(pt_surf* s, float u0, float u1, v3* refl) {
+    float th = sqrtf(u0), phi = 6.28318530717958647692f * u1;
+    v3 up = fabsf(s->N.z) < 0.999f ? mk(0, 0, 1) : mk(1, 0, 0);
+    v3 t = vnorm(vcross(up, s->N)), b = vcross(s->N, t);
+    s->L = vnorm(vadd(vadd(vmul(t, th * cosf(phi)), vmul(b, th * sinf(phi))), vmul(s->N, sqrtf(fmaxf(0.0f, 1.0f - u0)))));
+    pt_update(s);
+    *refl = pt_eval_diffuse(s);
+    return s->NdotL * 0.31830988618379067154f;
+}
+static float pt_sample_specular(pt_surf* s, float u0, float u1, v3* refl) {
+    float alpha = s->m.roughness * s->m.roughness;
+    s->V = vnorm(s->V);
+    v3 N = vnorm(s->N);
+    v3 up = fabsf(N.z) < 0.999f ? mk(0, 0, 1) : mk(1, 0, 0);
+    v3 t = vnorm(vcross(up, N)), b = vnorm(vcross(N, t));
+    v3 Vl = vnorm(mk(vdot(s->V, t), vdot(s->V, b), vdot(s->V, N)));
+    Vl = vnorm(mk(Vl.x * alpha, Vl.y * alpha, Vl.z));
+    float phi = 6.28318530717958647692f * u0;
+    float z = (1.0f - u1) * (1.0f + Vl.z) - Vl.z;
+    float rr = sqrtf(sat(1.0f - z * z));
+    v3 c = mk(cosf(phi) * rr, sinf(phi) * rr, z);
+    v3 Hh = vadd(c, Vl);
+    v3 Ml = mk(Hh.x * alpha, Hh.y * alpha, fmaxf(Hh.z, 0.0f));
+    v3 M = vnorm(vadd(vadd(vmul(t, Ml.x), vmul(b, Ml.y)), vmul(N, Ml.z)));
+    s->L = vadd(vmul(M, 2.0f * vdot(s->V, M)), vmul(s->V, -1.0f));
+    pt_update(s);
+    *refl = mk(0, 0, 0);
+    float pdf = 1.0f;
+    if (s->NdotL > 0.0f && s->LdotH > 0.0f) {
+        v3 F = pt_fresnel(s->F0, s->F90, s->LdotH);
+        float Vis = pt_vis_cor(s->NdotV, s->NdotL, alpha);
+        float G1 = pt_vis_sep(s->NdotV, alpha);
+        pdf = G1 / (4.0f * fabsf(vdot(s->V, s->N)));
+        *refl = vmul(F, Vis);
+    }
+    return pdf;
+}
+
+typedef struct {
+    v3 v0, v1, v2, n0, n1, n2;
+    int material;
+} pt_tri;
+
+static v3 xpoint(const float* m, v3 p) {
+    return mk(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+              m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+static v3 xdir(const float* m, v3 p) {
+    return mk(m[0] * p.x + m[1] * p.y + m[2] * p.z, m[4] * p.x + m[5] * p.y + m[6] * p.z,
+              m[8] * p.x + m[9] * p.y + m[10] * p.z);
+}
+
+typedef struct {
+    scene_t sc;
+    const float* inst_model;
+    const float* materials;
+    const float* lights;
+    uint32_t n_lights;
+    const float* cam;
+    uint32_t width, height, spp, sample_offset, max_bounces, seed;
+    float epsilon;
+    double* accum;
+    uint32_t begin, end;
+    size_t stack_cap;
+} pt_job_t;
+
+static pt_tri pt_load_tri(const pt_job_t* j, int32_t inst, int32_t tri) {
+    const aeo_instance* in = &j->sc.inst[inst];
+    const aeo_mesh* mesh = &j->sc.meshes[in->meshOffset];
+    const float* t = mesh->shading + (size_t)tri * 24;
+    const float* m = j->inst_model + (size_t)inst * 12;
+    pt_tri r;
+    r.v0 = xpoint(m, ld3(t));
+    r.v1 = xpoint(m, ld3(t + 4));
+    r.v2 = xpoint(m, ld3(t + 8));
+    r.n0 = vnorm(xdir(m, unpack10(t[3])));
+    r.n1 = vnorm(xdir(m, unpack10(t[7])));
+    r.n2 = vnorm(xdir(m, unpack10(t[11])));
+    int32_t mi;
+    memcpy(&mi, &t[15], 4);
+    r.material = mi + in->materialOffset;
+    return r;
+}
+
+static pt_mat pt_load_mat(const float* m) {
+    pt_mat r;
+    r.base = mk(m[1], m[2], m[3]);
+    r.emissive = mk(m[4], m[5], m[6]);
+    r.opacity = m[7]; r.roughness = m[8]; r.metalness = m[9]; r.ao = m[10]; r.reflectance = m[11];
+    memcpy(&r.twoSided, &m[14], 4);
+    return r;
+}
+
+static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* out) {
+    const float* c = j->cam;
+    for (uint32_t si = 0; si < j->spp; si++) {
+        uint32_t sample = j->sample_offset + si;
+        float jx = prng(pix, sample, 15, 0, j->seed), jy = prng(pix, sample, 15, 1, j->seed);
+        float u = ((float)(pix % j->width) + jx) / (float)j->width;
+        float v = ((float)(pix / j->width) + jy) / (float)j->height;
+        v3 ro = mk(c[0], c[1], c[2]);
+        v3 rd = vnorm(mk(c[3] + c[6] * u + c[9] * v - c[0], c[4] + c[7] * u + c[10] * v - c[1],
+                         c[5] + c[8] * u + c[11] * v - c[2]));
+        v3 thr = mk(1, 1, 1);
+        for (uint32_t bounce = 0; bounce <= j->max_bounces; bounce++) {
+            float r8[8] = { ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, 0.0f, 1e12f };
+            int32_t tp, ino;
+            float tuv[3];
+            scene_closest_one(&j->sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
+            if (tp < 0) break;   /* no environment light */
+            pt_tri tri = pt_load_tri(j, ino, tp);
+            float s = tuv[1], t = tuv[2], r = 1.0f - s - t;
+            pt_surf sf;
+            sf.m = pt_load_mat(j->materials + (size_t)tri.material * 23);
+            sf.P = vadd(ro, vmul(rd, tuv[0]));
+            v3 N = vnorm(vadd(vadd(vmul(tri.n0, r), vmul(tri.n1, s)), vmul(tri.n2, t)));
+            v3 triN = vnorm(vcross(sub(tri.v0, tri.v1), sub(tri.v0, tri.v2)));
+            int flip = vdot(triN, rd) > 0.0f;
+            if (flip && sf.m.twoSided > 0) triN = vmul(triN, -1.0f);
+            if (vdot(N, triN) < 0.0f && sf.m.twoSided > 0) N = vmul(N, -1.0f);
+            sf.V = vmul(rd, -1.0f);
+            sf.N = vnorm(N);
+            sf.geoN = triN;
+            sf.L = sf.N;
+            if (bounce == 0 && sf.m.emissive.x + sf.m.emissive.y + sf.m.emissive.z > 0.0f) {
+                out[0] += sf.m.emissive.x; out[1] += sf.m.emissive.y; out[2] += sf.m.emissive.z;
+            }
+            if (j->n_lights > 0) {
+                const float* sel = NULL;
+                float selW = 0.0f, total = 0.0f;
+                for (uint32_t li = 0; li < j->n_lights; li++) {
+                    const float* L = j->lights + (size_t)li * 16;
+                    uint32_t data;
+                    memcpy(&data, &L[12], 4);
+                    float bright = (L[8] + L[9] + L[10]) * 0.33333f;
+                    float w = 1.0f;
+                    if ((data >> 28) == 1u) {
+                        v3 toL = sub(ld3(L), sf.P);
+                        float d2 = vdot(toL, toL);
+                        float NdotL = fmaxf(vdot(ld3(L + 4), vmul(vnorm(toL), -1.0f)), 0.0f);
+                        w = bright * L[14] * NdotL / d2;
+                    } else {
+                        w = bright;
+                    }
+                    w = fminf(fmaxf(w, 0.0000001f), 1.0f);
+                    total += w;
+                    if (prng(pix, sample, bounce, 16u + li, j->seed) < w / total) { selW = w; sel = L; }
+                }
+                uint32_t data;
+                memcpy(&data, &sel[12], 4);
+                float lightPdf = selW / total * sel[13];
+                float solidAngle = 1.0f, dist = 1e12f;
+                if ((data >> 28) == 1u) {
+                    float r0 = prng(pix, sample, bounce, 1, j->seed), r1 = prng(pix, sample, bounce, 2, j->seed);
+                    int32_t linst;
+                    memcpy(&linst, &sel[15], 4);
+                    pt_tri lt = pt_load_tri(j, linst, (int32_t)(data & 0x0FFFFFFFu));
+                    float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
+                    v3 LP = vadd(vadd(vmul(lt.v0, lu), vmul(lt.v1, lv)), vmul(lt.v2, lw));
+                    v3 LN = vadd(vadd(vmul(lt.n0, lu), vmul(lt.n1, lv)), vmul(lt.n2, lw));
+                    v3 toL = sub(LP, sf.P);
+                    float d2 = vdot(toL, toL);
+                    dist = sqrtf(d2);
+                    sf.L = vmul(toL, 1.0f / dist);
+                    pt_update(&sf);
+                    float NdotLl = fmaxf(vdot(LN, vmul(sf.L, -1.0f)), 0.0f);
+                    solidAngle = NdotLl / (d2 * (1.0f / sel[14]));
+                } else {
+                    sf.L = vnorm(vmul(ld3(sel + 4), -1.0f));
+                    pt_update(&sf);
+                }
+                v3 refl = vmul(vadd(pt_eval_diffuse(&sf), pt_eval_specular(&sf)), sf.m.opacity);
+                v3 contrib = vmul(vmulv(vmul(thr, sf.m.opacity), vmulv(refl, ld3(sel + 8))),
+                                  solidAngle * sf.NdotL / lightPdf);
+                if (sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f) {
+                    v3 so = vadd(sf.P, vmul(sf.N, j->epsilon));
+                    float s8[8] = { so.x, so.y, so.z, sf.L.x, sf.L.y, sf.L.z, 0.0f, dist - 2.0f * j->epsilon };
+                    if (!scene_any_one(&j->sc, s8, 64u, stack)) {
+                        out[0] += contrib.x; out[1] += contrib.y; out[2] += contrib.z;
+                    }
+                }
+            }
+            if (bounce >= j->max_bounces) break;
+            v3 F = pt_fresnel(sf.F0, sf.F90, sf.NdotV);
+            float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+            float rnd = prng(pix, sample, bounce, 4, j->seed);
+            float u0 = prng(pix, sample, bounce, 5, j->seed), u1 = prng(pix, sample, bounce, 6, j->seed);
+            v3 refl;
+            float pdf;
+            if (rnd < specChance) {
+                pdf = pt_sample_specular(&sf, u0, u1, &refl);
+                refl = vmul(refl, sf.m.opacity);
+                pdf *= specChance;
+            } else {
+                pdf = pt_sample_diffuse(&sf, u0, u1, &refl);
+                refl = vmul(refl, (1.0f - sf.m.metalness) * sf.m.opacity);
+                pdf *= (1.0f - specChance);
+            }
+            v3 origin = vadd(sf.P, vmul(sf.V, j->epsilon));
+            if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = vmul(vmulv(thr, refl), sf.NdotL / pdf);
+            else thr = mk(0, 0, 0);
+            v3 dir = vnorm(sf.L);
+            thr = vmul(thr, sf.m.ao);
+            float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
+            prob = bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
+            int alive = thr.x + thr.y + thr.z > 0.0f && prng(pix, sample, bounce, 7, j->seed) <= prob &&
+                        vdot(dir, sf.geoN) > 0.0f;
+            if (!alive) break;
+            thr = vmul(thr, 1.0f / prob);
+            ro = origin;
+            rd = dir;
+        }
+    }
+}
+
+static void* run_pt_job(void* arg) {
+    pt_job_t* j = (pt_job_t*)arg;
+    int32_t* stack = (int32_t*)malloc(j->stack_cap * sizeof(int32_t));
+    for (uint32_t pix = j->begin; pix < j->end; pix++) {
+        double o[3] = { 0, 0, 0 };
+        pt_pixel(j, pix, stack, o);
+        j->accum[(size_t)pix * 3 + 0] += o[0];
+        j->accum[(size_t)pix * 3 + 1] += o[1];
+        j->accum[(size_t)pix * 3 + 2] += o[2];
+    }
+    free(stack);
+    return NULL;
+}
+
+void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
+                   uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
+                   const float* lights, uint32_t n_lights, const float* cam, uint32_t width, uint32_t height,
+                   uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
+                   int threads, double* accum) {
+    pt_job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    proto.sc = sc;
+    proto.inst_model = inst_model;
+    proto.materials = materials;
+    proto.lights = lights;
+    proto.n_lights = n_lights;
+    proto.cam = cam;
+    proto.width = width; proto.height = height; proto.spp = spp; proto.sample_offset = sample_offset;
+    proto.max_bounces = max_bounces; proto.seed = seed; proto.epsilon = epsilon;
+    proto.accum = accum;
+    proto.stack_cap = scene_stack_cap(&proto.sc);
+    uint32_t n = width * height;
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    pt_job_t jobs[256];
+    uint32_t chunk = (n + (uint32_t)threads - 1) / (uint32_t)threads;
+    int started = 0;
+    for (int t = 0; t < threads; t++) {
+        uint32_t b = (uint32_t)t * chunk;
+        if (b >= n) break;
+        jobs[t] = proto;
+        jobs[t].begin = b;
+        jobs[t].end = b + chunk < n ? b + chunk : n;
+        pthread_create(&th[t], NULL, run_pt_job, &jobs[t]);
+        started++;
+    }
+    for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}

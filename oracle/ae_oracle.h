@@ -78,6 +78,7 @@ typedef struct aeo_mesh {
     uint32_t n_nodes;
     const aeo_tri* tris;
     uint32_t n_tris;
+    const float* shading;     /* GPUTriangle, 24 floats each (path tracer only) */
 } aeo_mesh;
 
 /* Shader closest-hit over TLAS + BLASes: HitClosest with CheckInstance
@@ -91,6 +92,18 @@ void aeo_scene_closest_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_ins
 void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
                         const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
                         uint32_t cull_mask, int threads, uint8_t* occluded);
+
+/* Path tracer -- the restatement of the engine's non-real-time estimator
+ * (pathtracer/rayGen.csh, rayHit.csh, raytracer/direct.hsh, lights.hsh,
+ * brdf/*.hsh) without the indirect radiance clamp, accumulating every sample's
+ * radiance in double precision.  materials: GPUMaterial (23 words), lights:
+ * GPULight (16 floats), inst_model: object-to-world 3x4 rows per instance.
+ * cam: location[3], origin[3], right[3], bottom[3].  accum: w * h * 3. */
+void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
+                   uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
+                   const float* lights, uint32_t n_lights, const float* cam, uint32_t width, uint32_t height,
+                   uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
+                   int threads, double* accum);
 
 /* Exact-as-possible nearest hit in double precision by brute force over every
  * triangle (for small cases and for re-testing near ties): the double-precision

@@ -60,6 +60,9 @@ def port():
         L.aeo_scene_closest_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P, P, P, P, P]
         L.aeo_scene_any_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P]
         L.aeo_scene_closest_glsl.restype = None
+        L.aeo_pathtrace.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, U32, U32, U32, U32, U32,
+                                    C.c_float, C.c_int, P]
+        L.aeo_pathtrace.restype = None
         L.aeo_scene_any_glsl.restype = None
         for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
             f.restype = None
@@ -163,21 +166,26 @@ def closest_f64_brute(tris_f32, rays8, threads=os.cpu_count()):
 
 
 class _Mesh(C.Structure):
-    _fields_ = [("nodes", P), ("n_nodes", U32), ("tris", P), ("n_tris", U32)]
+    _fields_ = [("nodes", P), ("n_nodes", U32), ("tris", P), ("n_tris", U32), ("shading", P)]
 
 
 def _mesh_table(meshes):
-    """meshes: list of (nodes_f32 (n,16), tris_f32 (m,12)); keeps the arrays alive."""
+    """meshes: list of (nodes_f32 (n,16), tris_f32 (m,12)[, shading (m,24)]);
+    keeps the arrays alive."""
     keep = []
     table = (_Mesh * max(1, len(meshes)))()
-    for i, (nodes, tris) in enumerate(meshes):
-        nodes = _c(nodes, np.float32)
-        tris = _c(tris, np.float32)
+    for i, m in enumerate(meshes):
+        nodes = _c(m[0], np.float32)
+        tris = _c(m[1], np.float32)
         keep += [nodes, tris]
         table[i].nodes = nodes.ctypes.data if nodes.size else None
         table[i].n_nodes = len(nodes)
         table[i].tris = tris.ctypes.data if tris.size else None
         table[i].n_tris = len(tris)
+        if len(m) > 2 and m[2] is not None:
+            sh = _c(m[2], np.float32)
+            keep.append(sh)
+            table[i].shading = sh.ctypes.data
     return table, keep
 
 
@@ -213,6 +221,24 @@ def scene_any_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, thr
                               inst.ctypes.data, len(inst), table, len(meshes), rays8.ctypes.data, n,
                               cull_mask, threads, occ.ctypes.data)
     return occ
+
+
+def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, width, height, spp,
+              sample_offset=0, max_bounces=3, seed=1, epsilon=0.1, threads=os.cpu_count(), accum=None):
+    """CPU restatement of the path tracer; returns the summed radiance
+    (height, width, 3) float64 over spp samples (add to `accum` if given)."""
+    tlas_f32 = _c(tlas_f32, np.float32)
+    inst = np.ascontiguousarray(instances)
+    model = _c(inst_model, np.float32)
+    mats = np.ascontiguousarray(materials)
+    lights = _c(lights, np.float32)
+    cam = _c(cam, np.float32)
+    table, keep = _mesh_table(meshes)
+    out = np.zeros((height, width, 3), np.float64) if accum is None else accum
+    port().aeo_pathtrace(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst),
+                         table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), cam.ctypes.data,
+                         width, height, spp, sample_offset, max_bounces, seed, epsilon, threads, out.ctypes.data)
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,92 @@
+"""GPU path tracer against the CPU restatement of the same estimator.
+
+Both sides draw the same random numbers (PCG hash keyed by pixel, sample,
+bounce, dimension); their transcendental functions and summation orders
+differ, so individual paths can diverge and the comparison is statistical:
+at high sample counts the two images must agree to within their noise.
+"""
+import numpy as np
+import pytest
+
+import atlas_rt
+import pyoracle
+from atlas_rt import BVH, ptscene, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pt_setup():
+    ctx = atlas_rt.Context(device=0)
+    sc = ptscene.build()
+    mid, shading, lights, gt = ptscene.upload(ctx, sc)
+    bvh = sc["bvh"]
+    inst = np.array([atlas_rt.make_instance(np.eye(4), mid, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    lo, hi = atlas_rt.mesh_bounds(bvh)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    ordered = inst[top.order].copy()
+    model = np.tile(np.eye(3, 4, dtype=np.float32).reshape(-1), (len(ordered), 1))
+    oracle_scene = (top.nodes_f32, ordered, model, [(bvh.nodes_f32, gt, shading)], sc["materials"], lights)
+    yield ctx, sc, oracle_scene
+    ctx.close()
+
+
+def gpu_render(ctx, w, h, spp, offset=0, accum64=False, seed=1):
+    import torch
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h))
+    acc = torch.zeros((h * w, 4), dtype=torch.float32, device="cuda")
+    acc64 = torch.zeros((h * w, 3), dtype=torch.float64, device="cuda") if accum64 else None
+    ctx.pathtrace(cam, acc, acc64, spp=spp, sample_offset=offset, seed=seed)
+    ctx.synchronize()
+    img = acc.cpu().numpy()[:, :3].reshape(h, w, 3)
+    img64 = acc64.cpu().numpy().reshape(h, w, 3) if accum64 else None
+    return img, img64
+
+
+def cpu_render(oracle_scene, w, h, spp, offset=0, seed=1):
+    camd = scenes.pinhole_camera(w, h)
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(np.float32)
+    tl, inst, model, meshes, mats, lights = oracle_scene
+    return pyoracle.pathtrace(tl, inst, model, meshes, mats, lights, camv, w, h, spp, sample_offset=offset, seed=seed)
+
+
+def test_pt_matches_cpu_restatement(pt_setup):
+    ctx, sc, osc = pt_setup
+    w, h, spp = 64, 36, 2048
+    g, g64 = gpu_render(ctx, w, h, spp, accum64=True)
+    c = cpu_render(osc, w, h, spp)
+    g, g64, c = g / spp, g64 / spp, c / spp
+    # FP32 and FP64 accumulation of the same samples agree
+    np.testing.assert_allclose(g, g64, rtol=1e-3, atol=1e-6)
+    # whole-image energy within 1 %
+    assert abs(g64.mean() - c.mean()) / c.mean() < 0.01, (g64.mean(), c.mean())
+    # 4x4-pixel blocks within 5 % or 3e-4 absolute
+    gb = g64.reshape(h // 4, 4, w // 4, 4, 3).mean(axis=(1, 3))
+    cb = c.reshape(h // 4, 4, w // 4, 4, 3).mean(axis=(1, 3))
+    bad = np.abs(gb - cb) > np.maximum(0.05 * cb, 3e-4)
+    assert bad.mean() < 0.01, f"{bad.sum()} of {bad.size} blocks differ"
+    # the relative MSE between the two estimates is at the noise level
+    assert ptscene.rel_mse(g64, c) < 1e-4
+
+
+def test_pt_sample_streams_continue(pt_setup):
+    """Two calls of 256 samples (offset 0 and 256) equal one call of 512."""
+    ctx, sc, osc = pt_setup
+    a, _ = gpu_render(ctx, 48, 32, 256, offset=0)
+    b, _ = gpu_render(ctx, 48, 32, 256, offset=256)
+    ab, _ = gpu_render(ctx, 48, 32, 512, offset=0)
+    np.testing.assert_allclose(a + b, ab, rtol=1e-4, atol=1e-6)
+
+
+def test_pt_converges_with_spp(pt_setup):
+    """rel-MSE against a high-spp image falls roughly as 1/spp."""
+    ctx, sc, osc = pt_setup
+    w, h = 96, 54
+    ref, ref64 = gpu_render(ctx, w, h, 4096, offset=100000, accum64=True, seed=7)
+    ref64 /= 4096
+    errs = []
+    for spp in (16, 64, 256):
+        img, _ = gpu_render(ctx, w, h, spp, seed=3)
+        errs.append(ptscene.rel_mse(img / spp, ref64))
+    assert errs[0] > errs[1] > errs[2]
+    assert 2.0 < errs[0] / errs[1] < 8.0 and 2.0 < errs[1] / errs[2] < 8.0, errs
