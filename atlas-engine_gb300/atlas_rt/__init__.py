@@ -21,7 +21,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, PtParams, lib
+from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, PtParams, RcConfig, lib
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
@@ -359,6 +359,76 @@ class BatchPlan:
 
     def __del__(self):
         self.close()
+
+
+class RadianceCache:
+    """ae_rc: the learned radiance cache bound to a context's scene."""
+
+    def __init__(self, ctx: Context, aabb_min, aabb_max, log2_table=19, base_resolution=16, max_resolution=2048,
+                 learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, seed=1):
+        cfg = RcConfig()
+        cfg.log2_table, cfg.base_resolution, cfg.max_resolution = log2_table, base_resolution, max_resolution
+        cfg.learning_rate, cfg.beta1, cfg.beta2, cfg.epsilon, cfg.seed = learning_rate, beta1, beta2, epsilon, seed
+        for i in range(3):
+            cfg.aabb_min[i] = float(aabb_min[i])
+            cfg.aabb_max[i] = float(aabb_max[i])
+        self.ctx = ctx
+        self.cfg = cfg
+        h = C.c_void_p()
+        _check(lib().ae_rc_create(ctx.handle, C.byref(cfg), C.byref(h)), ctx.handle)
+        self._h = h
+        nm, ng = C.c_uint32(), C.c_uint64()
+        _check(lib().ae_rc_param_counts(h, C.byref(nm), C.byref(ng)), ctx.handle)
+        self.n_mlp, self.n_grid = nm.value, ng.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ae_rc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def get_params(self):
+        mlp = np.zeros(self.n_mlp, np.float32)
+        grid = np.zeros(self.n_grid, np.float32)
+        _check(lib().ae_rc_get_params(self._h, _ptr(mlp), _ptr(grid)), self.ctx.handle)
+        return mlp, grid
+
+    def set_params(self, mlp, grid):
+        mlp = np.ascontiguousarray(mlp, np.float32)
+        grid = np.ascontiguousarray(grid, np.float32)
+        _check(lib().ae_rc_set_params(self._h, _ptr(mlp), _ptr(grid)), self.ctx.handle)
+
+    def predict(self, queries, out, n=None, stream=None):
+        n = len(queries) if n is None else n
+        _check(lib().ae_rc_predict(self._h, _ptr(queries), n, _ptr(out), _stream_handle(stream)), self.ctx.handle)
+
+    def gradients(self, samples, grad_mlp, grad_grid, n=None, stream=None):
+        n = len(samples) if n is None else n
+        loss = C.c_float()
+        _check(lib().ae_rc_gradients(self._h, _ptr(samples), n, _ptr(grad_mlp), _ptr(grad_grid), C.byref(loss),
+                                     _stream_handle(stream)), self.ctx.handle)
+        return loss.value
+
+    def train_batch(self, samples, n=None, stream=None):
+        n = len(samples) if n is None else n
+        loss = C.c_float()
+        _check(lib().ae_rc_train_batch(self._h, _ptr(samples), n, C.byref(loss), _stream_handle(stream)),
+               self.ctx.handle)
+        return loss.value
+
+    def train_frame(self, cam: Camera, frame: int, n_paths=65536, steps=4, max_bounces=3, want_loss=False,
+                    stream=None):
+        loss = C.c_float()
+        _check(lib().ae_rc_train_frame(self._h, C.byref(cam), frame, n_paths, steps, max_bounces,
+                                       C.byref(loss) if want_loss else None, _stream_handle(stream)),
+               self.ctx.handle)
+        return loss.value if want_loss else None
+
+    def render(self, cam: Camera, frame: int, accum, last_bounce=2, stream=None):
+        _check(lib().ae_rc_render(self._h, C.byref(cam), frame, last_bounce, _ptr(accum), _stream_handle(stream)),
+               self.ctx.handle)
 
 
 def make_camera(cam: dict) -> Camera:

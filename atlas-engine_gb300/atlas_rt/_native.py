@@ -58,6 +58,12 @@ class PtParams(C.Structure):
                 ("epsilon", F32), ("reserved", U32 * 3)]
 
 
+class RcConfig(C.Structure):
+    _fields_ = [("log2_table", U32), ("base_resolution", U32), ("max_resolution", U32),
+                ("learning_rate", F32), ("beta1", F32), ("beta2", F32), ("epsilon", F32), ("seed", U32),
+                ("aabb_min", F32 * 3), ("aabb_max", F32 * 3), ("reserved", U32 * 4)]
+
+
 # (name, restype, argtypes)
 _SIGNATURES = [
     ("ae_bvh_build_triangles", C.c_int, [P, P, U32, C.c_int, C.POINTER(P)]),
@@ -88,6 +94,16 @@ _SIGNATURES = [
     ("ae_rt_scene_set_materials", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
+    ("ae_rc_create", C.c_int, [P, C.POINTER(RcConfig), C.POINTER(P)]),
+    ("ae_rc_destroy", None, [P]),
+    ("ae_rc_param_counts", C.c_int, [P, C.POINTER(U32), C.POINTER(C.c_uint64)]),
+    ("ae_rc_get_params", C.c_int, [P, P, P]),
+    ("ae_rc_set_params", C.c_int, [P, P, P]),
+    ("ae_rc_predict", C.c_int, [P, P, U32, P, P]),
+    ("ae_rc_gradients", C.c_int, [P, P, U32, P, P, C.POINTER(F32), P]),
+    ("ae_rc_train_batch", C.c_int, [P, P, U32, C.POINTER(F32), P]),
+    ("ae_rc_train_frame", C.c_int, [P, C.POINTER(Camera), U32, U32, U32, U32, C.POINTER(F32), P]),
+    ("ae_rc_render", C.c_int, [P, C.POINTER(Camera), U32, U32, P, P]),
     ("ae_rt_trace_closest_noalloc", C.c_int, [P, U32, P, U32, P, U32, F32, F32, P, P]),
     ("ae_rt_raygen", C.c_int, [P, C.POINTER(Camera), P, P]),
     ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),

@@ -57,7 +57,7 @@ __device__ __forceinline__ uint32_t slot_to_pixel(uint32_t i, uint32_t w, uint32
     return i;
 }
 
-__global__ void raygen_kernel(CameraParams c, float4* rays) {
+static __global__ void raygen_kernel(CameraParams c, float4* rays) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = c.width * c.height;
     if (i >= n) return;
@@ -110,7 +110,7 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want, ui
     return base + __popc(mask & lt);
 }
 
-__global__ void spawn_kernel(SpawnParams p) {
+static __global__ void spawn_kernel(SpawnParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;

@@ -1,0 +1,121 @@
+// Device context of the C ABI, shared by the library's translation units.
+#pragma once
+
+#include "atlas_rt.h"
+#include "trace_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+struct ae_rc;
+
+namespace atlas::rt::host {
+
+struct DeviceMesh {
+    float4* nodes = nullptr;
+    float4* tris = nullptr;
+    float4* shading = nullptr;
+    uint32_t n_nodes = 0;
+    uint32_t n_tris = 0;
+};
+
+// Grow-only device scratch buffer.
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+
+}  // namespace atlas::rt::host
+
+struct ae_rt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    uint32_t blocks_per_sm = 0;         // 0: occupancy of each kernel
+    int shape = 0;                      // index into kShapes
+    uint32_t threads = 128;
+    uint32_t max_steps_cfg = 0;
+    uint32_t refill_steps = 0;
+    bool count_fetches = false;
+    std::vector<atlas::rt::host::DeviceMesh> meshes;
+    // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot
+    float4* d_tlas = nullptr;
+    uint32_t n_tlas = 0;
+    float4* d_instances = nullptr;
+    uint32_t n_instances = 0;
+    atlas::rt::dev::MeshDesc* d_mesh_table = nullptr;
+    uint32_t n_mesh_table = 0;
+    uint32_t scene_steps = 0;
+    bool scene_ready = false;
+    float4* d_inst_model = nullptr;     // object-to-world rows per instance (shading)
+    float* d_materials = nullptr;       // GPUMaterial array
+    uint32_t n_materials = 0;
+    float4* d_lights = nullptr;         // GPULight array
+    uint32_t n_lights = 0;
+    // path tracer queues
+    atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
+    uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2] shadow queue
+    uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
+    unsigned long long* d_fetch = nullptr;
+    atlas::rt::host::Scratch rays_in, results_out, batch_table;
+    // buffers of ae_rt_cast_pass
+    atlas::rt::host::Scratch cast_primary, cast_primary_hits, cast_secondary, cast_secondary_hits, cast_shadow, cast_occluded;
+    uint32_t* d_cast_counts = nullptr;
+    std::string last_error;
+    std::mutex upload_mutex;
+};
+
+namespace atlas::rt::host {
+
+inline ae_rt_status Fail(ae_rt_ctx* ctx, ae_rt_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+inline ae_rt_status CudaFail(ae_rt_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return Fail(ctx, AE_RT_OUT_OF_MEMORY, m);
+    return Fail(ctx, AE_RT_CUDA_ERROR, m);
+}
+
+#define AE_CUDA(ctx, call)                                         \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return CudaFail((ctx), e_, #call);  \
+    } while (0)
+
+// True when the GPU can read `p` directly as device memory.
+inline bool IsDevicePointer(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+
+// Queue-driven trace over the context's two-level scene (rays, out and count
+// in device memory), for the other translation units.
+ae_rt_status TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity, float tmin,
+                             float tmax, void* out, void* stream, const uint32_t* count_dev, uint32_t cull_mask,
+                             bool per_ray_tmax);
+
+}  // namespace atlas::rt::host

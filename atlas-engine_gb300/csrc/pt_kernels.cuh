@@ -296,7 +296,7 @@ __device__ __forceinline__ Light load_light(const float4* l) {
     return r;
 }
 
-__global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
+static __global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = c.width * c.height;
     if (i >= n) return;
@@ -327,8 +327,122 @@ __device__ __forceinline__ void add_radiance(const PtParams& p, uint32_t pix, V3
     }
 }
 
+// GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit:
+// position, interpolated shading normal, geometric normal (both flipped
+// towards the ray on two-sided materials), material.
+__device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, float t, int32_t inst, int32_t triPtr,
+                                             float bu, float bv) {
+    const Tri tri = load_triangle(sc, inst, triPtr);
+    const float r = 1.0f - bu - bv;
+    Surf sf;
+    sf.mat = load_material(sc.materials + size_t(tri.material) * 23);
+    sf.P = ro + rd * t;
+    V3 N = normalize(tri.n0 * r + tri.n1 * bu + tri.n2 * bv);
+    V3 triN = normalize(cross(tri.v0 - tri.v1, tri.v0 - tri.v2));
+    const bool flip = dot(triN, rd) > 0.0f;
+    if (flip && sf.mat.twoSided > 0) triN = triN * -1.0f;
+    if (dot(N, triN) < 0.0f && sf.mat.twoSided > 0) N = N * -1.0f;
+    sf.V = rd * -1.0f;
+    sf.N = normalize(N);
+    sf.geoN = triN;
+    sf.L = sf.N;
+    return sf;
+}
+
+// EvaluateDirectLight (rayHit.csh:209-235) up to the visibility test: picks a
+// light, samples it, evaluates the BRDF.  Returns false when nothing needs a
+// shadow ray; otherwise the contribution (already scaled by the path
+// throughput) and the shadow ray (origin, direction, tmax).
+__device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr, uint32_t pix, uint32_t sample,
+                                             uint32_t bounce, uint32_t seed, float eps, V3& contrib, V3& so,
+                                             V3& sd, float& stmax) {
+    if (sc.n_lights == 0) return false;
+    Light sel{};
+    float selW = 0.0f, total = 0.0f;
+    for (uint32_t li = 0; li < sc.n_lights; li++) {
+        const Light L = load_light(sc.lights + size_t(li) * 4);
+        float w = 1.0f;
+        if (L.type == 1u) {
+            const V3 toL = L.P - sf.P;
+            const float d2 = dot(toL, toL);
+            const float NdotL = fmaxf(dot(L.N, normalize(toL) * -1.0f), 0.0f);
+            w = L.brightness * L.area * NdotL / d2;
+        } else {
+            w = L.brightness;
+        }
+        w = fminf(fmaxf(w, 0.0000001f), 1.0f);
+        total += w;
+        if (rng(pix, sample, bounce, 16u + li, seed) < w / total) {
+            selW = w;
+            sel = L;
+        }
+    }
+    const float lightPdf = selW / total * sel.pdf;
+    float solidAngle = 1.0f, dist = 1e12f;
+    if (sel.type == 1u) {
+        const float r0 = rng(pix, sample, bounce, 1, seed);
+        const float r1 = rng(pix, sample, bounce, 2, seed);
+        const Tri lt = load_triangle(sc, sel.inst, sel.tri);
+        const float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
+        const V3 LP = lt.v0 * lu + lt.v1 * lv + lt.v2 * lw;
+        const V3 LN = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
+        const V3 toL = LP - sf.P;
+        const float d2 = dot(toL, toL);
+        dist = sqrtf(d2);
+        sf.L = toL * (1.0f / dist);
+        update_surface(sf);
+        const float NdotLl = fmaxf(dot(LN, sf.L * -1.0f), 0.0f);
+        solidAngle = NdotLl / (d2 * (1.0f / sel.area));
+    } else {
+        sf.L = normalize(sel.N * -1.0f);
+        update_surface(sf);
+    }
+    const V3 refl = (eval_diffuse(sf) + eval_specular(sf)) * sf.mat.opacity;
+    contrib = thr * sf.mat.opacity * (refl * sel.radiance) * (solidAngle * sf.NdotL / lightPdf);
+    if (!(sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f)) return false;
+    so = sf.P + sf.N * eps;         // CheckVisibility, rayHit.csh:327-338
+    sd = sf.L;
+    stmax = dist - 2.0f * eps;
+    return true;
+}
+
+// EvaluateIndirectLight (rayHit.csh:237-325): lobe choice, BRDF sample,
+// throughput update, Russian roulette, termination below the surface.
+// Returns true when the path continues with (o, d) and throughput thr.
+__device__ __forceinline__ bool continue_path(Surf& sf, V3& thr, uint32_t pix, uint32_t sample, uint32_t bounce,
+                                              uint32_t seed, float eps, V3& o, V3& d) {
+    const Mat& mat = sf.mat;
+    const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
+    const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+    const float rnd = rng(pix, sample, bounce, 4, seed);
+    const float u0 = rng(pix, sample, bounce, 5, seed);
+    const float u1 = rng(pix, sample, bounce, 6, seed);
+    V3 refl;
+    float pdf;
+    if (rnd < specChance) {
+        pdf = sample_specular(sf, u0, u1, refl);
+        refl = refl * mat.opacity;
+        pdf *= specChance;
+    } else {
+        pdf = sample_diffuse(sf, u0, u1, refl);
+        refl = refl * ((1.0f - mat.metalness) * mat.opacity);
+        pdf *= (1.0f - specChance);
+    }
+    o = sf.P + sf.V * eps;
+    if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = thr * refl * (sf.NdotL / pdf);
+    else thr = v3(0, 0, 0);
+    d = normalize(sf.L);
+    thr = thr * mat.ao;
+    float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
+    prob = bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
+    const bool alive = thr.x + thr.y + thr.z > 0.0f && rng(pix, sample, bounce, 7, seed) <= prob &&
+                       dot(d, sf.geoN) > 0.0f;
+    if (alive) thr = thr * (1.0f / prob);
+    return alive;
+}
+
 // rayHit.csh:55-325 for one bounce of the wavefront.
-__global__ void pt_shade_kernel(PtParams p) {
+static __global__ void pt_shade_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = min(*p.n_in, p.width * p.height);
@@ -342,115 +456,25 @@ __global__ void pt_shade_kernel(PtParams p) {
         V3 thr = v3(pay.x, pay.y, pay.z);
         if (triPtr >= 0) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
-            const V3 ro = ld3(o4), rd = ld3(d4);
-            const int32_t inst = __float_as_int(h0.z);
             const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
-            const Tri tri = load_triangle(p.sc, inst, triPtr);
-            const float s = h1.x, t = h1.y, r = 1.0f - s - t;
-            Surf sf;
-            sf.mat = load_material(p.sc.materials + size_t(tri.material) * 23);
-            sf.P = ro + rd * h0.x;
-            V3 N = normalize(tri.n0 * r + tri.n1 * s + tri.n2 * t);
-            V3 triN = normalize(cross(tri.v0 - tri.v1, tri.v0 - tri.v2));
-            const bool flip = dot(triN, rd) > 0.0f;
-            if (flip && sf.mat.twoSided > 0) triN = triN * -1.0f;
-            if (dot(N, triN) < 0.0f && sf.mat.twoSided > 0) N = N * -1.0f;
-            sf.V = rd * -1.0f;
-            sf.N = normalize(N);
-            sf.geoN = triN;
-            sf.L = sf.N;
+            Surf sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
             // emission of the first hit (rayHit.csh:180-183)
-            V3 Lo = v3(0, 0, 0);
             if (p.bounce == 0 && sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f)
-                Lo = sf.mat.emissive;
-            // ---- direct light (EvaluateDirectLight, rayHit.csh:209-235) ----
-            if (p.sc.n_lights > 0) {
-                Light sel{};
-                float selW = 0.0f, total = 0.0f;
-                for (uint32_t li = 0; li < p.sc.n_lights; li++) {
-                    const Light L = load_light(p.sc.lights + size_t(li) * 4);
-                    float w = 1.0f;
-                    if (L.type == 1u) {
-                        const V3 toL = L.P - sf.P;
-                        const float d2 = dot(toL, toL);
-                        const float NdotL = fmaxf(dot(L.N, normalize(toL) * -1.0f), 0.0f);
-                        w = L.brightness * L.area * NdotL / d2;
-                    } else {
-                        w = L.brightness;
-                    }
-                    w = fminf(fmaxf(w, 0.0000001f), 1.0f);
-                    total += w;
-                    if (rng(pix, p.sample, p.bounce, 16u + li, p.seed) < w / total) {
-                        selW = w;
-                        sel = L;
-                    }
-                }
-                const float lightPdf = selW / total * sel.pdf;
-                float solidAngle = 1.0f, dist = 1e12f;
-                if (sel.type == 1u) {
-                    const float r0 = rng(pix, p.sample, p.bounce, 1, p.seed);
-                    const float r1 = rng(pix, p.sample, p.bounce, 2, p.seed);
-                    const Tri lt = load_triangle(p.sc, sel.inst, sel.tri);
-                    const float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
-                    const V3 LP = lt.v0 * lu + lt.v1 * lv + lt.v2 * lw;
-                    const V3 LN = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
-                    const V3 toL = LP - sf.P;
-                    const float d2 = dot(toL, toL);
-                    dist = sqrtf(d2);
-                    sf.L = toL * (1.0f / dist);
-                    update_surface(sf);
-                    const float NdotLl = fmaxf(dot(LN, sf.L * -1.0f), 0.0f);
-                    solidAngle = NdotLl / (d2 * (1.0f / sel.area));
-                } else {
-                    sf.L = normalize(sel.N * -1.0f);
-                    update_surface(sf);
-                }
-                const V3 refl = (eval_diffuse(sf) + eval_specular(sf)) * sf.mat.opacity;
-                const V3 contrib = thr * sf.mat.opacity * (refl * sel.radiance) *
-                                   (solidAngle * sf.NdotL / lightPdf);
-                if (sf.NdotL > 0.0f && lightPdf > 0.0f &&
-                    contrib.x + contrib.y + contrib.z > 0.0f) {   // CheckVisibility, rayHit.csh:327-338
-                    const V3 so = sf.P + sf.N * p.epsilon;
-                    emitShadow = true;
-                    shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
-                    shRay1 = make_float4(sf.L.x, sf.L.y, sf.L.z, dist - 2.0f * p.epsilon);
-                    shPay = make_float4(contrib.x, contrib.y, contrib.z, __uint_as_float(pix));
-                }
+                add_radiance(p, pix, sf.mat.emissive);
+            V3 c, so, sd;
+            float st;
+            if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st)) {
+                emitShadow = true;
+                shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
+                shRay1 = make_float4(sd.x, sd.y, sd.z, st);
+                shPay = make_float4(c.x, c.y, c.z, __uint_as_float(pix));
             }
-            if (Lo.x + Lo.y + Lo.z > 0.0f) add_radiance(p, pix, Lo);
-            // ---- continuation (EvaluateIndirectLight, rayHit.csh:237-325) ----
             if (p.bounce < p.max_bounces) {
-                const Mat& mat = sf.mat;
-                const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
-                const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
-                const float rnd = rng(pix, p.sample, p.bounce, 4, p.seed);
-                const float u0 = rng(pix, p.sample, p.bounce, 5, p.seed);
-                const float u1 = rng(pix, p.sample, p.bounce, 6, p.seed);
-                V3 refl;
-                float pdf;
-                if (rnd < specChance) {
-                    pdf = sample_specular(sf, u0, u1, refl);
-                    refl = refl * mat.opacity;
-                    pdf *= specChance;
-                } else {
-                    pdf = sample_diffuse(sf, u0, u1, refl);
-                    refl = refl * ((1.0f - mat.metalness) * mat.opacity);
-                    pdf *= (1.0f - specChance);
-                }
-                const V3 origin = sf.P + sf.V * p.epsilon;
-                if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = thr * refl * (sf.NdotL / pdf);
-                else thr = v3(0, 0, 0);
-                const V3 dir = normalize(sf.L);
-                thr = thr * mat.ao;
-                float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
-                prob = p.bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
-                const bool alive = thr.x + thr.y + thr.z > 0.0f && rng(pix, p.sample, p.bounce, 7, p.seed) <= prob &&
-                                   dot(dir, sf.geoN) > 0.0f;
-                if (alive) {
-                    thr = thr * (1.0f / prob);
+                V3 o, d;
+                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d)) {
                     emitRay = true;
-                    outRay0 = make_float4(origin.x, origin.y, origin.z, __uint_as_float(pix));
-                    outRay1 = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                    outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
+                    outRay1 = make_float4(d.x, d.y, d.z, 0.0f);
                     outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
                 }
             }
@@ -475,7 +499,7 @@ __global__ void pt_shade_kernel(PtParams p) {
 }
 
 // Adds the contributions of the unoccluded shadow rays.
-__global__ void pt_resolve_kernel(PtParams p) {
+static __global__ void pt_resolve_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = min(*p.n_shadow, p.width * p.height);
     if (i >= n || p.shadow_occ[i]) return;

@@ -1,0 +1,447 @@
+// Radiance cache entry points (include/atlas_rt.h, ae_rc_*): parameters and
+// optimizer state in device memory, online training from self-generated
+// paths, rendering with paths terminated into the cache.
+#include "atlas_rt.h"
+#include "context.cuh"
+#include "rc_kernels.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+using namespace atlas::rt::host;
+using namespace atlas::rt::dev;
+
+struct ae_rc {
+    ae_rt_ctx* ctx = nullptr;
+    ae_rc_config cfg{};
+    RcGrid grid{};                 // host-side description (device pointers inside)
+    size_t grid_params = 0;        // levels * T * 2
+    float* mlp_master = nullptr;
+    float* mlp_m = nullptr;
+    float* mlp_v = nullptr;
+    float* mlp_grad = nullptr;
+    __nv_bfloat16* mlp_bf16 = nullptr;
+    float* grid_master = nullptr;
+    float* grid_m = nullptr;
+    float* grid_v = nullptr;
+    float* grid_grad = nullptr;
+    __half* grid_f16 = nullptr;
+    float* d_loss = nullptr;
+    uint32_t* d_counts = nullptr;  // [0] training samples, [1] cache queries
+    Scratch samples, queries;
+    uint64_t step = 0;
+    int sm_count = 0;
+};
+
+namespace {
+
+constexpr size_t kTrainSmem = RC_WBYTES + (RC_HIDDEN + 1) * RC_ABYTES + 2 * RC_ABYTES;
+constexpr size_t kInferSmem = RC_WBYTES + RC_ABYTES;
+
+ae_rt_status RcFail(ae_rc* rc, ae_rt_status s, const std::string& m) { return Fail(rc ? rc->ctx : nullptr, s, m); }
+
+#define RC_CUDA(rc, call)                                                     \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) return CudaFail((rc)->ctx, e_, #call);         \
+    } while (0)
+
+RcMlpParams MlpParams(ae_rc* rc) {
+    RcMlpParams p{};
+    p.grid = rc->grid;
+    p.weights = rc->mlp_bf16;
+    p.grad_w = rc->mlp_grad;
+    p.loss = rc->d_loss;
+    return p;
+}
+
+uint32_t GridBlocks(ae_rc* rc, uint32_t n) {
+    const uint32_t tiles = (n + RC_TILE - 1) / RC_TILE;
+    uint32_t b = uint32_t(rc->sm_count);
+    return tiles < b ? (tiles ? tiles : 1) : b;
+}
+
+// Gradients of the relative L2 loss over n training records (device) into
+// mlp_grad / grid_grad (zeroed first); loss sum into d_loss.
+ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t* n_dev, uint32_t offset,
+                      float inv_norm, cudaStream_t s) {
+    RC_CUDA(rc, cudaMemsetAsync(rc->mlp_grad, 0, RC_NPARAM * sizeof(float), s));
+    RC_CUDA(rc, cudaMemsetAsync(rc->grid_grad, 0, rc->grid_params * sizeof(float), s));
+    RC_CUDA(rc, cudaMemsetAsync(rc->d_loss, 0, sizeof(float), s));
+    RcMlpParams p = MlpParams(rc);
+    p.recs = recs;
+    p.n = n;
+    p.n_dev = n_dev;
+    p.offset = offset;
+    p.inv_norm = inv_norm;
+    const uint32_t count = n > offset ? n - offset : 0;
+    rc_mlp_kernel<RC_TRAIN><<<GridBlocks(rc, count), RC_THREADS, kTrainSmem, s>>>(p);
+    RC_CUDA(rc, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+ae_rt_status AdamStep(ae_rc* rc, cudaStream_t s) {
+    rc->step++;
+    const double b1 = rc->cfg.beta1, b2 = rc->cfg.beta2;
+    const float scale = float(std::sqrt(1.0 - std::pow(b2, double(rc->step))) / (1.0 - std::pow(b1, double(rc->step))));
+    RcAdamParams a{};
+    a.lr = rc->cfg.learning_rate;
+    a.beta1 = rc->cfg.beta1;
+    a.beta2 = rc->cfg.beta2;
+    a.eps = rc->cfg.epsilon;
+    a.step_scale = scale;
+    a.master = rc->mlp_master; a.m = rc->mlp_m; a.v = rc->mlp_v; a.grad = rc->mlp_grad;
+    a.out_bf16 = rc->mlp_bf16; a.out_f16 = nullptr; a.n = RC_NPARAM;
+    rc_adam_kernel<<<(RC_NPARAM + 255) / 256, 256, 0, s>>>(a);
+    RC_CUDA(rc, cudaGetLastError());
+    a.master = rc->grid_master; a.m = rc->grid_m; a.v = rc->grid_v; a.grad = rc->grid_grad;
+    a.out_bf16 = nullptr; a.out_f16 = rc->grid_f16; a.n = rc->grid_params;
+    rc_adam_kernel<<<uint32_t(rc->sm_count) * 8u, 256, 0, s>>>(a);
+    RC_CUDA(rc, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+void Destroy(ae_rc* rc) {
+    if (!rc) return;
+    cudaSetDevice(rc->ctx->device);
+    for (void* p : { (void*)rc->mlp_master, (void*)rc->mlp_m, (void*)rc->mlp_v, (void*)rc->mlp_grad,
+                     (void*)rc->mlp_bf16, (void*)rc->grid_master, (void*)rc->grid_m, (void*)rc->grid_v,
+                     (void*)rc->grid_grad, (void*)rc->grid_f16, (void*)rc->d_loss, (void*)rc->d_counts })
+        cudaFree(p);
+    rc->samples.release();
+    rc->queries.release();
+    delete rc;
+}
+
+ae_rt_status UploadParams(ae_rc* rc, const float* mlp, const float* grid) {
+    RC_CUDA(rc, cudaMemcpy(rc->mlp_master, mlp, RC_NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+    RC_CUDA(rc, cudaMemcpy(rc->grid_master, grid, rc->grid_params * sizeof(float), cudaMemcpyHostToDevice));
+    std::vector<__nv_bfloat16> wb(RC_NPARAM);
+    for (int i = 0; i < RC_NPARAM; i++) wb[i] = __float2bfloat16_rn(mlp[i]);
+    RC_CUDA(rc, cudaMemcpy(rc->mlp_bf16, wb.data(), RC_NPARAM * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+    std::vector<__half> gh(rc->grid_params);
+    for (size_t i = 0; i < rc->grid_params; i++) gh[i] = __float2half_rn(grid[i]);
+    RC_CUDA(rc, cudaMemcpy(rc->grid_f16, gh.data(), rc->grid_params * sizeof(__half), cudaMemcpyHostToDevice));
+    RC_CUDA(rc, cudaMemset(rc->mlp_m, 0, RC_NPARAM * sizeof(float)));
+    RC_CUDA(rc, cudaMemset(rc->mlp_v, 0, RC_NPARAM * sizeof(float)));
+    RC_CUDA(rc, cudaMemset(rc->grid_m, 0, rc->grid_params * sizeof(float)));
+    RC_CUDA(rc, cudaMemset(rc->grid_v, 0, rc->grid_params * sizeof(float)));
+    rc->step = 0;
+    return AE_RT_OK;
+}
+
+bool DevPtr(const void* p) { return IsDevicePointer(p); }
+
+}  // namespace
+
+extern "C" {
+
+ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out) {
+    if (!ctx || !cfg || !out) return AE_RT_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->log2_table < 10 || cfg->log2_table > 24 || cfg->base_resolution < 2 ||
+        cfg->max_resolution < cfg->base_resolution || cfg->max_resolution > (1u << 20))
+        return Fail(ctx, AE_RT_INVALID_ARG, "radiance cache: encoding parameters out of range");
+    for (int a = 0; a < 3; a++)
+        if (!(cfg->aabb_max[a] > cfg->aabb_min[a])) return Fail(ctx, AE_RT_INVALID_ARG, "radiance cache: empty domain");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    ae_rc* rc = new (std::nothrow) ae_rc;
+    if (!rc) return AE_RT_OUT_OF_MEMORY;
+    rc->ctx = ctx;
+    rc->cfg = *cfg;
+    rc->sm_count = ctx->sm_count;
+    RcGrid& g = rc->grid;
+    g.T = 1u << cfg->log2_table;
+    g.lox = cfg->aabb_min[0]; g.loy = cfg->aabb_min[1]; g.loz = cfg->aabb_min[2];
+    g.sx = 1.0f / (cfg->aabb_max[0] - cfg->aabb_min[0]);
+    g.sy = 1.0f / (cfg->aabb_max[1] - cfg->aabb_min[1]);
+    g.sz = 1.0f / (cfg->aabb_max[2] - cfg->aabb_min[2]);
+    // geometric progression of resolutions from the base to the finest level
+    const double b = std::exp((std::log(double(cfg->max_resolution)) - std::log(double(cfg->base_resolution))) /
+                              double(RC_LEVELS - 1));
+    for (int l = 0; l < RC_LEVELS; l++) {
+        const double r = std::floor(double(cfg->base_resolution) * std::pow(b, double(l)) + 1e-6);
+        g.res[l] = float(r);
+        const double st = r + 1.0;
+        g.dense[l] = st * st * st <= double(g.T) ? uint32_t(st) : 0u;
+    }
+    rc->grid_params = size_t(RC_LEVELS) * g.T * 2;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void**)&rc->mlp_master, RC_NPARAM * sizeof(float));
+    alloc((void**)&rc->mlp_m, RC_NPARAM * sizeof(float));
+    alloc((void**)&rc->mlp_v, RC_NPARAM * sizeof(float));
+    alloc((void**)&rc->mlp_grad, RC_NPARAM * sizeof(float));
+    alloc((void**)&rc->mlp_bf16, RC_NPARAM * sizeof(__nv_bfloat16));
+    alloc((void**)&rc->grid_master, rc->grid_params * sizeof(float));
+    alloc((void**)&rc->grid_m, rc->grid_params * sizeof(float));
+    alloc((void**)&rc->grid_v, rc->grid_params * sizeof(float));
+    alloc((void**)&rc->grid_grad, rc->grid_params * sizeof(float));
+    alloc((void**)&rc->grid_f16, rc->grid_params * sizeof(__half));
+    alloc((void**)&rc->d_loss, sizeof(float));
+    alloc((void**)&rc->d_counts, 4 * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rc_mlp_kernel<RC_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rc_mlp_kernel<RC_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rc_mlp_kernel<RC_PREDICT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem));
+    if (e != cudaSuccess) {
+        Destroy(rc);
+        return CudaFail(ctx, e, "radiance cache allocation");
+    }
+    g.table = reinterpret_cast<const __half2*>(rc->grid_f16);
+    g.grad = reinterpret_cast<float2*>(rc->grid_grad);
+    // initial parameters: Glorot-uniform weights (output rows beyond RGB zero),
+    // grid features uniform in +-1e-4
+    std::mt19937 gen(cfg->seed);
+    std::vector<float> w(RC_NPARAM, 0.0f);
+    const float lim = std::sqrt(6.0f / float(RC_W + RC_W));
+    std::uniform_real_distribution<float> uw(-lim, lim);
+    for (int i = 0; i < RC_HIDDEN * RC_W * RC_W; i++) w[i] = uw(gen);
+    const float limo = std::sqrt(6.0f / float(RC_W + 3));
+    std::uniform_real_distribution<float> uo(-limo, limo);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < RC_W; c++) w[RC_HIDDEN * RC_W * RC_W + r * RC_W + c] = uo(gen);
+    std::vector<float> gp(rc->grid_params);
+    std::uniform_real_distribution<float> ug(-1e-4f, 1e-4f);
+    for (auto& x : gp) x = ug(gen);
+    ae_rt_status st = UploadParams(rc, w.data(), gp.data());
+    if (st != AE_RT_OK) {
+        Destroy(rc);
+        return st;
+    }
+    *out = rc;
+    return AE_RT_OK;
+}
+
+void ae_rc_destroy(ae_rc* rc) { Destroy(rc); }
+
+ae_rt_status ae_rc_param_counts(const ae_rc* rc, uint32_t* n_mlp, uint64_t* n_grid) {
+    if (!rc) return AE_RT_INVALID_ARG;
+    if (n_mlp) *n_mlp = RC_NPARAM;
+    if (n_grid) *n_grid = rc->grid_params;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_get_params(ae_rc* rc, float* mlp, float* grid) {
+    if (!rc) return AE_RT_INVALID_ARG;
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    RC_CUDA(rc, cudaDeviceSynchronize());
+    if (mlp) RC_CUDA(rc, cudaMemcpy(mlp, rc->mlp_master, RC_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    if (grid) RC_CUDA(rc, cudaMemcpy(grid, rc->grid_master, rc->grid_params * sizeof(float), cudaMemcpyDeviceToHost));
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_set_params(ae_rc* rc, const float* mlp, const float* grid) {
+    if (!rc || !mlp || !grid) return AE_RT_INVALID_ARG;
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    RC_CUDA(rc, cudaDeviceSynchronize());
+    return UploadParams(rc, mlp, grid);
+}
+
+ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* out, void* stream) {
+    if (!rc) return AE_RT_INVALID_ARG;
+    if (n == 0) return AE_RT_OK;
+    if (!DevPtr(queries) || !DevPtr(out)) return RcFail(rc, AE_RT_INVALID_ARG, "ae_rc_predict takes device buffers");
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    RcMlpParams p = MlpParams(rc);
+    p.recs = reinterpret_cast<const float4*>(queries);
+    p.n = n;
+    p.out = reinterpret_cast<float4*>(out);
+    rc_mlp_kernel<RC_PREDICT><<<GridBlocks(rc, n), RC_THREADS, kInferSmem, static_cast<cudaStream_t>(stream)>>>(p);
+    RC_CUDA(rc, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float* grad_mlp, float* grad_grid,
+                             float* loss_out, void* stream) {
+    if (!rc) return AE_RT_INVALID_ARG;
+    if (n == 0 || !DevPtr(samples)) return RcFail(rc, AE_RT_INVALID_ARG, "ae_rc_gradients takes device samples");
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 1.0f / (3.0f * float(n)), s);
+    if (st != AE_RT_OK) return st;
+    if (grad_mlp) RC_CUDA(rc, cudaMemcpyAsync(grad_mlp, rc->mlp_grad, RC_NPARAM * sizeof(float), cudaMemcpyDefault, s));
+    if (grad_grid)
+        RC_CUDA(rc, cudaMemcpyAsync(grad_grid, rc->grid_grad, rc->grid_params * sizeof(float), cudaMemcpyDefault, s));
+    if (loss_out) {
+        float l = 0.0f;
+        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(rc, cudaStreamSynchronize(s));
+        *loss_out = l / (3.0f * float(n));
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, float* loss_out, void* stream) {
+    if (!rc) return AE_RT_INVALID_ARG;
+    if (n == 0 || !DevPtr(samples)) return RcFail(rc, AE_RT_INVALID_ARG, "ae_rc_train_batch takes device samples");
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 1.0f / (3.0f * float(n)), s);
+    if (st != AE_RT_OK) return st;
+    st = AdamStep(rc, s);
+    if (st != AE_RT_OK) return st;
+    if (loss_out) {
+        float l = 0.0f;
+        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(rc, cudaStreamSynchronize(s));
+        *loss_out = l / (3.0f * float(n));
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
+                               uint32_t max_bounces, float* loss_out, void* stream) {
+    if (!rc || !cam) return AE_RT_INVALID_ARG;
+    ae_rt_ctx* ctx = rc->ctx;
+    if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
+    if (n_paths == 0 || steps == 0 || n_paths < steps) return RcFail(rc, AE_RT_INVALID_ARG, "bad training sizes");
+    RC_CUDA(rc, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    RC_CUDA(rc, rc->samples.ensure(size_t(n_paths) * 64));
+    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts, 0, sizeof(uint32_t), s));
+    RcPathParams pp{};
+    pp.tp.tlas = ctx->d_tlas;
+    pp.tp.n_tlas = ctx->n_tlas;
+    pp.tp.instances = ctx->d_instances;
+    pp.tp.n_instances = ctx->n_instances;
+    pp.tp.meshes = ctx->d_mesh_table;
+    pp.tp.n_meshes = ctx->n_mesh_table;
+    pp.tp.max_steps = ctx->scene_steps;
+    pp.sc.instances = ctx->d_instances;
+    pp.sc.inst_model = ctx->d_inst_model;
+    pp.sc.meshes = ctx->d_mesh_table;
+    pp.sc.materials = ctx->d_materials;
+    pp.sc.n_materials = ctx->n_materials;
+    pp.sc.lights = ctx->d_lights;
+    pp.sc.n_lights = ctx->n_lights;
+    CameraParams& c = pp.cam;
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+    pp.n_paths = n_paths;
+    pp.frame = frame;
+    pp.seed = rc->cfg.seed;
+    pp.max_bounces = max_bounces;
+    pp.epsilon = 0.1f;
+    pp.samples = static_cast<float4*>(rc->samples.ptr);
+    pp.n_samples = rc->d_counts;
+    rc_paths_kernel<<<(n_paths + 127) / 128, 128, 0, s>>>(pp);
+    RC_CUDA(rc, cudaGetLastError());
+    const uint32_t batch = n_paths / steps;
+    for (uint32_t k = 0; k < steps; k++) {
+        const uint32_t end = k + 1 == steps ? n_paths : (k + 1) * batch;
+        ae_rt_status st = Backprop(rc, static_cast<const float4*>(rc->samples.ptr), end, rc->d_counts, k * batch,
+                                   1.0f / (3.0f * float(batch)), s);
+        if (st != AE_RT_OK) return st;
+        st = AdamStep(rc, s);
+        if (st != AE_RT_OK) return st;
+    }
+    if (loss_out) {
+        float l = 0.0f;
+        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(rc, cudaStreamSynchronize(s));
+        *loss_out = l / (3.0f * float(batch));
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
+                          void* stream) {
+    if (!rc || !cam || !accum) return AE_RT_INVALID_ARG;
+    ae_rt_ctx* ctx = rc->ctx;
+    if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
+    if (!DevPtr(accum)) return RcFail(rc, AE_RT_INVALID_ARG, "accumulation buffer must be device memory");
+    RC_CUDA(rc, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t n = cam->width * cam->height;
+    for (int k = 0; k < 2; k++) {
+        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
+        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
+    }
+    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
+    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
+    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
+    RC_CUDA(rc, ctx->pt_occ.ensure(n));
+    RC_CUDA(rc, rc->queries.ensure(size_t(n) * 64));
+    if (!ctx->d_pt_counts) RC_CUDA(rc, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+
+    CameraParams c{};
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+    RcShadeParams rp{};
+    PtParams& p = rp.pt;
+    p.sc.instances = ctx->d_instances;
+    p.sc.inst_model = ctx->d_inst_model;
+    p.sc.meshes = ctx->d_mesh_table;
+    p.sc.materials = ctx->d_materials;
+    p.sc.n_materials = ctx->n_materials;
+    p.sc.lights = ctx->d_lights;
+    p.sc.n_lights = ctx->n_lights;
+    p.width = cam->width;
+    p.height = cam->height;
+    p.max_bounces = last_bounce;
+    p.epsilon = 0.1f;
+    p.seed = rc->cfg.seed + 17u;
+    p.sample = frame;
+    p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
+    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
+    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
+    p.n_shadow = ctx->d_pt_counts + 2;
+    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
+    p.accum = reinterpret_cast<float4*>(accum);
+    rp.queries = static_cast<float4*>(rc->queries.ptr);
+    rp.n_queries = rc->d_counts + 1;
+    rp.last_bounce = last_bounce;
+    const uint32_t blocks = (n + 255) / 256;
+    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts + 1, 0, sizeof(uint32_t), s));
+    p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
+    p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
+    p.n_out = ctx->d_pt_counts + 0;
+    pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
+    RC_CUDA(rc, cudaGetLastError());
+    for (uint32_t b = 0; b <= last_bounce; b++) {
+        const int in = int(b & 1), out = 1 - in;
+        p.bounce = b;
+        p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
+        p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
+        p.n_in = ctx->d_pt_counts + in;
+        p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
+        p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
+        p.n_out = ctx->d_pt_counts + out;
+        ae_rt_status st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n, 0.0f,
+                                          1e12f, ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
+        if (st != AE_RT_OK) return st;
+        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
+        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
+        rc_shade_kernel<<<blocks, 256, 0, s>>>(rp);
+        RC_CUDA(rc, cudaGetLastError());
+        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, 1e12f,
+                             ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
+        if (st != AE_RT_OK) return st;
+        pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
+        RC_CUDA(rc, cudaGetLastError());
+    }
+    RcMlpParams mp = MlpParams(rc);
+    mp.recs = static_cast<const float4*>(rc->queries.ptr);
+    mp.n = n;
+    mp.n_dev = rc->d_counts + 1;
+    mp.accum = reinterpret_cast<float4*>(accum);
+    rc_mlp_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RC_THREADS, kInferSmem, s>>>(mp);
+    RC_CUDA(rc, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+}  // extern "C"

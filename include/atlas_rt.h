@@ -460,6 +460,76 @@ typedef struct ae_pt_params {
 ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
                              double* accum64, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Learned radiance cache (no counterpart in the reference engine)           */
+/* ------------------------------------------------------------------------ */
+
+/* A neural radiance cache bound to a context's scene: a 16-level hash grid
+ * (2 FP16 features per entry, 2^log2_table entries per level, resolutions
+ * from base_resolution to max_resolution in a geometric progression) over
+ * the world box aabb_min..aabb_max, 16 spherical-harmonic coefficients of
+ * the outgoing direction, the normal and the roughness feed a 5 x 64 ReLU
+ * MLP (BF16 weights, FP32 accumulation) that predicts the radiance leaving a
+ * surface point.  Trained online with Adam on a relative L2 loss. */
+typedef struct ae_rc ae_rc;
+
+typedef struct ae_rc_config {
+    uint32_t log2_table;        /* 19 */
+    uint32_t base_resolution;   /* 16 */
+    uint32_t max_resolution;    /* 2048 */
+    float learning_rate;        /* 1e-2 */
+    float beta1;                /* 0.9 */
+    float beta2;                /* 0.99 */
+    float epsilon;              /* 1e-15 */
+    uint32_t seed;
+    float aabb_min[3];
+    float aabb_max[3];
+    uint32_t reserved[4];
+} ae_rc_config;
+
+ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out);
+void ae_rc_destroy(ae_rc* rc);
+
+/* Parameter counts: MLP weights (21,504: 5 matrices of 64 x 64 and a 16 x 64
+ * output matrix of which 3 rows are used, rows = output neurons) and grid
+ * features (16 x 2^log2_table x 2). */
+ae_rt_status ae_rc_param_counts(const ae_rc* rc, uint32_t* n_mlp, uint64_t* n_grid);
+
+/* FP32 master parameters to / from host memory (checkpoint and resume; a
+ * set also resets the optimizer state). */
+ae_rt_status ae_rc_get_params(ae_rc* rc, float* mlp, float* grid);
+ae_rt_status ae_rc_set_params(ae_rc* rc, const float* mlp, const float* grid);
+
+/* Query / training records, 16 floats each: position xyz, roughness;
+ * outgoing direction xyz (unit, towards the viewer), pixel index bits;
+ * normal xyz, 0; target (training) or path throughput (rendering) rgb, 1. */
+
+/* Predictions for n query records (device buffers; out: 4 floats each). */
+ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* out, void* stream);
+
+/* Loss gradients of n training records without an optimizer step (device
+ * records; grad_mlp / grad_grid may be host or device memory or NULL). */
+ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float* grad_mlp, float* grad_grid,
+                             float* loss_out, void* stream);
+
+/* One Adam step on n training records (device). */
+ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, float* loss_out, void* stream);
+
+/* One frame of online training: n_paths self-generated paths from random
+ * pixels of `cam`, each traced with the path tracer's estimator up to
+ * max_bounces further bounces; their first-hit radiance trains the cache in
+ * `steps` Adam steps.  loss_out (optional) synchronises. */
+ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
+                               uint32_t max_bounces, float* loss_out, void* stream);
+
+/* One sample per pixel with paths terminated into the cache: the first hit's
+ * emission, then at the first diffuse vertex (or at bounce last_bounce) the
+ * cache's prediction times the path throughput; metallic vertices before it
+ * take next-event estimation and continue.  Adds into accum (float4 per
+ * pixel, device). */
+ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
+                          void* stream);
+
 /* Waits for `stream` and reports device-side errors of the context's
  * preceding asynchronous calls (stack overflow, step cap, timeouts). */
 ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
