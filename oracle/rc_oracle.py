@@ -99,33 +99,40 @@ class Cache:
         X[:, 51] = rec[:, 3]
         return X
 
-    def forward(self, mlp, table, rec):
+    def forward(self, mlp, table, rec, bf16=False):
+        """bf16=True rounds the input and every activation to BF16, as the
+        kernel stores them."""
+        q = bf16_round if bf16 else (lambda x: x)
         Ws = [mlp[l * W * W:(l + 1) * W * W].reshape(W, W) for l in range(HIDDEN)]
         Wo = mlp[HIDDEN * W * W:].reshape(OUT, W)
-        A = [self.encode(table, rec)]
+        A = [q(self.encode(table, rec))]
         for Wl in Ws:
-            A.append(np.maximum(A[-1] @ Wl.T, 0.0))
+            A.append(q(np.maximum(A[-1] @ Wl.T, 0.0)))
         P = A[-1] @ Wo.T
         return A, P
 
-    def loss_and_grads(self, mlp, table, rec):
+    def loss_and_grads(self, mlp, table, rec, bf16=False):
+        """bf16=True also rounds the backward deltas to BF16 (the kernel keeps
+        them in BF16 shared-memory tiles)."""
+        q = bf16_round if bf16 else (lambda x: x)
         n = len(rec)
         Ws = [mlp[l * W * W:(l + 1) * W * W].reshape(W, W) for l in range(HIDDEN)]
         Wo = mlp[HIDDEN * W * W:].reshape(OUT, W)
-        A, P = self.forward(mlp, table, rec)
+        A, P = self.forward(mlp, table, rec, bf16)
         t = rec[:, 12:15].astype(np.float64)
         p = P[:, :3]
         den = p * p + 0.01
         loss = np.sum((p - t) ** 2 / den) / (3 * n)
         dP = np.zeros_like(P)
         dP[:, :3] = 2.0 * (p - t) / den / (3 * n)
+        dP = q(dP)
         gW = [None] * (HIDDEN + 1)
         gW[HIDDEN] = dP.T @ A[HIDDEN]
-        dA = dP @ Wo
+        dA = q(dP @ Wo)
         for l in range(HIDDEN - 1, -1, -1):
             dZ = dA * (A[l + 1] > 0)
             gW[l] = dZ.T @ A[l]
-            dA = dZ @ Ws[l]
+            dA = q(dZ @ Ws[l])
         gmlp = np.concatenate([g.reshape(-1) for g in gW])
         ggrid = np.zeros((LEVELS, self.T, 2))
         pos = rec[:, 0:3]

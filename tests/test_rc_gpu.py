@@ -3,9 +3,13 @@ and backward against the FP64 oracle (oracle/rc_oracle.py), training
 behaviour, and what the trained cache gains over the path tracer without it.
 
 Tolerances: the kernels round the network input, every activation and the
-backward deltas to BF16 (8-bit mantissa) and read FP16 table values, so
-predictions are compared at 3 % and gradient vectors at 6 % relative L2
-error, with a cosine similarity above 0.998.
+backward deltas to BF16 (8-bit mantissa) and read FP16 table values; the
+oracle applies the same roundings (emulate_params, bf16=True) and computes
+everything else in FP64, so the remaining differences are FP32 accumulation
+order and values that land on the other side of a BF16 rounding boundary:
+predictions are compared at 1 % and gradient vectors at 3 % relative L2
+error with cosine similarity above 0.999.  Against the unrounded FP64
+network the errors stay below 3 % (forward) and 10 % (gradients).
 """
 import numpy as np
 import pytest
@@ -72,8 +76,10 @@ def test_forward_matches_fp64_oracle(cache):
     got = out.cpu().numpy()[:, :3]
     orc = rc_oracle.Cache(2 ** 14, LO, HI)
     m64, g64 = rc_oracle.emulate_params(mlp, grid)
-    _, P = orc.forward(m64, g64.reshape(16, -1, 2), rec)
-    assert rel(got, P[:, :3]) < 0.03, rel(got, P[:, :3])
+    _, P = orc.forward(m64, g64.reshape(16, -1, 2), rec, bf16=True)
+    assert rel(got, P[:, :3]) < 0.01, rel(got, P[:, :3])
+    _, P64 = orc.forward(m64, g64.reshape(16, -1, 2), rec)
+    assert rel(got, P64[:, :3]) < 0.03, rel(got, P64[:, :3])
 
 
 def test_gradients_match_fp64_oracle(cache):
@@ -88,15 +94,17 @@ def test_gradients_match_fp64_oracle(cache):
     loss = rc.gradients(q, gm, gg)
     orc = rc_oracle.Cache(2 ** 14, LO, HI)
     m64, g64 = rc_oracle.emulate_params(mlp, grid)
-    l_ref, gm_ref, gg_ref, _ = orc.loss_and_grads(m64, g64.reshape(16, -1, 2), rec)
-    assert abs(loss - l_ref) / l_ref < 0.03, (loss, l_ref)
-    assert rel(gm, gm_ref) < 0.06 and cosine(gm, gm_ref) > 0.998, (rel(gm, gm_ref), cosine(gm, gm_ref))
-    assert rel(gg, gg_ref) < 0.06 and cosine(gg, gg_ref) > 0.998, (rel(gg, gg_ref), cosine(gg, gg_ref))
+    l_ref, gm_ref, gg_ref, _ = orc.loss_and_grads(m64, g64.reshape(16, -1, 2), rec, bf16=True)
+    assert abs(loss - l_ref) / l_ref < 0.01, (loss, l_ref)
+    assert rel(gm, gm_ref) < 0.03 and cosine(gm, gm_ref) > 0.999, (rel(gm, gm_ref), cosine(gm, gm_ref))
+    assert rel(gg, gg_ref) < 0.03 and cosine(gg, gg_ref) > 0.999, (rel(gg, gg_ref), cosine(gg, gg_ref))
+    _, gm64, gg64, _ = orc.loss_and_grads(m64, g64.reshape(16, -1, 2), rec)
+    assert rel(gm, gm64) < 0.10 and rel(gg, gg64) < 0.10, (rel(gm, gm64), rel(gg, gg64))
     # per-layer check of the weight gradients
     for l in range(6):
         a = l * 4096
         b = a + (4096 if l < 5 else 16 * 64)
-        assert cosine(gm[a:b], gm_ref[a:b]) > 0.995, l
+        assert cosine(gm[a:b], gm_ref[a:b]) > 0.998, l
 
 
 def test_training_fits_a_smooth_field(cache):
