@@ -319,9 +319,10 @@ class Context:
                self._h)
 
     def pathtrace(self, cam: "Camera", accum, accum64=None, spp=1, max_bounces=3, sample_offset=0, seed=1,
-                  epsilon=0.1, stream=None):
+                  epsilon=0.1, mis=False, stream=None):
         p = PtParams()
         p.spp, p.max_bounces, p.sample_offset, p.seed, p.epsilon = spp, max_bounces, sample_offset, seed, epsilon
+        p.flags = 1 if mis else 0
         _check(lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
                                      _stream_handle(stream)), self._h)
 
@@ -365,8 +366,11 @@ class RadianceCache:
     """ae_rc: the learned radiance cache bound to a context's scene."""
 
     def __init__(self, ctx: Context, aabb_min, aabb_max, log2_table=19, base_resolution=16, max_resolution=2048,
-                 learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, seed=1):
+                 learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, seed=1, radiance_scale=1.0,
+                 rough_cut=0.35):
         cfg = RcConfig()
+        cfg.radiance_scale = float(radiance_scale)
+        cfg.rough_cut = float(rough_cut)
         cfg.log2_table, cfg.base_resolution, cfg.max_resolution = log2_table, base_resolution, max_resolution
         cfg.learning_rate, cfg.beta1, cfg.beta2, cfg.epsilon, cfg.seed = learning_rate, beta1, beta2, epsilon, seed
         for i in range(3):

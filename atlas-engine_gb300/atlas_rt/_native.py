@@ -55,13 +55,14 @@ class CastOutputs(C.Structure):
 
 class PtParams(C.Structure):
     _fields_ = [("spp", U32), ("max_bounces", U32), ("sample_offset", U32), ("seed", U32),
-                ("epsilon", F32), ("reserved", U32 * 3)]
+                ("epsilon", F32), ("flags", U32), ("reserved", U32 * 2)]
 
 
 class RcConfig(C.Structure):
     _fields_ = [("log2_table", U32), ("base_resolution", U32), ("max_resolution", U32),
                 ("learning_rate", F32), ("beta1", F32), ("beta2", F32), ("epsilon", F32), ("seed", U32),
-                ("aabb_min", F32 * 3), ("aabb_max", F32 * 3), ("reserved", U32 * 4)]
+                ("aabb_min", F32 * 3), ("aabb_max", F32 * 3), ("radiance_scale", F32), ("rough_cut", F32),
+                ("reserved", U32 * 2)]
 
 
 # (name, restype, argtypes)

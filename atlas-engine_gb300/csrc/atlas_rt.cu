@@ -770,6 +770,7 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
     p.max_bounces = params->max_bounces;
     p.epsilon = params->epsilon;
     p.seed = params->seed;
+    p.mis = (params->flags & AE_PT_MIS) ? 1u : 0u;
     p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
     p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
     p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);

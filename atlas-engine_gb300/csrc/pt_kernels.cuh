@@ -56,6 +56,7 @@ struct PtParams {
     uint32_t max_bounces;
     float epsilon;
     uint32_t seed;
+    uint32_t mis;                 // 1: next-event estimation combined with BRDF sampling (power heuristic)
     // queues
     const float4* rays_in;        // PackedRay
     const float4* hits_in;        // ae_hit
@@ -349,28 +350,33 @@ __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, fl
     return sf;
 }
 
+// Selection weight of a light seen from P (raytracer/direct.hsh:12-49).
+__device__ __forceinline__ float light_weight(const Light& L, V3 P) {
+    float w = 1.0f;
+    if (L.type == 1u) {
+        const V3 toL = L.P - P;
+        const float d2 = dot(toL, toL);
+        const float NdotL = fmaxf(dot(L.N, normalize(toL) * -1.0f), 0.0f);
+        w = L.brightness * L.area * NdotL / d2;
+    } else {
+        w = L.brightness;
+    }
+    return fminf(fmaxf(w, 0.0000001f), 1.0f);
+}
+
 // EvaluateDirectLight (rayHit.csh:209-235) up to the visibility test: picks a
 // light, samples it, evaluates the BRDF.  Returns false when nothing needs a
 // shadow ray; otherwise the contribution (already scaled by the path
 // throughput) and the shadow ray (origin, direction, tmax).
 __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr, uint32_t pix, uint32_t sample,
                                              uint32_t bounce, uint32_t seed, float eps, V3& contrib, V3& so,
-                                             V3& sd, float& stmax) {
+                                             V3& sd, float& stmax, float* pdf_sa = nullptr) {
     if (sc.n_lights == 0) return false;
     Light sel{};
     float selW = 0.0f, total = 0.0f;
     for (uint32_t li = 0; li < sc.n_lights; li++) {
         const Light L = load_light(sc.lights + size_t(li) * 4);
-        float w = 1.0f;
-        if (L.type == 1u) {
-            const V3 toL = L.P - sf.P;
-            const float d2 = dot(toL, toL);
-            const float NdotL = fmaxf(dot(L.N, normalize(toL) * -1.0f), 0.0f);
-            w = L.brightness * L.area * NdotL / d2;
-        } else {
-            w = L.brightness;
-        }
-        w = fminf(fmaxf(w, 0.0000001f), 1.0f);
+        const float w = light_weight(L, sf.P);
         total += w;
         if (rng(pix, sample, bounce, 16u + li, seed) < w / total) {
             selW = w;
@@ -399,6 +405,7 @@ __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr
     }
     const V3 refl = (eval_diffuse(sf) + eval_specular(sf)) * sf.mat.opacity;
     contrib = thr * sf.mat.opacity * (refl * sel.radiance) * (solidAngle * sf.NdotL / lightPdf);
+    if (pdf_sa) *pdf_sa = sel.type == 1u ? (solidAngle > 0.0f ? lightPdf / solidAngle : 0.0f) : 0.0f;
     if (!(sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f)) return false;
     so = sf.P + sf.N * eps;         // CheckVisibility, rayHit.csh:327-338
     sd = sf.L;
@@ -410,7 +417,7 @@ __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr
 // throughput update, Russian roulette, termination below the surface.
 // Returns true when the path continues with (o, d) and throughput thr.
 __device__ __forceinline__ bool continue_path(Surf& sf, V3& thr, uint32_t pix, uint32_t sample, uint32_t bounce,
-                                              uint32_t seed, float eps, V3& o, V3& d) {
+                                              uint32_t seed, float eps, V3& o, V3& d, bool* spec_lobe = nullptr) {
     const Mat& mat = sf.mat;
     const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
     const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
@@ -419,6 +426,7 @@ __device__ __forceinline__ bool continue_path(Surf& sf, V3& thr, uint32_t pix, u
     const float u1 = rng(pix, sample, bounce, 6, seed);
     V3 refl;
     float pdf;
+    if (spec_lobe) *spec_lobe = rnd < specChance;
     if (rnd < specChance) {
         pdf = sample_specular(sf, u0, u1, refl);
         refl = refl * mat.opacity;
@@ -441,6 +449,92 @@ __device__ __forceinline__ bool continue_path(Surf& sf, V3& thr, uint32_t pix, u
     return alive;
 }
 
+// ---- combining next-event estimation with BRDF sampling (power heuristic) ----
+// Not part of the engine's estimator: used by the radiance-cache renderer and
+// its training paths, and by the path tracer when PtParams::mis is set.  Both
+// strategies estimate the engine's direct-light integral: the GGX term the
+// engine evaluates for lights carries a 1e-7 in its denominator (ggx_d), which
+// caps it below roughness ~0.2, while the VNDF continuation follows the
+// uncapped lobe; a BRDF-sampled light hit is therefore scaled by
+// D_capped / D_true, and by opacity / ao for the engine's opacity^2 and ao
+// factors, so that the sum stays unbiased with respect to the engine.
+
+__device__ __forceinline__ float ggx_d_true(float NdotH, float a) {
+    const float a2 = a * a;
+    const float f = (NdotH * a2 - NdotH) * NdotH + 1.0f;
+    return a2 / fmaxf(kPi * f * f, 1e-30f);
+}
+
+// Density (per solid angle) of continue_path's direction sampling towards L.
+__device__ __forceinline__ float bsdf_pdf(Surf s, V3 L) {
+    s.L = L;
+    update_surface(s);
+    if (!(s.NdotL > 0.0f)) return 0.0f;
+    const V3 F = fresnel(s.F0, s.F90, s.NdotV);
+    const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+    const float a = s.mat.roughness * s.mat.roughness;
+    const float nv = fmaxf(s.NdotV, 1e-4f);
+    const float ps = vis_separable(nv, a) * ggx_d_true(s.NdotH, a) / (4.0f * nv);
+    const float pd = s.NdotL * kInvPi * (1.0f - s.mat.metalness);
+    return specChance * ps + (1.0f - specChance) * pd;
+}
+
+// Density (per solid angle) with which direct_light at P samples the first
+// emissive triangle along (P, d); 0 when the ray meets none or its back.
+__device__ __forceinline__ float light_pdf_dir(const PtScene& sc, V3 P, V3 d) {
+    float total = 0.0f, best = 1e30f, bw = 0.0f, bpdf = 0.0f, barea = 0.0f, bcos = 0.0f;
+    for (uint32_t li = 0; li < sc.n_lights; li++) {
+        const Light L = load_light(sc.lights + size_t(li) * 4);
+        const float w = light_weight(L, P);
+        total += w;
+        if (L.type != 1u) continue;
+        const Tri lt = load_triangle(sc, L.inst, L.tri);
+        // Moller-Trumbore
+        const V3 e1 = lt.v1 - lt.v0, e2 = lt.v2 - lt.v0;
+        const V3 pv = cross(d, e2);
+        const float det = dot(e1, pv);
+        if (fabsf(det) < 1e-20f) continue;
+        const float inv = 1.0f / det;
+        const V3 tv = P - lt.v0;
+        const float u = dot(tv, pv) * inv;
+        if (u < 0.0f || u > 1.0f) continue;
+        const V3 qv = cross(tv, e1);
+        const float v = dot(d, qv) * inv;
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float t = dot(e2, qv) * inv;
+        if (t <= 0.0f || t >= best) continue;
+        const V3 LN = lt.n0 * (1.0f - u - v) + lt.n1 * u + lt.n2 * v;
+        best = t;
+        bw = w;
+        bpdf = L.pdf;
+        barea = L.area;
+        bcos = fmaxf(dot(LN, d * -1.0f), 0.0f);
+    }
+    if (best >= 1e30f || bcos <= 0.0f || total <= 0.0f) return 0.0f;
+    return bw / total * bpdf * best * best / (bcos * barea);
+}
+
+__device__ __forceinline__ float power_weight(float a, float b) {
+    const float a2 = a * a, b2 = b * b;
+    return a2 + b2 > 0.0f ? a2 / (a2 + b2) : 0.0f;
+}
+
+// Multiplier of the emission found by the continuation (sf after
+// continue_path: sf.L is the sampled direction, sf.H its half vector).
+__device__ __forceinline__ float mis_hit_factor(const PtScene& sc, const Surf& sf, V3 d, bool spec_lobe) {
+    const float pl = light_pdf_dir(sc, sf.P, d);
+    if (pl <= 0.0f) return 0.0f;
+    float m = power_weight(bsdf_pdf(sf, d), pl);
+    if (spec_lobe) {
+        // the engine's capped D over the sampled (true) D
+        const float a = sf.mat.roughness * sf.mat.roughness;
+        const float a2 = a * a;
+        const float f = (sf.NdotH * a2 - sf.NdotH) * sf.NdotH + 1.0f;
+        m *= f * f / (f * f + 0.0000001f);
+    }
+    return sf.mat.ao > 0.0f ? m * sf.mat.opacity / sf.mat.ao : 0.0f;
+}
+
 // rayHit.csh:55-325 for one bounce of the wavefront.
 static __global__ void pt_shade_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -458,23 +552,28 @@ static __global__ void pt_shade_kernel(PtParams p) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
             const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
             Surf sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
-            // emission of the first hit (rayHit.csh:180-183)
-            if (p.bounce == 0 && sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f)
-                add_radiance(p, pix, sf.mat.emissive);
+            // emission of the first hit (rayHit.csh:180-183); with MIS, also
+            // the emission a continuation finds, weighted by its factor (ray dir.w)
+            const bool emissive = sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f;
+            if (p.bounce == 0 && emissive) add_radiance(p, pix, sf.mat.emissive);
+            if (p.bounce > 0 && emissive && d4.w > 0.0f) add_radiance(p, pix, thr * sf.mat.emissive * d4.w);
+            const bool cont = p.bounce < p.max_bounces;
             V3 c, so, sd;
-            float st;
-            if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st)) {
+            float st, pl = 0.0f;
+            if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st, &pl)) {
+                if (p.mis && cont) c = c * power_weight(pl, bsdf_pdf(sf, sf.L));
                 emitShadow = true;
                 shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
                 shRay1 = make_float4(sd.x, sd.y, sd.z, st);
                 shPay = make_float4(c.x, c.y, c.z, __uint_as_float(pix));
             }
-            if (p.bounce < p.max_bounces) {
+            if (cont) {
                 V3 o, d;
-                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d)) {
+                bool spec = false;
+                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec)) {
                     emitRay = true;
                     outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
-                    outRay1 = make_float4(d.x, d.y, d.z, 0.0f);
+                    outRay1 = make_float4(d.x, d.y, d.z, p.mis ? mis_hit_factor(p.sc, sf, d, spec) : 0.0f);
                     outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
                 }
             }

@@ -34,6 +34,8 @@ struct ae_rc {
     Scratch samples, queries;
     uint64_t step = 0;
     int sm_count = 0;
+    float scale = 1.0f;            // radiance scale of the stored values
+    uint32_t max_bounces = 3;      // bounce budget of the most recent training frame
 };
 
 namespace {
@@ -66,8 +68,8 @@ uint32_t GridBlocks(ae_rc* rc, uint32_t n) {
 
 // Gradients of the relative L2 loss over n training records (device) into
 // mlp_grad / grid_grad (zeroed first); loss sum into d_loss.
-ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t* n_dev, uint32_t offset,
-                      float inv_norm, cudaStream_t s) {
+ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t* n_dev, uint32_t slice,
+                      uint32_t slices, cudaStream_t s) {
     RC_CUDA(rc, cudaMemsetAsync(rc->mlp_grad, 0, RC_NPARAM * sizeof(float), s));
     RC_CUDA(rc, cudaMemsetAsync(rc->grid_grad, 0, rc->grid_params * sizeof(float), s));
     RC_CUDA(rc, cudaMemsetAsync(rc->d_loss, 0, sizeof(float), s));
@@ -75,9 +77,9 @@ ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t*
     p.recs = recs;
     p.n = n;
     p.n_dev = n_dev;
-    p.offset = offset;
-    p.inv_norm = inv_norm;
-    const uint32_t count = n > offset ? n - offset : 0;
+    p.slice = slice;
+    p.slices = slices;
+    const uint32_t count = slices ? (n + slices - 1) / slices : n;
     rc_mlp_kernel<RC_TRAIN><<<GridBlocks(rc, count), RC_THREADS, kTrainSmem, s>>>(p);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
@@ -95,10 +97,11 @@ ae_rt_status AdamStep(ae_rc* rc, cudaStream_t s) {
     a.step_scale = scale;
     a.master = rc->mlp_master; a.m = rc->mlp_m; a.v = rc->mlp_v; a.grad = rc->mlp_grad;
     a.out_bf16 = rc->mlp_bf16; a.out_f16 = nullptr; a.n = RC_NPARAM;
-    rc_adam_kernel<<<(RC_NPARAM + 255) / 256, 256, 0, s>>>(a);
+    rc_adam_kernel<<<(RC_NPARAM / 4 + 255) / 256, 256, 0, s>>>(a);
     RC_CUDA(rc, cudaGetLastError());
     a.master = rc->grid_master; a.m = rc->grid_m; a.v = rc->grid_v; a.grad = rc->grid_grad;
     a.out_bf16 = nullptr; a.out_f16 = rc->grid_f16; a.n = rc->grid_params;
+    a.skip_zero = 1;
     rc_adam_kernel<<<uint32_t(rc->sm_count) * 8u, 256, 0, s>>>(a);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
@@ -145,6 +148,8 @@ ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out) 
     if (cfg->log2_table < 10 || cfg->log2_table > 24 || cfg->base_resolution < 2 ||
         cfg->max_resolution < cfg->base_resolution || cfg->max_resolution > (1u << 20))
         return Fail(ctx, AE_RT_INVALID_ARG, "radiance cache: encoding parameters out of range");
+    if (!(cfg->radiance_scale >= 0.0f) || !std::isfinite(cfg->radiance_scale))
+        return Fail(ctx, AE_RT_INVALID_ARG, "radiance cache: bad radiance scale");
     for (int a = 0; a < 3; a++)
         if (!(cfg->aabb_max[a] > cfg->aabb_min[a])) return Fail(ctx, AE_RT_INVALID_ARG, "radiance cache: empty domain");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -153,6 +158,7 @@ ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out) 
     rc->ctx = ctx;
     rc->cfg = *cfg;
     rc->sm_count = ctx->sm_count;
+    rc->scale = cfg->radiance_scale > 0.0f ? cfg->radiance_scale : 1.0f;
     RcGrid& g = rc->grid;
     g.T = 1u << cfg->log2_table;
     g.lox = cfg->aabb_min[0]; g.loy = cfg->aabb_min[1]; g.loz = cfg->aabb_min[2];
@@ -265,7 +271,7 @@ ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float*
     if (n == 0 || !DevPtr(samples)) return RcFail(rc, AE_RT_INVALID_ARG, "ae_rc_gradients takes device samples");
     RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 1.0f / (3.0f * float(n)), s);
+    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 0, s);
     if (st != AE_RT_OK) return st;
     if (grad_mlp) RC_CUDA(rc, cudaMemcpyAsync(grad_mlp, rc->mlp_grad, RC_NPARAM * sizeof(float), cudaMemcpyDefault, s));
     if (grad_grid)
@@ -274,7 +280,7 @@ ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float*
         float l = 0.0f;
         RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
         RC_CUDA(rc, cudaStreamSynchronize(s));
-        *loss_out = l / (3.0f * float(n));
+        *loss_out = l;
     }
     return AE_RT_OK;
 }
@@ -284,7 +290,7 @@ ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, floa
     if (n == 0 || !DevPtr(samples)) return RcFail(rc, AE_RT_INVALID_ARG, "ae_rc_train_batch takes device samples");
     RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 1.0f / (3.0f * float(n)), s);
+    ae_rt_status st = Backprop(rc, reinterpret_cast<const float4*>(samples), n, nullptr, 0, 0, s);
     if (st != AE_RT_OK) return st;
     st = AdamStep(rc, s);
     if (st != AE_RT_OK) return st;
@@ -292,7 +298,7 @@ ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, floa
         float l = 0.0f;
         RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
         RC_CUDA(rc, cudaStreamSynchronize(s));
-        *loss_out = l / (3.0f * float(n));
+        *loss_out = l;
     }
     return AE_RT_OK;
 }
@@ -305,7 +311,8 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
     if (n_paths == 0 || steps == 0 || n_paths < steps) return RcFail(rc, AE_RT_INVALID_ARG, "bad training sizes");
     RC_CUDA(rc, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    RC_CUDA(rc, rc->samples.ensure(size_t(n_paths) * 64));
+    if (max_bounces == 0 || max_bounces > 16) return RcFail(rc, AE_RT_INVALID_ARG, "max_bounces out of range");
+    RC_CUDA(rc, rc->samples.ensure(size_t(n_paths) * RC_MAX_DEPTH * 64));
     RC_CUDA(rc, cudaMemsetAsync(rc->d_counts, 0, sizeof(uint32_t), s));
     RcPathParams pp{};
     pp.tp.tlas = ctx->d_tlas;
@@ -333,15 +340,17 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
     pp.seed = rc->cfg.seed;
     pp.max_bounces = max_bounces;
     pp.epsilon = 0.1f;
+    pp.scale = rc->scale;
     pp.samples = static_cast<float4*>(rc->samples.ptr);
     pp.n_samples = rc->d_counts;
     rc_paths_kernel<<<(n_paths + 127) / 128, 128, 0, s>>>(pp);
     RC_CUDA(rc, cudaGetLastError());
-    const uint32_t batch = n_paths / steps;
+    rc->max_bounces = max_bounces;
+    // the records (up to RC_MAX_DEPTH per path; count on the device) in
+    // `steps` equal slices, one Adam step each
     for (uint32_t k = 0; k < steps; k++) {
-        const uint32_t end = k + 1 == steps ? n_paths : (k + 1) * batch;
-        ae_rt_status st = Backprop(rc, static_cast<const float4*>(rc->samples.ptr), end, rc->d_counts, k * batch,
-                                   1.0f / (3.0f * float(batch)), s);
+        ae_rt_status st = Backprop(rc, static_cast<const float4*>(rc->samples.ptr), n_paths * RC_MAX_DEPTH,
+                                   rc->d_counts, k, steps, s);
         if (st != AE_RT_OK) return st;
         st = AdamStep(rc, s);
         if (st != AE_RT_OK) return st;
@@ -350,7 +359,7 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
         float l = 0.0f;
         RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
         RC_CUDA(rc, cudaStreamSynchronize(s));
-        *loss_out = l / (3.0f * float(batch));
+        *loss_out = l;
     }
     return AE_RT_OK;
 }
@@ -392,7 +401,7 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
     p.sc.n_lights = ctx->n_lights;
     p.width = cam->width;
     p.height = cam->height;
-    p.max_bounces = last_bounce;
+    p.max_bounces = rc->max_bounces;
     p.epsilon = 0.1f;
     p.seed = rc->cfg.seed + 17u;
     p.sample = frame;
@@ -405,6 +414,8 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
     rp.queries = static_cast<float4*>(rc->queries.ptr);
     rp.n_queries = rc->d_counts + 1;
     rp.last_bounce = last_bounce;
+    rp.inv_scale = 1.0f / rc->scale;
+    rp.rough_cut = rc->cfg.rough_cut > 0.0f ? rc->cfg.rough_cut : 0.35f;
     const uint32_t blocks = (n + 255) / 256;
     RC_CUDA(rc, cudaMemsetAsync(rc->d_counts + 1, 0, sizeof(uint32_t), s));
     p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
@@ -412,7 +423,8 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
     p.n_out = ctx->d_pt_counts + 0;
     pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
     RC_CUDA(rc, cudaGetLastError());
-    for (uint32_t b = 0; b <= last_bounce; b++) {
+    const uint32_t final_bounce = last_bounce < rc->max_bounces ? last_bounce : rc->max_bounces;
+    for (uint32_t b = 0; b <= final_bounce; b++) {
         const int in = int(b & 1), out = 1 - in;
         p.bounce = b;
         p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);

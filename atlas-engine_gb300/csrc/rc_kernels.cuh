@@ -8,7 +8,17 @@
 //
 // Network input (64 BF16 per query): 16 levels x 2 features of the hash grid
 // (trilinear), 16 real spherical-harmonic coefficients of degree < 4 of the
-// outgoing direction, the shading normal, the roughness, zero padding.
+// outgoing direction, the shading normal, the roughness, the vertex depth
+// (bounces from the camera, which fixes how many bounces of indirect light
+// the path tracer's budget leaves), zero padding.
+//
+// What the cache stores: the INDIRECT radiance leaving a vertex towards the
+// previous one (everything the path tracer adds after the vertex's own
+// next-event estimate, within the bounce budget), divided by the vertex's
+// base colour and multiplied by a fixed radiance scale.  Direct light stays
+// with next-event estimation at render time, so the cache's error only
+// touches the smooth indirect part, and its output is modulated back by the
+// base colour.
 // MLP: 5 hidden layers of 64 with ReLU, no biases, linear RGB output (padded
 // to 16 columns), BF16 weights, FP32 accumulation (mma.sync m16n8k16).
 // One CTA of 4 warps handles tiles of 128 queries; each warp owns 32 rows of
@@ -41,7 +51,7 @@ constexpr size_t RC_WBYTES = size_t(RC_WROWS) * RC_STRIDE * 2;
 constexpr size_t RC_ABYTES = size_t(RC_TILE) * RC_STRIDE * 2;
 
 // Query / training-sample record, 4 float4: (pos, roughness), (outgoing dir,
-// pixel bits), (normal, -), (throughput or target rgb, valid).
+// pixel bits), (normal, depth), (render weight or training target rgb, 1).
 struct RcGrid {
     const __half2* table;      // [levels][T]
     float2* grad;              // [levels][T] (training)
@@ -116,7 +126,8 @@ __device__ __forceinline__ void rc_encode(const RcGrid& g, const float4& q0, con
     for (int k = 0; k < 8; k++) v[16 + k] = __floats2bfloat162_rn(sh[2 * k], sh[2 * k + 1]);
     v[24] = __floats2bfloat162_rn(q2.x, q2.y);
     v[25] = __floats2bfloat162_rn(q2.z, q0.w);
-    for (int k = 26; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
+    v[26] = __floats2bfloat162_rn(q2.w, 0.0f);
+    for (int k = 27; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
     uint4* dst = reinterpret_cast<uint4*>(row);
     const uint4* src = reinterpret_cast<const uint4*>(v);
 #pragma unroll
@@ -276,10 +287,10 @@ struct RcMlpParams {
     const uint32_t* n_dev;           // optional device count
     uint32_t n;                      // count, or capacity with n_dev
     uint32_t offset;                 // first record (training steps over one buffer)
+    uint32_t slice, slices;          // slices > 0: train on slice `slice` of the device count
     float4* accum;                   // RC_INFER: image
     float4* out;                     // RC_PREDICT
-    float* loss;                     // RC_TRAIN: sum of per-element losses
-    float inv_norm;                  // RC_TRAIN: 1 / (samples x 3)
+    float* loss;                     // RC_TRAIN: mean per-element loss (accumulated)
 };
 
 template <int MODE>
@@ -300,7 +311,12 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
     __syncthreads();
 
     const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
-    const uint32_t count = n > p.offset ? n - p.offset : 0u;
+    uint32_t first = p.offset, count = n > p.offset ? n - p.offset : 0u;
+    if (p.slices) {
+        first = uint32_t(uint64_t(n) * p.slice / p.slices);
+        count = uint32_t(uint64_t(n) * (p.slice + 1) / p.slices) - first;
+    }
+    const float inv_norm = count ? 1.0f / (3.0f * float(count)) : 0.0f;
     const uint32_t tiles = (count + RC_TILE - 1) / RC_TILE;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t row0 = warp * 32u;
@@ -308,7 +324,7 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
         const bool valid = gi < count;
         float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
         if (valid) {
-            const float4* rec = p.recs + size_t(p.offset + gi) * 4;
+            const float4* rec = p.recs + size_t(first + gi) * 4;
             q0 = rec[0]; q1 = rec[1]; q2 = rec[2]; q3 = rec[3];
         }
         __nv_bfloat16* x0 = act + size_t(row0) * RC_STRIDE;
@@ -353,7 +369,7 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
                     const uint32_t pix = __float_as_uint(__shfl_sync(0xffffffffu, q1.w, rowInWarp));
                     if (cq == 0 && gj < count) {
                         if (MODE == RC_PREDICT) {
-                            p.out[p.offset + gj] = make_float4(c0, c1, c2, 0.0f);
+                            p.out[first + gj] = make_float4(c0, c1, c2, 0.0f);
                         } else {
                             float4* a = p.accum + pix;
                             a->x += r3.x * fmaxf(c0, 0.0f);
@@ -388,7 +404,7 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
                             const float den = pr * pr + 0.01f;
                             const float diff = pr - tg;
                             lsum += diff * diff / den;
-                            dd = 2.0f * diff / den * p.inv_norm;
+                            dd = 2.0f * diff / den * inv_norm;
                         }
                         if (e == 0) d0 = dd; else d1 = dd;
                     }
@@ -397,7 +413,7 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
                     *reinterpret_cast<uint32_t*>(drow + 8 + cq * 2) = 0u;
                 }
             for (int off = 16; off > 0; off >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, off);
-            if (lane == 0) atomicAdd(p.loss, lsum);
+            if (lane == 0) atomicAdd(p.loss, lsum * inv_norm);
         }
         __syncthreads();
         // ---- output layer: dA5 = dP * W5, dW5 += dP^T * A5 ----
@@ -461,8 +477,11 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
     }
 }
 
-// Adam over [0, n): FP32 master, moments; also writes the low-precision copy
-// (BF16 for the MLP, FP16 for the grid).
+// Adam over [0, n) (n a multiple of 4; 16-byte aligned arrays): FP32 master,
+// moments; also writes the low-precision copy (BF16 for the MLP, FP16 for the
+// grid).  skip_zero: entries whose gradient is exactly zero (hash-grid
+// entries no record touched) keep their parameter and moments -- the sparse
+// update usual for hash encodings; it also saves most of the pass's writes.
 struct RcAdamParams {
     float* master;
     float* m;
@@ -472,21 +491,45 @@ struct RcAdamParams {
     __half* out_f16;
     size_t n;
     float lr, beta1, beta2, eps;
-    float step_scale;     // lr * sqrt(1 - beta2^t) / (1 - beta1^t) / lr
+    float step_scale;     // sqrt(1 - beta2^t) / (1 - beta1^t)
+    uint32_t skip_zero;
 };
+
+__device__ __forceinline__ void adam1(const RcAdamParams& a, float gr, float& w, float& m, float& v) {
+    m = a.beta1 * m + (1.0f - a.beta1) * gr;
+    v = a.beta2 * v + (1.0f - a.beta2) * gr * gr;
+    w = w - a.lr * a.step_scale * m / (sqrtf(v) + a.eps);
+}
 
 static __global__ void rc_adam_kernel(RcAdamParams a) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-        const float gr = a.grad[i];
-        const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * gr;
-        const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * gr * gr;
-        a.m[i] = m;
-        a.v[i] = v;
-        const float w = a.master[i] - a.lr * a.step_scale * m / (sqrtf(v) + a.eps);
-        a.master[i] = w;
-        if (a.out_bf16) a.out_bf16[i] = __float2bfloat16_rn(w);
-        if (a.out_f16) a.out_f16[i] = __float2half_rn(w);
+    const size_t n4 = a.n / 4;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float4 g = reinterpret_cast<const float4*>(a.grad)[i];
+        const bool z[4] = { g.x == 0.0f, g.y == 0.0f, g.z == 0.0f, g.w == 0.0f };
+        if (a.skip_zero && z[0] && z[1] && z[2] && z[3]) continue;
+        float4 w = reinterpret_cast<float4*>(a.master)[i];
+        float4 m = reinterpret_cast<float4*>(a.m)[i];
+        float4 v = reinterpret_cast<float4*>(a.v)[i];
+        const bool upd[4] = { !(a.skip_zero && z[0]), !(a.skip_zero && z[1]), !(a.skip_zero && z[2]),
+                              !(a.skip_zero && z[3]) };
+        if (upd[0]) adam1(a, g.x, w.x, m.x, v.x);
+        if (upd[1]) adam1(a, g.y, w.y, m.y, v.y);
+        if (upd[2]) adam1(a, g.z, w.z, m.z, v.z);
+        if (upd[3]) adam1(a, g.w, w.w, m.w, v.w);
+        reinterpret_cast<float4*>(a.master)[i] = w;
+        reinterpret_cast<float4*>(a.m)[i] = m;
+        reinterpret_cast<float4*>(a.v)[i] = v;
+        if (a.out_bf16) {
+            __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(a.out_bf16) + 2 * i;
+            o[0] = __floats2bfloat162_rn(w.x, w.y);
+            o[1] = __floats2bfloat162_rn(w.z, w.w);
+        }
+        if (a.out_f16) {
+            __half2* o = reinterpret_cast<__half2*>(a.out_f16) + 2 * i;
+            o[0] = __floats2half2_rn(w.x, w.y);
+            o[1] = __floats2half2_rn(w.z, w.w);
+        }
     }
 }
 
@@ -594,6 +637,8 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
     return ANY ? occl : hitID >= 0;
 }
 
+constexpr int RC_MAX_DEPTH = 3;   // vertices per training path that give records
+
 struct RcPathParams {
     TraceParams tp;          // scene pointers for the inline traversal
     PtScene sc;
@@ -603,19 +648,28 @@ struct RcPathParams {
     uint32_t seed;
     uint32_t max_bounces;
     float epsilon;
-    float4* samples;         // 4 float4 per sample
+    float scale;             // radiance scale of the stored targets
+    float4* samples;         // 4 float4 per sample, up to RC_MAX_DEPTH per path
     uint32_t* n_samples;
 };
 
-// Self-generated training paths: a random pixel, its camera ray, and the
-// radiance the path tracer's estimator finds leaving the first hit towards
-// the camera (next-event estimation at every vertex, up to max_bounces
-// further bounces; the first hit's own emission excluded).
+__device__ __forceinline__ float safe_div(float a, float b) { return b > 1e-30f ? a / b : 0.0f; }
+
+// Self-generated training paths: a random pixel, its camera ray, and the path
+// tracer's estimator (next-event estimation at every vertex, continuation,
+// Russian roulette) up to max_bounces bounces, with next-event estimation
+// and BRDF-sampled light hits combined by the power heuristic (same
+// expectation as the engine's estimator, fewer outliers in the targets).  Every vertex k < max_bounces
+// (k < RC_MAX_DEPTH) with a non-black base colour gives one record: its
+// indirect radiance estimate -- the next-event contributions of the later
+// vertices divided by the path throughput that arrived at k -- divided by
+// the base colour and scaled.
 static __global__ void rc_paths_kernel(RcPathParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    bool emit = false;
-    float4 s0{}, s1{}, s2{}, s3{};
+    float4 rec[RC_MAX_DEPTH][3] = {};
+    V3 arrive[RC_MAX_DEPTH] = {}, base[RC_MAX_DEPTH] = {}, acc[RC_MAX_DEPTH] = {};
+    uint32_t nv = 0;
     if (i < p.n_paths) {
         const uint32_t npix = p.cam.width * p.cam.height;
         const uint32_t key = i + (p.frame << 20);
@@ -628,7 +682,8 @@ static __global__ void rc_paths_kernel(RcPathParams p) {
         V3 rd = normalize(v3(c.ox + c.rx * u + c.bx * v - c.lx, c.oy + c.ry * u + c.by * v - c.ly,
                              c.oz + c.rz * u + c.bz * v - c.lz));
         V3 ro = v3(c.lx, c.ly, c.lz);
-        V3 thr = v3(1, 1, 1), target = v3(0, 0, 0);
+        V3 thr = v3(1, 1, 1);
+        float hitW = 0.0f;       // MIS factor of the emission the current ray may find
         const uint32_t key2 = i ^ (p.frame * 0x9E3779B9u);
         for (uint32_t b = 0; b <= p.max_bounces; b++) {
             TraceParams tp = p.tp;
@@ -638,46 +693,82 @@ static __global__ void rc_paths_kernel(RcPathParams p) {
             if (!scene_trace_inline<false>(tp, ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, 0.0f, 1e12f, t, tri, inst, bu, bv))
                 break;
             Surf sf = make_surface(p.sc, ro, rd, t, inst, tri, bu, bv);
-            if (b == 0) {
-                emit = true;
-                s0 = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
-                s1 = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(pix));
-                s2 = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
+            // emission found by the previous vertex's continuation: part of
+            // that vertex's direct light, so indirect light of the ones before
+            if (b >= 2 && hitW > 0.0f && sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f) {
+                const V3 e = thr * sf.mat.emissive * hitW;
+#pragma unroll
+                for (int k = 0; k < RC_MAX_DEPTH; k++)
+                    if (k + 1 < int(b) && k < int(nv)) acc[k] = acc[k] + e;
             }
+            if (b < p.max_bounces && b < uint32_t(RC_MAX_DEPTH)) {
+#pragma unroll
+                for (int k = 0; k < RC_MAX_DEPTH; k++)
+                    if (k == int(b)) {
+                        rec[k][0] = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
+                        rec[k][1] = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(pix));
+                        rec[k][2] = make_float4(sf.N.x, sf.N.y, sf.N.z, float(b));
+                        arrive[k] = thr;
+                        base[k] = sf.mat.base;
+                        acc[k] = v3(0, 0, 0);
+                    }
+                nv = b + 1;
+            }
+            const bool cont = b < p.max_bounces;
             V3 cth, so, sd;
-            float st;
-            if (direct_light(p.sc, sf, thr, key2, sample, b, p.seed, p.epsilon, cth, so, sd, st)) {
+            float st, pl = 0.0f;
+            if (b > 0 && direct_light(p.sc, sf, thr, key2, sample, b, p.seed, p.epsilon, cth, so, sd, st, &pl)) {
+                if (cont) cth = cth * power_weight(pl, bsdf_pdf(sf, sf.L));
                 tp.cull_mask = 0x40u;   // INSTANCE_MASK_SHADOW
                 float t2, u2, v2;
                 int32_t tr2, in2;
-                if (!scene_trace_inline<true>(tp, so.x, so.y, so.z, sd.x, sd.y, sd.z, 0.0f, st, t2, tr2, in2, u2, v2))
-                    target = target + cth;
+                if (!scene_trace_inline<true>(tp, so.x, so.y, so.z, sd.x, sd.y, sd.z, 0.0f, st, t2, tr2, in2, u2, v2)) {
+#pragma unroll
+                    for (int k = 0; k < RC_MAX_DEPTH; k++)
+                        if (k < int(b) && k < int(nv)) acc[k] = acc[k] + cth;
+                }
             }
-            if (b >= p.max_bounces) break;
+            if (!cont) break;
             V3 o, d;
-            if (!continue_path(sf, thr, key2, sample, b, p.seed, p.epsilon, o, d)) break;
+            bool spec = false;
+            if (!continue_path(sf, thr, key2, sample, b, p.seed, p.epsilon, o, d, &spec)) break;
+            hitW = b + 1 >= 2 ? mis_hit_factor(p.sc, sf, d, spec) : 0.0f;
             ro = o;
             rd = d;
         }
-        s3 = make_float4(target.x, target.y, target.z, 1.0f);
     }
-    const uint32_t si = warp_append(p.n_samples, emit, lane);
-    if (emit) {
-        float4* s = p.samples + size_t(si) * 4;
-        s[0] = s0; s[1] = s1; s[2] = s2; s[3] = s3;
+#pragma unroll
+    for (int k = 0; k < RC_MAX_DEPTH; k++) {
+        const bool emit = k < int(nv) && base[k].x + base[k].y + base[k].z > 0.0f;
+        const uint32_t si = warp_append(p.n_samples, emit, lane);
+        if (emit) {
+            const V3 tg = v3(safe_div(acc[k].x, arrive[k].x * base[k].x), safe_div(acc[k].y, arrive[k].y * base[k].y),
+                             safe_div(acc[k].z, arrive[k].z * base[k].z)) * p.scale;
+            float4* o = p.samples + size_t(si) * 4;
+            o[0] = rec[k][0];
+            o[1] = rec[k][1];
+            o[2] = rec[k][2];
+            o[3] = make_float4(tg.x, tg.y, tg.z, 1.0f);
+        }
     }
 }
 
 struct RcShadeParams {
-    PtParams pt;             // queues, scene, accumulation (shadow queue for metal vertices)
+    PtParams pt;             // queues, scene, accumulation, bounce budget (pt.max_bounces)
     float4* queries;         // cache queries (4 float4)
     uint32_t* n_queries;
     uint32_t last_bounce;    // query the cache here whatever the material
+    float inv_scale;         // 1 / radiance scale of the cache
+    float rough_cut;         // metals at least this rough end in the cache too
 };
 
-// Rendering with the cache: emission of the first hit; a diffuse vertex (or
-// the last bounce) ends the path in a cache query weighted by the path
-// throughput; a metallic vertex takes next-event estimation and continues.
+// Rendering with the cache: emission of the first hit and next-event
+// estimation at every vertex (as the path tracer).  A diffuse vertex, a metal
+// with roughness >= rough_cut, or the vertex at last_bounce ends the path
+// with a cache query for its indirect radiance, weighted by path throughput x
+// base colour / scale.  A glossier metal continues the path; its next-event
+// estimate and the emission its continuation finds are combined by the power
+// heuristic (the factor travels in the continuation ray's dir.w).
 static __global__ void rc_shade_kernel(RcShadeParams rp) {
     const PtParams& p = rp.pt;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -695,29 +786,41 @@ static __global__ void rc_shade_kernel(RcShadeParams rp) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
             const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
             Surf sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
-            if (p.bounce == 0 && sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f)
-                add_radiance(p, pix, sf.mat.emissive);
-            if (sf.mat.metalness < 0.5f || p.bounce >= rp.last_bounce) {
-                emitQuery = true;
-                q0 = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
-                q1 = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(pix));
-                q2 = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
-                q3 = make_float4(thr.x, thr.y, thr.z, 1.0f);
-            } else {
-                V3 c, so, sd;
-                float st;
-                if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st)) {
-                    emitShadow = true;
-                    shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
-                    shRay1 = make_float4(sd.x, sd.y, sd.z, st);
-                    shPay = make_float4(c.x, c.y, c.z, __uint_as_float(pix));
-                }
-                V3 o, d;
-                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d)) {
-                    emitRay = true;
-                    outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
-                    outRay1 = make_float4(d.x, d.y, d.z, 0.0f);
-                    outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
+            const bool emissive = sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f;
+            if (p.bounce == 0 && emissive) add_radiance(p, pix, sf.mat.emissive);
+            if (p.bounce > 0 && emissive && d4.w > 0.0f) add_radiance(p, pix, thr * sf.mat.emissive * d4.w);
+            const V3 V = sf.V, N = sf.N;     // the query's direction and normal (direct_light moves sf.L only)
+            const bool query = sf.mat.metalness < 0.5f || sf.mat.roughness >= rp.rough_cut ||
+                               p.bounce >= rp.last_bounce || p.bounce + 1 >= uint32_t(RC_MAX_DEPTH);
+            const bool cont = p.bounce < p.max_bounces && !query;
+            V3 c, so, sd;
+            float st, pl = 0.0f;
+            if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st, &pl)) {
+                if (cont) c = c * power_weight(pl, bsdf_pdf(sf, sf.L));
+                emitShadow = true;
+                shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
+                shRay1 = make_float4(sd.x, sd.y, sd.z, st);
+                shPay = make_float4(c.x, c.y, c.z, __uint_as_float(pix));
+            }
+            if (p.bounce < p.max_bounces) {
+                if (query) {
+                    const V3 w = thr * sf.mat.base * rp.inv_scale;
+                    if (w.x + w.y + w.z > 0.0f) {
+                        emitQuery = true;
+                        q0 = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
+                        q1 = make_float4(V.x, V.y, V.z, __uint_as_float(pix));
+                        q2 = make_float4(N.x, N.y, N.z, float(p.bounce));
+                        q3 = make_float4(w.x, w.y, w.z, 1.0f);
+                    }
+                } else {
+                    V3 o, d;
+                    bool spec = false;
+                    if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec)) {
+                        emitRay = true;
+                        outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
+                        outRay1 = make_float4(d.x, d.y, d.z, mis_hit_factor(p.sc, sf, d, spec));
+                        outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
+                    }
                 }
             }
         }

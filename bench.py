@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline pass only (no extra workloads)")
     ap.add_argument("--autotune", action="store_true", help="re-run the launch-parameter autotuner")
+    ap.add_argument("--workloads", default="random65536,batched64,pathtrace,radiance_cache",
+                    help="comma-separated extra workloads (radiance_cache needs pathtrace)")
+    ap.add_argument("--pt-ref-spp", type=int, default=4096, help="samples of the converged image")
+    ap.add_argument("--rc-max-frames", type=int, default=320, help="frame cap of the radiance-cache run")
     return ap.parse_args()
 
 
@@ -428,12 +432,95 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
         im = (acc[:, :3] / done).cpu().numpy().reshape(H, W, 3)
         curve.append({"spp": done, "ms_cum": ms_total * done / spp, "rel_mse": ptscene.rel_mse(im, ref)})
     curve.append({"spp": spp, "ms_cum": ms_total, "rel_mse": final_err, "rmse": final_rmse})
-    ctx.close()
     final = curve[-1]
-    return {"resolution": [W, H], "bounces": 3, "spp": spp, "ms_to_spp": final["ms_cum"],
-            "ms_per_spp": final["ms_cum"] / spp, "rel_mse": final["rel_mse"], "rmse": final["rmse"],
-            "reference_spp": ref_spp, "reference_seconds": t_ref, "rel_mse_eps": 1e-2,
-            "curve": [{k: c[k] for k in ("spp", "ms_cum", "rel_mse")} for c in curve]}
+    res = {"resolution": [W, H], "bounces": 3, "spp": spp, "ms_to_spp": final["ms_cum"],
+           "ms_per_spp": final["ms_cum"] / spp, "rel_mse": final["rel_mse"], "rmse": final["rmse"],
+           "reference_spp": ref_spp, "reference_seconds": t_ref, "rel_mse_eps": 1e-2,
+           "curve": [{k: c[k] for k in ("spp", "ms_cum", "rel_mse")} for c in curve]}
+    return res, (ctx, sc, cam, ref)
+
+
+def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32), max_frames=320,
+                            n_paths=65536, steps=2, rough_cut=0.35, close=True):
+    """Radiance-cache path tracer on the same scene, camera and converged
+    image as the plain path tracer: the cache starts untrained; every frame
+    trains it on `n_paths` self-generated 3-bounce paths (`steps` Adam
+    steps, lr 1e-2) and renders 1 spp with paths ending in the cache.  Frame
+    times are CUDA-event times on the stream (the error read-backs between
+    frames are outside them).  The rendered frames are averaged from frame
+    `start` on (the frames before only train); for each start the GPU time
+    from the cold cache to the frame where the average reaches the plain
+    path tracer's 64-spp rel-MSE is reported, and the best start is the
+    result."""
+    import atlas_rt
+    from atlas_rt import ptscene, scenes
+    ctx, sc, cam, ref = scene
+    target = pt["rel_mse"]
+    pt_ms = pt["ms_to_spp"]
+    n = W * H
+    ref_t = torch.from_numpy(ref.reshape(n, 3)).to(dev)
+    den = ref_t * ref_t + 1e-2
+    lo, hi = atlas_rt.mesh_bounds(sc["bvh"])
+    small = atlas_rt.make_camera(scenes.pinhole_camera(160, 90))
+    frame_buf = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    probe = torch.zeros((160 * 90, 4), dtype=torch.float32, device=dev)
+    accs = {s: torch.zeros((n, 3), dtype=torch.float64, device=dev) for s in starts}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize(dev)
+    # radiance scale from a 1-spp 160x90 plain image (inside the timed budget)
+    ev[0].record(stream)
+    ctx.pathtrace(small, probe, spp=1, sample_offset=1 << 27, seed=11, stream=stream)
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    t_cum = ev[0].elapsed_time(ev[1])
+    mean = float(probe[:, :3].mean())
+    scale = 1.0 / max(mean, 1e-6)
+    rc = atlas_rt.RadianceCache(ctx, lo - 0.5, hi + 0.5, seed=5, radiance_scale=scale, rough_cut=rough_cut)
+    reached = {}
+    curve = []
+    train_ms = render_ms = 0.0
+    evf = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for f in range(max_frames):
+        render = f >= min(starts)
+        evf[0].record(stream)
+        rc.train_frame(cam, f, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
+        evf[1].record(stream)
+        if render:
+            frame_buf.zero_()
+            rc.render(cam, f, frame_buf, stream=stream)
+        evf[2].record(stream)
+        torch.cuda.synchronize(dev)
+        tr, tt = evf[0].elapsed_time(evf[1]), evf[0].elapsed_time(evf[2])
+        train_ms += tr
+        render_ms += tt - tr
+        t_cum += tt
+        if not render:
+            continue
+        rgb = frame_buf[:, :3].double()
+        for s0 in starts:
+            if f >= s0:
+                accs[s0] += rgb
+                if s0 not in reached:
+                    e = float((((accs[s0] / (f - s0 + 1)) - ref_t) ** 2 / den).mean())
+                    if e <= target:
+                        reached[s0] = {"frame": f, "ms": t_cum, "rel_mse": e}
+                    if (f - s0 + 1) in (1, 2, 4, 8, 16, 32, 64, 128, 256):
+                        curve.append({"start": s0, "frames": f - s0 + 1, "ms_cum": t_cum, "rel_mse": e})
+        if len(reached) == len(starts):
+            break
+    rc.close()
+    if close:
+        ctx.close()
+    out = {"resolution": [W, H], "n_paths": n_paths, "adam_steps_per_frame": steps, "radiance_scale": scale,
+           "rough_cut": rough_cut,
+           "target_rel_mse": target, "plain_pt_ms_to_64spp": pt_ms, "frames_run": f + 1,
+           "train_ms_per_frame": train_ms / (f + 1),
+           "render_ms_per_frame": render_ms / max(f + 1 - min(starts), 1),
+           "starts": {str(s): reached.get(s) for s in starts}, "curve": curve}
+    best = min((r["ms"] for r in reached.values()), default=None)
+    out["ms_to_equal_rel_mse"] = best
+    out["speedup_vs_plain_pt"] = pt_ms / best if best else None
+    return out
 
 
 def main():
@@ -575,13 +662,23 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
     }
     if not args.quick:
-        line["workloads"] = {
-            "random65536": workload_random65536(torch, dev, stream, flush, max(args.steps // 2, 3)),
-            "batched64": workload_batched(torch, dev, stream, flush, max(args.steps // 2, 3),
-                                          autotune=args.autotune,
-                                          log=(lambda m: print(m, file=sys.stderr))),
-            "pathtrace": workload_pathtrace(torch, dev, stream),
-        }
+        wl = set(args.workloads.split(","))
+        line["workloads"] = {}
+        if "random65536" in wl:
+            line["workloads"]["random65536"] = workload_random65536(torch, dev, stream, flush,
+                                                                    max(args.steps // 2, 3))
+        if "batched64" in wl:
+            line["workloads"]["batched64"] = workload_batched(torch, dev, stream, flush, max(args.steps // 2, 3),
+                                                              autotune=args.autotune,
+                                                              log=(lambda m: print(m, file=sys.stderr)))
+        if "pathtrace" in wl:
+            pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp)
+            line["workloads"]["pathtrace"] = pt
+            if "radiance_cache" in wl:
+                line["workloads"]["radiance_cache"] = workload_radiance_cache(torch, dev, stream, pt, scene,
+                                                                              max_frames=args.rc_max_frames)
+            else:
+                scene[0].close()
     clk = clocks.stop()
     clk["window"] = "warm-up, timed steps, e2e and extra workloads"
     line["clocks"] = clk

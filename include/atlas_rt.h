@@ -447,8 +447,14 @@ typedef struct ae_pt_params {
     uint32_t sample_offset;  /* index of the first sample (random streams continue across calls) */
     uint32_t seed;
     float epsilon;           /* ray origin offset (EPSILON = 0.1, common.hsh:9) */
-    uint32_t reserved[3];
+    uint32_t flags;          /* AE_PT_MIS: not the engine's estimator (below) */
+    uint32_t reserved[2];
 } ae_pt_params;
+
+/* Next-event estimation combined with BRDF sampling by the power heuristic
+ * (BRDF-sampled light hits at bounces >= 1 count, weighted).  Same expected
+ * image as the engine's estimator, fewer outliers on glossy surfaces. */
+#define AE_PT_MIS 0x1u
 
 /* Path-traces spp samples of every pixel of `cam` over the scene (which needs
  * shading triangles, materials and lights) and adds the radiance of each
@@ -469,8 +475,11 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
  * from base_resolution to max_resolution in a geometric progression) over
  * the world box aabb_min..aabb_max, 16 spherical-harmonic coefficients of
  * the outgoing direction, the normal and the roughness feed a 5 x 64 ReLU
- * MLP (BF16 weights, FP32 accumulation) that predicts the radiance leaving a
- * surface point.  Trained online with Adam on a relative L2 loss. */
+ * MLP (BF16 weights, FP32 accumulation) that predicts the indirect radiance
+ * leaving a surface point (what the path tracer adds after the point's own
+ * next-event estimate, within its bounce budget), divided by the point's base
+ * colour and times radiance_scale.  Trained online with Adam on a relative L2
+ * loss. */
 typedef struct ae_rc ae_rc;
 
 typedef struct ae_rc_config {
@@ -484,7 +493,9 @@ typedef struct ae_rc_config {
     uint32_t seed;
     float aabb_min[3];
     float aabb_max[3];
-    uint32_t reserved[4];
+    float radiance_scale;       /* stored value = radiance x scale (0: 1) */
+    float rough_cut;            /* rendering: metals at least this rough end in the cache (0: 0.35) */
+    uint32_t reserved[2];
 } ae_rc_config;
 
 ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out);
@@ -502,7 +513,8 @@ ae_rt_status ae_rc_set_params(ae_rc* rc, const float* mlp, const float* grid);
 
 /* Query / training records, 16 floats each: position xyz, roughness;
  * outgoing direction xyz (unit, towards the viewer), pixel index bits;
- * normal xyz, 0; target (training) or path throughput (rendering) rgb, 1. */
+ * normal xyz, vertex depth (bounces from the camera); target (training) or
+ * render weight rgb, 1. */
 
 /* Predictions for n query records (device buffers; out: 4 floats each). */
 ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* out, void* stream);
@@ -517,16 +529,20 @@ ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, floa
 
 /* One frame of online training: n_paths self-generated paths from random
  * pixels of `cam`, each traced with the path tracer's estimator up to
- * max_bounces further bounces; their first-hit radiance trains the cache in
- * `steps` Adam steps.  loss_out (optional) synchronises. */
+ * max_bounces bounces (1..16); every vertex at depth < min(max_bounces, 3)
+ * gives one record of its indirect radiance, and the records train the cache
+ * in `steps` Adam steps (equal slices).  The render uses the same bounce
+ * budget.  loss_out (optional, mean loss of the last step) synchronises. */
 ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
                                uint32_t max_bounces, float* loss_out, void* stream);
 
 /* One sample per pixel with paths terminated into the cache: the first hit's
- * emission, then at the first diffuse vertex (or at bounce last_bounce) the
- * cache's prediction times the path throughput; metallic vertices before it
- * take next-event estimation and continue.  Adds into accum (float4 per
- * pixel, device). */
+ * emission and next-event estimation at every vertex, as the path tracer;
+ * at the first diffuse vertex or metal with roughness >= rough_cut (or at
+ * bounce last_bounce, or depth 2) the cache's indirect radiance times path
+ * throughput x base colour ends the path; glossier metals before it continue,
+ * their light combining next-event estimation and BRDF sampling (power
+ * heuristic).  Adds into accum (float4 per pixel, device). */
 ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
                           void* stream);
 

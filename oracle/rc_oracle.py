@@ -97,6 +97,7 @@ class Cache:
         X[:, 32:48] = sh16(rec[:, 4:7].astype(np.float64))
         X[:, 48:51] = rec[:, 8:11]
         X[:, 51] = rec[:, 3]
+        X[:, 52] = rec[:, 11]
         return X
 
     def forward(self, mlp, table, rec, bf16=False):
