@@ -45,6 +45,9 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
 
 W, H = 1920, 1080
+# DRAM bytes (read + write) of the primary closest-hit launch of this workload,
+# from ncu (131,443,968 + 39,079,680)
+TRAFFIC_PRIMARY_BYTES = 170_523_648
 TMIN, TINF = 0.0, 1e12
 EPSILON = 0.1
 LIGHT = (0.4, 1.0, 0.3)
@@ -656,7 +659,9 @@ def main():
                      "peak_source": "L2-resident copy measured live (2 x 16 MiB, CUDA graph of 32 copies)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "hbm_frac": achieved / hbm_peak, "hbm_peak": hbm_peak, "hbm_peak_source": hbm_src,
-                     "traffic": None},
+                     "traffic": TRAFFIC_PRIMARY_BYTES,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of this launch, one ncu "
+                                       "capture (profiles/trace_kernel_terrain_boxes_cast.md)"},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "ae_rt_cast_pass, pinned host result buffers"},
         "gpu_launches": launches_per_step * args.steps,
