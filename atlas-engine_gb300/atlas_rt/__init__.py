@@ -43,6 +43,10 @@ HIT_FLAG_HIT = 0x1
 HIT_FLAG_NEAR_TIE = 0x2
 HIT_FLAG_OVERFLOW = 0x4
 HIT_FLAG_ITER_CAP = 0x8
+HIT_FLAG_RETESTED = 0x10
+HIT64_DTYPE = np.dtype([("t", "<f8"), ("t_second", "<f8"), ("triPtr", "<i4"), ("flags", "<u4"),
+                        ("reserved", "<i4", (2,))])
+assert HIT64_DTYPE.itemsize == 32
 
 MASK_ALL = 1 << 7
 MASK_SHADOW = 1 << 6
@@ -193,6 +197,18 @@ class Context:
         _check(lib().ae_rt_trace_closest(self._h, mesh, _ptr(rays), n_rays, tmin, tmax, _ptr(out),
                                          _stream_handle(stream)), self._h)
         return out
+
+    def retest_near_ties(self, mesh: int, rays, hits, tmin: float, tmax: float, out, n_rays: int | None = None,
+                         stream=None) -> int:
+        """FP64 re-test of the rays flagged HIT_FLAG_NEAR_TIE (device buffers:
+        rays (n, 12) float32, hits (n, 8) float32, out (n, 8) float32 viewed
+        as HIT64_DTYPE).  Returns the number of flagged rays."""
+        if n_rays is None:
+            n_rays = rays.numel() * rays.element_size() // 48
+        cnt = C.c_uint32()
+        _check(lib().ae_rt_retest_near_ties(self._h, mesh, _ptr(rays), _ptr(hits), n_rays, tmin, tmax, _ptr(out),
+                                            C.byref(cnt), _stream_handle(stream)), self._h)
+        return cnt.value
 
     def trace_any(self, mesh: int, rays, tmin: float, tmax: float, out=None, stream=None,
                   n_rays: int | None = None):

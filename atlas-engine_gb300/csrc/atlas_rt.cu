@@ -346,7 +346,7 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     for (Scratch* sc : { &ctx->pt_rays[0], &ctx->pt_rays[1], &ctx->pt_pay[0], &ctx->pt_pay[1], &ctx->pt_hits,
                          &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ })
         sc->release();
-    for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->cast_primary, &ctx->cast_primary_hits,
+    for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->retest_count, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
         sc->release();
     delete ctx;

@@ -74,7 +74,7 @@ struct ae_rt_ctx {
     uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2] shadow queue
     uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
     unsigned long long* d_fetch = nullptr;
-    atlas::rt::host::Scratch rays_in, results_out, batch_table;
+    atlas::rt::host::Scratch rays_in, results_out, batch_table, retest_count;
     // buffers of ae_rt_cast_pass
     atlas::rt::host::Scratch cast_primary, cast_primary_hits, cast_secondary, cast_secondary_hits, cast_shadow, cast_occluded;
     uint32_t* d_cast_counts = nullptr;

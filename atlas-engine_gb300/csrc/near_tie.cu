@@ -1,0 +1,212 @@
+// FP64 re-test of near ties (include/atlas_rt.h, ae_rt_retest_near_ties).
+//
+// The FP32 traversal reproduces the engine's shader bit for bit, and flags a
+// ray whose second-nearest accepted hit lies within 1e-6 relative t of the
+// nearest (AE_HIT_NEAR_TIE): for those rays the FP32 winner is decided by
+// rounding and traversal order.  This kernel finds, for each flagged ray, the
+// nearest triangle in double precision: a closest-hit traversal of the same
+// BVH with conservative double slab tests (every box is widened by a relative
+// 1e-9 so that no triangle the double test accepts is culled by rounding) and
+// the double form of the shader's triangle test (intersections.hsh:36-57),
+// accepting tmin < t < tmax.  Exactly equal double distances resolve to the
+// lower BVH-order triangle index, and t_second is the second smallest
+// accepted distance over the BVH-order triangle entries (two entries at the
+// same distance make t_second equal to t); the oracle's brute-force pass over
+// every entry gives the same pair.
+#include "atlas_rt.h"
+#include "context.cuh"
+#include "trace_kernels.cuh"
+
+#include <cmath>
+
+using namespace atlas::rt::host;
+
+namespace {
+
+constexpr uint32_t kRetestStack = 64;
+
+struct RetestParams {
+    const float4* nodes;
+    const float4* tris;
+    uint32_t n_nodes;
+    uint32_t n_tris;
+    const float4* rays;      // PackedRay (3 float4)
+    const float4* hits;      // ae_hit (2 float4)
+    uint32_t n;
+    double tmin, tmax;
+    uint32_t max_steps;
+    ae_hit_f64* out;
+    uint32_t* n_retested;
+    uint32_t* error_word;
+};
+
+// Conservative slab test in double: [tn, tf] of the ray inside the box,
+// widened by 1e-9 relative; an axis with zero direction constrains only by
+// whether the origin lies in the (equally widened) slab.
+__device__ __forceinline__ bool box64(const double o[3], const double d[3], float lx, float ly, float lz, float hx,
+                                      float hy, float hz, double tmin, double tmax) {
+    const double lo[3] = { lx, ly, lz }, hi[3] = { hx, hy, hz };
+    double tn = tmin, tf = tmax;
+    for (int k = 0; k < 3; k++) {
+        if (d[k] == 0.0) {
+            const double w = 1e-9 * (fabs(lo[k]) + fabs(hi[k])) + 1e-300;
+            if (o[k] < lo[k] - w || o[k] > hi[k] + w) return false;
+            continue;
+        }
+        double a = (lo[k] - o[k]) / d[k], b = (hi[k] - o[k]) / d[k];
+        if (a > b) { const double t = a; a = b; b = t; }
+        const double w = 1e-9 * (fabs(a) + fabs(b)) + 1e-300;
+        tn = fmax(tn, a - w);
+        tf = fmin(tf, b + w);
+    }
+    return tn <= tf;
+}
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double cr(double a, double b, double c, double d) { return ds(dm(a, b), dm(c, d)); }
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+    return da(da(dm(a[0], b[0]), dm(a[1], b[1])), dm(a[2], b[2]));
+}
+
+// intersections.hsh:36-57 in double, every operation rounded separately in
+// the formula's order (no contraction), so that exactly equal distances are
+// decided as the double-precision restatement decides them.  Returns the
+// accept test; t out.
+__device__ __forceinline__ bool tri64(const double o[3], const double d[3], const float4& A, const float4& B,
+                                      const float4& C, double& t) {
+    const double v0[3] = { A.x, A.y, A.z };
+    const double e0[3] = { ds(B.x, v0[0]), ds(B.y, v0[1]), ds(B.z, v0[2]) };
+    const double e1[3] = { ds(C.x, v0[0]), ds(C.y, v0[1]), ds(C.z, v0[2]) };
+    const double s[3] = { ds(o[0], v0[0]), ds(o[1], v0[1]), ds(o[2], v0[2]) };
+    const double p[3] = { cr(s[1], e0[2], e0[1], s[2]), cr(s[2], e0[0], e0[2], s[0]), cr(s[0], e0[1], e0[0], s[1]) };
+    const double q[3] = { cr(d[1], e1[2], e1[1], d[2]), cr(d[2], e1[0], e1[2], d[0]), cr(d[0], e1[1], e1[0], d[1]) };
+    const double den = dot3(q, e0);
+    t = __ddiv_rn(dot3(p, e1), den);
+    const double u = __ddiv_rn(dot3(q, s), den);
+    const double v = __ddiv_rn(dot3(p, d), den);
+    return t >= 0.0 && u >= 0.0 && v >= 0.0 && da(u, v) <= 1.0;
+}
+
+__global__ void retest_kernel(RetestParams p) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+        const float4 h0 = p.hits[i * 2], h1 = p.hits[i * 2 + 1];
+        const uint32_t flags = __float_as_uint(h0.w);
+        ae_hit_f64 r;
+        r.t = double(h0.x);
+        r.t_second = double(h1.z);
+        r.triPtr = __float_as_int(h0.y);
+        r.flags = flags & AE_HIT_HIT;
+        if (!(flags & AE_HIT_NEAR_TIE) || p.n_nodes == 0) {
+            p.out[i] = r;
+            continue;
+        }
+        atomicAdd(p.n_retested, 1u);
+        const float4 o4 = p.rays[i * 3], d4 = p.rays[i * 3 + 1];
+        const double o[3] = { o4.x, o4.y, o4.z }, d[3] = { d4.x, d4.y, d4.z };
+        double best = INFINITY, second = INFINITY;
+        int32_t bi = -1;
+        int32_t stack[kRetestStack];
+        uint32_t sp = 0, steps = 0;
+        int32_t node = 0;
+        bool bad = false;
+        while (true) {
+            if (++steps > p.max_steps) { bad = true; atomicOr(p.error_word, atlas::rt::dev::kErrIterationCap); break; }
+            if (node < 0) {
+                int32_t tp = ~node;
+                bool end = false;
+                do {
+                    if (uint32_t(tp) >= p.n_tris) { bad = true; break; }
+                    const float4 A = __ldg(p.tris + size_t(tp) * 3), B = __ldg(p.tris + size_t(tp) * 3 + 1),
+                                 C = __ldg(p.tris + size_t(tp) * 3 + 2);
+                    end = A.w > 0.0f;
+                    double t;
+                    if (tri64(o, d, A, B, C, t) && t > p.tmin && t < p.tmax) {
+                        if (t < best || (t == best && tp < bi)) {
+                            if (tp != bi) second = best;
+                            best = t;
+                            bi = tp;
+                        } else if (t < second && tp != bi) {
+                            second = t;
+                        }
+                    }
+                    tp++;
+                } while (!end);
+                if (bad || sp == 0) break;
+                node = stack[--sp];
+                continue;
+            }
+            if (uint32_t(node) >= p.n_nodes) { bad = true; break; }
+            const float4* np = p.nodes + size_t(node) * 4;
+            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            // prune by the second distance so that t_second is exact as well
+            const double bound = fmin(p.tmax, second);
+            const bool il = box64(o, d, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, p.tmin, bound);
+            const bool ir = box64(o, d, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, p.tmin, bound);
+            const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
+            if (il && ir) {
+                if (sp >= kRetestStack) { bad = true; atomicOr(p.error_word, atlas::rt::dev::kErrStackOverflow); break; }
+                stack[sp++] = rr;
+                node = l;
+            } else if (il) {
+                node = l;
+            } else if (ir) {
+                node = rr;
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp];
+            }
+        }
+        r.flags = AE_HIT_RETESTED | (bi >= 0 ? AE_HIT_HIT : 0u) | (bad ? AE_HIT_OVERFLOW : 0u);
+        r.triPtr = bi;
+        r.t = best;
+        r.t_second = second;
+        p.out[i] = r;
+    }
+}
+
+}  // namespace
+
+extern "C" ae_rt_status ae_rt_retest_near_ties(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays,
+                                               const ae_hit* hits, uint32_t n_rays, float tmin, float tmax,
+                                               ae_hit_f64* out, uint32_t* n_retested, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
+        return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
+    if (n_retested) *n_retested = 0;
+    if (n_rays == 0) return AE_RT_OK;
+    if (!rays || !hits || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray, hit or result buffer");
+    if (!IsDevicePointer(rays) || !IsDevicePointer(hits) || !IsDevicePointer(out))
+        return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_retest_near_ties takes device buffers");
+    if (n_rays > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one call");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const DeviceMesh& m = ctx->meshes[size_t(mesh_id)];
+    RetestParams p{};
+    p.nodes = m.nodes;
+    p.tris = m.tris;
+    p.n_nodes = m.n_nodes;
+    p.n_tris = m.n_tris;
+    p.rays = reinterpret_cast<const float4*>(rays);
+    p.hits = reinterpret_cast<const float4*>(hits);
+    p.n = n_rays;
+    p.tmin = tmin;
+    p.tmax = tmax;
+    p.max_steps = 4u * m.n_nodes + 64u;
+    p.out = out;
+    AE_CUDA(ctx, ctx->retest_count.ensure(sizeof(uint32_t)));
+    p.n_retested = static_cast<uint32_t*>(ctx->retest_count.ptr);
+    p.error_word = ctx->d_counter + 1;
+    AE_CUDA(ctx, cudaMemsetAsync(p.n_retested, 0, sizeof(uint32_t), s));
+    const uint32_t blocks = (n_rays + 255) / 256 < uint32_t(ctx->sm_count) * 8u ? (n_rays + 255) / 256
+                                                                                 : uint32_t(ctx->sm_count) * 8u;
+    retest_kernel<<<blocks, 256, 0, s>>>(p);
+    AE_CUDA(ctx, cudaGetLastError());
+    if (n_retested) {
+        AE_CUDA(ctx, cudaMemcpyAsync(n_retested, p.n_retested, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        return ae_rt_synchronize(ctx, stream);
+    }
+    return AE_RT_OK;
+}

@@ -162,6 +162,7 @@ typedef struct ae_hit {
 #define AE_HIT_NEAR_TIE  0x2u  /* a second hit lies within 1e-6 relative t */
 #define AE_HIT_OVERFLOW  0x4u  /* traversal stack overflowed; result invalid */
 #define AE_HIT_ITER_CAP  0x8u  /* traversal step cap hit; result invalid */
+#define AE_HIT_RETESTED  0x10u /* ae_hit_f64 only: the double-precision re-test decided it */
 
 /* ------------------------------------------------------------------------ */
 /* Host BVH builder -- replaces Volume::BVH::BVH (BVH.cpp:14, :58)           */
@@ -545,6 +546,27 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
  * heuristic).  Adds into accum (float4 per pixel, device). */
 ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
                           void* stream);
+
+/* Double-precision re-test of near ties.  For every ray whose ae_hit (from
+ * ae_rt_trace_closest / _queue on the same mesh, tmin and tmax) carries
+ * AE_HIT_NEAR_TIE, the nearest triangle is searched again in double precision:
+ * a closest-hit traversal of the same BVH with conservative double slab
+ * tests and the double form of the shader's triangle test (tmin < t < tmax);
+ * equal double distances resolve to the lower BVH-order index, t_second is
+ * the second smallest accepted distance.  Other rays are passed through (t,
+ * triPtr, tSecond, AE_HIT_HIT).  Device buffers; n_retested (optional, host)
+ * receives the number of flagged rays and synchronises.  The engine has no
+ * counterpart: its shader keeps the FP32 winner (bvh.hsh:62-63). */
+typedef struct ae_hit_f64 {
+    double t;             /* +inf: no hit */
+    double t_second;
+    int32_t triPtr;       /* BVH order, -1: miss */
+    uint32_t flags;       /* AE_HIT_HIT, AE_HIT_RETESTED, AE_HIT_OVERFLOW */
+    int32_t reserved[2];
+} ae_hit_f64;
+ae_rt_status ae_rt_retest_near_ties(ae_rt_ctx* ctx, int32_t mesh, const ae_packed_ray* rays, const ae_hit* hits,
+                                    uint32_t n_rays, float tmin, float tmax, ae_hit_f64* out,
+                                    uint32_t* n_retested, void* stream);
 
 /* Waits for `stream` and reports device-side errors of the context's
  * preceding asynchronous calls (stack overflow, step cap, timeouts). */
