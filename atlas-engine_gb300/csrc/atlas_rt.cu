@@ -346,6 +346,10 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     for (Scratch* sc : { &ctx->pt_rays[0], &ctx->pt_rays[1], &ctx->pt_pay[0], &ctx->pt_pay[1], &ctx->pt_hits,
                          &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ })
         sc->release();
+    for (cudaEvent_t e : ctx->cast_events)
+        if (e) cudaEventDestroy(e);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->h_cast_counts) cudaFreeHost(ctx->h_cast_counts);
     for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->retest_count, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
         sc->release();
@@ -909,30 +913,50 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     auto* occ = static_cast<uint8_t*>(ctx->cast_occluded.ptr);
     uint32_t* counts = ctx->d_cast_counts;
     const float kInf = 1e12f;   // INF of common.hsh:8
+    // The result copies run on a second stream, each as soon as the stage
+    // that produced it is done, so they overlap the later stages: primary hits
+    // during the spawn and bounce trace, bounce rays and hits during the
+    // shadow trace.  The host learns the queue lengths from a pinned word
+    // written right after the spawn, while the bounce trace runs.
+    if (!ctx->copy_stream) AE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ctx->cast_events)
+        if (!e) AE_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!ctx->h_cast_counts) AE_CUDA(ctx, cudaMallocHost(&ctx->h_cast_counts, 2 * sizeof(uint32_t)));
+    cudaStream_t cs = ctx->copy_stream;
+    cudaEvent_t evPrim = ctx->cast_events[0], evCounts = ctx->cast_events[1], evSec = ctx->cast_events[2],
+                evShd = ctx->cast_events[3];
+    auto copy = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!dst || !bytes) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, cs);
+    };
     ae_rt_status st;
     if ((st = ae_rt_raygen(ctx, cam, prim, stream)) != AE_RT_OK) return st;
     if ((st = Trace(ctx, false, mesh_id, prim, n, 0.0f, kInf, primHits, stream)) != AE_RT_OK) return st;
+    AE_CUDA(ctx, cudaEventRecord(evPrim, s));
+    AE_CUDA(ctx, cudaStreamWaitEvent(cs, evPrim, 0));
+    AE_CUDA(ctx, copy(out->primary_hits, primHits, hb));
     AE_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s));
     if ((st = ae_rt_spawn_bounce(ctx, mesh_id, prim, primHits, nullptr, n, params, sec, shd, counts, stream)) != AE_RT_OK)
         return st;
+    AE_CUDA(ctx, cudaMemcpyAsync(ctx->h_cast_counts, counts, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    AE_CUDA(ctx, cudaEventRecord(evCounts, s));
     if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
+    AE_CUDA(ctx, cudaEventRecord(evSec, s));
     const float shadowMax = kInf - 2.0f * params->epsilon;   // rayHit.csh:333
     if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, stream, counts + 1)) != AE_RT_OK) return st;
-    uint32_t hc[2] = { 0, 0 };
-    AE_CUDA(ctx, cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
-    AE_CUDA(ctx, cudaStreamSynchronize(s));
+    AE_CUDA(ctx, cudaEventRecord(evShd, s));
+    AE_CUDA(ctx, cudaEventSynchronize(evCounts));
+    const uint32_t nSec = ctx->h_cast_counts[0], nShd = ctx->h_cast_counts[1];
     out->counts[0] = n;
-    out->counts[1] = hc[0];
-    out->counts[2] = hc[1];
-    auto copy = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
-        if (!dst || !bytes) return cudaSuccess;
-        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s);
-    };
-    AE_CUDA(ctx, copy(out->primary_hits, primHits, hb));
-    AE_CUDA(ctx, copy(out->secondary_rays, sec, size_t(hc[0]) * sizeof(ae_packed_ray)));
-    AE_CUDA(ctx, copy(out->secondary_hits, secHits, size_t(hc[0]) * sizeof(ae_hit)));
-    AE_CUDA(ctx, copy(out->shadow_rays, shd, size_t(hc[1]) * sizeof(ae_packed_ray)));
-    AE_CUDA(ctx, copy(out->shadow_occluded, occ, hc[1]));
+    out->counts[1] = nSec;
+    out->counts[2] = nShd;
+    AE_CUDA(ctx, cudaStreamWaitEvent(cs, evSec, 0));
+    AE_CUDA(ctx, copy(out->secondary_rays, sec, size_t(nSec) * sizeof(ae_packed_ray)));
+    AE_CUDA(ctx, copy(out->secondary_hits, secHits, size_t(nSec) * sizeof(ae_hit)));
+    AE_CUDA(ctx, copy(out->shadow_rays, shd, size_t(nShd) * sizeof(ae_packed_ray)));
+    AE_CUDA(ctx, cudaStreamWaitEvent(cs, evShd, 0));
+    AE_CUDA(ctx, copy(out->shadow_occluded, occ, nShd));
+    AE_CUDA(ctx, cudaStreamSynchronize(cs));
     return ae_rt_synchronize(ctx, stream);
 }
 

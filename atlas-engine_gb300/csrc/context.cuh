@@ -78,6 +78,10 @@ struct ae_rt_ctx {
     // buffers of ae_rt_cast_pass
     atlas::rt::host::Scratch cast_primary, cast_primary_hits, cast_secondary, cast_secondary_hits, cast_shadow, cast_occluded;
     uint32_t* d_cast_counts = nullptr;
+    // result copies of ae_rt_cast_pass overlap the later stages on this stream
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t cast_events[4] = { nullptr, nullptr, nullptr, nullptr };
+    uint32_t* h_cast_counts = nullptr;  // pinned
     std::string last_error;
     std::mutex upload_mutex;
 };
