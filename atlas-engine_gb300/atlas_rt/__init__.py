@@ -259,6 +259,28 @@ class Context:
                                            _stream_handle(stream)), self._h)
         return out
 
+    def trace_scene_closest_transparency(self, rays, tmin, tmax, cull_mask=0xFFFFFFFF, out=None, stream=None,
+                                         n_rays: int | None = None):
+        """HitClosestTransparency over the scene (hits with opacity > 0)."""
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, HIT_DTYPE)
+        _check(lib().ae_rt_trace_scene_closest_transparency(self._h, _ptr(rays), n_rays, tmin, tmax, cull_mask,
+                                                            _ptr(out), _stream_handle(stream)), self._h)
+        return out
+
+    def trace_scene_any_transparency(self, rays, tmin, tmax, cull_mask=0xFFFFFFFF, out=None, stream=None,
+                                     n_rays: int | None = None):
+        """HitAnyTransparency over the scene: transparency per ray (1 = clear)."""
+        if n_rays is None:
+            n_rays = (rays.nbytes if isinstance(rays, np.ndarray) else rays.numel() * rays.element_size()) // 48
+        if out is None:
+            out = np.zeros(n_rays, np.float32)
+        _check(lib().ae_rt_trace_scene_any_transparency(self._h, _ptr(rays), n_rays, tmin, tmax, cull_mask,
+                                                        _ptr(out), _stream_handle(stream)), self._h)
+        return out
+
     def trace_scene_closest_queue(self, rays, count, capacity, tmin, tmax, hits, cull_mask=0xFFFFFFFF,
                                   stream=None):
         _check(lib().ae_rt_trace_scene_closest_queue(self._h, _ptr(rays), _ptr(count), capacity, tmin, tmax,

@@ -87,6 +87,8 @@ _SIGNATURES = [
     ("ae_rt_scene_build", C.c_int, [P, P, P, U32, P, P]),
     ("ae_rt_trace_scene_closest", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_scene_any", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_scene_closest_transparency", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
+    ("ae_rt_trace_scene_any_transparency", C.c_int, [P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_scene_closest_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_scene_any_queue", C.c_int, [P, P, P, U32, F32, F32, U32, P, P]),
     ("ae_rt_trace_batched", C.c_int, [P, P, U32, P]),

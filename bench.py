@@ -634,9 +634,8 @@ def main():
     ms_trace = float(np.mean(trace_ms))
     e2e = float(np.mean(e2e_ms))
     if world > 1:
-        t = torch.tensor([ms, e2e, ms_trace], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e, ms_trace = (float(x) for x in t.cpu())
+        from atlas_rt.distributed import max_over_ranks
+        ms, e2e, ms_trace = max_over_ranks([ms, e2e, ms_trace], device=dev)
     value = world * rays_per_step / (ms * 1e-3) / 1e6
     e2e_value = world * rays_per_step / (e2e * 1e-3) / 1e6
 

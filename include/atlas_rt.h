@@ -298,6 +298,21 @@ ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* ra
                                          uint32_t capacity, float tmin, float tmax, uint32_t cull_mask,
                                          uint8_t* occluded, void* stream);
 
+/* The transparency variants over the scene (every mesh needs its shading
+ * triangles; materials from ae_rt_scene_set_materials, or opacity 1 when
+ * none are set).  Opacity = GPUTriangle d2.w, or, when negative, the
+ * material's opacity (opacity textures are not sampled: factor 1).
+ * Replace HitClosestTransparency (bvh.hsh:275-357: only hits with opacity > 0
+ * count) and HitAnyTransparency (bvh.hsh:443-524: `transparency` receives
+ * the shader's return value, 1 = unoccluded, including its per-leaf
+ * re-multiplication, bvh.hsh:500).  Host or device buffers. */
+ae_rt_status ae_rt_trace_scene_closest_transparency(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays,
+                                                    float tmin, float tmax, uint32_t cull_mask, ae_hit* out,
+                                                    void* stream);
+ae_rt_status ae_rt_trace_scene_any_transparency(ae_rt_ctx* ctx, const ae_packed_ray* rays, uint32_t n_rays,
+                                                float tmin, float tmax, uint32_t cull_mask, float* transparency,
+                                                void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Batched multi-mesh traces in one persistent launch                        */
 /* ------------------------------------------------------------------------ */

@@ -285,7 +285,29 @@ typedef struct {
     const aeo_node* tlas; uint32_t n_tlas;
     const aeo_instance* inst; uint32_t n_inst;
     const aeo_mesh* meshes; uint32_t n_meshes;
+    const float* materials;   /* transparency variants: GPUMaterial (23 words); NULL: opaque queries */
 } scene_t;
+
+/* Leaf triangle of the transparency variants: UnpackTriangle of the shading
+ * triangle (common.hsh:17-44) -- vertices, endOfNode = d1.z > 0, opacity =
+ * d2.w -- and GetOpacity (surface.hsh:147-159) when the stored opacity is
+ * negative: the material's opacity times its opacity texture, which samples
+ * as 1.0 when absent (texture.hsh:18-25); bound textures are not sampled and
+ * count as 1.0 as well. */
+static inline float shading_opacity(const scene_t* sc, const float* s, int32_t materialOffset) {
+    if (s[23] >= 0.0f) return s[23];
+    int32_t idx;
+    memcpy(&idx, &s[15], 4);
+    const float* m = sc->materials + (size_t)(idx + materialOffset) * 23;
+    return 1.0f * m[7];
+}
+
+static inline aeo_tri shading_tri(const float* s) {
+    aeo_tri t;
+    memset(&t, 0, sizeof(t));
+    for (int k = 0; k < 3; k++) { t.v0[k] = s[k]; t.v1[k] = s[4 + k]; t.v2[k] = s[8 + k]; }
+    return t;
+}
 
 /* HitClosest -- bvh.hsh:191-273.  The TLAS/BLAS switch is keyed on the stack
  * depth at which the instance was entered (tlasIndex). */
@@ -336,13 +358,26 @@ static void scene_closest_one(const scene_t* sc, const float* r, uint32_t cull, 
                     int32_t tp = ~nodePtr;
                     int end = 0;
                     while (!end) {
-                        const aeo_tri* t = &mesh->tris[tp];
-                        end = t->v0[3] > 0.0f;
-                        triFetches++;
                         float st, su, sv;
-                        int hit = tri_test(o, d, t, &st, &su, &sv);
-                        if (hit && st > tMin && st < hitDist) {
-                            hitDist = st; hitID = tp; hu = su; hv = sv; hitInst = curInst;
+                        int hit;
+                        triFetches++;
+                        if (sc->materials) {
+                            /* CheckLeafClosestTransparency -- bvh.hsh:106-138 */
+                            const float* sh = mesh->shading + (size_t)tp * 24;
+                            const aeo_tri t = shading_tri(sh);
+                            end = sh[18] > 0.0f;
+                            hit = tri_test(o, d, &t, &st, &su, &sv);
+                            if (hit && st > tMin && st < hitDist &&
+                                shading_opacity(sc, sh, sc->inst[curInst].materialOffset) > 0.0f) {
+                                hitDist = st; hitID = tp; hu = su; hv = sv; hitInst = curInst;
+                            }
+                        } else {
+                            const aeo_tri* t = &mesh->tris[tp];
+                            end = t->v0[3] > 0.0f;
+                            hit = tri_test(o, d, t, &st, &su, &sv);
+                            if (hit && st > tMin && st < hitDist) {
+                                hitDist = st; hitID = tp; hu = su; hv = sv; hitInst = curInst;
+                            }
                         }
                         tp++;
                     }
@@ -432,9 +467,85 @@ static int scene_any_one(const scene_t* sc, const float* r, uint32_t cull, int32
     return hit;
 }
 
+/* HitAnyTransparency -- bvh.hsh:443-524 with CheckLeafTransparency :140-170.
+ * Every accepted triangle multiplies the leaf's running transparency, which
+ * starts from the current value; the leaf's result multiplies the current
+ * value again (transparency *= CheckLeafTransparency(..., transparency)),
+ * and values below 1e-6 become 0, which ends the traversal. */
+static float scene_any_transparency_one(const scene_t* sc, const float* r, uint32_t cull, int32_t* stack) {
+    v3 wo = ld3(r), wd = ld3(r + 3);
+    float tMin = r[6], tMax = r[7];
+    if (isnan3(wd)) return 1.0f;
+    float transparency = 1.0f;
+    if (!sc->n_tlas) return transparency;
+    v3 o = wo, d = wd;
+    const aeo_mesh* mesh = NULL;
+    int32_t matOffset = 0;
+    uint32_t sp = 1, tlasIndex = TLAS_INVALID;
+    int32_t nodePtr = 0;
+    stack[0] = 0;
+    while (sp != 0 && transparency > 0.0f) {
+        if (sp < tlasIndex) {
+            o = wo; d = wd;
+            tlasIndex = TLAS_INVALID;
+            if (nodePtr < 0) {
+                const aeo_instance* in = &sc->inst[~nodePtr];
+                o = xform(in, wo, 1.0f);
+                d = xform(in, wd, 0.0f);
+                mesh = &sc->meshes[in->meshOffset];
+                matOffset = in->materialOffset;
+                if ((in->mask & cull) > 0 && mesh->n_nodes > 0) {
+                    nodePtr = 0;
+                    tlasIndex = sp;
+                } else {
+                    nodePtr = stack[--sp];
+                }
+            } else {
+                const aeo_node* nd = &sc->tlas[nodePtr];
+                float dl, dr;
+                int il = box_glsl(o, d, tMin, tMax, nd->lmin, nd->lmax, &dl);
+                int ir = box_glsl(o, d, tMin, tMax, nd->rmin, nd->rmax, &dr);
+                int32_t next = il ? nd->left : nd->right;
+                if (!ir && !il) next = stack[--sp];
+                if (ir && il) stack[sp++] = nd->right;
+                nodePtr = next;
+            }
+        } else {
+            if (nodePtr < 0) {
+                int32_t tp = ~nodePtr;
+                int end = 0;
+                float leaf = transparency;
+                while (!end) {
+                    const float* sh = mesh->shading + (size_t)tp * 24;
+                    const aeo_tri t = shading_tri(sh);
+                    end = sh[18] > 0.0f;
+                    float st, su, sv;
+                    if (tri_test(o, d, &t, &st, &su, &sv) && st > tMin && st < tMax)
+                        leaf = leaf * (1.0f - shading_opacity(sc, sh, matOffset));
+                    tp++;
+                }
+                transparency = transparency * leaf;
+                if (transparency < 0.000001f) transparency = 0.0f;
+                nodePtr = stack[--sp];
+            } else {
+                const aeo_node* nd = &mesh->nodes[nodePtr];
+                float dl, dr;
+                int il = box_glsl(o, d, tMin, tMax, nd->lmin, nd->lmax, &dl);
+                int ir = box_glsl(o, d, tMin, tMax, nd->rmin, nd->rmax, &dr);
+                int32_t next = il ? nd->left : nd->right;
+                if (!ir && !il) next = stack[--sp];
+                if (ir && il) stack[sp++] = nd->right;
+                nodePtr = next;
+            }
+        }
+    }
+    return transparency;
+}
+
 typedef struct {
     const scene_t* sc; const float* rays; uint32_t begin, end; uint32_t cull; int any;
-    int32_t* ptr; int32_t* inst; float* tuv; uint8_t* occ; uint32_t* nf; uint32_t* tf; size_t stack_cap;
+    int32_t* ptr; int32_t* inst; float* tuv; uint8_t* occ; float* transparency; uint32_t* nf; uint32_t* tf;
+    size_t stack_cap;
 } scene_job_t;
 
 static void* run_scene_job(void* arg) {
@@ -442,7 +553,8 @@ static void* run_scene_job(void* arg) {
     int32_t* stack = (int32_t*)malloc(j->stack_cap * sizeof(int32_t));
     for (uint32_t i = j->begin; i < j->end; i++) {
         const float* r = j->rays + (size_t)i * 8;
-        if (j->any) j->occ[i] = (uint8_t)scene_any_one(j->sc, r, j->cull, stack);
+        if (j->transparency) j->transparency[i] = scene_any_transparency_one(j->sc, r, j->cull, stack);
+        else if (j->any) j->occ[i] = (uint8_t)scene_any_one(j->sc, r, j->cull, stack);
         else scene_closest_one(j->sc, r, j->cull, stack, &j->ptr[i], &j->inst[i], &j->tuv[(size_t)i * 3],
                                j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL);
     }
@@ -477,7 +589,7 @@ void aeo_scene_closest_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_ins
                             const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
                             uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out, float* tuv,
                             uint32_t* node_fetches, uint32_t* tri_fetches) {
-    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, NULL };
     scene_job_t p; memset(&p, 0, sizeof(p));
     p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 0; p.ptr = tri_ptr; p.inst = inst_out; p.tuv = tuv;
     p.nf = node_fetches; p.tf = tri_fetches; p.stack_cap = scene_stack_cap(&sc);
@@ -487,9 +599,32 @@ void aeo_scene_closest_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_ins
 void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, uint32_t n_inst,
                         const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
                         uint32_t cull_mask, int threads, uint8_t* occluded) {
-    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, NULL };
     scene_job_t p; memset(&p, 0, sizeof(p));
     p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 1; p.occ = occluded; p.stack_cap = scene_stack_cap(&sc);
+    run_scene(p, n_rays, threads);
+}
+
+void aeo_scene_closest_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
+                                         uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
+                                         const float* materials, const float* rays, uint32_t n_rays,
+                                         uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out,
+                                         float* tuv) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials };
+    scene_job_t p; memset(&p, 0, sizeof(p));
+    p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 0; p.ptr = tri_ptr; p.inst = inst_out; p.tuv = tuv;
+    p.stack_cap = scene_stack_cap(&sc);
+    run_scene(p, n_rays, threads);
+}
+
+void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
+                                     uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
+                                     const float* materials, const float* rays, uint32_t n_rays,
+                                     uint32_t cull_mask, int threads, float* transparency) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials };
+    scene_job_t p; memset(&p, 0, sizeof(p));
+    p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 1; p.transparency = transparency;
+    p.stack_cap = scene_stack_cap(&sc);
     run_scene(p, n_rays, threads);
 }
 
@@ -952,7 +1087,7 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    int threads, double* accum) {
     pt_job_t proto;
     memset(&proto, 0, sizeof(proto));
-    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes };
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, NULL };
     proto.sc = sc;
     proto.inst_model = inst_model;
     proto.materials = materials;

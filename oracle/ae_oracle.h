@@ -105,6 +105,23 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum);
 
+/* The transparency variants over TLAS + BLASes (meshes need `shading`):
+ * HitClosestTransparency (bvh.hsh:275-357: a hit counts only where the
+ * triangle's opacity is > 0) and HitAnyTransparency (bvh.hsh:443-524: the
+ * returned transparency, 1 = unoccluded).  Opacity: GPUTriangle d2.w, or,
+ * when negative, the material's opacity (materials: GPUMaterial, 23 words,
+ * indexed by the triangle's material index + the instance's materialOffset);
+ * opacity textures are not sampled (factor 1). */
+void aeo_scene_closest_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
+                                         uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
+                                         const float* materials, const float* rays, uint32_t n_rays,
+                                         uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out,
+                                         float* tuv);
+void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
+                                     uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
+                                     const float* materials, const float* rays, uint32_t n_rays,
+                                     uint32_t cull_mask, int threads, float* transparency);
+
 /* Exact-as-possible nearest hit in double precision by brute force over every
  * triangle (for small cases and for re-testing near ties): the double-precision
  * form of the same triangle test, accepting tmin < t < tmax.  t2 = second

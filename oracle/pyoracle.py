@@ -64,6 +64,10 @@ def port():
                                     C.c_float, C.c_int, P]
         L.aeo_pathtrace.restype = None
         L.aeo_scene_any_glsl.restype = None
+        L.aeo_scene_closest_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, P, U32, U32, C.c_int, P, P, P]
+        L.aeo_scene_closest_transparency_glsl.restype = None
+        L.aeo_scene_any_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, P, U32, U32, C.c_int, P]
+        L.aeo_scene_any_transparency_glsl.restype = None
         for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
             f.restype = None
         _port = L
@@ -221,6 +225,40 @@ def scene_any_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, thr
                               inst.ctypes.data, len(inst), table, len(meshes), rays8.ctypes.data, n,
                               cull_mask, threads, occ.ctypes.data)
     return occ
+
+
+def scene_closest_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, cull_mask=0xFFFFFFFF,
+                                    threads=os.cpu_count()):
+    """HitClosestTransparency (bvh.hsh:275-357); meshes carry shading
+    triangles, materials is the GPUMaterial array."""
+    n = len(rays8)
+    tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
+    inst = np.ascontiguousarray(instances)
+    mats = np.ascontiguousarray(materials)
+    table, keep = _mesh_table(meshes)
+    ptr = np.empty(n, np.int32)
+    ino = np.empty(n, np.int32)
+    tuv = np.empty((n, 3), np.float32)
+    port().aeo_scene_closest_transparency_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
+                                               inst.ctypes.data, len(inst), table, len(meshes), mats.ctypes.data,
+                                               rays8.ctypes.data, n, cull_mask, threads, ptr.ctypes.data,
+                                               ino.ctypes.data, tuv.ctypes.data)
+    return ptr, ino, tuv
+
+
+def scene_any_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, cull_mask=0xFFFFFFFF,
+                                threads=os.cpu_count()):
+    """HitAnyTransparency (bvh.hsh:443-524): transparency per ray (1 = clear)."""
+    n = len(rays8)
+    tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
+    inst = np.ascontiguousarray(instances)
+    mats = np.ascontiguousarray(materials)
+    table, keep = _mesh_table(meshes)
+    out = np.empty(n, np.float32)
+    port().aeo_scene_any_transparency_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
+                                           inst.ctypes.data, len(inst), table, len(meshes), mats.ctypes.data,
+                                           rays8.ctypes.data, n, cull_mask, threads, out.ctypes.data)
+    return out
 
 
 def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, width, height, spp,
