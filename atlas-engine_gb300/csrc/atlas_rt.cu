@@ -154,6 +154,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     AE_CUDA(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
+    p.refill_below = ctx->refill_below;
     void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
@@ -303,6 +304,8 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     ctx->max_steps_cfg = c.max_steps;
     ctx->count_fetches = (c.flags & AE_RT_CFG_COUNT_FETCHES) != 0;
     ctx->refill_steps = c.refill_steps;
+    ctx->refill_below = c.refill_below == 0 ? atlas::rt::dev::kDefaultRefillBelow
+                                            : (c.refill_below > 32 ? 0u : c.refill_below);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 2 * sizeof(uint32_t));
@@ -606,6 +609,7 @@ TraceParams BatchParams(ae_rt_ctx* ctx, const atlas::rt::dev::BatchDesc* d_batch
     p.batches = d_batches;
     p.n_batches = n;
     p.refill_steps = ctx->refill_steps;
+    p.refill_below = ctx->refill_below;
     p.max_steps = 0xffffffffu;
     return p;
 }

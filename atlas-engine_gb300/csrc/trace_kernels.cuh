@@ -74,6 +74,7 @@ struct TraceParams {
     const struct BatchDesc* batches;
     uint32_t n_batches;
     uint32_t refill_steps;       // traversal steps between warp refills
+    uint32_t refill_below;       // refill early when fewer lanes than this still traverse (0: never)
     uint32_t per_ray_tmax;       // nonzero: a ray's tmax is its PackedRay hit.x (shadow queues)
 };
 
@@ -94,6 +95,11 @@ struct BatchDesc {
     uint32_t max_steps;
 };
 static_assert(sizeof(BatchDesc) == 64, "batch descriptor layout");
+
+// ae_rt_config::refill_below when left 0 (lanes; 0 = never refill early):
+// measured best with a 32-step burst on the terrain + boxes camera pass
+// (0.913 against 0.974 ms for 64 steps and no early refill).
+constexpr uint32_t kDefaultRefillBelow = 8;
 
 constexpr int MODE_MESH = 0;     // one BLAS
 constexpr int MODE_SCENE = 1;    // TLAS over instances
@@ -299,7 +305,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     unsigned long long nodeCount = 0, triCount = 0;
     const uint32_t nRays = p.n_rays_dev ? min(*p.n_rays_dev, p.n_rays) : p.n_rays;
     const uint32_t nTop = TLAS ? p.n_tlas : p.n_nodes;
-    const int refill = p.refill_steps ? int(p.refill_steps) : 64;
+    const int refill = p.refill_steps ? int(p.refill_steps) : 32;
+    const uint32_t refillBelow = p.refill_below;
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
@@ -357,6 +364,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
             const bool anyQ = ANY || (BATCH && laneAny);
             bool done = node == INT32_MIN;
             for (int k = 0; k < refill && !done; k++) {
+                // dynamic fetch: leave the burst for a refill once too few lanes
+                // are still traversing (while the queue still has rays)
+                if (refillBelow && !queueDry && uint32_t(__popc(__activemask())) < refillBelow) break;
                 if (++steps > maxSteps) {
                     flags |= kHitFlagIterCap;
                     atomicOr(p.error_word, kErrIterationCap);

@@ -226,9 +226,10 @@ typedef struct ae_rt_config {
     uint32_t threads_per_block;   /* 0 = 128 */
     uint32_t max_steps;           /* traversal step cap per ray (0 = 4 x nodes + 64) */
     uint32_t flags;               /* AE_RT_CFG_* */
-    uint32_t refill_steps;        /* traversal steps between warp refills (0 = 64) */
+    uint32_t refill_steps;        /* traversal steps between warp refills (0 = 32) */
     uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
-    uint32_t reserved;
+    uint32_t refill_below;        /* also refill as soon as fewer than this many lanes of a warp
+                                     are still traversing (1..32; 0 = the default; > 32 = never) */
 } ae_rt_config;
 
 ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out);
