@@ -199,6 +199,36 @@ class Context:
                                          _stream_handle(stream)), self._h)
         return out
 
+    def build_mesh(self, verts, material=None, opacity=None, stream=None):
+        """GPU BVH build of a triangle mesh (verts (n, 3, 3) float32, host or
+        device); returns (mesh_id, order) with order[i] the input index of
+        BVH-order triangle i (numpy)."""
+        if isinstance(verts, np.ndarray):
+            verts = np.ascontiguousarray(verts, np.float32)
+            n = verts.size // 9
+        else:
+            n = verts.numel() // 9
+        if material is not None and isinstance(material, np.ndarray):
+            material = np.ascontiguousarray(material, np.int32)
+        if opacity is not None and isinstance(opacity, np.ndarray):
+            opacity = np.ascontiguousarray(opacity, np.float32)
+        order = np.zeros(max(n, 2 if n == 1 else 0), np.uint32)
+        mid = C.c_int32()
+        _check(lib().ae_rt_mesh_build(self._h, _ptr(verts) if n else None, n, _ptr(material), _ptr(opacity),
+                                      C.byref(mid), _ptr(order) if len(order) else None, _stream_handle(stream)),
+               self._h)
+        return mid.value, order
+
+    def mesh_bvh(self, mesh: int):
+        """(nodes NODE_DTYPE, bvh_tris (n, 12) float32) of a mesh of this context."""
+        nn, nt = C.c_uint32(), C.c_uint32()
+        _check(lib().ae_rt_mesh_get_bvh(self._h, mesh, None, None, C.byref(nn), C.byref(nt)), self._h)
+        nodes = np.zeros(nn.value, NODE_DTYPE)
+        tris = np.zeros((nt.value, 12), np.float32)
+        _check(lib().ae_rt_mesh_get_bvh(self._h, mesh, _ptr(nodes) if nn.value else None,
+                                        _ptr(tris) if nt.value else None, None, None), self._h)
+        return nodes, tris
+
     def retest_near_ties(self, mesh: int, rays, hits, tmin: float, tmax: float, out, n_rays: int | None = None,
                          stream=None) -> int:
         """FP64 re-test of the rays flagged HIT_FLAG_NEAR_TIE (device buffers:

@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline pass only (no extra workloads)")
     ap.add_argument("--autotune", action="store_true", help="re-run the launch-parameter autotuner")
-    ap.add_argument("--workloads", default="random65536,batched64,pathtrace,radiance_cache",
+    ap.add_argument("--workloads", default="random65536,batched64,bvh_build,pathtrace,radiance_cache",
                     help="comma-separated extra workloads (radiance_cache needs pathtrace)")
     ap.add_argument("--pt-ref-spp", type=int, default=4096, help="samples of the converged image")
     ap.add_argument("--rc-max-frames", type=int, default=320, help="frame cap of the radiance-cache run")
@@ -371,6 +371,60 @@ def workload_batched(torch, dev, stream, flush, steps, autotune=False, log=None)
             "speedup_vs_per_scene": per_ms / graph_ms, "tuning": tuning_info}
 
 
+def workload_bvh_build(torch, dev, stream, flush, reps=5):
+    """GPU BVH build (ae_rt_mesh_build, linear BVH) of the terrain + boxes
+    mesh and of the 65,536 random triangles, vertices already on the device:
+    wall time of the call (it returns after the build), against the engine's
+    own CPU builder (the library's byte-identical restatement, parallel, all
+    host threads) on the same mesh; and the camera pass's primary closest-hit
+    trace on each tree."""
+    import atlas_rt
+    from atlas_rt import BVH, scenes
+    out = {}
+    for name, verts in (("terrain_boxes", scenes.terrain_boxes()[0]), ("random65536", scenes.random_triangles())):
+        ctx = atlas_rt.Context(device=dev.index or 0)
+        dv = torch.from_numpy(verts).to(dev)
+        ctx.build_mesh(dv)                       # warm-up
+        ms = []
+        for _ in range(reps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            mid, _ = ctx.build_mesh(dv)
+            ms.append((time.perf_counter() - t0) * 1e3)
+        cpu = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            b = BVH(verts)
+            cpu.append(time.perf_counter() - t0)
+        rec = {"triangles": int(len(verts)), "gpu_build_ms": float(np.median(ms)),
+               "cpu_build_ms": float(min(cpu) * 1e3), "cpu_threads": os.cpu_count(),
+               "speedup": float(min(cpu) * 1e3 / np.median(ms))}
+        if name == "terrain_boxes":
+            gt = b.pack_triangles()
+            mid_sah = ctx.upload_mesh(b.nodes, gt)
+            cam = atlas_rt.make_camera(scenes.pinhole_camera(W, H))
+            n = W * H
+            rays = torch.empty((n, 12), dtype=torch.float32, device=dev)
+            hits = torch.empty((n, 8), dtype=torch.float32, device=dev)
+            ctx.raygen(cam, rays, stream)
+            for tag, m in (("lbvh", mid), ("sah", mid_sah)):
+                for _ in range(3):
+                    ctx.trace_closest(m, rays, TMIN, TINF, out=hits, stream=stream, n_rays=n)
+                tt = []
+                for k in range(reps):
+                    flush.fill_(k & 0xFF)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    ctx.trace_closest(m, rays, TMIN, TINF, out=hits, stream=stream, n_rays=n)
+                    e1.record(stream)
+                    torch.cuda.synchronize(dev)
+                    tt.append(e0.elapsed_time(e1))
+                rec[f"primary_closest_mrays_s_{tag}"] = n / (float(np.median(tt)) * 1e-3) / 1e6
+        ctx.close()
+        out[name] = rec
+    return out
+
+
 def pt_context(dev):
     """Context + uploaded path-tracing scene (terrain + boxes + 4x4 light)."""
     import atlas_rt
@@ -675,6 +729,8 @@ def main():
             line["workloads"]["batched64"] = workload_batched(torch, dev, stream, flush, max(args.steps // 2, 3),
                                                               autotune=args.autotune,
                                                               log=(lambda m: print(m, file=sys.stderr)))
+        if "bvh_build" in wl:
+            line["workloads"]["bvh_build"] = workload_bvh_build(torch, dev, stream, flush)
         if "pathtrace" in wl:
             pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp)
             line["workloads"]["pathtrace"] = pt

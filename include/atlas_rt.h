@@ -563,6 +563,27 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
 ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
                           void* stream);
 
+/* GPU BVH build: a linear BVH (Morton order of triangle centroids, Karras's
+ * parallel hierarchy, bounds bottom-up) built on the device and registered
+ * as a mesh of the context, in the engine's GPUBVHNode / GPUBVHTriangle
+ * layouts (one triangle per leaf; root = node 0; n - 1 nodes for n >= 2).
+ * verts: n * 9 floats (v0, v1, v2); material / opacity: optional, per input
+ * triangle; order_out (optional, n entries, or 2 for n == 1) receives the
+ * input index of each BVH-order triangle.  Host or device buffers; returns
+ * after the build.  The engine builds on the CPU (Volume::BVH, BVH.cpp:14;
+ * MeshData::BuildBVH, MeshData.cpp:63-271): this is the GPU alternative, not
+ * a reproduction of that tree -- traces on it return the same nearest
+ * distance for every ray, and the same triangle except between triangles at
+ * exactly equal distance. */
+ae_rt_status ae_rt_mesh_build(ae_rt_ctx* ctx, const float* verts, uint32_t n, const int32_t* material,
+                              const float* opacity, int32_t* mesh_id, uint32_t* order_out, void* stream);
+
+/* The BVH of a mesh of the context (uploaded or built) back into host or
+ * device memory; n_nodes / n_tris (optional) receive the counts; nodes / tris
+ * may be NULL to query them. */
+ae_rt_status ae_rt_mesh_get_bvh(ae_rt_ctx* ctx, int32_t mesh, ae_bvh_node* nodes, ae_bvh_triangle* tris,
+                                uint32_t* n_nodes, uint32_t* n_tris);
+
 /* Double-precision re-test of near ties.  For every ray whose ae_hit (from
  * ae_rt_trace_closest / _queue on the same mesh, tmin and tmax) carries
  * AE_HIT_NEAR_TIE, the nearest triangle is searched again in double precision:
