@@ -499,6 +499,15 @@ class RadianceCache:
                self.ctx.handle)
         return loss.value if want_loss else None
 
+    def frame(self, cam: Camera, frame: int, accum, n_paths=65536, steps=2, max_bounces=3, last_bounce=2,
+              want_loss=False, stream=None):
+        """ae_rc_frame: render one sample per pixel with the current cache while
+        the frame's training paths are traced beside it, then train."""
+        loss = C.c_float()
+        _check(lib().ae_rc_frame(self._h, C.byref(cam), frame, n_paths, steps, max_bounces, last_bounce, _ptr(accum),
+                                 C.byref(loss) if want_loss else None, _stream_handle(stream)), self.ctx.handle)
+        return loss.value if want_loss else None
+
     def render(self, cam: Camera, frame: int, accum, last_bounce=2, stream=None):
         _check(lib().ae_rc_render(self._h, C.byref(cam), frame, last_bounce, _ptr(accum), _stream_handle(stream)),
                self.ctx.handle)

@@ -83,6 +83,7 @@ _SIGNATURES = [
     ("ae_rt_trace_closest", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
     ("ae_rt_retest_near_ties", C.c_int, [P, I32, P, P, U32, F32, F32, P, C.POINTER(U32), P]),
     ("ae_rt_mesh_build", C.c_int, [P, P, U32, P, P, C.POINTER(I32), P, P]),
+    ("ae_rc_frame", C.c_int, [P, P, U32, U32, U32, U32, U32, P, P, P]),
     ("ae_rt_mesh_get_bvh", C.c_int, [P, I32, P, P, C.POINTER(U32), C.POINTER(U32)]),
     ("ae_rt_trace_any", C.c_int, [P, I32, P, U32, F32, F32, P, P]),
     ("ae_rt_scene_set", C.c_int, [P, P, U32, P, U32]),

@@ -4,6 +4,7 @@
 #include "atlas_rt.h"
 #include "context.cuh"
 #include "rc_kernels.cuh"
+#include "rc_tc_kernels.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -36,12 +37,14 @@ struct ae_rc {
     int sm_count = 0;
     float scale = 1.0f;            // radiance scale of the stored values
     uint32_t max_bounces = 3;      // bounce budget of the most recent training frame
+    // work that overlaps the render: [0] first-vertex inference, [1] training paths
+    cudaStream_t aux[2] = { nullptr, nullptr };
+    cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr };
 };
 
 namespace {
 
 constexpr size_t kTrainSmem = RC_WBYTES + (RC_HIDDEN + 1) * RC_ABYTES + 2 * RC_ABYTES;
-constexpr size_t kInferSmem = RC_WBYTES + RC_ABYTES;
 
 ae_rt_status RcFail(ae_rc* rc, ae_rt_status s, const std::string& m) { return Fail(rc ? rc->ctx : nullptr, s, m); }
 
@@ -57,6 +60,7 @@ RcMlpParams MlpParams(ae_rc* rc) {
     p.weights = rc->mlp_bf16;
     p.grad_w = rc->mlp_grad;
     p.loss = rc->d_loss;
+    p.error_word = rc->ctx->d_counter + 1;
     return p;
 }
 
@@ -116,6 +120,10 @@ void Destroy(ae_rc* rc) {
         cudaFree(p);
     rc->samples.release();
     rc->queries.release();
+    for (cudaEvent_t e : rc->ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : rc->aux)
+        if (st) cudaStreamDestroy(st);
     delete rc;
 }
 
@@ -137,6 +145,196 @@ ae_rt_status UploadParams(ae_rc* rc, const float* mlp, const float* grid) {
 }
 
 bool DevPtr(const void* p) { return IsDevicePointer(p); }
+
+ae_rt_status EnsureStreams(ae_rc* rc) {
+    for (cudaStream_t& st : rc->aux)
+        if (!st) RC_CUDA(rc, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : rc->ev)
+        if (!e) RC_CUDA(rc, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return AE_RT_OK;
+}
+
+CameraParams CamParams(const ae_camera* cam) {
+    CameraParams c{};
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+    return c;
+}
+
+// The self-generated training records of one frame into rc->samples (count
+// in d_counts[0]).  Reads the scene only, never the cache.
+ae_rt_status GeneratePaths(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t max_bounces,
+                           cudaStream_t s) {
+    ae_rt_ctx* ctx = rc->ctx;
+    RC_CUDA(rc, rc->samples.ensure(size_t(n_paths) * RC_MAX_DEPTH * 64));
+    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts, 0, sizeof(uint32_t), s));
+    RcPathParams pp{};
+    pp.tp.tlas = ctx->d_tlas;
+    pp.tp.n_tlas = ctx->n_tlas;
+    pp.tp.instances = ctx->d_instances;
+    pp.tp.n_instances = ctx->n_instances;
+    pp.tp.meshes = ctx->d_mesh_table;
+    pp.tp.n_meshes = ctx->n_mesh_table;
+    pp.tp.max_steps = ctx->scene_steps;
+    pp.sc.instances = ctx->d_instances;
+    pp.sc.inst_model = ctx->d_inst_model;
+    pp.sc.meshes = ctx->d_mesh_table;
+    pp.sc.materials = ctx->d_materials;
+    pp.sc.n_materials = ctx->n_materials;
+    pp.sc.lights = ctx->d_lights;
+    pp.sc.n_lights = ctx->n_lights;
+    pp.cam = CamParams(cam);
+    pp.n_paths = n_paths;
+    pp.frame = frame;
+    pp.seed = rc->cfg.seed;
+    pp.max_bounces = max_bounces;
+    pp.epsilon = 0.1f;
+    pp.scale = rc->scale;
+    pp.samples = static_cast<float4*>(rc->samples.ptr);
+    pp.n_samples = rc->d_counts;
+    rc_paths_kernel<<<(n_paths + 127) / 128, 128, 0, s>>>(pp);
+    RC_CUDA(rc, cudaGetLastError());
+    return AE_RT_OK;
+}
+
+// The records in `steps` equal slices (count on the device), one Adam step each.
+ae_rt_status TrainSteps(ae_rc* rc, uint32_t n_paths, uint32_t steps, float* loss_out, cudaStream_t s) {
+    for (uint32_t k = 0; k < steps; k++) {
+        ae_rt_status st = Backprop(rc, static_cast<const float4*>(rc->samples.ptr), n_paths * RC_MAX_DEPTH,
+                                   rc->d_counts, k, steps, s);
+        if (st != AE_RT_OK) return st;
+        st = AdamStep(rc, s);
+        if (st != AE_RT_OK) return st;
+    }
+    if (loss_out) {
+        float l = 0.0f;
+        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(rc, cudaStreamSynchronize(s));
+        *loss_out = l;
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status CheckTrainArgs(ae_rc* rc, const ae_camera* cam, uint32_t n_paths, uint32_t steps, uint32_t max_bounces) {
+    ae_rt_ctx* ctx = rc->ctx;
+    if (!cam) return AE_RT_INVALID_ARG;
+    if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
+    if (n_paths == 0 || steps == 0 || n_paths < steps) return RcFail(rc, AE_RT_INVALID_ARG, "bad training sizes");
+    if (max_bounces == 0 || max_bounces > 16) return RcFail(rc, AE_RT_INVALID_ARG, "max_bounces out of range");
+    return AE_RT_OK;
+}
+
+// One sample per pixel with paths ending in the cache (see ae_rc_render).
+// The cache queries of the first vertex are answered on rc->aux[0] while the
+// later bounces (glossy continuations, a few percent of the pixels, whose
+// time is set by their longest rays) are traced on `s`: the two write
+// disjoint pixels of accum (a path that ends in a query at the first vertex
+// adds nothing later).  Joined before returning.
+ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
+                         cudaStream_t s) {
+    ae_rt_ctx* ctx = rc->ctx;
+    const uint32_t n = cam->width * cam->height;
+    for (int k = 0; k < 2; k++) {
+        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
+        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
+    }
+    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
+    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
+    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
+    RC_CUDA(rc, ctx->pt_occ.ensure(n));
+    RC_CUDA(rc, rc->queries.ensure(size_t(n) * 64));
+    if (!ctx->d_pt_counts) RC_CUDA(rc, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+    ae_rt_status st = EnsureStreams(rc);
+    if (st != AE_RT_OK) return st;
+    void* stream = s;
+
+    const CameraParams c = CamParams(cam);
+    RcShadeParams rp{};
+    PtParams& p = rp.pt;
+    p.sc.instances = ctx->d_instances;
+    p.sc.inst_model = ctx->d_inst_model;
+    p.sc.meshes = ctx->d_mesh_table;
+    p.sc.materials = ctx->d_materials;
+    p.sc.n_materials = ctx->n_materials;
+    p.sc.lights = ctx->d_lights;
+    p.sc.n_lights = ctx->n_lights;
+    p.width = cam->width;
+    p.height = cam->height;
+    p.max_bounces = rc->max_bounces;
+    p.epsilon = 0.1f;
+    p.seed = rc->cfg.seed + 17u;
+    p.sample = frame;
+    p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
+    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
+    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
+    p.n_shadow = ctx->d_pt_counts + 2;
+    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
+    p.accum = reinterpret_cast<float4*>(accum);
+    rp.queries = static_cast<float4*>(rc->queries.ptr);
+    rp.n_queries = rc->d_counts + 1;
+    rp.last_bounce = last_bounce;
+    rp.inv_scale = 1.0f / rc->scale;
+    rp.rough_cut = rc->cfg.rough_cut > 0.0f ? rc->cfg.rough_cut : 0.35f;
+    const uint32_t blocks = (n + 255) / 256;
+    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts + 1, 0, sizeof(uint32_t), s));
+    p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
+    p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
+    p.n_out = ctx->d_pt_counts + 0;
+    pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
+    RC_CUDA(rc, cudaGetLastError());
+    RcMlpParams mp = MlpParams(rc);
+    mp.recs = static_cast<const float4*>(rc->queries.ptr);
+    mp.n = n;
+    mp.accum = reinterpret_cast<float4*>(accum);
+    cudaStream_t a0 = rc->aux[0];
+    const uint32_t final_bounce = last_bounce < rc->max_bounces ? last_bounce : rc->max_bounces;
+    for (uint32_t b = 0; b <= final_bounce; b++) {
+        const int in = int(b & 1), out = 1 - in;
+        p.bounce = b;
+        p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
+        p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
+        p.n_in = ctx->d_pt_counts + in;
+        p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
+        p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
+        p.n_out = ctx->d_pt_counts + out;
+        st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n, 0.0f, 1e12f,
+                             ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
+        if (st != AE_RT_OK) return st;
+        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
+        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
+        rc_shade_kernel<<<blocks, 256, 0, s>>>(rp);
+        RC_CUDA(rc, cudaGetLastError());
+        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, 1e12f,
+                             ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
+        if (st != AE_RT_OK) return st;
+        pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
+        RC_CUDA(rc, cudaGetLastError());
+        if (b == 0) {
+            // the first vertex's queries, answered on the side stream once
+            // every write of this vertex into accum is done
+            RC_CUDA(rc, cudaMemcpyAsync(rc->d_counts + 2, rc->d_counts + 1, sizeof(uint32_t),
+                                        cudaMemcpyDeviceToDevice, s));
+            RC_CUDA(rc, cudaEventRecord(rc->ev[0], s));
+            RC_CUDA(rc, cudaStreamWaitEvent(a0, rc->ev[0], 0));
+            RcMlpParams m0 = mp;
+            m0.n_dev = rc->d_counts + 2;
+            rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RCT_THREADS, RCT_SMEM, a0>>>(m0);
+            RC_CUDA(rc, cudaGetLastError());
+            RC_CUDA(rc, cudaEventRecord(rc->ev[1], a0));
+        }
+    }
+    // the queries of the later vertices (after the first vertex's ones)
+    RcMlpParams m1 = mp;
+    m1.n_dev = rc->d_counts + 1;
+    m1.offset_dev = rc->d_counts + 2;
+    rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RCT_THREADS, RCT_SMEM, s>>>(m1);
+    RC_CUDA(rc, cudaGetLastError());
+    RC_CUDA(rc, cudaStreamWaitEvent(s, rc->ev[1], 0));
+    return AE_RT_OK;
+}
 
 }  // namespace
 
@@ -194,9 +392,11 @@ ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out) 
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(rc_mlp_kernel<RC_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmem));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rc_mlp_kernel<RC_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem));
+        e = cudaFuncSetAttribute(rc_infer_tc_kernel<RC_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(RCT_SMEM));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rc_mlp_kernel<RC_PREDICT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem));
+        e = cudaFuncSetAttribute(rc_infer_tc_kernel<RC_PREDICT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(RCT_SMEM));
     if (e != cudaSuccess) {
         Destroy(rc);
         return CudaFail(ctx, e, "radiance cache allocation");
@@ -260,7 +460,7 @@ ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* o
     p.recs = reinterpret_cast<const float4*>(queries);
     p.n = n;
     p.out = reinterpret_cast<float4*>(out);
-    rc_mlp_kernel<RC_PREDICT><<<GridBlocks(rc, n), RC_THREADS, kInferSmem, static_cast<cudaStream_t>(stream)>>>(p);
+    rc_infer_tc_kernel<RC_PREDICT><<<GridBlocks(rc, n) * 3, RCT_THREADS, RCT_SMEM, static_cast<cudaStream_t>(stream)>>>(p);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
 }
@@ -305,63 +505,15 @@ ae_rt_status ae_rc_train_batch(ae_rc* rc, const float* samples, uint32_t n, floa
 
 ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
                                uint32_t max_bounces, float* loss_out, void* stream) {
-    if (!rc || !cam) return AE_RT_INVALID_ARG;
-    ae_rt_ctx* ctx = rc->ctx;
-    if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
-    if (n_paths == 0 || steps == 0 || n_paths < steps) return RcFail(rc, AE_RT_INVALID_ARG, "bad training sizes");
-    RC_CUDA(rc, cudaSetDevice(ctx->device));
+    if (!rc) return AE_RT_INVALID_ARG;
+    ae_rt_status st = CheckTrainArgs(rc, cam, n_paths, steps, max_bounces);
+    if (st != AE_RT_OK) return st;
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (max_bounces == 0 || max_bounces > 16) return RcFail(rc, AE_RT_INVALID_ARG, "max_bounces out of range");
-    RC_CUDA(rc, rc->samples.ensure(size_t(n_paths) * RC_MAX_DEPTH * 64));
-    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts, 0, sizeof(uint32_t), s));
-    RcPathParams pp{};
-    pp.tp.tlas = ctx->d_tlas;
-    pp.tp.n_tlas = ctx->n_tlas;
-    pp.tp.instances = ctx->d_instances;
-    pp.tp.n_instances = ctx->n_instances;
-    pp.tp.meshes = ctx->d_mesh_table;
-    pp.tp.n_meshes = ctx->n_mesh_table;
-    pp.tp.max_steps = ctx->scene_steps;
-    pp.sc.instances = ctx->d_instances;
-    pp.sc.inst_model = ctx->d_inst_model;
-    pp.sc.meshes = ctx->d_mesh_table;
-    pp.sc.materials = ctx->d_materials;
-    pp.sc.n_materials = ctx->n_materials;
-    pp.sc.lights = ctx->d_lights;
-    pp.sc.n_lights = ctx->n_lights;
-    CameraParams& c = pp.cam;
-    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
-    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
-    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
-    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
-    c.width = cam->width; c.height = cam->height;
-    pp.n_paths = n_paths;
-    pp.frame = frame;
-    pp.seed = rc->cfg.seed;
-    pp.max_bounces = max_bounces;
-    pp.epsilon = 0.1f;
-    pp.scale = rc->scale;
-    pp.samples = static_cast<float4*>(rc->samples.ptr);
-    pp.n_samples = rc->d_counts;
-    rc_paths_kernel<<<(n_paths + 127) / 128, 128, 0, s>>>(pp);
-    RC_CUDA(rc, cudaGetLastError());
+    st = GeneratePaths(rc, cam, frame, n_paths, max_bounces, s);
+    if (st != AE_RT_OK) return st;
     rc->max_bounces = max_bounces;
-    // the records (up to RC_MAX_DEPTH per path; count on the device) in
-    // `steps` equal slices, one Adam step each
-    for (uint32_t k = 0; k < steps; k++) {
-        ae_rt_status st = Backprop(rc, static_cast<const float4*>(rc->samples.ptr), n_paths * RC_MAX_DEPTH,
-                                   rc->d_counts, k, steps, s);
-        if (st != AE_RT_OK) return st;
-        st = AdamStep(rc, s);
-        if (st != AE_RT_OK) return st;
-    }
-    if (loss_out) {
-        float l = 0.0f;
-        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
-        RC_CUDA(rc, cudaStreamSynchronize(s));
-        *loss_out = l;
-    }
-    return AE_RT_OK;
+    return TrainSteps(rc, n_paths, steps, loss_out, s);
 }
 
 ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
@@ -371,89 +523,31 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
     if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
     if (!DevPtr(accum)) return RcFail(rc, AE_RT_INVALID_ARG, "accumulation buffer must be device memory");
     RC_CUDA(rc, cudaSetDevice(ctx->device));
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const uint32_t n = cam->width * cam->height;
-    for (int k = 0; k < 2; k++) {
-        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
-        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
-    }
-    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
-    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
-    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
-    RC_CUDA(rc, ctx->pt_occ.ensure(n));
-    RC_CUDA(rc, rc->queries.ensure(size_t(n) * 64));
-    if (!ctx->d_pt_counts) RC_CUDA(rc, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+    return RenderFrame(rc, cam, frame, last_bounce, accum, static_cast<cudaStream_t>(stream));
+}
 
-    CameraParams c{};
-    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
-    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
-    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
-    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
-    c.width = cam->width; c.height = cam->height;
-    RcShadeParams rp{};
-    PtParams& p = rp.pt;
-    p.sc.instances = ctx->d_instances;
-    p.sc.inst_model = ctx->d_inst_model;
-    p.sc.meshes = ctx->d_mesh_table;
-    p.sc.materials = ctx->d_materials;
-    p.sc.n_materials = ctx->n_materials;
-    p.sc.lights = ctx->d_lights;
-    p.sc.n_lights = ctx->n_lights;
-    p.width = cam->width;
-    p.height = cam->height;
-    p.max_bounces = rc->max_bounces;
-    p.epsilon = 0.1f;
-    p.seed = rc->cfg.seed + 17u;
-    p.sample = frame;
-    p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
-    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
-    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
-    p.n_shadow = ctx->d_pt_counts + 2;
-    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
-    p.accum = reinterpret_cast<float4*>(accum);
-    rp.queries = static_cast<float4*>(rc->queries.ptr);
-    rp.n_queries = rc->d_counts + 1;
-    rp.last_bounce = last_bounce;
-    rp.inv_scale = 1.0f / rc->scale;
-    rp.rough_cut = rc->cfg.rough_cut > 0.0f ? rc->cfg.rough_cut : 0.35f;
-    const uint32_t blocks = (n + 255) / 256;
-    RC_CUDA(rc, cudaMemsetAsync(rc->d_counts + 1, 0, sizeof(uint32_t), s));
-    p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
-    p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
-    p.n_out = ctx->d_pt_counts + 0;
-    pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
-    RC_CUDA(rc, cudaGetLastError());
-    const uint32_t final_bounce = last_bounce < rc->max_bounces ? last_bounce : rc->max_bounces;
-    for (uint32_t b = 0; b <= final_bounce; b++) {
-        const int in = int(b & 1), out = 1 - in;
-        p.bounce = b;
-        p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
-        p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
-        p.n_in = ctx->d_pt_counts + in;
-        p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
-        p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
-        p.n_out = ctx->d_pt_counts + out;
-        ae_rt_status st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n, 0.0f,
-                                          1e12f, ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
-        if (st != AE_RT_OK) return st;
-        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
-        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
-        rc_shade_kernel<<<blocks, 256, 0, s>>>(rp);
-        RC_CUDA(rc, cudaGetLastError());
-        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, 1e12f,
-                             ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
-        if (st != AE_RT_OK) return st;
-        pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
-        RC_CUDA(rc, cudaGetLastError());
-    }
-    RcMlpParams mp = MlpParams(rc);
-    mp.recs = static_cast<const float4*>(rc->queries.ptr);
-    mp.n = n;
-    mp.n_dev = rc->d_counts + 1;
-    mp.accum = reinterpret_cast<float4*>(accum);
-    rc_mlp_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RC_THREADS, kInferSmem, s>>>(mp);
-    RC_CUDA(rc, cudaGetLastError());
-    return AE_RT_OK;
+ae_rt_status ae_rc_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
+                         uint32_t max_bounces, uint32_t last_bounce, float* accum, float* loss_out, void* stream) {
+    if (!rc || !accum) return AE_RT_INVALID_ARG;
+    ae_rt_status st = CheckTrainArgs(rc, cam, n_paths, steps, max_bounces);
+    if (st != AE_RT_OK) return st;
+    if (!DevPtr(accum)) return RcFail(rc, AE_RT_INVALID_ARG, "accumulation buffer must be device memory");
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    st = EnsureStreams(rc);
+    if (st != AE_RT_OK) return st;
+    // training paths (scene only) on the side stream, beside the render
+    cudaStream_t a1 = rc->aux[1];
+    RC_CUDA(rc, cudaEventRecord(rc->ev[2], s));
+    RC_CUDA(rc, cudaStreamWaitEvent(a1, rc->ev[2], 0));
+    st = GeneratePaths(rc, cam, frame, n_paths, max_bounces, a1);
+    if (st != AE_RT_OK) return st;
+    RC_CUDA(rc, cudaEventRecord(rc->ev[3], a1));
+    rc->max_bounces = max_bounces;
+    st = RenderFrame(rc, cam, frame, last_bounce, accum, s);
+    if (st != AE_RT_OK) return st;
+    RC_CUDA(rc, cudaStreamWaitEvent(s, rc->ev[3], 0));
+    return TrainSteps(rc, n_paths, steps, loss_out, s);
 }
 
 }  // extern "C"

@@ -101,10 +101,9 @@ __device__ __forceinline__ void rc_cell(const RcGrid& g, const float4& q0, int l
     }
 }
 
-// Encodes one query into a 64-wide BF16 row in shared memory.
-__device__ __forceinline__ void rc_encode(const RcGrid& g, const float4& q0, const float4& q1, const float4& q2,
-                                          __nv_bfloat16* row) {
-    __nv_bfloat162 v[32];
+// Encodes one query into the 64 BF16 network inputs (32 pairs).
+__device__ __forceinline__ void rc_encode_values(const RcGrid& g, const float4& q0, const float4& q1,
+                                                 const float4& q2, __nv_bfloat162 v[32]) {
     for (int l = 0; l < RC_LEVELS; l++) {
         uint32_t c[3];
         float f[3];
@@ -128,6 +127,13 @@ __device__ __forceinline__ void rc_encode(const RcGrid& g, const float4& q0, con
     v[25] = __floats2bfloat162_rn(q2.z, q0.w);
     v[26] = __floats2bfloat162_rn(q2.w, 0.0f);
     for (int k = 27; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
+}
+
+// Encodes one query into a 64-wide BF16 row in shared memory.
+__device__ __forceinline__ void rc_encode(const RcGrid& g, const float4& q0, const float4& q1, const float4& q2,
+                                          __nv_bfloat16* row) {
+    __nv_bfloat162 v[32];
+    rc_encode_values(g, q0, q1, q2, v);
     uint4* dst = reinterpret_cast<uint4*>(row);
     const uint4* src = reinterpret_cast<const uint4*>(v);
 #pragma unroll
@@ -287,10 +293,12 @@ struct RcMlpParams {
     const uint32_t* n_dev;           // optional device count
     uint32_t n;                      // count, or capacity with n_dev
     uint32_t offset;                 // first record (training steps over one buffer)
+    const uint32_t* offset_dev;      // inference: first record read from the device (overrides offset)
     uint32_t slice, slices;          // slices > 0: train on slice `slice` of the device count
     float4* accum;                   // RC_INFER: image
     float4* out;                     // RC_PREDICT
     float* loss;                     // RC_TRAIN: mean per-element loss (accumulated)
+    uint32_t* error_word;            // tensor-memory kernels: a bounded wait that gave up
 };
 
 template <int MODE>

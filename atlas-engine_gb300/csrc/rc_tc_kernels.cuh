@@ -1,0 +1,275 @@
+// Radiance-cache inference on the 5th-generation tensor cores: the fused
+// hash-grid encoding + 6-layer BF16 MLP of rc_kernels.cuh with every layer
+// a tcgen05.mma (M = 128 queries, N = 64 or 16, K = 64 in four K = 16 steps)
+// accumulating in FP32 tensor memory.
+//
+// Per CTA (two independent groups of 128 threads, one query row per thread;
+// 3 CTAs per SM), per group:
+//  * shared memory holds the weights of all six layers (shared by the
+//    groups) and the group's 128 x 64 BF16 activation tile, both in the
+//    no-swizzle core-matrix layout the MMA
+//    descriptors describe: 8 rows x 16 bytes per core matrix, core matrices
+//    128 bytes apart along K (leading byte offset) and 1024 bytes apart along
+//    M / N (stride byte offset);
+//  * warp 0 allocates 128 tensor-memory columns, 64 per group (lane i =
+//    query row i of the group's tile);
+//  * per layer thread 0 issues the four MMAs and commits them to an
+//    mbarrier; every thread waits on it (bounded by the global timer), reads
+//    its own row back with tcgen05.ld (the group's warp w owns lanes
+//    32w..32w+31),
+//    applies ReLU, rounds to BF16 and writes the row of the next layer's
+//    input tile; a proxy fence and the group's named barrier hand the tile
+//    back to the tensor core;
+//  * after the output layer each thread has its query's RGB in registers and
+//    adds (throughput x max(0, prediction)) into the image or writes the
+//    prediction.
+// A wait that times out sets kErrTimeout in the context's error word (the
+// next ae_rt_synchronize reports AE_RT_TIMEOUT), stops the CTA's loop and
+// still frees the tensor memory.
+#pragma once
+
+#include "rc_kernels.cuh"
+
+namespace atlas::rt::dev {
+
+constexpr uint32_t kErrTimeout = 0x4u;
+
+constexpr uint32_t RCT_LBO = 128;                       // core matrices along K
+constexpr uint32_t RCT_SBO = 1024;                      // core matrices along M / N (8 x 128 B of K = 64)
+constexpr uint32_t RCT_ABYTES = RC_TILE * RC_W * 2;     // 16 KB activation tile
+constexpr uint32_t RCT_WLAYER = RC_W * RC_W * 2;        // 8 KB per hidden layer
+constexpr uint32_t RCT_WBYTES = RC_HIDDEN * RCT_WLAYER + RC_OUT * RC_W * 2;   // 43,008
+constexpr uint32_t RCT_GROUPS = 2;                      // independent 128-row tile groups per CTA
+constexpr uint32_t RCT_THREADS = RCT_GROUPS * RC_TILE;
+constexpr uint32_t RCT_SMEM = RCT_WBYTES + RCT_GROUPS * RCT_ABYTES + 64;      // + mbarriers, flags, TMEM address
+constexpr uint32_t RCT_TMEM_COLS = RCT_GROUPS * 64;
+
+// Byte offset of the 16-byte chunk (row, k-block kb) in the blocked layout.
+__device__ __forceinline__ uint32_t rct_off(uint32_t row, uint32_t kb) {
+    return (row >> 3) * RCT_SBO + kb * RCT_LBO + (row & 7u) * 16u;
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading and stride
+// byte offsets (all >> 4), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t rct_desc(uint32_t saddr) {
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(RCT_LBO >> 4) << 16) | (uint64_t(RCT_SBO >> 4) << 32) |
+           (uint64_t(1) << 46);
+}
+
+// Instruction descriptor of kind::f16: F32 accumulator, BF16 A and B, both
+// K-major, N >> 3 and M >> 4.
+__host__ __device__ constexpr uint32_t rct_idesc(uint32_t m, uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the mbarrier phase with parity `parity`; false after ~200 ms.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    const uint64_t start = global_ns();
+    for (uint32_t it = 0;; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+        if (done) return true;
+        if ((it & 63u) == 63u && global_ns() - start > 200000000ull) return false;
+    }
+}
+
+// Barrier of one 128-thread tile group (named barrier 1 + group).
+__device__ __forceinline__ void group_sync(uint32_t g) {
+    static_assert(RCT_GROUPS == 2, "one named barrier per group");
+    if (g == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+    else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+
+// rc_encode_values with four levels' table reads in flight at once.
+__device__ __forceinline__ void rc_encode_values_wide(const RcGrid& g, const float4& q0, const float4& q1,
+                                                      const float4& q2, __nv_bfloat162 v[32]) {
+#pragma unroll 4
+    for (int l = 0; l < RC_LEVELS; l++) {
+        uint32_t c[3];
+        float f[3];
+        rc_cell(g, q0, l, c, f);
+        float a0 = 0.0f, a1 = 0.0f;
+        const __half2* tab = g.table + size_t(l) * g.T;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+            const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+            const float2 e = __half22float2(tab[rc_index(g, l, c[0] + dx, c[1] + dy, c[2] + dz)]);
+            a0 += w * e.x;
+            a1 += w * e.y;
+        }
+        v[l] = __floats2bfloat162_rn(a0, a1);
+    }
+    float sh[16];
+    sh16(q1.x, q1.y, q1.z, sh);
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[16 + k] = __floats2bfloat162_rn(sh[2 * k], sh[2 * k + 1]);
+    v[24] = __floats2bfloat162_rn(q2.x, q2.y);
+    v[25] = __floats2bfloat162_rn(q2.z, q0.w);
+    v[26] = __floats2bfloat162_rn(q2.w, 0.0f);
+#pragma unroll
+    for (int k = 27; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
+}
+
+// 16 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
+}
+
+template <int MODE>
+static __global__ void __launch_bounds__(RCT_THREADS) rc_infer_tc_kernel(RcMlpParams p) {
+    extern __shared__ __align__(1024) unsigned char rct_smem[];
+    unsigned char* wsm = rct_smem;
+    unsigned char* tail = rct_smem + RCT_WBYTES + RCT_GROUPS * RCT_ABYTES;
+    uint64_t* mbars = reinterpret_cast<uint64_t*>(tail);                       // one per group
+    uint32_t* fail = reinterpret_cast<uint32_t*>(tail + 8 * RCT_GROUPS);       // one per group
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tail + 12 * RCT_GROUPS);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t g = tid / RC_TILE, row = tid % RC_TILE, gwarp = warp & 3u;
+    unsigned char* act = rct_smem + RCT_WBYTES + g * RCT_ABYTES;
+
+    // weights of every layer in the blocked layout (rows = output neurons, K = 64)
+    for (uint32_t i = tid; i < uint32_t(RC_WROWS) * 8u; i += blockDim.x) {
+        const uint32_t r = i >> 3, kb = i & 7u;
+        const uint32_t layer = r < uint32_t(RC_HIDDEN * RC_W) ? r / RC_W : uint32_t(RC_HIDDEN);
+        const uint32_t n = r - layer * RC_W;
+        *reinterpret_cast<uint4*>(wsm + layer * RCT_WLAYER + rct_off(n, kb)) =
+            reinterpret_cast<const uint4*>(p.weights + size_t(r) * RC_W)[kb];
+    }
+    if (row == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbars[g])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fail[g] = 0u;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(tslot)), "r"(RCT_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot + g * 64u;                     // this group's 64 columns
+    const uint32_t a_addr = smem_u32(act), w_addr = smem_u32(wsm), mbar_addr = smem_u32(&mbars[g]);
+    const uint32_t lane_base = tmem + ((gwarp * 32u) << 16);
+
+    const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
+    const uint32_t first = p.offset_dev ? min(*p.offset_dev, n) : p.offset;
+    const uint32_t count = n > first ? n - first : 0u;
+    const uint32_t tiles = (count + RC_TILE - 1) / RC_TILE;
+    uint32_t parity = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x * RCT_GROUPS + g; tile < tiles && ok; tile += gridDim.x * RCT_GROUPS) {
+        const uint32_t gi = tile * RC_TILE + row;
+        const bool valid = gi < count;
+        float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
+        __nv_bfloat162 v[32];
+        if (valid) {
+            const float4* rec = p.recs + size_t(first + gi) * 4;
+            q0 = rec[0]; q1 = rec[1]; q2 = rec[2]; q3 = rec[3];
+            rc_encode_values_wide(p.grid, q0, q1, q2, v);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (uint32_t kb = 0; kb < 8; kb++)
+            *reinterpret_cast<uint4*>(act + rct_off(row, kb)) = reinterpret_cast<const uint4*>(v)[kb];
+        proxy_fence();
+        tc_fence_before();
+        group_sync(g);
+        tc_fence_after();
+#pragma unroll 1
+        for (int l = 0; l <= RC_HIDDEN; l++) {
+            const uint32_t nn = l < RC_HIDDEN ? uint32_t(RC_W) : uint32_t(RC_OUT);
+            if (row == 0) {
+                const uint32_t idesc = rct_idesc(RC_TILE, nn);
+#pragma unroll
+                for (uint32_t s = 0; s < 4; s++)
+                    tc_mma(tmem, rct_desc(a_addr + s * 2u * RCT_LBO),
+                           rct_desc(w_addr + uint32_t(l) * RCT_WLAYER + s * 2u * RCT_LBO), idesc, s);
+                tc_commit(mbar_addr);
+            }
+            if (!mbar_wait(mbar_addr, parity)) fail[g] = 1u;
+            parity ^= 1u;
+            // every thread of the group takes the same decision (a late arrival
+            // seen by some threads only must not split the group's barriers)
+            group_sync(g);
+            ok = fail[g] == 0u;
+            tc_fence_after();
+            if (!ok) break;
+            if (l < RC_HIDDEN) {
+#pragma unroll
+                for (uint32_t c = 0; c < 4; c++) {
+                    float x[16];
+                    tc_ld16(lane_base + c * 16u, x);
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) pk[k] = pack_bf16(fmaxf(x[2 * k], 0.0f), fmaxf(x[2 * k + 1], 0.0f));
+                    *reinterpret_cast<uint4*>(act + rct_off(row, 2 * c)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    *reinterpret_cast<uint4*>(act + rct_off(row, 2 * c + 1)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
+                proxy_fence();
+            } else {
+                float x[16];
+                tc_ld16(lane_base, x);
+                if (valid) {
+                    if (MODE == RC_PREDICT) {
+                        p.out[first + gi] = make_float4(x[0], x[1], x[2], 0.0f);
+                    } else {
+                        float4* a = p.accum + __float_as_uint(q1.w);
+                        a->x += q3.x * fmaxf(x[0], 0.0f);
+                        a->y += q3.y * fmaxf(x[1], 0.0f);
+                        a->z += q3.z * fmaxf(x[2], 0.0f);
+                    }
+                }
+            }
+            tc_fence_before();
+            group_sync(g);
+            tc_fence_after();
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (!ok && row == 0 && p.error_word) atomicOr(p.error_word, kErrTimeout);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tslot), "r"(RCT_TMEM_COLS)
+                     : "memory");
+}
+
+}  // namespace atlas::rt::dev

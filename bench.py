@@ -502,7 +502,10 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32)
     """Radiance-cache path tracer on the same scene, camera and converged
     image as the plain path tracer: the cache starts untrained; every frame
     trains it on `n_paths` self-generated 3-bounce paths (`steps` Adam
-    steps, lr 1e-2) and renders 1 spp with paths ending in the cache.  Frame
+    steps, lr 1e-2) and, from frame `start` on, renders 1 spp with paths
+    ending in the cache (ae_rc_frame: the render uses the cache as trained up
+    to the previous frame, while this frame's training paths are traced
+    beside it).  Frame
     times are CUDA-event times on the stream (the error read-backs between
     frames are outside them).  The rendered frames are averaged from frame
     `start` on (the frames before only train); for each start the GPU time
@@ -535,21 +538,25 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32)
     rc = atlas_rt.RadianceCache(ctx, lo - 0.5, hi + 0.5, seed=5, radiance_scale=scale, rough_cut=rough_cut)
     reached = {}
     curve = []
-    train_ms = render_ms = 0.0
+    train_ms = frame_ms = 0.0
     evf = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     for f in range(max_frames):
         render = f >= min(starts)
         evf[0].record(stream)
-        rc.train_frame(cam, f, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
-        evf[1].record(stream)
         if render:
+            # one online frame: render with the cache as it stands while the
+            # frame's training paths are traced beside it, then train
             frame_buf.zero_()
-            rc.render(cam, f, frame_buf, stream=stream)
-        evf[2].record(stream)
+            rc.frame(cam, f, frame_buf, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
+        else:
+            rc.train_frame(cam, f, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
+        evf[1].record(stream)
         torch.cuda.synchronize(dev)
-        tr, tt = evf[0].elapsed_time(evf[1]), evf[0].elapsed_time(evf[2])
-        train_ms += tr
-        render_ms += tt - tr
+        tt = evf[0].elapsed_time(evf[1])
+        if render:
+            frame_ms += tt
+        else:
+            train_ms += tt
         t_cum += tt
         if not render:
             continue
@@ -571,8 +578,8 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32)
     out = {"resolution": [W, H], "n_paths": n_paths, "adam_steps_per_frame": steps, "radiance_scale": scale,
            "rough_cut": rough_cut,
            "target_rel_mse": target, "plain_pt_ms_to_64spp": pt_ms, "frames_run": f + 1,
-           "train_ms_per_frame": train_ms / (f + 1),
-           "render_ms_per_frame": render_ms / max(f + 1 - min(starts), 1),
+           "train_only_ms_per_frame": train_ms / min(starts),
+           "frame_ms": frame_ms / max(f + 1 - min(starts), 1),
            "starts": {str(s): reached.get(s) for s in starts}, "curve": curve}
     best = min((r["ms"] for r in reached.values()), default=None)
     out["ms_to_equal_rel_mse"] = best

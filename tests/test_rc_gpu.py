@@ -150,8 +150,8 @@ def test_params_roundtrip_and_checkpoint(cache):
 
 
 def test_cache_gains_over_plain_path_tracer():
-    """Online use (every frame trains the cache on 65,536 paths, then renders
-    one sample per pixel with paths ending in it): after 16 training frames,
+    """Online use (every frame trains the cache on 65,536 paths and renders
+    one sample per pixel with paths ending in it, ae_rc_frame): after 16 training frames,
     4 rendered frames are at least twice as close (rel-MSE) to the converged
     image as the plain path tracer at 4 samples per pixel.  (960 x 540: at
     lower resolutions the variance of pixel-footprint sampling, which both
@@ -183,9 +183,10 @@ def test_cache_gains_over_plain_path_tracer():
         try:
             acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
             for f in range(20):
-                rc.train_frame(cam, f, n_paths=65536, steps=2)
-                if f >= 16:
-                    rc.render(cam, f, acc)
+                if f < 16:
+                    rc.train_frame(cam, f, n_paths=65536, steps=2)
+                else:
+                    rc.frame(cam, f, acc, n_paths=65536, steps=2)     # render beside training, then train
             ctx.synchronize()
             rc_img = (acc[:, :3] / 4).cpu().numpy().reshape(h, w, 3)
             rc_err = ptscene.rel_mse(rc_img, refimg)
