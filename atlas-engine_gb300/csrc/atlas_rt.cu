@@ -891,6 +891,13 @@ ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed
     return AE_RT_OK;
 }
 
+namespace {
+__global__ void publish_counts_kernel(const uint32_t* counts, uint32_t* host_mapped) {
+    if (threadIdx.x < 2) host_mapped[threadIdx.x] = counts[threadIdx.x];
+    __threadfence_system();
+}
+}  // namespace
+
 ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam,
                              const ae_bounce_params* params, ae_cast_outputs* out, void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
@@ -925,7 +932,11 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     if (!ctx->copy_stream) AE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     for (cudaEvent_t& e : ctx->cast_events)
         if (!e) AE_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    if (!ctx->h_cast_counts) AE_CUDA(ctx, cudaMallocHost(&ctx->h_cast_counts, 2 * sizeof(uint32_t)));
+    if (!ctx->h_cast_counts) {
+        AE_CUDA(ctx, cudaHostAlloc(&ctx->h_cast_counts, 2 * sizeof(uint32_t), cudaHostAllocMapped));
+        AE_CUDA(ctx, cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->d_cast_counts_mapped),
+                                              ctx->h_cast_counts, 0));
+    }
     cudaStream_t cs = ctx->copy_stream;
     cudaEvent_t evPrim = ctx->cast_events[0], evCounts = ctx->cast_events[1], evSec = ctx->cast_events[2],
                 evShd = ctx->cast_events[3];
@@ -942,7 +953,11 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     AE_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s));
     if ((st = ae_rt_spawn_bounce(ctx, mesh_id, prim, primHits, nullptr, n, params, sec, shd, counts, stream)) != AE_RT_OK)
         return st;
-    AE_CUDA(ctx, cudaMemcpyAsync(ctx->h_cast_counts, counts, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    // the queue lengths reach the host through mapped memory, written by a
+    // kernel: a copy here would queue on the copy engine behind the primary
+    // hits and hold back the bounce trace that follows in stream order
+    publish_counts_kernel<<<1, 32, 0, s>>>(counts, ctx->d_cast_counts_mapped);
+    AE_CUDA(ctx, cudaGetLastError());
     AE_CUDA(ctx, cudaEventRecord(evCounts, s));
     if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
     AE_CUDA(ctx, cudaEventRecord(evSec, s));
@@ -950,7 +965,8 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, stream, counts + 1)) != AE_RT_OK) return st;
     AE_CUDA(ctx, cudaEventRecord(evShd, s));
     AE_CUDA(ctx, cudaEventSynchronize(evCounts));
-    const uint32_t nSec = ctx->h_cast_counts[0], nShd = ctx->h_cast_counts[1];
+    const volatile uint32_t* hc = ctx->h_cast_counts;
+    const uint32_t nSec = hc[0], nShd = hc[1];
     out->counts[0] = n;
     out->counts[1] = nSec;
     out->counts[2] = nShd;

@@ -82,7 +82,8 @@ struct ae_rt_ctx {
     // result copies of ae_rt_cast_pass overlap the later stages on this stream
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t cast_events[4] = { nullptr, nullptr, nullptr, nullptr };
-    uint32_t* h_cast_counts = nullptr;  // pinned
+    uint32_t* h_cast_counts = nullptr;  // pinned, mapped
+    uint32_t* d_cast_counts_mapped = nullptr;   // its device address
     std::string last_error;
     std::mutex upload_mutex;
 };
