@@ -436,10 +436,11 @@ class RadianceCache:
 
     def __init__(self, ctx: Context, aabb_min, aabb_max, log2_table=19, base_resolution=16, max_resolution=2048,
                  learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, seed=1, radiance_scale=1.0,
-                 rough_cut=0.35):
+                 rough_cut=0.35, glossy_split=4):
         cfg = RcConfig()
         cfg.radiance_scale = float(radiance_scale)
         cfg.rough_cut = float(rough_cut)
+        cfg.glossy_split = int(glossy_split)
         cfg.log2_table, cfg.base_resolution, cfg.max_resolution = log2_table, base_resolution, max_resolution
         cfg.learning_rate, cfg.beta1, cfg.beta2, cfg.epsilon, cfg.seed = learning_rate, beta1, beta2, epsilon, seed
         for i in range(3):

@@ -990,6 +990,8 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
         AE_CUDA(ctx, cudaMemset(ctx->d_counter + 1, 0, sizeof(uint32_t)));
         if (err & 0x4u)   // kErrTimeout of the tensor-memory kernels
             return Fail(ctx, AE_RT_TIMEOUT, "a bounded device wait gave up");
+        if (err & atlas::rt::dev::kErrQueueOverflow)
+            return Fail(ctx, AE_RT_OUT_OF_MEMORY, "a wavefront queue was full; rays were dropped");
         if (err & atlas::rt::dev::kErrStackOverflow)
             return Fail(ctx, AE_RT_STACK_OVERFLOW, "a ray needed more than " +
                                                    std::to_string(kStackEntries) + " stack entries");

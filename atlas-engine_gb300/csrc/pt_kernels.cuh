@@ -71,7 +71,15 @@ struct PtParams {
     const uint8_t* shadow_occ;
     float4* accum;                // W*H float4 (rgb, sample count in .w from raygen)
     double* accum64;              // W*H*3 or null
+    uint32_t atomic_accum;        // several contributions per pixel and pass: add atomically
+    uint32_t capacity;            // queue capacity in rays (0: width * height)
+    uint32_t* overflow;           // set when an append would pass the capacity (ray dropped)
 };
+
+// Pixel keys carried by rays and payloads: the pixel index in the low 24
+// bits; the radiance-cache renderer's path splits keep their split index in
+// bits 24-26, which gives every split its own random streams.
+constexpr uint32_t kPixelMask = 0x00FFFFFFu;
 
 // ---- small vector helpers (fast math is fine here: statistics, not parity) ----
 struct V3 {
@@ -315,17 +323,34 @@ static __global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
     if (i == 0) *p.n_out = n;
 }
 
-__device__ __forceinline__ void add_radiance(const PtParams& p, uint32_t pix, V3 L) {
+__device__ __forceinline__ void add_radiance(const PtParams& p, uint32_t key, V3 L) {
+    const uint32_t pix = key & kPixelMask;
     float4* a = p.accum + pix;
-    a->x += L.x;
-    a->y += L.y;
-    a->z += L.z;
+    if (p.atomic_accum) {
+        atomicAdd(&a->x, L.x);
+        atomicAdd(&a->y, L.y);
+        atomicAdd(&a->z, L.z);
+    } else {
+        a->x += L.x;
+        a->y += L.y;
+        a->z += L.z;
+    }
     if (p.accum64) {
         double* d = p.accum64 + size_t(pix) * 3;
-        d[0] += double(L.x);
-        d[1] += double(L.y);
-        d[2] += double(L.z);
+        if (p.atomic_accum) {
+            atomicAdd(d, double(L.x));
+            atomicAdd(d + 1, double(L.y));
+            atomicAdd(d + 2, double(L.z));
+        } else {
+            d[0] += double(L.x);
+            d[1] += double(L.y);
+            d[2] += double(L.z);
+        }
     }
+}
+
+__device__ __forceinline__ uint32_t queue_capacity(const PtParams& p) {
+    return p.capacity ? p.capacity : p.width * p.height;
 }
 
 // GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit:
@@ -539,7 +564,7 @@ __device__ __forceinline__ float mis_hit_factor(const PtScene& sc, const Surf& s
 static __global__ void pt_shade_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t n = min(*p.n_in, p.width * p.height);
+    const uint32_t n = min(*p.n_in, queue_capacity(p));
     bool emitRay = false, emitShadow = false;
     float4 outRay0{}, outRay1{}, outPay{}, shRay0{}, shRay1{}, shPay{};
     if (i < n) {
@@ -600,7 +625,7 @@ static __global__ void pt_shade_kernel(PtParams p) {
 // Adds the contributions of the unoccluded shadow rays.
 static __global__ void pt_resolve_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = min(*p.n_shadow, p.width * p.height);
+    const uint32_t n = min(*p.n_shadow, queue_capacity(p));
     if (i >= n || p.shadow_occ[i]) return;
     const float4 c = p.shadow_pay[i];
     add_radiance(p, __float_as_uint(c.w), v3(c.x, c.y, c.z));

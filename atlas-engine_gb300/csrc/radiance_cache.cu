@@ -237,15 +237,18 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
                          cudaStream_t s) {
     ae_rt_ctx* ctx = rc->ctx;
     const uint32_t n = cam->width * cam->height;
+    if (n > kPixelMask + 1u) return RcFail(rc, AE_RT_INVALID_ARG, "more than 2^24 pixels");
+    // queues hold twice the pixels: split glossy paths add rays
+    const uint32_t cap = 2u * n;
     for (int k = 0; k < 2; k++) {
-        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
-        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
+        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(cap) * sizeof(ae_packed_ray)));
+        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(cap) * sizeof(float4)));
     }
-    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
-    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
-    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
-    RC_CUDA(rc, ctx->pt_occ.ensure(n));
-    RC_CUDA(rc, rc->queries.ensure(size_t(n) * 64));
+    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(cap) * sizeof(ae_hit)));
+    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(cap) * sizeof(ae_packed_ray)));
+    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(cap) * sizeof(float4)));
+    RC_CUDA(rc, ctx->pt_occ.ensure(cap));
+    RC_CUDA(rc, rc->queries.ensure(size_t(cap) * 64));
     if (!ctx->d_pt_counts) RC_CUDA(rc, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
     ae_rt_status st = EnsureStreams(rc);
     if (st != AE_RT_OK) return st;
@@ -273,12 +276,17 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     p.n_shadow = ctx->d_pt_counts + 2;
     p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
     p.accum = reinterpret_cast<float4*>(accum);
+    p.atomic_accum = 1;
+    p.capacity = cap;
+    p.overflow = ctx->d_counter + 1;
     rp.queries = static_cast<float4*>(rc->queries.ptr);
     rp.n_queries = rc->d_counts + 1;
+    rp.query_capacity = cap;
     rp.last_bounce = last_bounce;
     rp.inv_scale = 1.0f / rc->scale;
     rp.rough_cut = rc->cfg.rough_cut > 0.0f ? rc->cfg.rough_cut : 0.35f;
-    const uint32_t blocks = (n + 255) / 256;
+    rp.split = rc->cfg.glossy_split == 0 ? 4u : (rc->cfg.glossy_split > RC_MAX_SPLIT ? RC_MAX_SPLIT : rc->cfg.glossy_split);
+    const uint32_t blocks = (cap + 255) / 256;
     RC_CUDA(rc, cudaMemsetAsync(rc->d_counts + 1, 0, sizeof(uint32_t), s));
     p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
     p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
@@ -287,7 +295,7 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     RC_CUDA(rc, cudaGetLastError());
     RcMlpParams mp = MlpParams(rc);
     mp.recs = static_cast<const float4*>(rc->queries.ptr);
-    mp.n = n;
+    mp.n = cap;
     mp.accum = reinterpret_cast<float4*>(accum);
     cudaStream_t a0 = rc->aux[0];
     const uint32_t final_bounce = last_bounce < rc->max_bounces ? last_bounce : rc->max_bounces;
@@ -300,14 +308,14 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
         p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
         p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
         p.n_out = ctx->d_pt_counts + out;
-        st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n, 0.0f, 1e12f,
+        st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), cap, 0.0f, 1e12f,
                              ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
         if (st != AE_RT_OK) return st;
         RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
         RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
         rc_shade_kernel<<<blocks, 256, 0, s>>>(rp);
         RC_CUDA(rc, cudaGetLastError());
-        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, 1e12f,
+        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), cap, 0.0f, 1e12f,
                              ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
         if (st != AE_RT_OK) return st;
         pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
@@ -321,7 +329,7 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
             RC_CUDA(rc, cudaStreamWaitEvent(a0, rc->ev[0], 0));
             RcMlpParams m0 = mp;
             m0.n_dev = rc->d_counts + 2;
-            rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RCT_THREADS, RCT_SMEM, a0>>>(m0);
+            rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, cap) * 3, RCT_THREADS, RCT_SMEM, a0>>>(m0);
             RC_CUDA(rc, cudaGetLastError());
             RC_CUDA(rc, cudaEventRecord(rc->ev[1], a0));
         }
@@ -330,7 +338,7 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     RcMlpParams m1 = mp;
     m1.n_dev = rc->d_counts + 1;
     m1.offset_dev = rc->d_counts + 2;
-    rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, n) * 3, RCT_THREADS, RCT_SMEM, s>>>(m1);
+    rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, cap) * 3, RCT_THREADS, RCT_SMEM, s>>>(m1);
     RC_CUDA(rc, cudaGetLastError());
     RC_CUDA(rc, cudaStreamWaitEvent(s, rc->ev[1], 0));
     return AE_RT_OK;

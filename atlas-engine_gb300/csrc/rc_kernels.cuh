@@ -761,14 +761,30 @@ static __global__ void rc_paths_kernel(RcPathParams p) {
     }
 }
 
+constexpr uint32_t RC_MAX_SPLIT = 4;
+
 struct RcShadeParams {
     PtParams pt;             // queues, scene, accumulation, bounce budget (pt.max_bounces)
     float4* queries;         // cache queries (4 float4)
     uint32_t* n_queries;
+    uint32_t query_capacity;
     uint32_t last_bounce;    // query the cache here whatever the material
     float inv_scale;         // 1 / radiance scale of the cache
     float rough_cut;         // metals at least this rough end in the cache too
+    uint32_t split;          // paths per glossy metal at the first vertex (1..RC_MAX_SPLIT)
 };
+
+// Appends one item per lane that wants one (warp-aggregated), or drops it and
+// flags the overflow when the queue is full.
+__device__ __forceinline__ bool rc_append(uint32_t* counter, uint32_t cap, bool want, uint32_t lane, uint32_t* overflow,
+                                          uint32_t& idx) {
+    idx = warp_append(counter, want, lane);
+    if (want && idx >= cap) {
+        if (overflow) atomicOr(overflow, kErrQueueOverflow);
+        return false;
+    }
+    return want;
+}
 
 // Rendering with the cache: emission of the first hit and next-event
 // estimation at every vertex (as the path tracer).  A diffuse vertex, a metal
@@ -776,83 +792,108 @@ struct RcShadeParams {
 // with a cache query for its indirect radiance, weighted by path throughput x
 // base colour / scale.  A glossier metal continues the path; its next-event
 // estimate and the emission its continuation finds are combined by the power
-// heuristic (the factor travels in the continuation ray's dir.w).
+// heuristic (the factor travels in the continuation ray's dir.w).  At the
+// first vertex a glossy metal splits into `split` independent paths (a light
+// sample and a continuation each, weight 1/split), with their own random
+// streams (split index in bits 24-26 of the pixel key): those pixels carry
+// most of the variance of a cache-terminated frame.
 static __global__ void rc_shade_kernel(RcShadeParams rp) {
     const PtParams& p = rp.pt;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t n = min(*p.n_in, p.width * p.height);
-    bool emitRay = false, emitShadow = false, emitQuery = false;
-    float4 outRay0{}, outRay1{}, outPay{}, shRay0{}, shRay1{}, shPay{}, q0{}, q1{}, q2{}, q3{};
+    const uint32_t cap = queue_capacity(p);
+    const uint32_t n = min(*p.n_in, cap);
+    bool emitQuery = false, cont = false;
+    uint32_t S = 0, key = 0;
+    float4 q0{}, q1{}, q2{}, q3{};
+    Surf sf{};
+    V3 thr = v3(0, 0, 0);
     if (i < n) {
         const float4 h0 = p.hits_in[size_t(i) * 2];
         const int32_t triPtr = __float_as_int(h0.y);
         const float4 pay = p.pay_in[i];
-        const uint32_t pix = __float_as_uint(pay.w);
-        V3 thr = v3(pay.x, pay.y, pay.z);
+        key = __float_as_uint(pay.w);
+        thr = v3(pay.x, pay.y, pay.z);
         if (triPtr >= 0) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
             const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
-            Surf sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
+            sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
             const bool emissive = sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f;
-            if (p.bounce == 0 && emissive) add_radiance(p, pix, sf.mat.emissive);
-            if (p.bounce > 0 && emissive && d4.w > 0.0f) add_radiance(p, pix, thr * sf.mat.emissive * d4.w);
-            const V3 V = sf.V, N = sf.N;     // the query's direction and normal (direct_light moves sf.L only)
+            if (p.bounce == 0 && emissive) add_radiance(p, key, sf.mat.emissive);
+            if (p.bounce > 0 && emissive && d4.w > 0.0f) add_radiance(p, key, thr * sf.mat.emissive * d4.w);
             const bool query = sf.mat.metalness < 0.5f || sf.mat.roughness >= rp.rough_cut ||
                                p.bounce >= rp.last_bounce || p.bounce + 1 >= uint32_t(RC_MAX_DEPTH);
-            const bool cont = p.bounce < p.max_bounces && !query;
-            V3 c, so, sd;
-            float st, pl = 0.0f;
-            if (direct_light(p.sc, sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st, &pl)) {
-                if (cont) c = c * power_weight(pl, bsdf_pdf(sf, sf.L));
-                emitShadow = true;
-                shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(pix));
-                shRay1 = make_float4(sd.x, sd.y, sd.z, st);
-                shPay = make_float4(c.x, c.y, c.z, __uint_as_float(pix));
-            }
-            if (p.bounce < p.max_bounces) {
-                if (query) {
-                    const V3 w = thr * sf.mat.base * rp.inv_scale;
-                    if (w.x + w.y + w.z > 0.0f) {
-                        emitQuery = true;
-                        q0 = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
-                        q1 = make_float4(V.x, V.y, V.z, __uint_as_float(pix));
-                        q2 = make_float4(N.x, N.y, N.z, float(p.bounce));
-                        q3 = make_float4(w.x, w.y, w.z, 1.0f);
-                    }
-                } else {
-                    V3 o, d;
-                    bool spec = false;
-                    if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec)) {
-                        emitRay = true;
-                        outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
-                        outRay1 = make_float4(d.x, d.y, d.z, mis_hit_factor(p.sc, sf, d, spec));
-                        outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
-                    }
+            cont = p.bounce < p.max_bounces && !query;
+            // a glossy metal at the first vertex splits (light sample +
+            // continuation per split); splitting the light sample of the
+            // metals that end in the cache was measured and gains nothing
+            S = cont && p.bounce == 0 ? rp.split : 1u;
+            if (query && p.bounce < p.max_bounces) {
+                const V3 w = thr * sf.mat.base * rp.inv_scale;
+                if (w.x + w.y + w.z > 0.0f) {
+                    emitQuery = true;
+                    q0 = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
+                    q1 = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(key));
+                    q2 = make_float4(sf.N.x, sf.N.y, sf.N.z, float(p.bounce));
+                    q3 = make_float4(w.x, w.y, w.z, 1.0f);
                 }
             }
         }
     }
-    const uint32_t ri = warp_append(p.n_out, emitRay, lane);
-    if (emitRay) {
-        float4* r = p.rays_out + size_t(ri) * 3;
-        r[0] = outRay0;
-        r[1] = outRay1;
-        r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
-        p.pay_out[ri] = outPay;
-    }
-    const uint32_t si = warp_append(p.n_shadow, emitShadow, lane);
-    if (emitShadow) {
-        float4* r = p.shadow_rays + size_t(si) * 3;
-        r[0] = shRay0;
-        r[1] = make_float4(shRay1.x, shRay1.y, shRay1.z, 0.0f);
-        r[2] = make_float4(shRay1.w, __int_as_float(-1), __int_as_float(-1), 0.0f);
-        p.shadow_pay[si] = shPay;
-    }
-    const uint32_t qi = warp_append(rp.n_queries, emitQuery, lane);
-    if (emitQuery) {
+    uint32_t qi;
+    if (rc_append(rp.n_queries, rp.query_capacity, emitQuery, lane, p.overflow, qi)) {
         float4* q = rp.queries + size_t(qi) * 4;
         q[0] = q0; q[1] = q1; q[2] = q2; q[3] = q3;
+    }
+    const float invS = S > 1u ? 1.0f / float(S) : 1.0f;
+#pragma unroll 1
+    for (uint32_t s = 0; s < RC_MAX_SPLIT; s++) {
+        const bool active = s < S;
+        const uint32_t k = key | (s << 24);        // split 0 keeps the plain key
+        bool emitShadow = false, emitRay = false;
+        float4 shRay0{}, shRay1{}, shPay{}, outRay0{}, outRay1{}, outPay{};
+        if (active) {
+            Surf ss = sf;
+            V3 c, so, sd;
+            float st, pl = 0.0f;
+            if (direct_light(p.sc, ss, thr, k, p.sample, p.bounce, p.seed, p.epsilon, c, so, sd, st, &pl)) {
+                c = c * (cont ? power_weight(pl, bsdf_pdf(ss, ss.L)) * invS : invS);
+                emitShadow = true;
+                shRay0 = make_float4(so.x, so.y, so.z, __uint_as_float(k));
+                shRay1 = make_float4(sd.x, sd.y, sd.z, st);
+                shPay = make_float4(c.x, c.y, c.z, __uint_as_float(k));
+            }
+            if (cont) {
+                V3 o, d, t2 = thr;
+                bool spec = false;
+                if (continue_path(ss, t2, k, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec)) {
+                    emitRay = true;
+                    t2 = t2 * invS;
+                    outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(k));
+                    outRay1 = make_float4(d.x, d.y, d.z, mis_hit_factor(p.sc, ss, d, spec));
+                    outPay = make_float4(t2.x, t2.y, t2.z, __uint_as_float(k));
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, emitShadow || emitRay)) {
+            if (!__any_sync(0xffffffffu, s + 1 < S)) break;
+            continue;
+        }
+        uint32_t si, ri;
+        if (rc_append(p.n_shadow, cap, emitShadow, lane, p.overflow, si)) {
+            float4* r = p.shadow_rays + size_t(si) * 3;
+            r[0] = shRay0;
+            r[1] = make_float4(shRay1.x, shRay1.y, shRay1.z, 0.0f);
+            r[2] = make_float4(shRay1.w, __int_as_float(-1), __int_as_float(-1), 0.0f);
+            p.shadow_pay[si] = shPay;
+        }
+        if (rc_append(p.n_out, cap, emitRay, lane, p.overflow, ri)) {
+            float4* r = p.rays_out + size_t(ri) * 3;
+            r[0] = outRay0;
+            r[1] = outRay1;
+            r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
+            p.pay_out[ri] = outPay;
+        }
     }
 }
 

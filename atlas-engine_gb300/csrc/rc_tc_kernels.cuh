@@ -252,10 +252,11 @@ static __global__ void __launch_bounds__(RCT_THREADS) rc_infer_tc_kernel(RcMlpPa
                     if (MODE == RC_PREDICT) {
                         p.out[first + gi] = make_float4(x[0], x[1], x[2], 0.0f);
                     } else {
-                        float4* a = p.accum + __float_as_uint(q1.w);
-                        a->x += q3.x * fmaxf(x[0], 0.0f);
-                        a->y += q3.y * fmaxf(x[1], 0.0f);
-                        a->z += q3.z * fmaxf(x[2], 0.0f);
+                        // split paths can query for the same pixel in one launch
+                        float4* a = p.accum + (__float_as_uint(q1.w) & kPixelMask);
+                        atomicAdd(&a->x, q3.x * fmaxf(x[0], 0.0f));
+                        atomicAdd(&a->y, q3.y * fmaxf(x[1], 0.0f));
+                        atomicAdd(&a->z, q3.z * fmaxf(x[2], 0.0f));
                     }
                 }
             }

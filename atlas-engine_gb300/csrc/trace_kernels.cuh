@@ -30,6 +30,7 @@ namespace atlas::rt::dev {
 
 constexpr uint32_t kErrStackOverflow = 0x1u;
 constexpr uint32_t kErrIterationCap = 0x2u;
+constexpr uint32_t kErrQueueOverflow = 0x8u;   // a wavefront queue append found the queue full
 
 constexpr uint32_t kHitFlagHit = 0x1u;
 constexpr uint32_t kHitFlagNearTie = 0x2u;

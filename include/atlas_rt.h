@@ -512,7 +512,8 @@ typedef struct ae_rc_config {
     float aabb_max[3];
     float radiance_scale;       /* stored value = radiance x scale (0: 1) */
     float rough_cut;            /* rendering: metals at least this rough end in the cache (0: 0.35) */
-    uint32_t reserved[2];
+    uint32_t glossy_split;      /* rendering: paths per glossier metal at the first vertex (0: 4; max 4) */
+    uint32_t reserved;
 } ae_rc_config;
 
 ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out);
@@ -559,7 +560,9 @@ ae_rt_status ae_rc_train_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, 
  * bounce last_bounce, or depth 2) the cache's indirect radiance times path
  * throughput x base colour ends the path; glossier metals before it continue,
  * their light combining next-event estimation and BRDF sampling (power
- * heuristic).  Adds into accum (float4 per pixel, device). */
+ * heuristic); at the first vertex they split into glossy_split paths of
+ * weight 1/glossy_split.  Adds into accum (float4 per pixel, device;
+ * atomically).  At most 2^24 pixels. */
 ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
                           void* stream);
 
