@@ -497,8 +497,8 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
     return res, (ctx, sc, cam, ref)
 
 
-def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32), max_frames=320,
-                            n_paths=65536, steps=2, rough_cut=0.35, close=True):
+def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(1, 2, 3, 4, 6, 8, 16), max_frames=320,
+                            n_paths=65536, steps=2, rough_cut=0.35, last_bounce=1, close=True):
     """Radiance-cache path tracer on the same scene, camera and converged
     image as the plain path tracer: the cache starts untrained; every frame
     trains it on `n_paths` self-generated 3-bounce paths (`steps` Adam
@@ -547,7 +547,8 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32)
             # one online frame: render with the cache as it stands while the
             # frame's training paths are traced beside it, then train
             frame_buf.zero_()
-            rc.frame(cam, f, frame_buf, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
+            rc.frame(cam, f, frame_buf, n_paths=n_paths, steps=steps, max_bounces=3, last_bounce=last_bounce,
+                     stream=stream)
         else:
             rc.train_frame(cam, f, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
         evf[1].record(stream)
@@ -576,7 +577,7 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(4, 8, 16, 32)
     if close:
         ctx.close()
     out = {"resolution": [W, H], "n_paths": n_paths, "adam_steps_per_frame": steps, "radiance_scale": scale,
-           "rough_cut": rough_cut,
+           "rough_cut": rough_cut, "last_bounce": last_bounce,
            "target_rel_mse": target, "plain_pt_ms_to_64spp": pt_ms, "frames_run": f + 1,
            "train_only_ms_per_frame": train_ms / min(starts),
            "frame_ms": frame_ms / max(f + 1 - min(starts), 1),
