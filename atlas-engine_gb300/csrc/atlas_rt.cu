@@ -150,8 +150,17 @@ uint32_t GridFor(const ae_rt_ctx* ctx, const void* fn, uint32_t n_rays) {
     return grid == 0 ? 1 : grid;
 }
 
+// Work-counter words of the context's launches, used in rotation so that
+// launches on different streams (up to kWorkSlots at a time) can overlap.
+constexpr uint32_t kWorkSlots = 6;
+uint32_t* WorkCounter(ae_rt_ctx* ctx) {
+    const uint32_t k = ctx->next_work_slot++ % kWorkSlots;
+    return ctx->d_counter + (k == 0 ? 0u : k + 1u);          // word 1 is the error word
+}
+
 ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s) {
-    AE_CUDA(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(uint32_t), s));
+    if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
+    AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
@@ -308,8 +317,8 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
                                             : (c.refill_below > 32 ? 0u : c.refill_below);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 2 * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 8 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 8 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_fetch, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_fetch, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cast_counts, 4 * sizeof(uint32_t));
@@ -352,6 +361,7 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     for (cudaEvent_t e : ctx->cast_events)
         if (e) cudaEventDestroy(e);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->trace_stream) cudaStreamDestroy(ctx->trace_stream);
     if (ctx->h_cast_counts) cudaFreeHost(ctx->h_cast_counts);
     for (Scratch* sc : { &ctx->rays_in, &ctx->results_out, &ctx->batch_table, &ctx->retest_count, &ctx->cast_primary, &ctx->cast_primary_hits,
                          &ctx->cast_secondary, &ctx->cast_secondary_hits, &ctx->cast_shadow, &ctx->cast_occluded })
@@ -959,11 +969,29 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     publish_counts_kernel<<<1, 32, 0, s>>>(counts, ctx->d_cast_counts_mapped);
     AE_CUDA(ctx, cudaGetLastError());
     AE_CUDA(ctx, cudaEventRecord(evCounts, s));
-    if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
-    AE_CUDA(ctx, cudaEventRecord(evSec, s));
     const float shadowMax = kInf - 2.0f * params->epsilon;   // rayHit.csh:333
-    if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, stream, counts + 1)) != AE_RT_OK) return st;
-    AE_CUDA(ctx, cudaEventRecord(evShd, s));
+    const bool secToHost = (out->secondary_hits && !IsDevicePointer(out->secondary_hits)) ||
+                           (out->secondary_rays && !IsDevicePointer(out->secondary_rays));
+    if (secToHost) {
+        // the bounce hits' copy to the host then runs during the shadow trace
+        if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
+        AE_CUDA(ctx, cudaEventRecord(evSec, s));
+        if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, stream, counts + 1)) != AE_RT_OK)
+            return st;
+        AE_CUDA(ctx, cudaEventRecord(evShd, s));
+    } else {
+        // the shadow trace beside the bounce trace (both read only the spawn's
+        // queues; separate work counters), each hiding the other's tail
+        if (!ctx->trace_stream) AE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->trace_stream, cudaStreamNonBlocking));
+        AE_CUDA(ctx, cudaStreamWaitEvent(ctx->trace_stream, evCounts, 0));
+        if ((st = Trace(ctx, true, mesh_id, shd, n, 0.0f, shadowMax, occ, ctx->trace_stream, counts + 1)) !=
+            AE_RT_OK)
+            return st;
+        AE_CUDA(ctx, cudaEventRecord(evShd, ctx->trace_stream));
+        if ((st = Trace(ctx, false, mesh_id, sec, n, 0.0f, kInf, secHits, stream, counts)) != AE_RT_OK) return st;
+        AE_CUDA(ctx, cudaEventRecord(evSec, s));
+        AE_CUDA(ctx, cudaStreamWaitEvent(s, evShd, 0));
+    }
     AE_CUDA(ctx, cudaEventSynchronize(evCounts));
     const volatile uint32_t* hc = ctx->h_cast_counts;
     const uint32_t nSec = hc[0], nShd = hc[1];

@@ -73,7 +73,8 @@ struct ae_rt_ctx {
     // path tracer queues
     atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
     uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2] shadow queue
-    uint32_t* d_counter = nullptr;     // [0] work counter, [1] error word
+    uint32_t* d_counter = nullptr;     // [1] error word; [0], [2..6] work counters (rotated per launch)
+    uint32_t next_work_slot = 0;
     unsigned long long* d_fetch = nullptr;
     atlas::rt::host::Scratch rays_in, results_out, batch_table, retest_count;
     // buffers of ae_rt_cast_pass
@@ -81,6 +82,7 @@ struct ae_rt_ctx {
     uint32_t* d_cast_counts = nullptr;
     // result copies of ae_rt_cast_pass overlap the later stages on this stream
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t trace_stream = nullptr;  // ae_rt_cast_pass: the shadow trace beside the bounce trace
     cudaEvent_t cast_events[4] = { nullptr, nullptr, nullptr, nullptr };
     uint32_t* h_cast_counts = nullptr;  // pinned, mapped
     uint32_t* d_cast_counts_mapped = nullptr;   // its device address

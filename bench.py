@@ -623,6 +623,9 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     launches_per_step = 5
 
+    side = torch.cuda.Stream(dev)
+    ev_spawn, ev_shadow = torch.cuda.Event(), torch.cuda.Event()
+
     def step(ev_trace=None):
         ctx.raygen(cam, prim, stream)
         if ev_trace is not None:
@@ -632,8 +635,13 @@ def main():
             ev_trace[1].record(stream)
         counts.zero_()
         ctx.spawn_bounce(mid, prim, prim_hits, n, bp, sec, shd, counts, stream=stream)
+        # the shadow trace beside the bounce trace, joined before the step ends
+        ev_spawn.record(stream)
+        side.wait_event(ev_spawn)
+        ctx.trace_any_queue(mid, shd, counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=side)
+        ev_shadow.record(side)
         ctx.trace_closest_queue(mid, sec, counts[0:1], n, TMIN, TINF, sec_hits, stream=stream)
-        ctx.trace_any_queue(mid, shd, counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=stream)
+        stream.wait_event(ev_shadow)
 
     # clocks are sampled from the warm-up through the last GPU workload
     clocks = ClockSampler(local)
