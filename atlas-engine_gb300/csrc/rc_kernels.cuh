@@ -20,11 +20,13 @@
 // touches the smooth indirect part, and its output is modulated back by the
 // base colour.
 // MLP: 5 hidden layers of 64 with ReLU, no biases, linear RGB output (padded
-// to 16 columns), BF16 weights, FP32 accumulation (mma.sync m16n8k16).
-// One CTA of 4 warps handles tiles of 128 queries; each warp owns 32 rows of
-// the activation tile in shared memory, so a layer needs only warp-level
-// synchronisation; the training kernel keeps every layer's activations of the
-// tile for the backward pass and reduces weight gradients with atomics.
+// to 16 columns), BF16 weights, FP32 accumulation.  Inference runs on the
+// tcgen05 tensor cores (rc_tc_kernels.cuh).  Training (this file) runs on
+// mma.sync m16n8k16 fragments: one CTA of 4 warps handles tiles of 128
+// records; each warp owns 32 rows of the activation tiles in shared memory,
+// so a layer needs only warp-level synchronisation; the kernel keeps every
+// layer's activations of the tile for the backward pass and reduces weight
+// gradients with atomics.
 #pragma once
 
 #include <cstdint>
@@ -281,8 +283,8 @@ __device__ __forceinline__ void store_rows(__nv_bfloat16* y, const float (&acc)[
         }
 }
 
-constexpr int RC_INFER = 0;    // accumulate throughput * max(prediction, 0) into the image
-constexpr int RC_PREDICT = 1;  // write predictions
+constexpr int RC_INFER = 0;    // inference: accumulate throughput * max(prediction, 0) into the image
+constexpr int RC_PREDICT = 1;  // inference: write predictions
 constexpr int RC_TRAIN = 2;    // relative-L2 loss, gradients
 
 struct RcMlpParams {
@@ -301,13 +303,16 @@ struct RcMlpParams {
     uint32_t* error_word;            // tensor-memory kernels: a bounded wait that gave up
 };
 
+// Training (fused encode + forward + relative-L2 loss + backward with weight
+// and hash-grid gradient atomics) on mma.sync BF16 fragments; inference runs
+// on the tcgen05 kernel of rc_tc_kernels.cuh.
 template <int MODE>
 static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParams p) {
+    static_assert(MODE == RC_TRAIN, "inference is rc_infer_tc_kernel");
     extern __shared__ __align__(16) unsigned char rc_smem[];
     __nv_bfloat16* wsm = reinterpret_cast<__nv_bfloat16*>(rc_smem);
-    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(rc_smem + RC_WBYTES);   // [6 or 1][128][72]
-    constexpr int NACT = MODE == RC_TRAIN ? RC_HIDDEN + 1 : 1;
-    __nv_bfloat16* dbuf = act + size_t(NACT) * RC_TILE * RC_STRIDE;                // [2][128][72] (train)
+    __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(rc_smem + RC_WBYTES);   // [6][128][72]
+    __nv_bfloat16* dbuf = act + size_t(RC_HIDDEN + 1) * RC_TILE * RC_STRIDE;       // [2][128][72]
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 
     // weights into shared memory (rows of 64 -> stride 72)
@@ -346,8 +351,8 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
         // ---- forward ----
 #pragma unroll 1
         for (int l = 0; l < RC_HIDDEN; l++) {
-            const __nv_bfloat16* xin = act + size_t(MODE == RC_TRAIN ? l : 0) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
-            __nv_bfloat16* yout = act + size_t(MODE == RC_TRAIN ? l + 1 : 0) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
+            const __nv_bfloat16* xin = act + size_t(l) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
+            __nv_bfloat16* yout = act + size_t(l + 1) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
             float acc[2][8][4];
             warp_gemm<8, 4>(xin, wsm + l * RC_W * RC_STRIDE, acc, lane);
             __syncwarp();
@@ -355,39 +360,10 @@ static __global__ void __launch_bounds__(RC_THREADS, 1) rc_mlp_kernel(RcMlpParam
             __syncwarp();
         }
         float oacc[2][2][4];
-        const __nv_bfloat16* xlast = act + size_t(MODE == RC_TRAIN ? RC_HIDDEN : 0) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
+        const __nv_bfloat16* xlast = act + size_t(RC_HIDDEN) * RC_TILE * RC_STRIDE + row0 * RC_STRIDE;
         warp_gemm<2, 4>(xlast, wsm + RC_HIDDEN * RC_W * RC_STRIDE, oacc, lane);
         // output element (row mb*16 + g (+8), col 2*(lane&3) + {0,1}) of n-block 0 holds RGB
         const uint32_t g = lane >> 2, cq = lane & 3u;
-        if (MODE != RC_TRAIN) {
-            // rows g and g+8 of each m-block: col 0,1 in cq==0, col 2 in cq==1
-#pragma unroll
-            for (int mb = 0; mb < 2; mb++)
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const float c0 = oacc[mb][0][2 * h], c1 = oacc[mb][0][2 * h + 1];
-                    const float c2 = __shfl_down_sync(0xffffffffu, c0, 1);
-                    const uint32_t rowInWarp = mb * 16 + g + 8 * h;
-                    const uint32_t src = row0 + rowInWarp;
-                    const uint32_t gj = tile * RC_TILE + src;
-                    // the record of that row: fetched by its own lane, shuffled here
-                    const float4 r3 = make_float4(__shfl_sync(0xffffffffu, q3.x, rowInWarp),
-                                                  __shfl_sync(0xffffffffu, q3.y, rowInWarp),
-                                                  __shfl_sync(0xffffffffu, q3.z, rowInWarp), 0.0f);
-                    const uint32_t pix = __float_as_uint(__shfl_sync(0xffffffffu, q1.w, rowInWarp));
-                    if (cq == 0 && gj < count) {
-                        if (MODE == RC_PREDICT) {
-                            p.out[first + gj] = make_float4(c0, c1, c2, 0.0f);
-                        } else {
-                            float4* a = p.accum + pix;
-                            a->x += r3.x * fmaxf(c0, 0.0f);
-                            a->y += r3.y * fmaxf(c1, 0.0f);
-                            a->z += r3.z * fmaxf(c2, 0.0f);
-                        }
-                    }
-                }
-            continue;
-        }
         // ---- relative L2 loss and its gradient (rows of the warp) ----
         __nv_bfloat16* dcur = dbuf;
         __nv_bfloat16* doth = dbuf + size_t(RC_TILE) * RC_STRIDE;
