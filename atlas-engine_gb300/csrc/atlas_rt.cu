@@ -244,6 +244,25 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
 
 }  // namespace
 
+ae_rt_status atlas::rt::host::EnsureBounceQueues(ae_rt_ctx* ctx, uint32_t capacity) {
+    for (int k = 0; k < 2; k++) {
+        AE_CUDA(ctx, ctx->pt_rays[k].ensure(size_t(capacity) * sizeof(ae_packed_ray)));
+        AE_CUDA(ctx, ctx->pt_pay[k].ensure(size_t(capacity) * sizeof(float4)));
+    }
+    AE_CUDA(ctx, ctx->pt_hits.ensure(size_t(capacity) * sizeof(ae_hit)));
+    for (Scratch* sc : { &ctx->pt_shadow, &ctx->pt_shadow2 })
+        AE_CUDA(ctx, sc->ensure(size_t(capacity) * sizeof(ae_packed_ray)));
+    for (Scratch* sc : { &ctx->pt_shadow_pay, &ctx->pt_shadow_pay2 })
+        AE_CUDA(ctx, sc->ensure(size_t(capacity) * sizeof(float4)));
+    for (Scratch* sc : { &ctx->pt_occ, &ctx->pt_occ2 })
+        AE_CUDA(ctx, sc->ensure(capacity));
+    if (!ctx->d_pt_counts) AE_CUDA(ctx, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+    if (!ctx->trace_stream) AE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->trace_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : ctx->pt_events)
+        if (!e) AE_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return AE_RT_OK;
+}
+
 ae_rt_status atlas::rt::host::TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity,
                                              float tmin, float tmax, void* out, void* stream,
                                              const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax) {
@@ -356,8 +375,11 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     cudaFree(ctx->d_lights);
     cudaFree(ctx->d_pt_counts);
     for (Scratch* sc : { &ctx->pt_rays[0], &ctx->pt_rays[1], &ctx->pt_pay[0], &ctx->pt_pay[1], &ctx->pt_hits,
-                         &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ })
+                         &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ, &ctx->pt_shadow2, &ctx->pt_shadow_pay2,
+                         &ctx->pt_occ2 })
         sc->release();
+    for (cudaEvent_t e : ctx->pt_events)
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->cast_events)
         if (e) cudaEventDestroy(e);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -758,15 +780,8 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t n = cam->width * cam->height;
-    for (int k = 0; k < 2; k++) {
-        AE_CUDA(ctx, ctx->pt_rays[k].ensure(size_t(n) * sizeof(ae_packed_ray)));
-        AE_CUDA(ctx, ctx->pt_pay[k].ensure(size_t(n) * sizeof(float4)));
-    }
-    AE_CUDA(ctx, ctx->pt_hits.ensure(size_t(n) * sizeof(ae_hit)));
-    AE_CUDA(ctx, ctx->pt_shadow.ensure(size_t(n) * sizeof(ae_packed_ray)));
-    AE_CUDA(ctx, ctx->pt_shadow_pay.ensure(size_t(n) * sizeof(float4)));
-    AE_CUDA(ctx, ctx->pt_occ.ensure(n));
-    if (!ctx->d_pt_counts) AE_CUDA(ctx, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
+    ae_rt_status qs = EnsureBounceQueues(ctx, n);
+    if (qs != AE_RT_OK) return qs;
 
     atlas::rt::dev::CameraParams c{};
     c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
@@ -789,15 +804,24 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
     p.epsilon = params->epsilon;
     p.seed = params->seed;
     p.mis = (params->flags & AE_PT_MIS) ? 1u : 0u;
+    // with MIS a later bounce's shading adds light hits into the pixels that
+    // the previous bounce's resolve (running beside it) adds into
+    p.atomic_accum = p.mis;
     p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
-    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
-    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
-    p.n_shadow = ctx->d_pt_counts + 2;
-    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
     p.accum = reinterpret_cast<float4*>(accum);
     p.accum64 = accum64;
     const uint32_t blocks = (n + 255) / 256;
     const float kInf = 1e12f;   // INF of common.hsh:8
+    // Shadow queues alternate between two buffers: a bounce's shadow trace and
+    // resolve run on the side stream while the next bounce is traced and shaded
+    // on `s` (the plain estimator's later bounces add nothing into accum, so
+    // only the resolves write it).  Events: [0], [1] shade done per queue,
+    // [2], [3] resolve done per queue.
+    Scratch* shadowRays[2] = { &ctx->pt_shadow, &ctx->pt_shadow2 };
+    Scratch* shadowPay[2] = { &ctx->pt_shadow_pay, &ctx->pt_shadow_pay2 };
+    Scratch* shadowOcc[2] = { &ctx->pt_occ, &ctx->pt_occ2 };
+    cudaStream_t side = ctx->trace_stream;
+    bool pending[2] = { false, false };
     for (uint32_t smp = 0; smp < params->spp; smp++) {
         p.sample = params->sample_offset + smp;
         // ray generation into queue 0
@@ -807,7 +831,7 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
         atlas::rt::dev::pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
         AE_CUDA(ctx, cudaGetLastError());
         for (uint32_t b = 0; b <= params->max_bounces; b++) {
-            const int in = int(b & 1), out = 1 - in;
+            const int in = int(b & 1), out = 1 - in, q = int(b & 1);
             p.bounce = b;
             p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
             p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
@@ -815,19 +839,33 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
             p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
             p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
             p.n_out = ctx->d_pt_counts + out;
+            p.shadow_rays = static_cast<float4*>(shadowRays[q]->ptr);
+            p.shadow_pay = static_cast<float4*>(shadowPay[q]->ptr);
+            p.n_shadow = ctx->d_pt_counts + 2 + q;
+            p.shadow_occ = static_cast<const uint8_t*>(shadowOcc[q]->ptr);
             ae_rt_status st = Trace(ctx, false, kSceneTarget, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n,
                                     0.0f, kInf, ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL);
             if (st != AE_RT_OK) return st;
+            // this shadow queue's previous resolve must be done before it is refilled
+            if (pending[q]) AE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
             AE_CUDA(ctx, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
-            AE_CUDA(ctx, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
+            AE_CUDA(ctx, cudaMemsetAsync(p.n_shadow, 0, sizeof(uint32_t), s));
             atlas::rt::dev::pt_shade_kernel<<<blocks, 256, 0, s>>>(p);
             AE_CUDA(ctx, cudaGetLastError());
-            st = Trace(ctx, true, kSceneTarget, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), n, 0.0f, kInf,
-                       ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
+            AE_CUDA(ctx, cudaEventRecord(ctx->pt_events[q], s));
+            AE_CUDA(ctx, cudaStreamWaitEvent(side, ctx->pt_events[q], 0));
+            st = Trace(ctx, true, kSceneTarget, static_cast<const ae_packed_ray*>(shadowRays[q]->ptr), n, 0.0f, kInf,
+                       shadowOcc[q]->ptr, side, p.n_shadow, AE_RT_MASK_SHADOW, true);
             if (st != AE_RT_OK) return st;
-            atlas::rt::dev::pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
+            atlas::rt::dev::pt_resolve_kernel<<<blocks, 256, 0, side>>>(p);
             AE_CUDA(ctx, cudaGetLastError());
+            AE_CUDA(ctx, cudaEventRecord(ctx->pt_events[2 + q], side));
+            pending[q] = true;
         }
+        // the sample's resolves finish before the next sample's first hits
+        // (whose emission goes into accum) are shaded
+        for (int q = 0; q < 2; q++)
+            if (pending[q]) AE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
     }
     return AE_RT_OK;
 }

@@ -72,7 +72,10 @@ struct ae_rt_ctx {
     uint32_t n_lights = 0;
     // path tracer queues
     atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
-    uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2] shadow queue
+    // a second shadow queue: a bounce's shadow trace runs beside the next bounce's trace
+    atlas::rt::host::Scratch pt_shadow2, pt_shadow_pay2, pt_occ2;
+    cudaEvent_t pt_events[4] = { nullptr, nullptr, nullptr, nullptr };
+    uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2], [3] shadow queues
     uint32_t* d_counter = nullptr;     // [1] error word; [0], [2..6] work counters (rotated per launch)
     uint32_t next_work_slot = 0;
     unsigned long long* d_fetch = nullptr;
@@ -125,5 +128,10 @@ inline bool IsDevicePointer(const void* p) {
 ae_rt_status TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity, float tmin,
                              float tmax, void* out, void* stream, const uint32_t* count_dev, uint32_t cull_mask,
                              bool per_ray_tmax);
+
+// The bounce loop's queues for `capacity` rays: two ray/payload queues, the
+// hit buffer, two shadow queues (a bounce's shadow trace runs on
+// ctx->trace_stream beside the next bounce), their counts and events.
+ae_rt_status EnsureBounceQueues(ae_rt_ctx* ctx, uint32_t capacity);
 
 }  // namespace atlas::rt::host

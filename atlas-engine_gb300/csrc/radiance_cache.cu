@@ -240,17 +240,10 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     if (n > kPixelMask + 1u) return RcFail(rc, AE_RT_INVALID_ARG, "more than 2^24 pixels");
     // queues hold twice the pixels: split glossy paths add rays
     const uint32_t cap = 2u * n;
-    for (int k = 0; k < 2; k++) {
-        RC_CUDA(rc, ctx->pt_rays[k].ensure(size_t(cap) * sizeof(ae_packed_ray)));
-        RC_CUDA(rc, ctx->pt_pay[k].ensure(size_t(cap) * sizeof(float4)));
-    }
-    RC_CUDA(rc, ctx->pt_hits.ensure(size_t(cap) * sizeof(ae_hit)));
-    RC_CUDA(rc, ctx->pt_shadow.ensure(size_t(cap) * sizeof(ae_packed_ray)));
-    RC_CUDA(rc, ctx->pt_shadow_pay.ensure(size_t(cap) * sizeof(float4)));
-    RC_CUDA(rc, ctx->pt_occ.ensure(cap));
+    ae_rt_status st = EnsureBounceQueues(ctx, cap);
+    if (st != AE_RT_OK) return st;
     RC_CUDA(rc, rc->queries.ensure(size_t(cap) * 64));
-    if (!ctx->d_pt_counts) RC_CUDA(rc, cudaMalloc(&ctx->d_pt_counts, 4 * sizeof(uint32_t)));
-    ae_rt_status st = EnsureStreams(rc);
+    st = EnsureStreams(rc);
     if (st != AE_RT_OK) return st;
     void* stream = s;
 
@@ -271,10 +264,6 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     p.seed = rc->cfg.seed + 17u;
     p.sample = frame;
     p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
-    p.shadow_rays = static_cast<float4*>(ctx->pt_shadow.ptr);
-    p.shadow_pay = static_cast<float4*>(ctx->pt_shadow_pay.ptr);
-    p.n_shadow = ctx->d_pt_counts + 2;
-    p.shadow_occ = static_cast<const uint8_t*>(ctx->pt_occ.ptr);
     p.accum = reinterpret_cast<float4*>(accum);
     p.atomic_accum = 1;
     p.capacity = cap;
@@ -298,9 +287,18 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     mp.n = cap;
     mp.accum = reinterpret_cast<float4*>(accum);
     cudaStream_t a0 = rc->aux[0];
+    // A vertex's shadow trace and resolve run on ctx->trace_stream beside the
+    // next vertex's trace and shading, with the shadow queues alternating
+    // (every write into accum here is atomic).
+    Scratch* shadowRays[2] = { &ctx->pt_shadow, &ctx->pt_shadow2 };
+    Scratch* shadowPay[2] = { &ctx->pt_shadow_pay, &ctx->pt_shadow_pay2 };
+    Scratch* shadowOcc[2] = { &ctx->pt_occ, &ctx->pt_occ2 };
+    cudaStream_t side = ctx->trace_stream;
+    void* sideStream = side;
+    bool pending[2] = { false, false };
     const uint32_t final_bounce = last_bounce < rc->max_bounces ? last_bounce : rc->max_bounces;
     for (uint32_t b = 0; b <= final_bounce; b++) {
-        const int in = int(b & 1), out = 1 - in;
+        const int in = int(b & 1), out = 1 - in, q = int(b & 1);
         p.bounce = b;
         p.rays_in = static_cast<const float4*>(ctx->pt_rays[in].ptr);
         p.pay_in = static_cast<const float4*>(ctx->pt_pay[in].ptr);
@@ -308,21 +306,30 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
         p.rays_out = static_cast<float4*>(ctx->pt_rays[out].ptr);
         p.pay_out = static_cast<float4*>(ctx->pt_pay[out].ptr);
         p.n_out = ctx->d_pt_counts + out;
+        p.shadow_rays = static_cast<float4*>(shadowRays[q]->ptr);
+        p.shadow_pay = static_cast<float4*>(shadowPay[q]->ptr);
+        p.n_shadow = ctx->d_pt_counts + 2 + q;
+        p.shadow_occ = static_cast<const uint8_t*>(shadowOcc[q]->ptr);
         st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), cap, 0.0f, 1e12f,
                              ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
         if (st != AE_RT_OK) return st;
+        if (pending[q]) RC_CUDA(rc, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
         RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
-        RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + 2, 0, sizeof(uint32_t), s));
+        RC_CUDA(rc, cudaMemsetAsync(p.n_shadow, 0, sizeof(uint32_t), s));
         rc_shade_kernel<<<blocks, 256, 0, s>>>(rp);
         RC_CUDA(rc, cudaGetLastError());
-        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(ctx->pt_shadow.ptr), cap, 0.0f, 1e12f,
-                             ctx->pt_occ.ptr, stream, ctx->d_pt_counts + 2, AE_RT_MASK_SHADOW, true);
+        RC_CUDA(rc, cudaEventRecord(ctx->pt_events[q], s));
+        RC_CUDA(rc, cudaStreamWaitEvent(side, ctx->pt_events[q], 0));
+        st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(shadowRays[q]->ptr), cap, 0.0f, 1e12f,
+                             shadowOcc[q]->ptr, sideStream, p.n_shadow, AE_RT_MASK_SHADOW, true);
         if (st != AE_RT_OK) return st;
-        pt_resolve_kernel<<<blocks, 256, 0, s>>>(p);
+        pt_resolve_kernel<<<blocks, 256, 0, side>>>(p);
         RC_CUDA(rc, cudaGetLastError());
+        RC_CUDA(rc, cudaEventRecord(ctx->pt_events[2 + q], side));
+        pending[q] = true;
         if (b == 0) {
-            // the first vertex's queries, answered on the side stream once
-            // every write of this vertex into accum is done
+            // the first vertex's queries (all appended by this vertex's
+            // shading), answered on another side stream
             RC_CUDA(rc, cudaMemcpyAsync(rc->d_counts + 2, rc->d_counts + 1, sizeof(uint32_t),
                                         cudaMemcpyDeviceToDevice, s));
             RC_CUDA(rc, cudaEventRecord(rc->ev[0], s));
@@ -341,6 +348,8 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     rc_infer_tc_kernel<RC_INFER><<<GridBlocks(rc, cap) * 3, RCT_THREADS, RCT_SMEM, s>>>(m1);
     RC_CUDA(rc, cudaGetLastError());
     RC_CUDA(rc, cudaStreamWaitEvent(s, rc->ev[1], 0));
+    for (int q = 0; q < 2; q++)
+        if (pending[q]) RC_CUDA(rc, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
     return AE_RT_OK;
 }
 
