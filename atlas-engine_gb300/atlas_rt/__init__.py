@@ -134,6 +134,17 @@ class BVH:
             _check(lib().ae_bvh_pack_shading(self._h, _ptr(self._verts), _ptr(nrm), _ptr(m), _ptr(o), _ptr(out)))
         return out
 
+    def pack_uvs(self, shading: np.ndarray, uvs) -> np.ndarray:
+        """Writes per-input-triangle UVs ((n, 3, 2) or (n, 6) float32) into the
+        GPUTriangle array from pack_shading as packHalf2x16 (MeshData.cpp:172-239)."""
+        uv = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6)
+        if self._verts is None or len(uv) != self.n_input or shading.shape != (len(self.order), 24) or shading.dtype != np.float32 \
+                or not shading.flags.c_contiguous:
+            raise ValueError("uvs must hold 6 floats per triangle and shading be the (n, 24) pack_shading array")
+        if len(self.order):
+            _check(lib().ae_bvh_pack_uvs(self._h, _ptr(uv), _ptr(shading)))
+        return shading
+
     @property
     def nodes_f32(self) -> np.ndarray:
         return self.nodes.view(np.float32).reshape(-1, 16)
@@ -143,6 +154,25 @@ class BVH:
         if h:
             lib().ae_bvh_destroy(h)
             self._h = None
+
+
+class _Texture(C.Structure):
+    """ae_texture"""
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32),
+                ("row_pitch", C.c_uint32)]
+
+
+TEX_R8_UNORM, TEX_RGBA8_UNORM, TEX_R32_FLOAT = 0, 1, 2
+
+
+def _texture_format(a: np.ndarray) -> int:
+    if a.dtype == np.uint8 and a.ndim == 2:
+        return TEX_R8_UNORM
+    if a.dtype == np.uint8 and a.ndim == 3 and a.shape[2] == 4:
+        return TEX_RGBA8_UNORM
+    if a.dtype == np.float32 and a.ndim == 2:
+        return TEX_R32_FLOAT
+    raise ValueError(f"unsupported texel array {a.dtype} {a.shape}: uint8 (h, w), uint8 (h, w, 4) or float32 (h, w)")
 
 
 class Context:
@@ -381,6 +411,19 @@ class Context:
         materials = np.ascontiguousarray(materials, MATERIAL_DTYPE)
         _check(lib().ae_rt_scene_set_materials(self._h, _ptr(materials) if len(materials) else None,
                                                len(materials)), self._h)
+
+    def set_textures(self, textures):
+        """The scene's texture table (ae_rt_scene_set_textures): a list of
+        texel arrays, uint8 (h, w) = R8 UNORM, uint8 (h, w, 4) = RGBA8 UNORM,
+        float32 (h, w) = R32 float; entry i is the materials' texture index i."""
+        arrs = [np.ascontiguousarray(t) for t in textures]
+        table = (_Texture * max(1, len(arrs)))()
+        for i, t in enumerate(arrs):
+            table[i].texels = t.ctypes.data
+            table[i].height, table[i].width = t.shape[0], t.shape[1]
+            table[i].format = _texture_format(t)
+            table[i].row_pitch = 0
+        _check(lib().ae_rt_scene_set_textures(self._h, table if arrs else None, len(arrs)), self._h)
 
     def set_lights(self, lights):
         lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 16)

@@ -76,6 +76,7 @@ _SIGNATURES = [
     ("ae_bvh_get_order", C.c_int, [P, P, P]),
     ("ae_bvh_pack_triangles", C.c_int, [P, P, P, P, P]),
     ("ae_bvh_pack_shading", C.c_int, [P, P, P, P, P, P]),
+    ("ae_bvh_pack_uvs", C.c_int, [P, P, P]),
     ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     ("ae_rt_ctx_destroy", None, [P]),
     ("ae_rt_last_error", C.c_char_p, [P]),
@@ -99,6 +100,7 @@ _SIGNATURES = [
     ("ae_rt_batch_plan_launch", C.c_int, [P, P]),
     ("ae_rt_batch_plan_destroy", None, [P]),
     ("ae_rt_scene_set_materials", C.c_int, [P, P, U32]),
+    ("ae_rt_scene_set_textures", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
     ("ae_rc_create", C.c_int, [P, C.POINTER(RcConfig), C.POINTER(P)]),

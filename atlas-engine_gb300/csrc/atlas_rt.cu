@@ -4,6 +4,7 @@
 #include "trace_kernels.cuh"
 #include "cast_kernels.cuh"
 #include "pt_kernels.cuh"
+#include "texture.cuh"
 #include "bvh_builder.h"
 
 #include <cuda_runtime.h>
@@ -372,11 +373,14 @@ void ae_rt_ctx_destroy(ae_rt_ctx* ctx) {
     cudaFree(ctx->d_mesh_table);
     cudaFree(ctx->d_inst_model);
     cudaFree(ctx->d_materials);
+    cudaFree(ctx->d_tex_pool);
+    cudaFree(ctx->d_tex_desc);
     cudaFree(ctx->d_lights);
     cudaFree(ctx->d_pt_counts);
     for (Scratch* sc : { &ctx->pt_rays[0], &ctx->pt_rays[1], &ctx->pt_pay[0], &ctx->pt_pay[1], &ctx->pt_hits,
                          &ctx->pt_shadow, &ctx->pt_shadow_pay, &ctx->pt_occ, &ctx->pt_shadow2, &ctx->pt_shadow_pay2,
-                         &ctx->pt_occ2 })
+                         &ctx->pt_occ2, &ctx->pass_rays, &ctx->pass_key, &ctx->pass_hits, &ctx->pass_rad,
+                         &ctx->pass_shadow, &ctx->pass_shadow_pay, &ctx->pass_vis, &ctx->pass_counts })
         sc->release();
     for (cudaEvent_t e : ctx->pt_events)
         if (e) cudaEventDestroy(e);
@@ -738,6 +742,52 @@ ae_rt_status ae_rt_scene_set_materials(ae_rt_ctx* ctx, const ae_material* materi
         AE_CUDA(ctx, cudaMemcpy(ctx->d_materials, materials, size_t(n) * sizeof(ae_material), cudaMemcpyHostToDevice));
     }
     ctx->n_materials = n;
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n) {
+    if (!ctx || (n && !textures)) return AE_RT_INVALID_ARG;
+    std::vector<atlas::rt::dev::TexDesc> desc(n);
+    size_t total = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const ae_texture& t = textures[i];
+        const std::string what = "texture " + std::to_string(i) + ": ";
+        if (!t.texels) return Fail(ctx, AE_RT_INVALID_ARG, what + "null texels");
+        if (t.width == 0 || t.height == 0 || t.width > 65536u || t.height > 65536u)
+            return Fail(ctx, AE_RT_INVALID_ARG, what + "width and height must lie in [1, 65536]");
+        if (t.format > AE_TEX_R32_FLOAT) return Fail(ctx, AE_RT_INVALID_ARG, what + "unknown format");
+        const uint32_t texel = t.format == AE_TEX_R8_UNORM ? 1u : 4u;
+        const uint32_t row = t.width * texel;
+        if (t.row_pitch != 0 && t.row_pitch < row) return Fail(ctx, AE_RT_INVALID_ARG, what + "row pitch below a row");
+        desc[i] = atlas::rt::dev::TexDesc{};
+        desc[i].offset = total;
+        desc[i].width = t.width;
+        desc[i].height = t.height;
+        desc[i].format = t.format;
+        desc[i].row_pitch = row;
+        total += (size_t(row) * t.height + 15u) & ~size_t(15);
+    }
+    std::vector<uint8_t> pool(total);
+    for (uint32_t i = 0; i < n; i++) {
+        const ae_texture& t = textures[i];
+        const size_t pitch = t.row_pitch ? t.row_pitch : desc[i].row_pitch;
+        for (uint32_t y = 0; y < t.height; y++)
+            std::memcpy(pool.data() + desc[i].offset + size_t(y) * desc[i].row_pitch,
+                        static_cast<const uint8_t*>(t.texels) + size_t(y) * pitch, desc[i].row_pitch);
+    }
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaFree(ctx->d_tex_pool);
+    cudaFree(ctx->d_tex_desc);
+    ctx->d_tex_pool = nullptr;
+    ctx->d_tex_desc = nullptr;
+    ctx->n_textures = 0;
+    if (n) {
+        AE_CUDA(ctx, cudaMalloc(&ctx->d_tex_pool, total));
+        AE_CUDA(ctx, cudaMalloc(&ctx->d_tex_desc, desc.size() * sizeof(desc[0])));
+        AE_CUDA(ctx, cudaMemcpy(ctx->d_tex_pool, pool.data(), total, cudaMemcpyHostToDevice));
+        AE_CUDA(ctx, cudaMemcpy(ctx->d_tex_desc, desc.data(), desc.size() * sizeof(desc[0]), cudaMemcpyHostToDevice));
+    }
+    ctx->n_textures = n;
     return AE_RT_OK;
 }
 

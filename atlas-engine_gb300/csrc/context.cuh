@@ -68,6 +68,9 @@ struct ae_rt_ctx {
     float4* d_inst_model = nullptr;     // object-to-world rows per instance (shading)
     float* d_materials = nullptr;       // GPUMaterial array
     uint32_t n_materials = 0;
+    uint8_t* d_tex_pool = nullptr;      // level 0 of every texture (texture.cuh)
+    void* d_tex_desc = nullptr;         // dev::TexDesc per texture
+    uint32_t n_textures = 0;
     float4* d_lights = nullptr;         // GPULight array
     uint32_t n_lights = 0;
     // path tracer queues
@@ -75,6 +78,9 @@ struct ae_rt_ctx {
     // a second shadow queue: a bounce's shadow trace runs beside the next bounce's trace
     atlas::rt::host::Scratch pt_shadow2, pt_shadow_pay2, pt_occ2;
     cudaEvent_t pt_events[4] = { nullptr, nullptr, nullptr, nullptr };
+    // scratch of the RTAO / reflection / GI / DDGI passes (consumers.cu)
+    atlas::rt::host::Scratch pass_rays, pass_key, pass_hits, pass_rad, pass_shadow, pass_shadow_pay, pass_vis,
+        pass_counts;
     uint32_t* d_pt_counts = nullptr;    // [0], [1] ray queues, [2], [3] shadow queues
     uint32_t* d_counter = nullptr;     // [1] error word; [0], [2..6] work counters (rotated per launch)
     uint32_t next_work_slot = 0;
@@ -128,6 +134,13 @@ inline bool IsDevicePointer(const void* p) {
 ae_rt_status TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity, float tmin,
                              float tmax, void* out, void* stream, const uint32_t* count_dev, uint32_t cull_mask,
                              bool per_ray_tmax);
+
+// The transparency traversal variants over the scene (transparency.cu); with
+// count_dev, `n` is the queue capacity and the count lives on the device;
+// with per_ray_tmax, ray i's tmax is its third vector's x.
+ae_rt_status TraceTransparency(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t n, float tmin,
+                               float tmax, uint32_t cull_mask, void* out, void* stream,
+                               const uint32_t* count_dev = nullptr, bool per_ray_tmax = false);
 
 // The bounce loop's queues for `capacity` rays: two ray/payload queues, the
 // hit buffer, two shadow queues (a bounce's shadow trace runs on

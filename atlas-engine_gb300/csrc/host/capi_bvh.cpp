@@ -109,6 +109,33 @@ float Bits(int32_t v) {
     return f;
 }
 
+// IEEE binary16 bits of f, rounded to nearest even (glm::packHalf2x16):
+// overflow to infinity, NaN payloads keep their top mantissa bits.
+uint16_t HalfBits(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7FFFFFFFu;
+    if (ax >= 0x7F800000u) {
+        const uint32_t m = (ax & 0x7FFFFFu) >> 13;
+        return uint16_t(sign | 0x7C00u | (ax > 0x7F800000u ? (m ? m : 1u) : 0u));
+    }
+    if (ax >= 0x477FF000u) return uint16_t(sign | 0x7C00u);   // rounds to 65520 or more
+    uint32_t r, rem, halfway;
+    if (ax < 0x38800000u) {                                      // half subnormal (or zero)
+        if (ax < 0x33000000u) return uint16_t(sign);
+        const uint32_t e = ax >> 23, m = (ax & 0x7FFFFFu) | 0x800000u, shift = 126u - e;
+        r = m >> shift;
+        rem = m & ((1u << shift) - 1u);
+        halfway = 1u << (shift - 1u);
+    } else {
+        r = (ax - 0x38000000u) >> 13;                            // exponent rebiased by -112
+        rem = ax & 0x1FFFu;
+        halfway = 0x1000u;
+    }
+    if (rem > halfway || (rem == halfway && (r & 1u))) r++;
+    return uint16_t(sign | r);
+}
+
 void Normalize3(const float* in, float* out) {
     const float l = std::sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
     const float s = l > 0.0f ? 1.0f / l : 0.0f;
@@ -160,6 +187,19 @@ ae_rt_status ae_bvh_pack_shading(const ae_bvh* bvh, const float* verts, const fl
         const int32_t white = int32_t(0xFFFFFFFFu);
         o.d2[0] = Bits(white); o.d2[1] = Bits(white); o.d2[2] = Bits(white);
         o.d2[3] = opacity ? opacity[src] : 1.0f;
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_bvh_pack_uvs(const ae_bvh* bvh, const float* uvs, ae_triangle* inout) {
+    if (!bvh || (bvh->primitives && (!uvs || !inout))) return AE_RT_INVALID_ARG;
+    for (uint32_t i = 0; i < bvh->primitives; i++) {
+        const float* uv = uvs + size_t(bvh->built.order[i]) * 6;
+        for (int k = 0; k < 3; k++) {
+            // packHalf2x16: x in the low half, y in the high half
+            const uint32_t bits = uint32_t(HalfBits(uv[2 * k])) | (uint32_t(HalfBits(uv[2 * k + 1])) << 16);
+            inout[i].d0[k] = Bits(int32_t(bits));
+        }
     }
     return AE_RT_OK;
 }

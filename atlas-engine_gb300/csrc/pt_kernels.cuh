@@ -115,7 +115,7 @@ __device__ __forceinline__ float rng(uint32_t pixel, uint32_t sample, uint32_t b
 struct Mat {
     V3 base, emissive;
     float opacity, roughness, metalness, ao, reflectance;
-    int twoSided;
+    int twoSided, cullBackFaces;
 };
 
 __device__ __forceinline__ Mat load_material(const float* m) {
@@ -128,6 +128,7 @@ __device__ __forceinline__ Mat load_material(const float* m) {
     r.ao = m[10];
     r.reflectance = m[11];
     r.twoSided = __float_as_int(m[14]);
+    r.cullBackFaces = __float_as_int(m[15]);
     return r;
 }
 
@@ -137,6 +138,7 @@ struct Surf {
     V3 F0;
     float F90;
     Mat mat;
+    bool backface;      // backfaceHit of GetSurfaceParameters (surface.hsh:99)
 };
 
 // UpdateSurface (brdf/surface.hsh:25-41)
@@ -366,6 +368,7 @@ __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, fl
     V3 N = normalize(tri.n0 * r + tri.n1 * bu + tri.n2 * bv);
     V3 triN = normalize(cross(tri.v0 - tri.v1, tri.v0 - tri.v2));
     const bool flip = dot(triN, rd) > 0.0f;
+    sf.backface = sf.mat.twoSided > 0 || sf.mat.cullBackFaces == 0 ? false : flip;
     if (flip && sf.mat.twoSided > 0) triN = triN * -1.0f;
     if (dot(N, triN) < 0.0f && sf.mat.twoSided > 0) N = N * -1.0f;
     sf.V = rd * -1.0f;
@@ -393,9 +396,16 @@ __device__ __forceinline__ float light_weight(const Light& L, V3 P) {
 // light, samples it, evaluates the BRDF.  Returns false when nothing needs a
 // shadow ray; otherwise the contribution (already scaled by the path
 // throughput) and the shadow ray (origin, direction, tmax).
-__device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr, uint32_t pix, uint32_t sample,
-                                             uint32_t bounce, uint32_t seed, float eps, V3& contrib, V3& so,
-                                             V3& sd, float& stmax, float* pdf_sa = nullptr) {
+// GetLight + SampleLight (raytracer/direct.hsh:12-86): picks one light by
+// streaming weighted selection, samples a point on it (triangle lights) and
+// points sf.L at it (UpdateSurface).  False when the scene has no lights.
+struct LightSample {
+    V3 radiance;
+    float pdf, solidAngle, dist;
+    uint32_t type;
+};
+__device__ __forceinline__ bool sample_light(const PtScene& sc, Surf& sf, uint32_t pix, uint32_t sample,
+                                             uint32_t bounce, uint32_t seed, LightSample& ls) {
     if (sc.n_lights == 0) return false;
     Light sel{};
     float selW = 0.0f, total = 0.0f;
@@ -408,8 +418,11 @@ __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr
             sel = L;
         }
     }
-    const float lightPdf = selW / total * sel.pdf;
-    float solidAngle = 1.0f, dist = 1e12f;
+    ls.pdf = selW / total * sel.pdf;
+    ls.solidAngle = 1.0f;
+    ls.dist = 1e12f;
+    ls.type = sel.type;
+    ls.radiance = sel.radiance;
     if (sel.type == 1u) {
         const float r0 = rng(pix, sample, bounce, 1, seed);
         const float r1 = rng(pix, sample, bounce, 2, seed);
@@ -419,18 +432,27 @@ __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr
         const V3 LN = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
         const V3 toL = LP - sf.P;
         const float d2 = dot(toL, toL);
-        dist = sqrtf(d2);
-        sf.L = toL * (1.0f / dist);
+        ls.dist = sqrtf(d2);
+        sf.L = toL * (1.0f / ls.dist);
         update_surface(sf);
         const float NdotLl = fmaxf(dot(LN, sf.L * -1.0f), 0.0f);
-        solidAngle = NdotLl / (d2 * (1.0f / sel.area));
+        ls.solidAngle = NdotLl / (d2 * (1.0f / sel.area));
     } else {
         sf.L = normalize(sel.N * -1.0f);
         update_surface(sf);
     }
+    return true;
+}
+
+__device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr, uint32_t pix, uint32_t sample,
+                                             uint32_t bounce, uint32_t seed, float eps, V3& contrib, V3& so,
+                                             V3& sd, float& stmax, float* pdf_sa = nullptr) {
+    LightSample ls;
+    if (!sample_light(sc, sf, pix, sample, bounce, seed, ls)) return false;
+    const float lightPdf = ls.pdf, solidAngle = ls.solidAngle, dist = ls.dist;
     const V3 refl = (eval_diffuse(sf) + eval_specular(sf)) * sf.mat.opacity;
-    contrib = thr * sf.mat.opacity * (refl * sel.radiance) * (solidAngle * sf.NdotL / lightPdf);
-    if (pdf_sa) *pdf_sa = sel.type == 1u ? (solidAngle > 0.0f ? lightPdf / solidAngle : 0.0f) : 0.0f;
+    contrib = thr * sf.mat.opacity * (refl * ls.radiance) * (solidAngle * sf.NdotL / lightPdf);
+    if (pdf_sa) *pdf_sa = ls.type == 1u ? (solidAngle > 0.0f ? lightPdf / solidAngle : 0.0f) : 0.0f;
     if (!(sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f)) return false;
     so = sf.P + sf.N * eps;         // CheckVisibility, rayHit.csh:327-338
     sd = sf.L;

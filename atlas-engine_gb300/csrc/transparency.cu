@@ -8,10 +8,9 @@
 // the instance transform are the bit-exact ones of the opaque traversal
 // (trace_kernels.cuh); the leaves read the 96-byte shading triangle
 // (UnpackTriangle, common.hsh:17-44): its vertices, endOfNode = d1.z > 0 and
-// opacity = d2.w, or, when that is negative, GetOpacity (surface.hsh:147-159):
-// the material's opacity times its opacity texture, which samples as 1.0
-// when absent (texture.hsh:18-25) -- bound opacity textures are not sampled
-// here (factor 1.0).
+// opacity = d2.w, or, when that is negative, GetOpacity (surface.hsh:147-159,
+// texture.cuh): the material's opacity times its opacity texture sampled at
+// the hit's interpolated UV, 1.0 when absent (texture.hsh:18-25).
 //  * closest: a triangle hit counts only where its opacity is > 0;
 //  * any: every accepted triangle multiplies the leaf's running
 //    transparency, which starts from the current value; the leaf's result
@@ -23,6 +22,7 @@
 #include "atlas_rt.h"
 #include "context.cuh"
 #include "trace_kernels.cuh"
+#include "texture.cuh"
 
 using namespace atlas::rt::host;
 using namespace atlas::rt::dev;
@@ -37,8 +37,12 @@ struct TransParams {
     const float4* instances;
     const MeshDesc* meshes;
     const float* materials;      // GPUMaterial (23 words), may be null (opacity 1)
+    uint32_t n_materials;
+    TexTable textures;
     const float4* rays;
-    uint32_t n;
+    uint32_t n;                  // rays, or the queue's capacity when count is set
+    const uint32_t* count;       // device-side ray count (queues), or null
+    uint32_t per_ray_tmax;       // tmax of ray i = its third vector's x
     float tmin, tmax;
     uint32_t cull_mask;
     uint32_t max_steps;
@@ -47,24 +51,25 @@ struct TransParams {
     uint32_t* error_word;
 };
 
-__device__ __forceinline__ float shading_opacity(const TransParams& p, float4 d0, float4 d2, int32_t matOffset) {
-    if (d2.w >= 0.0f) return d2.w;
-    if (!p.materials) return 1.0f;
-    const float* m = p.materials + size_t(__float_as_int(d0.w) + matOffset) * 23;
-    return __fmul_rn(1.0f, m[7]);
+// `tri.opacity < 0.0 ? GetOpacity(tri, sol.yz, materialOffset, 0) : tri.opacity`
+__device__ __forceinline__ float shading_opacity(const TransParams& p, float4 d0, float4 d2, int32_t matOffset,
+                                                 float u, float v) {
+    if (!(d2.w < 0.0f)) return d2.w;
+    return get_opacity(p.materials, p.n_materials, p.textures, d0, matOffset, u, v);
 }
 
 template <bool ANY>
 __global__ void transparency_kernel(TransParams p) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+    const uint32_t n = p.count ? min(*p.count, p.n) : p.n;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
         const float4 o4 = p.rays[i * 3], d4 = p.rays[i * 3 + 1];
         TRay wr{};
         wr.ox = o4.x; wr.oy = o4.y; wr.oz = o4.z;
         wr.dx = d4.x; wr.dy = d4.y; wr.dz = d4.z;
         wr.prepare();
         TRay r = wr;
-        const float tMin = p.tmin, tMax = p.tmax;
+        const float tMin = p.tmin, tMax = p.per_ray_tmax ? p.rays[i * 3 + 2].x : p.tmax;
         float hitDist = tMax, hu = 0.0f, hv = 0.0f, transparency = 1.0f;
         int32_t hitID = -1, hitInst = -1, curInst = -1, matOffset = 0;
         uint32_t flags = 0;
@@ -145,8 +150,8 @@ __global__ void transparency_kernel(TransParams p) {
                         const bool hit = tri_test(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
                         if (ANY) {
                             if (hit && t > tMin && t < tMax)
-                                leaf = __fmul_rn(leaf, __fsub_rn(1.0f, shading_opacity(p, d0, d2, matOffset)));
-                        } else if (hit && t > tMin && t < hitDist && shading_opacity(p, d0, d2, matOffset) > 0.0f) {
+                                leaf = __fmul_rn(leaf, __fsub_rn(1.0f, shading_opacity(p, d0, d2, matOffset, u, v)));
+                        } else if (hit && t > tMin && t < hitDist && shading_opacity(p, d0, d2, matOffset, u, v) > 0.0f) {
                             hitDist = t; hitID = tp; hu = u; hv = v; hitInst = curInst;
                         }
                         tp++;
@@ -192,13 +197,18 @@ __global__ void transparency_kernel(TransParams p) {
     }
 }
 
-ae_rt_status TraceTransparency(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t n, float tmin,
-                               float tmax, uint32_t cull_mask, void* out, void* stream) {
+}  // namespace
+
+ae_rt_status atlas::rt::host::TraceTransparency(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t n,
+                                                float tmin, float tmax, uint32_t cull_mask, void* out, void* stream,
+                                                const uint32_t* count_dev, bool per_ray_tmax) {
     if (!ctx) return AE_RT_INVALID_ARG;
     if (!ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
     if (n == 0) return AE_RT_OK;
     if (!rays || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray or result buffer");
     if (n > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one call");
+    if (count_dev && (!IsDevicePointer(rays) || !IsDevicePointer(out)))
+        return Fail(ctx, AE_RT_INVALID_ARG, "queue traces take device buffers");
     for (const DeviceMesh& m : ctx->meshes)
         if (m.n_nodes > 0 && !m.shading)
             return Fail(ctx, AE_RT_INVALID_ARG, "transparency queries need the meshes' shading triangles");
@@ -223,8 +233,14 @@ ae_rt_status TraceTransparency(ae_rt_ctx* ctx, bool any, const ae_packed_ray* ra
     p.instances = ctx->d_instances;
     p.meshes = ctx->d_mesh_table;
     p.materials = ctx->d_materials;
+    p.n_materials = ctx->n_materials;
+    p.textures.pool = ctx->d_tex_pool;
+    p.textures.desc = static_cast<const TexDesc*>(ctx->d_tex_desc);
+    p.textures.n = ctx->n_textures;
     p.rays = static_cast<const float4*>(d_rays);
     p.n = n;
+    p.count = count_dev;
+    p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
     p.tmin = tmin;
     p.tmax = tmax;
     p.cull_mask = cull_mask;
@@ -241,8 +257,6 @@ ae_rt_status TraceTransparency(ae_rt_ctx* ctx, bool any, const ae_packed_ray* ra
     if (!out_dev || !rays_dev) return ae_rt_synchronize(ctx, stream);
     return AE_RT_OK;
 }
-
-}  // namespace
 
 extern "C" {
 

@@ -209,6 +209,12 @@ ae_rt_status ae_bvh_pack_triangles(const ae_bvh* bvh, const float* verts, const 
 ae_rt_status ae_bvh_pack_shading(const ae_bvh* bvh, const float* verts, const float* normals,
                                  const int32_t* material, const float* opacity, ae_triangle* out);
 
+/* Texture coordinates into GPUTriangle d0.xyz (MeshData.cpp:172-239:
+ * packHalf2x16 of the three vertices' UVs, round to nearest even): uvs is
+ * n * 6 floats per input triangle (u0, v0, u1, v1, u2, v2), `inout` the
+ * GPUTriangle array in BVH order that ae_bvh_pack_shading filled. */
+ae_rt_status ae_bvh_pack_uvs(const ae_bvh* bvh, const float* uvs, ae_triangle* inout);
+
 /* ------------------------------------------------------------------------ */
 /* Device context                                                            */
 /* ------------------------------------------------------------------------ */
@@ -301,8 +307,11 @@ ae_rt_status ae_rt_trace_scene_any_queue(ae_rt_ctx* ctx, const ae_packed_ray* ra
 
 /* The transparency variants over the scene (every mesh needs its shading
  * triangles; materials from ae_rt_scene_set_materials, or opacity 1 when
- * none are set).  Opacity = GPUTriangle d2.w, or, when negative, the
- * material's opacity (opacity textures are not sampled: factor 1).
+ * none are set).  Opacity = GPUTriangle d2.w, or, when negative, GetOpacity
+ * (surface.hsh:147-159): the material's opacity times its opacity texture
+ * (ae_rt_scene_set_textures) sampled at the hit's interpolated UV, with v
+ * flipped when the material's invertUVs > 0; a material index outside the
+ * material array counts as opacity 1.
  * Replace HitClosestTransparency (bvh.hsh:275-357: only hits with opacity > 0
  * count) and HitAnyTransparency (bvh.hsh:443-524: `transparency` receives
  * the shader's return value, 1 = unoccluded, including its per-leaf
@@ -456,6 +465,37 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
  * Replaces RayTracingWorld::UpdateMaterials (RayTracingWorld.cpp:171-251)
  * and RayTracingHelper::UpdateLights (RayTracingHelper.cpp:436-500). */
 ae_rt_status ae_rt_scene_set_materials(ae_rt_ctx* ctx, const ae_material* materials, uint32_t n);
+
+/* Texel formats of ae_texture; sampling reads the first channel. */
+#define AE_TEX_R8_UNORM    0u
+#define AE_TEX_RGBA8_UNORM 1u
+#define AE_TEX_R32_FLOAT   2u
+
+/* One texture's base level in host memory: `height` rows of `row_pitch`
+ * bytes (0 = tightly packed), 1 <= width, height <= 65536. */
+typedef struct ae_texture {
+    const void* texels;
+    uint32_t width;
+    uint32_t height;
+    uint32_t format;
+    uint32_t row_pitch;
+} ae_texture;
+
+/* The scene's textures: the bindless texture array (globals.hsh:33) that
+ * RayTracingWorld::UpdateMaterials indexes through
+ * Scene::textureToBindlessIdx (RayTracingWorld.cpp:217-237); texture i is
+ * what a material's *Texture field i names, and a negative or out-of-range
+ * index samples as 1.0 (texture.hsh:18-25 for negative ones).  Only level 0
+ * is kept: every traversal lookup samples level 0 (bvh.hsh:127, :163).
+ * Sampling follows the engine's bindless sampler (linear filter, repeat
+ * addressing, MainRenderer.cpp:922-929) in FP32, one rounding per
+ * operation: x = u * width - 0.5, i = floor(x), a = x - i, texels i and i+1
+ * modulo width (likewise y with v and height), value = ((w00*c00 + w10*c10)
+ * + w01*c01) + w11*c11 with w00 = (1-a)(1-b), w10 = a(1-b), w01 = (1-a)b,
+ * w11 = ab; UNORM texels are byte / 255; a non-finite x (or y) becomes 0,
+ * which reads texel 0 of that axis alone.  Copies the texels into device memory and replaces the previous
+ * table (n = 0 clears it). */
+ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n);
 ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n);
 
 typedef struct ae_pt_params {
@@ -482,6 +522,115 @@ typedef struct ae_pt_params {
  * non-real-time mode, without the indirect radiance clamp (rayHit.csh:196-201). */
 ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
                              double* accum64, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* The traversal's other consumers: RTAO, reflections, RTGI, DDGI probe rays  */
+/* ------------------------------------------------------------------------ */
+
+/* The G-buffer that a screen-space pass reads, all device memory, `width` x
+ * `height` pixels row by row:
+ *   depth      one float per pixel, NDC depth (>= 1: nothing drawn);
+ *   normal     two floats per pixel, the octahedral view-space normal
+ *              (DecodeNormal, common/normalencode.hsh:18-30);
+ *   offset     optional byte per pixel, 0..3: which pixel of its 2x2 block a
+ *              half-resolution depth sample came from (offsets[],
+ *              ao/rtao.csh:27-32); NULL = 0;
+ *   roughness  one float per pixel, the material roughness after its map
+ *              (reflections only; rtreflection.csh:92-96);
+ *   samples    optional two floats per pixel in [0, 1): the shader's
+ *              blue-noise vector; NULL = the library's PCG hash of (pixel,
+ *              frame_seed);
+ *   ip_matrix, iv_matrix  inverse projection and inverse view, column-major
+ *              like GLSL's mat4 (globalData.ipMatrix / ivMatrix);
+ *   half_res   1: this buffer has half the depth buffer's resolution, and
+ *              positions are reconstructed at 2*pixel + offset + 0.5 of the
+ *              full one (ao/rtao.csh:66, rtreflection.csh:75-79).
+ * World position = iv * (ConvertDepthToViewSpace: ip * (2*tc - 1, depth, 1),
+ * divided by w); world normal = normalize(iv * (DecodeNormal(normal), 0)). */
+typedef struct ae_gbuffer {
+    const float* depth;
+    const float* normal;
+    const uint8_t* offset;
+    const float* roughness;
+    const float* samples;
+    uint32_t width;
+    uint32_t height;
+    uint32_t half_res;
+    uint32_t reserved;
+    float ip_matrix[16];
+    float iv_matrix[16];
+} ae_gbuffer;
+
+#define AE_PASS_OPACITY_CHECK 0x1u   /* trace with the transparency variants (OPACITY_CHECK) */
+
+/* Uniforms of the passes. */
+typedef struct ae_rt_pass_params {
+    float radius;            /* RTAO: length of the occlusion rays */
+    float bias;              /* reflections: sample.y *= 1 - bias; RTGI: sample.x *= 1 - bias */
+    float roughness_cutoff;  /* reflections: rougher pixels trace nothing (radiance 0) */
+    float radiance_limit;    /* reflections, RTGI: colours scaled so no channel exceeds it */
+    float environment[3];    /* radiance of rays that hit nothing (the environment map's place) */
+    uint32_t flags;          /* AE_PASS_OPACITY_CHECK */
+    uint32_t frame_seed;     /* uniforms.frameSeed: the sample index of the random streams */
+    uint32_t seed;           /* random stream of light choices (and of samples when none are given) */
+} ae_rt_pass_params;
+
+/* Ray-traced ambient occlusion, ao/rtao.csh:40-112: per pixel with depth < 1
+ * one cosine-weighted ray (SampleDiffuseBRDF, brdf/brdfSample.hsh:8-32) from
+ * P + L*EPSILON + N*EPSILON, HitAny (or, with AE_PASS_OPACITY_CHECK,
+ * 1 - HitAnyTransparency) over [0, radius], mask ALL; ao = 1 - occlusion,
+ * 1 where nothing was drawn.  ao: one float per pixel, device memory. */
+ae_rt_status ae_rt_rtao(ae_rt_ctx* ctx, const ae_gbuffer* gb, const ae_rt_pass_params* params, float* ao,
+                        void* stream);
+
+/* Ray-traced reflections, reflection/rtreflection.csh:60-245: per pixel with
+ * depth < 1 and roughness <= 1, a GGX VNDF sample (roughness > 0.01) or the
+ * mirror direction, from P offset by EPSILON * 0.1 * max(1, |viewPos|) * 0.1
+ * along L and N; pixels with roughness <= roughness_cutoff trace HitClosest
+ * (HitClosestTransparency) over [0, INF] and shade the hit: emission + one
+ * light sample with the Disney diffuse + GGX specular BRDF times opacity,
+ * visible through HitAnyTransparency (mask SHADOW, up to the light distance
+ * - 2*EPSILON); misses return `environment`; no DDGI term.  Then the
+ * radiance limit.  radiance: four floats per pixel (rgb, 1), device memory. */
+ae_rt_status ae_rt_reflections(ae_rt_ctx* ctx, const ae_gbuffer* gb, const ae_rt_pass_params* params,
+                               float* radiance, void* stream);
+
+/* Ray-traced diffuse GI, rtgi/rtgi.csh:100-234: a cosine-weighted sample
+ * (ImportanceSampleCosDir, brdf/importanceSample.hsh:82-101) from P offset by
+ * EPSILON * max(1, |viewPos|) * 0.01 along L and N, traced and shaded like
+ * the reflections.  radiance: four floats per pixel, device memory. */
+ae_rt_status ae_rt_rtgi(ae_rt_ctx* ctx, const ae_gbuffer* gb, const ae_rt_pass_params* params, float* radiance,
+                        void* stream);
+
+/* DDGI probe rays, ddgi/rayGen.csh:39-81 + ddgi/rayHit.csh:37-151.
+ *   probes    n_probes x 4 floats: probe position + offset (xyz) and the
+ *             probe state's bits in w (0 new, 1 active, 2 inactive);
+ *   ray_dirs / ray_dirs_inactive  ray_count / inactive_ray_count x 4 floats;
+ *   rotation  the frame's random rotation (mat4, column-major; its 3x3 part
+ *             turns every direction).
+ * Probe p traces ray_count rays (inactive probes: inactive_ray_count, along
+ * ray_dirs_inactive) with HitClosest (HitClosestTransparency) and shades
+ * each like rayHit.csh: a miss returns `environment`; a backface hit on a
+ * one-sided material that culls back faces has radiance 0 and a negative
+ * distance; otherwise emission + one light sample with the diffuse BRDF
+ * times opacity, visible through HitAny (mask SHADOW).  The irradiance
+ * volume's indirect term is not added.  Output: PackRayHit (ddgi.hsh:85-98)
+ * at hits[p * ray_count + i] (4 floats: half2 direction.xy, half2
+ * radiance.xy, half2 (direction.z, radiance.z), distance; radiance clamped
+ * to 3200); entries beyond a probe's ray count are left as they were.  All
+ * buffers are device memory. */
+typedef struct ae_ddgi_probes {
+    const float* probes;
+    const float* ray_dirs;
+    const float* ray_dirs_inactive;
+    float rotation[16];
+    uint32_t n_probes;
+    uint32_t ray_count;
+    uint32_t inactive_ray_count;
+    uint32_t reserved;
+} ae_ddgi_probes;
+ae_rt_status ae_rt_ddgi_trace(ae_rt_ctx* ctx, const ae_ddgi_probes* probes, const ae_rt_pass_params* params,
+                              float* hits, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Learned radiance cache (no counterpart in the reference engine)           */

@@ -286,6 +286,8 @@ typedef struct {
     const aeo_instance* inst; uint32_t n_inst;
     const aeo_mesh* meshes; uint32_t n_meshes;
     const float* materials;   /* transparency variants: GPUMaterial (23 words); NULL: opaque queries */
+    uint32_t n_materials;
+    const aeo_texture* textures; uint32_t n_textures;
 } scene_t;
 
 /* Leaf triangle of the transparency variants: UnpackTriangle of the shading
@@ -294,12 +296,90 @@ typedef struct {
  * negative: the material's opacity times its opacity texture, which samples
  * as 1.0 when absent (texture.hsh:18-25); bound textures are not sampled and
  * count as 1.0 as well. */
-static inline float shading_opacity(const scene_t* sc, const float* s, int32_t materialOffset) {
-    if (s[23] >= 0.0f) return s[23];
+float aeo_half_to_float(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16, e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+    uint32_t bits;
+    if (e == 0x1Fu) {
+        bits = sign | 0x7F800000u | (m << 13);
+    } else if (e != 0) {
+        bits = sign | ((e + 112u) << 23) | (m << 13);
+    } else {
+        /* zero or subnormal: m * 2^-24, exact in float */
+        float f = (float)m * 5.9604644775390625e-8f;
+        memcpy(&bits, &f, 4);
+        bits |= sign;
+    }
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+static float texel_r(const aeo_texture* t, uint32_t x, uint32_t y) {
+    const uint32_t texel = t->format == 0 ? 1u : 4u;
+    const uint32_t pitch = t->row_pitch ? t->row_pitch : t->width * texel;
+    const uint8_t* row = (const uint8_t*)t->texels + (size_t)y * pitch;
+    if (t->format == 0) return (float)row[x] / 255.0f;
+    if (t->format == 1) return (float)row[(size_t)x * 4] / 255.0f;
+    float f;
+    memcpy(&f, row + (size_t)x * 4, 4);
+    return f;
+}
+
+static void tex_axis(float s, uint32_t n, uint32_t* i0, uint32_t* i1, float* a) {
+    float x = s * (float)n - 0.5f;
+    if (!(fabsf(x) < 9.0e18f)) x = 0.0f;
+    const float fx = floorf(x);
+    *a = x - fx;
+    long long i = (long long)fx % (long long)n;
+    if (i < 0) i += n;
+    *i0 = (uint32_t)i;
+    *i1 = *i0 + 1u == n ? 0u : *i0 + 1u;
+}
+
+float aeo_sample_r_bilinear(const aeo_texture* textures, uint32_t n_textures, int32_t id, float u, float v) {
+    if (id < 0 || (uint32_t)id >= n_textures) return 1.0f;
+    const aeo_texture* t = &textures[id];
+    uint32_t x0, x1, y0, y1;
+    float a, b;
+    tex_axis(u, t->width, &x0, &x1, &a);
+    tex_axis(v, t->height, &y0, &y1, &b);
+    const float c00 = texel_r(t, x0, y0), c10 = texel_r(t, x1, y0), c01 = texel_r(t, x0, y1), c11 = texel_r(t, x1, y1);
+    const float ia = 1.0f - a, ib = 1.0f - b;
+    float r = (ia * ib) * c00;
+    r = r + (a * ib) * c10;
+    r = r + (ia * b) * c01;
+    return r + (a * b) * c11;
+}
+
+static inline void half2_of(float bits, float* x, float* y) {
+    uint32_t u;
+    memcpy(&u, &bits, 4);
+    *x = aeo_half_to_float((uint16_t)(u & 0xFFFFu));
+    *y = aeo_half_to_float((uint16_t)(u >> 16));
+}
+
+/* `tri.opacity < 0.0 ? GetOpacity(tri, sol.yz, materialOffset, 0) : tri.opacity`
+ * (bvh.hsh:127, :163; GetOpacity surface.hsh:147-159, whose interpolated
+ * vertex alpha is unused). */
+static inline float shading_opacity(const scene_t* sc, const float* s, int32_t materialOffset, float bs, float bt) {
+    if (!(s[23] < 0.0f)) return s[23];
     int32_t idx;
     memcpy(&idx, &s[15], 4);
-    const float* m = sc->materials + (size_t)(idx + materialOffset) * 23;
-    return 1.0f * m[7];
+    idx += materialOffset;
+    if (idx < 0 || (uint32_t)idx >= sc->n_materials) return 1.0f;
+    const float* m = sc->materials + (size_t)idx * 23;
+    const float r = (1.0f - bs) - bt;
+    float u0, v0, u1, v1, u2, v2;
+    half2_of(s[12], &u0, &v0);
+    half2_of(s[13], &u1, &v1);
+    half2_of(s[14], &u2, &v2);
+    const float tu = (r * u0 + bs * u1) + bt * u2;
+    float tv = (r * v0 + bs * v1) + bt * v2;
+    int32_t invert, tex;
+    memcpy(&invert, &m[13], 4);
+    memcpy(&tex, &m[18], 4);
+    if (invert > 0) tv = 1.0f - tv;
+    return aeo_sample_r_bilinear(sc->textures, sc->n_textures, tex, tu, tv) * m[7];
 }
 
 static inline aeo_tri shading_tri(const float* s) {
@@ -368,7 +448,7 @@ static void scene_closest_one(const scene_t* sc, const float* r, uint32_t cull, 
                             end = sh[18] > 0.0f;
                             hit = tri_test(o, d, &t, &st, &su, &sv);
                             if (hit && st > tMin && st < hitDist &&
-                                shading_opacity(sc, sh, sc->inst[curInst].materialOffset) > 0.0f) {
+                                shading_opacity(sc, sh, sc->inst[curInst].materialOffset, su, sv) > 0.0f) {
                                 hitDist = st; hitID = tp; hu = su; hv = sv; hitInst = curInst;
                             }
                         } else {
@@ -521,7 +601,7 @@ static float scene_any_transparency_one(const scene_t* sc, const float* r, uint3
                     end = sh[18] > 0.0f;
                     float st, su, sv;
                     if (tri_test(o, d, &t, &st, &su, &sv) && st > tMin && st < tMax)
-                        leaf = leaf * (1.0f - shading_opacity(sc, sh, matOffset));
+                        leaf = leaf * (1.0f - shading_opacity(sc, sh, matOffset, su, sv));
                     tp++;
                 }
                 transparency = transparency * leaf;
@@ -607,10 +687,11 @@ void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instanc
 
 void aeo_scene_closest_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
                                          uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
-                                         const float* materials, const float* rays, uint32_t n_rays,
-                                         uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out,
-                                         float* tuv) {
-    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials };
+                                         const float* materials, uint32_t n_materials,
+                                         const aeo_texture* textures, uint32_t n_textures, const float* rays,
+                                         uint32_t n_rays, uint32_t cull_mask, int threads, int32_t* tri_ptr,
+                                         int32_t* inst_out, float* tuv) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials, n_materials, textures, n_textures };
     scene_job_t p; memset(&p, 0, sizeof(p));
     p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 0; p.ptr = tri_ptr; p.inst = inst_out; p.tuv = tuv;
     p.stack_cap = scene_stack_cap(&sc);
@@ -619,9 +700,10 @@ void aeo_scene_closest_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, 
 
 void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
                                      uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
-                                     const float* materials, const float* rays, uint32_t n_rays,
-                                     uint32_t cull_mask, int threads, float* transparency) {
-    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials };
+                                     const float* materials, uint32_t n_materials, const aeo_texture* textures,
+                                     uint32_t n_textures, const float* rays, uint32_t n_rays, uint32_t cull_mask,
+                                     int threads, float* transparency) {
+    scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials, n_materials, textures, n_textures };
     scene_job_t p; memset(&p, 0, sizeof(p));
     p.sc = &sc; p.rays = rays; p.cull = cull_mask; p.any = 1; p.transparency = transparency;
     p.stack_cap = scene_stack_cap(&sc);

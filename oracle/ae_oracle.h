@@ -105,22 +105,47 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum);
 
+/* One texture's level 0 (the layout of the library's ae_texture): `height`
+ * rows of `row_pitch` bytes (0 = tight); format 0 = R8 UNORM, 1 = RGBA8
+ * UNORM, 2 = R32 float; the first channel is sampled. */
+typedef struct aeo_texture {
+    const void* texels;
+    uint32_t width, height, format, row_pitch;
+} aeo_texture;
+
+/* textureLod(sampler2D(bindlessTextures[id], bindlessSampler), (u, v), 0).r
+ * (texture.hsh:18-25) with the engine's bindless sampler (linear filter,
+ * repeat addressing, MainRenderer.cpp:922-929), in FP32 with one rounding
+ * per operation: x = u * width - 0.5, i = floor(x), a = x - i, texels i and
+ * i + 1 modulo width (likewise v), ((w00 c00 + w10 c10) + w01 c01) + w11 c11
+ * with w00 = (1-a)(1-b), w10 = a(1-b), w01 = (1-a)b, w11 = ab; UNORM texels
+ * are byte / 255; a non-finite x (or y) becomes 0 (texel 0 alone); a negative or
+ * out-of-range id samples as 1.0. */
+float aeo_sample_r_bilinear(const aeo_texture* textures, uint32_t n_textures, int32_t id, float u, float v);
+
+/* IEEE binary16 bits to float (unpackHalf2x16 of one half). */
+float aeo_half_to_float(uint16_t h);
+
 /* The transparency variants over TLAS + BLASes (meshes need `shading`):
  * HitClosestTransparency (bvh.hsh:275-357: a hit counts only where the
  * triangle's opacity is > 0) and HitAnyTransparency (bvh.hsh:443-524: the
  * returned transparency, 1 = unoccluded).  Opacity: GPUTriangle d2.w, or,
- * when negative, the material's opacity (materials: GPUMaterial, 23 words,
- * indexed by the triangle's material index + the instance's materialOffset);
- * opacity textures are not sampled (factor 1). */
+ * when negative, GetOpacity (surface.hsh:147-159): the material's opacity
+ * (materials: GPUMaterial, 23 words, indexed by the triangle's material
+ * index + the instance's materialOffset; outside [0, n_materials) the
+ * opacity is 1) times its opacity texture sampled at the UV interpolated
+ * from the triangle's half2 UVs, v flipped when invertUVs > 0. */
 void aeo_scene_closest_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
                                          uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
-                                         const float* materials, const float* rays, uint32_t n_rays,
-                                         uint32_t cull_mask, int threads, int32_t* tri_ptr, int32_t* inst_out,
-                                         float* tuv);
+                                         const float* materials, uint32_t n_materials,
+                                         const aeo_texture* textures, uint32_t n_textures, const float* rays,
+                                         uint32_t n_rays, uint32_t cull_mask, int threads, int32_t* tri_ptr,
+                                         int32_t* inst_out, float* tuv);
 void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst,
                                      uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes,
-                                     const float* materials, const float* rays, uint32_t n_rays,
-                                     uint32_t cull_mask, int threads, float* transparency);
+                                     const float* materials, uint32_t n_materials, const aeo_texture* textures,
+                                     uint32_t n_textures, const float* rays, uint32_t n_rays, uint32_t cull_mask,
+                                     int threads, float* transparency);
 
 /* Exact-as-possible nearest hit in double precision by brute force over every
  * triangle (for small cases and for re-testing near ties): the double-precision

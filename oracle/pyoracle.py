@@ -64,10 +64,16 @@ def port():
                                     C.c_float, C.c_int, P]
         L.aeo_pathtrace.restype = None
         L.aeo_scene_any_glsl.restype = None
-        L.aeo_scene_closest_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, P, U32, U32, C.c_int, P, P, P]
+        L.aeo_scene_closest_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32,
+                                                          C.c_int, P, P, P]
         L.aeo_scene_closest_transparency_glsl.restype = None
-        L.aeo_scene_any_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, P, U32, U32, C.c_int, P]
+        L.aeo_scene_any_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32,
+                                                      C.c_int, P]
         L.aeo_scene_any_transparency_glsl.restype = None
+        L.aeo_sample_r_bilinear.argtypes = [P, U32, C.c_int32, C.c_float, C.c_float]
+        L.aeo_sample_r_bilinear.restype = C.c_float
+        L.aeo_half_to_float.argtypes = [C.c_uint16]
+        L.aeo_half_to_float.restype = C.c_float
         for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
             f.restype = None
         _port = L
@@ -193,6 +199,48 @@ def _mesh_table(meshes):
     return table, keep
 
 
+class _Texture(C.Structure):
+    _fields_ = [("texels", P), ("width", U32), ("height", U32), ("format", U32), ("row_pitch", U32)]
+
+
+TEX_FORMATS = {"r8": 0, "rgba8": 1, "r32f": 2}
+
+
+def texture_format(a: np.ndarray) -> int:
+    """AE_TEX_* of a texel array: uint8 (h, w) R8, uint8 (h, w, 4) RGBA8,
+    float32 (h, w) R32F."""
+    if a.dtype == np.uint8 and a.ndim == 2:
+        return 0
+    if a.dtype == np.uint8 and a.ndim == 3 and a.shape[2] == 4:
+        return 1
+    if a.dtype == np.float32 and a.ndim == 2:
+        return 2
+    raise ValueError(f"unsupported texel array {a.dtype} {a.shape}")
+
+
+def _texture_table(textures):
+    """textures: list of texel arrays (see texture_format); keeps them alive."""
+    textures = list(textures or [])
+    keep = [np.ascontiguousarray(t) for t in textures]
+    table = (_Texture * max(1, len(keep)))()
+    for i, t in enumerate(keep):
+        table[i].texels = t.ctypes.data
+        table[i].height, table[i].width = t.shape[0], t.shape[1]
+        table[i].format = texture_format(t)
+        table[i].row_pitch = 0
+    return table, len(keep), keep
+
+
+def sample_r_bilinear(textures, tex_id, u, v):
+    """The traversal's opacity lookup of one texture at (u, v)."""
+    table, n, keep = _texture_table(textures)
+    return port().aeo_sample_r_bilinear(table, n, tex_id, u, v)
+
+
+def half_to_float(h: int) -> float:
+    return port().aeo_half_to_float(h)
+
+
 def scene_closest_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, threads=os.cpu_count(),
                        counters=False):
     """HitClosest over TLAS + instances + BLASes.  instances: structured array
@@ -228,36 +276,40 @@ def scene_any_glsl(tlas_f32, instances, meshes, rays8, cull_mask=0xFFFFFFFF, thr
 
 
 def scene_closest_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, cull_mask=0xFFFFFFFF,
-                                    threads=os.cpu_count()):
+                                    threads=os.cpu_count(), textures=None):
     """HitClosestTransparency (bvh.hsh:275-357); meshes carry shading
-    triangles, materials is the GPUMaterial array."""
+    triangles, materials is the GPUMaterial array, textures the texel arrays
+    that the materials' opacityTexture indexes."""
     n = len(rays8)
     tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
     inst = np.ascontiguousarray(instances)
     mats = np.ascontiguousarray(materials)
     table, keep = _mesh_table(meshes)
+    ttab, ntex, tkeep = _texture_table(textures)
     ptr = np.empty(n, np.int32)
     ino = np.empty(n, np.int32)
     tuv = np.empty((n, 3), np.float32)
     port().aeo_scene_closest_transparency_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
                                                inst.ctypes.data, len(inst), table, len(meshes), mats.ctypes.data,
-                                               rays8.ctypes.data, n, cull_mask, threads, ptr.ctypes.data,
-                                               ino.ctypes.data, tuv.ctypes.data)
+                                               len(mats), ttab, ntex, rays8.ctypes.data, n, cull_mask, threads,
+                                               ptr.ctypes.data, ino.ctypes.data, tuv.ctypes.data)
     return ptr, ino, tuv
 
 
 def scene_any_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, cull_mask=0xFFFFFFFF,
-                                threads=os.cpu_count()):
+                                threads=os.cpu_count(), textures=None):
     """HitAnyTransparency (bvh.hsh:443-524): transparency per ray (1 = clear)."""
     n = len(rays8)
     tlas_f32, rays8 = _c(tlas_f32, np.float32), _c(rays8, np.float32)
     inst = np.ascontiguousarray(instances)
     mats = np.ascontiguousarray(materials)
     table, keep = _mesh_table(meshes)
+    ttab, ntex, tkeep = _texture_table(textures)
     out = np.empty(n, np.float32)
     port().aeo_scene_any_transparency_glsl(tlas_f32.ctypes.data if tlas_f32.size else None, len(tlas_f32),
                                            inst.ctypes.data, len(inst), table, len(meshes), mats.ctypes.data,
-                                           rays8.ctypes.data, n, cull_mask, threads, out.ctypes.data)
+                                           len(mats), ttab, ntex, rays8.ctypes.data, n, cull_mask, threads,
+                                           out.ctypes.data)
     return out
 
 
