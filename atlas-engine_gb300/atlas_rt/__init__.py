@@ -21,7 +21,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._native import AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, PtParams, RcConfig, lib
+from ._native import (AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, DdgiProbes, GBuffer, PassParams,
+                      PtParams, RcConfig, lib)
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
                        ("rightMin", "<f4", 3), ("rightMax", "<f4", 3),
@@ -163,6 +164,7 @@ class _Texture(C.Structure):
 
 
 TEX_R8_UNORM, TEX_RGBA8_UNORM, TEX_R32_FLOAT = 0, 1, 2
+PASS_OPACITY_CHECK = 0x1
 
 
 def _texture_format(a: np.ndarray) -> int:
@@ -437,6 +439,62 @@ class Context:
         p.flags = 1 if mis else 0
         _check(lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
                                      _stream_handle(stream)), self._h)
+
+    # -- the traversal's other consumers (RTAO, reflections, RTGI, DDGI) ------
+
+    @staticmethod
+    def _gbuffer(gb: dict):
+        """ae_gbuffer from a dict of device tensors: depth (h, w), normal
+        (h, w, 2), optional offset (h, w) uint8, roughness (h, w), samples
+        (h, w, 2); ip_matrix / iv_matrix as 4x4 row-major arrays (stored
+        column-major, like GLSL); half_res."""
+        g = GBuffer()
+        depth = gb["depth"]
+        g.height, g.width = int(depth.shape[0]), int(depth.shape[1])
+        g.depth, g.normal = _ptr(depth), _ptr(gb["normal"])
+        g.offset, g.roughness, g.samples = _ptr(gb.get("offset")), _ptr(gb.get("roughness")), _ptr(gb.get("samples"))
+        g.half_res = int(gb.get("half_res", 0))
+        for name in ("ip_matrix", "iv_matrix"):
+            m = np.asarray(gb[name], np.float32).reshape(4, 4)
+            getattr(g, name)[:] = list(m.T.reshape(-1))
+        return g
+
+    @staticmethod
+    def _pass_params(radius=1.0, bias=0.0, roughness_cutoff=1.0, radiance_limit=10.0, environment=(0, 0, 0),
+                     opacity_check=False, frame_seed=0, seed=1):
+        p = PassParams()
+        p.radius, p.bias, p.roughness_cutoff, p.radiance_limit = radius, bias, roughness_cutoff, radiance_limit
+        p.environment[:] = [float(x) for x in environment]
+        p.flags = PASS_OPACITY_CHECK if opacity_check else 0
+        p.frame_seed, p.seed = frame_seed, seed
+        return p
+
+    def rtao(self, gbuffer: dict, out, stream=None, **params):
+        """ae_rt_rtao: ambient occlusion per pixel into `out` (h, w) float32 (device)."""
+        _check(lib().ae_rt_rtao(self._h, C.byref(self._gbuffer(gbuffer)), C.byref(self._pass_params(**params)),
+                                _ptr(out), _stream_handle(stream)), self._h)
+
+    def reflections(self, gbuffer: dict, out, stream=None, **params):
+        """ae_rt_reflections: reflected radiance per pixel into `out` (h, w, 4) float32 (device)."""
+        _check(lib().ae_rt_reflections(self._h, C.byref(self._gbuffer(gbuffer)),
+                                       C.byref(self._pass_params(**params)), _ptr(out), _stream_handle(stream)),
+               self._h)
+
+    def rtgi(self, gbuffer: dict, out, stream=None, **params):
+        """ae_rt_rtgi: one-bounce diffuse radiance per pixel into `out` (h, w, 4) float32 (device)."""
+        _check(lib().ae_rt_rtgi(self._h, C.byref(self._gbuffer(gbuffer)), C.byref(self._pass_params(**params)),
+                                _ptr(out), _stream_handle(stream)), self._h)
+
+    def ddgi_trace(self, probes, ray_dirs, rotation, out, ray_dirs_inactive=None, inactive_ray_count=0,
+                   stream=None, **params):
+        """ae_rt_ddgi_trace: PackRayHit per probe ray into `out` (n_probes * ray_count, 4) float32 (device).
+        probes (n, 4) float32 with the state's bits in w; ray_dirs (ray_count, 4); rotation 4x4 row-major."""
+        d = DdgiProbes()
+        d.probes, d.ray_dirs, d.ray_dirs_inactive = _ptr(probes), _ptr(ray_dirs), _ptr(ray_dirs_inactive)
+        d.rotation[:] = list(np.asarray(rotation, np.float32).reshape(4, 4).T.reshape(-1))
+        d.n_probes, d.ray_count, d.inactive_ray_count = int(probes.shape[0]), int(ray_dirs.shape[0]), inactive_ray_count
+        _check(lib().ae_rt_ddgi_trace(self._h, C.byref(d), C.byref(self._pass_params(**params)), _ptr(out),
+                                      _stream_handle(stream)), self._h)
 
     def synchronize(self, stream=None):
         _check(lib().ae_rt_synchronize(self._h, _stream_handle(stream)), self._h)

@@ -65,6 +65,22 @@ class RcConfig(C.Structure):
                 ("glossy_split", U32), ("reserved", U32)]
 
 
+class GBuffer(C.Structure):
+    _fields_ = [("depth", P), ("normal", P), ("offset", P), ("roughness", P), ("samples", P), ("width", U32),
+                ("height", U32), ("half_res", U32), ("reserved", U32), ("ip_matrix", F32 * 16),
+                ("iv_matrix", F32 * 16)]
+
+
+class PassParams(C.Structure):
+    _fields_ = [("radius", F32), ("bias", F32), ("roughness_cutoff", F32), ("radiance_limit", F32),
+                ("environment", F32 * 3), ("flags", U32), ("frame_seed", U32), ("seed", U32)]
+
+
+class DdgiProbes(C.Structure):
+    _fields_ = [("probes", P), ("ray_dirs", P), ("ray_dirs_inactive", P), ("rotation", F32 * 16),
+                ("n_probes", U32), ("ray_count", U32), ("inactive_ray_count", U32), ("reserved", U32)]
+
+
 # (name, restype, argtypes)
 _SIGNATURES = [
     ("ae_bvh_build_triangles", C.c_int, [P, P, U32, C.c_int, C.POINTER(P)]),
@@ -103,6 +119,10 @@ _SIGNATURES = [
     ("ae_rt_scene_set_textures", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
+    ("ae_rt_rtao", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
+    ("ae_rt_reflections", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
+    ("ae_rt_rtgi", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
+    ("ae_rt_ddgi_trace", C.c_int, [P, C.POINTER(DdgiProbes), C.POINTER(PassParams), P, P]),
     ("ae_rc_create", C.c_int, [P, C.POINTER(RcConfig), C.POINTER(P)]),
     ("ae_rc_destroy", None, [P]),
     ("ae_rc_param_counts", C.c_int, [P, C.POINTER(U32), C.POINTER(C.c_uint64)]),
