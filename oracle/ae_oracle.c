@@ -12,6 +12,7 @@
 #include <string.h>
 
 typedef struct { float x, y, z; } v3;
+typedef struct { float x, y, z, w; } float4_t;
 
 static inline v3 mk(float x, float y, float z) { v3 r = { x, y, z }; return r; }
 static inline v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -1026,6 +1027,84 @@ static pt_mat pt_load_mat(const float* m) {
     return r;
 }
 
+/* GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit,
+ * without textures or normal maps; returns backfaceHit (surface.hsh:99). */
+static int pt_make_surface(const pt_job_t* j, v3 ro, v3 rd, int32_t tp, int32_t ino, const float* tuv,
+                           pt_surf* sf) {
+    pt_tri tri = pt_load_tri(j, ino, tp);
+    float s = tuv[1], t = tuv[2], r = 1.0f - s - t;
+    const float* mw = j->materials + (size_t)tri.material * 23;
+    sf->m = pt_load_mat(mw);
+    sf->P = vadd(ro, vmul(rd, tuv[0]));
+    v3 N = vnorm(vadd(vadd(vmul(tri.n0, r), vmul(tri.n1, s)), vmul(tri.n2, t)));
+    v3 triN = vnorm(vcross(sub(tri.v0, tri.v1), sub(tri.v0, tri.v2)));
+    int flip = vdot(triN, rd) > 0.0f;
+    int32_t cull;
+    memcpy(&cull, &mw[15], 4);
+    int backface = sf->m.twoSided > 0 || cull == 0 ? 0 : flip;
+    if (flip && sf->m.twoSided > 0) triN = vmul(triN, -1.0f);
+    if (vdot(N, triN) < 0.0f && sf->m.twoSided > 0) N = vmul(N, -1.0f);
+    sf->V = vmul(rd, -1.0f);
+    sf->N = vnorm(N);
+    sf->geoN = triN;
+    sf->L = sf->N;
+    return backface;
+}
+
+/* GetLight + SampleLight (raytracer/direct.hsh:12-86): one light by streaming
+ * weighted selection, a uniform point on it, sf->L towards it (UpdateSurface).
+ * 0 when there are no lights. */
+static int pt_sample_light(const pt_job_t* j, pt_surf* sf, uint32_t pix, uint32_t sample, uint32_t bounce,
+                           uint32_t seed, v3* radiance, float* lightPdf, float* solidAngle, float* dist) {
+    if (j->n_lights == 0) return 0;
+    const float* sel = NULL;
+    float selW = 0.0f, total = 0.0f;
+    for (uint32_t li = 0; li < j->n_lights; li++) {
+        const float* L = j->lights + (size_t)li * 16;
+        uint32_t data;
+        memcpy(&data, &L[12], 4);
+        float bright = (L[8] + L[9] + L[10]) * 0.33333f;
+        float w = 1.0f;
+        if ((data >> 28) == 1u) {
+            v3 toL = sub(ld3(L), sf->P);
+            float d2 = vdot(toL, toL);
+            float NdotL = fmaxf(vdot(ld3(L + 4), vmul(vnorm(toL), -1.0f)), 0.0f);
+            w = bright * L[14] * NdotL / d2;
+        } else {
+            w = bright;
+        }
+        w = fminf(fmaxf(w, 0.0000001f), 1.0f);
+        total += w;
+        if (prng(pix, sample, bounce, 16u + li, seed) < w / total) { selW = w; sel = L; }
+    }
+    uint32_t data;
+    memcpy(&data, &sel[12], 4);
+    *lightPdf = selW / total * sel[13];
+    *solidAngle = 1.0f;
+    *dist = 1e12f;
+    *radiance = ld3(sel + 8);
+    if ((data >> 28) == 1u) {
+        float r0 = prng(pix, sample, bounce, 1, seed), r1 = prng(pix, sample, bounce, 2, seed);
+        int32_t linst;
+        memcpy(&linst, &sel[15], 4);
+        pt_tri lt = pt_load_tri(j, linst, (int32_t)(data & 0x0FFFFFFFu));
+        float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
+        v3 LP = vadd(vadd(vmul(lt.v0, lu), vmul(lt.v1, lv)), vmul(lt.v2, lw));
+        v3 LN = vadd(vadd(vmul(lt.n0, lu), vmul(lt.n1, lv)), vmul(lt.n2, lw));
+        v3 toL = sub(LP, sf->P);
+        float d2 = vdot(toL, toL);
+        *dist = sqrtf(d2);
+        sf->L = vmul(toL, 1.0f / *dist);
+        pt_update(sf);
+        float NdotLl = fmaxf(vdot(LN, vmul(sf->L, -1.0f)), 0.0f);
+        *solidAngle = NdotLl / (d2 * (1.0f / sel[14]));
+    } else {
+        sf->L = vnorm(vmul(ld3(sel + 4), -1.0f));
+        pt_update(sf);
+    }
+    return 1;
+}
+
 static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* out) {
     const float* c = j->cam;
     for (uint32_t si = 0; si < j->spp; si++) {
@@ -1043,69 +1122,16 @@ static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* ou
             float tuv[3];
             scene_closest_one(&j->sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
             if (tp < 0) break;   /* no environment light */
-            pt_tri tri = pt_load_tri(j, ino, tp);
-            float s = tuv[1], t = tuv[2], r = 1.0f - s - t;
             pt_surf sf;
-            sf.m = pt_load_mat(j->materials + (size_t)tri.material * 23);
-            sf.P = vadd(ro, vmul(rd, tuv[0]));
-            v3 N = vnorm(vadd(vadd(vmul(tri.n0, r), vmul(tri.n1, s)), vmul(tri.n2, t)));
-            v3 triN = vnorm(vcross(sub(tri.v0, tri.v1), sub(tri.v0, tri.v2)));
-            int flip = vdot(triN, rd) > 0.0f;
-            if (flip && sf.m.twoSided > 0) triN = vmul(triN, -1.0f);
-            if (vdot(N, triN) < 0.0f && sf.m.twoSided > 0) N = vmul(N, -1.0f);
-            sf.V = vmul(rd, -1.0f);
-            sf.N = vnorm(N);
-            sf.geoN = triN;
-            sf.L = sf.N;
+            pt_make_surface(j, ro, rd, tp, ino, tuv, &sf);
             if (bounce == 0 && sf.m.emissive.x + sf.m.emissive.y + sf.m.emissive.z > 0.0f) {
                 out[0] += sf.m.emissive.x; out[1] += sf.m.emissive.y; out[2] += sf.m.emissive.z;
             }
-            if (j->n_lights > 0) {
-                const float* sel = NULL;
-                float selW = 0.0f, total = 0.0f;
-                for (uint32_t li = 0; li < j->n_lights; li++) {
-                    const float* L = j->lights + (size_t)li * 16;
-                    uint32_t data;
-                    memcpy(&data, &L[12], 4);
-                    float bright = (L[8] + L[9] + L[10]) * 0.33333f;
-                    float w = 1.0f;
-                    if ((data >> 28) == 1u) {
-                        v3 toL = sub(ld3(L), sf.P);
-                        float d2 = vdot(toL, toL);
-                        float NdotL = fmaxf(vdot(ld3(L + 4), vmul(vnorm(toL), -1.0f)), 0.0f);
-                        w = bright * L[14] * NdotL / d2;
-                    } else {
-                        w = bright;
-                    }
-                    w = fminf(fmaxf(w, 0.0000001f), 1.0f);
-                    total += w;
-                    if (prng(pix, sample, bounce, 16u + li, j->seed) < w / total) { selW = w; sel = L; }
-                }
-                uint32_t data;
-                memcpy(&data, &sel[12], 4);
-                float lightPdf = selW / total * sel[13];
-                float solidAngle = 1.0f, dist = 1e12f;
-                if ((data >> 28) == 1u) {
-                    float r0 = prng(pix, sample, bounce, 1, j->seed), r1 = prng(pix, sample, bounce, 2, j->seed);
-                    int32_t linst;
-                    memcpy(&linst, &sel[15], 4);
-                    pt_tri lt = pt_load_tri(j, linst, (int32_t)(data & 0x0FFFFFFFu));
-                    float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
-                    v3 LP = vadd(vadd(vmul(lt.v0, lu), vmul(lt.v1, lv)), vmul(lt.v2, lw));
-                    v3 LN = vadd(vadd(vmul(lt.n0, lu), vmul(lt.n1, lv)), vmul(lt.n2, lw));
-                    v3 toL = sub(LP, sf.P);
-                    float d2 = vdot(toL, toL);
-                    dist = sqrtf(d2);
-                    sf.L = vmul(toL, 1.0f / dist);
-                    pt_update(&sf);
-                    float NdotLl = fmaxf(vdot(LN, vmul(sf.L, -1.0f)), 0.0f);
-                    solidAngle = NdotLl / (d2 * (1.0f / sel[14]));
-                } else {
-                    sf.L = vnorm(vmul(ld3(sel + 4), -1.0f));
-                    pt_update(&sf);
-                }
+            v3 lrad;
+            float lightPdf, solidAngle, dist;
+            if (pt_sample_light(j, &sf, pix, sample, bounce, j->seed, &lrad, &lightPdf, &solidAngle, &dist)) {
                 v3 refl = vmul(vadd(pt_eval_diffuse(&sf), pt_eval_specular(&sf)), sf.m.opacity);
-                v3 contrib = vmul(vmulv(vmul(thr, sf.m.opacity), vmulv(refl, ld3(sel + 8))),
+                v3 contrib = vmul(vmulv(vmul(thr, sf.m.opacity), vmulv(refl, lrad)),
                                   solidAngle * sf.NdotL / lightPdf);
                 if (sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f) {
                     v3 so = vadd(sf.P, vmul(sf.N, j->epsilon));
@@ -1197,4 +1223,319 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
         started++;
     }
     for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+/* ---------------------------------------------------------------------- */
+/* The traversal's other consumers: RTAO, reflections, RTGI, DDGI probe     */
+/* rays (statistical / tolerance oracle of the library's passes)            */
+/* ---------------------------------------------------------------------- */
+
+#define PASS_EPS 0.1f          /* EPSILON, raytracer/common.hsh:9 */
+#define PASS_INF 1e12f         /* INF, raytracer/common.hsh:8 */
+#define PASS_SAMPLE_SLOT 13u
+#define PASS_LIGHT_SLOT 14u
+
+enum { PASS_AO = 0, PASS_REFL = 1, PASS_GI = 2, PASS_DDGI = 3 };
+
+typedef struct {
+    pt_job_t j;               /* scene (opaque), instance transforms, materials, lights */
+    scene_t tsc;              /* the same scene for the transparency variants */
+    const aeo_gbuffer* gb;
+    const aeo_ddgi_probes* dp;
+    const aeo_pass_params* pp;
+    int kind;
+    float* out;
+    uint32_t begin, end;
+} pass_job_t;
+
+static float4_t mat4_col(const float* m, float x, float y, float z, float w) {
+    float4_t r;
+    r.x = ((m[0] * x + m[4] * y) + m[8] * z) + m[12] * w;
+    r.y = ((m[1] * x + m[5] * y) + m[9] * z) + m[13] * w;
+    r.z = ((m[2] * x + m[6] * y) + m[10] * z) + m[14] * w;
+    r.w = ((m[3] * x + m[7] * y) + m[11] * z) + m[15] * w;
+    return r;
+}
+
+/* DecodeNormal, common/normalencode.hsh:18-30 */
+static v3 decode_oct(float cx, float cy) {
+    float y = 1.0f - (fabsf(cx) + fabsf(cy));
+    if (y < 0.0f) {
+        float ox = cx, oy = cy;
+        cx = (ox >= 0.0f ? 1.0f : -1.0f) * (1.0f - fabsf(oy));
+        cy = (oy >= 0.0f ? 1.0f : -1.0f) * (1.0f - fabsf(ox));
+    }
+    return vnorm(mk(cx, y, cy));
+}
+
+static void frame_of(v3 N, v3* t, v3* b, int normalize_b) {
+    v3 up = fabsf(N.z) < 0.999f ? mk(0, 0, 1) : mk(1, 0, 0);
+    *t = vnorm(vcross(up, N));
+    *b = normalize_b ? vnorm(vcross(N, *t)) : vcross(N, *t);
+}
+
+/* ImportanceSampleCosDir, brdf/importanceSample.hsh:82-101 */
+static v3 cos_dir(v3 N, float u0, float u1) {
+    float th = sqrtf(u0), phi = 6.28318530717958647692f * u1;
+    v3 t, b;
+    frame_of(N, &t, &b, 0);
+    return vnorm(vadd(vadd(vmul(t, th * cosf(phi)), vmul(b, th * sinf(phi))), vmul(N, sqrtf(1.0f - u0))));
+}
+
+/* ImportanceSampleGGXVNDF, brdf/importanceSample.hsh:37-80 (alpha = roughness^2) */
+static v3 vndf_dir(v3 N, v3 V, float alpha, float u0, float u1) {
+    v3 t, b;
+    frame_of(N, &t, &b, 1);
+    v3 Vl = vnorm(mk(vdot(V, t) * alpha, vdot(V, b) * alpha, vdot(V, N)));
+    float phi = 6.28318530717958647692f * u0;
+    float z = (1.0f - u1) * (1.0f + Vl.z) + -Vl.z;
+    float s = sqrtf(fminf(fmaxf(1.0f - z * z, 0.0f), 1.0f));
+    v3 Hh = mk(cosf(phi) * s + Vl.x, sinf(phi) * s + Vl.y, z + Vl.z);
+    v3 H = vnorm(vadd(vadd(vmul(t, Hh.x * alpha), vmul(b, Hh.y * alpha)), vmul(N, fmaxf(Hh.z, 0.0f))));
+    return vnorm(sub(vmul(H, 2.0f * vdot(V, H)), V));
+}
+
+/* EvaluateHit of rtreflection.csh / rtgi.csh (diffuse + specular, visibility
+ * by HitAnyTransparency) and ddgi/rayHit.csh (diffuse, HitAny; backface hits
+ * give radiance 0 and a negative distance).  rgb + distance into out4. */
+static void pass_eval_hit(const pass_job_t* p, v3 ro, v3 rd, uint32_t key, int32_t* stack, float* out4) {
+    const aeo_pass_params* pp = p->pp;
+    int opacity = (pp->flags & 1u) != 0;
+    float r8[8] = { ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, 0.0f, PASS_INF };
+    int32_t tp, ino;
+    float tuv[3];
+    scene_closest_one(opacity ? &p->tsc : &p->j.sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
+    v3 rad = mk(pp->environment[0], pp->environment[1], pp->environment[2]);
+    float dist = tp >= 0 ? tuv[0] : PASS_INF;
+    if (tp >= 0) {
+        pt_surf sf;
+        int backface = pt_make_surface(&p->j, ro, rd, tp, ino, tuv, &sf);
+        if (p->kind == PASS_DDGI && backface) {
+            rad = mk(0, 0, 0);
+            dist = -dist;
+        } else {
+            rad = sf.m.emissive;
+            v3 lrad;
+            float lightPdf, solidAngle, ldist;
+            if (pt_sample_light(&p->j, &sf, key, pp->frame_seed, PASS_LIGHT_SLOT, pp->seed, &lrad, &lightPdf,
+                                &solidAngle, &ldist)) {
+                v3 refl = p->kind == PASS_DDGI ? pt_eval_diffuse(&sf)
+                                               : vadd(pt_eval_diffuse(&sf), pt_eval_specular(&sf));
+                refl = vmul(refl, sf.m.opacity);
+                v3 c = vmul(vmulv(refl, vmul(lrad, solidAngle)), sf.NdotL / lightPdf);
+                if (sf.NdotL > 0.0f && c.x + c.y + c.z > 0.0f) {
+                    v3 so = vadd(sf.P, vmul(sf.N, PASS_EPS));
+                    float s8[8] = { so.x, so.y, so.z, sf.L.x, sf.L.y, sf.L.z, 0.0f, ldist - 2.0f * PASS_EPS };
+                    float vis;
+                    if (p->kind == PASS_DDGI) vis = scene_any_one(&p->j.sc, s8, 64u, stack) ? 0.0f : 1.0f;
+                    else vis = scene_any_transparency_one(&p->tsc, s8, 64u, stack);
+                    rad = vadd(rad, vmul(c, vis));
+                }
+            }
+        }
+    }
+    out4[0] = rad.x; out4[1] = rad.y; out4[2] = rad.z; out4[3] = dist;
+}
+
+static uint16_t half_of(float f) {   /* binary16, round to nearest even */
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7FFFFFFFu, r, rem, halfway;
+    if (ax >= 0x7F800000u) return (uint16_t)(sign | 0x7C00u | (ax > 0x7F800000u ? 0x200u : 0u));
+    if (ax >= 0x477FF000u) return (uint16_t)(sign | 0x7C00u);
+    if (ax < 0x38800000u) {
+        if (ax < 0x33000000u) return (uint16_t)sign;
+        uint32_t e = ax >> 23, m = (ax & 0x7FFFFFu) | 0x800000u, shift = 126u - e;
+        r = m >> shift; rem = m & ((1u << shift) - 1u); halfway = 1u << (shift - 1u);
+    } else {
+        r = (ax - 0x38000000u) >> 13; rem = ax & 0x1FFFu; halfway = 0x1000u;
+    }
+    if (rem > halfway || (rem == halfway && (r & 1u))) r++;
+    return (uint16_t)(sign | r);
+}
+
+static void pass_pixel(const pass_job_t* p, uint32_t pix, int32_t* stack) {
+    const aeo_gbuffer* g = p->gb;
+    const aeo_pass_params* pp = p->pp;
+    uint32_t px = pix % g->width, py = pix / g->width;
+    float depth = g->depth[pix];
+    int traced = depth < 1.0f;
+    float rough = 1.0f;
+    if (p->kind == PASS_REFL) {
+        rough = g->roughness[pix];
+        traced = traced && rough <= 1.0f;
+    }
+    int emit = 0;
+    v3 O = mk(0, 0, 0), L = mk(0, 0, 0);
+    if (traced) {
+        float tx, ty;
+        if (g->half_res) {
+            uint32_t off = g->offset ? (g->offset[pix] & 3u) : 0u;
+            tx = (2.0f * (float)px + (float)(off & 1u) + 0.5f) / (2.0f * (float)g->width);
+            ty = (2.0f * (float)py + (float)(off >> 1) + 0.5f) / (2.0f * (float)g->height);
+        } else {
+            tx = ((float)px + 0.5f) / (float)g->width;
+            ty = ((float)py + 0.5f) / (float)g->height;
+        }
+        float4_t vs = mat4_col(g->ip_matrix, tx * 2.0f - 1.0f, ty * 2.0f - 1.0f, depth, 1.0f);
+        v3 viewPos = mk(vs.x / vs.w, vs.y / vs.w, vs.z / vs.w);
+        float4_t wp = mat4_col(g->iv_matrix, viewPos.x, viewPos.y, viewPos.z, 1.0f);
+        float4_t vv = mat4_col(g->iv_matrix, viewPos.x, viewPos.y, viewPos.z, 0.0f);
+        v3 vn = decode_oct(g->normal[(size_t)pix * 2], g->normal[(size_t)pix * 2 + 1]);
+        float4_t wn = mat4_col(g->iv_matrix, vn.x, vn.y, vn.z, 0.0f);
+        v3 P = mk(wp.x, wp.y, wp.z), N = vnorm(mk(wn.x, wn.y, wn.z));
+        float u0, u1;
+        if (g->samples) {
+            u0 = g->samples[(size_t)pix * 2];
+            u1 = g->samples[(size_t)pix * 2 + 1];
+        } else {
+            u0 = prng(pix, pp->frame_seed, PASS_SAMPLE_SLOT, 0, pp->seed);
+            u1 = prng(pix, pp->frame_seed, PASS_SAMPLE_SLOT, 1, pp->seed);
+        }
+        float viewLen = sqrtf(vdot(viewPos, viewPos));
+        if (p->kind == PASS_AO) {
+            L = vnorm(cos_dir(N, u0, u1));
+            O = vadd(vadd(P, vmul(L, PASS_EPS)), vmul(N, PASS_EPS));
+            emit = 1;
+        } else {
+            if (p->kind == PASS_REFL) {
+                u1 *= (1.0f - pp->bias);
+                v3 V = vnorm(mk(-vv.x, -vv.y, -vv.z));
+                if (rough > 0.01f) {
+                    L = vndf_dir(N, V, rough * rough, u0, u1);
+                } else {
+                    v3 I = vmul(V, -1.0f);
+                    L = vnorm(sub(I, vmul(N, 2.0f * vdot(N, I))));
+                }
+            } else {
+                u0 *= (1.0f - pp->bias);
+                L = cos_dir(N, u0, u1);
+            }
+            int valid = !(isnan(L.x) && isnan(L.y) && isnan(L.z));
+            if (p->kind == PASS_REFL) {
+                float viewOffset = fmaxf(1.0f, viewLen) * 0.1f;
+                O = vadd(vadd(P, vmul(L, PASS_EPS * 0.1f * viewOffset)), vmul(N, PASS_EPS * viewOffset * 0.1f));
+                emit = valid && rough <= pp->roughness_cutoff;
+            } else {
+                float viewOffset = fmaxf(1.0f, viewLen);
+                O = vadd(vadd(P, vmul(L, PASS_EPS * viewOffset * 0.01f)), vmul(N, PASS_EPS * 0.01f * viewOffset));
+                emit = valid;
+            }
+        }
+    }
+    if (p->kind == PASS_AO) {
+        float ao = 1.0f;
+        if (emit) {
+            float r8[8] = { O.x, O.y, O.z, L.x, L.y, L.z, 0.0f, pp->radius };
+            float hit = (pp->flags & 1u) ? 1.0f - scene_any_transparency_one(&p->tsc, r8, 128u, stack)
+                                         : (scene_any_one(&p->j.sc, r8, 128u, stack) ? 1.0f : 0.0f);
+            ao = 1.0f - hit;
+        }
+        p->out[pix] = ao;
+        return;
+    }
+    float* o4 = p->out + (size_t)pix * 4;
+    o4[0] = o4[1] = o4[2] = 0.0f;
+    o4[3] = 1.0f;
+    if (!emit) return;
+    float r4[4];
+    pass_eval_hit(p, O, L, pix, stack, r4);
+    float m = fmaxf(fmaxf(fmaxf(r4[0], fmaxf(r4[1], r4[2])), pp->radiance_limit), 0.01f);
+    float s = pp->radiance_limit / m;
+    o4[0] = r4[0] * s; o4[1] = r4[1] * s; o4[2] = r4[2] * s;
+}
+
+static void pass_probe_ray(const pass_job_t* p, uint32_t idx, int32_t* stack) {
+    const aeo_ddgi_probes* d = p->dp;
+    uint32_t probe = idx / d->ray_count, i = idx % d->ray_count;
+    const float* pr = d->probes + (size_t)probe * 4;
+    uint32_t state;
+    memcpy(&state, &pr[3], 4);
+    int inactive = state == 2u;
+    uint32_t inactive_count = d->inactive_ray_count < d->ray_count ? d->inactive_ray_count : d->ray_count;
+    if (i >= (inactive ? inactive_count : d->ray_count)) return;
+    const float* v = (inactive ? d->ray_dirs_inactive : d->ray_dirs) + (size_t)i * 4;
+    const float* m = d->rotation;
+    v3 D = vnorm(mk(m[0] * v[0] + m[4] * v[1] + m[8] * v[2], m[1] * v[0] + m[5] * v[1] + m[9] * v[2],
+                    m[2] * v[0] + m[6] * v[1] + m[10] * v[2]));
+    float r4[4];
+    pass_eval_hit(p, mk(pr[0], pr[1], pr[2]), D, idx, stack, r4);
+    float rx = fminf(r4[0], 3200.0f), ry = fminf(r4[1], 3200.0f), rz = fminf(r4[2], 3200.0f);
+    uint32_t w0 = (uint32_t)half_of(D.x) | ((uint32_t)half_of(D.y) << 16);
+    uint32_t w1 = (uint32_t)half_of(rx) | ((uint32_t)half_of(ry) << 16);
+    uint32_t w2 = (uint32_t)half_of(D.z) | ((uint32_t)half_of(rz) << 16);
+    float* o = p->out + (size_t)idx * 4;
+    memcpy(&o[0], &w0, 4);
+    memcpy(&o[1], &w1, 4);
+    memcpy(&o[2], &w2, 4);
+    o[3] = r4[3];
+}
+
+static void* run_pass_job(void* arg) {
+    pass_job_t* p = (pass_job_t*)arg;
+    int32_t* stack = (int32_t*)malloc(p->j.stack_cap * sizeof(int32_t));
+    for (uint32_t k = p->begin; k < p->end; k++) {
+        if (p->kind == PASS_DDGI) pass_probe_ray(p, k, stack);
+        else pass_pixel(p, k, stack);
+    }
+    free(stack);
+    return NULL;
+}
+
+static void run_pass(const aeo_pass_scene* s, int kind, const aeo_gbuffer* gb, const aeo_ddgi_probes* dp,
+                     const aeo_pass_params* pp, uint32_t n, int threads, float* out) {
+    pass_job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    scene_t sc = { s->tlas, s->n_tlas, s->inst, s->n_inst, s->meshes, s->n_meshes, NULL, 0, NULL, 0 };
+    scene_t tsc = { s->tlas, s->n_tlas, s->inst, s->n_inst, s->meshes, s->n_meshes, s->materials, s->n_materials,
+                    s->textures, s->n_textures };
+    proto.j.sc = sc;
+    proto.j.inst_model = s->inst_model;
+    proto.j.materials = s->materials;
+    proto.j.lights = s->lights;
+    proto.j.n_lights = s->n_lights;
+    proto.j.epsilon = PASS_EPS;
+    proto.j.stack_cap = scene_stack_cap(&sc);
+    proto.tsc = tsc;
+    proto.gb = gb;
+    proto.dp = dp;
+    proto.pp = pp;
+    proto.kind = kind;
+    proto.out = out;
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    pass_job_t jobs[256];
+    uint32_t chunk = (n + (uint32_t)threads - 1) / (uint32_t)threads;
+    int started = 0;
+    for (int t = 0; t < threads; t++) {
+        uint32_t b = (uint32_t)t * chunk;
+        if (b >= n) break;
+        jobs[t] = proto;
+        jobs[t].begin = b;
+        jobs[t].end = b + chunk < n ? b + chunk : n;
+        pthread_create(&th[t], NULL, run_pass_job, &jobs[t]);
+        started++;
+    }
+    for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+void aeo_pass_rtao(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                   float* ao) {
+    run_pass(s, PASS_AO, gb, NULL, pp, gb->width * gb->height, threads, ao);
+}
+
+void aeo_pass_reflections(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                          float* rgba) {
+    run_pass(s, PASS_REFL, gb, NULL, pp, gb->width * gb->height, threads, rgba);
+}
+
+void aeo_pass_rtgi(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                   float* rgba) {
+    run_pass(s, PASS_GI, gb, NULL, pp, gb->width * gb->height, threads, rgba);
+}
+
+void aeo_pass_ddgi(const aeo_pass_scene* s, const aeo_ddgi_probes* dp, const aeo_pass_params* pp, int threads,
+                   float* hits) {
+    run_pass(s, PASS_DDGI, NULL, dp, pp, dp->n_probes * dp->ray_count, threads, hits);
 }

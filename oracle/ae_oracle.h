@@ -147,6 +147,57 @@ void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, cons
                                      uint32_t n_textures, const float* rays, uint32_t n_rays, uint32_t cull_mask,
                                      int threads, float* transparency);
 
+/* The traversal's other consumers -- ao/rtao.csh, reflection/rtreflection.csh,
+ * rtgi/rtgi.csh, ddgi/rayGen.csh + rayHit.csh -- restated per pixel / probe
+ * ray with the library's random streams (pixel samples: PCG hash slot 13 of
+ * (pixel, frame_seed) unless `samples` is given; light choices: slot 14 keyed
+ * by the pixel or probe-ray index).  Structs mirror the library's
+ * ae_gbuffer, ae_rt_pass_params and ae_ddgi_probes (host memory here). */
+typedef struct aeo_gbuffer {
+    const float* depth;
+    const float* normal;
+    const uint8_t* offset;
+    const float* roughness;
+    const float* samples;
+    uint32_t width, height, half_res, reserved;
+    float ip_matrix[16], iv_matrix[16];
+} aeo_gbuffer;
+
+typedef struct aeo_pass_params {
+    float radius, bias, roughness_cutoff, radiance_limit;
+    float environment[3];
+    uint32_t flags;        /* 1: opacity check (transparency traversals) */
+    uint32_t frame_seed, seed;
+} aeo_pass_params;
+
+typedef struct aeo_ddgi_probes {
+    const float* probes;
+    const float* ray_dirs;
+    const float* ray_dirs_inactive;
+    float rotation[16];
+    uint32_t n_probes, ray_count, inactive_ray_count, reserved;
+} aeo_ddgi_probes;
+
+/* The scene of the passes: TLAS, instances (+ object-to-world 3x4 rows),
+ * meshes with shading triangles, materials, opacity textures, lights. */
+typedef struct aeo_pass_scene {
+    const aeo_node* tlas; uint32_t n_tlas;
+    const aeo_instance* inst; const float* inst_model; uint32_t n_inst;
+    const aeo_mesh* meshes; uint32_t n_meshes;
+    const float* materials; uint32_t n_materials;
+    const aeo_texture* textures; uint32_t n_textures;
+    const float* lights; uint32_t n_lights;
+} aeo_pass_scene;
+
+void aeo_pass_rtao(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                   float* ao);
+void aeo_pass_reflections(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                          float* rgba);
+void aeo_pass_rtgi(const aeo_pass_scene* s, const aeo_gbuffer* gb, const aeo_pass_params* pp, int threads,
+                   float* rgba);
+void aeo_pass_ddgi(const aeo_pass_scene* s, const aeo_ddgi_probes* dp, const aeo_pass_params* pp, int threads,
+                   float* hits);
+
 /* Exact-as-possible nearest hit in double precision by brute force over every
  * triangle (for small cases and for re-testing near ties): the double-precision
  * form of the same triangle test, accepting tmin < t < tmax.  t2 = second

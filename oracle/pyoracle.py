@@ -403,3 +403,113 @@ def ref_build_aabbs(boxes, parallel=True):
         L.aeref_get_refs(h, order.ctypes.data)
     L.aeref_free(h)
     return nodes, order
+
+
+# ---------------------------------------------------------------------------
+# The traversal's other consumers (RTAO, reflections, RTGI, DDGI probe rays)
+# ---------------------------------------------------------------------------
+
+class _GBuffer(C.Structure):
+    _fields_ = [("depth", P), ("normal", P), ("offset", P), ("roughness", P), ("samples", P), ("width", U32),
+                ("height", U32), ("half_res", U32), ("reserved", U32), ("ip_matrix", C.c_float * 16),
+                ("iv_matrix", C.c_float * 16)]
+
+
+class _PassParams(C.Structure):
+    _fields_ = [("radius", C.c_float), ("bias", C.c_float), ("roughness_cutoff", C.c_float),
+                ("radiance_limit", C.c_float), ("environment", C.c_float * 3), ("flags", U32),
+                ("frame_seed", U32), ("seed", U32)]
+
+
+class _DdgiProbes(C.Structure):
+    _fields_ = [("probes", P), ("ray_dirs", P), ("ray_dirs_inactive", P), ("rotation", C.c_float * 16),
+                ("n_probes", U32), ("ray_count", U32), ("inactive_ray_count", U32), ("reserved", U32)]
+
+
+class _PassScene(C.Structure):
+    _fields_ = [("tlas", P), ("n_tlas", U32), ("inst", P), ("inst_model", P), ("n_inst", U32), ("meshes", P),
+                ("n_meshes", U32), ("materials", P), ("n_materials", U32), ("textures", P), ("n_textures", U32),
+                ("lights", P), ("n_lights", U32)]
+
+
+def _pass_fns():
+    L = port()
+    if not getattr(L, "_pass_ready", False):
+        for name in ("aeo_pass_rtao", "aeo_pass_reflections", "aeo_pass_rtgi"):
+            getattr(L, name).argtypes = [C.POINTER(_PassScene), C.POINTER(_GBuffer), C.POINTER(_PassParams),
+                                         C.c_int, P]
+            getattr(L, name).restype = None
+        L.aeo_pass_ddgi.argtypes = [C.POINTER(_PassScene), C.POINTER(_DdgiProbes), C.POINTER(_PassParams),
+                                    C.c_int, P]
+        L.aeo_pass_ddgi.restype = None
+        L._pass_ready = True
+    return L
+
+
+def _pass_scene(tlas_f32, instances, inst_model, meshes, materials, lights, textures):
+    tlas_f32 = _c(tlas_f32, np.float32)
+    inst = np.ascontiguousarray(instances)
+    model = _c(inst_model, np.float32)
+    mats = np.ascontiguousarray(materials)
+    lights = _c(lights, np.float32).reshape(-1, 16)
+    table, keep = _mesh_table(meshes)
+    ttab, ntex, tkeep = _texture_table(textures)
+    s = _PassScene(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst), C.cast(table, P),
+                   len(meshes), mats.ctypes.data, len(mats), C.cast(ttab, P), ntex,
+                   lights.ctypes.data if len(lights) else None, len(lights))
+    return s, [tlas_f32, inst, model, mats, lights, table, keep, ttab, tkeep]
+
+
+def _pass_params(radius=1.0, bias=0.0, roughness_cutoff=1.0, radiance_limit=10.0, environment=(0, 0, 0),
+                 opacity_check=False, frame_seed=0, seed=1):
+    return _PassParams(radius, bias, roughness_cutoff, radiance_limit, (C.c_float * 3)(*environment),
+                       1 if opacity_check else 0, frame_seed, seed)
+
+
+def _gbuffer(gb):
+    """gb: dict of numpy arrays like atlas_rt.Context._gbuffer takes."""
+    depth = _c(gb["depth"], np.float32)
+    normal = _c(gb["normal"], np.float32)
+    keep = [depth, normal]
+    g = _GBuffer()
+    g.height, g.width = depth.shape[0], depth.shape[1]
+    g.depth, g.normal = depth.ctypes.data, normal.ctypes.data
+    for name, dt in (("offset", np.uint8), ("roughness", np.float32), ("samples", np.float32)):
+        if gb.get(name) is not None:
+            a = np.ascontiguousarray(gb[name], dt)
+            keep.append(a)
+            setattr(g, name, a.ctypes.data)
+    g.half_res = int(gb.get("half_res", 0))
+    for name in ("ip_matrix", "iv_matrix"):
+        getattr(g, name)[:] = list(np.asarray(gb[name], np.float32).reshape(4, 4).T.reshape(-1))
+    return g, keep
+
+
+def pass_screen(kind, scene, gbuffer, threads=os.cpu_count(), **params):
+    """kind: "rtao" -> (h, w) float32; "reflections" / "rtgi" -> (h, w, 4).
+    scene: (tlas_f32, instances, inst_model, meshes, materials, lights[, textures])."""
+    s, skeep = _pass_scene(*scene[:6], scene[6] if len(scene) > 6 else None)
+    g, gkeep = _gbuffer(gbuffer)
+    pp = _pass_params(**params)
+    h, w = gbuffer["depth"].shape
+    out = np.zeros((h, w) if kind == "rtao" else (h, w, 4), np.float32)
+    getattr(_pass_fns(), f"aeo_pass_{kind}")(C.byref(s), C.byref(g), C.byref(pp), threads, out.ctypes.data)
+    return out
+
+
+def pass_ddgi(scene, probes, ray_dirs, rotation, out, ray_dirs_inactive=None, inactive_ray_count=0,
+              threads=os.cpu_count(), **params):
+    """DDGI probe rays into `out` ((n_probes * ray_count, 4) float32, entries
+    beyond a probe's ray count untouched)."""
+    s, skeep = _pass_scene(*scene[:6], scene[6] if len(scene) > 6 else None)
+    probes = _c(probes, np.float32)
+    dirs = _c(ray_dirs, np.float32)
+    dirs_in = None if ray_dirs_inactive is None else _c(ray_dirs_inactive, np.float32)
+    d = _DdgiProbes()
+    d.probes, d.ray_dirs = probes.ctypes.data, dirs.ctypes.data
+    d.ray_dirs_inactive = None if dirs_in is None else dirs_in.ctypes.data
+    d.rotation[:] = list(np.asarray(rotation, np.float32).reshape(4, 4).T.reshape(-1))
+    d.n_probes, d.ray_count, d.inactive_ray_count = len(probes), len(dirs), inactive_ray_count
+    assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == len(probes) * len(dirs) * 4
+    _pass_fns().aeo_pass_ddgi(C.byref(s), C.byref(d), C.byref(_pass_params(**params)), threads, out.ctypes.data)
+    return out

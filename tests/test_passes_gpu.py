@@ -1,0 +1,184 @@
+"""The library's RTAO, reflection, GI and DDGI passes on the GPU: the
+oracle's known answers on the sandwich scene (exact), and agreement with the
+oracle on the terrain-and-boxes scene with lights.  Both sides draw the same
+random numbers; their sin/cos/sqrt and the device's fused multiply-adds
+differ in the last bits, so a ray that grazes an edge can land differently
+and the comparison allows a small fraction of differing pixels."""
+import numpy as np
+import pytest
+
+import atlas_rt
+import pyoracle
+
+from passes_util import fibonacci_dirs, gbuffer, small_scene, to_device, unpack_ray_hits, upload
+from test_passes_oracle import EMIT, floor_gbuffer, sandwich
+
+pytestmark = pytest.mark.gpu
+
+
+def upload_sandwich(ctx, s):
+    mid = ctx.upload_mesh(s["bvh"].nodes, s["gt"], s["shading"])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), mid, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    ctx.scene_build(inst, s["boxes"])
+    ctx.set_materials(s["materials"])
+    ctx.set_lights(np.zeros((0, 16), np.float32))
+
+
+def run(ctx, kind, gb, **params):
+    import torch
+    h, w = gb["depth"].shape
+    out = torch.full((h, w) if kind == "rtao" else (h, w, 4), -5.0, dtype=torch.float32, device="cuda")
+    getattr(ctx, kind)(to_device(gb), out, **params)
+    ctx.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def sand_ctx():
+    ctx = atlas_rt.Context(device=0)
+    s = sandwich()
+    upload_sandwich(ctx, s)
+    yield ctx, s
+    ctx.close()
+
+
+@pytest.mark.parametrize("half_res", [False, True])
+@pytest.mark.parametrize("opacity", [False, True])
+def test_rtao_known_answers(sand_ctx, half_res, opacity):
+    ctx, s = sand_ctx
+    gb = floor_gbuffer(s, half_res=half_res)
+    assert np.all(run(ctx, "rtao", gb, radius=0.5, opacity_check=opacity) == 1.0)
+    assert np.all(run(ctx, "rtao", gb, radius=1e5, opacity_check=opacity) == 0.0)
+    far = dict(gb, depth=np.ones_like(gb["depth"]))
+    assert np.all(run(ctx, "rtao", far, radius=1e5, opacity_check=opacity) == 1.0)
+
+
+@pytest.mark.parametrize("kind", ["reflections", "rtgi"])
+def test_reflection_and_gi_known_answers(sand_ctx, kind):
+    ctx, s = sand_ctx
+    h, w = 16, 24
+    rough = np.where(np.arange(h * w) % 3 == 0, 0.0, 0.008).reshape(h, w)
+    gb = floor_gbuffer(s, roughness=rough, samples=True)
+    out = run(ctx, kind, gb, radiance_limit=10.0, roughness_cutoff=0.9)
+    np.testing.assert_array_equal(out[..., :3], np.broadcast_to(EMIT, (h, w, 3)))
+    assert np.all(out[..., 3] == 1.0)
+    out = run(ctx, kind, gb, radiance_limit=2.5, roughness_cutoff=0.9)
+    np.testing.assert_allclose(out[..., :3], np.broadcast_to(EMIT * np.float32(2.5 / 4.0), (h, w, 3)), rtol=1e-6)
+
+
+def test_ddgi_known_answers():
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    try:
+        s = sandwich(ceiling_two_sided=False)
+        upload_sandwich(ctx, s)
+        dirs, dirs_in = fibonacci_dirs(32), fibonacci_dirs(8)
+        probes = np.array([[0.0, 0.4, 0.0, 0.0], [3.0, 0.7, 1.0, 0.0], [0.0, 0.5, 0.0, 0.0], [0.0, 5.0, 0.0, 0.0]],
+                          np.float32)
+        probes[1, 3] = np.uint32(1).view(np.float32)
+        probes[2, 3] = np.uint32(2).view(np.float32)
+        rot = np.eye(4)
+        c, si = np.cos(0.3), np.sin(0.3)
+        rot[:3, :3] = [[c, 0, si], [0, 1, 0], [-si, 0, c]]
+        ref = np.full((len(probes) * len(dirs), 4), -7.0, np.float32)
+        pyoracle.pass_ddgi(s["oracle"], probes, dirs, rot, ref, ray_dirs_inactive=dirs_in, inactive_ray_count=8,
+                           environment=(0.25, 0.5, 0.75))
+        out = torch.full(ref.shape, -7.0, dtype=torch.float32, device="cuda")
+        dev = lambda a: torch.from_numpy(a).cuda()
+        ctx.ddgi_trace(dev(probes), dev(dirs), rot, out, ray_dirs_inactive=dev(dirs_in), inactive_ray_count=8,
+                       environment=(0.25, 0.5, 0.75))
+        ctx.synchronize()
+        got = out.cpu().numpy()
+        gd, gr, gdist = unpack_ray_hits(got)
+        rd, rr, rdist = unpack_ray_hits(ref)
+        untouched = np.all(ref == -7.0, axis=1)
+        assert np.array_equal(untouched, np.all(got == -7.0, axis=1))
+        np.testing.assert_array_equal(gr[~untouched], rr[~untouched])       # radiance: EMIT, 0 or environment
+        np.testing.assert_allclose(gd[~untouched], rd[~untouched], atol=1e-3)
+        np.testing.assert_allclose(gdist[~untouched], rdist[~untouched], rtol=1e-5)
+        assert (gdist[~untouched] < 0).sum() > 0                            # back faces were met
+    finally:
+        ctx.close()
+
+
+@pytest.fixture(scope="module")
+def terrain_ctx():
+    ctx = atlas_rt.Context(device=0)
+    s = small_scene(cull_terrain_backfaces=False)
+    upload(ctx, s)
+    yield ctx, s
+    ctx.close()
+
+
+@pytest.mark.parametrize("half_res,samples", [(False, False), (True, True)])
+@pytest.mark.parametrize("opacity", [False, True])
+def test_rtao_matches_oracle(terrain_ctx, half_res, samples, opacity):
+    ctx, s = terrain_ctx
+    gb = gbuffer(s, 160, 90, half_res=half_res, samples=samples)
+    params = dict(radius=25.0, opacity_check=opacity, frame_seed=5, seed=3)
+    got = run(ctx, "rtao", gb, **params)
+    ref = pyoracle.pass_screen("rtao", s["oracle"], gb, **params)
+    drawn = gb["depth"] < 1.0
+    assert drawn.mean() > 0.5 and 0.03 < (ref[drawn] < 1.0).mean() < 0.97
+    assert np.all(got[~drawn] == 1.0)
+    assert (got == ref).mean() > 0.99
+
+
+@pytest.mark.parametrize("kind", ["reflections", "rtgi"])
+@pytest.mark.parametrize("opacity", [False, True])
+def test_shading_passes_match_oracle(terrain_ctx, kind, opacity):
+    ctx, s = terrain_ctx
+    rng = np.random.default_rng(11)
+    rough = rng.uniform(0.0, 1.1, (90, 160)).astype(np.float32)
+    rough[rng.random((90, 160)) < 0.2] = 0.0
+    gb = gbuffer(s, 160, 90, roughness=rough, samples=kind == "rtgi")
+    params = dict(radiance_limit=4.0, roughness_cutoff=0.8, bias=0.1, environment=(0.05, 0.1, 0.2),
+                  opacity_check=opacity, frame_seed=2, seed=9)
+    got = run(ctx, kind, gb, **params)
+    ref = pyoracle.pass_screen(kind, s["oracle"], gb, **params)
+    assert np.all(got[..., 3] == 1.0)
+    close = np.all(np.abs(got[..., :3] - ref[..., :3]) <= 1e-3 * np.abs(ref[..., :3]) + 1e-5, axis=2)
+    assert close.mean() > 0.97
+    lit = ref[..., :3].sum(axis=2) > 0.0
+    assert lit.mean() > 0.3
+    # the image means agree to within the few differing pixels
+    np.testing.assert_allclose(got[..., :3].mean(), ref[..., :3].mean(), rtol=0.02)
+
+
+def test_ddgi_matches_oracle():
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    try:
+        s = small_scene(cull_terrain_backfaces=True)
+        upload(ctx, s)
+        g = np.stack(np.meshgrid(np.linspace(5, 95, 8), [-3.0, 6.0, 15.0], np.linspace(5, 95, 8), indexing="ij"),
+                     -1).reshape(-1, 3)
+        probes = np.concatenate([g, np.zeros((len(g), 1))], 1).astype(np.float32)
+        states = np.arange(len(g)) % 3
+        probes[:, 3] = states.astype(np.uint32).view(np.float32)
+        dirs, dirs_in = fibonacci_dirs(96), fibonacci_dirs(24)
+        rot = np.eye(4)
+        rot[:3, :3] = np.linalg.qr(np.random.default_rng(4).normal(size=(3, 3)))[0]
+        params = dict(environment=(0.3, 0.4, 0.5), frame_seed=7, seed=2)
+        ref = np.full((len(probes) * len(dirs), 4), -7.0, np.float32)
+        pyoracle.pass_ddgi(s["oracle"], probes, dirs, rot, ref, ray_dirs_inactive=dirs_in, inactive_ray_count=24,
+                           **params)
+        out = torch.full(ref.shape, -7.0, dtype=torch.float32, device="cuda")
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        ctx.ddgi_trace(dev(probes), dev(dirs), rot, out, ray_dirs_inactive=dev(dirs_in), inactive_ray_count=24,
+                       **params)
+        ctx.synchronize()
+        got = out.cpu().numpy()
+        untouched = np.all(ref == -7.0, axis=1)
+        assert untouched.sum() == (states == 2).sum() * (96 - 24)
+        assert np.array_equal(untouched, np.all(got == -7.0, axis=1))
+        gd, gr, gdist = unpack_ray_hits(got[~untouched])
+        rd, rr, rdist = unpack_ray_hits(ref[~untouched])
+        np.testing.assert_allclose(gd, rd, atol=1e-3)
+        same_t = np.abs(gdist - rdist) <= 1e-4 * np.abs(rdist)
+        assert same_t.mean() > 0.99
+        assert (rdist < 0).mean() > 0.05                     # probes under the one-sided terrain
+        close = np.all(np.abs(gr - rr) <= 4e-3 * np.abs(rr) + 1e-4, axis=1)
+        assert close.mean() > 0.97
+    finally:
+        ctx.close()
