@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline pass only (no extra workloads)")
     ap.add_argument("--autotune", action="store_true", help="re-run the launch-parameter autotuner")
-    ap.add_argument("--workloads", default="random65536,batched64,bvh_build,pathtrace,radiance_cache",
+    ap.add_argument("--workloads", default="random65536,batched64,bvh_build,passes,pathtrace,radiance_cache",
                     help="comma-separated extra workloads (radiance_cache needs pathtrace)")
     ap.add_argument("--pt-ref-spp", type=int, default=4096, help="samples of the converged image")
     ap.add_argument("--rc-max-frames", type=int, default=320, help="frame cap of the radiance-cache run")
@@ -449,6 +449,84 @@ def converged_image(torch, dev, stream, ctx, cam, spp, chunk=256, seed=7, offset
     return (acc64 / spp).cpu().numpy().reshape(cam.height, cam.width, 3)
 
 
+def workload_passes(torch, dev, stream, flush, steps, cpu_threads):
+    """The traversal's other consumers on the terrain + boxes scene with its
+    area light: RTAO at half resolution (960x540, radius 25), reflections
+    (1920x1080, per-pixel roughness U[0, 1], cutoff 0.9), RTGI (1920x1080)
+    and DDGI probe rays (32 x 8 x 32 probes x 256 rays).  G-buffers come from
+    the library's own closest hits (atlas_rt.gbuffer).  Device time per pass
+    (inputs resident, L2 flushed before each step); the oracle's time for the
+    same pass on the host cores beside it."""
+    import atlas_rt
+    from atlas_rt import gbuffer as G, ptscene
+    if cpu_threads:
+        sys.path.insert(0, str(REPO / "oracle"))
+        import pyoracle
+    ctx = atlas_rt.Context(device=dev.index or 0)
+    sc = ptscene.build()
+    mid, shading, lights, gt = ptscene.upload(ctx, sc)
+    W, H = 1920, 1080
+    V = G.look_at((50.0, 40.0, -15.0), (50.0, 0.0, 50.0))
+    P = G.perspective(60.0, W / H, 0.5, 400.0)
+    gb = G.device_gbuffer(ctx, shading, V, P, W, H)
+    gb_half = G.device_gbuffer(ctx, shading, V, P, W // 2, H // 2, half_res=True)
+    gen = torch.Generator(device=dev).manual_seed(5)
+    gb_refl = dict(gb, roughness=torch.rand((H, W), generator=gen, device=dev))
+    out_ao = torch.empty((H // 2, W // 2), dtype=torch.float32, device=dev)
+    out_rad = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    g = np.stack(np.meshgrid(np.linspace(2, 98, 32), np.linspace(-2, 20, 8), np.linspace(2, 98, 32), indexing="ij"),
+                 -1).reshape(-1, 3)
+    probes_h = np.concatenate([g, np.full((len(g), 1), np.uint32(1).view(np.float32))], 1).astype(np.float32)
+    i = np.arange(256) + 0.5
+    ph, th = np.arccos(1 - 2 * i / 256), np.pi * (1 + 5 ** 0.5) * i
+    dirs_h = np.stack([np.cos(th) * np.sin(ph), np.cos(ph), np.sin(th) * np.sin(ph), np.zeros(256)], 1).astype(np.float32)
+    rot = np.eye(4)
+    rot[:3, :3] = np.linalg.qr(np.random.default_rng(9).normal(size=(3, 3)))[0]
+    probes, dirs = torch.from_numpy(probes_h).to(dev), torch.from_numpy(dirs_h).to(dev)
+    hits = torch.empty((len(probes_h) * 256, 4), dtype=torch.float32, device=dev)
+    drawn_full = int((gb["depth"] < 1.0).sum())
+    passes = {
+        "rtao_half_res": (lambda k: ctx.rtao(gb_half, out_ao, stream=stream, radius=25.0, frame_seed=k),
+                          int((gb_half["depth"] < 1.0).sum()), "rtao", gb_half, dict(radius=25.0)),
+        "reflections": (lambda k: ctx.reflections(gb_refl, out_rad, stream=stream, roughness_cutoff=0.9,
+                                                  radiance_limit=10.0, frame_seed=k),
+                        int(((gb_refl["depth"] < 1.0) & (gb_refl["roughness"] <= 0.9)).sum()), "reflections",
+                        gb_refl, dict(roughness_cutoff=0.9, radiance_limit=10.0)),
+        "rtgi": (lambda k: ctx.rtgi(gb, out_rad, stream=stream, radiance_limit=10.0, frame_seed=k), drawn_full,
+                 "rtgi", gb, dict(radiance_limit=10.0)),
+        "ddgi_probe_rays": (lambda k: ctx.ddgi_trace(probes, dirs, rot, hits, stream=stream, frame_seed=k),
+                            len(probes_h) * 256, None, None, None),
+    }
+    oscene = None
+    out = {"resolution": [W, H], "probes": len(probes_h), "rays_per_probe": 256}
+    for name, (fn, rays, kind, gbuf, params) in passes.items():
+        for k in range(3):
+            fn(k)
+        ks = iter(range(3, 3 + steps))
+        ms = float(np.mean(timed_steps(torch, dev, stream, lambda: fn(next(ks)), steps, flush)))
+        rec = {"ms": ms, "primary_rays": rays, "primary_mrays_s": rays / (ms * 1e-3) / 1e6}
+        if cpu_threads:
+            if oscene is None:
+                top = atlas_rt.BVH(boxes_only=np.concatenate(atlas_rt.mesh_bounds(sc["bvh"]))[None, :])
+                inst = np.array([atlas_rt.make_instance(np.eye(4), 0, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+                model = np.eye(3, 4, dtype=np.float32).reshape(1, -1)
+                oscene = (top.nodes_f32, inst[top.order].copy(), model, [(sc["bvh"].nodes_f32, gt, shading)],
+                          sc["materials"], lights)
+            t0 = time.perf_counter()
+            if kind is None:
+                ref = np.zeros((len(probes_h) * 256, 4), np.float32)
+                pyoracle.pass_ddgi(oscene, probes_h, dirs_h, rot, ref, threads=cpu_threads)
+            else:
+                host = {k2: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k2, v in gbuf.items()}
+                pyoracle.pass_screen(kind, oscene, host, threads=cpu_threads, **params)
+            rec["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+            rec["cpu_threads"] = cpu_threads
+        out[name] = rec
+    ctx.synchronize(stream)
+    ctx.close()
+    return out
+
+
 def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
     """Plain GPU path tracer on the terrain + boxes scene at 1920x1080, 3
     bounces: wall time to `spp` samples and rel-MSE against a
@@ -751,6 +829,9 @@ def main():
                                                               log=(lambda m: print(m, file=sys.stderr)))
         if "bvh_build" in wl:
             line["workloads"]["bvh_build"] = workload_bvh_build(torch, dev, stream, flush)
+        if "passes" in wl:
+            line["workloads"]["passes"] = workload_passes(torch, dev, stream, flush, max(args.steps // 2, 3),
+                                                          0 if args.no_cpu_baseline else (os.cpu_count() or 1))
         if "pathtrace" in wl:
             pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp)
             line["workloads"]["pathtrace"] = pt

@@ -8,6 +8,7 @@ import numpy as np
 import atlas_rt
 import pyoracle
 from atlas_rt import BVH, ptscene, scenes
+from atlas_rt.gbuffer import encode_normal, look_at, perspective, view_rays
 
 
 def small_scene(seed=7, cull_terrain_backfaces=False):
@@ -38,39 +39,6 @@ def upload(ctx, s):
     ctx.set_lights(s["lights"])
 
 
-def look_at(eye, target, up=(0.0, 1.0, 0.0)):
-    eye, target, up = (np.asarray(v, np.float64) for v in (eye, target, up))
-    f = target - eye
-    f /= np.linalg.norm(f)
-    r = np.cross(f, up)
-    r /= np.linalg.norm(r)
-    u = np.cross(r, f)
-    V = np.eye(4)
-    V[0, :3], V[1, :3], V[2, :3] = r, u, -f
-    V[:3, 3] = -V[:3, :3] @ eye
-    return V
-
-
-def perspective(fovy_deg, aspect, near, far):
-    f = 1.0 / np.tan(np.radians(fovy_deg) / 2)
-    P = np.zeros((4, 4))
-    P[0, 0], P[1, 1] = f / aspect, f
-    P[2, 2], P[2, 3] = far / (near - far), far * near / (near - far)   # depth 0 at near, 1 at far
-    P[3, 2] = -1.0
-    return P
-
-
-def encode_normal(n):
-    """EncodeNormal (common/normalencode.hsh:3-16) of unit vectors (n, 3)."""
-    n = n / np.abs(n).sum(axis=1, keepdims=True)
-    x, y, z = n[:, 0].copy(), n[:, 1], n[:, 2].copy()
-    low = y < 0
-    ox, oz = x[low].copy(), z[low].copy()
-    x[low] = np.where(ox >= 0, 1.0, -1.0) * (1.0 - np.abs(oz))
-    z[low] = np.where(oz >= 0, 1.0, -1.0) * (1.0 - np.abs(ox))
-    return np.stack([x, z], axis=1)
-
-
 def gbuffer(s, w, h, eye=(50.0, 40.0, -15.0), target=(50.0, 0.0, 50.0), up=(0.0, 1.0, 0.0), half_res=False,
             seed=3, roughness=None, samples=False):
     """A G-buffer of the scene seen from `eye`.  With half_res, the depth
@@ -78,21 +46,8 @@ def gbuffer(s, w, h, eye=(50.0, 40.0, -15.0), target=(50.0, 0.0, 50.0), up=(0.0,
     rng = np.random.default_rng(seed)
     V = look_at(eye, target, up)
     P = perspective(60.0, w / h, 0.5, 400.0)
-    inv_pv = np.linalg.inv(P @ V)
-    py, px = np.mgrid[0:h, 0:w]
-    px, py = px.reshape(-1).astype(np.float64), py.reshape(-1).astype(np.float64)
     offset = rng.integers(0, 4, w * h).astype(np.uint8) if half_res else None
-    if half_res:
-        tx = (2 * px + (offset & 1) + 0.5) / (2 * w)
-        ty = (2 * py + (offset >> 1) + 0.5) / (2 * h)
-    else:
-        tx, ty = (px + 0.5) / w, (py + 0.5) / h
-    ndc = np.stack([2 * tx - 1, 2 * ty - 1], axis=1)
-    far = np.concatenate([ndc, np.ones((len(ndc), 2))], axis=1) @ inv_pv.T
-    far = far[:, :3] / far[:, 3:]
-    o = np.tile(np.asarray(eye, np.float64), (len(ndc), 1))
-    d = far - o
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o, d = view_rays(V, P, w, h, offset)
     rays8 = scenes.rays8(o.astype(np.float32), d.astype(np.float32), 0.0, 1e12)
     tl, inst, model, meshes, mats, lights = s["oracle"]
     ptr, ino, tuv = pyoracle.scene_closest_glsl(tl, inst, meshes, rays8)

@@ -182,3 +182,23 @@ def test_ddgi_matches_oracle():
         assert close.mean() > 0.97
     finally:
         ctx.close()
+
+
+def test_device_gbuffer_matches_oracle_gbuffer(terrain_ctx):
+    """atlas_rt.gbuffer.device_gbuffer (the library's closest hits) against
+    the G-buffer made with the oracle's traversal."""
+    from atlas_rt.gbuffer import device_gbuffer, look_at, perspective
+    ctx, s = terrain_ctx
+    w, h = 160, 90
+    for half_res in (False, True):
+        ref = gbuffer(s, w, h, half_res=half_res)
+        V = look_at((50.0, 40.0, -15.0), (50.0, 0.0, 50.0))
+        P = perspective(60.0, w / h, 0.5, 400.0)
+        got = device_gbuffer(ctx, s["shading"], V, P, w, h, half_res=half_res)
+        if half_res:
+            np.testing.assert_array_equal(got["offset"].cpu().numpy(), ref["offset"])
+        gd, rd = got["depth"].cpu().numpy(), ref["depth"]
+        np.testing.assert_array_equal(gd >= 1.0, rd >= 1.0)
+        assert (np.abs(gd - rd) <= 1e-6).mean() > 0.99
+        same_n = np.all(np.abs(got["normal"].cpu().numpy() - ref["normal"]) <= 1e-5, axis=2)
+        assert same_n.mean() > 0.99
