@@ -110,9 +110,44 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want, ui
     return base + __popc(mask & lt);
 }
 
+// Queue appends aggregated over the block: one atomicAdd per block and
+// queue.  Appending per warp instead puts 8k-65k atomics on one address for
+// a full-screen queue, and they serialise in L2.  Every thread of the block
+// must call this the same number of times (it synchronises the block), with
+// blockDim.x a multiple of 32 and at most 1024.  slot[q] is valid where
+// want[q] is set.
+template <int NQ>
+__device__ __forceinline__ void block_append(uint32_t* const (&counters)[NQ], const bool (&want)[NQ],
+                                             uint32_t (&slot)[NQ]) {
+    __shared__ uint32_t sm[NQ][33];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    uint32_t mask[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        mask[q] = __ballot_sync(0xffffffffu, want[q]);
+        if (lane == 0) sm[q][warp] = __popc(mask[q]);
+    }
+    __syncthreads();
+    if (threadIdx.x < uint32_t(NQ)) {
+        const uint32_t q = threadIdx.x;
+        uint32_t total = 0;
+        for (uint32_t w = 0; w < warps; w++) {
+            const uint32_t c = sm[q][w];
+            sm[q][w] = total;
+            total += c;
+        }
+        sm[q][32] = total ? atomicAdd(counters[q], total) : 0u;
+    }
+    __syncthreads();
+    uint32_t lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+#pragma unroll
+    for (int q = 0; q < NQ; q++) slot[q] = sm[q][32] + sm[q][warp] + __popc(mask[q] & lt);
+    __syncthreads();
+}
+
 static __global__ void spawn_kernel(SpawnParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
     bool sec = false, shd = false;
     float3 P = make_float3(0, 0, 0), N = make_float3(0, 0, 0), D = make_float3(0, 0, 0), S = make_float3(0, 0, 0);
@@ -152,14 +187,17 @@ static __global__ void spawn_kernel(SpawnParams p) {
             shd = N.x * p.lightx + N.y * p.lighty + N.z * p.lightz > 0.0f;
         }
     }
-    const uint32_t si = warp_append(p.counts, sec, lane);
+    uint32_t* const counters[2] = { p.counts, p.counts + 1 };
+    const bool want[2] = { sec, shd };
+    uint32_t slot[2];
+    block_append<2>(counters, want, slot);
+    const uint32_t si = slot[0], hi = slot[1];
     if (sec) {
         float4* r = p.secondary + size_t(si) * 3;
         r[0] = make_float4(S.x, S.y, S.z, __int_as_float(id));
         r[1] = make_float4(D.x, D.y, D.z, 0.0f);
         r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
     }
-    const uint32_t hi = warp_append(p.counts + 1, shd, lane);
     if (shd) {
         float4* r = p.shadow + size_t(hi) * 3;
         r[0] = make_float4(P.x + N.x * p.epsilon, P.y + N.y * p.epsilon, P.z + N.z * p.epsilon, __int_as_float(id));

@@ -112,7 +112,6 @@ __device__ __forceinline__ V3 ggx_vndf_dir(V3 N, V3 V, float alpha, float u0, fl
 template <int KIND>
 __global__ void gb_raygen_kernel(GbParams g, PassP pp, Queue q, float* ao_out, float4* rad_out) {
     const uint32_t n = g.w * g.h;
-    const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t pix = base + threadIdx.x;
         bool emit = false;
@@ -194,7 +193,11 @@ __global__ void gb_raygen_kernel(GbParams g, PassP pp, Queue q, float* ao_out, f
                 else rad_out[pix] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
             }
         }
-        const uint32_t slot = warp_append(q.count, emit, lane);
+        uint32_t* const counters[1] = { q.count };
+        const bool want[1] = { emit };
+        uint32_t slots[1];
+        block_append<1>(counters, want, slots);
+        const uint32_t slot = slots[0];
         if (emit && slot < q.capacity) {
             float4* r = q.rays + size_t(slot) * 3;
             r[0] = make_float4(O.x, O.y, O.z, 0.0f);
@@ -216,7 +219,6 @@ struct DdgiP {
 // ddgi/rayGen.csh:39-81
 __global__ void ddgi_raygen_kernel(DdgiP d, Queue q) {
     const uint32_t total = d.n_probes * d.ray_count;
-    const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t idx = base + threadIdx.x;
         bool emit = false;
@@ -234,7 +236,11 @@ __global__ void ddgi_raygen_kernel(DdgiP d, Queue q) {
                 emit = true;
             }
         }
-        const uint32_t slot = warp_append(q.count, emit, lane);
+        uint32_t* const counters[1] = { q.count };
+        const bool want[1] = { emit };
+        uint32_t slots[1];
+        block_append<1>(counters, want, slots);
+        const uint32_t slot = slots[0];
         if (emit && slot < q.capacity) {
             float4* r = q.rays + size_t(slot) * 3;
             r[0] = make_float4(O.x, O.y, O.z, 0.0f);
@@ -269,7 +275,6 @@ struct ShadeP {
 template <int KIND>
 __global__ void pass_shade_kernel(ShadeP p) {
     const uint32_t n = min(*p.q.count, p.q.capacity);
-    const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
         bool emit = false;
@@ -306,7 +311,11 @@ __global__ void pass_shade_kernel(ShadeP p) {
             }
             p.rad[e] = make_float4(rad.x, rad.y, rad.z, dist);
         }
-        const uint32_t slot = warp_append(p.sq.count, emit, lane);
+        uint32_t* const counters[1] = { p.sq.count };
+        const bool want[1] = { emit };
+        uint32_t slots[1];
+        block_append<1>(counters, want, slots);
+        const uint32_t slot = slots[0];
         if (emit && slot < p.sq.capacity) {
             float4* r = p.sq.rays + size_t(slot) * 3;
             r[0] = sr0;

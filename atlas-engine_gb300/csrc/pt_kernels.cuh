@@ -585,7 +585,6 @@ __device__ __forceinline__ float mis_hit_factor(const PtScene& sc, const Surf& s
 // rayHit.csh:55-325 for one bounce of the wavefront.
 static __global__ void pt_shade_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = min(*p.n_in, queue_capacity(p));
     bool emitRay = false, emitShadow = false;
     float4 outRay0{}, outRay1{}, outPay{}, shRay0{}, shRay1{}, shPay{};
@@ -626,7 +625,11 @@ static __global__ void pt_shade_kernel(PtParams p) {
             }
         }
     }
-    const uint32_t ri = warp_append(p.n_out, emitRay, lane);
+    uint32_t* const counters[2] = { p.n_out, p.n_shadow };
+    const bool want[2] = { emitRay, emitShadow };
+    uint32_t slot[2];
+    block_append<2>(counters, want, slot);
+    const uint32_t ri = slot[0], si = slot[1];
     if (emitRay) {
         float4* r = p.rays_out + size_t(ri) * 3;
         r[0] = outRay0;
@@ -634,7 +637,6 @@ static __global__ void pt_shade_kernel(PtParams p) {
         r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
         p.pay_out[ri] = outPay;
     }
-    const uint32_t si = warp_append(p.n_shadow, emitShadow, lane);
     if (emitShadow) {
         float4* r = p.shadow_rays + size_t(si) * 3;
         r[0] = shRay0;
