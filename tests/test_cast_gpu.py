@@ -46,7 +46,11 @@ def test_raygen_matches_host_formula(ctx, w, h):
         assert set((first % w).tolist()) == set(range(8)) and set((first // w).tolist()) == set(range(8))
 
 
-def test_cast_pass_parity(ctx, terrain):
+@pytest.mark.parametrize("host", ["pageable", "pinned"])
+def test_cast_pass_parity(ctx, terrain, host):
+    """Pageable host outputs go through device scratch and copies; pinned
+    ones are written by the trace kernels directly where nothing on the
+    device reads them again (bounce hits, shadow occlusion)."""
     b, gt, mid = terrain
     import torch
     w, h = 640, 360
@@ -54,13 +58,22 @@ def test_cast_pass_parity(ctx, terrain):
     cam = atlas_rt.make_camera(camd)
     bp = atlas_rt.make_bounce_params((0.4, 1.0, 0.3), 0.1, seed=3)
     n = w * h
-    ph = np.zeros(n, atlas_rt.HIT_DTYPE)
-    sr = np.zeros((n, 12), np.float32)
-    sh = np.zeros(n, atlas_rt.HIT_DTYPE)
-    dr = np.zeros((n, 12), np.float32)
-    oc = np.zeros(n, np.uint8)
-    n0, n1, n2 = ctx.cast_pass(mid, cam, bp, primary_hits=ph, secondary_rays=sr, secondary_hits=sh,
-                               shadow_rays=dr, shadow_occluded=oc)
+    if host == "pinned":
+        bufs = [torch.full(shape, -3, dtype=dt, pin_memory=True)
+                for shape, dt in (((n, 8), torch.float32), ((n, 12), torch.float32), ((n, 8), torch.float32),
+                                  ((n, 12), torch.float32), ((n,), torch.uint8))]
+        args = bufs
+        ph, sr, sh, dr, oc = (t.numpy() for t in bufs)
+        ph, sh = ph.view(atlas_rt.HIT_DTYPE).reshape(n), sh.view(atlas_rt.HIT_DTYPE).reshape(n)
+    else:
+        ph = np.zeros(n, atlas_rt.HIT_DTYPE)
+        sr = np.zeros((n, 12), np.float32)
+        sh = np.zeros(n, atlas_rt.HIT_DTYPE)
+        dr = np.zeros((n, 12), np.float32)
+        oc = np.zeros(n, np.uint8)
+        args = [ph, sr, sh, dr, oc]
+    n0, n1, n2 = ctx.cast_pass(mid, cam, bp, primary_hits=args[0], secondary_rays=args[1], secondary_hits=args[2],
+                               shadow_rays=args[3], shadow_occluded=args[4])
     assert n0 == n and 0 < n1 <= n and 0 < n2 <= n1
     # primary rays regenerated on the host in the same tile order
     prim = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
