@@ -95,6 +95,8 @@ struct ae_rt_ctx {
     cudaEvent_t cast_events[4] = { nullptr, nullptr, nullptr, nullptr };
     uint32_t* h_cast_counts = nullptr;  // pinned, mapped
     uint32_t* d_cast_counts_mapped = nullptr;   // its device address
+    uint32_t* h_error = nullptr;        // pinned, mapped: the error word as last published
+    uint32_t* d_error_mapped = nullptr;
     std::string last_error;
     std::mutex upload_mutex;
 };
