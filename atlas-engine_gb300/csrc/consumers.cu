@@ -216,15 +216,21 @@ struct DdgiP {
     uint32_t n_probes, ray_count, inactive_count;
 };
 
-// ddgi/rayGen.csh:39-81
+// ddgi/rayGen.csh:39-81.  The queue is filled direction-major: the 32 rays
+// of a warp share one direction of the set and start from 32 neighbouring
+// probes, so they cross the scene side by side (probe-major order would give
+// every warp 32 directions spread over the sphere).  Results still land at
+// probe * ray_count + i through the key.
 __global__ void ddgi_raygen_kernel(DdgiP d, Queue q) {
     const uint32_t total = d.n_probes * d.ray_count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-        const uint32_t idx = base + threadIdx.x;
+        const uint32_t t = base + threadIdx.x;
         bool emit = false;
         V3 O = v3(0, 0, 0), D = v3(0, 0, 0);
-        if (idx < total) {
-            const uint32_t probe = idx / d.ray_count, i = idx % d.ray_count;
+        uint32_t idx = 0;
+        if (t < total) {
+            const uint32_t probe = t % d.n_probes, i = t / d.n_probes;
+            idx = probe * d.ray_count + i;
             const float4 pr = d.probes[probe];
             const bool inactive = __float_as_uint(pr.w) == 2u;
             if (i < (inactive ? d.inactive_count : d.ray_count)) {
