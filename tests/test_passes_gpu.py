@@ -202,3 +202,41 @@ def test_device_gbuffer_matches_oracle_gbuffer(terrain_ctx):
         assert (np.abs(gd - rd) <= 1e-6).mean() > 0.99
         same_n = np.all(np.abs(got["normal"].cpu().numpy() - ref["normal"]) <= 1e-5, axis=2)
         assert same_n.mean() > 0.99
+
+
+def test_pass_argument_errors(sand_ctx):
+    """Invalid calls return a status (no launch): host G-buffer planes, a
+    missing roughness plane for reflections, host outputs, no scene."""
+    import torch
+    ctx, s = sand_ctx
+    gb = floor_gbuffer(s)
+    dev = to_device(gb)
+    out = torch.empty((16, 24, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(atlas_rt.AeRtError) as e:
+        ctx.rtao(gb, out[..., 0].contiguous())                 # host planes
+    assert "device memory" in str(e.value)
+    with pytest.raises(atlas_rt.AeRtError) as e:
+        ctx.reflections(dev, out)                              # no roughness plane
+    assert "roughness" in str(e.value)
+    with pytest.raises(atlas_rt.AeRtError):
+        ctx.rtgi(dev, np.zeros((16, 24, 4), np.float32))       # host output
+    empty = atlas_rt.Context(device=0)
+    try:
+        with pytest.raises(atlas_rt.AeRtError) as e:
+            empty.rtao(dev, out[..., 0].contiguous())
+        assert "scene" in str(e.value)
+    finally:
+        empty.close()
+    # an empty G-buffer is a no-op
+    z = dict(dev, depth=dev["depth"][:0], normal=dev["normal"][:0])
+    ctx.rtao(z, out[..., 0].contiguous())
+    ctx.synchronize()
+
+
+def test_texture_argument_errors(sand_ctx):
+    ctx, _ = sand_ctx
+    with pytest.raises(ValueError):
+        ctx.set_textures([np.zeros((4, 4, 3), np.uint8)])     # RGB8 is not a format
+    with pytest.raises(atlas_rt.AeRtError):
+        ctx.set_textures([np.zeros((0, 4), np.uint8)])        # empty texture
+    ctx.set_textures([])                                       # clears the table
