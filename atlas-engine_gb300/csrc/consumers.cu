@@ -506,11 +506,12 @@ ae_rt_status ScreenPass(ae_rt_ctx* ctx, const ae_gbuffer* gb, const ae_rt_pass_p
                         void* stream) {
     ae_rt_status st = CheckScene(ctx, params, KIND != kPassAO);
     if (st != AE_RT_OK) return st;
+    if (!gb) return Fail(ctx, AE_RT_INVALID_ARG, "null G-buffer");
+    if (gb->width == 0 || gb->height == 0) return AE_RT_OK;
     st = CheckGBuffer(ctx, gb, KIND == kPassRefl);
     if (st != AE_RT_OK) return st;
     if (!out || !IsDevicePointer(out)) return Fail(ctx, AE_RT_INVALID_ARG, "the output must be device memory");
     const uint32_t n = gb->width * gb->height;
-    if (n == 0) return AE_RT_OK;
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Queue q, sq;
