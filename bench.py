@@ -576,22 +576,47 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
 
 
 def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(1, 2, 3, 4, 6, 8, 16), max_frames=320,
-                            n_paths=65536, steps=2, rough_cut=0.35, last_bounce=1, close=True):
+                            n_paths=65536, steps=2, rough_cut=0.35, last_bounce=1, close=True,
+                            samples_per_frame=(1, 2, 4)):
     """Radiance-cache path tracer on the same scene, camera and converged
     image as the plain path tracer: the cache starts untrained; every frame
     trains it on `n_paths` self-generated 3-bounce paths (`steps` Adam
-    steps, lr 1e-2) and, from frame `start` on, renders 1 spp with paths
-    ending in the cache (ae_rc_frame: the render uses the cache as trained up
-    to the previous frame, while this frame's training paths are traced
-    beside it).  Frame
-    times are CUDA-event times on the stream (the error read-backs between
-    frames are outside them).  The rendered frames are averaged from frame
-    `start` on (the frames before only train); for each start the GPU time
-    from the cold cache to the frame where the average reaches the plain
-    path tracer's 64-spp rel-MSE is reported, and the best start is the
-    result."""
+    steps, lr 1e-2) and, from frame `start` on, renders `spf` samples per
+    pixel with paths ending in the cache: one through ae_rc_frame (the render
+    uses the cache as trained up to the previous frame, while this frame's
+    training paths are traced beside it), the others through ae_rc_render
+    with the same cache.  Frame times are CUDA-event times on the stream
+    (the error read-backs between frames are outside them).  The rendered
+    frames are averaged from frame `start` on (the frames before only
+    train); for each start and spf the GPU time from the cold cache to the
+    frame where the average reaches the plain path tracer's 64-spp rel-MSE is
+    reported, and the best is the result."""
     import atlas_rt
-    from atlas_rt import ptscene, scenes
+    ctx, sc, cam, ref = scene
+    out = {"by_samples_per_frame": {}}
+    best = None
+    for spf in samples_per_frame:
+        r = _rc_run(torch, dev, stream, pt, scene, starts, max_frames, n_paths, steps, rough_cut, last_bounce, spf)
+        out["by_samples_per_frame"][str(spf)] = r
+        if r["ms_to_equal_rel_mse"] is not None and (best is None or r["ms_to_equal_rel_mse"] < best[1]):
+            best = (spf, r["ms_to_equal_rel_mse"])
+    if close:
+        ctx.close()
+    top = out["by_samples_per_frame"][str(best[0] if best else samples_per_frame[0])]
+    for k in ("resolution", "n_paths", "adam_steps_per_frame", "radiance_scale", "rough_cut", "last_bounce",
+              "target_rel_mse", "plain_pt_ms_to_64spp"):
+        out[k] = top[k]
+    out["samples_per_frame"] = best[0] if best else None
+    out["ms_to_equal_rel_mse"] = best[1] if best else None
+    out["speedup_vs_plain_pt"] = pt["ms_to_spp"] / best[1] if best else None
+    return out
+
+
+def _rc_run(torch, dev, stream, pt, scene, starts, max_frames, n_paths, steps, rough_cut, last_bounce, spf):
+    """One cold-cache run of the radiance-cache schedule at `spf` samples
+    per training frame."""
+    import atlas_rt
+    from atlas_rt import scenes
     ctx, sc, cam, ref = scene
     target = pt["rel_mse"]
     pt_ms = pt["ms_to_spp"]
@@ -623,10 +648,13 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(1, 2, 3, 4, 6
         evf[0].record(stream)
         if render:
             # one online frame: render with the cache as it stands while the
-            # frame's training paths are traced beside it, then train
+            # frame's training paths are traced beside it, then train; the
+            # frame's further samples render with the same cache
             frame_buf.zero_()
             rc.frame(cam, f, frame_buf, n_paths=n_paths, steps=steps, max_bounces=3, last_bounce=last_bounce,
                      stream=stream)
+            for k in range(1, spf):
+                rc.render(cam, (1 << 22) + f * 8 + k, frame_buf, last_bounce=last_bounce, stream=stream)
         else:
             rc.train_frame(cam, f, n_paths=n_paths, steps=steps, max_bounces=3, stream=stream)
         evf[1].record(stream)
@@ -639,7 +667,7 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(1, 2, 3, 4, 6
         t_cum += tt
         if not render:
             continue
-        rgb = frame_buf[:, :3].double()
+        rgb = frame_buf[:, :3].double() / spf
         for s0 in starts:
             if f >= s0:
                 accs[s0] += rgb
@@ -652,10 +680,8 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, starts=(1, 2, 3, 4, 6
         if len(reached) == len(starts):
             break
     rc.close()
-    if close:
-        ctx.close()
     out = {"resolution": [W, H], "n_paths": n_paths, "adam_steps_per_frame": steps, "radiance_scale": scale,
-           "rough_cut": rough_cut, "last_bounce": last_bounce,
+           "rough_cut": rough_cut, "last_bounce": last_bounce, "samples_per_frame": spf,
            "target_rel_mse": target, "plain_pt_ms_to_64spp": pt_ms, "frames_run": f + 1,
            "train_only_ms_per_frame": train_ms / min(starts),
            "frame_ms": frame_ms / max(f + 1 - min(starts), 1),
