@@ -46,8 +46,8 @@ sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
 
 W, H = 1920, 1080
 # DRAM bytes (read + write) of the primary closest-hit launch of this workload,
-# from ncu (131,443,968 + 39,079,680)
-TRAFFIC_PRIMARY_BYTES = 170_523_648
+# from ncu (131,451,904 + 38,706,432)
+TRAFFIC_PRIMARY_BYTES = 170_158_336
 TMIN, TINF = 0.0, 1e12
 EPSILON = 0.1
 LIGHT = (0.4, 1.0, 0.3)
