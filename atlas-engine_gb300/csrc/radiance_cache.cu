@@ -30,6 +30,10 @@ struct ae_rc {
     float* grid_v = nullptr;
     float* grid_grad = nullptr;
     __half* grid_f16 = nullptr;
+    // what ae_rc_frame's render reads: the cache as trained up to the frame
+    // before, while this frame's training updates grid_f16 / mlp_bf16
+    __half* grid_snap = nullptr;
+    __nv_bfloat16* mlp_snap = nullptr;
     float* d_loss = nullptr;
     uint32_t* d_counts = nullptr;  // [0] training samples, [1] cache queries
     Scratch samples, queries;
@@ -116,7 +120,8 @@ void Destroy(ae_rc* rc) {
     cudaSetDevice(rc->ctx->device);
     for (void* p : { (void*)rc->mlp_master, (void*)rc->mlp_m, (void*)rc->mlp_v, (void*)rc->mlp_grad,
                      (void*)rc->mlp_bf16, (void*)rc->grid_master, (void*)rc->grid_m, (void*)rc->grid_v,
-                     (void*)rc->grid_grad, (void*)rc->grid_f16, (void*)rc->d_loss, (void*)rc->d_counts })
+                     (void*)rc->grid_grad, (void*)rc->grid_f16, (void*)rc->d_loss, (void*)rc->d_counts,
+                     (void*)rc->grid_snap, (void*)rc->mlp_snap })
         cudaFree(p);
     rc->samples.release();
     rc->queries.release();
@@ -234,7 +239,7 @@ ae_rt_status CheckTrainArgs(ae_rc* rc, const ae_camera* cam, uint32_t n_paths, u
 // disjoint pixels of accum (a path that ends in a query at the first vertex
 // adds nothing later).  Joined before returning.
 ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t last_bounce, float* accum,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool from_snapshot = false) {
     ae_rt_ctx* ctx = rc->ctx;
     const uint32_t n = cam->width * cam->height;
     if (n > kPixelMask + 1u) return RcFail(rc, AE_RT_INVALID_ARG, "more than 2^24 pixels");
@@ -283,6 +288,10 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     pt_raygen_kernel<<<blocks, 256, 0, s>>>(c, p);
     RC_CUDA(rc, cudaGetLastError());
     RcMlpParams mp = MlpParams(rc);
+    if (from_snapshot) {
+        mp.grid.table = reinterpret_cast<const __half2*>(rc->grid_snap);
+        mp.weights = rc->mlp_snap;
+    }
     mp.recs = static_cast<const float4*>(rc->queries.ptr);
     mp.n = cap;
     mp.accum = reinterpret_cast<float4*>(accum);
@@ -553,18 +562,37 @@ ae_rt_status ae_rc_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     st = EnsureStreams(rc);
     if (st != AE_RT_OK) return st;
-    // training paths (scene only) on the side stream, beside the render
+    // The render reads a snapshot of the cache as trained up to the previous
+    // frame (the FP16 grid and BF16 weights, ~34 MB, copied on the device),
+    // so that this frame's training -- its paths (scene only) and its Adam
+    // steps -- runs beside the render on the side stream.
+    if (!rc->grid_snap) {
+        RC_CUDA(rc, cudaMalloc(&rc->grid_snap, rc->grid_params * sizeof(__half)));
+        RC_CUDA(rc, cudaMalloc(&rc->mlp_snap, RC_NPARAM * sizeof(__nv_bfloat16)));
+    }
+    RC_CUDA(rc, cudaMemcpyAsync(rc->grid_snap, rc->grid_f16, rc->grid_params * sizeof(__half),
+                                cudaMemcpyDeviceToDevice, s));
+    RC_CUDA(rc, cudaMemcpyAsync(rc->mlp_snap, rc->mlp_bf16, RC_NPARAM * sizeof(__nv_bfloat16),
+                                cudaMemcpyDeviceToDevice, s));
     cudaStream_t a1 = rc->aux[1];
     RC_CUDA(rc, cudaEventRecord(rc->ev[2], s));
     RC_CUDA(rc, cudaStreamWaitEvent(a1, rc->ev[2], 0));
     st = GeneratePaths(rc, cam, frame, n_paths, max_bounces, a1);
     if (st != AE_RT_OK) return st;
+    st = TrainSteps(rc, n_paths, steps, nullptr, a1);
+    if (st != AE_RT_OK) return st;
     RC_CUDA(rc, cudaEventRecord(rc->ev[3], a1));
     rc->max_bounces = max_bounces;
-    st = RenderFrame(rc, cam, frame, last_bounce, accum, s);
+    st = RenderFrame(rc, cam, frame, last_bounce, accum, s, true);
     if (st != AE_RT_OK) return st;
     RC_CUDA(rc, cudaStreamWaitEvent(s, rc->ev[3], 0));
-    return TrainSteps(rc, n_paths, steps, loss_out, s);
+    if (loss_out) {
+        float l = 0.0f;
+        RC_CUDA(rc, cudaMemcpyAsync(&l, rc->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        RC_CUDA(rc, cudaStreamSynchronize(s));
+        *loss_out = l;
+    }
+    return AE_RT_OK;
 }
 
 }  // extern "C"

@@ -716,10 +716,12 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
                           void* stream);
 
 /* One online frame: renders one sample per pixel as ae_rc_render with the
- * cache as it stands, while the frame's n_paths training paths are traced
- * on a second stream (they read the scene only), then trains on them in
- * `steps` Adam steps (ae_rc_train_frame).  Same work as train + render, with
- * the render one training step behind, and the path tracing overlapped. */
+ * cache as it stands at the call (a device-side snapshot of its FP16 grid
+ * and BF16 weights), while on a second stream the frame's n_paths training
+ * paths are traced (they read the scene only) and trained on in `steps`
+ * Adam steps (ae_rc_train_frame).  Same work as train + render, with the
+ * render one training step behind and the training overlapped with it; the
+ * call's stream waits for both. */
 ae_rt_status ae_rc_frame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32_t n_paths, uint32_t steps,
                          uint32_t max_bounces, uint32_t last_bounce, float* accum, float* loss_out, void* stream);
 
