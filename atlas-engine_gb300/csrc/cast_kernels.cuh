@@ -146,6 +146,33 @@ __device__ __forceinline__ void block_append(uint32_t* const (&counters)[NQ], co
     __syncthreads();
 }
 
+// Append to one queue in an order sorted by a small key within the block:
+// a counting sort over KEYS buckets in shared memory, one atomicAdd per block
+// on the global counter.  Rays of one bucket (e.g. one direction octant)
+// land next to each other, so a warp of the tracing kernel gets rays that
+// cross the BVH the same way.  Every thread of the block must call it.
+template <int KEYS>
+__device__ __forceinline__ uint32_t block_append_sorted(uint32_t* counter, bool want, uint32_t key) {
+    __shared__ uint32_t hist[KEYS + 1];
+    if (threadIdx.x <= uint32_t(KEYS)) hist[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t rank = want ? atomicAdd(&hist[key], 1u) : 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (int k = 0; k < KEYS; k++) {
+            const uint32_t c = hist[k];
+            hist[k] = total;
+            total += c;
+        }
+        hist[KEYS] = total ? atomicAdd(counter, total) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = hist[KEYS] + hist[want ? key : 0u] + rank;
+    __syncthreads();
+    return slot;
+}
+
 static __global__ void spawn_kernel(SpawnParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
@@ -187,11 +214,15 @@ static __global__ void spawn_kernel(SpawnParams p) {
             shd = N.x * p.lightx + N.y * p.lighty + N.z * p.lightz > 0.0f;
         }
     }
-    uint32_t* const counters[2] = { p.counts, p.counts + 1 };
-    const bool want[2] = { sec, shd };
-    uint32_t slot[2];
-    block_append<2>(counters, want, slot);
-    const uint32_t si = slot[0], hi = slot[1];
+    // bounce rays sorted by direction octant within the block; shadow rays
+    // all share the light's direction
+    const uint32_t octant = (D.x < 0.0f ? 1u : 0u) | (D.y < 0.0f ? 2u : 0u) | (D.z < 0.0f ? 4u : 0u);
+    const uint32_t si = block_append_sorted<8>(p.counts, sec, octant);
+    uint32_t* const counters[1] = { p.counts + 1 };
+    const bool want[1] = { shd };
+    uint32_t slot[1];
+    block_append<1>(counters, want, slot);
+    const uint32_t hi = slot[0];
     if (sec) {
         float4* r = p.secondary + size_t(si) * 3;
         r[0] = make_float4(S.x, S.y, S.z, __int_as_float(id));
