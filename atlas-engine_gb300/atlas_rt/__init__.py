@@ -146,6 +146,22 @@ class BVH:
             _check(lib().ae_bvh_pack_uvs(self._h, _ptr(uv), _ptr(shading)))
         return shading
 
+    def pack_attributes(self, shading: np.ndarray, uvs, normals=None, colors=None) -> np.ndarray:
+        """UVs, the UV-derived tangent frame and vertex colours (RGBA per
+        vertex, (n, 3, 4) or (n, 12)) into the GPUTriangle array from
+        pack_shading, as MeshData.cpp:172-239 packs them."""
+        uv = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+        col = None if colors is None else np.ascontiguousarray(colors, np.float32).reshape(-1, 12)
+        if self._verts is None or len(uv) != self.n_input or shading.shape != (len(self.order), 24) \
+                or shading.dtype != np.float32 or not shading.flags.c_contiguous \
+                or (nrm is not None and len(nrm) != self.n_input) or (col is not None and len(col) != self.n_input):
+            raise ValueError("per-input-triangle uvs / normals / colors and the (n, 24) pack_shading array expected")
+        if len(self.order):
+            _check(lib().ae_bvh_pack_attributes(self._h, _ptr(self._verts), _ptr(nrm), _ptr(uv), _ptr(col),
+                                                _ptr(shading)))
+        return shading
+
     @property
     def nodes_f32(self) -> np.ndarray:
         return self.nodes.view(np.float32).reshape(-1, 16)

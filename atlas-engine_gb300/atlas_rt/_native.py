@@ -93,6 +93,7 @@ _SIGNATURES = [
     ("ae_bvh_pack_triangles", C.c_int, [P, P, P, P, P]),
     ("ae_bvh_pack_shading", C.c_int, [P, P, P, P, P, P]),
     ("ae_bvh_pack_uvs", C.c_int, [P, P, P]),
+    ("ae_bvh_pack_attributes", C.c_int, [P, P, P, P, P, P]),
     ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     ("ae_rt_ctx_destroy", None, [P]),
     ("ae_rt_last_error", C.c_char_p, [P]),

@@ -849,6 +849,9 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
     p.sc.n_materials = ctx->n_materials;
     p.sc.lights = ctx->d_lights;
     p.sc.n_lights = ctx->n_lights;
+    p.sc.tex.pool = ctx->d_tex_pool;
+    p.sc.tex.desc = static_cast<const atlas::rt::dev::TexDesc*>(ctx->d_tex_desc);
+    p.sc.tex.n = ctx->n_textures;
     p.width = cam->width;
     p.height = cam->height;
     p.max_bounces = params->max_bounces;

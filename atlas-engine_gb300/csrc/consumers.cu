@@ -379,6 +379,9 @@ PtScene Scene(ae_rt_ctx* ctx) {
     sc.n_materials = ctx->n_materials;
     sc.lights = ctx->d_lights;
     sc.n_lights = ctx->n_lights;
+    sc.tex.pool = ctx->d_tex_pool;
+    sc.tex.desc = static_cast<const atlas::rt::dev::TexDesc*>(ctx->d_tex_desc);
+    sc.tex.n = ctx->n_textures;
     return sc;
 }
 

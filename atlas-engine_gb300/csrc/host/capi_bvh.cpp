@@ -144,6 +144,16 @@ void Normalize3(const float* in, float* out) {
     out[2] = in[2] * s;
 }
 
+// glm::packUnorm4x8: round(clamp(c, 0, 1) * 255) per channel, x lowest
+uint32_t PackUnorm4(const float* c) {
+    uint32_t out = 0;
+    for (int k = 0; k < 4; k++) {
+        const float v = std::fmin(std::fmax(c[k], 0.0f), 1.0f);
+        out |= uint32_t(std::lround(v * 255.0f)) << (8 * k);
+    }
+    return out;
+}
+
 }  // namespace
 
 // GPUTriangle packing in BVH order (MeshData.cpp:172-239), without texture
@@ -199,6 +209,53 @@ ae_rt_status ae_bvh_pack_uvs(const ae_bvh* bvh, const float* uvs, ae_triangle* i
             // packHalf2x16: x in the low half, y in the high half
             const uint32_t bits = uint32_t(HalfBits(uv[2 * k])) | (uint32_t(HalfBits(uv[2 * k + 1])) << 16);
             inout[i].d0[k] = Bits(int32_t(bits));
+        }
+    }
+    return AE_RT_OK;
+}
+
+ae_rt_status ae_bvh_pack_attributes(const ae_bvh* bvh, const float* verts, const float* normals, const float* uvs,
+                                    const float* colors, ae_triangle* inout) {
+    if (!bvh || (bvh->primitives && (!verts || !uvs || !inout))) return AE_RT_INVALID_ARG;
+    ae_rt_status st = ae_bvh_pack_uvs(bvh, uvs, inout);
+    if (st != AE_RT_OK) return st;
+    for (uint32_t i = 0; i < bvh->primitives; i++) {
+        const uint32_t src = bvh->built.order[i];
+        const float* v = verts + size_t(src) * 9;
+        const float* uv = uvs + size_t(src) * 6;
+        float n[3][3];
+        if (normals) {
+            for (int k = 0; k < 3; k++) Normalize3(normals + size_t(src) * 9 + 3 * k, n[k]);
+        } else {
+            const float a[3] = { v[3] - v[0], v[4] - v[1], v[5] - v[2] }, b[3] = { v[6] - v[0], v[7] - v[1], v[8] - v[2] };
+            const float c[3] = { a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0] };
+            Normalize3(c, n[0]);
+            for (int k = 0; k < 3; k++) n[1][k] = n[2][k] = n[0][k];
+        }
+        // MeshData.cpp:176-197: UV-space derivatives of position
+        const float e1[3] = { v[3] - v[0], v[4] - v[1], v[5] - v[2] }, e2[3] = { v[6] - v[0], v[7] - v[1], v[8] - v[2] };
+        const float du1 = uv[2] - uv[0], dv1 = uv[3] - uv[1], du2 = uv[4] - uv[0], dv2 = uv[5] - uv[1];
+        const float r = 1.0f / (du1 * dv2 - du2 * dv1);
+        float sdir[3], tdir[3], nsum[3], nn[3];
+        for (int k = 0; k < 3; k++) {
+            sdir[k] = (dv2 * e1[k] - dv1 * e2[k]) * r;
+            tdir[k] = (du1 * e2[k] - du2 * e1[k]) * r;
+            nsum[k] = n[0][k] + n[1][k] + n[2][k];
+        }
+        Normalize3(nsum, nn);
+        const float ns = nn[0] * sdir[0] + nn[1] * sdir[1] + nn[2] * sdir[2];
+        const float tg0[3] = { sdir[0] - nn[0] * ns, sdir[1] - nn[1] * ns, sdir[2] - nn[2] * ns };
+        float tg[3];
+        Normalize3(tg0, tg);
+        const float cr[3] = { tg[1] * nn[2] - tg[2] * nn[1], tg[2] * nn[0] - tg[0] * nn[2], tg[0] * nn[1] - tg[1] * nn[0] };
+        const float hand = (cr[0] * tdir[0] + cr[1] * tdir[1] + cr[2] * tdir[2]) < 0.0f ? 1.0f : -1.0f;
+        float bt[3];
+        Normalize3(cr, bt);
+        for (int k = 0; k < 3; k++) bt[k] *= hand;
+        inout[i].d1[0] = Bits(PackSigned10(tg[0], tg[1], tg[2], 0.0f));
+        inout[i].d1[1] = Bits(PackSigned10(bt[0], bt[1], bt[2], 0.0f));
+        if (colors) {
+            for (int k = 0; k < 3; k++) inout[i].d2[k] = Bits(int32_t(PackUnorm4(colors + size_t(src) * 12 + 4 * k)));
         }
     }
     return AE_RT_OK;

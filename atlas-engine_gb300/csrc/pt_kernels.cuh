@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "cast_kernels.cuh"
+#include "texture.cuh"
 
 namespace atlas::rt::dev {
 
@@ -46,6 +47,7 @@ struct PtScene {
     uint32_t n_materials;
     const float4* lights;         // GPULight (4 float4)
     uint32_t n_lights;
+    TexTable tex;                 // the scene's textures (texture.cuh)
 };
 
 struct PtParams {
@@ -114,8 +116,9 @@ __device__ __forceinline__ float rng(uint32_t pixel, uint32_t sample, uint32_t b
 
 struct Mat {
     V3 base, emissive;
-    float opacity, roughness, metalness, ao, reflectance;
-    int twoSided, cullBackFaces;
+    float opacity, roughness, metalness, ao, reflectance, normalScale;
+    int twoSided, cullBackFaces, invertUVs, useVertexColors;
+    int baseTex, opacityTex, normalTex, roughTex, metalTex, aoTex;
 };
 
 __device__ __forceinline__ Mat load_material(const float* m) {
@@ -127,8 +130,17 @@ __device__ __forceinline__ Mat load_material(const float* m) {
     r.metalness = m[9];
     r.ao = m[10];
     r.reflectance = m[11];
+    r.normalScale = m[12];
+    r.invertUVs = __float_as_int(m[13]);
     r.twoSided = __float_as_int(m[14]);
     r.cullBackFaces = __float_as_int(m[15]);
+    r.useVertexColors = __float_as_int(m[16]);
+    r.baseTex = __float_as_int(m[17]);
+    r.opacityTex = __float_as_int(m[18]);
+    r.normalTex = __float_as_int(m[19]);
+    r.roughTex = __float_as_int(m[20]);
+    r.metalTex = __float_as_int(m[21]);
+    r.aoTex = __float_as_int(m[22]);
     return r;
 }
 
@@ -358,6 +370,59 @@ __device__ __forceinline__ uint32_t queue_capacity(const PtParams& p) {
 // GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit:
 // position, interpolated shading normal, geometric normal (both flipped
 // towards the ray on two-sided materials), material.
+// unpackUnorm4x8 (one vertex colour of GPUTriangle d2)
+__device__ __forceinline__ float4 unpack_unorm4(float bits) {
+    const uint32_t c = __float_as_uint(bits);
+    return make_float4(float(c & 255u) / 255.0f, float((c >> 8) & 255u) / 255.0f, float((c >> 16) & 255u) / 255.0f,
+                       float(c >> 24) / 255.0f);
+}
+
+// The material terms of GetSurfaceParameters (surface.hsh:83-124) at the
+// hit's barycentrics: vertex colours, base colour / opacity / roughness /
+// metalness / ao textures and the normal map, all at texture level 0 (the
+// path tracer's level, rayHit.csh:177).  N is the interpolated normal (in and
+// out).
+__device__ __forceinline__ void surface_textures(const PtScene& sc, int32_t inst, int32_t triPtr, float r, float s,
+                                                 float t, Mat& mat, V3& N) {
+    const float4* ip = sc.instances + size_t(inst) * 4;
+    const MeshDesc m = sc.meshes[__float_as_int(__ldg(ip + 3).x)];
+    const float4* tp = m.shading + size_t(triPtr) * 6;
+    const float4 d0 = __ldg(tp + 3), d1 = __ldg(tp + 4), d2 = __ldg(tp + 5);
+    const float2 uv0 = unpack_half2(d0.x), uv1 = unpack_half2(d0.y), uv2 = unpack_half2(d0.z);
+    const float tu = r * uv0.x + s * uv1.x + t * uv2.x;
+    float tv = r * uv0.y + s * uv1.y + t * uv2.y;
+    if (mat.invertUVs > 0) tv = 1.0f - tv;
+    if (mat.useVertexColors > 0) {
+        const float4 c0 = unpack_unorm4(d2.x), c1 = unpack_unorm4(d2.y), c2 = unpack_unorm4(d2.z);
+        mat.base = mat.base * v3(r * c0.x + s * c1.x + t * c2.x, r * c0.y + s * c1.y + t * c2.y,
+                                 r * c0.z + s * c1.z + t * c2.z);
+    }
+    const float4 bc = sample_rgba_bilinear(sc.tex, mat.baseTex, tu, tv);
+    mat.base = mat.base * v3(bc.x, bc.y, bc.z);
+    mat.opacity *= sample_r_bilinear(sc.tex, mat.opacityTex, tu, tv);
+    mat.roughness *= sample_r_bilinear(sc.tex, mat.roughTex, tu, tv);
+    mat.metalness *= sample_r_bilinear(sc.tex, mat.metalTex, tu, tv);
+    mat.ao *= sample_r_bilinear(sc.tex, mat.aoTex, tu, tv);
+    if (mat.normalTex >= 0) {
+        // TBN = (tangent, +-bitangent, normal) in world space (TransformTriangle)
+        const float4* M = sc.inst_model + size_t(inst) * 3;
+        float4 mm[3] = { __ldg(M), __ldg(M + 1), __ldg(M + 2) };
+        const V3 T = normalize(xform_dir(mm, unpack_unit(d1.x)));
+        V3 B = normalize(xform_dir(mm, unpack_unit(d1.y)));
+        if (!(mat.invertUVs > 0)) B = B * -1.0f;
+        const float4 tn = sample_rgba_bilinear(sc.tex, mat.normalTex, tu, tv);
+        V3 n = T * (2.0f * tn.x - 1.0f) + B * (2.0f * tn.y - 1.0f) + N * (2.0f * tn.z - 1.0f);
+        n = n * (1.0f / fmaxf(sqrtf(dot(n, n)), 0.00001f));
+        const float w = saturate(mat.normalScale);
+        N = N * (1.0f - w) + n * w;
+    }
+}
+
+__device__ __forceinline__ bool has_surface_textures(const Mat& m) {
+    // some index is >= 0 exactly when the AND of all of them has its sign bit clear
+    return m.useVertexColors > 0 || (m.baseTex & m.opacityTex & m.normalTex & m.roughTex & m.metalTex & m.aoTex) >= 0;
+}
+
 __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, float t, int32_t inst, int32_t triPtr,
                                              float bu, float bv) {
     const Tri tri = load_triangle(sc, inst, triPtr);
@@ -370,6 +435,7 @@ __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, fl
     const bool flip = dot(triN, rd) > 0.0f;
     sf.backface = sf.mat.twoSided > 0 || sf.mat.cullBackFaces == 0 ? false : flip;
     if (flip && sf.mat.twoSided > 0) triN = triN * -1.0f;
+    if (has_surface_textures(sf.mat)) surface_textures(sc, inst, triPtr, r, bu, bv, sf.mat, N);
     if (dot(N, triN) < 0.0f && sf.mat.twoSided > 0) N = N * -1.0f;
     sf.V = rd * -1.0f;
     sf.N = normalize(N);

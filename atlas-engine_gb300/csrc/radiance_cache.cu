@@ -191,6 +191,9 @@ ae_rt_status GeneratePaths(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint
     pp.sc.n_materials = ctx->n_materials;
     pp.sc.lights = ctx->d_lights;
     pp.sc.n_lights = ctx->n_lights;
+    pp.sc.tex.pool = ctx->d_tex_pool;
+    pp.sc.tex.desc = static_cast<const atlas::rt::dev::TexDesc*>(ctx->d_tex_desc);
+    pp.sc.tex.n = ctx->n_textures;
     pp.cam = CamParams(cam);
     pp.n_paths = n_paths;
     pp.frame = frame;
@@ -262,6 +265,9 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     p.sc.n_materials = ctx->n_materials;
     p.sc.lights = ctx->d_lights;
     p.sc.n_lights = ctx->n_lights;
+    p.sc.tex.pool = ctx->d_tex_pool;
+    p.sc.tex.desc = static_cast<const atlas::rt::dev::TexDesc*>(ctx->d_tex_desc);
+    p.sc.tex.n = ctx->n_textures;
     p.width = cam->width;
     p.height = cam->height;
     p.max_bounces = rc->max_bounces;

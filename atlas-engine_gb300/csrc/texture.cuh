@@ -68,6 +68,45 @@ __device__ __forceinline__ float sample_r_bilinear(const TexTable& tt, int32_t i
     return __fadd_rn(r, __fmul_rn(__fmul_rn(a, b), c11));
 }
 
+// All four channels of texel (x, y) as the sampler returns them: R8 gives
+// (r, 0, 0, 1), RGBA8 (r, g, b, a), R32F (r, 0, 0, 1).
+__device__ __forceinline__ float4 texel_rgba(const TexTable& tt, const TexDesc& t, uint32_t x, uint32_t y) {
+    const uint8_t* row = tt.pool + t.offset + size_t(y) * t.row_pitch;
+    if (t.format == 0u) return make_float4(__fdiv_rn(float(__ldg(row + x)), 255.0f), 0.0f, 0.0f, 1.0f);
+    if (t.format == 1u) {
+        const uchar4 c = __ldg(reinterpret_cast<const uchar4*>(row) + x);
+        return make_float4(__fdiv_rn(float(c.x), 255.0f), __fdiv_rn(float(c.y), 255.0f),
+                           __fdiv_rn(float(c.z), 255.0f), __fdiv_rn(float(c.w), 255.0f));
+    }
+    return make_float4(__ldg(reinterpret_cast<const float*>(row) + x), 0.0f, 0.0f, 1.0f);
+}
+
+__device__ __forceinline__ float bilerp(float ia, float ib, float a, float b, float c00, float c10, float c01,
+                                        float c11) {
+    float r = __fmul_rn(__fmul_rn(ia, ib), c00);
+    r = __fadd_rn(r, __fmul_rn(__fmul_rn(a, ib), c10));
+    r = __fadd_rn(r, __fmul_rn(__fmul_rn(ia, b), c01));
+    return __fadd_rn(r, __fmul_rn(__fmul_rn(a, b), c11));
+}
+
+// textureLod(sampler2D(bindlessTextures[id], bindlessSampler), uv, 0) with
+// every channel filtered as sample_r_bilinear filters the first; (1, 1, 1, 1)
+// for a negative or out-of-range id (SampleBaseColorBilinear and friends,
+// texture.hsh:9-60).
+__device__ __forceinline__ float4 sample_rgba_bilinear(const TexTable& tt, int32_t id, float u, float v) {
+    if (id < 0 || uint32_t(id) >= tt.n) return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    const TexDesc t = tt.desc[id];
+    uint32_t x0, x1, y0, y1;
+    float a, b;
+    tex_axis(u, t.width, x0, x1, a);
+    tex_axis(v, t.height, y0, y1, b);
+    const float4 c00 = texel_rgba(tt, t, x0, y0), c10 = texel_rgba(tt, t, x1, y0);
+    const float4 c01 = texel_rgba(tt, t, x0, y1), c11 = texel_rgba(tt, t, x1, y1);
+    const float ia = __fsub_rn(1.0f, a), ib = __fsub_rn(1.0f, b);
+    return make_float4(bilerp(ia, ib, a, b, c00.x, c10.x, c01.x, c11.x), bilerp(ia, ib, a, b, c00.y, c10.y, c01.y, c11.y),
+                       bilerp(ia, ib, a, b, c00.z, c10.z, c01.z, c11.z), bilerp(ia, ib, a, b, c00.w, c10.w, c01.w, c11.w));
+}
+
 __device__ __forceinline__ float2 unpack_half2(float bits) {
     const uint32_t u = __float_as_uint(bits);
     return make_float2(__half2float(__ushort_as_half(uint16_t(u & 0xFFFFu))),

@@ -215,6 +215,18 @@ ae_rt_status ae_bvh_pack_shading(const ae_bvh* bvh, const float* verts, const fl
  * GPUTriangle array in BVH order that ae_bvh_pack_shading filled. */
 ae_rt_status ae_bvh_pack_uvs(const ae_bvh* bvh, const float* uvs, ae_triangle* inout);
 
+/* The rest of MeshData's GPUTriangle packing (MeshData.cpp:172-239) for
+ * meshes with texture coordinates: UVs into d0.xyz as ae_bvh_pack_uvs; the
+ * tangent frame from the UVs into d1.xy (tangent = the UV-space s direction
+ * made orthogonal to the normalised vertex-normal sum, bitangent = +-
+ * normalize(cross(tangent, normal)) by the handedness of the t direction,
+ * both packed 10:10:10:2); vertex colours (optional, n * 12 floats, RGBA per
+ * vertex) into d2.xyz as packUnorm4x8.  normals: n * 9 floats per vertex, or
+ * NULL for the face normal.  `inout` is the GPUTriangle array in BVH order
+ * that ae_bvh_pack_shading filled. */
+ae_rt_status ae_bvh_pack_attributes(const ae_bvh* bvh, const float* verts, const float* normals, const float* uvs,
+                                    const float* colors, ae_triangle* inout);
+
 /* ------------------------------------------------------------------------ */
 /* Device context                                                            */
 /* ------------------------------------------------------------------------ */

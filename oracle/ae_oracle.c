@@ -992,6 +992,7 @@ typedef struct {
     const float* materials;
     const float* lights;
     uint32_t n_lights;
+    const aeo_texture* textures; uint32_t n_textures;   /* surface textures (GetSurfaceParameters) */
     const float* cam;
     uint32_t width, height, spp, sample_offset, max_bounces, seed;
     float epsilon;
@@ -1027,8 +1028,100 @@ static pt_mat pt_load_mat(const float* m) {
     return r;
 }
 
-/* GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit,
- * without textures or normal maps; returns backfaceHit (surface.hsh:99). */
+/* All four channels of a texel as the sampler returns them: R8 (r, 0, 0, 1),
+ * RGBA8 (r, g, b, a), R32F (r, 0, 0, 1). */
+static void texel_rgba(const aeo_texture* t, uint32_t x, uint32_t y, float c[4]) {
+    const uint32_t texel = t->format == 0 ? 1u : 4u;
+    const uint32_t pitch = t->row_pitch ? t->row_pitch : t->width * texel;
+    const uint8_t* row = (const uint8_t*)t->texels + (size_t)y * pitch;
+    c[1] = c[2] = 0.0f;
+    c[3] = 1.0f;
+    if (t->format == 0) {
+        c[0] = (float)row[x] / 255.0f;
+    } else if (t->format == 1) {
+        for (int k = 0; k < 4; k++) c[k] = (float)row[(size_t)x * 4 + k] / 255.0f;
+    } else {
+        memcpy(&c[0], row + (size_t)x * 4, 4);
+    }
+}
+
+/* textureLod(...) with all channels filtered like aeo_sample_r_bilinear's
+ * first; (1, 1, 1, 1) for a negative or out-of-range id (texture.hsh:9-60). */
+static void sample_rgba_bilinear(const aeo_texture* textures, uint32_t n_textures, int32_t id, float u, float v,
+                                 float out[4]) {
+    if (id < 0 || (uint32_t)id >= n_textures) {
+        out[0] = out[1] = out[2] = out[3] = 1.0f;
+        return;
+    }
+    const aeo_texture* t = &textures[id];
+    uint32_t x0, x1, y0, y1;
+    float a, b;
+    tex_axis(u, t->width, &x0, &x1, &a);
+    tex_axis(v, t->height, &y0, &y1, &b);
+    float c00[4], c10[4], c01[4], c11[4];
+    texel_rgba(t, x0, y0, c00);
+    texel_rgba(t, x1, y0, c10);
+    texel_rgba(t, x0, y1, c01);
+    texel_rgba(t, x1, y1, c11);
+    const float ia = 1.0f - a, ib = 1.0f - b;
+    for (int k = 0; k < 4; k++) {
+        float r = (ia * ib) * c00[k];
+        r = r + (a * ib) * c10[k];
+        r = r + (ia * b) * c01[k];
+        out[k] = r + (a * b) * c11[k];
+    }
+}
+
+static float unorm8(uint32_t c, int k) { return (float)((c >> (8 * k)) & 255u) / 255.0f; }
+
+/* The material terms of GetSurfaceParameters (surface.hsh:83-124) at
+ * barycentrics (r, s, t): vertex colours, base colour / opacity / roughness /
+ * metalness / ao textures and the normal map, level 0.  N: the interpolated
+ * normal, in and out. */
+static void pt_surface_textures(const pt_job_t* j, int32_t inst, int32_t tp, const float* mw, float r, float s,
+                                float t, pt_mat* m, v3* N) {
+    const aeo_instance* in = &j->sc.inst[inst];
+    const float* g = j->sc.meshes[in->meshOffset].shading + (size_t)tp * 24;
+    float u0, v0, u1, v1, u2, v2;
+    half2_of(g[12], &u0, &v0);
+    half2_of(g[13], &u1, &v1);
+    half2_of(g[14], &u2, &v2);
+    int32_t w[23];
+    memcpy(w, mw, sizeof w);
+    const float tu = r * u0 + s * u1 + t * u2;
+    float tv = r * v0 + s * v1 + t * v2;
+    if (w[13] > 0) tv = 1.0f - tv;
+    if (w[16] > 0) {
+        uint32_t c0, c1, c2;
+        memcpy(&c0, &g[20], 4);
+        memcpy(&c1, &g[21], 4);
+        memcpy(&c2, &g[22], 4);
+        m->base = vmulv(m->base, mk(r * unorm8(c0, 0) + s * unorm8(c1, 0) + t * unorm8(c2, 0),
+                                    r * unorm8(c0, 1) + s * unorm8(c1, 1) + t * unorm8(c2, 1),
+                                    r * unorm8(c0, 2) + s * unorm8(c1, 2) + t * unorm8(c2, 2)));
+    }
+    float c[4];
+    sample_rgba_bilinear(j->textures, j->n_textures, w[17], tu, tv, c);
+    m->base = vmulv(m->base, mk(c[0], c[1], c[2]));
+    m->opacity *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[18], tu, tv);
+    m->roughness *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[20], tu, tv);
+    m->metalness *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[21], tu, tv);
+    m->ao *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[22], tu, tv);
+    if (w[19] >= 0) {
+        const float* mm = j->inst_model + (size_t)inst * 12;
+        v3 T = vnorm(xdir(mm, unpack10(g[16])));
+        v3 B = vnorm(xdir(mm, unpack10(g[17])));
+        if (!(w[13] > 0)) B = vmul(B, -1.0f);
+        sample_rgba_bilinear(j->textures, j->n_textures, w[19], tu, tv, c);
+        v3 n = vadd(vadd(vmul(T, 2.0f * c[0] - 1.0f), vmul(B, 2.0f * c[1] - 1.0f)), vmul(*N, 2.0f * c[2] - 1.0f));
+        n = vmul(n, 1.0f / fmaxf(sqrtf(vdot(n, n)), 0.00001f));
+        const float wgt = sat(mw[12]);
+        *N = vadd(vmul(*N, 1.0f - wgt), vmul(n, wgt));
+    }
+}
+
+/* GetSurfaceParameters (raytracer/surface.hsh:63-140) at a closest hit;
+ * returns backfaceHit (surface.hsh:99). */
 static int pt_make_surface(const pt_job_t* j, v3 ro, v3 rd, int32_t tp, int32_t ino, const float* tuv,
                            pt_surf* sf) {
     pt_tri tri = pt_load_tri(j, ino, tp);
@@ -1043,6 +1136,12 @@ static int pt_make_surface(const pt_job_t* j, v3 ro, v3 rd, int32_t tp, int32_t 
     memcpy(&cull, &mw[15], 4);
     int backface = sf->m.twoSided > 0 || cull == 0 ? 0 : flip;
     if (flip && sf->m.twoSided > 0) triN = vmul(triN, -1.0f);
+    {
+        int32_t w[23];
+        memcpy(w, mw, sizeof w);
+        if (w[16] > 0 || (w[17] & w[18] & w[19] & w[20] & w[21] & w[22]) >= 0)
+            pt_surface_textures(j, ino, tp, mw, r, s, t, &sf->m, &N);
+    }
     if (vdot(N, triN) < 0.0f && sf->m.twoSided > 0) N = vmul(N, -1.0f);
     sf->V = vmul(rd, -1.0f);
     sf->N = vnorm(N);
@@ -1190,7 +1289,8 @@ static void* run_pt_job(void* arg) {
 
 void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
                    uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
-                   const float* lights, uint32_t n_lights, const float* cam, uint32_t width, uint32_t height,
+                   const float* lights, uint32_t n_lights, const aeo_texture* textures, uint32_t n_textures,
+                   const float* cam, uint32_t width, uint32_t height,
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum) {
     pt_job_t proto;
@@ -1201,6 +1301,8 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
     proto.materials = materials;
     proto.lights = lights;
     proto.n_lights = n_lights;
+    proto.textures = textures;
+    proto.n_textures = n_textures;
     proto.cam = cam;
     proto.width = width; proto.height = height; proto.spp = spp; proto.sample_offset = sample_offset;
     proto.max_bounces = max_bounces; proto.seed = seed; proto.epsilon = epsilon;
@@ -1494,6 +1596,8 @@ static void run_pass(const aeo_pass_scene* s, int kind, const aeo_gbuffer* gb, c
     proto.j.materials = s->materials;
     proto.j.lights = s->lights;
     proto.j.n_lights = s->n_lights;
+    proto.j.textures = s->textures;
+    proto.j.n_textures = s->n_textures;
     proto.j.epsilon = PASS_EPS;
     proto.j.stack_cap = scene_stack_cap(&sc);
     proto.tsc = tsc;

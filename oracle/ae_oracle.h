@@ -93,18 +93,6 @@ void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instanc
                         const aeo_mesh* meshes, uint32_t n_meshes, const float* rays, uint32_t n_rays,
                         uint32_t cull_mask, int threads, uint8_t* occluded);
 
-/* Path tracer -- the restatement of the engine's non-real-time estimator
- * (pathtracer/rayGen.csh, rayHit.csh, raytracer/direct.hsh, lights.hsh,
- * brdf/*.hsh) without the indirect radiance clamp, accumulating every sample's
- * radiance in double precision.  materials: GPUMaterial (23 words), lights:
- * GPULight (16 floats), inst_model: object-to-world 3x4 rows per instance.
- * cam: location[3], origin[3], right[3], bottom[3].  accum: w * h * 3. */
-void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
-                   uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
-                   const float* lights, uint32_t n_lights, const float* cam, uint32_t width, uint32_t height,
-                   uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
-                   int threads, double* accum);
-
 /* One texture's level 0 (the layout of the library's ae_texture): `height`
  * rows of `row_pitch` bytes (0 = tight); format 0 = R8 UNORM, 1 = RGBA8
  * UNORM, 2 = R32 float; the first channel is sampled. */
@@ -112,6 +100,22 @@ typedef struct aeo_texture {
     const void* texels;
     uint32_t width, height, format, row_pitch;
 } aeo_texture;
+
+/* Path tracer -- the restatement of the engine's non-real-time estimator
+ * (pathtracer/rayGen.csh, rayHit.csh, raytracer/direct.hsh, lights.hsh,
+ * brdf/*.hsh) without the indirect radiance clamp, accumulating every sample's
+ * radiance in double precision.  materials: GPUMaterial (23 words), lights:
+ * GPULight (16 floats), inst_model: object-to-world 3x4 rows per instance,
+ * textures: the materials' texture table (vertex colours, base colour,
+ * opacity, roughness, metalness, ao, normal maps at level 0).
+ * cam: location[3], origin[3], right[3], bottom[3].  accum: w * h * 3. */
+void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
+                   uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
+                   const float* lights, uint32_t n_lights, const aeo_texture* textures, uint32_t n_textures,
+                   const float* cam, uint32_t width, uint32_t height,
+                   uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
+                   int threads, double* accum);
+
 
 /* textureLod(sampler2D(bindlessTextures[id], bindlessSampler), (u, v), 0).r
  * (texture.hsh:18-25) with the engine's bindless sampler (linear filter,

@@ -60,7 +60,7 @@ def port():
         L.aeo_scene_closest_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P, P, P, P, P]
         L.aeo_scene_any_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P]
         L.aeo_scene_closest_glsl.restype = None
-        L.aeo_pathtrace.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, U32, U32, U32, U32, U32,
+        L.aeo_pathtrace.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U32,
                                     C.c_float, C.c_int, P]
         L.aeo_pathtrace.restype = None
         L.aeo_scene_any_glsl.restype = None
@@ -314,7 +314,8 @@ def scene_any_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, c
 
 
 def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, width, height, spp,
-              sample_offset=0, max_bounces=3, seed=1, epsilon=0.1, threads=os.cpu_count(), accum=None):
+              sample_offset=0, max_bounces=3, seed=1, epsilon=0.1, threads=os.cpu_count(), accum=None,
+              textures=None):
     """CPU restatement of the path tracer; returns the summed radiance
     (height, width, 3) float64 over spp samples (add to `accum` if given)."""
     tlas_f32 = _c(tlas_f32, np.float32)
@@ -325,9 +326,11 @@ def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, w
     cam = _c(cam, np.float32)
     table, keep = _mesh_table(meshes)
     out = np.zeros((height, width, 3), np.float64) if accum is None else accum
+    ttab, ntex, tkeep = _texture_table(textures)
     port().aeo_pathtrace(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst),
-                         table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), cam.ctypes.data,
-                         width, height, spp, sample_offset, max_bounces, seed, epsilon, threads, out.ctypes.data)
+                         table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), ttab, ntex,
+                         cam.ctypes.data, width, height, spp, sample_offset, max_bounces, seed, epsilon, threads,
+                         out.ctypes.data)
     return out
 
 

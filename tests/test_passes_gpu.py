@@ -240,3 +240,26 @@ def test_texture_argument_errors(sand_ctx):
     with pytest.raises(atlas_rt.AeRtError):
         ctx.set_textures([np.zeros((0, 4), np.uint8)])        # empty texture
     ctx.set_textures([])                                       # clears the table
+
+
+@pytest.mark.parametrize("kind", ["reflections", "rtgi"])
+def test_shading_passes_textured_match_oracle(kind):
+    """The passes shade hits with the full material model too."""
+    import textured_util
+    ctx = atlas_rt.Context(device=0)
+    try:
+        sc, gt, sh, tex = textured_util.build()
+        textured_util.upload(ctx, sc, gt, sh, tex)
+        osc, _ = textured_util.oracle_scene(sc, gt, sh)
+        s = {"oracle": osc, "shading": sh}
+        rng = np.random.default_rng(12)
+        rough = rng.uniform(0.0, 0.9, (90, 160)).astype(np.float32)
+        gb = gbuffer(s, 160, 90, roughness=rough, samples=True)
+        params = dict(radiance_limit=4.0, roughness_cutoff=0.8, environment=(0.05, 0.1, 0.2), frame_seed=4, seed=5)
+        got = run(ctx, kind, gb, **params)
+        ref = pyoracle.pass_screen(kind, osc + (tex,), gb, **params)
+        close = np.all(np.abs(got[..., :3] - ref[..., :3]) <= 1e-3 * np.abs(ref[..., :3]) + 1e-5, axis=2)
+        assert close.mean() > 0.97, close.mean()
+        np.testing.assert_allclose(got[..., :3].mean(), ref[..., :3].mean(), rtol=0.02)
+    finally:
+        ctx.close()

@@ -113,3 +113,29 @@ def test_pt_mis_same_image(pt_setup):
     e_plain = ptscene.rel_mse(plain64 / 64, ref)
     e_mis = ptscene.rel_mse(mis64 / 64, ref)
     assert e_mis < 1.2 * e_plain, (e_mis, e_plain)
+
+
+def test_pt_textured_matches_cpu_restatement():
+    """The material model of GetSurfaceParameters (vertex colours, base
+    colour / roughness / metalness / ao textures, normal maps) on the GPU
+    against the oracle's restatement, statistically, as the untextured test."""
+    import textured_util
+    ctx = atlas_rt.Context(device=0)
+    try:
+        sc, gt, sh, tex = textured_util.build()
+        textured_util.upload(ctx, sc, gt, sh, tex)
+        osc, _ = textured_util.oracle_scene(sc, gt, sh)
+        w, h, spp = 64, 36, 2048
+        _, g64 = gpu_render(ctx, w, h, spp, accum64=True)
+        camd = scenes.pinhole_camera(w, h)
+        camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(np.float32)
+        c = pyoracle.pathtrace(*osc, camv, w, h, spp, textures=tex)
+        g64, c = g64 / spp, c / spp
+        assert abs(g64.mean() - c.mean()) / c.mean() < 0.01, (g64.mean(), c.mean())
+        gb = g64.reshape(h // 4, 4, w // 4, 4, 3).mean(axis=(1, 3))
+        cb = c.reshape(h // 4, 4, w // 4, 4, 3).mean(axis=(1, 3))
+        bad = np.abs(gb - cb) > np.maximum(0.05 * cb, 3e-4)
+        assert bad.mean() < 0.01, f"{bad.sum()} of {bad.size} blocks differ"
+        assert ptscene.rel_mse(g64, c) < 1e-4
+    finally:
+        ctx.close()

@@ -159,3 +159,61 @@ def test_textured_quad_opacity(invert):
     # without the texture the material's opacity alone counts: every ray hits
     ptr, _, _ = pyoracle.scene_closest_transparency_glsl(top.nodes_f32, inst, meshes, mats, rays8)
     assert np.all(ptr >= 0)
+
+
+def test_attribute_packing_tangent_frame_and_colours():
+    """ae_bvh_pack_attributes: the UV-derived tangent frame (MeshData.cpp:
+    176-197) against a float64 restatement, vertex colours as packUnorm4x8."""
+    rng = np.random.default_rng(9)
+    tris = scenes.terrain_boxes(seed=4, grid=16, extent=4.0, n_boxes=2)[0]
+    n = len(tris)
+    b = BVH(tris)
+    sh = b.pack_shading()
+    uv = rng.uniform(-1, 1, (n, 6)).astype(np.float32)
+    col = rng.uniform(-0.2, 1.2, (n, 12)).astype(np.float32)
+    b.pack_attributes(sh, uv, None, col)
+    src = b.order
+    t = tris[src].astype(np.float64)
+    u = uv[src].astype(np.float64)
+    e1, e2 = t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]
+    du1, dv1, du2, dv2 = u[:, 2] - u[:, 0], u[:, 3] - u[:, 1], u[:, 4] - u[:, 0], u[:, 5] - u[:, 1]
+    r = 1.0 / (du1 * dv2 - du2 * dv1)
+    sdir = (dv2[:, None] * e1 - dv1[:, None] * e2) * r[:, None]
+    tdir = (du1[:, None] * e2 - du2[:, None] * e1) * r[:, None]
+    nrm = np.cross(e1, e2)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    tg = sdir - nrm * (nrm * sdir).sum(1, keepdims=True)
+    tg /= np.linalg.norm(tg, axis=1, keepdims=True)
+    cr = np.cross(tg, nrm)
+    hand = np.where((cr * tdir).sum(1) < 0, 1.0, -1.0)
+    bt = hand[:, None] * cr / np.linalg.norm(cr, axis=1, keepdims=True)
+
+    def unpack10(bits):
+        c = bits.view(np.int32)
+        return np.stack([((c >> s) & 1023) / 1023.0 * 2.0 - 1.0 for s in (0, 10, 20)], axis=1)
+
+    ok = np.abs(r) < 1e4          # well-conditioned UV triangles
+    np.testing.assert_allclose(unpack10(sh[:, 16].copy())[ok], tg[ok], atol=4e-3)
+    np.testing.assert_allclose(unpack10(sh[:, 17].copy())[ok], bt[ok], atol=4e-3)
+    packed = sh[:, 20:23].copy().view(np.uint32)
+    want = np.round(np.clip(col[src].reshape(-1, 3, 4), 0, 1) * 255).astype(np.uint32)
+    want = want[..., 0] | (want[..., 1] << 8) | (want[..., 2] << 16) | (want[..., 3] << 24)
+    np.testing.assert_array_equal(packed, want)
+
+
+def test_textured_oracle_image_differs_from_plain():
+    """The material textures reach the oracle's shading: a textured render
+    differs from the same scene with the texture indices cleared."""
+    from textured_util import build, oracle_scene
+    sc, gt, sh, tex = build(grid=24, n_boxes=4)
+    osc, _ = oracle_scene(sc, gt, sh)
+    cam = scenes.pinhole_camera(32, 18)
+    camv = np.concatenate([cam["location"], cam["origin"], cam["right"], cam["bottom"]]).astype(np.float32)
+    a = pyoracle.pathtrace(*osc, camv, 32, 18, 16, textures=tex)
+    plain = osc[4].copy()
+    for t in ("baseColorTexture", "roughnessTexture", "metalnessTexture", "aoTexture", "normalTexture"):
+        plain[t] = -1
+    plain["useVertexColors"] = 0
+    b = pyoracle.pathtrace(*osc[:4], plain, osc[5], camv, 32, 18, 16, textures=tex)
+    assert np.isfinite(a).all() and a.mean() > 0
+    assert abs(a.mean() - b.mean()) / b.mean() > 0.05
