@@ -626,6 +626,13 @@ class RadianceCache:
                                  C.byref(loss) if want_loss else None, _stream_handle(stream)), self.ctx.handle)
         return loss.value if want_loss else None
 
+    def selftest_wait_timeout(self) -> bool:
+        """ae_rc_selftest_wait_timeout: True when the tensor-memory kernel's
+        bounded wait ran out and was reported as a timeout."""
+        t = C.c_uint32()
+        _check(lib().ae_rc_selftest_wait_timeout(self._h, C.byref(t)), self.ctx.handle)
+        return bool(t.value)
+
     def render(self, cam: Camera, frame: int, accum, last_bounce=2, stream=None):
         _check(lib().ae_rc_render(self._h, C.byref(cam), frame, last_bounce, _ptr(accum), _stream_handle(stream)),
                self.ctx.handle)

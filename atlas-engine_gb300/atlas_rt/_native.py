@@ -130,6 +130,7 @@ _SIGNATURES = [
     ("ae_rc_get_params", C.c_int, [P, P, P]),
     ("ae_rc_set_params", C.c_int, [P, P, P]),
     ("ae_rc_predict", C.c_int, [P, P, U32, P, P]),
+    ("ae_rc_selftest_wait_timeout", C.c_int, [P, C.POINTER(U32)]),
     ("ae_rc_gradients", C.c_int, [P, P, U32, P, P, C.POINTER(F32), P]),
     ("ae_rc_train_batch", C.c_int, [P, P, U32, C.POINTER(F32), P]),
     ("ae_rc_train_frame", C.c_int, [P, C.POINTER(Camera), U32, U32, U32, U32, C.POINTER(F32), P]),

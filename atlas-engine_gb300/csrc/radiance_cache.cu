@@ -497,6 +497,32 @@ ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* o
     return AE_RT_OK;
 }
 
+ae_rt_status ae_rc_selftest_wait_timeout(ae_rc* rc, uint32_t* timed_out) {
+    if (!rc || !timed_out) return AE_RT_INVALID_ARG;
+    *timed_out = 0;
+    RC_CUDA(rc, cudaSetDevice(rc->ctx->device));
+    ae_rt_status st = ae_rt_synchronize(rc->ctx, nullptr);   // start from a clean error word
+    if (st != AE_RT_OK) return st;
+    RC_CUDA(rc, rc->queries.ensure(size_t(RCT_THREADS) * 64));
+    RC_CUDA(rc, cudaMemset(rc->queries.ptr, 0, size_t(RCT_THREADS) * 64));
+    float4* out = nullptr;
+    RC_CUDA(rc, cudaMalloc(&out, size_t(RCT_THREADS) * sizeof(float4)));
+    RcMlpParams p = MlpParams(rc);
+    p.recs = static_cast<const float4*>(rc->queries.ptr);
+    p.n = RCT_THREADS;
+    p.out = out;
+    p.skip_mma = 1;
+    rc_infer_tc_kernel<RC_PREDICT><<<1, RCT_THREADS, RCT_SMEM>>>(p);
+    cudaError_t e = cudaGetLastError();
+    st = e == cudaSuccess ? ae_rt_synchronize(rc->ctx, nullptr) : CudaFail(rc->ctx, e, "self-test launch");
+    cudaFree(out);
+    if (st == AE_RT_TIMEOUT) {
+        *timed_out = 1;
+        return AE_RT_OK;
+    }
+    return st;
+}
+
 ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float* grad_mlp, float* grad_grid,
                              float* loss_out, void* stream) {
     if (!rc) return AE_RT_INVALID_ARG;

@@ -301,6 +301,7 @@ struct RcMlpParams {
     float4* out;                     // RC_PREDICT
     float* loss;                     // RC_TRAIN: mean per-element loss (accumulated)
     uint32_t* error_word;            // tensor-memory kernels: a bounded wait that gave up
+    uint32_t skip_mma;               // self-test only: issue no MMA, so every wait runs out
 };
 
 // Training (fused encode + forward + relative-L2 loss + backward with weight

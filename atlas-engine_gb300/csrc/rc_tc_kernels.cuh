@@ -84,10 +84,11 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// Waits for the mbarrier phase with parity `parity`; false after ~200 ms.
+// Waits for the mbarrier phase with parity `parity`; false after ~200 ms of
+// the global timer, or after 2^25 polls whatever the timer says.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     const uint64_t start = global_ns();
-    for (uint32_t it = 0;; it++) {
+    for (uint32_t it = 0; it < (1u << 25); it++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -96,6 +97,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
         if (done) return true;
         if ((it & 63u) == 63u && global_ns() - start > 200000000ull) return false;
     }
+    return false;
 }
 
 // Barrier of one 128-thread tile group (named barrier 1 + group).
@@ -217,7 +219,7 @@ static __global__ void __launch_bounds__(RCT_THREADS) rc_infer_tc_kernel(RcMlpPa
 #pragma unroll 1
         for (int l = 0; l <= RC_HIDDEN; l++) {
             const uint32_t nn = l < RC_HIDDEN ? uint32_t(RC_W) : uint32_t(RC_OUT);
-            if (row == 0) {
+            if (row == 0 && !p.skip_mma) {
                 const uint32_t idesc = rct_idesc(RC_TILE, nn);
 #pragma unroll
                 for (uint32_t s = 0; s < 4; s++)

@@ -698,6 +698,14 @@ ae_rt_status ae_rc_set_params(ae_rc* rc, const float* mlp, const float* grid);
 /* Predictions for n query records (device buffers; out: 4 floats each). */
 ae_rt_status ae_rc_predict(ae_rc* rc, const float* queries, uint32_t n, float* out, void* stream);
 
+/* Diagnostic of the tensor-memory kernels' bounded waits: runs the inference
+ * kernel on one CTA with no MMA issued, so that nothing ever completes the
+ * mbarrier it waits on; the wait gives up after ~200 ms, the kernel frees its
+ * tensor memory and returns, and the error word reports the timeout.
+ * *timed_out = 1 when ae_rt_synchronize reported AE_RT_TIMEOUT as expected;
+ * the context remains usable.  Synchronous. */
+ae_rt_status ae_rc_selftest_wait_timeout(ae_rc* rc, uint32_t* timed_out);
+
 /* Loss gradients of n training records without an optimizer step (device
  * records; grad_mlp / grad_grid may be host or device memory or NULL). */
 ae_rt_status ae_rc_gradients(ae_rc* rc, const float* samples, uint32_t n, float* grad_mlp, float* grad_grid,

@@ -84,6 +84,30 @@ def test_forward_matches_fp64_oracle(cache):
     assert rel(got, P64[:, :3]) < 0.03, rel(got, P64[:, :3])
 
 
+def test_tensor_memory_wait_times_out_cleanly():
+    """Failure detection without a fault: the inference kernel run with no
+    MMA issued waits on an mbarrier that nothing completes; the bounded wait
+    gives up (~200 ms), the kernel frees its tensor memory and returns, and
+    the host reads AE_RT_TIMEOUT.  The context then still predicts correctly."""
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    rc = atlas_rt.RadianceCache(ctx, LO, HI, log2_table=14, seed=3)
+    try:
+        assert rc.selftest_wait_timeout()
+        mlp, grid = scaled_params(rc, 1)
+        rc.set_params(mlp, grid)
+        rec = random_records(300, 4)
+        out = torch.zeros((len(rec), 4), dtype=torch.float32, device="cuda")
+        rc.predict(torch.from_numpy(rec).cuda(), out)
+        ctx.synchronize()
+        m64, g64 = rc_oracle.emulate_params(mlp, grid)
+        _, P = rc_oracle.Cache(2 ** 14, LO, HI).forward(m64, g64.reshape(16, -1, 2), rec, bf16=True)
+        assert rel(out.cpu().numpy()[:, :3], P[:, :3]) < 0.01
+    finally:
+        rc.close()
+        ctx.close()
+
+
 def test_gradients_match_fp64_oracle(cache):
     import torch
     ctx, rc = cache
