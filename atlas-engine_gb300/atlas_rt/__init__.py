@@ -477,8 +477,9 @@ class Context:
 
     @staticmethod
     def _pass_params(radius=1.0, bias=0.0, roughness_cutoff=1.0, radiance_limit=10.0, environment=(0, 0, 0),
-                     opacity_check=False, frame_seed=0, seed=1):
+                     opacity_check=False, frame_seed=0, seed=1, texture_level=0):
         p = PassParams()
+        p.texture_level = texture_level
         p.radius, p.bias, p.roughness_cutoff, p.radiance_limit = radius, bias, roughness_cutoff, radiance_limit
         p.environment[:] = [float(x) for x in environment]
         p.flags = PASS_OPACITY_CHECK if opacity_check else 0

@@ -73,7 +73,8 @@ class GBuffer(C.Structure):
 
 class PassParams(C.Structure):
     _fields_ = [("radius", F32), ("bias", F32), ("roughness_cutoff", F32), ("radiance_limit", F32),
-                ("environment", F32 * 3), ("flags", U32), ("frame_seed", U32), ("seed", U32)]
+                ("environment", F32 * 3), ("flags", U32), ("frame_seed", U32), ("seed", U32),
+                ("texture_level", U32), ("reserved", U32)]
 
 
 class DdgiProbes(C.Structure):

@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -746,6 +747,37 @@ ae_rt_status ae_rt_scene_set_materials(ae_rt_ctx* ctx, const ae_material* materi
     return AE_RT_OK;
 }
 
+namespace {
+
+// One level of a texture's mip chain down from `src` (w x h texels of `texel`
+// bytes): texel (x, y) of the next level averages texels (2x + {0, 1},
+// 2y + {0, 1}), the indices clamped to the level; UNORM bytes as
+// (a + b + c + d + 2) / 4 in integers, floats as ((a + b) + (c + d)) * 0.25.
+void DownsampleLevel(const uint8_t* src, uint32_t w, uint32_t h, uint32_t format, uint8_t* dst) {
+    const uint32_t texel = format == AE_TEX_R8_UNORM ? 1u : 4u, nw = w > 1 ? w >> 1 : 1u, nh = h > 1 ? h >> 1 : 1u;
+    for (uint32_t y = 0; y < nh; y++)
+        for (uint32_t x = 0; x < nw; x++) {
+            const uint32_t x0 = std::min(2 * x, w - 1), x1 = std::min(2 * x + 1, w - 1);
+            const uint32_t y0 = std::min(2 * y, h - 1), y1 = std::min(2 * y + 1, h - 1);
+            const uint8_t* a = src + (size_t(y0) * w + x0) * texel;
+            const uint8_t* b = src + (size_t(y0) * w + x1) * texel;
+            const uint8_t* c = src + (size_t(y1) * w + x0) * texel;
+            const uint8_t* d = src + (size_t(y1) * w + x1) * texel;
+            uint8_t* o = dst + (size_t(y) * nw + x) * texel;
+            if (format == AE_TEX_R32_FLOAT) {
+                float fa, fb, fc, fd;
+                std::memcpy(&fa, a, 4); std::memcpy(&fb, b, 4); std::memcpy(&fc, c, 4); std::memcpy(&fd, d, 4);
+                const float f = ((fa + fb) + (fc + fd)) * 0.25f;
+                std::memcpy(o, &f, 4);
+            } else {
+                for (uint32_t k = 0; k < texel; k++)
+                    o[k] = uint8_t((uint32_t(a[k]) + b[k] + c[k] + d[k] + 2u) >> 2);
+            }
+        }
+}
+
+}  // namespace
+
 ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n) {
     if (!ctx || (n && !textures)) return AE_RT_INVALID_ARG;
     std::vector<atlas::rt::dev::TexDesc> desc(n);
@@ -766,15 +798,34 @@ ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures
         desc[i].height = t.height;
         desc[i].format = t.format;
         desc[i].row_pitch = row;
-        total += (size_t(row) * t.height + 15u) & ~size_t(15);
+        // the full mip chain down to 1 x 1, every level 16-byte aligned
+        uint32_t levels = 0, w = t.width, h = t.height;
+        for (;;) {
+            total += (size_t(w) * texel * h + 15u) & ~size_t(15);
+            levels++;
+            if (w == 1 && h == 1) break;
+            w = w > 1 ? w >> 1 : 1u;
+            h = h > 1 ? h >> 1 : 1u;
+        }
+        desc[i].levels = levels;
     }
     std::vector<uint8_t> pool(total);
     for (uint32_t i = 0; i < n; i++) {
         const ae_texture& t = textures[i];
+        const uint32_t texel = t.format == AE_TEX_R8_UNORM ? 1u : 4u;
         const size_t pitch = t.row_pitch ? t.row_pitch : desc[i].row_pitch;
+        uint8_t* lv = pool.data() + desc[i].offset;
         for (uint32_t y = 0; y < t.height; y++)
-            std::memcpy(pool.data() + desc[i].offset + size_t(y) * desc[i].row_pitch,
-                        static_cast<const uint8_t*>(t.texels) + size_t(y) * pitch, desc[i].row_pitch);
+            std::memcpy(lv + size_t(y) * desc[i].row_pitch, static_cast<const uint8_t*>(t.texels) + size_t(y) * pitch,
+                        desc[i].row_pitch);
+        uint32_t w = t.width, h = t.height;
+        for (uint32_t k = 1; k < desc[i].levels; k++) {
+            uint8_t* next = lv + ((size_t(w) * texel * h + 15u) & ~size_t(15));
+            DownsampleLevel(lv, w, h, t.format, next);
+            lv = next;
+            w = w > 1 ? w >> 1 : 1u;
+            h = h > 1 ? h >> 1 : 1u;
+        }
     }
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaFree(ctx->d_tex_pool);

@@ -50,7 +50,7 @@ struct GbParams {
 struct PassP {
     float radius, bias, cutoff, limit;
     float env[3];
-    uint32_t frame_seed, seed;
+    uint32_t frame_seed, seed, tex_level;
 };
 
 struct Queue {
@@ -425,6 +425,7 @@ PassP Pass(const ae_rt_pass_params* params) {
     for (int k = 0; k < 3; k++) pp.env[k] = params->environment[k];
     pp.frame_seed = params->frame_seed;
     pp.seed = params->seed;
+    pp.tex_level = params->texture_level;
     return pp;
 }
 
@@ -476,6 +477,7 @@ ae_rt_status ShadeAndResolve(ae_rt_ctx* ctx, const PassP& pp, const Queue& q, co
                              cudaStream_t s) {
     ShadeP sp{};
     sp.sc = Scene(ctx);
+    sp.sc.tex_level = KIND == kPassDDGI ? 4u : pp.tex_level;   // ddgi/rayHit.csh:79
     sp.pp = pp;
     sp.q = q;
     sp.hits = static_cast<const float4*>(ctx->pass_hits.ptr);

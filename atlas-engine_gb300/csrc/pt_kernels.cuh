@@ -48,6 +48,7 @@ struct PtScene {
     const float4* lights;         // GPULight (4 float4)
     uint32_t n_lights;
     TexTable tex;                 // the scene's textures (texture.cuh)
+    uint32_t tex_level;           // mip level of the surface textures (GetSurfaceParameters' textureLevel)
 };
 
 struct PtParams {
@@ -379,9 +380,9 @@ __device__ __forceinline__ float4 unpack_unorm4(float bits) {
 
 // The material terms of GetSurfaceParameters (surface.hsh:83-124) at the
 // hit's barycentrics: vertex colours, base colour / opacity / roughness /
-// metalness / ao textures and the normal map, all at texture level 0 (the
-// path tracer's level, rayHit.csh:177).  N is the interpolated normal (in and
-// out).
+// metalness / ao textures and the normal map, all at mip level sc.tex_level
+// (0 for the path tracer, rayHit.csh:177; 4 for DDGI probe rays,
+// ddgi/rayHit.csh:79).  N is the interpolated normal (in and out).
 __device__ __forceinline__ void surface_textures(const PtScene& sc, int32_t inst, int32_t triPtr, float r, float s,
                                                  float t, Mat& mat, V3& N) {
     const float4* ip = sc.instances + size_t(inst) * 4;
@@ -397,12 +398,13 @@ __device__ __forceinline__ void surface_textures(const PtScene& sc, int32_t inst
         mat.base = mat.base * v3(r * c0.x + s * c1.x + t * c2.x, r * c0.y + s * c1.y + t * c2.y,
                                  r * c0.z + s * c1.z + t * c2.z);
     }
-    const float4 bc = sample_rgba_bilinear(sc.tex, mat.baseTex, tu, tv);
+    const uint32_t lv = sc.tex_level;
+    const float4 bc = sample_rgba_bilinear(sc.tex, mat.baseTex, tu, tv, lv);
     mat.base = mat.base * v3(bc.x, bc.y, bc.z);
-    mat.opacity *= sample_r_bilinear(sc.tex, mat.opacityTex, tu, tv);
-    mat.roughness *= sample_r_bilinear(sc.tex, mat.roughTex, tu, tv);
-    mat.metalness *= sample_r_bilinear(sc.tex, mat.metalTex, tu, tv);
-    mat.ao *= sample_r_bilinear(sc.tex, mat.aoTex, tu, tv);
+    mat.opacity *= sample_r_bilinear(sc.tex, mat.opacityTex, tu, tv, lv);
+    mat.roughness *= sample_r_bilinear(sc.tex, mat.roughTex, tu, tv, lv);
+    mat.metalness *= sample_r_bilinear(sc.tex, mat.metalTex, tu, tv, lv);
+    mat.ao *= sample_r_bilinear(sc.tex, mat.aoTex, tu, tv, lv);
     if (mat.normalTex >= 0) {
         // TBN = (tangent, +-bitangent, normal) in world space (TransformTriangle)
         const float4* M = sc.inst_model + size_t(inst) * 3;
@@ -410,7 +412,7 @@ __device__ __forceinline__ void surface_textures(const PtScene& sc, int32_t inst
         const V3 T = normalize(xform_dir(mm, unpack_unit(d1.x)));
         V3 B = normalize(xform_dir(mm, unpack_unit(d1.y)));
         if (!(mat.invertUVs > 0)) B = B * -1.0f;
-        const float4 tn = sample_rgba_bilinear(sc.tex, mat.normalTex, tu, tv);
+        const float4 tn = sample_rgba_bilinear(sc.tex, mat.normalTex, tu, tv, lv);
         V3 n = T * (2.0f * tn.x - 1.0f) + B * (2.0f * tn.y - 1.0f) + N * (2.0f * tn.z - 1.0f);
         n = n * (1.0f / fmaxf(sqrtf(dot(n, n)), 0.00001f));
         const float w = saturate(mat.normalScale);

@@ -4,9 +4,11 @@
 // that a CPU restatement reproduces every sample bit for bit.  Hardware
 // filtering is not used: its interpolation weights have 8 fractional bits.
 //
-// Layout: every texture's level 0 lies tightly packed (row pitch = width x
-// texel bytes) in one pool, each starting on a 16-byte boundary; TexDesc
-// gives its offset, size and format.
+// Layout: every texture's mip chain lies tightly packed (row pitch = width x
+// texel bytes) in one pool, level after level, each level starting on a
+// 16-byte boundary; TexDesc gives level 0's offset, size and format.  Level
+// k + 1 is the 2 x 2 box filter of level k (indices clamped at odd edges;
+// built on the host when the textures are set).
 #pragma once
 
 #include <cstdint>
@@ -15,11 +17,12 @@
 namespace atlas::rt::dev {
 
 struct TexDesc {
-    unsigned long long offset;   // bytes into the pool
-    uint32_t width, height;
+    unsigned long long offset;   // bytes into the pool (level 0)
+    uint32_t width, height;      // level 0
     uint32_t format;             // AE_TEX_*
-    uint32_t row_pitch;          // bytes
-    uint32_t pad[2];
+    uint32_t row_pitch;          // bytes (level 0)
+    uint32_t levels;             // mip levels stored after level 0, down to 1 x 1
+    uint32_t pad;
 };
 static_assert(sizeof(TexDesc) == 32, "TexDesc is 32 bytes");
 
@@ -50,11 +53,26 @@ __device__ __forceinline__ void tex_axis(float s, uint32_t n, uint32_t& i0, uint
     i1 = i0 + 1u == n ? 0u : i0 + 1u;
 }
 
-// textureLod(sampler2D(bindlessTextures[id], bindlessSampler), uv, 0).r;
-// 1.0 for a negative or out-of-range id.
-__device__ __forceinline__ float sample_r_bilinear(const TexTable& tt, int32_t id, float u, float v) {
+// The descriptor of mip level `level` (clamped to the chain) of texture t.
+__device__ __forceinline__ TexDesc tex_level(TexDesc t, uint32_t level) {
+    const uint32_t texel = t.format == 0u ? 1u : 4u;
+    const uint32_t last = t.levels ? t.levels - 1u : 0u;
+    for (uint32_t k = 0; k < level && k < last; k++) {
+        t.offset += ((unsigned long long)(t.width * texel) * t.height + 15ull) & ~15ull;
+        t.width = t.width > 1u ? t.width >> 1 : 1u;
+        t.height = t.height > 1u ? t.height >> 1 : 1u;
+        t.row_pitch = t.width * texel;
+    }
+    return t;
+}
+
+// textureLod(sampler2D(bindlessTextures[id], bindlessSampler), uv, level).r
+// for an integer level (one mip level, no blending between levels); 1.0
+// for a negative or out-of-range id.
+__device__ __forceinline__ float sample_r_bilinear(const TexTable& tt, int32_t id, float u, float v,
+                                                   uint32_t level = 0) {
     if (id < 0 || uint32_t(id) >= tt.n) return 1.0f;
-    const TexDesc t = tt.desc[id];
+    const TexDesc t = tex_level(tt.desc[id], level);
     uint32_t x0, x1, y0, y1;
     float a, b;
     tex_axis(u, t.width, x0, x1, a);
@@ -93,9 +111,10 @@ __device__ __forceinline__ float bilerp(float ia, float ib, float a, float b, fl
 // every channel filtered as sample_r_bilinear filters the first; (1, 1, 1, 1)
 // for a negative or out-of-range id (SampleBaseColorBilinear and friends,
 // texture.hsh:9-60).
-__device__ __forceinline__ float4 sample_rgba_bilinear(const TexTable& tt, int32_t id, float u, float v) {
+__device__ __forceinline__ float4 sample_rgba_bilinear(const TexTable& tt, int32_t id, float u, float v,
+                                                     uint32_t level = 0) {
     if (id < 0 || uint32_t(id) >= tt.n) return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    const TexDesc t = tt.desc[id];
+    const TexDesc t = tex_level(tt.desc[id], level);
     uint32_t x0, x1, y0, y1;
     float a, b;
     tex_axis(u, t.width, x0, x1, a);

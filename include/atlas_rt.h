@@ -497,16 +497,22 @@ typedef struct ae_texture {
  * RayTracingWorld::UpdateMaterials indexes through
  * Scene::textureToBindlessIdx (RayTracingWorld.cpp:217-237); texture i is
  * what a material's *Texture field i names, and a negative or out-of-range
- * index samples as 1.0 (texture.hsh:18-25 for negative ones).  Only level 0
- * is kept: every traversal lookup samples level 0 (bvh.hsh:127, :163).
+ * index samples as 1.0 (texture.hsh:18-25 for negative ones).  The
+ * traversal's opacity lookups sample level 0 (bvh.hsh:127, :163); surface
+ * shading samples the level its pass reads (0 for the path tracer, 4 for
+ * DDGI, ae_rt_pass_params.texture_level for reflections and RTGI).
  * Sampling follows the engine's bindless sampler (linear filter, repeat
  * addressing, MainRenderer.cpp:922-929) in FP32, one rounding per
  * operation: x = u * width - 0.5, i = floor(x), a = x - i, texels i and i+1
  * modulo width (likewise y with v and height), value = ((w00*c00 + w10*c10)
  * + w01*c01) + w11*c11 with w00 = (1-a)(1-b), w10 = a(1-b), w01 = (1-a)b,
  * w11 = ab; UNORM texels are byte / 255; a non-finite x (or y) becomes 0,
- * which reads texel 0 of that axis alone.  Copies the texels into device memory and replaces the previous
- * table (n = 0 clears it). */
+ * which reads texel 0 of that axis alone.  Copies the texels into device
+ * memory together with their mip chain down to 1 x 1 (level k + 1 = the
+ * 2 x 2 box filter of level k, indices clamped at odd edges; UNORM bytes
+ * as (a + b + c + d + 2) / 4, floats as ((a + b) + (c + d)) * 0.25) and
+ * replaces the previous table (n = 0 clears it).  An integer level samples
+ * that one level, as textureLod does. */
 ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n);
 ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n);
 
@@ -585,6 +591,9 @@ typedef struct ae_rt_pass_params {
     uint32_t flags;          /* AE_PASS_OPACITY_CHECK */
     uint32_t frame_seed;     /* uniforms.frameSeed: the sample index of the random streams */
     uint32_t seed;           /* random stream of light choices (and of samples when none are given) */
+    uint32_t texture_level;  /* reflections, RTGI: mip level of the hit's surface textures
+                                (uniforms.textureLevel); DDGI always reads level 4 (ddgi/rayHit.csh:79) */
+    uint32_t reserved;
 } ae_rt_pass_params;
 
 /* Ray-traced ambient occlusion, ao/rtao.csh:40-112: per pixel with depth < 1

@@ -993,6 +993,7 @@ typedef struct {
     const float* lights;
     uint32_t n_lights;
     const aeo_texture* textures; uint32_t n_textures;   /* surface textures (GetSurfaceParameters) */
+    uint32_t tex_level;                                  /* their mip level (textureLevel) */
     const float* cam;
     uint32_t width, height, spp, sample_offset, max_bounces, seed;
     float epsilon;
@@ -1047,13 +1048,26 @@ static void texel_rgba(const aeo_texture* t, uint32_t x, uint32_t y, float c[4])
 
 /* textureLod(...) with all channels filtered like aeo_sample_r_bilinear's
  * first; (1, 1, 1, 1) for a negative or out-of-range id (texture.hsh:9-60). */
+/* Mip level `level` of texture t, clamped to the levels given. */
+static const aeo_texture* tex_at_level(const aeo_texture* t, uint32_t level) {
+    if (level == 0 || t->n_mips == 0) return t;
+    return &t->mips[(level < t->n_mips ? level : t->n_mips) - 1];
+}
+
+/* aeo_sample_r_bilinear at mip level `level` */
+static float sample_r_level(const aeo_texture* textures, uint32_t n_textures, int32_t id, float u, float v,
+                            uint32_t level) {
+    if (id < 0 || (uint32_t)id >= n_textures) return 1.0f;
+    return aeo_sample_r_bilinear(tex_at_level(&textures[id], level), 1, 0, u, v);
+}
+
 static void sample_rgba_bilinear(const aeo_texture* textures, uint32_t n_textures, int32_t id, float u, float v,
-                                 float out[4]) {
+                                 uint32_t level, float out[4]) {
     if (id < 0 || (uint32_t)id >= n_textures) {
         out[0] = out[1] = out[2] = out[3] = 1.0f;
         return;
     }
-    const aeo_texture* t = &textures[id];
+    const aeo_texture* t = tex_at_level(&textures[id], level);
     uint32_t x0, x1, y0, y1;
     float a, b;
     tex_axis(u, t->width, &x0, &x1, &a);
@@ -1101,18 +1115,19 @@ static void pt_surface_textures(const pt_job_t* j, int32_t inst, int32_t tp, con
                                     r * unorm8(c0, 2) + s * unorm8(c1, 2) + t * unorm8(c2, 2)));
     }
     float c[4];
-    sample_rgba_bilinear(j->textures, j->n_textures, w[17], tu, tv, c);
+    const uint32_t lv = j->tex_level;
+    sample_rgba_bilinear(j->textures, j->n_textures, w[17], tu, tv, lv, c);
     m->base = vmulv(m->base, mk(c[0], c[1], c[2]));
-    m->opacity *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[18], tu, tv);
-    m->roughness *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[20], tu, tv);
-    m->metalness *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[21], tu, tv);
-    m->ao *= aeo_sample_r_bilinear(j->textures, j->n_textures, w[22], tu, tv);
+    m->opacity *= sample_r_level(j->textures, j->n_textures, w[18], tu, tv, lv);
+    m->roughness *= sample_r_level(j->textures, j->n_textures, w[20], tu, tv, lv);
+    m->metalness *= sample_r_level(j->textures, j->n_textures, w[21], tu, tv, lv);
+    m->ao *= sample_r_level(j->textures, j->n_textures, w[22], tu, tv, lv);
     if (w[19] >= 0) {
         const float* mm = j->inst_model + (size_t)inst * 12;
         v3 T = vnorm(xdir(mm, unpack10(g[16])));
         v3 B = vnorm(xdir(mm, unpack10(g[17])));
         if (!(w[13] > 0)) B = vmul(B, -1.0f);
-        sample_rgba_bilinear(j->textures, j->n_textures, w[19], tu, tv, c);
+        sample_rgba_bilinear(j->textures, j->n_textures, w[19], tu, tv, lv, c);
         v3 n = vadd(vadd(vmul(T, 2.0f * c[0] - 1.0f), vmul(B, 2.0f * c[1] - 1.0f)), vmul(*N, 2.0f * c[2] - 1.0f));
         n = vmul(n, 1.0f / fmaxf(sqrtf(vdot(n, n)), 0.00001f));
         const float wgt = sat(mw[12]);
@@ -1598,6 +1613,7 @@ static void run_pass(const aeo_pass_scene* s, int kind, const aeo_gbuffer* gb, c
     proto.j.n_lights = s->n_lights;
     proto.j.textures = s->textures;
     proto.j.n_textures = s->n_textures;
+    proto.j.tex_level = kind == PASS_DDGI ? 4u : pp->texture_level;   /* ddgi/rayHit.csh:79 */
     proto.j.epsilon = PASS_EPS;
     proto.j.stack_cap = scene_stack_cap(&sc);
     proto.tsc = tsc;

@@ -99,6 +99,10 @@ void aeo_scene_any_glsl(const aeo_node* tlas, uint32_t n_tlas, const aeo_instanc
 typedef struct aeo_texture {
     const void* texels;
     uint32_t width, height, format, row_pitch;
+    /* levels 1, 2, ... of the mip chain (tight rows), for the surface
+     * lookups at a level > 0; NULL / 0 when only level 0 is given */
+    const struct aeo_texture* mips;
+    uint32_t n_mips;
 } aeo_texture;
 
 /* Path tracer -- the restatement of the engine's non-real-time estimator
@@ -172,6 +176,7 @@ typedef struct aeo_pass_params {
     float environment[3];
     uint32_t flags;        /* 1: opacity check (transparency traversals) */
     uint32_t frame_seed, seed;
+    uint32_t texture_level, reserved;   /* reflections / RTGI surface textures; DDGI reads level 4 */
 } aeo_pass_params;
 
 typedef struct aeo_ddgi_probes {

@@ -200,7 +200,37 @@ def _mesh_table(meshes):
 
 
 class _Texture(C.Structure):
-    _fields_ = [("texels", P), ("width", U32), ("height", U32), ("format", U32), ("row_pitch", U32)]
+    pass
+
+
+_Texture._fields_ = [("texels", P), ("width", U32), ("height", U32), ("format", U32), ("row_pitch", U32),
+                     ("mips", C.POINTER(_Texture)), ("n_mips", U32)]
+
+
+def mip_chain(tex: np.ndarray) -> list:
+    """Levels 1.. down to 1 x 1 of a texel array: texel (x, y) of level k + 1
+    averages texels (2x + {0, 1}, 2y + {0, 1}) of level k, the indices
+    clamped to the level; UNORM bytes as (a + b + c + d + 2) // 4, floats as
+    ((a + b) + (c + d)) * 0.25 in float32."""
+    out = []
+    cur = tex
+    while cur.shape[0] > 1 or cur.shape[1] > 1:
+        h, w = cur.shape[:2]
+        nh, nw = max(1, h >> 1), max(1, w >> 1)
+        x0 = np.minimum(2 * np.arange(nw), w - 1)
+        x1 = np.minimum(2 * np.arange(nw) + 1, w - 1)
+        y0 = np.minimum(2 * np.arange(nh), h - 1)
+        y1 = np.minimum(2 * np.arange(nh) + 1, h - 1)
+        a, b = cur[y0][:, x0], cur[y0][:, x1]
+        c, d = cur[y1][:, x0], cur[y1][:, x1]
+        if cur.dtype == np.uint8:
+            nxt = ((a.astype(np.uint32) + b + c + d + 2) >> 2).astype(np.uint8)
+        else:
+            nxt = ((a + b) + (c + d)) * np.float32(0.25)
+        nxt = np.ascontiguousarray(nxt)
+        out.append(nxt)
+        cur = nxt
+    return out
 
 
 TEX_FORMATS = {"r8": 0, "rgba8": 1, "r32f": 2}
@@ -223,12 +253,22 @@ def _texture_table(textures):
     textures = list(textures or [])
     keep = [np.ascontiguousarray(t) for t in textures]
     table = (_Texture * max(1, len(keep)))()
+    extra = []
     for i, t in enumerate(keep):
         table[i].texels = t.ctypes.data
         table[i].height, table[i].width = t.shape[0], t.shape[1]
         table[i].format = texture_format(t)
         table[i].row_pitch = 0
-    return table, len(keep), keep
+        levels = mip_chain(t)
+        mt = (_Texture * max(1, len(levels)))()
+        for k, lv in enumerate(levels):
+            mt[k].texels = lv.ctypes.data
+            mt[k].height, mt[k].width = lv.shape[0], lv.shape[1]
+            mt[k].format = table[i].format
+        table[i].mips = mt
+        table[i].n_mips = len(levels)
+        extra += [levels, mt]
+    return table, len(keep), keep + extra
 
 
 def sample_r_bilinear(textures, tex_id, u, v):
@@ -421,7 +461,7 @@ class _GBuffer(C.Structure):
 class _PassParams(C.Structure):
     _fields_ = [("radius", C.c_float), ("bias", C.c_float), ("roughness_cutoff", C.c_float),
                 ("radiance_limit", C.c_float), ("environment", C.c_float * 3), ("flags", U32),
-                ("frame_seed", U32), ("seed", U32)]
+                ("frame_seed", U32), ("seed", U32), ("texture_level", U32), ("reserved", U32)]
 
 
 class _DdgiProbes(C.Structure):
@@ -464,9 +504,9 @@ def _pass_scene(tlas_f32, instances, inst_model, meshes, materials, lights, text
 
 
 def _pass_params(radius=1.0, bias=0.0, roughness_cutoff=1.0, radiance_limit=10.0, environment=(0, 0, 0),
-                 opacity_check=False, frame_seed=0, seed=1):
+                 opacity_check=False, frame_seed=0, seed=1, texture_level=0):
     return _PassParams(radius, bias, roughness_cutoff, radiance_limit, (C.c_float * 3)(*environment),
-                       1 if opacity_check else 0, frame_seed, seed)
+                       1 if opacity_check else 0, frame_seed, seed, texture_level, 0)
 
 
 def _gbuffer(gb):

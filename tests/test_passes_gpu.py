@@ -242,9 +242,11 @@ def test_texture_argument_errors(sand_ctx):
     ctx.set_textures([])                                       # clears the table
 
 
-@pytest.mark.parametrize("kind", ["reflections", "rtgi"])
-def test_shading_passes_textured_match_oracle(kind):
-    """The passes shade hits with the full material model too."""
+@pytest.mark.parametrize("kind,level", [("reflections", 0), ("rtgi", 0), ("rtgi", 2)])
+def test_shading_passes_textured_match_oracle(kind, level):
+    """The passes shade hits with the full material model too, at the
+    texture level they are given (the device's mip chain against the
+    oracle's)."""
     import textured_util
     ctx = atlas_rt.Context(device=0)
     try:
@@ -255,11 +257,42 @@ def test_shading_passes_textured_match_oracle(kind):
         rng = np.random.default_rng(12)
         rough = rng.uniform(0.0, 0.9, (90, 160)).astype(np.float32)
         gb = gbuffer(s, 160, 90, roughness=rough, samples=True)
-        params = dict(radiance_limit=4.0, roughness_cutoff=0.8, environment=(0.05, 0.1, 0.2), frame_seed=4, seed=5)
+        params = dict(radiance_limit=4.0, roughness_cutoff=0.8, environment=(0.05, 0.1, 0.2), frame_seed=4, seed=5,
+                      texture_level=level)
         got = run(ctx, kind, gb, **params)
         ref = pyoracle.pass_screen(kind, osc + (tex,), gb, **params)
         close = np.all(np.abs(got[..., :3] - ref[..., :3]) <= 1e-3 * np.abs(ref[..., :3]) + 1e-5, axis=2)
         assert close.mean() > 0.97, close.mean()
         np.testing.assert_allclose(got[..., :3].mean(), ref[..., :3].mean(), rtol=0.02)
+    finally:
+        ctx.close()
+
+
+def test_ddgi_textured_matches_oracle():
+    """DDGI probe rays shade their hits with the surface textures at level 4
+    (ddgi/rayHit.csh:79), on the GPU as in the oracle."""
+    import torch
+    import textured_util
+    ctx = atlas_rt.Context(device=0)
+    try:
+        sc, gt, sh, tex = textured_util.build()
+        textured_util.upload(ctx, sc, gt, sh, tex)
+        osc, _ = textured_util.oracle_scene(sc, gt, sh)
+        g = np.stack(np.meshgrid(np.linspace(5, 95, 6), [4.0, 12.0], np.linspace(5, 95, 6), indexing="ij"),
+                     -1).reshape(-1, 3)
+        probes = np.concatenate([g, np.zeros((len(g), 1))], 1).astype(np.float32)
+        dirs = fibonacci_dirs(64)
+        rot = np.eye(4)
+        params = dict(environment=(0.3, 0.4, 0.5), frame_seed=3, seed=6)
+        ref = np.zeros((len(probes) * len(dirs), 4), np.float32)
+        pyoracle.pass_ddgi(osc + (tex,), probes, dirs, rot, ref, **params)
+        out = torch.zeros(ref.shape, dtype=torch.float32, device="cuda")
+        ctx.ddgi_trace(torch.from_numpy(probes).cuda(), torch.from_numpy(dirs).cuda(), rot, out, **params)
+        ctx.synchronize()
+        _, gr, gd = unpack_ray_hits(out.cpu().numpy())
+        _, rr, rd = unpack_ray_hits(ref)
+        assert (np.abs(gd - rd) <= 1e-4 * np.abs(rd)).mean() > 0.99
+        close = np.all(np.abs(gr - rr) <= 4e-3 * np.abs(rr) + 1e-4, axis=1)
+        assert close.mean() > 0.97, close.mean()
     finally:
         ctx.close()

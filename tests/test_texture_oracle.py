@@ -217,3 +217,35 @@ def test_textured_oracle_image_differs_from_plain():
     b = pyoracle.pathtrace(*osc[:4], plain, osc[5], camv, 32, 18, 16, textures=tex)
     assert np.isfinite(a).all() and a.mean() > 0
     assert abs(a.mean() - b.mean()) / b.mean() > 0.05
+
+
+def test_mip_chain_known_answers():
+    """Level k + 1 = 2 x 2 box of level k (UNORM rounding (a+b+c+d+2)//4),
+    indices clamped at odd edges, down to 1 x 1."""
+    t = np.array([[0, 4, 8, 12], [2, 6, 10, 255]], np.uint8)
+    levels = pyoracle.mip_chain(t)
+    assert [lv.shape for lv in levels] == [(1, 2), (1, 1)]
+    np.testing.assert_array_equal(levels[0], [[(0 + 4 + 2 + 6 + 2) // 4, (8 + 12 + 10 + 255 + 2) // 4]])
+    np.testing.assert_array_equal(levels[1], [[(3 + 3 + 71 + 71 + 2) // 4]])
+    odd = np.arange(9, dtype=np.float32).reshape(3, 3)
+    lv = pyoracle.mip_chain(odd)
+    assert [x.shape for x in lv] == [(1, 1)]
+    assert lv[0][0, 0] == np.float32(((0 + 1) + (3 + 4)) * 0.25)
+    rgba = np.zeros((2, 2, 4), np.uint8)
+    rgba[..., 2] = [[10, 20], [30, 41]]
+    assert pyoracle.mip_chain(rgba)[0][0, 0, 2] == (10 + 20 + 30 + 41 + 2) // 4
+
+
+def test_surface_lookups_read_the_requested_level():
+    """The passes' surface lookups read uniforms.textureLevel: on the textured
+    scene, RTGI at level 3 (box-filtered textures) differs from level 0,
+    while levels past the chain's end clamp to its last level."""
+    from passes_util import gbuffer
+    from textured_util import build, oracle_scene
+    sc, gt, sh, tex = build(grid=24, n_boxes=4)
+    osc, _ = oracle_scene(sc, gt, sh)
+    gb = gbuffer({"oracle": osc, "shading": sh}, 48, 27, samples=True)
+    run = lambda lv: pyoracle.pass_screen("rtgi", osc + (tex,), gb, radiance_limit=4.0, texture_level=lv)
+    a, b = run(0), run(3)
+    assert np.abs(a - b).max() > 1e-3
+    np.testing.assert_array_equal(run(20), run(5))     # the largest texture has 6 levels
