@@ -456,6 +456,23 @@ class Context:
         _check(lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
                                      _stream_handle(stream)), self._h)
 
+    def pathtrace_realtime(self, cam: "Camera", frame_accum, max_radiance=0.0, spp=1, max_bounces=3,
+                           sample_offset=0, seed=1, epsilon=0.1, mis=False, stream=None):
+        """ae_rt_pathtrace_realtime: the engine's real-time accumulation into
+        frame_accum, a (3, h, w) 32-bit device tensor (float bits at spp = 1,
+        quantised unsigned sums at spp > 1)."""
+        p = PtParams()
+        p.spp, p.max_bounces, p.sample_offset, p.seed, p.epsilon = spp, max_bounces, sample_offset, seed, epsilon
+        p.flags = 1 if mis else 0
+        _check(lib().ae_rt_pathtrace_realtime(self._h, C.byref(cam), C.byref(p), _ptr(frame_accum), max_radiance,
+                                              _stream_handle(stream)), self._h)
+
+    def tonemap(self, accum, width: int, height: int, samples: int, exposure: float, gamma: float, out,
+                stream=None):
+        """ae_rt_pt_tonemap: the non-real-time output image into `out` (float4 per pixel)."""
+        _check(lib().ae_rt_pt_tonemap(self._h, _ptr(accum), width, height, samples, exposure, gamma, _ptr(out),
+                                      _stream_handle(stream)), self._h)
+
     # -- the traversal's other consumers (RTAO, reflections, RTGI, DDGI) ------
 
     @staticmethod

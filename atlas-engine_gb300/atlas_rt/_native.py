@@ -121,6 +121,8 @@ _SIGNATURES = [
     ("ae_rt_scene_set_textures", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
+    ("ae_rt_pathtrace_realtime", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, F32, P]),
+    ("ae_rt_pt_tonemap", C.c_int, [P, P, U32, U32, U32, F32, F32, P, P]),
     ("ae_rt_rtao", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
     ("ae_rt_reflections", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
     ("ae_rt_rtgi", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),

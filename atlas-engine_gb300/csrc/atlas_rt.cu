@@ -867,18 +867,28 @@ ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint
     return AE_RT_OK;
 }
 
-ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
-                             double* accum64, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// The path tracer's sample loop (ae_rt_pathtrace / ae_rt_pathtrace_realtime):
+// radiance into accum (+ accum64), or, with frame_accum, into the real-time
+// [3][H][W] uint32 frame accumulation.
+ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
+                       double* accum64, uint32_t* frame_accum, float max_radiance, void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
-    if (!cam || !params || !accum) return Fail(ctx, AE_RT_INVALID_ARG, "null argument");
+    if (!cam || !params || (!accum && !frame_accum)) return Fail(ctx, AE_RT_INVALID_ARG, "null argument");
     if (!ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
     if (!ctx->d_materials) return Fail(ctx, AE_RT_INVALID_ARG, "no materials have been set");
     for (const auto& m : ctx->meshes)
         if (!m.shading && m.n_tris) return Fail(ctx, AE_RT_INVALID_ARG, "path tracing needs shading triangles");
     if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 28))
         return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
-    if (!IsDevicePointer(accum) || (accum64 && !IsDevicePointer(accum64)))
+    if ((accum && !IsDevicePointer(accum)) || (accum64 && !IsDevicePointer(accum64)) ||
+        (frame_accum && !IsDevicePointer(frame_accum)))
         return Fail(ctx, AE_RT_INVALID_ARG, "accumulation buffers must be device memory");
+    if (frame_accum && !(max_radiance > 0.0f) && params->spp > 1)
+        return Fail(ctx, AE_RT_INVALID_ARG, "the quantised real-time accumulation needs max_radiance > 0");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t n = cam->width * cam->height;
@@ -912,6 +922,15 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
     // with MIS a later bounce's shading adds light hits into the pixels that
     // the previous bounce's resolve (running beside it) adds into
     p.atomic_accum = p.mis;
+    if (frame_accum) {
+        // cleared here; the engine's renderer clears its frame image before
+        // the dispatch (one store per pixel at one sample, atomics otherwise)
+        AE_CUDA(ctx, cudaMemsetAsync(frame_accum, 0, size_t(n) * 3 * sizeof(uint32_t), s));
+        p.frame_accum = frame_accum;
+        p.rt_max_radiance = max_radiance;
+        p.rt_max_per_sample = params->spp > 1 ? 0xFFFFFFFFu / params->spp : 0u;
+        p.atomic_accum = 1;
+    }
     p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
     p.accum = reinterpret_cast<float4*>(accum);
     p.accum64 = accum64;
@@ -972,6 +991,39 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
         for (int q = 0; q < 2; q++)
             if (pending[q]) AE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
     }
+    return AE_RT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
+                             double* accum64, void* stream) {
+    if (ctx && !accum) return Fail(ctx, AE_RT_INVALID_ARG, "null accumulation buffer");
+    return PathTrace(ctx, cam, params, accum, accum64, nullptr, 0.0f, stream);
+}
+
+ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params,
+                                      uint32_t* frame_accum, float max_radiance, void* stream) {
+    if (ctx && !frame_accum) return Fail(ctx, AE_RT_INVALID_ARG, "null frame accumulation buffer");
+    return PathTrace(ctx, cam, params, nullptr, nullptr, frame_accum, max_radiance, stream);
+}
+
+ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,
+                              float exposure, float gamma, float* out, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    const uint64_t n = uint64_t(width) * height;
+    if (n == 0) return AE_RT_OK;
+    if (!accum || !out || !IsDevicePointer(accum) || !IsDevicePointer(out))
+        return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_pt_tonemap takes device buffers");
+    if (samples == 0 || n > (1ull << 28)) return Fail(ctx, AE_RT_INVALID_ARG, "bad sample count or size");
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    const uint32_t blocks = uint32_t(std::min<uint64_t>((n + 255) / 256, uint64_t(ctx->sm_count) * 8u));
+    atlas::rt::dev::pt_tonemap_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(accum), uint32_t(n), exposure / float(samples), gamma,
+        reinterpret_cast<float4*>(out));
+    AE_CUDA(ctx, cudaGetLastError());
     return AE_RT_OK;
 }
 

@@ -77,6 +77,11 @@ struct PtParams {
     uint32_t atomic_accum;        // several contributions per pixel and pass: add atomically
     uint32_t capacity;            // queue capacity in rays (0: width * height)
     uint32_t* overflow;           // set when an append would pass the capacity (ray dropped)
+    // real-time mode (rayHit.csh:134-150): radiance into a [3][H][W] uint32
+    // frame accumulation instead of accum / accum64
+    uint32_t* frame_accum;
+    float rt_max_radiance;
+    uint32_t rt_max_per_sample;   // 0: one sample per frame, float bits
 };
 
 // Pixel keys carried by rays and payloads: the pixel index in the low 24
@@ -340,6 +345,25 @@ static __global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
 
 __device__ __forceinline__ void add_radiance(const PtParams& p, uint32_t key, V3 L) {
     const uint32_t pix = key & kPixelMask;
+    if (p.frame_accum) {
+        // real-time accumulation: the float itself at one sample per frame,
+        // else radiance / maxRadiance clamped to [0, 1] and quantised to
+        // 0xFFFFFFFF / samplesPerFrame steps, added atomically per channel
+        const size_t plane = size_t(p.width) * p.height;
+        const float c[3] = { L.x, L.y, L.z };
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            uint32_t* d = p.frame_accum + k * plane + pix;
+            if (!p.rt_max_per_sample) {
+                atomicAdd(reinterpret_cast<float*>(d), c[k]);
+            } else {
+                const float nr = fminf(fmaxf(c[k] / p.rt_max_radiance, 0.0f), 1.0f);
+                const uint32_t q = min(uint32_t(nr * float(p.rt_max_per_sample)), p.rt_max_per_sample);
+                if (q) atomicAdd(d, q);
+            }
+        }
+        return;
+    }
     float4* a = p.accum + pix;
     if (p.atomic_accum) {
         atomicAdd(&a->x, L.x);
@@ -721,6 +745,20 @@ static __global__ void pt_resolve_kernel(PtParams p) {
     if (i >= n || p.shadow_occ[i]) return;
     const float4 c = p.shadow_pay[i];
     add_radiance(p, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+}
+
+}  // namespace atlas::rt::dev
+
+namespace atlas::rt::dev {
+
+// The non-real-time output image (rayHit.csh:124-130): colour = accum.rgb *
+// exposure / samples, mapped by 1 - exp(-colour) and raised to gamma.
+static __global__ void pt_tonemap_kernel(const float4* accum, uint32_t n, float scale, float gamma, float4* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = accum[i];
+        out[i] = make_float4(powf(1.0f - expf(-(a.x * scale)), gamma), powf(1.0f - expf(-(a.y * scale)), gamma),
+                             powf(1.0f - expf(-(a.z * scale)), gamma), 1.0f);
+    }
 }
 
 }  // namespace atlas::rt::dev

@@ -541,6 +541,26 @@ typedef struct ae_pt_params {
 ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
                              double* accum64, void* stream);
 
+/* The engine's real-time accumulation of the same estimator
+ * (rayHit.csh:134-150, REALTIME): params->spp samples per pixel into
+ * frame_accum, a [3][height][width] uint32 image (one layer per channel,
+ * the engine's frameAccumImage), cleared by the call.  At spp = 1 each
+ * pixel holds the float bits of its radiance; at spp > 1 every radiance
+ * contribution is divided by max_radiance, clamped to [0, 1], scaled to
+ * 0xFFFFFFFF / spp and added as an unsigned integer.  The engine quantises
+ * a path's total; here each contribution (emission, each light sample) is
+ * quantised, which differs only where the clamp or the rounding bites.
+ * Device memory. */
+ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params,
+                                      uint32_t* frame_accum, float max_radiance, void* stream);
+
+/* The non-real-time output image (rayHit.csh:124-130): for every pixel of
+ * accum (float4, the sum of `samples` samples), colour = accum.rgb *
+ * exposure / samples, out = (pow(1 - exp(-colour), gamma), 1).  Device
+ * memory, float4 per pixel. */
+ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,
+                              float exposure, float gamma, float* out, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* The traversal's other consumers: RTAO, reflections, RTGI, DDGI probe rays  */
 /* ------------------------------------------------------------------------ */

@@ -139,3 +139,47 @@ def test_pt_textured_matches_cpu_restatement():
         assert ptscene.rel_mse(g64, c) < 1e-4
     finally:
         ctx.close()
+
+
+def test_realtime_accumulation(pt_setup):
+    """The real-time mode (rayHit.csh:134-150): at one sample per frame the
+    frame holds each pixel's radiance as float bits, the same sum the
+    non-real-time accumulation gets; at 4 samples the quantised unsigned
+    sums, scaled back, agree with the float sums to the quantisation step
+    per contribution."""
+    import torch
+    ctx, sc, osc = pt_setup
+    w, h = 64, 36
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h))
+    for spp, offset in ((1, 5), (4, 40)):
+        acc = torch.zeros((h * w, 4), dtype=torch.float32, device="cuda")
+        ctx.pathtrace(cam, acc, spp=spp, sample_offset=offset)
+        fr = torch.full((3, h, w), 7, dtype=torch.int32, device="cuda")
+        ctx.pathtrace_realtime(cam, fr, max_radiance=64.0, spp=spp, sample_offset=offset)
+        ctx.synchronize()
+        ref = acc.cpu().numpy()[:, :3].reshape(h, w, 3).transpose(2, 0, 1)
+        got = fr.cpu().numpy()
+        if spp == 1:
+            np.testing.assert_allclose(got.view(np.float32), ref, rtol=1e-5, atol=1e-7)
+        else:
+            step = 64.0 / (0xFFFFFFFF // spp)
+            scaled = got.view(np.uint32).astype(np.float64) * step
+            np.testing.assert_allclose(scaled, ref, rtol=1e-5, atol=64 * step)
+        assert (ref > 0).mean() > 0.3
+
+
+def test_tonemap_output():
+    """ae_rt_pt_tonemap against the formula of rayHit.csh:124-130."""
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    try:
+        rng = np.random.default_rng(3)
+        acc = rng.uniform(0, 50, (33 * 17, 4)).astype(np.float32)
+        out = torch.zeros((33 * 17, 4), dtype=torch.float32, device="cuda")
+        ctx.tonemap(torch.from_numpy(acc).cuda(), 33, 17, 16, 1.5, 1 / 2.2, out)
+        ctx.synchronize()
+        want = np.power(1 - np.exp(-acc[:, :3].astype(np.float64) * 1.5 / 16), 1 / 2.2)
+        np.testing.assert_allclose(out.cpu().numpy()[:, :3], want, rtol=2e-6, atol=1e-6)
+        assert np.all(out.cpu().numpy()[:, 3] == 1.0)
+    finally:
+        ctx.close()
