@@ -100,6 +100,10 @@ def ref():
         L.aeref_get_nodes.argtypes = [P, P]
         L.aeref_get_data.argtypes = [P, P, P, P]
         L.aeref_get_refs.argtypes = [P, P]
+        L.aeref_get_refs_full.argtypes = [P, P, P, P, P]
+        L.aeref_aabbs_count.restype = U32
+        L.aeref_aabbs_count.argtypes = [P]
+        L.aeref_get_aabbs.argtypes = [P, P]
         L.aeref_closest.argtypes = [P, P, U32, C.c_int, P, P, P]
         L.aeref_any.argtypes = [P, P, U32, C.c_int, P]
         L.aeref_free.argtypes = [P]
@@ -429,6 +433,40 @@ class RefBVH:
         if getattr(self, "h", None):
             ref().aeref_free(self.h)
             self.h = None
+
+
+def ref_members(verts=None, boxes=None, parallel=True):
+    """Every public member of the reference's Volume::BVH (BVH.h:133-137)
+    after the triangle build (verts; boxes are the triangles' bounds) or the
+    AABB-only build (boxes): nodes (n, 16) in the GPUBVHNode layout, data
+    (verts, idx, endOfNode), refs (idx, nodeIdx, endOfNode, aabb) and aabbs."""
+    L = ref()
+    if verts is not None:
+        v = _c(verts, np.float32).reshape(-1, 9)
+        h = L.aeref_build(v.ctypes.data if len(v) else None, len(v), int(parallel))
+    else:
+        b = _c(boxes, np.float32).reshape(-1, 6)
+        h = L.aeref_build_aabbs(b.ctypes.data if len(b) else None, len(b), int(parallel))
+    try:
+        nn, nd, nr = L.aeref_node_count(h), L.aeref_data_count(h), L.aeref_refs_count(h)
+        na = L.aeref_aabbs_count(h)
+        out = {"nodes": np.zeros((nn, 16), np.float32), "data_verts": np.zeros((nd, 9), np.float32),
+               "data_idx": np.zeros(nd, np.uint32), "data_eon": np.zeros(nd, np.uint8),
+               "refs_idx": np.zeros(nr, np.uint32), "refs_node": np.zeros(nr, np.uint32),
+               "refs_eon": np.zeros(nr, np.uint8), "refs_aabb": np.zeros((nr, 6), np.float32),
+               "aabbs": np.zeros((na, 6), np.float32)}
+        if nn:
+            L.aeref_get_nodes(h, out["nodes"].ctypes.data)
+        if nd:
+            L.aeref_get_data(h, out["data_verts"].ctypes.data, out["data_idx"].ctypes.data, out["data_eon"].ctypes.data)
+        if nr:
+            L.aeref_get_refs_full(h, out["refs_idx"].ctypes.data, out["refs_node"].ctypes.data,
+                                  out["refs_eon"].ctypes.data, out["refs_aabb"].ctypes.data)
+        if na:
+            L.aeref_get_aabbs(h, out["aabbs"].ctypes.data)
+        return out
+    finally:
+        L.aeref_free(h)
 
 
 def ref_build_aabbs(boxes, parallel=True):

@@ -131,6 +131,30 @@ void aeref_get_refs(void* h, uint32_t* idx) {
     for (size_t i = 0; i < refs.size(); i++) idx[i] = refs[i].idx;
 }
 
+// Every field of BVH::refs (BVHBuilder::Ref, BVH.h): idx, nodeIdx, endOfNode
+// and the reference box (min, max) per reference, in list order.
+void aeref_get_refs_full(void* h, uint32_t* idx, uint32_t* node_idx, uint8_t* end_of_node, float* aabb) {
+    auto& refs = static_cast<Volume::BVH*>(h)->refs;
+    for (size_t i = 0; i < refs.size(); i++) {
+        idx[i] = refs[i].idx;
+        node_idx[i] = refs[i].nodeIdx;
+        end_of_node[i] = refs[i].endOfNode ? 1 : 0;
+        const float f[6] = { refs[i].aabb.min.x, refs[i].aabb.min.y, refs[i].aabb.min.z,
+                             refs[i].aabb.max.x, refs[i].aabb.max.y, refs[i].aabb.max.z };
+        std::memcpy(aabb + i * 6, f, sizeof(f));
+    }
+}
+
+// BVH::aabbs (min, max per entry), in list order.
+uint32_t aeref_aabbs_count(void* h) { return uint32_t(static_cast<Volume::BVH*>(h)->aabbs.size()); }
+void aeref_get_aabbs(void* h, float* out) {
+    auto& a = static_cast<Volume::BVH*>(h)->aabbs;
+    for (size_t i = 0; i < a.size(); i++) {
+        const float f[6] = { a[i].min.x, a[i].min.y, a[i].min.z, a[i].max.x, a[i].max.y, a[i].max.z };
+        std::memcpy(out + i * 6, f, sizeof(f));
+    }
+}
+
 // Closest-hit host query over a batch of rays on `threads` std::threads.
 // rays: n * 8 floats (origin.xyz, dir.xyz, tMin, tMax).
 // Outputs per ray: orig_idx = data[closestPtr].idx, or -1 when the hit test
