@@ -53,6 +53,17 @@ class CastOutputs(C.Structure):
                 ("shadow_rays", P), ("shadow_occluded", P), ("counts", U32 * 3)]
 
 
+class MeshAssetInfo(C.Structure):
+    _fields_ = [("vertex_count", U32), ("index_count", U32), ("triangle_count", U32), ("sub_count", U32),
+                ("material_count", U32), ("tex_coord_count", U32), ("normal_count", U32), ("tangent_count", U32),
+                ("color_count", U32), ("cull_back_faces", I32), ("invert_uvs", I32), ("cast_shadow", I32),
+                ("primitive_type", I32), ("mobility", I32), ("usage", I32), ("radius", F32), ("aabb", F32 * 6)]
+
+
+class MeshSub(C.Structure):
+    _fields_ = [("indices_offset", U32), ("indices_count", U32), ("material_idx", I32), ("aabb", F32 * 6)]
+
+
 class PtParams(C.Structure):
     _fields_ = [("spp", U32), ("max_bounces", U32), ("sample_offset", U32), ("seed", U32),
                 ("epsilon", F32), ("flags", U32), ("reserved", U32 * 2)]
@@ -95,6 +106,22 @@ _SIGNATURES = [
     ("ae_bvh_pack_shading", C.c_int, [P, P, P, P, P, P]),
     ("ae_bvh_pack_uvs", C.c_int, [P, P, P]),
     ("ae_bvh_pack_attributes", C.c_int, [P, P, P, P, P, P]),
+    ("ae_asset_last_error", C.c_char_p, []),
+    ("ae_mesh_asset_load", C.c_int, [P, C.c_size_t, C.POINTER(P)]),
+    ("ae_mesh_asset_load_file", C.c_int, [C.c_char_p, C.POINTER(P)]),
+    ("ae_mesh_asset_destroy", None, [P]),
+    ("ae_mesh_asset_get_info", C.c_int, [P, C.POINTER(MeshAssetInfo)]),
+    ("ae_mesh_asset_name", C.c_char_p, [P]),
+    ("ae_mesh_asset_material_path", C.c_char_p, [P, U32]),
+    ("ae_mesh_asset_get_sub", C.c_int, [P, U32, C.POINTER(MeshSub)]),
+    ("ae_mesh_asset_get_arrays", C.c_int, [P, P, P, P, P, P, P]),
+    ("ae_mesh_asset_triangles", C.c_int, [P, P, U32, P, P, P, P, P, P]),
+    ("ae_material_asset_load", C.c_int, [P, C.c_size_t, C.POINTER(P)]),
+    ("ae_material_asset_load_file", C.c_int, [C.c_char_p, C.POINTER(P)]),
+    ("ae_material_asset_destroy", None, [P]),
+    ("ae_material_asset_name", C.c_char_p, [P]),
+    ("ae_material_asset_map_path", C.c_char_p, [P, U32]),
+    ("ae_material_asset_to_gpu", C.c_int, [P, P, P, I32, P]),
     ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     ("ae_rt_ctx_destroy", None, [P]),
     ("ae_rt_last_error", C.c_char_p, [P]),

@@ -228,6 +228,111 @@ ae_rt_status ae_bvh_pack_attributes(const ae_bvh* bvh, const float* verts, const
                                     const float* colors, ae_triangle* inout);
 
 /* ------------------------------------------------------------------------ */
+/* Engine assets: .aemesh and .aematerial                                    */
+/* ------------------------------------------------------------------------ */
+
+/* A mesh file as Loader::MeshLoader::LoadMesh reads it
+ * (src/engine/loader/MeshLoader.cpp:6-36; layout MeshSerializer.cpp:7-134):
+ * the MessagePack document the engine's importer saves (binaryJson = true)
+ * or the same document as JSON text.  Per-vertex components keep their file
+ * form: vertices 3 floats, texCoords 2, normals / tangents / colors 4. */
+typedef struct ae_mesh_asset ae_mesh_asset;
+
+typedef struct ae_mesh_asset_info {
+    uint32_t vertex_count;     /* elements of each component actually present */
+    uint32_t index_count;
+    uint32_t triangle_count;   /* sum over sub-meshes of indicesCount / 3 (MeshData.cpp:91-93) */
+    uint32_t sub_count;
+    uint32_t material_count;   /* material paths in the file */
+    uint32_t tex_coord_count;
+    uint32_t normal_count;
+    uint32_t tangent_count;
+    uint32_t color_count;
+    int32_t cull_back_faces;   /* Mesh::cullBackFaces */
+    int32_t invert_uvs;        /* Mesh::invertUVs */
+    int32_t cast_shadow;
+    int32_t primitive_type;
+    int32_t mobility;
+    int32_t usage;
+    float radius;
+    float aabb[6];             /* min, max */
+} ae_mesh_asset_info;
+
+/* MeshSubData (MeshSerializer.cpp:136-156) */
+typedef struct ae_mesh_sub {
+    uint32_t indices_offset;
+    uint32_t indices_count;
+    int32_t material_idx;
+    float aabb[6];
+} ae_mesh_sub;
+
+/* Message of the last failed asset call on this thread ("" when none). */
+const char* ae_asset_last_error(void);
+
+/* Decodes a mesh document (size bytes, MessagePack or JSON text).  A
+ * malformed, truncated or incomplete document is AE_RT_INVALID_ARG with a
+ * message; the reference throws from nlohmann::json there. */
+ae_rt_status ae_mesh_asset_load(const void* bytes, size_t size, ae_mesh_asset** out);
+ae_rt_status ae_mesh_asset_load_file(const char* path, ae_mesh_asset** out);
+void ae_mesh_asset_destroy(ae_mesh_asset* asset);
+ae_rt_status ae_mesh_asset_get_info(const ae_mesh_asset* asset, ae_mesh_asset_info* info);
+const char* ae_mesh_asset_name(const ae_mesh_asset* asset);
+/* The i-th material path (MeshSerializer.cpp:89-93), NULL past the end. */
+const char* ae_mesh_asset_material_path(const ae_mesh_asset* asset, uint32_t i);
+ae_rt_status ae_mesh_asset_get_sub(const ae_mesh_asset* asset, uint32_t i, ae_mesh_sub* out);
+/* Copies the components out (any pointer may be NULL); sizes from
+ * ae_mesh_asset_info. */
+ae_rt_status ae_mesh_asset_get_arrays(const ae_mesh_asset* asset, uint32_t* indices, float* vertices,
+                                      float* tex_coords, float* normals, float* tangents, float* colors);
+
+/* MeshData::BuildBVH's triangle assembly (MeshData.cpp:89-155): triangle k
+ * (counted over the sub-meshes in order) takes indices 3k .. 3k + 2; per
+ * triangle verts (9 floats), normals (9: the file's xyz, which the shading
+ * packer normalises; engine files store w = 0), uvs (6; 0 without
+ * texCoords), colors (12; 1.0 without colors), material (the sub-mesh's
+ * materialIdx) and opacity (-1 where materials[materialIdx] has an opacity
+ * texture, else its opacity; 1.0 with no material table).  Every index is
+ * checked against the component buffers first: out-of-range input is
+ * AE_RT_INVALID_ARG, where the reference reads past its arrays.  Any output
+ * may be NULL.  The outputs feed ae_bvh_build_triangles, ae_bvh_pack_triangles,
+ * ae_bvh_pack_shading and ae_bvh_pack_attributes in that order. */
+ae_rt_status ae_mesh_asset_triangles(const ae_mesh_asset* asset, const ae_material* materials, uint32_t n_materials,
+                                     float* verts, float* normals, float* uvs, float* colors, int32_t* material,
+                                     float* opacity);
+
+/* A material file (JSON text, Material from_json, MeshSerializer.cpp:212-256). */
+typedef struct ae_material_asset ae_material_asset;
+
+/* Texture slots of a material, in GPUMaterial's order */
+#define AE_MAP_BASE_COLOR   0u
+#define AE_MAP_OPACITY      1u
+#define AE_MAP_NORMAL       2u
+#define AE_MAP_ROUGHNESS    3u
+#define AE_MAP_METALNESS    4u
+#define AE_MAP_AO           5u
+#define AE_MAP_DISPLACEMENT 6u
+
+ae_rt_status ae_material_asset_load(const void* bytes, size_t size, ae_material_asset** out);
+ae_rt_status ae_material_asset_load_file(const char* path, ae_material_asset** out);
+void ae_material_asset_destroy(ae_material_asset* material);
+const char* ae_material_asset_name(const ae_material_asset* material);
+/* The texture path of one AE_MAP_* slot ("" when the material has none). */
+const char* ae_material_asset_map_path(const ae_material_asset* material, uint32_t which);
+
+/* GPUMaterial of this material the way RayTracingWorld::UpdateMaterials
+ * fills it (RayTracingWorld.cpp:186-240): baseColor = pow(c, 2.2),
+ * emissiveColor = pow(c, 2.2) * emissiveIntensity (ColorConverter.h:18-23),
+ * opacity / roughness / metalness / ao / reflectance / normalScale /
+ * twoSided / useVertexColors from the material, invertUVs and cullBackFaces
+ * from `mesh` (NULL: 0).  texture_ids (6 entries in AE_MAP_* order, or
+ * NULL) are the texture-table indices the caller gave the material's maps
+ * (the engine's textureToBindlessIdx); a slot without a map, or with a
+ * negative id, is -1.  ID is the caller's `id` (the engine hashes its mesh
+ * id there). */
+ae_rt_status ae_material_asset_to_gpu(const ae_material_asset* material, const ae_mesh_asset* mesh,
+                                      const int32_t* texture_ids, int32_t id, ae_material* out);
+
+/* ------------------------------------------------------------------------ */
 /* Device context                                                            */
 /* ------------------------------------------------------------------------ */
 
