@@ -107,6 +107,11 @@ _SIGNATURES = [
     ("ae_bvh_pack_uvs", C.c_int, [P, P, P]),
     ("ae_bvh_pack_attributes", C.c_int, [P, P, P, P, P, P]),
     ("ae_asset_last_error", C.c_char_p, []),
+    ("ae_lights_from_mesh", C.c_int, [P, U32, P, P, U32, P, U32, C.POINTER(U32)]),
+    ("ae_lights_instance", C.c_int, [P, U32, P, I32, P]),
+    ("ae_light_directional", C.c_int, [P, F32, P, U32, P]),
+    ("ae_lights_normalize", C.c_int, [P, U32]),
+    ("ae_lights_select", C.c_int, [P, U32, U32, P, P, C.POINTER(U32)]),
     ("ae_mesh_asset_load", C.c_int, [P, C.c_size_t, C.POINTER(P)]),
     ("ae_mesh_asset_load_file", C.c_int, [C.c_char_p, C.POINTER(P)]),
     ("ae_mesh_asset_destroy", None, [P]),

@@ -621,6 +621,54 @@ typedef struct ae_texture {
 ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n);
 ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n);
 
+/* The light list the engine builds on the host before each path-tracing
+ * dispatch.  Arithmetic follows the reference in float32, operation by
+ * operation; pow is the C library's powf, as glm::pow calls it.
+ *
+ * ae_lights_from_mesh: RayTracingWorld::BuildTriangleLightsForMesh
+ * (RayTracingWorld.cpp:322-376).  One GPULight per triangle of `shading` (the
+ * mesh's GPUTriangle array, BVH order) whose material (d0.w, an index into
+ * the mesh's materials) has brightness = dot(pow(emissive, 2.2), 0.3333) > 0:
+ * P = the vertex mean, N = the mean of the unpacked 10:10:10:2 vertex normals
+ * (not normalised), area by Heron's formula, colour = pow(pow(emissive, 2.2),
+ * 2.2) * emissiveIntensity (the reference converts twice), data = (type 1 |
+ * triangle index, area * brightness, area, 0).  emissive_srgb (3 floats per
+ * material) and emissive_intensity are the engine Material's sRGB
+ * emissiveColor and emissiveIntensity.  *n_out = the number of emissive
+ * triangles; out may be NULL to count them; more than `capacity` fills
+ * `capacity` and returns AE_RT_OUT_OF_MEMORY. */
+ae_rt_status ae_lights_from_mesh(const ae_triangle* shading, uint32_t n_tris, const float* emissive_srgb,
+                                 const float* emissive_intensity, uint32_t n_materials, ae_light* out,
+                                 uint32_t capacity, uint32_t* n_out);
+
+/* RayTracingWorld::UpdateTriangleLights (RayTracingWorld.cpp:378-407): a
+ * mesh's lights placed by one instance.  P = model * (P, 1), N = model *
+ * (N, 0) with `model` the 4 x 4 world matrix in row-major order (glm's
+ * pairwise column sum), data.w = the instance index bits. */
+ae_rt_status ae_lights_instance(const ae_light* mesh_lights, uint32_t n, const float* model, int32_t instance,
+                                ae_light* out);
+
+/* The directional branch of RayTracingHelper::UpdateLights
+ * (RayTracingHelper.cpp:440-474): colour = pow(color, 2.2) * intensity,
+ * N = direction (the light travels along it), data = (type 0 | index,
+ * brightness, 0, 0). */
+ae_rt_status ae_light_directional(const float color_srgb[3], float intensity, const float direction[3],
+                                  uint32_t index, ae_light* out);
+
+/* UpdateLights' weights (RayTracingHelper.cpp:481-499): data.y raised to at
+ * least 0.005 x the largest, then divided by their sum. */
+ae_rt_status ae_lights_normalize(ae_light* lights, uint32_t n);
+
+/* DispatchAndHit's selection (RayTracingHelper.cpp:72-105): when n <=
+ * capacity (the engine's light buffer holds 128), every light with data.y =
+ * 1; otherwise `capacity` draws with replacement from the piecewise-constant
+ * distribution over data.y (Common::Piecewise1D, Piecewise.cpp:11-78, one
+ * draw per entry of `uniforms`, each in [0, 1)), each drawn light's data.y
+ * multiplied by capacity.  The engine draws from an unseeded std::mt19937;
+ * the caller supplies the uniforms here.  *n_out = min(n, capacity). */
+ae_rt_status ae_lights_select(const ae_light* lights, uint32_t n, uint32_t capacity, const float* uniforms,
+                              ae_light* out, uint32_t* n_out);
+
 typedef struct ae_pt_params {
     uint32_t spp;            /* samples per pixel in this call */
     uint32_t max_bounces;    /* the engine's `bounces`: bounces + 1 hit evaluations */

@@ -594,3 +594,126 @@ def pass_ddgi(scene, probes, ray_dirs, rotation, out, ray_dirs_inactive=None, in
     assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == len(probes) * len(dirs) * 4
     _pass_fns().aeo_pass_ddgi(C.byref(s), C.byref(d), C.byref(_pass_params(**params)), threads, out.ctypes.data)
     return out
+
+
+# ---------------------------------------------------------------------------
+# The engine's host light list (numpy restatement, float32 operation by operation)
+# ---------------------------------------------------------------------------
+
+def _srgb_to_linear(c):
+    """ColorConverter::ConvertSRGBToLinear (common/ColorConverter.h:18-23):
+    pow(c, 2.2) in float32, rounded once as the C library's powf rounds."""
+    return (np.asarray(c, np.float32).astype(np.float64) ** np.float64(np.float32(2.2))).astype(np.float32)
+
+
+def _dot3(a, b):
+    """glm dot of vec3: (x*x' + y*y') + z*z' in float32."""
+    p = (np.asarray(a, np.float32) * np.asarray(b, np.float32)).astype(np.float32)
+    return ((p[..., 0] + p[..., 1]) + p[..., 2]).astype(np.float32)
+
+
+def _unpack10(bits):
+    """Common::Packing::UnpackSignedVector3x10_1x2 (common/Packing.cpp:37-48), xyz."""
+    c = np.asarray(bits, np.float32).view(np.int32)
+    f32 = np.float32
+    return np.stack([((c >> s) & 1023).astype(f32) / f32(1023.0) * f32(2.0) - f32(1.0) for s in (0, 10, 20)], -1)
+
+
+def triangle_lights(shading, emissive_srgb, emissive_intensity):
+    """RayTracingWorld::BuildTriangleLightsForMesh (RayTracingWorld.cpp:322-376)
+    over a GPUTriangle array (n, 24) float32: GPULight records (m, 16)."""
+    f32 = np.float32
+    sh = np.asarray(shading, f32).reshape(-1, 24)
+    mat = sh[:, 15].view(np.int32)
+    rad = _srgb_to_linear(np.asarray(emissive_srgb, f32).reshape(-1, 3))[mat]
+    bright = _dot3(rad, np.full(3, 0.3333, f32))
+    keep = np.nonzero(bright > 0)[0]
+    out = np.zeros((len(keep), 16), f32)
+    for k, i in enumerate(keep):
+        t = sh[i]
+        v0, v1, v2 = t[0:3], t[4:7], t[8:11]
+        n = _unpack10(np.array([t[3], t[7], t[11]], f32))
+        P = ((v0 + v1) + v2) / f32(3.0)
+        N = ((n[0] + n[1]) + n[2]) / f32(3.0)
+        dist = lambda a, b: np.sqrt(_dot3(a - b, a - b))   # noqa: E731
+        a, b, c = dist(v1, v0), dist(v2, v0), dist(v1, v2)
+        p = f32(0.5) * ((a + b) + c)
+        area = np.sqrt(((p * (p - a)) * (p - b)) * (p - c))
+        color = _srgb_to_linear(rad[i]) * f32(np.asarray(emissive_intensity, f32)[mat[i]])
+        out[k, 0:3], out[k, 3] = P, 1.0
+        out[k, 4:7] = N
+        out[k, 8:11] = color
+        out[k, 12] = np.uint32((1 << 28) | int(i)).view(f32)
+        out[k, 13] = area * bright[i]
+        out[k, 14] = area
+    return out
+
+
+def lights_instance(lights, model, instance):
+    """RayTracingWorld::UpdateTriangleLights (:378-407): P = M (P, 1), N = M (N, 0)
+    with glm's pairwise column sum, data.w = the instance bits."""
+    f32 = np.float32
+    L = np.asarray(lights, f32).reshape(-1, 16).copy()
+    M = np.asarray(model, f32).reshape(4, 4)
+    for v, w in ((slice(0, 3), f32(1.0)), (slice(4, 7), f32(0.0))):
+        x = L[:, v].copy()
+        for r in range(3):
+            m = M[r]
+            L[:, v.start + r] = (m[0] * x[:, 0] + m[1] * x[:, 1]) + (m[2] * x[:, 2] + m[3] * w)
+    L[:, 15] = np.int32(instance).view(f32)
+    return L
+
+
+def lights_normalize(lights):
+    """RayTracingHelper::UpdateLights' weights (RayTracingHelper.cpp:481-499)."""
+    f32 = np.float32
+    L = np.asarray(lights, f32).reshape(-1, 16).copy()
+    w = L[:, 13]
+    mx = f32(0.0)
+    for x in w:
+        mx = max(mx, x)
+    mn = f32(0.005) * mx
+    total = f32(0.0)
+    for k in range(len(w)):
+        w[k] = max(w[k], mn)
+        total = f32(total + w[k])
+    L[:, 13] = w / total
+    return L
+
+
+def lights_select(lights, capacity, uniforms):
+    """DispatchAndHit's selection (RayTracingHelper.cpp:72-105) with
+    Common::Piecewise1D (Piecewise.cpp:11-78) on the given uniforms."""
+    f32 = np.float32
+    L = np.asarray(lights, f32).reshape(-1, 16)
+    n = len(L)
+    if n <= capacity:
+        out = L.copy()
+        out[:, 13] = 1.0
+        return out
+    cdf = np.zeros(n + 1, f32)
+    s = f32(0.0)
+    for k in range(n):
+        cdf[k] = s
+        s = f32(s + f32(L[k, 13] / f32(n)))
+    cdf[n] = s
+    cdf = (cdf / s).astype(f32)
+    out = np.zeros((capacity, 16), f32)
+    for j in range(capacity):
+        x = f32(uniforms[j])
+        lo, hi, found = 0, n, -1
+        while lo <= hi:
+            m = lo + (hi - lo) // 2
+            k = m if m + 1 > n else m + 1
+            if cdf[m] <= x <= cdf[k]:
+                found = m
+                break
+            if cdf[m] < x:
+                lo = m + 1
+            else:
+                hi = m - 1
+        if found < 0 or found >= n:
+            found = n - 1
+        out[j] = L[found]
+        out[j, 13] = L[found, 13] * f32(capacity)
+    return out
