@@ -22,6 +22,7 @@ import ctypes as C
 import numpy as np
 
 from ._native import (AeRtError, BatchDesc, BounceParams, Camera, CastOutputs, Config, DdgiProbes, GBuffer, PassParams,
+                      PtRealtime,
                       PtParams, RcConfig, lib)
 
 NODE_DTYPE = np.dtype([("leftMin", "<f4", 3), ("leftMax", "<f4", 3),
@@ -48,6 +49,9 @@ HIT_FLAG_RETESTED = 0x10
 HIT64_DTYPE = np.dtype([("t", "<f8"), ("t_second", "<f8"), ("triPtr", "<i4"), ("flags", "<u4"),
                         ("reserved", "<i4", (2,))])
 assert HIT64_DTYPE.itemsize == 32
+
+PT_MIS = 0x1
+PT_CENTERED = 0x2
 
 MASK_ALL = 1 << 7
 MASK_SHADOW = 1 << 6
@@ -448,23 +452,50 @@ class Context:
         _check(lib().ae_rt_scene_set_lights(self._h, _ptr(lights) if len(lights) else None, len(lights)),
                self._h)
 
-    def pathtrace(self, cam: "Camera", accum, accum64=None, spp=1, max_bounces=3, sample_offset=0, seed=1,
-                  epsilon=0.1, mis=False, stream=None):
+    @staticmethod
+    def _pt_params(spp, max_bounces, sample_offset, seed, epsilon, mis, centered=False):
         p = PtParams()
         p.spp, p.max_bounces, p.sample_offset, p.seed, p.epsilon = spp, max_bounces, sample_offset, seed, epsilon
-        p.flags = 1 if mis else 0
-        _check(lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
-                                     _stream_handle(stream)), self._h)
+        p.flags = (PT_MIS if mis else 0) | (PT_CENTERED if centered else 0)
+        return p
+
+    def pathtrace(self, cam: "Camera", accum, accum64=None, spp=1, max_bounces=3, sample_offset=0, seed=1,
+                  epsilon=0.1, mis=False, centered=False, tile=None, stream=None):
+        """ae_rt_pathtrace (whole image) or, with tile = (x0, y0, w, h),
+        ae_rt_pathtrace_tile: accumulates into the whole-image buffers."""
+        p = self._pt_params(spp, max_bounces, sample_offset, seed, epsilon, mis, centered)
+        if tile is None:
+            st = lib().ae_rt_pathtrace(self._h, C.byref(cam), C.byref(p), _ptr(accum), _ptr(accum64),
+                                       _stream_handle(stream))
+        else:
+            x0, y0, w, h = (int(v) for v in tile)
+            st = lib().ae_rt_pathtrace_tile(self._h, C.byref(cam), C.byref(p), x0, y0, w, h, _ptr(accum),
+                                            _ptr(accum64), _stream_handle(stream))
+        _check(st, self._h)
 
     def pathtrace_realtime(self, cam: "Camera", frame_accum, max_radiance=0.0, spp=1, max_bounces=3,
-                           sample_offset=0, seed=1, epsilon=0.1, mis=False, stream=None):
+                           sample_offset=0, seed=1, epsilon=0.1, mis=False, gbuffer=None, stream=None):
         """ae_rt_pathtrace_realtime: the engine's real-time accumulation into
         frame_accum, a (3, h, w) 32-bit device tensor (float bits at spp = 1,
-        quantised unsigned sums at spp > 1)."""
-        p = PtParams()
-        p.spp, p.max_bounces, p.sample_offset, p.seed, p.epsilon = spp, max_bounces, sample_offset, seed, epsilon
-        p.flags = 1 if mis else 0
-        _check(lib().ae_rt_pathtrace_realtime(self._h, C.byref(cam), C.byref(p), _ptr(frame_accum), max_radiance,
+        quantised unsigned sums at spp > 1).  gbuffer: a dict with any of the
+        device planes depth / material_idx / normal / velocity and the
+        matrices view / proj / pv_last (4 x 4) and last_matrices ((n, 3, 4))."""
+        p = self._pt_params(spp, max_bounces, sample_offset, seed, epsilon, mis)
+        rt = None
+        keep = []
+        if gbuffer is not None:
+            rt = PtRealtime()
+            for k in ("depth", "material_idx", "normal", "velocity"):
+                setattr(rt, k, _ptr(gbuffer.get(k)))
+            for k in ("view", "proj", "pv_last"):
+                m = np.ascontiguousarray(gbuffer.get(k, np.eye(4)), np.float32).reshape(16)
+                getattr(rt, k)[:] = m.tolist()
+            if gbuffer.get("last_matrices") is not None:
+                lm = np.ascontiguousarray(gbuffer["last_matrices"], np.float32).reshape(-1, 12)
+                keep.append(lm)
+                rt.last_matrices, rt.n_last_matrices = _ptr(lm), len(lm)
+        _check(lib().ae_rt_pathtrace_realtime(self._h, C.byref(cam), C.byref(p),
+                                              None if rt is None else C.byref(rt), _ptr(frame_accum), max_radiance,
                                               _stream_handle(stream)), self._h)
 
     def tonemap(self, accum, width: int, height: int, samples: int, exposure: float, gamma: float, out,

@@ -64,6 +64,11 @@ class MeshSub(C.Structure):
     _fields_ = [("indices_offset", U32), ("indices_count", U32), ("material_idx", I32), ("aabb", F32 * 6)]
 
 
+class PtRealtime(C.Structure):
+    _fields_ = [("depth", P), ("material_idx", P), ("normal", P), ("velocity", P), ("view", F32 * 16),
+                ("proj", F32 * 16), ("pv_last", F32 * 16), ("last_matrices", P), ("n_last_matrices", U32)]
+
+
 class PtParams(C.Structure):
     _fields_ = [("spp", U32), ("max_bounces", U32), ("sample_offset", U32), ("seed", U32),
                 ("epsilon", F32), ("flags", U32), ("reserved", U32 * 2)]
@@ -153,7 +158,8 @@ _SIGNATURES = [
     ("ae_rt_scene_set_textures", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
-    ("ae_rt_pathtrace_realtime", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, F32, P]),
+    ("ae_rt_pathtrace_tile", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), U32, U32, U32, U32, P, P, P]),
+    ("ae_rt_pathtrace_realtime", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, F32, P]),
     ("ae_rt_pt_tonemap", C.c_int, [P, P, U32, U32, U32, F32, F32, P, P]),
     ("ae_rt_rtao", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),
     ("ae_rt_reflections", C.c_int, [P, C.POINTER(GBuffer), C.POINTER(PassParams), P, P]),

@@ -874,9 +874,26 @@ namespace {
 // The path tracer's sample loop (ae_rt_pathtrace / ae_rt_pathtrace_realtime):
 // radiance into accum (+ accum64), or, with frame_accum, into the real-time
 // [3][H][W] uint32 frame accumulation.
-ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
-                       double* accum64, uint32_t* frame_accum, float max_radiance, void* stream) {
+// What one path-tracing call writes: the non-real-time accumulation (accum,
+// accum64) or the real-time frame image (frame_accum) and G-buffer (rt), over
+// the whole image or one tile of it.
+struct PtCall {
+    float* accum = nullptr;
+    double* accum64 = nullptr;
+    uint32_t* frame_accum = nullptr;
+    float max_radiance = 0.0f;
+    const ae_pt_realtime* rt = nullptr;
+    bool tiled = false;
+    uint32_t x0 = 0, y0 = 0, w = 0, h = 0;
+};
+
+ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, const PtCall& call,
+                       void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
+    float* const accum = call.accum;
+    double* const accum64 = call.accum64;
+    uint32_t* const frame_accum = call.frame_accum;
+    const float max_radiance = call.max_radiance;
     if (!cam || !params || (!accum && !frame_accum)) return Fail(ctx, AE_RT_INVALID_ARG, "null argument");
     if (!ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
     if (!ctx->d_materials) return Fail(ctx, AE_RT_INVALID_ARG, "no materials have been set");
@@ -889,9 +906,22 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
         return Fail(ctx, AE_RT_INVALID_ARG, "accumulation buffers must be device memory");
     if (frame_accum && !(max_radiance > 0.0f) && params->spp > 1)
         return Fail(ctx, AE_RT_INVALID_ARG, "the quantised real-time accumulation needs max_radiance > 0");
+    const uint32_t tx0 = call.tiled ? call.x0 : 0u, ty0 = call.tiled ? call.y0 : 0u;
+    const uint32_t tw = call.tiled ? call.w : cam->width, th = call.tiled ? call.h : cam->height;
+    if (tw == 0 || th == 0 || tx0 > cam->width - tw || ty0 > cam->height - th || tw > cam->width || th > cam->height)
+        return Fail(ctx, AE_RT_INVALID_ARG, "the tile does not lie inside the image");
+    const ae_pt_realtime* rt = call.rt;
+    if (rt) {
+        const void* outs[4] = { rt->depth, rt->material_idx, rt->normal, rt->velocity };
+        for (const void* o : outs)
+            if (o && !IsDevicePointer(o)) return Fail(ctx, AE_RT_INVALID_ARG, "G-buffer planes must be device memory");
+        if (rt->last_matrices && rt->n_last_matrices != ctx->n_instances)
+            return Fail(ctx, AE_RT_INVALID_ARG, "last_matrices must hold one matrix per scene instance");
+    }
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t n = cam->width * cam->height;
+    const uint32_t n_tile = tw * th;
     ae_rt_status qs = EnsureBounceQueues(ctx, n);
     if (qs != AE_RT_OK) return qs;
 
@@ -934,7 +964,32 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
     p.hits_in = static_cast<const float4*>(ctx->pt_hits.ptr);
     p.accum = reinterpret_cast<float4*>(accum);
     p.accum64 = accum64;
-    const uint32_t blocks = (n + 255) / 256;
+    p.tile_x0 = tx0;
+    p.tile_y0 = ty0;
+    p.tile_w = tw;
+    p.tile_h = th;
+    p.centered = (frame_accum || (params->flags & AE_PT_CENTERED)) ? 1u : 0u;
+    p.jitter_x = cam->jitter[0];
+    p.jitter_y = cam->jitter[1];
+    if (rt && (rt->depth || rt->material_idx || rt->normal || rt->velocity)) {
+        // view, projection and last view-projection rows, then the previous
+        // object-to-world rows of every instance
+        std::vector<float> m(48 + (rt->last_matrices ? size_t(ctx->n_instances) * 12 : 0));
+        std::memcpy(m.data(), rt->view, 16 * sizeof(float));
+        std::memcpy(m.data() + 16, rt->proj, 16 * sizeof(float));
+        std::memcpy(m.data() + 32, rt->pv_last, 16 * sizeof(float));
+        if (rt->last_matrices) std::memcpy(m.data() + 48, rt->last_matrices, size_t(ctx->n_instances) * 12 * sizeof(float));
+        AE_CUDA(ctx, ctx->pt_gb.ensure(m.size() * sizeof(float)));
+        AE_CUDA(ctx, cudaMemcpyAsync(ctx->pt_gb.ptr, m.data(), m.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        p.gb_depth = rt->depth;
+        p.gb_material = rt->material_idx;
+        p.gb_normal = reinterpret_cast<float2*>(rt->normal);
+        p.gb_velocity = reinterpret_cast<float2*>(rt->velocity);
+        p.gb_mats = static_cast<const float4*>(ctx->pt_gb.ptr);
+        p.gb_last_model = rt->last_matrices ? static_cast<const float4*>(ctx->pt_gb.ptr) + 12 : nullptr;
+    }
+    // every queue holds at most one ray per pixel of the tile
+    const uint32_t blocks = (n_tile + 255) / 256;
     const float kInf = 1e12f;   // INF of common.hsh:8
     // Shadow queues alternate between two buffers: a bounce's shadow trace and
     // resolve run on the side stream while the next bounce is traced and shaded
@@ -948,6 +1003,7 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
     bool pending[2] = { false, false };
     for (uint32_t smp = 0; smp < params->spp; smp++) {
         p.sample = params->sample_offset + smp;
+        p.gb_write = (smp == 0 && p.gb_mats) ? 1u : 0u;
         // ray generation into queue 0
         p.rays_out = static_cast<float4*>(ctx->pt_rays[0].ptr);
         p.pay_out = static_cast<float4*>(ctx->pt_pay[0].ptr);
@@ -1001,13 +1057,36 @@ extern "C" {
 ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
                              double* accum64, void* stream) {
     if (ctx && !accum) return Fail(ctx, AE_RT_INVALID_ARG, "null accumulation buffer");
-    return PathTrace(ctx, cam, params, accum, accum64, nullptr, 0.0f, stream);
+    PtCall call;
+    call.accum = accum;
+    call.accum64 = accum64;
+    return PathTrace(ctx, cam, params, call, stream);
+}
+
+ae_rt_status ae_rt_pathtrace_tile(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, uint32_t x0,
+                                  uint32_t y0, uint32_t width, uint32_t height, float* accum, double* accum64,
+                                  void* stream) {
+    if (ctx && !accum) return Fail(ctx, AE_RT_INVALID_ARG, "null accumulation buffer");
+    PtCall call;
+    call.accum = accum;
+    call.accum64 = accum64;
+    call.tiled = true;
+    call.x0 = x0;
+    call.y0 = y0;
+    call.w = width;
+    call.h = height;
+    return PathTrace(ctx, cam, params, call, stream);
 }
 
 ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params,
-                                      uint32_t* frame_accum, float max_radiance, void* stream) {
+                                      const ae_pt_realtime* rt, uint32_t* frame_accum, float max_radiance,
+                                      void* stream) {
     if (ctx && !frame_accum) return Fail(ctx, AE_RT_INVALID_ARG, "null frame accumulation buffer");
-    return PathTrace(ctx, cam, params, nullptr, nullptr, frame_accum, max_radiance, stream);
+    PtCall call;
+    call.frame_accum = frame_accum;
+    call.max_radiance = max_radiance;
+    call.rt = rt;
+    return PathTrace(ctx, cam, params, call, stream);
 }
 
 ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,

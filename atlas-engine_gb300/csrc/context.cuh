@@ -75,6 +75,7 @@ struct ae_rt_ctx {
     uint32_t n_lights = 0;
     // path tracer queues
     atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
+    atlas::rt::host::Scratch pt_gb;     // real-time G-buffer matrices
     // a second shadow queue: a bounce's shadow trace runs beside the next bounce's trace
     atlas::rt::host::Scratch pt_shadow2, pt_shadow_pay2, pt_occ2;
     cudaEvent_t pt_events[4] = { nullptr, nullptr, nullptr, nullptr };

@@ -82,6 +82,21 @@ struct PtParams {
     uint32_t* frame_accum;
     float rt_max_radiance;
     uint32_t rt_max_per_sample;   // 0: one sample per frame, float bits
+    // primary rays: the pixels of one tile (pixelOffset / tileSize of
+    // rayGen.csh:27-30); centred = through pixel centres + jitter * 0.25 as the
+    // real-time ray generation does (rayGen.csh:37-38), else a random sub-pixel offset
+    uint32_t tile_x0, tile_y0, tile_w, tile_h;
+    uint32_t centered;
+    float jitter_x, jitter_y;
+    // real-time G-buffer of the frame's first sample (rayHit.csh:76-116),
+    // written by the bounce-0 shading when gb_write is set
+    uint32_t gb_write;
+    float* gb_depth;              // view-space z of the hit, INF on a miss
+    uint32_t* gb_material;        // GPUMaterial.ID, 65535 on a miss
+    float2* gb_normal;            // EncodeNormal(geometry normal)
+    float2* gb_velocity;          // (ndc last - ndc current) * 0.5
+    const float4* gb_mats;        // rows of the view, projection and last view-projection matrices
+    const float4* gb_last_model;  // previous object-to-world rows per instance; null: the current ones
 };
 
 // Pixel keys carried by rays and payloads: the pixel index in the low 24
@@ -121,6 +136,7 @@ __device__ __forceinline__ float rng(uint32_t pixel, uint32_t sample, uint32_t b
 }
 
 struct Mat {
+    int id;                     // GPUMaterial.ID
     V3 base, emissive;
     float opacity, roughness, metalness, ao, reflectance, normalScale;
     int twoSided, cullBackFaces, invertUVs, useVertexColors;
@@ -129,6 +145,7 @@ struct Mat {
 
 __device__ __forceinline__ Mat load_material(const float* m) {
     Mat r;
+    r.id = __float_as_int(m[0]);
     r.base = v3(m[1], m[2], m[3]);
     r.emissive = v3(m[4], m[5], m[6]);
     r.opacity = m[7];
@@ -327,12 +344,20 @@ __device__ __forceinline__ Light load_light(const float4* l) {
 
 static __global__ void pt_raygen_kernel(CameraParams c, PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = c.width * c.height;
+    const uint32_t n = p.tile_w * p.tile_h;
     if (i >= n) return;
-    const uint32_t pix = slot_to_pixel(i, c.width, c.height);
-    const float jx = rng(pix, p.sample, 15, 0, p.seed), jy = rng(pix, p.sample, 15, 1, p.seed);
-    const float u = (float(pix % c.width) + jx) / float(c.width);
-    const float v = (float(pix / c.width) + jy) / float(c.height);
+    const uint32_t t = slot_to_pixel(i, p.tile_w, p.tile_h);
+    const uint32_t px = p.tile_x0 + t % p.tile_w, py = p.tile_y0 + t / p.tile_w;
+    const uint32_t pix = py * c.width + px;
+    float u, v;
+    if (p.centered) {
+        u = p.jitter_x * 0.25f + (float(px) + 0.5f) / float(c.width);
+        v = p.jitter_y * 0.25f + (float(py) + 0.5f) / float(c.height);
+    } else {
+        const float jx = rng(pix, p.sample, 15, 0, p.seed), jy = rng(pix, p.sample, 15, 1, p.seed);
+        u = (float(px) + jx) / float(c.width);
+        v = (float(py) + jy) / float(c.height);
+    }
     V3 d = v3(c.ox + c.rx * u + c.bx * v - c.lx, c.oy + c.ry * u + c.by * v - c.ly, c.oz + c.rz * u + c.bz * v - c.lz);
     d = normalize(d);
     float4* r = p.rays_out + size_t(i) * 3;
@@ -675,6 +700,48 @@ __device__ __forceinline__ float mis_hit_factor(const PtScene& sc, const Surf& s
 }
 
 // rayHit.csh:55-325 for one bounce of the wavefront.
+// The real-time G-buffer entry of one pixel (rayHit.csh:76-116): the hit's
+// world position (or origin + direction * 100 on a miss) carried into the
+// previous frame through the instance's inverse and last matrices, projected
+// with the current and the last view-projection; view-space depth, material
+// id and the encoded geometry normal.
+__device__ __forceinline__ float dot4(float4 r, V3 v, float w) {
+    return r.x * v.x + r.y * v.y + r.z * v.z + r.w * w;
+}
+__device__ __forceinline__ float dot4(float4 r, float4 v) {
+    return r.x * v.x + r.y * v.y + r.z * v.z + r.w * v.w;
+}
+__device__ __forceinline__ void write_gbuffer(const PtParams& p, uint32_t pix, bool hit, V3 P, V3 geoN, int mat_id, int inst) {
+    V3 last = P;
+    if (hit) {
+        const float4* im = p.sc.instances + size_t(inst) * 4;   // transposed inverse: object = (P, 1) . column
+        const V3 obj = v3(dot4(__ldg(im + 0), P, 1.0f), dot4(__ldg(im + 1), P, 1.0f), dot4(__ldg(im + 2), P, 1.0f));
+        const float4* lm = (p.gb_last_model ? p.gb_last_model : p.sc.inst_model) + size_t(inst) * 3;
+        last = v3(dot4(__ldg(lm + 0), obj, 1.0f), dot4(__ldg(lm + 1), obj, 1.0f), dot4(__ldg(lm + 2), obj, 1.0f));
+    }
+    const float4* M = p.gb_mats;   // rows 0-3 view, 4-7 projection, 8-11 last view-projection
+    const float4 vs = make_float4(dot4(M[0], P, 1.0f), dot4(M[1], P, 1.0f), dot4(M[2], P, 1.0f), dot4(M[3], P, 1.0f));
+    const float4 pc = make_float4(dot4(M[4], vs), dot4(M[5], vs), dot4(M[6], vs), dot4(M[7], vs));
+    const float4 pl = make_float4(dot4(M[8], last, 1.0f), dot4(M[9], last, 1.0f), dot4(M[10], last, 1.0f),
+                                  dot4(M[11], last, 1.0f));
+    if (p.gb_velocity)
+        p.gb_velocity[pix] = make_float2((pl.x / pl.w - pc.x / pc.w) * 0.5f, (pl.y / pl.w - pc.y / pc.w) * 0.5f);
+    if (p.gb_depth) p.gb_depth[pix] = hit ? vs.z : 1e12f;
+    if (p.gb_material) p.gb_material[pix] = hit ? uint32_t(mat_id) : 65535u;
+    if (p.gb_normal) {
+        // EncodeNormal (common/normalencode.hsh:3-16): octahedral xz, lower hemisphere folded
+        const V3 n = hit ? geoN : v3(1.0f, 0.0f, 0.0f);
+        const float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+        float x = n.x / s, z = n.z / s;
+        if (n.y < 0.0f) {
+            const float ox = x, oz = z;
+            x = (ox >= 0.0f ? 1.0f : -1.0f) * (1.0f - fabsf(oz));
+            z = (oz >= 0.0f ? 1.0f : -1.0f) * (1.0f - fabsf(ox));
+        }
+        p.gb_normal[pix] = make_float2(x, z);
+    }
+}
+
 static __global__ void pt_shade_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = min(*p.n_in, queue_capacity(p));
@@ -686,10 +753,16 @@ static __global__ void pt_shade_kernel(PtParams p) {
         const float4 pay = p.pay_in[i];
         const uint32_t pix = __float_as_uint(pay.w);
         V3 thr = v3(pay.x, pay.y, pay.z);
+        const bool gbuffer = p.gb_write && p.bounce == 0;
+        if (gbuffer && triPtr < 0) {
+            const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
+            write_gbuffer(p, pix & kPixelMask, false, ld3(o4) + ld3(d4) * 100.0f, v3(1.0f, 0.0f, 0.0f), 0, 0);
+        }
         if (triPtr >= 0) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
             const float4 h1 = p.hits_in[size_t(i) * 2 + 1];
             Surf sf = make_surface(p.sc, ld3(o4), ld3(d4), h0.x, __float_as_int(h0.z), triPtr, h1.x, h1.y);
+            if (gbuffer) write_gbuffer(p, pix & kPixelMask, true, sf.P, sf.geoN, sf.mat.id, __float_as_int(h0.z));
             // emission of the first hit (rayHit.csh:180-183); with MIS, also
             // the emission a continuation finds, weighted by its factor (ray dir.w)
             const bool emissive = sf.mat.emissive.x + sf.mat.emissive.y + sf.mat.emissive.z > 0.0f;

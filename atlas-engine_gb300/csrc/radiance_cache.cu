@@ -270,6 +270,8 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
     p.sc.tex.n = ctx->n_textures;
     p.width = cam->width;
     p.height = cam->height;
+    p.tile_w = cam->width;    // primary rays over the whole image
+    p.tile_h = cam->height;
     p.max_bounces = rc->max_bounces;
     p.epsilon = 0.1f;
     p.seed = rc->cfg.seed + 17u;

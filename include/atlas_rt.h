@@ -684,6 +684,12 @@ typedef struct ae_pt_params {
  * image as the engine's estimator, fewer outliers on glossy surfaces. */
 #define AE_PT_MIS 0x1u
 
+/* Primary rays through the pixel centres offset by ae_camera.jitter * 0.25
+ * (the engine's TAA jitter, globalData.jitterCurrent) instead of a random
+ * sub-pixel offset per sample: the real-time ray generation
+ * (rayGen.csh:37-38), which ae_rt_pathtrace_realtime always uses. */
+#define AE_PT_CENTERED 0x2u
+
 /* Path-traces spp samples of every pixel of `cam` over the scene (which needs
  * shading triangles, materials and lights) and adds the radiance of each
  * sample into accum (float4 per pixel, rgb) and, if given, accum64 (double x3
@@ -694,6 +700,36 @@ typedef struct ae_pt_params {
 ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, float* accum,
                              double* accum64, void* stream);
 
+/* The same over one tile of the image: the pixels x0 <= x < x0 + width,
+ * y0 <= y < y0 + height of cam's resolution, as PathTracingRenderer::Render
+ * traces one of imageSubdivisions tiles per call (rayGen.csh:25-30,
+ * pixelOffset and tileSize).  accum / accum64 are whole-image buffers; the
+ * other pixels are left alone.  A pixel's samples do not depend on the
+ * tiling. */
+ae_rt_status ae_rt_pathtrace_tile(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params, uint32_t x0,
+                                  uint32_t y0, uint32_t width, uint32_t height, float* accum, double* accum64,
+                                  void* stream);
+
+/* The real-time G-buffer that the first sample's first hit writes for the
+ * temporal pass (rayHit.csh:76-116); every plane is optional device memory
+ * of one entry per pixel. */
+typedef struct ae_pt_realtime {
+    float* depth;              /* view-space z of the hit (view * (P, 1)).z, INF = 1e12 on a miss */
+    uint32_t* material_idx;    /* GPUMaterial.ID of the hit, 65535 on a miss */
+    float* normal;             /* 2 floats: EncodeNormal of the world-space geometry normal, (1, 0, 0) on a miss */
+    float* velocity;           /* 2 floats: (ndcLast - ndcCurrent) * 0.5 */
+    float view[16];            /* globalData.vMatrix, row-major */
+    float proj[16];            /* globalData.pMatrix */
+    float pv_last[16];         /* globalData.pvMatrixLast */
+    /* previous frame's object-to-world matrix of every scene instance (12
+     * floats, 3 rows of 4), indexed like the instances on the device (the
+     * order given to ae_rt_scene_set, or the order ae_rt_scene_build
+     * reports); NULL: the current ones.  A miss moves with the camera only
+     * (position = origin + direction * 100). */
+    const float* last_matrices;
+    uint32_t n_last_matrices;
+} ae_pt_realtime;
+
 /* The engine's real-time accumulation of the same estimator
  * (rayHit.csh:134-150, REALTIME): params->spp samples per pixel into
  * frame_accum, a [3][height][width] uint32 image (one layer per channel,
@@ -703,9 +739,12 @@ ae_rt_status ae_rt_pathtrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_p
  * 0xFFFFFFFF / spp and added as an unsigned integer.  The engine quantises
  * a path's total; here each contribution (emission, each light sample) is
  * quantised, which differs only where the clamp or the rounding bites.
- * Device memory. */
+ * Primary rays go through the pixel centres offset by cam->jitter * 0.25
+ * (AE_PT_CENTERED).  rt (optional) names the G-buffer planes the first
+ * sample writes.  Device memory. */
 ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params* params,
-                                      uint32_t* frame_accum, float max_radiance, void* stream);
+                                      const ae_pt_realtime* rt, uint32_t* frame_accum, float max_radiance,
+                                      void* stream);
 
 /* The non-real-time output image (rayHit.csh:124-130): for every pixel of
  * accum (float4, the sum of `samples` samples), colour = accum.rgb *

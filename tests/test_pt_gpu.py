@@ -146,14 +146,17 @@ def test_realtime_accumulation(pt_setup):
     frame holds each pixel's radiance as float bits, the same sum the
     non-real-time accumulation gets; at 4 samples the quantised unsigned
     sums, scaled back, agree with the float sums to the quantisation step
-    per contribution."""
+    per contribution.  Both trace the real-time primary rays: pixel centres
+    plus the camera jitter / 4 (rayGen.csh:37-38)."""
     import torch
     ctx, sc, osc = pt_setup
     w, h = 64, 36
-    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h))
+    camd = scenes.pinhole_camera(w, h)
+    camd["jitter"] = (0.3, -0.2)
+    cam = atlas_rt.make_camera(camd)
     for spp, offset in ((1, 5), (4, 40)):
         acc = torch.zeros((h * w, 4), dtype=torch.float32, device="cuda")
-        ctx.pathtrace(cam, acc, spp=spp, sample_offset=offset)
+        ctx.pathtrace(cam, acc, spp=spp, sample_offset=offset, centered=True)
         fr = torch.full((3, h, w), 7, dtype=torch.int32, device="cuda")
         ctx.pathtrace_realtime(cam, fr, max_radiance=64.0, spp=spp, sample_offset=offset)
         ctx.synchronize()
@@ -183,3 +186,105 @@ def test_tonemap_output():
         assert np.all(out.cpu().numpy()[:, 3] == 1.0)
     finally:
         ctx.close()
+
+
+def test_tiles_reproduce_the_whole_image(pt_setup):
+    """PathTracingRenderer's image subdivisions (rayGen.csh:25-30): tracing
+    the image as 3 x 2 tiles (edges not multiples of 8) gives every pixel the
+    same samples as one whole-image call, and a tile leaves the other pixels
+    alone."""
+    import torch
+    ctx, sc, osc = pt_setup
+    w, h = 66, 38
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h))
+    whole = torch.zeros((h * w, 4), dtype=torch.float32, device="cuda")
+    ctx.pathtrace(cam, whole, spp=8, sample_offset=3)
+    tiled = torch.zeros_like(whole)
+    xs, ys = [0, 22, 44, 66], [0, 19, 38]
+    for j in range(2):
+        for i in range(3):
+            ctx.pathtrace(cam, tiled, spp=8, sample_offset=3, tile=(xs[i], ys[j], xs[i + 1] - xs[i], ys[j + 1] - ys[j]))
+    one = torch.zeros_like(whole)
+    ctx.pathtrace(cam, one, spp=8, sample_offset=3, tile=(22, 19, 22, 19))
+    ctx.synchronize()
+    a, b, c = (t.cpu().numpy()[:, :3].reshape(h, w, 3) for t in (whole, tiled, one))
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(c[19:38, 22:44], a[19:38, 22:44])
+    mask = np.ones((h, w), bool)
+    mask[19:38, 22:44] = False
+    assert np.all(c[mask] == 0) and (a > 0).mean() > 0.3
+    for bad in ((60, 0, 10, 4), (0, 0, 0, 4), (0, 30, 4, 9)):
+        with pytest.raises(atlas_rt.AeRtError):
+            ctx.pathtrace(cam, one, spp=1, tile=bad)
+
+
+def test_realtime_gbuffer(pt_setup):
+    """The G-buffer of the real-time mode's first sample (rayHit.csh:76-116)
+    against the same quantities rebuilt on the host from the primary rays'
+    closest hits: view-space depth, material id, encoded geometry normal and
+    the velocity under a camera that moved and an object that moved."""
+    import torch
+    from atlas_rt import gbuffer as gbm
+    ctx, sc, osc = pt_setup
+    w, h = 80, 45
+    camd = scenes.pinhole_camera(w, h)
+    camd["jitter"] = (0.0, 0.0)
+    cam = atlas_rt.make_camera(camd)
+    eye, target = np.array([50.0, 45.0, -22.0]), np.array([50.0, 0.0, 48.0])
+    V = gbm.look_at(eye, target)
+    P = gbm.perspective(60.0, w / h, 0.5, 2000.0)
+    PV_last = P @ gbm.look_at(eye + [0.7, 0.2, 0.0], target + [0.7, 0.0, 0.0])
+    last = np.eye(4)[:3].copy()
+    last[:, 3] = [0.5, 0.0, -0.25]                      # the terrain instance moved since the last frame
+    planes = {"depth": torch.zeros(h * w, dtype=torch.float32, device="cuda"),
+              "material_idx": torch.zeros(h * w, dtype=torch.int32, device="cuda"),
+              "normal": torch.zeros((h * w, 2), dtype=torch.float32, device="cuda"),
+              "velocity": torch.zeros((h * w, 2), dtype=torch.float32, device="cuda")}
+    fr = torch.zeros((3, h, w), dtype=torch.int32, device="cuda")
+    # one matrix per instance on the device: a one-instance scene holds its
+    # instance twice (the reference's single-box build, BVH.cpp:58-100)
+    n_dev = len(osc[1])
+    ctx.pathtrace_realtime(cam, fr, spp=1, gbuffer=dict(planes, view=V, proj=P, pv_last=PV_last,
+                                                          last_matrices=np.repeat(last[None], n_dev, axis=0)))
+    ctx.synchronize()
+    depth = planes["depth"].cpu().numpy()
+    mat = planes["material_idx"].cpu().numpy().view(np.uint32)
+    nrm = planes["normal"].cpu().numpy()
+    vel = planes["velocity"].cpu().numpy()
+
+    # the host side: centre rays, their closest hits, the same formulas in float64
+    px, py = np.meshgrid(np.arange(w), np.arange(h))
+    u = ((px.reshape(-1) + 0.5) / w).astype(np.float32)
+    v = ((py.reshape(-1) + 0.5) / h).astype(np.float32)
+    d = camd["origin"] + camd["right"] * u[:, None] + camd["bottom"] * v[:, None] - camd["location"]
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    o = np.tile(camd["location"], (w * h, 1)).astype(np.float32)
+    hits = torch.zeros((w * h, 8), dtype=torch.float32, device="cuda")
+    ctx.trace_scene_closest(torch.from_numpy(scenes.pack_rays(o, d)).cuda(), 0.0, 1e12, out=hits, n_rays=w * h)
+    ctx.synchronize()
+    hh = hits.cpu().numpy()
+    t, tri = hh[:, 0].astype(np.float64), hh[:, 1].view(np.int32)
+    hit = tri >= 0
+    assert 0.5 < hit.mean() < 1.0
+    shading = sc["bvh"].pack_shading(sc["normals"], sc["obj"])
+    tv = shading[np.maximum(tri, 0)]
+    want_mat = np.where(hit, tv[:, 15].view(np.int32), 65535).astype(np.uint32)
+    agree = want_mat == mat
+    assert agree.mean() > 0.98, agree.mean()           # silhouettes may pick the neighbour
+    Pw = np.where(hit[:, None], o + d.astype(np.float64) * t[:, None], o + d.astype(np.float64) * 100.0)
+    vs = np.c_[Pw, np.ones(len(Pw))] @ V.T
+    want_depth = np.where(hit, vs[:, 2], 1e12)
+    m = agree & hit
+    np.testing.assert_allclose(depth[m], want_depth[m], rtol=2e-4)
+    assert np.all(depth[~hit & agree] == np.float32(1e12))
+    n = np.cross(tv[:, 0:3] - tv[:, 4:7], tv[:, 0:3] - tv[:, 8:11])
+    n /= np.linalg.norm(n, axis=1, keepdims=True) + 1e-30
+    n = np.where(((n * d).sum(1) > 0)[:, None], -n, n)          # two-sided: faces the ray
+    n = np.where(hit[:, None], n, [1.0, 0.0, 0.0])
+    np.testing.assert_allclose(nrm[agree], gbm.encode_normal(n)[agree], atol=2e-3)
+    lastP = np.where(hit[:, None], Pw + last[:, 3], Pw)
+    cur = np.c_[Pw, np.ones(len(Pw))] @ (P @ V).T
+    prev = np.c_[lastP, np.ones(len(Pw))] @ PV_last.T
+    want_vel = (prev[:, :2] / prev[:, 3:] - cur[:, :2] / cur[:, 3:]) * 0.5
+    np.testing.assert_allclose(vel[agree], want_vel[agree], atol=2e-4 + 1e-3 * np.abs(want_vel[agree]).max())
+    assert np.abs(vel[m]).max() > 1e-3                          # the motion is visible
