@@ -426,13 +426,35 @@ def workload_bvh_build(torch, dev, stream, flush, reps=5):
 
 
 def pt_context(dev):
-    """Context + uploaded path-tracing scene (terrain + boxes + 4x4 light)."""
+    """Context + uploaded path-tracing scene (terrain + boxes + 4x4 light);
+    sc["upload"] keeps (mesh id, shading triangles, lights, BVH triangles)."""
     import atlas_rt
     from atlas_rt import ptscene
     ctx = atlas_rt.Context(device=dev.index or 0)
     sc = ptscene.build()
-    ptscene.upload(ctx, sc)
+    sc["upload"] = ptscene.upload(ctx, sc)
     return ctx, sc
+
+
+def pt_cpu_seconds_per_spp(sc, threads):
+    """The oracle's restatement of the engine's path tracer (rayGen + rayHit)
+    over the same scene at 1920x1080, one sample, on `threads` host cores."""
+    import atlas_rt
+    from atlas_rt import BVH, scenes
+    sys.path.insert(0, str(REPO / "oracle"))
+    import pyoracle
+    mid, shading, lights, gt = sc["upload"]
+    bvh = sc["bvh"]
+    inst = np.array([atlas_rt.make_instance(np.eye(4), mid, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    lo, hi = atlas_rt.mesh_bounds(bvh)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    model = np.tile(np.eye(3, 4, dtype=np.float32).reshape(-1), (len(top.order), 1))
+    camd = scenes.pinhole_camera(W, H)
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(np.float32)
+    t0 = time.perf_counter()
+    pyoracle.pathtrace(top.nodes_f32, inst[top.order].copy(), model, [(bvh.nodes_f32, gt, shading)], sc["materials"],
+                       lights, camv, W, H, 1, seed=3, threads=threads)
+    return time.perf_counter() - t0
 
 
 def converged_image(torch, dev, stream, ctx, cam, spp, chunk=256, seed=7, offset=1 << 20):
@@ -527,10 +549,11 @@ def workload_passes(torch, dev, stream, flush, steps, cpu_threads):
     return out
 
 
-def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
+def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     """Plain GPU path tracer on the terrain + boxes scene at 1920x1080, 3
     bounces: wall time to `spp` samples and rel-MSE against a
-    `ref_spp`-sample FP64-accumulated converged image."""
+    `ref_spp`-sample FP64-accumulated converged image; with cpu_threads, the
+    oracle's seconds per sample at full resolution on that many host cores."""
     import atlas_rt
     from atlas_rt import ptscene, scenes
     ctx, sc = pt_context(dev)
@@ -572,6 +595,10 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64):
            "ms_per_spp": final["ms_cum"] / spp, "rel_mse": final["rel_mse"], "rmse": final["rmse"],
            "reference_spp": ref_spp, "reference_seconds": t_ref, "rel_mse_eps": 1e-2,
            "curve": [{k: c[k] for k in ("spp", "ms_cum", "rel_mse")} for c in curve]}
+    if cpu_threads:
+        cpu_s = pt_cpu_seconds_per_spp(sc, cpu_threads)
+        res.update(cpu_oracle_s_per_spp=cpu_s, cpu_threads=cpu_threads,
+                   gpu_speedup_per_spp=cpu_s / (res["ms_per_spp"] * 1e-3))
     return res, (ctx, sc, cam, ref)
 
 
@@ -859,7 +886,8 @@ def main():
             line["workloads"]["passes"] = workload_passes(torch, dev, stream, flush, max(args.steps // 2, 3),
                                                           0 if args.no_cpu_baseline else (os.cpu_count() or 1))
         if "pathtrace" in wl:
-            pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp)
+            pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp,
+                                           cpu_threads=0 if args.no_cpu_baseline else (os.cpu_count() or 1))
             line["workloads"]["pathtrace"] = pt
             if "radiance_cache" in wl:
                 line["workloads"]["radiance_cache"] = workload_radiance_cache(torch, dev, stream, pt, scene,
