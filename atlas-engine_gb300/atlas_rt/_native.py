@@ -131,6 +131,7 @@ _SIGNATURES = [
     ("ae_material_asset_destroy", None, [P]),
     ("ae_material_asset_name", C.c_char_p, [P]),
     ("ae_material_asset_map_path", C.c_char_p, [P, U32]),
+    ("ae_material_asset_get_emissive", C.c_int, [P, P, P]),
     ("ae_material_asset_to_gpu", C.c_int, [P, P, P, I32, P]),
     ("ae_rt_ctx_create", C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     ("ae_rt_ctx_destroy", None, [P]),
@@ -158,6 +159,7 @@ _SIGNATURES = [
     ("ae_rt_scene_set_textures", C.c_int, [P, P, U32]),
     ("ae_rt_scene_set_lights", C.c_int, [P, P, U32]),
     ("ae_rt_pathtrace", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, P]),
+    ("ae_rt_pt_tonemap_tile", C.c_int, [P, P, U32, U32, U32, U32, U32, U32, U32, F32, F32, P, P]),
     ("ae_rt_pathtrace_tile", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), U32, U32, U32, U32, P, P, P]),
     ("ae_rt_pathtrace_realtime", C.c_int, [P, C.POINTER(Camera), C.POINTER(PtParams), P, P, F32, P]),
     ("ae_rt_pt_tonemap", C.c_int, [P, P, U32, U32, U32, F32, F32, P, P]),

@@ -988,6 +988,16 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
         p.gb_mats = static_cast<const float4*>(ctx->pt_gb.ptr);
         p.gb_last_model = rt->last_matrices ? static_cast<const float4*>(ctx->pt_gb.ptr) + 12 : nullptr;
     }
+    if (params->flags & AE_PT_RESTART) {
+        // the first sample replaces the tile's accumulation (rayHit.csh:121-122
+        // loads it only when sampleCount > 0)
+        if (accum)
+            AE_CUDA(ctx, cudaMemset2DAsync(accum + (size_t(ty0) * cam->width + tx0) * 4, size_t(cam->width) * 16, 0,
+                                           size_t(tw) * 16, th, s));
+        if (accum64)
+            AE_CUDA(ctx, cudaMemset2DAsync(accum64 + (size_t(ty0) * cam->width + tx0) * 3, size_t(cam->width) * 24, 0,
+                                           size_t(tw) * 24, th, s));
+    }
     // every queue holds at most one ray per pixel of the tile
     const uint32_t blocks = (n_tile + 255) / 256;
     const float kInf = 1e12f;   // INF of common.hsh:8
@@ -1089,21 +1099,30 @@ ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, cons
     return PathTrace(ctx, cam, params, call, stream);
 }
 
-ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,
-                              float exposure, float gamma, float* out, void* stream) {
+ae_rt_status ae_rt_pt_tonemap_tile(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t x0,
+                                   uint32_t y0, uint32_t tile_width, uint32_t tile_height, uint32_t samples,
+                                   float exposure, float gamma, float* out, void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
-    const uint64_t n = uint64_t(width) * height;
+    const uint64_t n = uint64_t(tile_width) * tile_height;
+    if (uint64_t(width) * height > (1ull << 28) || tile_width > width || tile_height > height ||
+        x0 > width - tile_width || y0 > height - tile_height)
+        return Fail(ctx, AE_RT_INVALID_ARG, "the tile does not lie inside the image");
     if (n == 0) return AE_RT_OK;
     if (!accum || !out || !IsDevicePointer(accum) || !IsDevicePointer(out))
         return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_pt_tonemap takes device buffers");
-    if (samples == 0 || n > (1ull << 28)) return Fail(ctx, AE_RT_INVALID_ARG, "bad sample count or size");
+    if (samples == 0) return Fail(ctx, AE_RT_INVALID_ARG, "the sample count must be positive");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     const uint32_t blocks = uint32_t(std::min<uint64_t>((n + 255) / 256, uint64_t(ctx->sm_count) * 8u));
     atlas::rt::dev::pt_tonemap_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        reinterpret_cast<const float4*>(accum), uint32_t(n), exposure / float(samples), gamma,
-        reinterpret_cast<float4*>(out));
+        reinterpret_cast<const float4*>(accum), width, x0, y0, tile_width, tile_height, exposure, float(samples),
+        gamma, reinterpret_cast<float4*>(out));
     AE_CUDA(ctx, cudaGetLastError());
     return AE_RT_OK;
+}
+
+ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,
+                              float exposure, float gamma, float* out, void* stream) {
+    return ae_rt_pt_tonemap_tile(ctx, accum, width, height, 0, 0, width, height, samples, exposure, gamma, out, stream);
 }
 
 ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* rays, void* stream) {

@@ -764,6 +764,13 @@ const char* ae_material_asset_map_path(const ae_material_asset* m, uint32_t whic
     return m && which < 7 ? m->maps[which].c_str() : "";
 }
 
+ae_rt_status ae_material_asset_get_emissive(const ae_material_asset* m, float srgb[3], float* intensity) {
+    if (!m || !srgb || !intensity) return Fail("null argument");
+    std::memcpy(srgb, m->emissiveColor, sizeof(m->emissiveColor));
+    *intensity = m->emissiveIntensity;
+    return AE_RT_OK;
+}
+
 ae_rt_status ae_material_asset_to_gpu(const ae_material_asset* m, const ae_mesh_asset* mesh,
                                       const int32_t* texture_ids, int32_t id, ae_material* out) {
     if (!m || !out) return Fail("null argument");

@@ -826,11 +826,18 @@ namespace atlas::rt::dev {
 
 // The non-real-time output image (rayHit.csh:124-130): colour = accum.rgb *
 // exposure / samples, mapped by 1 - exp(-colour) and raised to gamma.
-static __global__ void pt_tonemap_kernel(const float4* accum, uint32_t n, float scale, float gamma, float4* out) {
+// The output image of rayHit.csh:126-132 over the rectangle (x0, y0, tw, th)
+// of a width-wide image: colour = accum.rgb * exposure / samples, out =
+// (pow(1 - exp(-colour), gamma), 1).
+static __global__ void pt_tonemap_kernel(const float4* accum, uint32_t width, uint32_t x0, uint32_t y0, uint32_t tw,
+                                         uint32_t th, float exposure, float samples, float gamma, float4* out) {
+    const uint32_t n = tw * th;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = accum[i];
-        out[i] = make_float4(powf(1.0f - expf(-(a.x * scale)), gamma), powf(1.0f - expf(-(a.y * scale)), gamma),
-                             powf(1.0f - expf(-(a.z * scale)), gamma), 1.0f);
+        const size_t pix = size_t(y0 + i / tw) * width + x0 + i % tw;
+        const float4 a = accum[pix];
+        out[pix] = make_float4(powf(1.0f - expf(-(a.x * exposure / samples)), gamma),
+                               powf(1.0f - expf(-(a.y * exposure / samples)), gamma),
+                               powf(1.0f - expf(-(a.z * exposure / samples)), gamma), 1.0f);
     }
 }
 

@@ -319,6 +319,10 @@ const char* ae_material_asset_name(const ae_material_asset* material);
 /* The texture path of one AE_MAP_* slot ("" when the material has none). */
 const char* ae_material_asset_map_path(const ae_material_asset* material, uint32_t which);
 
+/* The material's emissiveColor (sRGB, as in the file) and emissiveIntensity:
+ * the inputs of ae_lights_from_mesh. */
+ae_rt_status ae_material_asset_get_emissive(const ae_material_asset* material, float srgb[3], float* intensity);
+
 /* GPUMaterial of this material the way RayTracingWorld::UpdateMaterials
  * fills it (RayTracingWorld.cpp:186-240): baseColor = pow(c, 2.2),
  * emissiveColor = pow(c, 2.2) * emissiveIntensity (ColorConverter.h:18-23),
@@ -690,6 +694,12 @@ typedef struct ae_pt_params {
  * (rayGen.csh:37-38), which ae_rt_pathtrace_realtime always uses. */
 #define AE_PT_CENTERED 0x2u
 
+/* The call's pixels (the whole image, or the tile) start a new accumulation:
+ * their accum / accum64 entries are cleared before the first sample, as the
+ * engine's rayHit overwrites its accumulation image at sampleCount 0
+ * (rayHit.csh:121-122). */
+#define AE_PT_RESTART 0x4u
+
 /* Path-traces spp samples of every pixel of `cam` over the scene (which needs
  * shading triangles, materials and lights) and adds the radiance of each
  * sample into accum (float4 per pixel, rgb) and, if given, accum64 (double x3
@@ -748,10 +758,17 @@ ae_rt_status ae_rt_pathtrace_realtime(ae_rt_ctx* ctx, const ae_camera* cam, cons
 
 /* The non-real-time output image (rayHit.csh:124-130): for every pixel of
  * accum (float4, the sum of `samples` samples), colour = accum.rgb *
- * exposure / samples, out = (pow(1 - exp(-colour), gamma), 1).  Device
- * memory, float4 per pixel. */
+ * exposure / samples (in that order), out = (pow(1 - exp(-colour), gamma),
+ * 1).  Device memory, float4 per pixel. */
 ae_rt_status ae_rt_pt_tonemap(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t samples,
                               float exposure, float gamma, float* out, void* stream);
+
+/* The same over the pixels x0 <= x < x0 + tile_width, y0 <= y < y0 +
+ * tile_height of the width x height images accum and out (the engine writes
+ * the output image of the tile it traced). */
+ae_rt_status ae_rt_pt_tonemap_tile(ae_rt_ctx* ctx, const float* accum, uint32_t width, uint32_t height, uint32_t x0,
+                                   uint32_t y0, uint32_t tile_width, uint32_t tile_height, uint32_t samples,
+                                   float exposure, float gamma, float* out, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* The traversal's other consumers: RTAO, reflections, RTGI, DDGI probe rays  */

@@ -15,6 +15,11 @@
  *   GetIntersection / GetIntersectionAny
  *                       the reference's one-ray host queries
  *                       (BVH.cpp:103-217), answered by the same GPU traversal.
+ *   atlas::rt::PathTracingRenderer
+ *                       the engine's path-tracing renderer (fields bounces,
+ *                       realTime, realTimeSamplesPerFrame, maxRadiance; Render,
+ *                       ResetSampleCount, GetSampleCount) over the library's
+ *                       path tracer, tiles and real-time mode included.
  *
  * Query semantics are those of the engine's shader traversal (HitClosest /
  * HitAny, bvh.hsh:191-273, :359-441), which every GPU consumer of the BVH
@@ -31,6 +36,7 @@
 
 #include "atlas_rt.h"
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -456,6 +462,119 @@ private:
     bool triangles_ = false;
     Context* ctx_ = nullptr;
     int32_t mesh_ = -1;
+};
+
+/* The images PathTracingRenderer writes, as device buffers the caller owns
+ * (the engine's PathTracerRenderTarget textures): the accumulation image
+ * (float4 per pixel; FP64 copy optional), the tonemapped output image
+ * (float4, optional) and, for the real-time mode, the [3][height][width]
+ * frame image and the G-buffer planes. */
+struct PathTracerRenderTarget {
+    uint32_t width = 0, height = 0;
+    float* accum = nullptr;
+    double* accum64 = nullptr;
+    float* output = nullptr;
+    uint32_t* frameAccum = nullptr;
+    ae_pt_realtime* gbuffer = nullptr;
+};
+
+/* PathTracingRenderer (src/engine/renderer/PathTracingRenderer.h:16-50,
+ * PathTracingRenderer.cpp:29-306) over the library's path tracer, with the
+ * engine's public fields and counters.  The scene (meshes with shading
+ * triangles, instances, materials, lights) is the context's. */
+class PathTracingRenderer {
+public:
+    explicit PathTracingRenderer(Context& ctx) : ctx_(&ctx) {}
+
+    /* Render (PathTracingRenderer.cpp:29-192, :266-281).  A camera that moved
+     * (location or frustum by more than 1e-3) or a new image size restarts the
+     * accumulation.  Non-real-time: traces one sample of one tile of
+     * imageSubdivisions per call (tile = resolution / subdivisions, at
+     * tile * imageOffset; the remainder rows and columns of a resolution
+     * that does not divide are not traced, as in the engine), adds it to the
+     * accumulation (replacing it at sample 0) and writes the tile's output
+     * image (exposure, gamma 1 / 2.2); after the last tile the sample count
+     * advances.  Real-time: traces realTimeSamplesPerFrame samples of every
+     * pixel into the frame image (and the G-buffer), the frame count
+     * advances and the sample count reads 1. */
+    void Render(PathTracerRenderTarget& target, const ae_camera& camera, float exposure = 1.0f,
+                int32_t subdivisionsX = 1, int32_t subdivisionsY = 1, void* stream = nullptr) {
+        if (target.width != camera.width || target.height != camera.height || subdivisionsX < 1 ||
+            subdivisionsY < 1 || uint32_t(subdivisionsX) > camera.width || uint32_t(subdivisionsY) > camera.height)
+            throw Error(AE_RT_INVALID_ARG, "PathTracingRenderer::Render: target, camera and subdivisions disagree");
+        if (Moved(camera) || target.width != width_ || target.height != height_) {
+            camera_ = camera;
+            width_ = target.width;
+            height_ = target.height;
+            sampleCount_ = 0;
+            offsetX_ = offsetY_ = 0;
+        }
+        ae_pt_params p;
+        std::memset(&p, 0, sizeof(p));
+        p.max_bounces = uint32_t(bounces);
+        p.seed = seed;
+        p.epsilon = epsilon;
+        if (realTime) {
+            subdivisionsX = subdivisionsY = 1;
+            sampleCount_ = 0;
+            frameCount_++;
+            if (!target.frameAccum) throw Error(AE_RT_INVALID_ARG, "the real-time mode writes target.frameAccum");
+            p.spp = uint32_t(realTimeSamplesPerFrame);
+            p.sample_offset = uint32_t(frameCount_) * p.spp;
+            ctx_->Check(ae_rt_pathtrace_realtime(ctx_->get(), &camera, &p, target.gbuffer, target.frameAccum,
+                                                 maxRadiance, stream),
+                        "ae_rt_pathtrace_realtime");
+        } else {
+            const uint32_t tw = camera.width / uint32_t(subdivisionsX), th = camera.height / uint32_t(subdivisionsY);
+            const uint32_t x0 = tw * uint32_t(offsetX_), y0 = th * uint32_t(offsetY_);
+            p.spp = 1;
+            p.sample_offset = uint32_t(sampleCount_);
+            p.flags = sampleCount_ == 0 ? AE_PT_RESTART : 0u;
+            ctx_->Check(ae_rt_pathtrace_tile(ctx_->get(), &camera, &p, x0, y0, tw, th, target.accum, target.accum64,
+                                             stream),
+                        "ae_rt_pathtrace_tile");
+            if (target.output)
+                ctx_->Check(ae_rt_pt_tonemap_tile(ctx_->get(), target.accum, camera.width, camera.height, x0, y0, tw,
+                                                  th, uint32_t(sampleCount_) + 1u, exposure, 1.0f / 2.2f,
+                                                  target.output, stream),
+                            "ae_rt_pt_tonemap_tile");
+        }
+        if (++offsetX_ == subdivisionsX) {
+            offsetX_ = 0;
+            offsetY_++;
+        }
+        if (offsetY_ >= subdivisionsY) {
+            offsetY_ = 0;
+            sampleCount_++;
+        }
+    }
+
+    void ResetSampleCount() { sampleCount_ = 0; }
+    int32_t GetSampleCount() const { return sampleCount_; }
+    int32_t GetFrameCount() const { return frameCount_; }
+
+    int32_t bounces = 10;
+    bool realTime = true;
+    int32_t realTimeSamplesPerFrame = 4;
+    float maxRadiance = 65535.0f;
+    uint32_t seed = 1;
+    float epsilon = 0.1f;   /* EPSILON, raytracer/common.hsh:9 */
+
+private:
+    bool Moved(const ae_camera& c) const {
+        auto dist = [](const float* a, const float* b) {
+            const float x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+            return std::sqrt(x * x + y * y + z * z);
+        };
+        return dist(c.location, camera_.location) > 1e-3f || dist(c.origin, camera_.origin) > 1e-3f ||
+               dist(c.right, camera_.right) > 1e-3f || dist(c.bottom, camera_.bottom) > 1e-3f;
+    }
+
+    Context* ctx_;
+    ae_camera camera_{};
+    uint32_t width_ = 0, height_ = 0;
+    int32_t sampleCount_ = 0, frameCount_ = 0;
+    int32_t offsetX_ = 0, offsetY_ = 0;
 };
 
 }  // namespace rt

@@ -10,6 +10,8 @@ and linked against libatlas_rt.so.
 * GPU: TraceClosest / TraceAny / GetIntersection / GetIntersectionAny equal the
   oracle's restatement of the shader traversal bit for bit, per-ray (tMin,
   tMax) included, and a query before Upload is refused.
+* GPU: atlas::rt::PathTracingRenderer driven from engine assets
+  (tests/cpp/renderer_check.cpp) equals the direct C ABI calls.
 """
 import subprocess
 from pathlib import Path
@@ -33,6 +35,38 @@ def wrapper_bin(tmp_path_factory):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return out
+
+
+@pytest.fixture(scope="module")
+def renderer_bin(tmp_path_factory):
+    """tests/cpp/renderer_check.cpp: assets -> light list -> PathTracingRenderer."""
+    lib = atlas_build.build()
+    cuda = Path(atlas_build._cuda_lib_dir(atlas_build._nvcc())).parent
+    out = tmp_path_factory.mktemp("cpp") / "renderer_check"
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{REPO / 'include'}", f"-I{cuda / 'include'}",
+           str(REPO / "tests" / "cpp" / "renderer_check.cpp"), f"-L{lib.parent}", "-latlas_rt",
+           f"-L{cuda / 'lib64'}", "-lcudart", f"-Wl,-rpath,{lib.parent}", f"-Wl,-rpath,{cuda / 'lib64'}",
+           "-Wl,--allow-shlib-undefined", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_renderer_program_builds(renderer_bin):
+    """The engine-side caller compiles against both headers and links."""
+    assert renderer_bin.exists()
+
+
+@pytest.mark.gpu
+def test_path_tracing_renderer_end_to_end(renderer_bin):
+    """.aemesh + .aematerial fixtures through the material table, triangle
+    assembly, BVH, scene, light list and atlas::rt::PathTracingRenderer:
+    progressive tiles, camera-move restart, non-dividing subdivisions and the
+    real-time mode each equal the direct C ABI calls."""
+    r = subprocess.run([str(renderer_bin), str(REPO / "tests" / "golden" / "assets")], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count("ok ") == 4, r.stdout
 
 
 class _Reader:
