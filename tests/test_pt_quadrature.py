@@ -1,0 +1,141 @@
+"""A known answer for the path tracer's estimator, independent of both
+implementations: a grey diffuse floor under a 2 x 2 emitter, one bounce
+(max_bounces = 0: the first hit's emission and next-event estimation).  Each
+pixel's expected radiance is the integral over the light of
+f(V, L) E cos(theta_x) cos(theta_l) / d^2, with f the engine's diffuse BRDF
+(EvaluateDiffuseBRDF and RenormalizedDisneyDiffuse, brdf/brdfEval.hsh:8-19 and
+brdf/brdf.hsh; the specular term vanishes for reflectance 0 and metalness 0),
+computed here by a 400 x 400 midpoint rule in float64.
+
+The oracle's restatement (CPU) and the GPU path tracer must both converge to
+it: this pins the light selection, the triangle sampling and its pdf, the
+area-to-solid-angle conversion and the shadow-ray setup (direct.hsh:12-86,
+lights.hsh:11-29, rayHit.csh:209-235, :327-338) against quadrature rather
+than against each other.
+"""
+import numpy as np
+import pytest
+
+import atlas_rt
+import pyoracle
+from atlas_rt import BVH, MATERIAL_DTYPE, ptscene, scenes
+
+F32 = np.float32
+ALBEDO, RADIANCE, LIGHT_Y, HALF = 0.5, 10.0, 2.0, 1.0
+EYE, TARGET = (0.3, 1.5, 0.2), (0.3, 0.0, 0.2)
+W = H = 16
+FOV = 40.0
+
+
+def furnace_scene():
+    """Floor (object 0) at y = 0 facing up, emitter (object 1) at y = 2 facing down."""
+    big = 10.0
+    a, b, c, d = [-big, 0, -big], [big, 0, -big], [big, 0, big], [-big, 0, big]
+    floor = [[a, c, b], [a, d, c]]
+    la, lb = [-HALF, LIGHT_Y, -HALF], [HALF, LIGHT_Y, -HALF]
+    lc, ld = [HALF, LIGHT_Y, HALF], [-HALF, LIGHT_Y, HALF]
+    light = [[la, lb, lc], [la, lc, ld]]
+    tris = np.array(floor + light, F32)
+    obj = np.array([0, 0, 1, 1], np.int32)
+    normals = np.zeros((4, 3, 3), F32)
+    normals[:2] = [0, 1, 0]
+    normals[2:] = [0, -1, 0]
+    mats = np.zeros(2, MATERIAL_DTYPE)
+    mats["ID"] = [0, 1]
+    mats["opacity"], mats["ao"], mats["normalScale"], mats["twoSided"] = 1.0, 1.0, 1.0, 1
+    mats["roughness"], mats["metalness"], mats["reflectance"] = 1.0, 0.0, 0.0
+    for t in ("baseColorTexture", "opacityTexture", "normalTexture", "roughnessTexture", "metalnessTexture",
+              "aoTexture"):
+        mats[t] = -1
+    mats[0]["baseColor"] = ALBEDO
+    mats[1]["baseColor"] = 0.0
+    mats[1]["emissiveColor"] = RADIANCE
+    return {"tris": tris, "obj": obj, "normals": normals, "materials": mats, "bvh": BVH(tris), "light_obj": 1}
+
+
+def camera():
+    return scenes.pinhole_camera(W, H, fov_deg=FOV, eye=EYE, target=TARGET, up=(0.0, 0.0, 1.0))
+
+
+def disney(NdotV, NdotL, LdotH, lr):
+    """RenormalizedDisneyDiffuse (brdf/brdf.hsh)."""
+    bias, factor = 0.5 * lr, 1.0 + (1.0 / 1.51 - 1.0) * lr
+    fd90 = bias + 2.0 * LdotH * LdotH * lr
+    return (1.0 + (fd90 - 1.0) * (1.0 - NdotL) ** 5) * (1.0 + (fd90 - 1.0) * (1.0 - NdotV) ** 5) * factor
+
+
+def expected_image(n=400):
+    """Per pixel centre: the floor point it sees and the midpoint-rule integral of the direct light."""
+    cam = camera()
+    u = (np.arange(W) + 0.5) / W
+    v = (np.arange(H) + 0.5) / H
+    d = (cam["origin"][None, None, :].astype(np.float64) + cam["right"][None, None, :] * u[None, :, None]
+         + cam["bottom"][None, None, :] * v[:, None, None] - cam["location"])
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    eye = np.asarray(EYE, np.float64)
+    x = eye + d * (-eye[1] / d[..., 1:2])                     # on the floor, y = 0
+    g = (np.arange(n) + 0.5) / n * 2 * HALF - HALF
+    ly = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    lp = np.stack([ly[:, 0], np.full(len(ly), LIGHT_Y), ly[:, 1]], 1)
+    dA = (2 * HALF / n) ** 2
+    out = np.zeros((H, W))
+    lr = 1.0                                                  # max(roughness^2, 1e-5)
+    for i in range(H):
+        for j in range(W):
+            p = x[i, j]
+            V = (eye - p) / np.linalg.norm(eye - p)
+            toL = lp - p
+            d2 = (toL ** 2).sum(1)
+            L = toL / np.sqrt(d2)[:, None]
+            Hh = L + V
+            Hh /= np.linalg.norm(Hh, axis=1, keepdims=True)
+            NdotL = np.clip(L[:, 1], 0, 1)
+            NdotV = np.clip(V[1], 0, 1)
+            LdotH = np.clip((L * Hh).sum(1), 0, 1)
+            cos_l = np.clip(L[:, 1], 0, 1)                    # the light faces down: dot((0,-1,0), -L)
+            f = ALBEDO / np.pi * disney(NdotV, NdotL, LdotH, lr)
+            out[i, j] = np.sum(f * RADIANCE * NdotL * cos_l / d2) * dA
+    return out
+
+
+@pytest.fixture(scope="module")
+def expected():
+    return expected_image()
+
+
+def test_oracle_direct_light_matches_quadrature(expected):
+    sc = furnace_scene()
+    b = sc["bvh"]
+    gt = b.pack_triangles(sc["obj"])
+    sh = b.pack_shading(sc["normals"], sc["obj"])
+    lights = ptscene.lights_for(sc, sh)
+    lo, hi = atlas_rt.mesh_bounds(b)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), 0, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    model = np.tile(np.eye(3, 4, dtype=F32).reshape(-1), (len(top.order), 1))
+    camd = camera()
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(F32)
+    spp = 4096
+    img = pyoracle.pathtrace(top.nodes_f32, inst[top.order].copy(), model, [(b.nodes_f32, gt, sh)], sc["materials"],
+                             lights, camv, W, H, spp, max_bounces=0)[..., 0] / spp
+    assert abs(img.mean() - expected.mean()) / expected.mean() < 0.005, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=0.03)
+
+
+@pytest.mark.gpu
+def test_gpu_direct_light_matches_quadrature(expected):
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    try:
+        ptscene.upload(ctx, furnace_scene())
+        cam = atlas_rt.make_camera(camera())
+        acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+        spp = 32768
+        ctx.pathtrace(cam, acc, acc64, spp=spp, max_bounces=0)
+        ctx.synchronize()
+        img = acc64.cpu().numpy()[:, 0].reshape(H, W) / spp
+    finally:
+        ctx.close()
+    assert abs(img.mean() - expected.mean()) / expected.mean() < 0.002, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=0.01)
