@@ -447,6 +447,11 @@ class Context:
             table[i].row_pitch = 0
         _check(lib().ae_rt_scene_set_textures(self._h, table if arrs else None, len(arrs)), self._h)
 
+    def set_environment(self, radiance):
+        """ae_rt_scene_set_environment: the constant radiance the path tracer's misses see."""
+        r = np.ascontiguousarray(radiance, np.float32).reshape(3)
+        _check(lib().ae_rt_scene_set_environment(self._h, _ptr(r)), self._h)
+
     def set_lights(self, lights):
         lights = np.ascontiguousarray(lights, np.float32).reshape(-1, 16)
         _check(lib().ae_rt_scene_set_lights(self._h, _ptr(lights) if len(lights) else None, len(lights)),

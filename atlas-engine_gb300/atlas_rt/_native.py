@@ -112,6 +112,7 @@ _SIGNATURES = [
     ("ae_bvh_pack_uvs", C.c_int, [P, P, P]),
     ("ae_bvh_pack_attributes", C.c_int, [P, P, P, P, P, P]),
     ("ae_asset_last_error", C.c_char_p, []),
+    ("ae_rt_scene_set_environment", C.c_int, [P, P]),
     ("ae_lights_from_mesh", C.c_int, [P, U32, P, P, U32, P, U32, C.POINTER(U32)]),
     ("ae_lights_instance", C.c_int, [P, U32, P, I32, P]),
     ("ae_light_directional", C.c_int, [P, F32, P, U32, P]),

@@ -843,6 +843,16 @@ ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures
     return AE_RT_OK;
 }
 
+ae_rt_status ae_rt_scene_set_environment(ae_rt_ctx* ctx, const float radiance[3]) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!radiance) return Fail(ctx, AE_RT_INVALID_ARG, "null environment radiance");
+    for (int c = 0; c < 3; c++)
+        if (!(radiance[c] >= 0.0f) || !std::isfinite(radiance[c]))
+            return Fail(ctx, AE_RT_INVALID_ARG, "the environment radiance must be finite and non-negative");
+    for (int c = 0; c < 3; c++) ctx->env[c] = radiance[c];
+    return AE_RT_OK;
+}
+
 ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n) {
     if (!ctx || (n && !lights)) return AE_RT_INVALID_ARG;
     for (uint32_t i = 0; i < n; i++) {
@@ -949,9 +959,14 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
     p.epsilon = params->epsilon;
     p.seed = params->seed;
     p.mis = (params->flags & AE_PT_MIS) ? 1u : 0u;
-    // with MIS a later bounce's shading adds light hits into the pixels that
-    // the previous bounce's resolve (running beside it) adds into
-    p.atomic_accum = p.mis;
+    p.sc.env_r = ctx->env[0];
+    p.sc.env_g = ctx->env[1];
+    p.sc.env_b = ctx->env[2];
+    const bool env = ctx->env[0] + ctx->env[1] + ctx->env[2] > 0.0f;
+    // with MIS (light hits) or an environment (misses) a later bounce's
+    // shading adds into the pixels that the previous bounce's resolve,
+    // running beside it, adds into
+    p.atomic_accum = (p.mis || env) ? 1u : 0u;
     if (frame_accum) {
         // cleared here; the engine's renderer clears its frame image before
         // the dispatch (one store per pixel at one sample, atomics otherwise)

@@ -73,6 +73,7 @@ struct ae_rt_ctx {
     uint32_t n_textures = 0;
     float4* d_lights = nullptr;         // GPULight array
     uint32_t n_lights = 0;
+    float env[3] = { 0.0f, 0.0f, 0.0f };  // constant environment radiance of the path tracer's misses
     // path tracer queues
     atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
     atlas::rt::host::Scratch pt_gb;     // real-time G-buffer matrices

@@ -16,7 +16,7 @@
 //     occlusion factor, Russian roulette with p = clamp(max(throughput),
 //     0.01, 0.99), tripled before bounce 3, and termination below the
 //     geometric surface (rayHit.csh:237-325);
-//   * no environment light (the scenes here have none), and -- deliberately --
+//   * a constant environment radiance on a miss (the engine samples its sky cubemap there), and -- deliberately --
 //     without the engine's clamp of indirect radiance at 10 (rayHit.csh:
 //     196-201), which biases the estimate; this renderer is the unbiased
 //     reference the radiance cache is judged against.
@@ -49,6 +49,7 @@ struct PtScene {
     uint32_t n_lights;
     TexTable tex;                 // the scene's textures (texture.cuh)
     uint32_t tex_level;           // mip level of the surface textures (GetSurfaceParameters' textureLevel)
+    float env_r, env_g, env_b;    // constant environment radiance a miss adds (rayHit.csh:166-171)
 };
 
 struct PtParams {
@@ -492,6 +493,10 @@ __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, fl
     sf.N = normalize(N);
     sf.geoN = triN;
     sf.L = sf.N;
+    // NdotV, F0 and F90 do not depend on L: set them here, as the light
+    // sample's UpdateSurface would, so that the lobe choice of the
+    // continuation (which reads them) is defined in a scene without lights
+    update_surface(sf);
     return sf;
 }
 
@@ -757,6 +762,11 @@ static __global__ void pt_shade_kernel(PtParams p) {
         if (gbuffer && triPtr < 0) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];
             write_gbuffer(p, pix & kPixelMask, false, ld3(o4) + ld3(d4) * 100.0f, v3(1.0f, 0.0f, 0.0f), 0, 0);
+        }
+        if (triPtr < 0 && p.sc.env_r + p.sc.env_g + p.sc.env_b > 0.0f) {
+            // EvaluateBounce's miss: the environment times the throughput, clamped per channel
+            add_radiance(p, pix, v3(fminf(p.sc.env_r * thr.x, 10.0f), fminf(p.sc.env_g * thr.y, 10.0f),
+                                    fminf(p.sc.env_b * thr.z, 10.0f)));
         }
         if (triPtr >= 0) {
             const float4 o4 = p.rays_in[size_t(i) * 3], d4 = p.rays_in[size_t(i) * 3 + 1];

@@ -625,6 +625,13 @@ typedef struct ae_texture {
 ae_rt_status ae_rt_scene_set_textures(ae_rt_ctx* ctx, const ae_texture* textures, uint32_t n);
 ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint32_t n);
 
+/* The environment the path tracer's misses see: a constant radiance (rgb,
+ * finite, >= 0; initially black), added as min(radiance * throughput, 10) per
+ * channel on every miss, the camera's included (EvaluateBounce,
+ * rayHit.csh:166-171, where the engine samples its sky cubemap).  The
+ * radiance cache models no environment: its calls refuse a non-black one. */
+ae_rt_status ae_rt_scene_set_environment(ae_rt_ctx* ctx, const float radiance[3]);
+
 /* The light list the engine builds on the host before each path-tracing
  * dispatch.  Arithmetic follows the reference in float32, operation by
  * operation; pow is the C library's powf, as glm::pow calls it.

@@ -997,6 +997,7 @@ typedef struct {
     const float* cam;
     uint32_t width, height, spp, sample_offset, max_bounces, seed;
     float epsilon;
+    const float* env;      /* constant environment radiance of a miss (rayHit.csh:166-171), or NULL */
     double* accum;
     uint32_t begin, end;
     size_t stack_cap;
@@ -1162,6 +1163,10 @@ static int pt_make_surface(const pt_job_t* j, v3 ro, v3 rd, int32_t tp, int32_t 
     sf->N = vnorm(N);
     sf->geoN = triN;
     sf->L = sf->N;
+    /* NdotV, F0 and F90 do not depend on L: set here as the light sample's
+     * UpdateSurface would, so the continuation's lobe choice is defined
+     * without lights */
+    pt_update(sf);
     return backface;
 }
 
@@ -1235,7 +1240,15 @@ static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* ou
             int32_t tp, ino;
             float tuv[3];
             scene_closest_one(&j->sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
-            if (tp < 0) break;   /* no environment light */
+            if (tp < 0) {
+                /* the environment, clamped per channel (rayHit.csh:166-171) */
+                if (j->env) {
+                    out[0] += fminf(j->env[0] * thr.x, 10.0f);
+                    out[1] += fminf(j->env[1] * thr.y, 10.0f);
+                    out[2] += fminf(j->env[2] * thr.z, 10.0f);
+                }
+                break;
+            }
             pt_surf sf;
             pt_make_surface(j, ro, rd, tp, ino, tuv, &sf);
             if (bounce == 0 && sf.m.emissive.x + sf.m.emissive.y + sf.m.emissive.z > 0.0f) {
@@ -1308,8 +1321,20 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    const float* cam, uint32_t width, uint32_t height,
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum) {
+    aeo_pathtrace_env(tlas, n_tlas, inst, inst_model, n_inst, meshes, n_meshes, materials, lights, n_lights, textures,
+                      n_textures, cam, width, height, spp, sample_offset, max_bounces, seed, epsilon, NULL, threads,
+                      accum);
+}
+
+void aeo_pathtrace_env(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
+                       uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
+                       const float* lights, uint32_t n_lights, const aeo_texture* textures, uint32_t n_textures,
+                       const float* cam, uint32_t width, uint32_t height,
+                       uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
+                       const float* env, int threads, double* accum) {
     pt_job_t proto;
     memset(&proto, 0, sizeof(proto));
+    proto.env = env;
     scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, NULL };
     proto.sc = sc;
     proto.inst_model = inst_model;

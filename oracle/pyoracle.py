@@ -63,6 +63,9 @@ def port():
         L.aeo_pathtrace.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U32,
                                     C.c_float, C.c_int, P]
         L.aeo_pathtrace.restype = None
+        L.aeo_pathtrace_env.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U32,
+                                        C.c_float, P, C.c_int, P]
+        L.aeo_pathtrace_env.restype = None
         L.aeo_scene_any_glsl.restype = None
         L.aeo_scene_closest_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32,
                                                           C.c_int, P, P, P]
@@ -359,9 +362,10 @@ def scene_any_transparency_glsl(tlas_f32, instances, meshes, materials, rays8, c
 
 def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, width, height, spp,
               sample_offset=0, max_bounces=3, seed=1, epsilon=0.1, threads=os.cpu_count(), accum=None,
-              textures=None):
+              textures=None, environment=None):
     """CPU restatement of the path tracer; returns the summed radiance
-    (height, width, 3) float64 over spp samples (add to `accum` if given)."""
+    (height, width, 3) float64 over spp samples (add to `accum` if given).
+    environment: a constant radiance added on a miss (rayHit.csh:166-171)."""
     tlas_f32 = _c(tlas_f32, np.float32)
     inst = np.ascontiguousarray(instances)
     model = _c(inst_model, np.float32)
@@ -371,10 +375,11 @@ def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, w
     table, keep = _mesh_table(meshes)
     out = np.zeros((height, width, 3), np.float64) if accum is None else accum
     ttab, ntex, tkeep = _texture_table(textures)
-    port().aeo_pathtrace(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst),
-                         table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), ttab, ntex,
-                         cam.ctypes.data, width, height, spp, sample_offset, max_bounces, seed, epsilon, threads,
-                         out.ctypes.data)
+    env = None if environment is None else _c(environment, np.float32).reshape(3)
+    port().aeo_pathtrace_env(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst),
+                             table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), ttab, ntex,
+                             cam.ctypes.data, width, height, spp, sample_offset, max_bounces, seed, epsilon,
+                             None if env is None else env.ctypes.data, threads, out.ctypes.data)
     return out
 
 

@@ -16,7 +16,9 @@ The oracle's restatement (CPU) and the GPU path tracer must both converge to
 it: this pins the light selection, the triangle sampling and its pdf, the
 area-to-solid-angle conversion and the shadow-ray setup (direct.hsh:12-86,
 lights.hsh:11-29, rayHit.csh:209-235, :327-338) against quadrature rather
-than against each other.
+than against each other.  A second set of scenes (the floor alone under a
+constant environment) does the same for the BRDF-sampled continuation; and
+on all of them the GPU equals the oracle pixel for pixel, sample for sample.
 """
 import numpy as np
 import pytest
@@ -181,3 +183,154 @@ def test_gpu_direct_light_matches_quadrature(kind):
     tm, tp = TOL_GPU[kind]
     assert abs(img.mean() - expected.mean()) / expected.mean() < tm, (img.mean(), expected.mean())
     np.testing.assert_allclose(img, expected, rtol=tp)
+
+
+# ---------------------------------------------------------------------------
+# BRDF-sampled continuations: the floor alone under a constant environment
+# ---------------------------------------------------------------------------
+#
+# No lights, max_bounces = 1: the first hit contributes nothing itself; its
+# continuation (lobe choice, cosine or GGX-VNDF sampling and their pdfs,
+# Russian roulette; rayHit.csh:237-325, brdfSample.hsh:8-90) escapes and adds
+# min(E * throughput, 10) (rayHit.csh:166-171).  The expectation is E times the
+# BRDF's directional albedo at the pixel's view angle, a hemisphere
+# quadrature here.
+
+ENV = 1.0
+
+
+def floor_only_scene(kind):
+    sc = furnace_scene(kind)
+    keep = sc["obj"] == 0
+    tris = sc["tris"][keep]
+    sc.update(tris=tris, obj=sc["obj"][keep], normals=sc["normals"][keep], bvh=BVH(tris))
+    sc["materials"] = sc["materials"][:1].copy()
+    return sc
+
+
+def directional_albedo(kind, mu_v, n_mu=2000, n_phi=720):
+    """Integral over the upper hemisphere of f(V, L) cos(theta_L) for
+    V at cos(theta) = mu_v (midpoint rule in cos(theta_L) and phi)."""
+    mu = (np.arange(n_mu) + 0.5) / n_mu
+    phi = (np.arange(n_phi) + 0.5) / n_phi * 2 * np.pi
+    M, P = np.meshgrid(mu, phi, indexing="ij")
+    s = np.sqrt(1 - M * M)
+    L = np.stack([s * np.cos(P), M, s * np.sin(P)], -1)
+    V = np.array([np.sqrt(1 - mu_v * mu_v), mu_v, 0.0])
+    Hh = L + V
+    Hh /= np.linalg.norm(Hh, axis=-1, keepdims=True)
+    f = brdf(kind, mu_v, M, np.clip(Hh[..., 1], 0, 1), np.clip((L * Hh).sum(-1), 0, 1))
+    return float(np.sum(f * M) * (1.0 / n_mu) * (2 * np.pi / n_phi))
+
+
+def expected_env_image(kind):
+    cam = camera()
+    u = (np.arange(W) + 0.5) / W
+    v = (np.arange(H) + 0.5) / H
+    d = (cam["origin"][None, None, :].astype(np.float64) + cam["right"][None, None, :] * u[None, :, None]
+         + cam["bottom"][None, None, :] * v[:, None, None] - cam["location"])
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    mu_v = -d[..., 1]                                         # N = (0, 1, 0), V = -d
+    grid = np.linspace(mu_v.min() - 1e-3, min(mu_v.max() + 1e-3, 1.0), 16)
+    table = np.array([directional_albedo(kind, m) for m in grid])
+    return ENV * np.interp(mu_v, grid, table)
+
+
+_ENV_EXPECTED = {}
+# measured spread at 16,384 samples: 1.0 % per pixel diffuse, 1.5 % metal
+TOL_ENV_ORACLE = {"diffuse": (0.005, 0.05), "metal": (0.005, 0.05)}
+TOL_ENV_GPU = {"diffuse": (0.002, 0.02), "metal": (0.002, 0.02)}
+
+
+def env_expected_for(kind):
+    if kind not in _ENV_EXPECTED:
+        _ENV_EXPECTED[kind] = expected_env_image(kind)
+    return _ENV_EXPECTED[kind]
+
+
+@pytest.mark.parametrize("kind", sorted(FLOORS))
+def test_oracle_continuation_matches_albedo_quadrature(kind):
+    expected = env_expected_for(kind)
+    sc = floor_only_scene(kind)
+    b = sc["bvh"]
+    gt = b.pack_triangles(sc["obj"])
+    sh = b.pack_shading(sc["normals"], sc["obj"])
+    lo, hi = atlas_rt.mesh_bounds(b)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), 0, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    model = np.tile(np.eye(3, 4, dtype=F32).reshape(-1), (len(top.order), 1))
+    camd = camera()
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(F32)
+    spp = 4096
+    img = pyoracle.pathtrace(top.nodes_f32, inst[top.order].copy(), model, [(b.nodes_f32, gt, sh)], sc["materials"],
+                             np.zeros((0, 16), F32), camv, W, H, spp, max_bounces=1,
+                             environment=(ENV, ENV, ENV))[..., 0] / spp
+    tm, tp = TOL_ENV_ORACLE[kind]
+    assert abs(img.mean() - expected.mean()) / expected.mean() < tm, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=tp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", sorted(FLOORS))
+def test_gpu_continuation_matches_albedo_quadrature(kind):
+    import torch
+    expected = env_expected_for(kind)
+    ctx = atlas_rt.Context(device=0)
+    try:
+        ptscene.upload(ctx, floor_only_scene(kind))
+        ctx.set_environment((ENV, ENV, ENV))
+        cam = atlas_rt.make_camera(camera())
+        acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+        spp = 32768
+        ctx.pathtrace(cam, acc, acc64, spp=spp, max_bounces=1)
+        ctx.synchronize()
+        img = acc64.cpu().numpy()[:, 0].reshape(H, W) / spp
+        # the radiance cache refuses a scene with an environment
+        rc = atlas_rt.RadianceCache(ctx, (-10.0, -1.0, -10.0), (10.0, 3.0, 10.0), log2_table=12)
+        with pytest.raises(atlas_rt.AeRtError):
+            rc.render(cam, 0, acc)
+        rc.close()
+    finally:
+        ctx.close()
+    tm, tp = TOL_ENV_GPU[kind]
+    assert abs(img.mean() - expected.mean()) / expected.mean() < tm, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=tp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", sorted(FLOORS))
+@pytest.mark.parametrize("mode", ["direct", "environment"])
+def test_gpu_equals_oracle_sample_for_sample(kind, mode):
+    """Both sides draw the same random numbers (keyed by pixel, sample,
+    bounce and dimension), and on these one-bounce scenes no path can take a
+    different branch: every pixel agrees to float rounding, not statistically."""
+    import torch
+    sc = floor_only_scene(kind) if mode == "environment" else furnace_scene(kind)
+    mb = 1 if mode == "environment" else 0
+    env = (ENV, ENV, ENV) if mode == "environment" else None
+    spp = 64
+    ctx = atlas_rt.Context(device=0)
+    try:
+        mid, sh, lights, gt = ptscene.upload(ctx, sc)
+        if env:
+            ctx.set_environment(env)
+        acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+        ctx.pathtrace(atlas_rt.make_camera(camera()), acc, acc64, spp=spp, max_bounces=mb)
+        ctx.synchronize()
+        g = acc64.cpu().numpy().reshape(H, W, 3)
+    finally:
+        ctx.close()
+    b = sc["bvh"]
+    lo, hi = atlas_rt.mesh_bounds(b)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), mid, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    model = np.tile(np.eye(3, 4, dtype=F32).reshape(-1), (len(top.order), 1))
+    camd = camera()
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(F32)
+    c = pyoracle.pathtrace(top.nodes_f32, inst[top.order].copy(), model, [(b.nodes_f32, gt, sh)], sc["materials"],
+                           lights if mode == "direct" else np.zeros((0, 16), F32), camv, W, H, spp, max_bounces=mb,
+                           environment=env)
+    assert (c > 0).mean() > 0.5
+    np.testing.assert_allclose(g, c, rtol=2e-5, atol=1e-6)
