@@ -114,8 +114,9 @@ def upload(ctx, scene: dict):
     """Uploads mesh, shading triangles, the one-instance scene, materials and
     lights to an atlas_rt.Context.  Returns (mesh_id, shading, lights)."""
     bvh = scene["bvh"]
-    gt = bvh.pack_triangles(scene["obj"])
-    shading = bvh.pack_shading(scene["normals"], scene["obj"])
+    opacity = scene.get("opacity")          # per input triangle, optional (1)
+    gt = bvh.pack_triangles(scene["obj"], opacity)
+    shading = bvh.pack_shading(scene["normals"], scene["obj"], opacity)
     mid = ctx.upload_mesh(bvh.nodes, gt, shading)
     inst = np.array([make_instance(np.eye(4), mid, MASK_ALL | MASK_SHADOW)])
     lo, hi = mesh_bounds(bvh)

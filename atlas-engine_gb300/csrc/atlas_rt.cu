@@ -412,6 +412,8 @@ ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_
     DeviceMesh m;
     m.n_nodes = n_nodes;
     m.n_tris = n_tris;
+    if (shading)
+        for (uint32_t i = 0; i < n_tris && !m.transparent; i++) m.transparent = shading[i].d2[3] != 1.0f;
     auto upload = [&](float4** dst, const void* src, size_t bytes) -> cudaError_t {
         if (!bytes) return cudaSuccess;
         cudaError_t e = cudaMalloc(dst, bytes);
@@ -963,6 +965,12 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
     p.sc.env_g = ctx->env[1];
     p.sc.env_b = ctx->env[2];
     const bool env = ctx->env[0] + ctx->env[1] + ctx->env[2] > 0.0f;
+    // The engine traces with its opacity check (PathTracingRenderer.cpp:186;
+    // rayHit.csh:327-338): closest hits skip surfaces of opacity 0, shadow
+    // rays see the product of (1 - opacity).  With every opacity 1 that is
+    // the opaque traversal, which runs here unless a mesh is not opaque.
+    bool transparent = false;
+    for (const auto& m : ctx->meshes) transparent = transparent || m.transparent;
     // with MIS (light hits) or an environment (misses) a later bounce's
     // shading adds into the pixels that the previous bounce's resolve,
     // running beside it, adds into
@@ -1048,8 +1056,12 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
             p.shadow_pay = static_cast<float4*>(shadowPay[q]->ptr);
             p.n_shadow = ctx->d_pt_counts + 2 + q;
             p.shadow_occ = static_cast<const uint8_t*>(shadowOcc[q]->ptr);
-            ae_rt_status st = Trace(ctx, false, kSceneTarget, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), n,
-                                    0.0f, kInf, ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL);
+            const ae_packed_ray* rays_in = static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr);
+            ae_rt_status st = transparent
+                ? TraceTransparency(ctx, false, rays_in, n, 0.0f, kInf, AE_RT_MASK_ALL, ctx->pt_hits.ptr, stream,
+                                    ctx->d_pt_counts + in)
+                : Trace(ctx, false, kSceneTarget, rays_in, n, 0.0f, kInf, ctx->pt_hits.ptr, stream,
+                        ctx->d_pt_counts + in, AE_RT_MASK_ALL);
             if (st != AE_RT_OK) return st;
             // this shadow queue's previous resolve must be done before it is refilled
             if (pending[q]) AE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
@@ -1059,8 +1071,17 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
             AE_CUDA(ctx, cudaGetLastError());
             AE_CUDA(ctx, cudaEventRecord(ctx->pt_events[q], s));
             AE_CUDA(ctx, cudaStreamWaitEvent(side, ctx->pt_events[q], 0));
-            st = Trace(ctx, true, kSceneTarget, static_cast<const ae_packed_ray*>(shadowRays[q]->ptr), n, 0.0f, kInf,
-                       shadowOcc[q]->ptr, side, p.n_shadow, AE_RT_MASK_SHADOW, true);
+            const ae_packed_ray* shadow_in = static_cast<const ae_packed_ray*>(shadowRays[q]->ptr);
+            if (transparent) {
+                AE_CUDA(ctx, ctx->pt_vis[q].ensure(size_t(n) * sizeof(float)));
+                p.shadow_vis = static_cast<const float*>(ctx->pt_vis[q].ptr);
+                st = TraceTransparency(ctx, true, shadow_in, n, 0.0f, kInf, AE_RT_MASK_SHADOW, ctx->pt_vis[q].ptr, side,
+                                       p.n_shadow, true);
+            } else {
+                p.shadow_vis = nullptr;
+                st = Trace(ctx, true, kSceneTarget, shadow_in, n, 0.0f, kInf, shadowOcc[q]->ptr, side, p.n_shadow,
+                           AE_RT_MASK_SHADOW, true);
+            }
             if (st != AE_RT_OK) return st;
             atlas::rt::dev::pt_resolve_kernel<<<blocks, 256, 0, side>>>(p);
             AE_CUDA(ctx, cudaGetLastError());

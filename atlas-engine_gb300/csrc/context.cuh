@@ -20,6 +20,7 @@ struct DeviceMesh {
     float4* shading = nullptr;
     uint32_t n_nodes = 0;
     uint32_t n_tris = 0;
+    bool transparent = false;   // a shading triangle's opacity (d2.w) is not 1: opacity texture or partial
 };
 
 // Grow-only device scratch buffer.
@@ -77,6 +78,7 @@ struct ae_rt_ctx {
     // path tracer queues
     atlas::rt::host::Scratch pt_rays[2], pt_pay[2], pt_hits, pt_shadow, pt_shadow_pay, pt_occ;
     atlas::rt::host::Scratch pt_gb;     // real-time G-buffer matrices
+    atlas::rt::host::Scratch pt_vis[2]; // shadow visibility of the transparency traversal, per shadow queue
     // a second shadow queue: a bounce's shadow trace runs beside the next bounce's trace
     atlas::rt::host::Scratch pt_shadow2, pt_shadow_pay2, pt_occ2;
     cudaEvent_t pt_events[4] = { nullptr, nullptr, nullptr, nullptr };

@@ -73,6 +73,7 @@ struct PtParams {
     float4* shadow_pay;           // contribution.rgb, pixel bits
     uint32_t* n_shadow;
     const uint8_t* shadow_occ;
+    const float* shadow_vis;      // with transparent surfaces: the visibility prod(1 - opacity) per shadow ray
     float4* accum;                // W*H float4 (rgb, sample count in .w from raygen)
     double* accum64;              // W*H*3 or null
     uint32_t atomic_accum;        // several contributions per pixel and pass: add atomically
@@ -825,9 +826,16 @@ static __global__ void pt_shade_kernel(PtParams p) {
 static __global__ void pt_resolve_kernel(PtParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = min(*p.n_shadow, queue_capacity(p));
-    if (i >= n || p.shadow_occ[i]) return;
+    if (i >= n) return;
+    float vis = 1.0f;
+    if (p.shadow_vis) {
+        vis = p.shadow_vis[i];            // CheckVisibility's HitAnyTransparency (rayHit.csh:327-338)
+        if (!(vis > 0.0f)) return;
+    } else if (p.shadow_occ[i]) {
+        return;
+    }
     const float4 c = p.shadow_pay[i];
-    add_radiance(p, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+    add_radiance(p, __float_as_uint(c.w), v3(c.x, c.y, c.z) * vis);
 }
 
 }  // namespace atlas::rt::dev

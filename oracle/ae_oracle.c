@@ -998,6 +998,8 @@ typedef struct {
     uint32_t width, height, spp, sample_offset, max_bounces, seed;
     float epsilon;
     const float* env;      /* constant environment radiance of a miss (rayHit.csh:166-171), or NULL */
+    scene_t tsc;           /* the scene with its materials: the transparency variants */
+    int transparent;       /* a shading triangle's opacity is not 1: trace with the opacity check */
     double* accum;
     uint32_t begin, end;
     size_t stack_cap;
@@ -1239,7 +1241,9 @@ static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* ou
             float r8[8] = { ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, 0.0f, 1e12f };
             int32_t tp, ino;
             float tuv[3];
-            scene_closest_one(&j->sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
+            /* the engine's opacity check (PathTracingRenderer.cpp:186): closest
+             * hits skip surfaces of opacity 0 */
+            scene_closest_one(j->transparent ? &j->tsc : &j->sc, r8, 128u, stack, &tp, &ino, tuv, NULL, NULL);
             if (tp < 0) {
                 /* the environment, clamped per channel (rayHit.csh:166-171) */
                 if (j->env) {
@@ -1263,7 +1267,13 @@ static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* ou
                 if (sf.NdotL > 0.0f && lightPdf > 0.0f && contrib.x + contrib.y + contrib.z > 0.0f) {
                     v3 so = vadd(sf.P, vmul(sf.N, j->epsilon));
                     float s8[8] = { so.x, so.y, so.z, sf.L.x, sf.L.y, sf.L.z, 0.0f, dist - 2.0f * j->epsilon };
-                    if (!scene_any_one(&j->sc, s8, 64u, stack)) {
+                    if (j->transparent) {
+                        /* CheckVisibility: HitAnyTransparency (rayHit.csh:327-338) */
+                        float vis = scene_any_transparency_one(&j->tsc, s8, 64u, stack);
+                        if (vis > 0.0f) {
+                            out[0] += contrib.x * vis; out[1] += contrib.y * vis; out[2] += contrib.z * vis;
+                        }
+                    } else if (!scene_any_one(&j->sc, s8, 64u, stack)) {
                         out[0] += contrib.x; out[1] += contrib.y; out[2] += contrib.z;
                     }
                 }
@@ -1321,20 +1331,28 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    const float* cam, uint32_t width, uint32_t height,
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum) {
-    aeo_pathtrace_env(tlas, n_tlas, inst, inst_model, n_inst, meshes, n_meshes, materials, lights, n_lights, textures,
-                      n_textures, cam, width, height, spp, sample_offset, max_bounces, seed, epsilon, NULL, threads,
-                      accum);
+    aeo_pathtrace_env(tlas, n_tlas, inst, inst_model, n_inst, meshes, n_meshes, materials, 0xFFFFFFFFu, lights,
+                      n_lights, textures, n_textures, cam, width, height, spp, sample_offset, max_bounces, seed, epsilon,
+                      NULL, threads, accum);
 }
 
 void aeo_pathtrace_env(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
                        uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
-                       const float* lights, uint32_t n_lights, const aeo_texture* textures, uint32_t n_textures,
-                       const float* cam, uint32_t width, uint32_t height,
+                       uint32_t n_materials, const float* lights, uint32_t n_lights, const aeo_texture* textures,
+                       uint32_t n_textures, const float* cam, uint32_t width, uint32_t height,
                        uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                        const float* env, int threads, double* accum) {
     pt_job_t proto;
     memset(&proto, 0, sizeof(proto));
     proto.env = env;
+    {
+        scene_t tsc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, materials, n_materials, textures, n_textures };
+        proto.tsc = tsc;
+    }
+    for (uint32_t m = 0; m < n_meshes && !proto.transparent; m++)
+        if (meshes[m].shading)
+            for (uint32_t i = 0; i < meshes[m].n_tris && !proto.transparent; i++)
+                proto.transparent = meshes[m].shading[(size_t)i * 24 + 23] != 1.0f;
     scene_t sc = { tlas, n_tlas, inst, n_inst, meshes, n_meshes, NULL };
     proto.sc = sc;
     proto.inst_model = inst_model;

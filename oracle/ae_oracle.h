@@ -120,11 +120,13 @@ void aeo_pathtrace(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* in
                    uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                    int threads, double* accum);
 /* The same with a constant environment radiance env[3] added on a miss,
- * min(env * throughput, 10) per channel (rayHit.csh:166-171); NULL = none. */
+ * min(env * throughput, 10) per channel (rayHit.csh:166-171; NULL = none),
+ * and the material count that the opacity check (used when a shading
+ * triangle's opacity is not 1) bounds its material reads with. */
 void aeo_pathtrace_env(const aeo_node* tlas, uint32_t n_tlas, const aeo_instance* inst, const float* inst_model,
                        uint32_t n_inst, const aeo_mesh* meshes, uint32_t n_meshes, const float* materials,
-                       const float* lights, uint32_t n_lights, const aeo_texture* textures, uint32_t n_textures,
-                       const float* cam, uint32_t width, uint32_t height,
+                       uint32_t n_materials, const float* lights, uint32_t n_lights, const aeo_texture* textures,
+                       uint32_t n_textures, const float* cam, uint32_t width, uint32_t height,
                        uint32_t spp, uint32_t sample_offset, uint32_t max_bounces, uint32_t seed, float epsilon,
                        const float* env, int threads, double* accum);
 

@@ -63,8 +63,8 @@ def port():
         L.aeo_pathtrace.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U32,
                                     C.c_float, C.c_int, P]
         L.aeo_pathtrace.restype = None
-        L.aeo_pathtrace_env.argtypes = [P, U32, P, P, U32, P, U32, P, P, U32, P, U32, P, U32, U32, U32, U32, U32, U32,
-                                        C.c_float, P, C.c_int, P]
+        L.aeo_pathtrace_env.argtypes = [P, U32, P, P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32, U32, U32, U32,
+                                        U32, C.c_float, P, C.c_int, P]
         L.aeo_pathtrace_env.restype = None
         L.aeo_scene_any_glsl.restype = None
         L.aeo_scene_closest_transparency_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32,
@@ -377,7 +377,7 @@ def pathtrace(tlas_f32, instances, inst_model, meshes, materials, lights, cam, w
     ttab, ntex, tkeep = _texture_table(textures)
     env = None if environment is None else _c(environment, np.float32).reshape(3)
     port().aeo_pathtrace_env(tlas_f32.ctypes.data, len(tlas_f32), inst.ctypes.data, model.ctypes.data, len(inst),
-                             table, len(meshes), mats.ctypes.data, lights.ctypes.data, len(lights), ttab, ntex,
+                             table, len(meshes), mats.ctypes.data, len(mats), lights.ctypes.data, len(lights), ttab, ntex,
                              cam.ctypes.data, width, height, spp, sample_offset, max_bounces, seed, epsilon,
                              None if env is None else env.ctypes.data, threads, out.ctypes.data)
     return out

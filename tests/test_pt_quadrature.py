@@ -334,3 +334,93 @@ def test_gpu_equals_oracle_sample_for_sample(kind, mode):
                            environment=env)
     assert (c > 0).mean() > 0.5
     np.testing.assert_allclose(g, c, rtol=2e-5, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# The opacity check: transparent surfaces in the path tracer's traversals
+# ---------------------------------------------------------------------------
+#
+# The engine traces the path tracer's rays with its opacity check
+# (PathTracingRenderer.cpp:186; CheckLeafClosestTransparency, bvh.hsh:106-134:
+# a hit counts where its opacity is > 0) and weights each light sample by
+# HitAnyTransparency (rayHit.csh:327-338).  Each case adds one large triangle
+# to the direct-light scene:
+#   * "half": opacity 0.5 between the floor and the light.  The shadow rays
+#     visit its leaf alone, so their visibility is 1 * (1 * 0.5): every light
+#     sample loses half (HitAnyTransparency multiplies the running value into
+#     each leaf's result again, bvh.hsh:495, so a ray through several partly
+#     transparent leaves would lose more; that order-dependent case is pinned
+#     against the oracle's restatement in tests/test_transparency_gpu.py).
+#   * "clear": opacity 0 between the camera and the floor: the camera sees
+#     through it and the shadow rays lose nothing.
+
+SHEETS = {"half": (1.8, 0.5, 0.5), "clear": (1.0, 0.0, 1.0)}     # (height, opacity, expected factor)
+
+
+def sheet_scene(case, kind="diffuse"):
+    sc = furnace_scene(kind)
+    y, opa, _ = SHEETS[case]
+    tri = np.array([[[-10.0, y, -10.0], [-10.0, y, 30.0], [30.0, y, -10.0]]], F32)   # covers x, z in [-10, 10]
+    tris = np.concatenate([sc["tris"], tri]).astype(F32)
+    obj = np.concatenate([sc["obj"], np.array([2], np.int32)])
+    normals = np.concatenate([sc["normals"], np.tile(np.array([0, 1, 0], F32), (1, 3, 1))]).astype(F32)
+    mats = np.zeros(3, MATERIAL_DTYPE)
+    mats[:2] = sc["materials"]
+    mats[2] = sc["materials"][0]
+    mats[2]["ID"] = 2
+    opacity = np.array([1, 1, 1, 1, opa], F32)
+    sc.update(tris=tris, obj=obj, normals=normals, materials=mats, bvh=BVH(tris), opacity=opacity)
+    return sc
+
+
+def _oracle_image(sc, spp, mb):
+    b = sc["bvh"]
+    gt = b.pack_triangles(sc["obj"], sc.get("opacity"))
+    sh = b.pack_shading(sc["normals"], sc["obj"], sc.get("opacity"))
+    lights = ptscene.lights_for(sc, sh)
+    lo, hi = atlas_rt.mesh_bounds(b)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), 0, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)])
+    model = np.tile(np.eye(3, 4, dtype=F32).reshape(-1), (len(top.order), 1))
+    camd = camera()
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(F32)
+    return pyoracle.pathtrace(top.nodes_f32, inst[top.order].copy(), model, [(b.nodes_f32, gt, sh)],
+                              sc["materials"], lights, camv, W, H, spp, max_bounces=mb)
+
+
+@pytest.mark.parametrize("case", sorted(SHEETS))
+def test_oracle_opacity_check_matches_quadrature(case):
+    expected = SHEETS[case][2] * expected_for("diffuse")
+    spp = 4096
+    img = _oracle_image(sheet_scene(case), spp, 0)[..., 0] / spp
+    tm, tp = TOL_ORACLE["diffuse"]
+    assert abs(img.mean() - expected.mean()) / expected.mean() < tm, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=tp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(SHEETS))
+def test_gpu_opacity_check_matches_quadrature_and_oracle(case):
+    import torch
+    expected = SHEETS[case][2] * expected_for("diffuse")
+    sc = sheet_scene(case)
+    ctx = atlas_rt.Context(device=0)
+    try:
+        ptscene.upload(ctx, sc)
+        cam = atlas_rt.make_camera(camera())
+        acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+        ctx.pathtrace(cam, acc, acc64, spp=32768, max_bounces=0)
+        ctx.synchronize()
+        img = acc64.cpu().numpy()[:, 0].reshape(H, W) / 32768
+        acc64.zero_()
+        ctx.pathtrace(cam, acc, acc64, spp=64, max_bounces=0)
+        ctx.synchronize()
+        g64 = acc64.cpu().numpy().reshape(H, W, 3)
+    finally:
+        ctx.close()
+    tm, tp = TOL_GPU["diffuse"]
+    assert abs(img.mean() - expected.mean()) / expected.mean() < tm, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=tp)
+    # the same random numbers as the oracle: equal sample for sample
+    np.testing.assert_allclose(g64, _oracle_image(sc, 64, 0), rtol=2e-5, atol=1e-6)
