@@ -232,6 +232,8 @@ ae_rt_status CheckTrainArgs(ae_rc* rc, const ae_camera* cam, uint32_t n_paths, u
     if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
     if (ctx->env[0] + ctx->env[1] + ctx->env[2] > 0.0f)
         return RcFail(rc, AE_RT_INVALID_ARG, "the radiance cache models no environment; set it black");
+    for (const auto& m : ctx->meshes)
+        if (m.transparent) return RcFail(rc, AE_RT_INVALID_ARG, "the radiance cache traces opaque scenes only");
     if (n_paths == 0 || steps == 0 || n_paths < steps) return RcFail(rc, AE_RT_INVALID_ARG, "bad training sizes");
     if (max_bounces == 0 || max_bounces > 16) return RcFail(rc, AE_RT_INVALID_ARG, "max_bounces out of range");
     return AE_RT_OK;
@@ -585,6 +587,8 @@ ae_rt_status ae_rc_render(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint3
     if (!ctx->scene_ready || !ctx->d_materials) return RcFail(rc, AE_RT_INVALID_ARG, "no scene / materials set");
     if (ctx->env[0] + ctx->env[1] + ctx->env[2] > 0.0f)
         return RcFail(rc, AE_RT_INVALID_ARG, "the radiance cache models no environment; set it black");
+    for (const auto& m : ctx->meshes)
+        if (m.transparent) return RcFail(rc, AE_RT_INVALID_ARG, "the radiance cache traces opaque scenes only");
     if (!DevPtr(accum)) return RcFail(rc, AE_RT_INVALID_ARG, "accumulation buffer must be device memory");
     RC_CUDA(rc, cudaSetDevice(ctx->device));
     return RenderFrame(rc, cam, frame, last_bounce, accum, static_cast<cudaStream_t>(stream));

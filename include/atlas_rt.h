@@ -629,7 +629,8 @@ ae_rt_status ae_rt_scene_set_lights(ae_rt_ctx* ctx, const ae_light* lights, uint
  * finite, >= 0; initially black), added as min(radiance * throughput, 10) per
  * channel on every miss, the camera's included (EvaluateBounce,
  * rayHit.csh:166-171, where the engine samples its sky cubemap).  The
- * radiance cache models no environment: its calls refuse a non-black one. */
+ * radiance cache models no environment: its calls refuse a non-black one,
+ * and a scene with a mesh that is not opaque (shading opacity other than 1). */
 ae_rt_status ae_rt_scene_set_environment(ae_rt_ctx* ctx, const float radiance[3]);
 
 /* The light list the engine builds on the host before each path-tracing

@@ -417,6 +417,11 @@ def test_gpu_opacity_check_matches_quadrature_and_oracle(case):
         ctx.pathtrace(cam, acc, acc64, spp=64, max_bounces=0)
         ctx.synchronize()
         g64 = acc64.cpu().numpy().reshape(H, W, 3)
+        # the radiance cache refuses a scene that is not opaque
+        rc = atlas_rt.RadianceCache(ctx, (-10.0, -1.0, -10.0), (10.0, 3.0, 10.0), log2_table=12)
+        with pytest.raises(atlas_rt.AeRtError):
+            rc.render(cam, 0, acc)
+        rc.close()
     finally:
         ctx.close()
     tm, tp = TOL_GPU["diffuse"]
