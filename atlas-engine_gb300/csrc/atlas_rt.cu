@@ -28,7 +28,7 @@ using atlas::rt::dev::TraceParams;
 // project's autotuner): warps per CTA and the shared-memory part of each
 // lane's 64-entry traversal stack (the rest spills to local memory).  The
 // register budget follows from the minimum resident CTAs per SM.
-constexpr int kStackEntries = 64;
+constexpr int kStackEntries = 128;
 struct Shape {
     int warps;
     int smem;

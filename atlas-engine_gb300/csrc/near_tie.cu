@@ -23,7 +23,7 @@ using namespace atlas::rt::host;
 
 namespace {
 
-constexpr uint32_t kRetestStack = 64;
+constexpr uint32_t kRetestStack = 128;
 
 struct RetestParams {
     const float4* nodes;

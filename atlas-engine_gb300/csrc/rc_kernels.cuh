@@ -525,7 +525,8 @@ template <bool ANY>
 __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, float oz, float dx, float dy, float dz,
                                    float tmin, float tmax, float& tOut, int32_t& triOut, int32_t& instOut,
                                    float& uOut, float& vOut) {
-    int32_t stack[64];
+    constexpr int kInlineStack = 128;
+    int32_t stack[kInlineStack];
     TRay wr{};
     wr.ox = ox; wr.oy = oy; wr.oz = oz; wr.dx = dx; wr.dy = dy; wr.dz = dz;
     wr.prepare();
@@ -609,7 +610,7 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
                 far = leftFirst ? rptr : lptr;
             }
             if (il && ir) {
-                if (sp >= 64) break;
+                if (sp >= kInlineStack) break;
                 stack[sp++] = far;
             } else if (!il && !ir) {
                 if (sp == 0) break;

@@ -29,7 +29,7 @@ using namespace atlas::rt::dev;
 
 namespace {
 
-constexpr uint32_t kTransStack = 64;
+constexpr uint32_t kTransStack = 128;
 
 struct TransParams {
     const float4* tlas;

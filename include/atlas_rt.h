@@ -345,7 +345,7 @@ typedef struct ae_rt_ctx ae_rt_ctx;
 /* Launch shape of the traversal kernels; the project's autotuner
  * (atlas_rt.autotune) picks these per workload.  Supported
  * (threads_per_block, stack_entries_smem) pairs: (128, 32) default, (64, 32),
- * (256, 16), (128, 16); each lane has 64 stack entries in total, the rest in
+ * (256, 16), (128, 16); each lane has 128 stack entries in total, the rest in
  * local memory. */
 typedef struct ae_rt_config {
     int32_t device;               /* CUDA device ordinal */

@@ -238,11 +238,15 @@ def test_stack_overflow_is_reported(ctx):
     with pytest.raises(atlas_rt.AeRtError) as e:
         ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
     assert e.value.status == 6
-    # a shallow comb traverses fine and misses
-    nodes, tris = comb_bvh(20)
-    mid = ctx.upload_mesh(nodes, tris)
-    hits = ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
-    assert hits["triPtr"][0] == -1
+    # shallower combs traverse fine and miss: 100 levels need more than 64
+    # entries, which a 65-deep top level (100,000 clustered boxes) over a
+    # 32-deep bottom level (the builder's depth cap, BVH.cpp:253) can need
+    for depth in (20, 100):
+        nodes, tris = comb_bvh(depth)
+        mid = ctx.upload_mesh(nodes, tris)
+        hits = ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
+        assert hits["triPtr"][0] == -1
+        assert not ctx.trace_any(mid, packed(rays8), 0.0, 10.0)[0]
 
 
 def test_step_cap_is_reported():
