@@ -2,8 +2,10 @@
 
 Both sides draw the same random numbers (PCG hash keyed by pixel, sample,
 bounce, dimension); their transcendental functions and summation orders
-differ, so individual paths can diverge and the comparison is statistical:
-at high sample counts the two images must agree to within their noise.
+differ, so a path can diverge where rounding sends it down another branch.
+Two comparisons follow: path for path (at low sample counts nearly every
+pixel equals the oracle's to 1e-4) and statistical (at high sample counts
+the two images agree to within their noise).
 """
 import numpy as np
 import pytest
