@@ -26,7 +26,7 @@ using atlas::rt::dev::TraceParams;
 
 // Kernel shapes the context can run (chosen by ae_rt_config, tuned by the
 // project's autotuner): warps per CTA and the shared-memory part of each
-// lane's 64-entry traversal stack (the rest spills to local memory).  The
+// lane's 128-entry traversal stack (the rest spills to local memory).  The
 // register budget follows from the minimum resident CTAs per SM.
 constexpr int kStackEntries = 128;
 struct Shape {
@@ -131,7 +131,7 @@ ae_rt_status ValidateBlas(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_t n_n
 
 uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
     if (ctx->max_steps_cfg) return ctx->max_steps_cfg;
-    return 4u * m.n_nodes + 64u;
+    return atlas::rt::dev::default_step_cap(m.n_nodes);
 }
 
 // Persistent grid for `fn`: SMs x resident CTAs (the configured count, or the

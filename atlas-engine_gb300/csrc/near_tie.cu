@@ -194,7 +194,7 @@ extern "C" ae_rt_status ae_rt_retest_near_ties(ae_rt_ctx* ctx, int32_t mesh_id, 
     p.n = n_rays;
     p.tmin = tmin;
     p.tmax = tmax;
-    p.max_steps = 4u * m.n_nodes + 64u;
+    p.max_steps = atlas::rt::dev::default_step_cap(m.n_nodes);
     p.out = out;
     AE_CUDA(ctx, ctx->retest_count.ensure(sizeof(uint32_t)));
     p.n_retested = static_cast<uint32_t*>(ctx->retest_count.ptr);

@@ -97,6 +97,14 @@ struct BatchDesc {
 };
 static_assert(sizeof(BatchDesc) == 64, "batch descriptor layout");
 
+// Default per-ray step cap of a BVH with n_nodes nodes: a valid tree visits
+// each node at most once per ray, so 4 n + 64 never cuts a correct traversal
+// short.  Computed in 64 bits and saturated, so that arrays of 2^30 nodes and
+// more (64 GB of nodes fits in HBM) do not wrap to a small cap.
+__host__ __device__ constexpr uint32_t default_step_cap(uint32_t n_nodes) {
+    return 4ull * n_nodes + 64ull > 0xffffffffull ? 0xffffffffu : uint32_t(4ull * n_nodes + 64ull);
+}
+
 // ae_rt_config::refill_below when left 0 (lanes; 0 = never refill early):
 // measured best with a 32-step burst on the terrain + boxes camera pass
 // (0.913 against 0.974 ms for 64 steps and no early refill).

@@ -23,8 +23,11 @@
 namespace {
 
 constexpr int kWarps = 4;
+// 128 stack entries per lane, as in every other trace entry point: 32 in
+// shared memory, the rest in local memory (touched only by deep rays)
+constexpr int kStackEntries = 128;
 constexpr int kSmemStack = 32;
-constexpr int kSpillStack = 32;
+constexpr int kSpillStack = kStackEntries - kSmemStack;
 constexpr int kMinBlocks = 8;
 constexpr uint32_t kScratchWords = 64;     // 256 bytes; this call uses words 0 (counter) and 1 (errors)
 constexpr uint32_t kWordsUsed = 2;
@@ -50,13 +53,16 @@ void* NoAllocKernel() {
                                        kMinBlocks, true>);
 }
 
-bool IsDeviceMemory(const void* p) {
+// Device (or managed) memory of device `dev`.  A buffer of another GPU is
+// refused: without peer access the kernel could not read it.
+bool IsDeviceMemory(const void* p, int dev) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 // Once per device, with that device current: the scratch symbol's device
@@ -96,15 +102,15 @@ extern "C" ae_rt_status ae_rt_trace_closest_noalloc(const ae_bvh_node* nodes, ui
     if (n_rays > AE_RT_NOALLOC_MAX_RAYS) return AE_RT_INVALID_ARG;   // the 32-bit work counter's range
     if (!rays || !hits || (n_nodes && !nodes) || (n_tris && !tris)) return AE_RT_INVALID_ARG;
     if (n_nodes >= (1u << 31) - 1 || n_tris >= (1u << 31) - 1) return AE_RT_INVALID_ARG;
-    if (!IsDeviceMemory(rays) || !IsDeviceMemory(hits) || (n_nodes && !IsDeviceMemory(nodes)) ||
-        (n_tris && !IsDeviceMemory(tris)))
-        return AE_RT_INVALID_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return AE_RT_CUDA_ERROR;
     }
     if (dev < 0 || dev >= kMaxDevices) return AE_RT_INVALID_ARG;
+    if (!IsDeviceMemory(rays, dev) || !IsDeviceMemory(hits, dev) || (n_nodes && !IsDeviceMemory(nodes, dev)) ||
+        (n_tris && !IsDeviceMemory(tris, dev)))
+        return AE_RT_INVALID_ARG;
     DeviceSetup* s = nullptr;
     ae_rt_status st = SetupDevice(dev, &s);
     if (st != AE_RT_OK) return st;
@@ -129,7 +135,7 @@ extern "C" ae_rt_status ae_rt_trace_closest_noalloc(const ae_bvh_node* nodes, ui
     p.work_counter = s->scratch;
     p.error_word = s->scratch + 1;
     p.fetch_counts = nullptr;
-    p.max_steps = 4u * n_nodes + 64u;
+    p.max_steps = atlas::rt::dev::default_step_cap(n_nodes);
     uint32_t grid = s->grid;
     const uint32_t needed = (n_rays + kWarps * 32 - 1) / (kWarps * 32);
     if (needed < grid) grid = needed;

@@ -488,7 +488,8 @@ void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan);
  *    need not have passed the upload validator: node and triangle indices are
  *    range-checked on the device, and a bad one ends that ray with
  *    AE_HIT_OVERFLOW in its flags.
- *  - Results and semantics are those of ae_rt_trace_closest.  The call is
+ *  - Results and semantics are those of ae_rt_trace_closest, with the same
+ *    128-entry traversal stack per ray.  The call is
  *    asynchronous on `stream` (NULL = legacy default stream) and reports
  *    device-side failures per ray in ae_hit.flags (AE_HIT_OVERFLOW,
  *    AE_HIT_ITER_CAP) rather than through a status.
@@ -498,7 +499,8 @@ void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan);
  *  - The first call on a device looks up that array's device address and
  *    the kernel's occupancy; make it before any stream capture.
  *  - n_rays above AE_RT_NOALLOC_MAX_RAYS is rejected with AE_RT_INVALID_ARG
- *    (the work counter is 32 bits wide), as are host pointers. */
+ *    (the work counter is 32 bits wide), as are host pointers and device
+ *    pointers of a GPU other than the current one. */
 #define AE_RT_NOALLOC_MAX_RAYS (1u << 30)
 ae_rt_status ae_rt_trace_closest_noalloc(const ae_bvh_node* nodes, uint32_t n_nodes,
                                          const ae_bvh_triangle* tris, uint32_t n_tris,

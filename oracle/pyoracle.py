@@ -21,7 +21,23 @@ import numpy as np
 ORACLE_DIR = Path(__file__).resolve().parent
 PORT_LIB = ORACLE_DIR / "_build" / "libaeoracle.so"
 REF_LIB = ORACLE_DIR / "_ref" / "libaeref.so"
-REFERENCE_ROOT = Path(os.environ.get("AE_REFERENCE_ROOT", "/root/reference"))
+
+
+def _reference_root() -> Path:
+    """Where the reference tree lies: AE_REFERENCE_ROOT, else the location the
+    oracle's build recipe (oracle/Makefile, REFERENCE_ROOT) names."""
+    env = os.environ.get("AE_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", str(ORACLE_DIR), "reference-root"],
+                           check=True, capture_output=True, text=True)
+        return Path(r.stdout.strip())
+    except (OSError, subprocess.CalledProcessError):
+        return ORACLE_DIR / "_no_reference"
+
+
+REFERENCE_ROOT = _reference_root()
 
 P = C.c_void_p
 U32 = C.c_uint32

@@ -73,3 +73,63 @@ def test_two_ranks_gloo():
     assert (b0, e1) == (0, n) and e0 == b1
     assert s0 + s1 == float(np.arange(n, dtype=np.float64).sum())
     assert t0 == t1 == [2.0, 5.0]
+
+
+def _trace_worker(rank, world, port, q):
+    """Each rank traces its ray shard with the oracle's shader-order closest
+    query; the shards are gathered on every rank (the test's check only: the
+    product path has no collective)."""
+    import sys
+    from pathlib import Path
+    import torch.distributed as dist
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+    import pyoracle
+    from atlas_rt import BVH, scenes
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        tris = scenes.random_triangles(4000, seed=31)
+        bvh = BVH(tris)
+        gt = bvh.pack_triangles()
+        o, d = scenes.sphere_rays(20011, seed=32)
+        r8 = scenes.rays8(o, d, 1e-4, 10.0)
+        begin, end = ray_shard(len(r8), rank, world)
+        ptr, tuv = pyoracle.closest_glsl(bvh.nodes_f32, gt, r8[begin:end], threads=2)
+        parts = [None] * world
+        dist.all_gather_object(parts, (begin, end, ptr, tuv))
+        q.put((rank, parts))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_shards_equal_unsharded_trace():
+    """World size 2 over gloo: the gathered per-rank closest hits of the
+    sharded rays equal the unsharded trace bit for bit."""
+    import sys
+    from pathlib import Path
+    import torch.multiprocessing as mp
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+    import pyoracle
+    from atlas_rt import BVH, scenes
+    pyoracle.build_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_trace_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=180) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    tris = scenes.random_triangles(4000, seed=31)
+    bvh = BVH(tris)
+    o, d = scenes.sphere_rays(20011, seed=32)
+    ptr, tuv = pyoracle.closest_glsl(bvh.nodes_f32, bvh.pack_triangles(), scenes.rays8(o, d, 1e-4, 10.0))
+    for _, parts in res:
+        parts = sorted(parts, key=lambda x: x[0])
+        assert parts[0][0] == 0 and parts[-1][1] == len(ptr) and parts[0][1] == parts[1][0]
+        assert np.array_equal(np.concatenate([p[2] for p in parts]), ptr)
+        assert np.array_equal(np.concatenate([p[3] for p in parts]).view(np.uint32), tuv.view(np.uint32))
+    assert (ptr >= 0).sum() > 1000
