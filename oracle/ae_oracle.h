@@ -41,6 +41,19 @@ typedef struct aeo_tri {
     float v2[4];
 } aeo_tri;
 
+/* The reference builder restated (oracle/ae_oracle_build.cpp, BVH.cpp:14-100,
+ * :249-870): the triangle BVH (triangle i gets original index i) and the
+ * AABB-only BVH of the top level (boxes: n * 6 floats, min then max).  The
+ * handle holds the 64-byte nodes and, per BVH-order primitive, its original
+ * index and end-of-leaf flag.  Empty input gives an empty tree. */
+typedef struct aeo_bvh aeo_bvh;
+aeo_bvh* aeo_build_triangles(const float* verts, uint32_t n_tris, int parallel);
+aeo_bvh* aeo_build_aabbs(const float* boxes, uint32_t n, int parallel);
+uint32_t aeo_bvh_node_count(const aeo_bvh* h);
+uint32_t aeo_bvh_prim_count(const aeo_bvh* h);
+void aeo_bvh_get(const aeo_bvh* h, aeo_node* nodes, uint32_t* order, uint8_t* end_of_node);
+void aeo_bvh_free(aeo_bvh* h);
+
 /* Host closest-hit query (BVH.cpp:103-174).  tri_ptr = BVH-order index of the
  * closest triangle or -1; tuv = (t, u, v) of that hit. */
 void aeo_closest_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,

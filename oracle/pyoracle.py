@@ -47,7 +47,7 @@ _ref = None
 
 
 def build_port(force: bool = False) -> Path:
-    src = [ORACLE_DIR / "ae_oracle.c", ORACLE_DIR / "ae_oracle.h"]
+    src = [ORACLE_DIR / "ae_oracle.c", ORACLE_DIR / "ae_oracle_build.cpp", ORACLE_DIR / "ae_oracle.h"]
     if force or not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in src):
         subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "port"], check=True)
     return PORT_LIB
@@ -91,6 +91,18 @@ def port():
         L.aeo_scene_any_transparency_glsl.restype = None
         L.aeo_sample_r_bilinear.argtypes = [P, U32, C.c_int32, C.c_float, C.c_float]
         L.aeo_sample_r_bilinear.restype = C.c_float
+        L.aeo_build_triangles.argtypes = [P, U32, C.c_int]
+        L.aeo_build_triangles.restype = P
+        L.aeo_build_aabbs.argtypes = [P, U32, C.c_int]
+        L.aeo_build_aabbs.restype = P
+        L.aeo_bvh_node_count.argtypes = [P]
+        L.aeo_bvh_node_count.restype = U32
+        L.aeo_bvh_prim_count.argtypes = [P]
+        L.aeo_bvh_prim_count.restype = U32
+        L.aeo_bvh_get.argtypes = [P, P, P, P]
+        L.aeo_bvh_get.restype = None
+        L.aeo_bvh_free.argtypes = [P]
+        L.aeo_bvh_free.restype = None
         L.aeo_half_to_float.argtypes = [C.c_uint16]
         L.aeo_half_to_float.restype = C.c_float
         for f in (L.aeo_closest_cpu, L.aeo_any_cpu, L.aeo_closest_glsl, L.aeo_any_glsl, L.aeo_closest_f64_brute):
@@ -156,6 +168,41 @@ def any_cpu(nodes_f32, tris_f32, rays8, threads=os.cpu_count()):
     port().aeo_any_cpu(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
                        rays8.ctypes.data, n, threads, occ.ctypes.data)
     return occ
+
+
+def build_bvh(verts=None, boxes=None, parallel=True):
+    """The reference builder restated (oracle/ae_oracle_build.cpp): triangles
+    (n, 3, 3) float32, or boxes (n, 6) for the top-level tree.  Returns
+    (nodes (m, 16) float32 in the 64-byte node layout, order uint32,
+    end_of_node uint8)."""
+    L = port()
+    if boxes is not None:
+        b = _c(np.asarray(boxes, np.float32).reshape(-1, 6), np.float32)
+        h = L.aeo_build_aabbs(b.ctypes.data if len(b) else None, len(b), int(parallel))
+    else:
+        v = _c(np.asarray(verts, np.float32).reshape(-1, 9), np.float32)
+        h = L.aeo_build_triangles(v.ctypes.data if len(v) else None, len(v), int(parallel))
+    try:
+        nn, npr = L.aeo_bvh_node_count(h), L.aeo_bvh_prim_count(h)
+        nodes = np.zeros((nn, 16), np.float32)
+        order = np.zeros(npr, np.uint32)
+        eon = np.zeros(npr, np.uint8)
+        L.aeo_bvh_get(h, nodes.ctypes.data if nn else None, order.ctypes.data if npr else None,
+                      eon.ctypes.data if npr else None)
+    finally:
+        L.aeo_bvh_free(h)
+    return nodes, order, eon
+
+
+def pack_bvh_triangles(verts, order, eon):
+    """GPUBVHTriangle rows (n, 12) float32 in BVH order, as MeshData.cpp:241-248
+    packs them with material 0 and opacity 1."""
+    v = np.asarray(verts, np.float32).reshape(-1, 9)[order]
+    out = np.zeros((len(order), 12), np.float32)
+    out[:, 0:3], out[:, 4:7], out[:, 8:11] = v[:, 0:3], v[:, 3:6], v[:, 6:9]
+    out[:, 3] = np.where(eon > 0, 1.0, -1.0)
+    out[:, 11] = 1.0
+    return out
 
 
 def closest_glsl(nodes_f32, tris_f32, rays8, threads=os.cpu_count(), counters=False):

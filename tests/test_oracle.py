@@ -130,3 +130,51 @@ def test_port_vs_compiled_reference_fresh_seeds(seed, n):
     assert np.array_equal(idx2, idx.astype(np.int64))
     assert np.array_equal(tuv2.view(np.uint32), tuv.view(np.uint32))
     assert np.array_equal(pyoracle.any_cpu(r.nodes_f32, gt, rays), r.any(rays))
+
+
+# ---- the oracle's restatement of the reference builder (ae_oracle_build.cpp) ----
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("parallel", [True, False])
+def test_oracle_builder_matches_reference_small(golden, name, parallel):
+    g, _ = golden
+    nodes, order, eon = pyoracle.build_bvh(g[f"{name}/tris"], parallel=parallel)
+    assert np.array_equal(nodes.view(np.uint32), g[f"{name}/nodes"].view(np.uint32))
+    assert np.array_equal(order, g[f"{name}/order"])
+    assert np.array_equal(eon, g[f"{name}/end_of_node"])
+
+
+@pytest.mark.parametrize("which", ["random65536", "terrain_boxes"])
+def test_oracle_builder_matches_reference_full_size(golden, which):
+    _, dg = golden
+    d = dg[which]
+    tris = scenes.random_triangles() if which == "random65536" else scenes.terrain_boxes()[0]
+    nodes, order, eon = pyoracle.build_bvh(tris)
+    assert len(nodes) == d["nodes"] and len(order) == d["primitives"]
+    assert sha(nodes) == d["nodes_sha"]
+    assert sha(order) == d["order_sha"]
+    assert sha(eon) == d["eon_sha"]
+
+
+def test_oracle_builder_empty():
+    nodes, order, eon = pyoracle.build_bvh(np.zeros((0, 3, 3), np.float32))
+    assert len(nodes) == 0 and len(order) == 0
+    nodes, order, eon = pyoracle.build_bvh(boxes=np.zeros((0, 6), np.float32))
+    assert len(nodes) == 0 and len(order) == 0
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 64, 1000])
+def test_oracle_aabb_builder_matches_compiled_reference(n):
+    """The top-level (AABB-only) builder, including the one-box special node,
+    against the reference compiled here (skipped where the reference tree is
+    absent)."""
+    if pyoracle.build_ref() is None:
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(40 + n)
+    lo = rng.uniform(-50, 50, (n, 3)).astype(np.float32)
+    boxes = np.concatenate([lo, lo + rng.uniform(0.1, 8, (n, 3)).astype(np.float32)], 1)
+    ref_nodes, ref_order = pyoracle.ref_build_aabbs(boxes)
+    nodes, order, eon = pyoracle.build_bvh(boxes=boxes)
+    assert np.array_equal(nodes.view(np.uint32), ref_nodes.view(np.uint32))
+    assert np.array_equal(order, ref_order)
+    assert eon[-1] == 1
