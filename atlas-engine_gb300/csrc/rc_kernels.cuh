@@ -598,7 +598,8 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
             float hl, hr;
             bool il, ir;
-            test_children<false>(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, hl, hr);
+            bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
+            test_children<false>(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, hl, hr, nearCullUnused);
             const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
             int32_t next, far;
             if (ANY) {

@@ -148,14 +148,38 @@ __device__ __forceinline__ bool in_fast_range(float v, bool zero_ok) {
     return (zero_ok && m == 0.0f) || (m >= kFastLo && m <= kFastHi);
 }
 
+// Near ties.  The nearest triangle of a closest-hit ray is decided by FP32
+// rounding when a second triangle lies within 1e-6 relative t of it; such
+// rays carry kHitFlagNearTie and are re-tested in double.  The flag must
+// cover every ray whose two nearest double-precision hits are that close,
+// including hits the FP32 traversal never sees, so it is set (a superset)
+// when any of these holds:
+//  * a second accepted triangle lies within kTieWindow relative t of the
+//    nearest (1e-6 plus the FP32 error of the two distances);
+//  * a child box rejected by the shader's test had its entry within
+//    kTieWindow of the bound it was tested against (its triangles could tie
+//    with the final hit, which is at most that bound);
+//  * a triangle rejected by the FP32 test lies within the rounding error of
+//    its barycentric tests (near_miss) at a distance up to kTieWindow past
+//    the current nearest hit -- a shared edge, where either side's FP32 test
+//    may fail;
+//  * the shader's descent dropped a hit right child whose entry equals the
+//    bound (bvh.hsh:234-236: a missed left child reports the bound too, and
+//    hitL <= hitR then picks it).
+// None of this changes which triangle the traversal returns.
+constexpr float kTieWindow = 4e-6f;
+constexpr float kTieWiden = 1.0f + kTieWindow;
+constexpr float kNearMissScale = 9.5367431640625e-07f;   // 2^-20
+
 // IntersectAABB(ray, aabb, tmin, tmax, out dist) -- intersections.hsh:18-34.
 // FAST: quotients through div_rn_from_rcp with (yx, yy, yz) = RN(1/d); the
-// result is bit-identical to the div.rn form.
+// result is bit-identical to the div.rn form.  nearCull: the box was
+// rejected but its entry lies within kTieWindow of the exit bound.
 template <bool FAST>
 __device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx, float dy, float dz,
                                          float yx, float yy, float yz,
                                          float lx, float ly, float lz, float hx, float hy, float hz,
-                                         float tmin, float tmax, float& dist) {
+                                         float tmin, float tmax, float& dist, bool& nearCull) {
     float t0x, t0y, t0z, t1x, t1y, t1z;
     if (FAST) {
         t0x = div_rn_from_rcp(fsub(lx, ox), dx, yx);
@@ -174,6 +198,7 @@ __device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx,
     const float tmaxf = fminf(fminf(tmax, bx), fminf(by, bz));
     const bool hit = tminf <= tmaxf;
     dist = hit ? tminf : tmax;
+    nearCull = !hit && tminf <= fmul(tmaxf, kTieWiden);
     return hit;
 }
 
@@ -197,6 +222,35 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
     u = fdiv(fadd(fadd(fmul(qx, sx), fmul(qy, sy)), fmul(qz, sz)), den);
     v = fdiv(fadd(fadd(fmul(px, dx), fmul(py, dy)), fmul(pz, dz)), den);
     return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
+}
+
+// A triangle whose FP32 test failed within the rounding error of its
+// barycentric coordinates (u, v as tri_test computed them).  With the L1
+// norms Sd, S0, S1, Ss of d, e0, e1 and s = o - v0, every operation of the
+// formula contributes at most a few ulps of products bounded by Sd (S0+S1)
+// (Ss+S0+S1), so |error(u)|, |error(v)| < beta = 2^-20 K with
+// K = Sd (S0+S1) (Ss+S0+S1) / |den| (2^-20 = 16 ulps of 1).  Every operation
+// is correctly rounded, so the oracle reproduces the decision.  The triangle
+// is read again (from L1: it was just tested) so that its vertices need not
+// stay in registers across the test.
+__device__ __forceinline__ bool near_miss(float ox, float oy, float oz, float dx, float dy, float dz,
+                                          const float4* tri, float u, float v) {
+    const float4 a = ldg4(tri), b = ldg4(tri + 1), c = ldg4(tri + 2);
+    const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
+    const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
+    const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
+    const float qx = fsub(fmul(dy, e1z), fmul(e1y, dz));
+    const float qy = fsub(fmul(dz, e1x), fmul(e1z, dx));
+    const float qz = fsub(fmul(dx, e1y), fmul(e1x, dy));
+    const float den = fadd(fadd(fmul(qx, e0x), fmul(qy, e0y)), fmul(qz, e0z));
+    const float sd = fadd(fadd(fabsf(dx), fabsf(dy)), fabsf(dz));
+    const float s0 = fadd(fadd(fabsf(e0x), fabsf(e0y)), fabsf(e0z));
+    const float s1 = fadd(fadd(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
+    const float ss = fadd(fadd(fabsf(sx), fabsf(sy)), fabsf(sz));
+    const float s01 = fadd(s0, s1);
+    const float k = fmul(fmul(fmul(sd, s01), fadd(ss, s01)), __frcp_rn(fabsf(den)));
+    const float beta = fmul(k, kNearMissScale);
+    return u >= -beta && v >= -beta && fadd(u, v) <= fadd(1.0f, fadd(beta, beta));
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -237,21 +291,25 @@ struct TRay {
 // node.padding0 != 0 marks a node holding a coordinate outside the fast window
 // (set by the upload); such nodes, out-of-window rays and the BOUNDS variant
 // (whose nodes did not go through the upload) divide with div.rn.
+// nearCull: either box was rejected with its entry within kTieWindow of the
+// bound (see kTieWindow); only closest-hit callers read it.
 template <bool BOUNDS>
 __device__ __forceinline__ void test_children(const TRay& r, const float4& n0, const float4& n1, const float4& n2,
                                               const float4& n3, float tmin, float bound, bool& il, bool& ir,
-                                              float& hl, float& hr) {
+                                              float& hl, float& hr, bool& nearCull) {
+    bool nl, nr;
     if (!BOUNDS && r.fast && __float_as_int(n3.z) == 0) {
         il = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y,
-                            tmin, bound, hl);
+                            tmin, bound, hl, nl);
         ir = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w,
-                            tmin, bound, hr);
+                            tmin, bound, hr, nr);
     } else {
         il = box_test<false>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n0.x, n0.y, n0.z, n0.w, n1.x,
-                             n1.y, tmin, bound, hl);
+                             n1.y, tmin, bound, hl, nl);
         ir = box_test<false>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z,
-                             n2.w, tmin, bound, hr);
+                             n2.w, tmin, bound, hr, nr);
     }
+    nearCull = nl || nr;
 }
 
 // vec4(v, w) * inverseMatrix (bvh.hsh:179-180): component i = dot(vec4(v, w),
@@ -307,6 +365,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     const float4* blasNodes = p.nodes;
     const float4* blasTris = p.tris;
     bool occl = false;
+    bool tieSuspect = false;        // closest hit: a near tie the second distance cannot show (kTieWindow)
     bool laneAny = ANY;             // batched: the lane's query kind
     float tmin = p.tmin, tmax = p.tmax;
     uint32_t maxSteps = p.max_steps;
@@ -356,7 +415,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         if (p.per_ray_tmax) tmax = ldg4(raySrc + size_t(ri) * 3 + 2).x;
                         hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
                         hitID = -1; hitInst = -1; curInst = -1;
-                        node = 0; sp = 0; steps = 0; flags = 0; occl = false;
+                        node = 0; sp = 0; steps = 0; flags = 0; occl = false; tieSuspect = false;
                         tlasIndex = kTlasInvalid;
                         if (MODE == MODE_MESH) { blasNodes = p.nodes; blasTris = p.tris; }
                         live = true;
@@ -450,6 +509,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                             } else if (t < second) {
                                 second = t;
                             }
+                        } else if (t > tmin && t < tmax && t <= fmul(hitDist, kTieWiden) &&
+                                   near_miss(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, blasTris + size_t(tp) * 3, u, v)) {
+                            tieSuspect = true;
                         }
                         tp++;
                     } while (!end);
@@ -463,8 +525,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     if (COUNT) nodeCount++;
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
                     float hl, hr;
-                    bool il, ir;
-                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, hl, hr);
+                    bool il, ir, nearCull;
+                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, hl, hr, nearCull);
+                    if (!anyQ) tieSuspect = tieSuspect || nearCull;
                     int32_t next, far;
                     if (anyQ) {
                         next = il ? lptr : rptr;
@@ -473,6 +536,11 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         const bool leftFirst = hl <= hr;
                         next = leftFirst ? lptr : rptr;
                         far = leftFirst ? rptr : lptr;
+                        // bvh.hsh:234-236: with only the right box hit and its
+                        // entry equal to the bound, the missed left box also
+                        // reports the bound, so the shader descends left and
+                        // drops the right subtree, whose triangles may tie
+                        tieSuspect = tieSuspect || (!il && ir && leftFirst);
                     }
                     if (il && ir) {
                         if (sp >= st.capacity) {
@@ -496,7 +564,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 } else {
                     const bool hit = hitID >= 0;
                     uint32_t f = flags | (hit ? kHitFlagHit : 0u);
-                    if (hit && fsub(second, hitDist) <= fmul(1e-6f, hitDist)) f |= kHitFlagNearTie;
+                    if ((hit && fsub(second, hitDist) <= fmul(kTieWindow, hitDist)) || tieSuspect)
+                        f |= kHitFlagNearTie;
                     float4* hp = (BATCH ? static_cast<float4*>(out) : p.hits) + size_t(rid) * 2;
                     hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(hitInst), __uint_as_float(f));
                     hp[1] = make_float4(hu, hv, second, 0.0f);

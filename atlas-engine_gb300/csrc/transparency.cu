@@ -120,7 +120,8 @@ __global__ void transparency_kernel(TransParams p) {
                         const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
                         bool il, ir;
                         float hl, hr;
-                        test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr);
+                        bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
+                        test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr, nearCullUnused);
                         const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
                         if (ANY) {
                             next = il ? l : rr;
@@ -166,7 +167,8 @@ __global__ void transparency_kernel(TransParams p) {
                     const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
                     bool il, ir;
                     float hl, hr;
-                    test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr);
+                    bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
+                    test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr, nearCullUnused);
                     const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
                     if (ANY) {
                         next = il ? l : rr;

@@ -159,7 +159,11 @@ typedef struct ae_hit {
 } ae_hit;
 
 #define AE_HIT_HIT       0x1u
-#define AE_HIT_NEAR_TIE  0x2u  /* a second hit lies within 1e-6 relative t */
+#define AE_HIT_NEAR_TIE  0x2u  /* the nearest triangle may be decided by FP32 rounding: set on
+                                  every ray whose two nearest hits lie within 1e-6 relative t
+                                  (a superset: a second hit within 4e-6, a box or triangle
+                                  rejected within rounding of the window; misses included);
+                                  ae_rt_retest_near_ties decides them in double */
 #define AE_HIT_OVERFLOW  0x4u  /* traversal stack overflowed; result invalid */
 #define AE_HIT_ITER_CAP  0x8u  /* traversal step cap hit; result invalid */
 #define AE_HIT_RETESTED  0x10u /* ae_hit_f64 only: the double-precision re-test decided it */

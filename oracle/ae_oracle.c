@@ -171,15 +171,58 @@ static inline int box_glsl(v3 o, v3 d, float tmin, float tmax, const float* bmin
 
 static inline int isnan3(v3 d) { return isnan(d.x) || isnan(d.y) || isnan(d.z); }
 
+/* Near-tie detection of the GPU closest-hit trace (trace_kernels.cuh,
+ * kTieWindow / near_miss), restated with the same correctly rounded
+ * operations so that both flag the same rays.  It does not change the
+ * traversal's result. */
+#define TIE_WINDOW 4e-6f
+static const float TIE_WIDEN = 1.0f + TIE_WINDOW;
+#define NEAR_MISS_SCALE 9.5367431640625e-07f   /* 2^-20 */
+
+/* The box test of box_glsl, also reporting a rejected box whose entry lies
+ * within TIE_WINDOW of the exit bound. */
+static inline int box_glsl_tie(v3 o, v3 d, float tmin, float tmax, const float* bmin, const float* bmax, float* dist,
+                               int* near_cull) {
+    float t0x = (bmin[0] - o.x) / d.x, t0y = (bmin[1] - o.y) / d.y, t0z = (bmin[2] - o.z) / d.z;
+    float t1x = (bmax[0] - o.x) / d.x, t1y = (bmax[1] - o.y) / d.y, t1z = (bmax[2] - o.z) / d.z;
+    float sx = fminf(t0x, t1x), sy = fminf(t0y, t1y), sz = fminf(t0z, t1z);
+    float bx = fmaxf(t0x, t1x), by = fmaxf(t0y, t1y), bz = fmaxf(t0z, t1z);
+    float tminf = fmaxf(fmaxf(tmin, sx), fmaxf(sy, sz));
+    float tmaxf = fminf(fminf(tmax, bx), fminf(by, bz));
+    int hit = tminf <= tmaxf;
+    *dist = hit ? tminf : tmax;
+    *near_cull = !hit && tminf <= tmaxf * TIE_WIDEN;
+    return hit;
+}
+
+/* A triangle rejected within the rounding error of its barycentric tests:
+ * beta = 2^-20 Sd (S0+S1) (Ss+S0+S1) / |den| with the L1 norms of d, e0, e1
+ * and s = o - v0. */
+static inline int near_miss(v3 o, v3 d, const aeo_tri* t, float u, float v) {
+    v3 v0 = ld3(t->v0), v1 = ld3(t->v1), v2 = ld3(t->v2);
+    v3 e0 = sub(v1, v0), e1 = sub(v2, v0), s = sub(o, v0);
+    v3 q = cross3(d, e1);
+    float den = dot3(q, e0);
+    float sd = (fabsf(d.x) + fabsf(d.y)) + fabsf(d.z);
+    float s0 = (fabsf(e0.x) + fabsf(e0.y)) + fabsf(e0.z);
+    float s1 = (fabsf(e1.x) + fabsf(e1.y)) + fabsf(e1.z);
+    float ss = (fabsf(s.x) + fabsf(s.y)) + fabsf(s.z);
+    float s01 = s0 + s1;
+    float k = ((sd * s01) * (ss + s01)) * (1.0f / fabsf(den));
+    float beta = k * NEAR_MISS_SCALE;
+    return u >= -beta && v >= -beta && u + v <= 1.0f + (beta + beta);
+}
+
 /* HitClosest -- bvh.hsh:191-273 on one BLAS, CheckLeafClosest :44-72.
  * The stack is unbounded here (the shader's holds 32 entries with no check). */
 static void closest_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris,
                              const float* r, int32_t* stack, int32_t* out_ptr, float* out_tuv,
-                             uint32_t* nf, uint32_t* tf) {
+                             uint32_t* nf, uint32_t* tf, uint32_t* out_flags, float* out_second) {
     v3 o = ld3(r), d = ld3(r + 3);
     float tMin = r[6], tMax = r[7];
-    float hitDist = tMax, hu = 0.0f, hv = 0.0f;
+    float hitDist = tMax, hu = 0.0f, hv = 0.0f, second = tMax;
     int32_t hitID = -1;
+    int suspect = 0;
     uint32_t nodeFetches = 0, triFetches = 0;
     if (n_nodes && !isnan3(d)) {
         uint32_t sp = 1;
@@ -196,8 +239,11 @@ static void closest_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_
                     float st, su, sv;
                     int hit = tri_test(o, d, t, &st, &su, &sv);
                     /* tmax of CheckLeafClosest is ray.hitDistance (bvh.hsh:246) */
-                    if (hit && st > tMin && st < hitDist) {
-                        if (st < hitDist) { hitDist = st; hitID = tp; hu = su; hv = sv; }
+                    if (hit && st > tMin && st < tMax) {
+                        if (st < hitDist) { second = hitDist; hitDist = st; hitID = tp; hu = su; hv = sv; }
+                        else if (st < second) second = st;
+                    } else if (st > tMin && st < tMax && st <= hitDist * TIE_WIDEN && near_miss(o, d, t, su, sv)) {
+                        suspect = 1;
                     }
                     tp++;
                 }
@@ -206,8 +252,12 @@ static void closest_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_
                 const aeo_node* nd = &nodes[nodePtr];
                 nodeFetches++;
                 float hl = 0.0f, hr = 0.0f;
-                int il = box_glsl(o, d, tMin, hitDist, nd->lmin, nd->lmax, &hl);
-                int ir = box_glsl(o, d, tMin, hitDist, nd->rmin, nd->rmax, &hr);
+                int nl = 0, nr = 0;
+                int il = box_glsl_tie(o, d, tMin, hitDist, nd->lmin, nd->lmax, &hl, &nl);
+                int ir = box_glsl_tie(o, d, tMin, hitDist, nd->rmin, nd->rmax, &hr, &nr);
+                suspect |= nl | nr;
+                /* bvh.hsh:234-236 drops a hit right child entered exactly at the bound */
+                suspect |= !il && ir && hl <= hr;
                 int none = !il && !ir;
                 int32_t next = (hl <= hr) ? nd->left : nd->right;
                 if (none) next = stack[--sp];
@@ -220,6 +270,12 @@ static void closest_glsl_one(const aeo_node* nodes, uint32_t n_nodes, const aeo_
     out_tuv[0] = hitDist; out_tuv[1] = hu; out_tuv[2] = hv;
     if (nf) *nf = nodeFetches;
     if (tf) *tf = triFetches;
+    if (out_flags) {
+        uint32_t f = hitID >= 0 ? 1u : 0u;
+        if ((hitID >= 0 && second - hitDist <= TIE_WINDOW * hitDist) || suspect) f |= 2u;
+        *out_flags = f;
+    }
+    if (out_second) *out_second = second;
 }
 
 /* HitAny -- bvh.hsh:359-441 on one BLAS, CheckLeaf :74-104. */
@@ -752,6 +808,7 @@ typedef struct {
     const float* rays; uint32_t begin, end;
     int32_t* ptr; float* tuv; uint8_t* occ; uint32_t* nf; uint32_t* tf;
     double* t64; double* t64b;
+    uint32_t* flags; float* second;
 } job_t;
 
 static void* run_job(void* arg) {
@@ -769,7 +826,8 @@ static void* run_job(void* arg) {
             break;
         case K_CLOSEST_GLSL:
             closest_glsl_one(j->nodes, j->n_nodes, j->tris, r, (int32_t*)stack, &j->ptr[i], &j->tuv[(size_t)i * 3],
-                             j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL);
+                             j->nf ? &j->nf[i] : NULL, j->tf ? &j->tf[i] : NULL,
+                             j->flags ? &j->flags[i] : NULL, j->second ? &j->second[i] : NULL);
             break;
         case K_ANY_GLSL:
             j->occ[i] = (uint8_t)any_glsl_one(j->nodes, j->n_nodes, j->tris, r, (int32_t*)stack,
@@ -825,6 +883,15 @@ void aeo_closest_glsl(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tr
     job_t p; memset(&p, 0, sizeof(p));
     p.kind = K_CLOSEST_GLSL; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
     p.rays = rays; p.ptr = tri_ptr; p.tuv = tuv; p.nf = node_fetches; p.tf = tri_fetches;
+    run_batch(p, n_rays, threads);
+}
+
+void aeo_closest_glsl_ties(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                           const float* rays, uint32_t n_rays, int threads,
+                           int32_t* tri_ptr, float* tuv, uint32_t* flags, float* t_second) {
+    job_t p; memset(&p, 0, sizeof(p));
+    p.kind = K_CLOSEST_GLSL; p.nodes = nodes; p.n_nodes = n_nodes; p.tris = tris; p.n_tris = n_tris;
+    p.rays = rays; p.ptr = tri_ptr; p.tuv = tuv; p.flags = flags; p.second = t_second;
     run_batch(p, n_rays, threads);
 }
 

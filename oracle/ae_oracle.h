@@ -60,6 +60,15 @@ void aeo_closest_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tri
                      const float* rays, uint32_t n_rays, int threads,
                      int32_t* tri_ptr, float* tuv);
 
+/* aeo_closest_glsl plus the GPU trace's near-tie flags (bit 0 hit, bit 1
+ * near tie: a second accepted triangle within 4e-6 relative t, a rejected
+ * box entered within that window of the bound, or a triangle rejected
+ * within the rounding error of its barycentric tests) and its second
+ * distance (the second smallest accepted t, tmax if none). */
+void aeo_closest_glsl_ties(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
+                           const float* rays, uint32_t n_rays, int threads,
+                           int32_t* tri_ptr, float* tuv, uint32_t* flags, float* t_second);
+
 /* Host any-hit query (BVH.cpp:176-217); occluded[i] = 0/1. */
 void aeo_any_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
                  const float* rays, uint32_t n_rays, int threads, uint8_t* occluded);

@@ -72,6 +72,8 @@ def port():
         L.aeo_any_cpu.argtypes = [P, U32, P, U32, P, U32, C.c_int, P]
         L.aeo_closest_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P, P]
         L.aeo_any_glsl.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P]
+        L.aeo_closest_glsl_ties.argtypes = [P, U32, P, U32, P, U32, C.c_int, P, P, P, P]
+        L.aeo_closest_glsl_ties.restype = None
         L.aeo_closest_f64_brute.argtypes = [P, U32, P, U32, C.c_int, P, P, P]
         L.aeo_scene_closest_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P, P, P, P, P]
         L.aeo_scene_any_glsl.argtypes = [P, U32, P, U32, P, U32, P, U32, U32, C.c_int, P]
@@ -218,6 +220,21 @@ def closest_glsl(nodes_f32, tris_f32, rays8, threads=os.cpu_count(), counters=Fa
     if counters:
         return ptr, tuv, nf, tf
     return ptr, tuv
+
+
+def closest_glsl_ties(nodes_f32, tris_f32, rays8, threads=os.cpu_count()):
+    """closest_glsl plus the GPU trace's near-tie flags and second distance:
+    (tri_ptr, tuv, flags (bit 0 hit, bit 1 near tie), t_second)."""
+    n = len(rays8)
+    nodes_f32, tris_f32, rays8 = _c(nodes_f32, np.float32), _c(tris_f32, np.float32), _c(rays8, np.float32)
+    ptr = np.empty(n, np.int32)
+    tuv = np.empty((n, 3), np.float32)
+    flags = np.empty(n, np.uint32)
+    second = np.empty(n, np.float32)
+    port().aeo_closest_glsl_ties(nodes_f32.ctypes.data, len(nodes_f32), tris_f32.ctypes.data, len(tris_f32),
+                                 rays8.ctypes.data, n, threads, ptr.ctypes.data, tuv.ctypes.data, flags.ctypes.data,
+                                 second.ctypes.data)
+    return ptr, tuv, flags, second
 
 
 def any_glsl(nodes_f32, tris_f32, rays8, threads=os.cpu_count(), counters=False):

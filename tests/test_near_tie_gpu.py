@@ -54,10 +54,13 @@ def check_against_brute(gt, rays8, h32, h64, cnt, limit=600):
     sel = flagged[:limit]
     ptr, t, t2 = pyoracle.closest_f64_brute(gt, rays8[sel])
     assert np.all(h64["flags"][sel] & HIT_FLAG_RETESTED)
-    assert np.all(h64["flags"][sel] & HIT_FLAG_HIT)
+    # a flagged ray may have no double-precision hit (a triangle rejected
+    # within its rounding error flags the ray too)
+    np.testing.assert_array_equal((h64["flags"][sel] & HIT_FLAG_HIT) != 0, ptr >= 0)
     np.testing.assert_array_equal(h64["triPtr"][sel], ptr)
-    np.testing.assert_array_equal(h64["t"][sel], t)
-    np.testing.assert_array_equal(h64["t_second"][sel], t2)
+    hit = ptr >= 0
+    np.testing.assert_array_equal(h64["t"][sel][hit], t[hit])
+    np.testing.assert_array_equal(h64["t_second"][sel][hit], t2[hit])
     return len(flagged)
 
 
@@ -94,3 +97,41 @@ def test_retest_terrain_grid_edges_and_vertices(ctx):
     assert (h32["triPtr"] >= 0).mean() > 0.9
     flagged = check_against_brute(gt, rays8, h32, h64, cnt)
     assert flagged > 100, flagged
+
+
+def test_flag_complete_and_equal_to_oracle(ctx):
+    """100,000 rays aimed at terrain grid edges and vertices, box edges and
+    the lines where box walls meet the terrain: the GPU's near-tie flags are
+    the oracle's bit for bit, every ray whose FP64 brute-force gap is
+    <= 1e-6 is flagged, and the re-test gives the brute force's answer on
+    every flagged ray."""
+    import near_tie_util as U
+    import torch
+    tris, obj = U.near_tie_scene()
+    r8, lab = U.near_tie_rays(tris, obj)
+    nodes, order, eon = pyoracle.build_bvh(tris)
+    b = BVH(tris)
+    gt = b.pack_triangles()
+    assert np.array_equal(b.nodes_f32.view(np.uint32), nodes.view(np.uint32))
+    mid = ctx.upload_mesh(b.nodes, gt)
+    rays = torch.from_numpy(scenes.pack_rays(r8[:, 0:3], r8[:, 3:6])).cuda()
+    n = len(r8)
+    hits = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+    ctx.trace_closest(mid, rays, 1e-4, 1e4, out=hits, n_rays=n)
+    out = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+    cnt = ctx.retest_near_ties(mid, rays, hits, 1e-4, 1e4, out, n_rays=n)
+    h32 = hits.cpu().numpy().view(atlas_rt.HIT_DTYPE).reshape(-1)
+    h64 = out.cpu().numpy().view(HIT64_DTYPE).reshape(-1)
+    p, tuv, flags, second = pyoracle.closest_glsl_ties(nodes, gt, r8)
+    assert np.array_equal(h32["triPtr"], p)
+    assert np.array_equal(h32["flags"] & (HIT_FLAG_HIT | HIT_FLAG_NEAR_TIE), flags)
+    assert np.array_equal(h32["tSecond"].view(np.uint32), second.view(np.uint32))
+    ptr, t1, t2, gap = U.brute_gaps(gt, r8)
+    flagged = (h32["flags"] & HIT_FLAG_NEAR_TIE) != 0
+    assert (gap <= 1e-6).sum() > 20000
+    assert not np.any((gap <= 1e-6) & ~flagged)
+    assert cnt == flagged.sum()
+    f = np.nonzero(flagged)[0]
+    np.testing.assert_array_equal(h64["triPtr"][f], ptr[f])
+    hit = ptr[f] >= 0
+    np.testing.assert_array_equal(h64["t"][f][hit], t1[f][hit])
