@@ -348,10 +348,14 @@ def timed_steps(torch, dev, stream, step, steps, flush):
     return [a.elapsed_time(b) for a, b in evs]
 
 
-# DRAM bytes (read + write) per launch from ncu captures (bench.py --profile ...):
-# filled per ray class; None where no capture exists yet
-TRAFFIC_BYTES = {"primary": TRAFFIC_PRIMARY_BYTES, "bounce": None, "shadow": None,
-                 "random65536_closest": None, "random65536_any": None, "batched64": None}
+# DRAM bytes (read + write) per launch from one ncu capture per ray class
+# (bench.py --profile cast / random65536 / batched64; profiles/trace_kernel_ray_classes.md)
+TRAFFIC_BYTES = {"primary": TRAFFIC_PRIMARY_BYTES,
+                 "bounce": 92_541_184 + 10_687_232,
+                 "shadow": 53_865_216 + 99_072,
+                 "random65536_closest": 57_691_648 + 4_169_472,
+                 "random65536_any": 57_688_576 + 143_104,
+                 "batched64": 1_200_891_136 + 263_677_952}
 
 
 def class_roofline(alg_bytes, ms, hbm_peak, l2_gbs, traffic=None):
