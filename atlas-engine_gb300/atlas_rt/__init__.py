@@ -202,7 +202,7 @@ class Context:
 
     def __init__(self, device: int = 0, count_fetches: bool = False, blocks_per_sm: int = 0,
                  max_steps: int = 0, refill_steps: int = 0, threads_per_block: int = 0,
-                 stack_entries_smem: int = 0, refill_below: int = 0):
+                 stack_entries_smem: int = 0, refill_below: int = 0, leaf_wait: int = 0):
         cfg = Config()
         cfg.device = device
         cfg.blocks_per_sm = blocks_per_sm
@@ -212,6 +212,7 @@ class Context:
         cfg.flags = CFG_COUNT_FETCHES if count_fetches else 0
         cfg.refill_steps = refill_steps
         cfg.refill_below = refill_below
+        cfg.leaf_wait = leaf_wait
         h = C.c_void_p()
         _check(lib().ae_rt_ctx_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -31,7 +31,7 @@ class AeRtError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("device", I32), ("blocks_per_sm", U32), ("threads_per_block", U32),
                 ("max_steps", U32), ("flags", U32), ("refill_steps", U32), ("stack_entries_smem", U32),
-                ("refill_below", U32)]
+                ("refill_below", U32), ("leaf_wait", U32)]
 
 
 class BatchDesc(C.Structure):

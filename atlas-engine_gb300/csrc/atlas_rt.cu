@@ -166,6 +166,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
+    p.leaf_wait = ctx->leaf_wait;
     void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
@@ -336,6 +337,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     ctx->refill_steps = c.refill_steps;
     ctx->refill_below = c.refill_below == 0 ? atlas::rt::dev::kDefaultRefillBelow
                                             : (c.refill_below > 32 ? 0u : c.refill_below);
+    ctx->leaf_wait = c.leaf_wait > 32 ? 32u : c.leaf_wait;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 8 * sizeof(uint32_t));
@@ -650,6 +652,7 @@ TraceParams BatchParams(ae_rt_ctx* ctx, const atlas::rt::dev::BatchDesc* d_batch
     p.n_batches = n;
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
+    p.leaf_wait = ctx->leaf_wait;
     p.max_steps = 0xffffffffu;
     return p;
 }

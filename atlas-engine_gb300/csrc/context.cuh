@@ -55,6 +55,7 @@ struct ae_rt_ctx {
     uint32_t max_steps_cfg = 0;
     uint32_t refill_steps = 0;
     uint32_t refill_below = 0;
+    uint32_t leaf_wait = 0;
     bool count_fetches = false;
     std::vector<atlas::rt::host::DeviceMesh> meshes;
     // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot

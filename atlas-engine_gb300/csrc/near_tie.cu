@@ -10,9 +10,11 @@
 // the double form of the shader's triangle test (intersections.hsh:36-57),
 // accepting tmin < t < tmax.  Exactly equal double distances resolve to the
 // lower BVH-order triangle index, and t_second is the second smallest
-// accepted distance over the BVH-order triangle entries (two entries at the
-// same distance make t_second equal to t); the oracle's brute-force pass over
-// every entry gives the same pair.
+// accepted distance over distinct triangles (two triangles at the same
+// distance make t_second equal to t).  An entry with the winner's vertices
+// is the winner itself (the root's spatial split stores a straddling
+// triangle twice), so the reported entry is one of its copies; the oracle's
+// brute-force pass over every entry gives the same triangle and pair.
 #include "atlas_rt.h"
 #include "context.cuh"
 #include "trace_kernels.cuh"
@@ -89,6 +91,15 @@ __device__ __forceinline__ bool tri64(const double o[3], const double d[3], cons
     return t >= 0.0 && u >= 0.0 && v >= 0.0 && da(u, v) <= 1.0;
 }
 
+// Two BVH entries with the same vertices are one triangle: the root spatial
+// split stores a straddling triangle in both children, each copy under a box
+// clipped to its side, so a traversal may find either copy but not both.
+__device__ __forceinline__ bool same_triangle(const float4* q, const float4& A, const float4& B, const float4& C) {
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    return a.x == A.x && a.y == A.y && a.z == A.z && b.x == B.x && b.y == B.y && b.z == B.z && c.x == C.x &&
+           c.y == C.y && c.z == C.z;
+}
+
 __global__ void retest_kernel(RetestParams p) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
@@ -123,7 +134,8 @@ __global__ void retest_kernel(RetestParams p) {
                                  C = __ldg(p.tris + size_t(tp) * 3 + 2);
                     end = A.w > 0.0f;
                     double t;
-                    if (tri64(o, d, A, B, C, t) && t > p.tmin && t < p.tmax) {
+                    if (tri64(o, d, A, B, C, t) && t > p.tmin && t < p.tmax &&
+                        !(bi >= 0 && t == best && same_triangle(p.tris + size_t(bi) * 3, A, B, C))) {
                         if (t < best || (t == best && tp < bi)) {
                             if (tp != bi) second = best;
                             best = t;

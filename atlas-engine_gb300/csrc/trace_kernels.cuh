@@ -77,6 +77,7 @@ struct TraceParams {
     uint32_t refill_steps;       // traversal steps between warp refills
     uint32_t refill_below;       // refill early when fewer lanes than this still traverse (0: never)
     uint32_t per_ray_tmax;       // nonzero: a ray's tmax is its PackedRay hit.x (shadow queues)
+    uint32_t leaf_wait;          // closest hit: a lane at a leaf waits for this many leaf lanes (0: never)
 };
 
 // One ray batch of a batched launch: its mesh, its rays and results, its
@@ -115,6 +116,21 @@ constexpr int MODE_SCENE = 1;    // TLAS over instances
 constexpr int MODE_BATCH = 2;    // many BLASes, one per batch
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// A 64-byte node as two 32-byte read-only loads, one L1 sector each: every lane
+// gathers its own node, so four 16-byte loads would look each sector up twice
+// (the L1 pipeline is the limiter of incoherent rays).  Needs the node at a
+// 32-byte boundary: node arrays are cudaMalloc'ed by the library (256-byte
+// aligned) and 64-byte strided.  Caller-owned arrays (the bounds-checked
+// instance) use ldg4.
+__device__ __forceinline__ void ldg_node(const float4* p, float4& n0, float4& n1, float4& n2, float4& n3) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(n0.x), "=f"(n0.y), "=f"(n0.z), "=f"(n0.w), "=f"(n1.x), "=f"(n1.y), "=f"(n1.z), "=f"(n1.w)
+        : "l"(p));
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8+32];"
+        : "=f"(n2.x), "=f"(n2.y), "=f"(n2.z), "=f"(n2.w), "=f"(n3.x), "=f"(n3.y), "=f"(n3.z), "=f"(n3.w)
+        : "l"(p));
+}
 
 // IEEE single operations with explicit rounding (no contraction into FMA).
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
@@ -375,6 +391,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     const uint32_t nTop = TLAS ? p.n_tlas : p.n_nodes;
     const int refill = p.refill_steps ? int(p.refill_steps) : 32;
     const uint32_t refillBelow = p.refill_below;
+    const uint32_t leafWait = ANY ? 0u : p.leaf_wait;
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
@@ -435,6 +452,16 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 // dynamic fetch: leave the burst for a refill once too few lanes
                 // are still traversing (while the queue still has rays)
                 if (refillBelow && !queueDry && uint32_t(__popc(__activemask())) < refillBelow) break;
+                // postponed leaves: a lane at a leaf skips this step while fewer
+                // than leafWait lanes are at leaves and others still descend, so
+                // that the warp's triangle tests run together instead of beside
+                // every node step (the order of each lane's own steps is kept)
+                if (leafWait) {
+                    const bool atLeaf = node < 0 && !(TLAS && sp < tlasIndex);
+                    const uint32_t act = __activemask();
+                    const uint32_t leaves = __ballot_sync(act, atLeaf);
+                    if (atLeaf && uint32_t(__popc(leaves)) < leafWait && leaves != act) continue;
+                }
                 if (++steps > maxSteps) {
                     flags |= kHitFlagIterCap;
                     atomicOr(p.error_word, kErrIterationCap);
@@ -521,7 +548,12 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     node = st.get(--sp);
                 } else {
                     const float4* np = nodesArr + size_t(node) * 4;
-                    const float4 n0 = ldg4(np), n1 = ldg4(np + 1), n2 = ldg4(np + 2), n3 = ldg4(np + 3);
+                    float4 n0, n1, n2, n3;
+                    if (BOUNDS) {
+                        n0 = ldg4(np); n1 = ldg4(np + 1); n2 = ldg4(np + 2); n3 = ldg4(np + 3);
+                    } else {
+                        ldg_node(np, n0, n1, n2, n3);
+                    }
                     if (COUNT) nodeCount++;
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
                     float hl, hr;

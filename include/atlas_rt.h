@@ -361,6 +361,10 @@ typedef struct ae_rt_config {
     uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
     uint32_t refill_below;        /* also refill as soon as fewer than this many lanes of a warp
                                      are still traversing (1..32; 0 = the default; > 32 = never) */
+    uint32_t leaf_wait;           /* closest-hit traces: a lane that reaches a leaf waits until this
+                                     many lanes of its warp are at leaves (or no lane is at an inner
+                                     node), so that leaf tests run together (0 = never wait;
+                                     scheduling only, results are unchanged) */
 } ae_rt_config;
 
 ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out);
@@ -1023,7 +1027,9 @@ ae_rt_status ae_rt_mesh_get_bvh(ae_rt_ctx* ctx, int32_t mesh, ae_bvh_node* nodes
  * AE_HIT_NEAR_TIE, the nearest triangle is searched again in double precision:
  * a closest-hit traversal of the same BVH with conservative double slab
  * tests and the double form of the shader's triangle test (tmin < t < tmax);
- * equal double distances resolve to the lower BVH-order index, t_second is
+ * equal double distances resolve to the lower BVH-order index (entries with
+ * the same vertices, the copies a spatial split makes, count as one triangle:
+ * triPtr is one of them), t_second is
  * the second smallest accepted distance.  Other rays are passed through (t,
  * triPtr, tSecond, AE_HIT_HIT).  Device buffers; n_retested (optional, host)
  * receives the number of flagged rays and synchronises.  The engine has no

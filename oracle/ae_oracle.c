@@ -770,6 +770,14 @@ void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, cons
 /* ---------------------------------------------------------------------- */
 /* Double-precision brute force                                            */
 /* ---------------------------------------------------------------------- */
+/* The vertex positions of two BVH entries are equal (the w fields hold the
+ * leaf flag, material and opacity, which may differ between the copies). */
+static int same_vertices(const aeo_tri* a, const aeo_tri* b) {
+    for (int k = 0; k < 3; k++)
+        if (a->v0[k] != b->v0[k] || a->v1[k] != b->v1[k] || a->v2[k] != b->v2[k]) return 0;
+    return 1;
+}
+
 static void closest_f64_one(const aeo_tri* tris, uint32_t n_tris, const float* r,
                             int32_t* out_ptr, double* out_t, double* out_t2) {
     double o[3] = { r[0], r[1], r[2] }, d[3] = { r[3], r[4], r[5] };
@@ -789,6 +797,9 @@ static void closest_f64_one(const aeo_tri* tris, uint32_t n_tris, const float* r
         double y = (q[0] * s[0] + q[1] * s[1] + q[2] * s[2]) / den;
         double z = (p[0] * d[0] + p[1] * d[1] + p[2] * d[2]) / den;
         if (x >= 0.0 && y >= 0.0 && z >= 0.0 && y + z <= 1.0 && x > tMin && x < tMax) {
+            /* an entry with the winner's vertices is the same triangle (a
+             * spatial split stores it in two leaves): not a second hit */
+            if (bi >= 0 && x == best && same_vertices(t, &tris[bi])) continue;
             if (x < best) { second = best; best = x; bi = (int32_t)i; }
             else if (x < second) second = x;
         }
