@@ -40,32 +40,36 @@ using atlas::rt::dev::MODE_BATCH;
 using atlas::rt::dev::MODE_MESH;
 using atlas::rt::dev::MODE_SCENE;
 
-template <bool ANY, bool COUNT, int MODE, int W, int S>
+template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true>
 void* KernelFor() {
     // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
     // more per-lane state and get ~73
     constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks>);
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks, false, TIES && !ANY>);
 }
 
+// ties = false: the caller discards the near-tie flag (the library's path
+// tracer, passes and radiance cache), so the scene kernels skip its detection.
 template <int W, int S>
-void* PickShape(bool any, bool count, int mode) {
+void* PickShape(bool any, bool count, int mode, bool ties) {
     if (mode == MODE_BATCH) return count ? KernelFor<false, true, MODE_BATCH, W, S>() : KernelFor<false, false, MODE_BATCH, W, S>();
     if (mode == MODE_SCENE) {
         if (any) return count ? KernelFor<true, true, MODE_SCENE, W, S>() : KernelFor<true, false, MODE_SCENE, W, S>();
+        if (!ties)
+            return count ? KernelFor<false, true, MODE_SCENE, W, S, false>() : KernelFor<false, false, MODE_SCENE, W, S, false>();
         return count ? KernelFor<false, true, MODE_SCENE, W, S>() : KernelFor<false, false, MODE_SCENE, W, S>();
     }
     if (any) return count ? KernelFor<true, true, MODE_MESH, W, S>() : KernelFor<true, false, MODE_MESH, W, S>();
     return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
 }
 
-void* PickKernelShape(int shape, bool any, bool count, int mode) {
+void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true) {
     switch (shape) {
-    case 1: return PickShape<2, 32>(any, count, mode);
-    case 2: return PickShape<8, 16>(any, count, mode);
-    case 3: return PickShape<4, 16>(any, count, mode);
-    default: return PickShape<4, 32>(any, count, mode);
+    case 1: return PickShape<2, 32>(any, count, mode, ties);
+    case 2: return PickShape<8, 16>(any, count, mode, ties);
+    case 3: return PickShape<4, 16>(any, count, mode, ties);
+    default: return PickShape<4, 32>(any, count, mode, ties);
     }
 }
 
@@ -160,14 +164,14 @@ uint32_t* WorkCounter(ae_rt_ctx* ctx) {
     return ctx->d_counter + (k == 0 ? 0u : k + 1u);          // word 1 is the error word
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s) {
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true) {
     if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
     AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
-    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode);
+    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -178,7 +182,7 @@ constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
 
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                    float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
-                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false) {
+                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true) {
     if (!ctx) return AE_RT_INVALID_ARG;
     const bool scene = mesh_id == kSceneTarget;
     if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
@@ -235,7 +239,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.cull_mask = cull_mask;
     }
     p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
-    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s);
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -269,7 +273,8 @@ ae_rt_status atlas::rt::host::EnsureBounceQueues(ae_rt_ctx* ctx, uint32_t capaci
 ae_rt_status atlas::rt::host::TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity,
                                              float tmin, float tmax, void* out, void* stream,
                                              const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax) {
-    return Trace(ctx, any, kSceneTarget, rays, capacity, tmin, tmax, out, stream, count_dev, cull_mask, per_ray_tmax);
+    return Trace(ctx, any, kSceneTarget, rays, capacity, tmin, tmax, out, stream, count_dev, cull_mask, per_ray_tmax,
+                 false);
 }
 
 namespace {
@@ -1064,7 +1069,7 @@ ae_rt_status PathTrace(ae_rt_ctx* ctx, const ae_camera* cam, const ae_pt_params*
                 ? TraceTransparency(ctx, false, rays_in, n, 0.0f, kInf, AE_RT_MASK_ALL, ctx->pt_hits.ptr, stream,
                                     ctx->d_pt_counts + in)
                 : Trace(ctx, false, kSceneTarget, rays_in, n, 0.0f, kInf, ctx->pt_hits.ptr, stream,
-                        ctx->d_pt_counts + in, AE_RT_MASK_ALL);
+                        ctx->d_pt_counts + in, AE_RT_MASK_ALL, false, false);
             if (st != AE_RT_OK) return st;
             // this shadow queue's previous resolve must be done before it is refilled
             if (pending[q]) AE_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));

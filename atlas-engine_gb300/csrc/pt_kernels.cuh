@@ -583,38 +583,65 @@ __device__ __forceinline__ bool direct_light(const PtScene& sc, Surf& sf, V3 thr
     return true;
 }
 
-// EvaluateIndirectLight (rayHit.csh:237-325): lobe choice, BRDF sample,
-// throughput update, Russian roulette, termination below the surface.
-// Returns true when the path continues with (o, d) and throughput thr.
+// Chance that EvaluateIndirectLight passes straight through a partially
+// opaque surface (rayHit.csh:252-253): clamp(1 - opacity, 0.1, 0.9), 0 for
+// an opaque one.
+__device__ __forceinline__ float refract_chance(float opacity) {
+    return opacity == 1.0f ? 0.0f : fminf(fmaxf(1.0f - opacity, 0.1f), 0.9f);
+}
+
+// EvaluateIndirectLight (rayHit.csh:237-325): the pass-through of a partially
+// opaque surface or a reflection lobe, BRDF sample, throughput update,
+// Russian roulette, termination below the surface.  Returns true when the
+// path continues with (o, d) and throughput thr; *passed tells a
+// pass-through (which keeps the ray's direction).
 __device__ __forceinline__ bool continue_path(Surf& sf, V3& thr, uint32_t pix, uint32_t sample, uint32_t bounce,
-                                              uint32_t seed, float eps, V3& o, V3& d, bool* spec_lobe = nullptr) {
+                                              uint32_t seed, float eps, V3& o, V3& d, bool* spec_lobe = nullptr,
+                                              bool* passed = nullptr) {
     const Mat& mat = sf.mat;
-    const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
-    const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
-    const float rnd = rng(pix, sample, bounce, 4, seed);
-    const float u0 = rng(pix, sample, bounce, 5, seed);
-    const float u1 = rng(pix, sample, bounce, 6, seed);
+    const float refractChance = refract_chance(mat.opacity);
     V3 refl;
     float pdf;
-    if (spec_lobe) *spec_lobe = rnd < specChance;
-    if (rnd < specChance) {
-        pdf = sample_specular(sf, u0, u1, refl);
-        refl = refl * mat.opacity;
-        pdf *= specChance;
+    bool through = false;
+    if (spec_lobe) *spec_lobe = false;
+    if (rng(pix, sample, bounce, 3, seed) >= refractChance) {
+        const V3 F = fresnel(sf.F0, sf.F90, sf.NdotV);
+        const float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+        const float rnd = rng(pix, sample, bounce, 4, seed);
+        const float u0 = rng(pix, sample, bounce, 5, seed);
+        const float u1 = rng(pix, sample, bounce, 6, seed);
+        if (spec_lobe) *spec_lobe = rnd < specChance;
+        if (rnd < specChance) {
+            pdf = sample_specular(sf, u0, u1, refl);
+            refl = refl * mat.opacity;
+            pdf *= specChance;
+        } else {
+            pdf = sample_diffuse(sf, u0, u1, refl);
+            refl = refl * ((1.0f - mat.metalness) * mat.opacity);
+            pdf *= (1.0f - specChance);
+        }
+        pdf *= (1.0f - refractChance);
+        o = sf.P + sf.V * eps;
     } else {
-        pdf = sample_diffuse(sf, u0, u1, refl);
-        refl = refl * ((1.0f - mat.metalness) * mat.opacity);
-        pdf *= (1.0f - specChance);
+        // straight through with reflectance 1 - opacity at full throughput
+        // (NdotL = 1), the origin pushed behind the surface (rayHit.csh:282-291)
+        sf.L = sf.V * -1.0f;
+        pdf = refractChance;
+        refl = v3(1.0f - mat.opacity, 1.0f - mat.opacity, 1.0f - mat.opacity);
+        sf.NdotL = 1.0f;
+        o = sf.P - sf.N * eps;
+        through = true;
     }
-    o = sf.P + sf.V * eps;
+    if (passed) *passed = through;
     if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = thr * refl * (sf.NdotL / pdf);
     else thr = v3(0, 0, 0);
     d = normalize(sf.L);
     thr = thr * mat.ao;
     float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
     prob = bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
+    // a pass-through is exempt from the below-surface termination (rayHit.csh:318)
     const bool alive = thr.x + thr.y + thr.z > 0.0f && rng(pix, sample, bounce, 7, seed) <= prob &&
-                       dot(d, sf.geoN) > 0.0f;
+                       (through || dot(d, sf.geoN) > 0.0f);
     if (alive) thr = thr * (1.0f / prob);
     return alive;
 }
@@ -646,7 +673,7 @@ __device__ __forceinline__ float bsdf_pdf(Surf s, V3 L) {
     const float nv = fmaxf(s.NdotV, 1e-4f);
     const float ps = vis_separable(nv, a) * ggx_d_true(s.NdotH, a) / (4.0f * nv);
     const float pd = s.NdotL * kInvPi * (1.0f - s.mat.metalness);
-    return specChance * ps + (1.0f - specChance) * pd;
+    return (1.0f - refract_chance(s.mat.opacity)) * (specChance * ps + (1.0f - specChance) * pd);
 }
 
 // Density (per solid angle) with which direct_light at P samples the first
@@ -791,11 +818,14 @@ static __global__ void pt_shade_kernel(PtParams p) {
             }
             if (cont) {
                 V3 o, d;
-                bool spec = false;
-                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec)) {
+                bool spec = false, passed = false;
+                if (continue_path(sf, thr, pix, p.sample, p.bounce, p.seed, p.epsilon, o, d, &spec, &passed)) {
                     emitRay = true;
                     outRay0 = make_float4(o.x, o.y, o.z, __uint_as_float(pix));
-                    outRay1 = make_float4(d.x, d.y, d.z, p.mis ? mis_hit_factor(p.sc, sf, d, spec) : 0.0f);
+                    // a light seen through a pass-through is not part of the
+                    // engine's direct light (its NEE evaluates reflection only)
+                    outRay1 = make_float4(d.x, d.y, d.z,
+                                          p.mis && !passed ? mis_hit_factor(p.sc, sf, d, spec) : 0.0f);
                     outPay = make_float4(thr.x, thr.y, thr.z, __uint_as_float(pix));
                 }
             }

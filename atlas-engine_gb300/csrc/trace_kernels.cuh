@@ -176,9 +176,9 @@ __device__ __forceinline__ bool in_fast_range(float v, bool zero_ok) {
 //    kTieWindow of the bound it was tested against (its triangles could tie
 //    with the final hit, which is at most that bound);
 //  * a triangle rejected by the FP32 test lies within the rounding error of
-//    its barycentric tests (near_miss) at a distance up to kTieWindow past
-//    the current nearest hit -- a shared edge, where either side's FP32 test
-//    may fail;
+//    its barycentric tests (tri_test's nearMiss) at a distance up to
+//    kTieWindow past the current nearest hit -- a shared edge, where either
+//    side's FP32 test may fail;
 //  * the shader's descent dropped a hit right child whose entry equals the
 //    bound (bvh.hsh:234-236: a missed left child reports the bound too, and
 //    hitL <= hitR then picks it).
@@ -219,13 +219,30 @@ __device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx,
 }
 
 // IntersectTriangle -- intersections.hsh:36-57.  Returns the shader's accept
-// test; (t, u, v) = sol.
+// test; (t, u, v) = sol.  NEAR: *nearMiss tells whether (u, v) lie within the
+// rounding error of the barycentric bounds.  With the L1 norms Sd, S0, S1, Ss
+// of d, e0, e1 and s = o - v0, every operation of the formula contributes at
+// most a few ulps of products bounded by Sd (S0+S1) (Ss+S0+S1), so
+// |error(u)|, |error(v)| < beta = m / |den| with
+// m = 2^-20 Sd (S0+S1) (Ss+S0+S1) (2^-20 = 16 ulps of 1).  The tests are
+// taken multiplied by |den| (u |den| + m >= 0, ...), one correctly rounded
+// FMA each, so the oracle reproduces them.
+template <bool NEAR = false>
 __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
                                          const float4& a, const float4& b, const float4& c,
-                                         float& t, float& u, float& v) {
+                                         float& t, float& u, float& v, bool* nearMiss = nullptr) {
     const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
     const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
     const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
+    // the slack's scale, folded at once so that one value stays live
+    float m = 0.0f;
+    if (NEAR) {
+        const float s01 = fadd(fadd(fadd(fabsf(e0x), fabsf(e0y)), fabsf(e0z)),
+                               fadd(fadd(fabsf(e1x), fabsf(e1y)), fabsf(e1z)));
+        const float ss = fadd(fadd(fabsf(sx), fabsf(sy)), fabsf(sz));
+        const float sd = fadd(fadd(fabsf(dx), fabsf(dy)), fabsf(dz));
+        m = fmul(fmul(fmul(sd, s01), fadd(ss, s01)), kNearMissScale);
+    }
     // p = cross(s, e0), q = cross(d, e1)
     const float px = fsub(fmul(sy, e0z), fmul(e0y, sz));
     const float py = fsub(fmul(sz, e0x), fmul(e0z, sx));
@@ -237,36 +254,12 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
     t = fdiv(fadd(fadd(fmul(px, e1x), fmul(py, e1y)), fmul(pz, e1z)), den);
     u = fdiv(fadd(fadd(fmul(qx, sx), fmul(qy, sy)), fmul(qz, sz)), den);
     v = fdiv(fadd(fadd(fmul(px, dx), fmul(py, dy)), fmul(pz, dz)), den);
+    if (NEAR) {
+        const float ad = fabsf(den);
+        *nearMiss = __fmaf_rn(u, ad, m) >= 0.0f && __fmaf_rn(v, ad, m) >= 0.0f &&
+                    __fmaf_rn(fsub(1.0f, fadd(u, v)), ad, fadd(m, m)) >= 0.0f;
+    }
     return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
-}
-
-// A triangle whose FP32 test failed within the rounding error of its
-// barycentric coordinates (u, v as tri_test computed them).  With the L1
-// norms Sd, S0, S1, Ss of d, e0, e1 and s = o - v0, every operation of the
-// formula contributes at most a few ulps of products bounded by Sd (S0+S1)
-// (Ss+S0+S1), so |error(u)|, |error(v)| < beta = 2^-20 K with
-// K = Sd (S0+S1) (Ss+S0+S1) / |den| (2^-20 = 16 ulps of 1).  Every operation
-// is correctly rounded, so the oracle reproduces the decision.  The triangle
-// is read again (from L1: it was just tested) so that its vertices need not
-// stay in registers across the test.
-__device__ __forceinline__ bool near_miss(float ox, float oy, float oz, float dx, float dy, float dz,
-                                          const float4* tri, float u, float v) {
-    const float4 a = ldg4(tri), b = ldg4(tri + 1), c = ldg4(tri + 2);
-    const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
-    const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
-    const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
-    const float qx = fsub(fmul(dy, e1z), fmul(e1y, dz));
-    const float qy = fsub(fmul(dz, e1x), fmul(e1z, dx));
-    const float qz = fsub(fmul(dx, e1y), fmul(e1x, dy));
-    const float den = fadd(fadd(fmul(qx, e0x), fmul(qy, e0y)), fmul(qz, e0z));
-    const float sd = fadd(fadd(fabsf(dx), fabsf(dy)), fabsf(dz));
-    const float s0 = fadd(fadd(fabsf(e0x), fabsf(e0y)), fabsf(e0z));
-    const float s1 = fadd(fadd(fabsf(e1x), fabsf(e1y)), fabsf(e1z));
-    const float ss = fadd(fadd(fabsf(sx), fabsf(sy)), fabsf(sz));
-    const float s01 = fadd(s0, s1);
-    const float k = fmul(fmul(fmul(sd, s01), fadd(ss, s01)), __frcp_rn(fabsf(den)));
-    const float beta = fmul(k, kNearMissScale);
-    return u >= -beta && v >= -beta && fadd(u, v) <= fadd(1.0f, fadd(beta, beta));
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -356,8 +349,11 @@ __device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, u
 // BOUNDS = true adds range checks of every node and triangle index against
 // n_nodes / n_tris (for callers whose BVH did not pass the host validator);
 // an out-of-range index ends the ray with the overflow flag set.
+// TIES: closest-hit rays get the complete near-tie flag (kTieWindow); the
+// library's own consumers that discard the flag (path tracer, passes,
+// radiance cache) launch TIES = false.
 template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
-          bool BOUNDS = false>
+          bool BOUNDS = false, bool TIES = true>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     constexpr bool TLAS = MODE == MODE_SCENE;
     constexpr bool BATCH = MODE == MODE_BATCH;
@@ -526,7 +522,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         end = a.w > 0.0f;
                         if (COUNT) triCount++;
                         float t, u, v;
-                        const bool hit = tri_test(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
+                        bool nearMiss = false;
+                        const bool hit = tri_test<TIES && !ANY>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v,
+                                                                &nearMiss);
                         if (anyQ) {
                             if (hit && t > tmin && t < tmax) { occl = true; end = true; }
                         } else if (hit && t > tmin && t < tmax) {
@@ -536,8 +534,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                             } else if (t < second) {
                                 second = t;
                             }
-                        } else if (t > tmin && t < tmax && t <= fmul(hitDist, kTieWiden) &&
-                                   near_miss(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, blasTris + size_t(tp) * 3, u, v)) {
+                        } else if (TIES && nearMiss && t > tmin && t < tmax && t <= fmul(hitDist, kTieWiden)) {
                             tieSuspect = true;
                         }
                         tp++;
@@ -559,7 +556,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     float hl, hr;
                     bool il, ir, nearCull;
                     test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, hl, hr, nearCull);
-                    if (!anyQ) tieSuspect = tieSuspect || nearCull;
+                    if (TIES && !anyQ) tieSuspect = tieSuspect || nearCull;
                     int32_t next, far;
                     if (anyQ) {
                         next = il ? lptr : rptr;
@@ -572,7 +569,7 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         // entry equal to the bound, the missed left box also
                         // reports the bound, so the shader descends left and
                         // drops the right subtree, whose triangles may tie
-                        tieSuspect = tieSuspect || (!il && ir && leftFirst);
+                        if (TIES) tieSuspect = tieSuspect || (!il && ir && leftFirst);
                     }
                     if (il && ir) {
                         if (sp >= st.capacity) {
@@ -596,7 +593,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 } else {
                     const bool hit = hitID >= 0;
                     uint32_t f = flags | (hit ? kHitFlagHit : 0u);
-                    if ((hit && fsub(second, hitDist) <= fmul(kTieWindow, hitDist)) || tieSuspect)
+                    if (TIES ? (hit && fsub(second, hitDist) <= fmul(kTieWindow, hitDist)) || tieSuspect
+                             : hit && fsub(second, hitDist) <= fmul(1e-6f, hitDist))
                         f |= kHitFlagNearTie;
                     float4* hp = (BATCH ? static_cast<float4*>(out) : p.hits) + size_t(rid) * 2;
                     hp[0] = make_float4(hitDist, __int_as_float(hitID), __int_as_float(hitInst), __uint_as_float(f));

@@ -196,21 +196,20 @@ static inline int box_glsl_tie(v3 o, v3 d, float tmin, float tmax, const float* 
 }
 
 /* A triangle rejected within the rounding error of its barycentric tests:
- * beta = 2^-20 Sd (S0+S1) (Ss+S0+S1) / |den| with the L1 norms of d, e0, e1
- * and s = o - v0. */
+ * |error(u)|, |error(v)| < m / |den| with m = 2^-20 Sd (S0+S1) (Ss+S0+S1)
+ * (the L1 norms of d, e0, e1 and s = o - v0); the tests are taken multiplied
+ * by |den|, one correctly rounded fmaf each, as tri_test<NEAR> does. */
 static inline int near_miss(v3 o, v3 d, const aeo_tri* t, float u, float v) {
     v3 v0 = ld3(t->v0), v1 = ld3(t->v1), v2 = ld3(t->v2);
     v3 e0 = sub(v1, v0), e1 = sub(v2, v0), s = sub(o, v0);
     v3 q = cross3(d, e1);
     float den = dot3(q, e0);
-    float sd = (fabsf(d.x) + fabsf(d.y)) + fabsf(d.z);
-    float s0 = (fabsf(e0.x) + fabsf(e0.y)) + fabsf(e0.z);
-    float s1 = (fabsf(e1.x) + fabsf(e1.y)) + fabsf(e1.z);
+    float s01 = ((fabsf(e0.x) + fabsf(e0.y)) + fabsf(e0.z)) + ((fabsf(e1.x) + fabsf(e1.y)) + fabsf(e1.z));
     float ss = (fabsf(s.x) + fabsf(s.y)) + fabsf(s.z);
-    float s01 = s0 + s1;
-    float k = ((sd * s01) * (ss + s01)) * (1.0f / fabsf(den));
-    float beta = k * NEAR_MISS_SCALE;
-    return u >= -beta && v >= -beta && u + v <= 1.0f + (beta + beta);
+    float sd = (fabsf(d.x) + fabsf(d.y)) + fabsf(d.z);
+    float m = ((sd * s01) * (ss + s01)) * NEAR_MISS_SCALE;
+    float ad = fabsf(den);
+    return fmaf(u, ad, m) >= 0.0f && fmaf(v, ad, m) >= 0.0f && fmaf(1.0f - (u + v), ad, m + m) >= 0.0f;
 }
 
 /* HitClosest -- bvh.hsh:191-273 on one BLAS, CheckLeafClosest :44-72.
@@ -1357,30 +1356,46 @@ static void pt_pixel(const pt_job_t* j, uint32_t pix, int32_t* stack, double* ou
                 }
             }
             if (bounce >= j->max_bounces) break;
-            v3 F = pt_fresnel(sf.F0, sf.F90, sf.NdotV);
-            float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
-            float rnd = prng(pix, sample, bounce, 4, j->seed);
-            float u0 = prng(pix, sample, bounce, 5, j->seed), u1 = prng(pix, sample, bounce, 6, j->seed);
-            v3 refl;
+            /* EvaluateIndirectLight (rayHit.csh:237-325): a partially opaque
+             * surface is passed straight through with chance
+             * clamp(1 - opacity, 0.1, 0.9) (:252-253, :282-291) */
+            float refractChance = sf.m.opacity == 1.0f ? 0.0f : fminf(fmaxf(1.0f - sf.m.opacity, 0.1f), 0.9f);
+            v3 refl, origin;
             float pdf;
-            if (rnd < specChance) {
-                pdf = pt_sample_specular(&sf, u0, u1, &refl);
-                refl = vmul(refl, sf.m.opacity);
-                pdf *= specChance;
+            int through = 0;
+            if (prng(pix, sample, bounce, 3, j->seed) >= refractChance) {
+                v3 F = pt_fresnel(sf.F0, sf.F90, sf.NdotV);
+                float specChance = fminf(fmaxf((F.x + F.y + F.z) * 0.33333f, 0.1f), 0.9f);
+                float rnd = prng(pix, sample, bounce, 4, j->seed);
+                float u0 = prng(pix, sample, bounce, 5, j->seed), u1 = prng(pix, sample, bounce, 6, j->seed);
+                if (rnd < specChance) {
+                    pdf = pt_sample_specular(&sf, u0, u1, &refl);
+                    refl = vmul(refl, sf.m.opacity);
+                    pdf *= specChance;
+                } else {
+                    pdf = pt_sample_diffuse(&sf, u0, u1, &refl);
+                    refl = vmul(refl, (1.0f - sf.m.metalness) * sf.m.opacity);
+                    pdf *= (1.0f - specChance);
+                }
+                pdf *= 1.0f - refractChance;
+                origin = vadd(sf.P, vmul(sf.V, j->epsilon));
             } else {
-                pdf = pt_sample_diffuse(&sf, u0, u1, &refl);
-                refl = vmul(refl, (1.0f - sf.m.metalness) * sf.m.opacity);
-                pdf *= (1.0f - specChance);
+                sf.L = vmul(sf.V, -1.0f);
+                pdf = refractChance;
+                refl = mk(1.0f - sf.m.opacity, 1.0f - sf.m.opacity, 1.0f - sf.m.opacity);
+                sf.NdotL = 1.0f;
+                origin = sub(sf.P, vmul(sf.N, j->epsilon));
+                through = 1;
             }
-            v3 origin = vadd(sf.P, vmul(sf.V, j->epsilon));
             if (pdf > 0.0f && refl.x + refl.y + refl.z > 0.0f) thr = vmul(vmulv(thr, refl), sf.NdotL / pdf);
             else thr = mk(0, 0, 0);
             v3 dir = vnorm(sf.L);
             thr = vmul(thr, sf.m.ao);
             float prob = fminf(fmaxf(fmaxf(thr.x, fmaxf(thr.y, thr.z)), 0.01f), 0.99f);
             prob = bounce < 3 ? fminf(3.0f * prob, 1.0f) : prob;
+            /* a pass-through is exempt from the below-surface termination (:318) */
             int alive = thr.x + thr.y + thr.z > 0.0f && prng(pix, sample, bounce, 7, j->seed) <= prob &&
-                        vdot(dir, sf.geoN) > 0.0f;
+                        (through || vdot(dir, sf.geoN) > 0.0f);
             if (!alive) break;
             thr = vmul(thr, 1.0f / prob);
             ro = origin;

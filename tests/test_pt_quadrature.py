@@ -429,3 +429,120 @@ def test_gpu_opacity_check_matches_quadrature_and_oracle(case):
     np.testing.assert_allclose(img, expected, rtol=tp)
     # the same random numbers as the oracle: equal sample for sample
     np.testing.assert_allclose(g64, _oracle_image(sc, 64, 0), rtol=2e-5, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# The pass-through of a partially opaque surface the camera sees
+# ---------------------------------------------------------------------------
+#
+# A diffuse sheet of opacity ALPHA at y = 1, between the camera (y = 1.5) and
+# the floor, under the light (y = 2); max_bounces = 1.  EvaluateIndirectLight
+# (rayHit.csh:237-325) passes through the sheet with chance
+# clamp(1 - opacity, 0.1, 0.9) and throughput (1 - opacity) / chance, keeping
+# the direction (:282-291); the reflection lobes take the rest and meet only
+# the light's back or nothing (emission counts at bounce 0 only).  So a
+# pixel's expectation is
+#     ALPHA^2 D_sheet + (1 - ALPHA)^2 D_floor
+# with D the direct-light quadrature at the sheet's and the floor's point on
+# the camera ray: the sheet's own light sample carries the engine's opacity^2
+# factor, and the floor's is reached with expected throughput 1 - ALPHA and
+# seen through the sheet with visibility 1 - ALPHA (HitAnyTransparency).
+
+ALPHA, SHEET_Y = 0.5, 1.0
+
+
+def expected_at_height(y0, n=400):
+    """expected_image's direct-light quadrature for a grey diffuse plane at
+    height y0 (its normal up), at the point each pixel centre's ray meets it."""
+    cam = camera()
+    u = (np.arange(W) + 0.5) / W
+    v = (np.arange(H) + 0.5) / H
+    d = (cam["origin"][None, None, :].astype(np.float64) + cam["right"][None, None, :] * u[None, :, None]
+         + cam["bottom"][None, None, :] * v[:, None, None] - cam["location"])
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    eye = np.asarray(EYE, np.float64)
+    x = eye + d * ((y0 - eye[1]) / d[..., 1:2])
+    g = (np.arange(n) + 0.5) / n * 2 * HALF - HALF
+    ly = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    lp = np.stack([ly[:, 0], np.full(len(ly), LIGHT_Y), ly[:, 1]], 1)
+    dA = (2 * HALF / n) ** 2
+    out = np.zeros((H, W))
+    for i in range(H):
+        for j in range(W):
+            p = x[i, j]
+            V = (eye - p) / np.linalg.norm(eye - p)
+            toL = lp - p
+            d2 = (toL ** 2).sum(1)
+            L = toL / np.sqrt(d2)[:, None]
+            Hh = L + V
+            Hh /= np.linalg.norm(Hh, axis=1, keepdims=True)
+            NdotL = np.clip(L[:, 1], 0, 1)
+            f = brdf("diffuse", np.clip(V[1], 0, 1), NdotL, np.clip(Hh[:, 1], 0, 1),
+                     np.clip((L * Hh).sum(1), 0, 1))
+            out[i, j] = np.sum(f * RADIANCE * NdotL * NdotL / d2) * dA
+    return out
+
+
+def pass_through_scene():
+    sc = furnace_scene("diffuse")
+    tri = np.array([[[-10.0, SHEET_Y, -10.0], [-10.0, SHEET_Y, 30.0], [30.0, SHEET_Y, -10.0]]], F32)
+    tris = np.concatenate([sc["tris"], tri]).astype(F32)
+    obj = np.concatenate([sc["obj"], np.array([2], np.int32)])
+    normals = np.concatenate([sc["normals"], np.tile(np.array([0, 1, 0], F32), (1, 3, 1))]).astype(F32)
+    mats = np.zeros(3, MATERIAL_DTYPE)
+    mats[:2] = sc["materials"]
+    mats[2] = sc["materials"][0]
+    mats[2]["ID"] = 2
+    mats[2]["opacity"] = ALPHA          # the triangles' opacity is the material's (MeshData.cpp:141)
+    opacity = np.array([1, 1, 1, 1, ALPHA], F32)
+    sc.update(tris=tris, obj=obj, normals=normals, materials=mats, bvh=BVH(tris), opacity=opacity)
+    return sc
+
+
+_PASS_EXPECTED = []
+
+
+def pass_expected():
+    if not _PASS_EXPECTED:
+        _PASS_EXPECTED.append(ALPHA ** 2 * expected_at_height(SHEET_Y) + (1 - ALPHA) ** 2 * expected_at_height(0.0))
+    return _PASS_EXPECTED[0]
+
+
+def test_quadrature_at_height_zero_is_the_floors():
+    np.testing.assert_allclose(expected_at_height(0.0, n=100), expected_image("diffuse", n=100), rtol=1e-12)
+
+
+def test_oracle_pass_through_matches_quadrature():
+    expected = pass_expected()
+    spp = 8192
+    img = _oracle_image(pass_through_scene(), spp, 1)[..., 0] / spp
+    # the branch choice doubles the per-pixel variance of the one-bounce case
+    assert abs(img.mean() - expected.mean()) / expected.mean() < 0.005, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=0.04)
+
+
+@pytest.mark.gpu
+def test_gpu_pass_through_matches_quadrature_and_oracle():
+    import torch
+    expected = pass_expected()
+    sc = pass_through_scene()
+    ctx = atlas_rt.Context(device=0)
+    try:
+        ptscene.upload(ctx, sc)
+        cam = atlas_rt.make_camera(camera())
+        acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+        spp = 65536
+        ctx.pathtrace(cam, acc, acc64, spp=spp, max_bounces=1)
+        ctx.synchronize()
+        img = acc64.cpu().numpy()[:, 0].reshape(H, W) / spp
+        acc64.zero_()
+        ctx.pathtrace(cam, acc, acc64, spp=64, max_bounces=1)
+        ctx.synchronize()
+        g64 = acc64.cpu().numpy().reshape(H, W, 3)
+    finally:
+        ctx.close()
+    assert abs(img.mean() - expected.mean()) / expected.mean() < 0.002, (img.mean(), expected.mean())
+    np.testing.assert_allclose(img, expected, rtol=0.015)
+    # both sides draw the same random numbers, the pass-through choice included
+    np.testing.assert_allclose(g64, _oracle_image(sc, 64, 1), rtol=2e-5, atol=1e-6)
