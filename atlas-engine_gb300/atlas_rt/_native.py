@@ -187,6 +187,7 @@ _SIGNATURES = [
     ("ae_rt_cast_pass", C.c_int, [P, I32, C.POINTER(Camera), C.POINTER(BounceParams), C.POINTER(CastOutputs), P]),
     ("ae_rt_synchronize", C.c_int, [P, P]),
     ("ae_rt_selftest_division", C.c_int, [P, C.c_uint64, U32, C.POINTER(C.c_uint64)]),
+    ("ae_rt_selftest_shading", C.c_int, [P, U32, P, U32, P]),
     ("ae_rt_get_fetch_counts", C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 ]
 

@@ -1379,6 +1379,124 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
     return AE_RT_OK;
 }
 
+namespace {
+
+// The path tracer's own device functions on rows of inputs (the layouts of
+// ae_rt_selftest_shading in include/atlas_rt.h).
+__global__ void selftest_shading_kernel(uint32_t kind, const float* in, uint32_t n, float* out) {
+    using namespace atlas::rt::dev;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto surf = [](const float* r, bool withL) {
+        Surf s{};
+        s.V = v3(r[0], r[1], r[2]);
+        s.N = v3(r[3], r[4], r[5]);
+        s.L = withL ? v3(r[6], r[7], r[8]) : s.N;
+        s.mat.base = v3(r[9], r[10], r[11]);
+        s.mat.roughness = r[12];
+        s.mat.metalness = r[13];
+        s.mat.reflectance = r[14];
+        s.mat.opacity = 1.0f;
+        s.mat.ao = 1.0f;
+        update_surface(s);
+        return s;
+    };
+    switch (kind) {
+    case AE_SELFTEST_EVAL: {
+        const Surf s = surf(in + size_t(i) * 15, true);
+        const V3 d = eval_diffuse(s), sp = eval_specular(s);
+        float* o = out + size_t(i) * 16;
+        const float v[16] = { d.x, d.y, d.z, sp.x, sp.y, sp.z, s.NdotL, s.NdotV, s.NdotH, s.LdotH,
+                              s.F0.x, s.F0.y, s.F0.z, s.F90, s.H.x, s.H.y };
+        for (int k = 0; k < 16; k++) o[k] = v[k];
+        break;
+    }
+    case AE_SELFTEST_SAMPLE_DIFFUSE:
+    case AE_SELFTEST_SAMPLE_SPECULAR: {
+        const float* r = in + size_t(i) * 17;
+        Surf s = surf(r, false);
+        V3 refl;
+        const float pdf = kind == AE_SELFTEST_SAMPLE_DIFFUSE ? sample_diffuse(s, r[15], r[16], refl)
+                                                              : sample_specular(s, r[15], r[16], refl);
+        float* o = out + size_t(i) * 8;
+        const float v[8] = { s.L.x, s.L.y, s.L.z, pdf, refl.x, refl.y, refl.z, s.NdotL };
+        for (int k = 0; k < 8; k++) o[k] = v[k];
+        break;
+    }
+    case AE_SELFTEST_TRIANGLE_LIGHT: {
+        const float* r = in + size_t(i) * 24;
+        Tri lt{};
+        lt.v0 = v3(r[0], r[1], r[2]); lt.v1 = v3(r[3], r[4], r[5]); lt.v2 = v3(r[6], r[7], r[8]);
+        lt.n0 = v3(r[9], r[10], r[11]); lt.n1 = v3(r[12], r[13], r[14]); lt.n2 = v3(r[15], r[16], r[17]);
+        V3 P, N;
+        triangle_light_point(lt, r[19], r[20], P, N);
+        float* o = out + size_t(i) * 7;
+        const float v[7] = { P.x, P.y, P.z, N.x, N.y, N.z, 1.0f / r[18] };
+        for (int k = 0; k < 7; k++) o[k] = v[k];
+        break;
+    }
+    case AE_SELFTEST_EVAL_TERMS: {
+        // NdotL NdotV NdotH LdotH F0(3) F90 baseColor(3) roughness metalness
+        const float* r = in + size_t(i) * 13;
+        Surf s{};
+        s.NdotL = r[0]; s.NdotV = r[1]; s.NdotH = r[2]; s.LdotH = r[3];
+        s.F0 = v3(r[4], r[5], r[6]);
+        s.F90 = r[7];
+        s.mat.base = v3(r[8], r[9], r[10]);
+        s.mat.roughness = r[11];
+        s.mat.metalness = r[12];
+        const V3 d = eval_diffuse(s), sp = eval_specular(s);
+        float* o = out + size_t(i) * 6;
+        o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = sp.x; o[4] = sp.y; o[5] = sp.z;
+        break;
+    }
+    case AE_SELFTEST_TRIANGLE: {
+        const float* r = in + size_t(i) * 15;
+        const float4 a = make_float4(r[6], r[7], r[8], 0.0f), b = make_float4(r[9], r[10], r[11], 0.0f),
+                     c = make_float4(r[12], r[13], r[14], 0.0f);
+        float t, u, v;
+        const bool hit = tri_test(r[0], r[1], r[2], r[3], r[4], r[5], a, b, c, t, u, v);
+        float* o = out + size_t(i) * 4;
+        o[0] = hit ? 1.0f : 0.0f; o[1] = t; o[2] = u; o[3] = v;
+        break;
+    }
+    case AE_SELFTEST_AABB: {
+        const float* r = in + size_t(i) * 14;
+        float dist;
+        bool nearCull;
+        const bool hit = box_test<false>(r[0], r[1], r[2], r[3], r[4], r[5], 0.0f, 0.0f, 0.0f, r[6], r[7], r[8],
+                                         r[9], r[10], r[11], r[12], r[13], dist, nearCull);
+        out[size_t(i) * 2] = hit ? 1.0f : 0.0f;
+        out[size_t(i) * 2 + 1] = dist;
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+}  // namespace
+
+ae_rt_status ae_rt_selftest_shading(ae_rt_ctx* ctx, uint32_t kind, const float* in, uint32_t n, float* out) {
+    static const uint32_t kIn[] = { 15, 17, 17, 24, 13, 15, 14 }, kOut[] = { 16, 8, 8, 7, 6, 4, 2 };
+    if (!ctx || (n && (!in || !out))) return AE_RT_INVALID_ARG;
+    if (kind > AE_SELFTEST_AABB) return Fail(ctx, AE_RT_INVALID_ARG, "unknown self-test kind");
+    if (n == 0) return AE_RT_OK;
+    AE_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t ib = size_t(n) * kIn[kind] * sizeof(float), ob = size_t(n) * kOut[kind] * sizeof(float);
+    float* d = nullptr;
+    AE_CUDA(ctx, cudaMalloc(&d, ib + ob));
+    cudaError_t e = cudaMemcpy(d, in, ib, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        selftest_shading_kernel<<<(n + 127) / 128, 128>>>(kind, d, n, d + size_t(n) * kIn[kind]);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + size_t(n) * kIn[kind], ob, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    AE_CUDA(ctx, e);
+    return AE_RT_OK;
+}
+
 ae_rt_status ae_rt_selftest_division(ae_rt_ctx* ctx, uint64_t n, uint32_t seed, uint64_t* mismatches) {
     if (!ctx || !mismatches) return AE_RT_INVALID_ARG;
     AE_CUDA(ctx, cudaSetDevice(ctx->device));

@@ -501,6 +501,14 @@ __device__ __forceinline__ Surf make_surface(const PtScene& sc, V3 ro, V3 rd, fl
     return sf;
 }
 
+// SampleTriangleLight (raytracer/lights.hsh:11-29): the point and normal of
+// a triangle light at (r0, r1), uniform over its area.
+__device__ __forceinline__ void triangle_light_point(const Tri& lt, float r0, float r1, V3& P, V3& N) {
+    const float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
+    P = lt.v0 * lu + lt.v1 * lv + lt.v2 * lw;
+    N = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
+}
+
 // Selection weight of a light seen from P (raytracer/direct.hsh:12-49).
 __device__ __forceinline__ float light_weight(const Light& L, V3 P) {
     float w = 1.0f;
@@ -550,9 +558,8 @@ __device__ __forceinline__ bool sample_light(const PtScene& sc, Surf& sf, uint32
         const float r0 = rng(pix, sample, bounce, 1, seed);
         const float r1 = rng(pix, sample, bounce, 2, seed);
         const Tri lt = load_triangle(sc, sel.inst, sel.tri);
-        const float lu = 1.0f - sqrtf(r0), lv = r1 * sqrtf(r0), lw = 1.0f - lu - lv;
-        const V3 LP = lt.v0 * lu + lt.v1 * lv + lt.v2 * lw;
-        const V3 LN = lt.n0 * lu + lt.n1 * lv + lt.n2 * lw;
+        V3 LP, LN;
+        triangle_light_point(lt, r0, r1, LP, LN);
         const V3 toL = LP - sf.P;
         const float d2 = dot(toL, toL);
         ls.dist = sqrtf(d2);

@@ -1063,6 +1063,35 @@ ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint
  * (0 expected).  Diagnostic only; uses the context's fetch-count scratch. */
 ae_rt_status ae_rt_selftest_division(ae_rt_ctx* ctx, uint64_t n, uint32_t seed, uint64_t* mismatches);
 
+/* Device self-test of the path tracer's shading and intersection functions:
+ * evaluates the very device functions the path tracer and the traversal use
+ * on n host rows of inputs and copies the n output rows back (synchronous;
+ * diagnostic only).  Row layouts (floats), the same as the golden vectors of
+ * the reference's GLSL helpers:
+ *   EVAL            in 15: V N L baseColor roughness metalness reflectance
+ *                   out 16: diffuse(3) specular(3) NdotL NdotV NdotH LdotH F0(3) F90 H.x H.y
+ *                   (UpdateSurface, EvaluateDiffuseBRDF / EvaluateSpecularBRDF,
+ *                   brdf/surface.hsh:25-41, brdf/brdfEval.hsh:8-32)
+ *   SAMPLE_DIFFUSE, SAMPLE_SPECULAR
+ *                   in 17: the EVAL row (L ignored) + u0 u1
+ *                   out 8: L(3) pdf reflectance(3) NdotL (brdf/brdfSample.hsh:8-90)
+ *   TRIANGLE_LIGHT  in 24: v0 v1 v2 n0 n1 n2 area r0 r1 P(3)
+ *                   out 7: P(3) N(3) pdf (raytracer/lights.hsh:11-29)
+ *   EVAL_TERMS      in 13: NdotL NdotV NdotH LdotH F0(3) F90 baseColor(3) roughness metalness
+ *                   out 6: diffuse(3) specular(3)
+ *   TRIANGLE        in 15: origin direction v0 v1 v2; out 4: hit t u v
+ *                   (IntersectTriangle, raytracer/intersections.hsh:36-57)
+ *   AABB            in 14: origin direction min max tmin tmax; out 2: hit dist
+ *                   (IntersectAABB, raytracer/intersections.hsh:18-34) */
+#define AE_SELFTEST_EVAL 0u
+#define AE_SELFTEST_SAMPLE_DIFFUSE 1u
+#define AE_SELFTEST_SAMPLE_SPECULAR 2u
+#define AE_SELFTEST_TRIANGLE_LIGHT 3u
+#define AE_SELFTEST_EVAL_TERMS 4u
+#define AE_SELFTEST_TRIANGLE 5u
+#define AE_SELFTEST_AABB 6u
+ae_rt_status ae_rt_selftest_shading(ae_rt_ctx* ctx, uint32_t kind, const float* in, uint32_t n, float* out);
+
 #ifdef __cplusplus
 }
 #endif

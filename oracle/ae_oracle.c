@@ -1049,6 +1049,102 @@ static float pt_sample_specular(pt_surf* s, float u0, float u1, v3* refl) {
     return pdf;
 }
 
+/* The shading functions above on rows of inputs, in the layouts of the
+ * golden vectors written by the reference's own GLSL compiled on the host
+ * (oracle/glsl/glsl_capi.cpp): surface rows V N L baseColor roughness
+ * metalness reflectance. */
+static pt_surf shade_surface(const float* r, int with_l) {
+    pt_surf s;
+    memset(&s, 0, sizeof(s));
+    s.V = ld3(r);
+    s.N = ld3(r + 3);
+    s.L = with_l ? ld3(r + 6) : ld3(r + 3);
+    s.m.base = ld3(r + 9);
+    s.m.roughness = r[12];
+    s.m.metalness = r[13];
+    s.m.reflectance = r[14];
+    s.m.opacity = 1.0f;
+    s.m.ao = 1.0f;
+    pt_update(&s);
+    return s;
+}
+
+void aeo_shade_eval(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        pt_surf s = shade_surface(in + (size_t)i * 15, 1);
+        float* o = out + (size_t)i * 16;
+        v3 d = pt_eval_diffuse(&s), sp = pt_eval_specular(&s);
+        o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = sp.x; o[4] = sp.y; o[5] = sp.z;
+        o[6] = s.NdotL; o[7] = s.NdotV; o[8] = s.NdotH; o[9] = s.LdotH;
+        o[10] = s.F0.x; o[11] = s.F0.y; o[12] = s.F0.z; o[13] = s.F90; o[14] = s.H.x; o[15] = s.H.y;
+    }
+}
+
+void aeo_shade_sample(const float* in, int n, int specular, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + (size_t)i * 17;
+        pt_surf s = shade_surface(r, 0);
+        v3 refl;
+        float pdf = specular ? pt_sample_specular(&s, r[15], r[16], &refl) : pt_sample_diffuse(&s, r[15], r[16], &refl);
+        float* o = out + (size_t)i * 8;
+        o[0] = s.L.x; o[1] = s.L.y; o[2] = s.L.z; o[3] = pdf;
+        o[4] = refl.x; o[5] = refl.y; o[6] = refl.z; o[7] = s.NdotL;
+    }
+}
+
+/* The BRDF evaluation from given surface terms: rows NdotL NdotV NdotH LdotH
+ * F0(3) F90 baseColor(3) roughness metalness -> diffuse(3) specular(3). */
+void aeo_shade_eval_terms(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + (size_t)i * 13;
+        pt_surf s;
+        memset(&s, 0, sizeof(s));
+        s.NdotL = r[0]; s.NdotV = r[1]; s.NdotH = r[2]; s.LdotH = r[3];
+        s.F0 = ld3(r + 4); s.F90 = r[7];
+        s.m.base = ld3(r + 8); s.m.roughness = r[11]; s.m.metalness = r[12];
+        v3 d = pt_eval_diffuse(&s), sp = pt_eval_specular(&s);
+        float* o = out + (size_t)i * 6;
+        o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = sp.x; o[4] = sp.y; o[5] = sp.z;
+    }
+}
+
+/* The point and normal of a triangle light at (r0, r1) as pt_sample_light
+ * forms them (SampleTriangleLight, lights.hsh:11-29), pdf = 1 / area. */
+void aeo_shade_triangle_light(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + (size_t)i * 24;
+        float lu = 1.0f - sqrtf(r[19]), lv = r[20] * sqrtf(r[19]), lw = 1.0f - lu - lv;
+        v3 P = vadd(vadd(vmul(ld3(r), lu), vmul(ld3(r + 3), lv)), vmul(ld3(r + 6), lw));
+        v3 N = vadd(vadd(vmul(ld3(r + 9), lu), vmul(ld3(r + 12), lv)), vmul(ld3(r + 15), lw));
+        float* o = out + (size_t)i * 7;
+        o[0] = P.x; o[1] = P.y; o[2] = P.z; o[3] = N.x; o[4] = N.y; o[5] = N.z; o[6] = 1.0f / r[18];
+    }
+}
+
+/* The triangle and slab tests of the shader query on rows: origin direction
+ * v0 v1 v2 -> hit t u v; origin direction min max tmin tmax -> hit dist. */
+void aeo_shade_intersect_triangle(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + (size_t)i * 15;
+        aeo_tri t;
+        memcpy(t.v0, r + 6, 12); memcpy(t.v1, r + 9, 12); memcpy(t.v2, r + 12, 12);
+        float st, su, sv;
+        int hit = tri_test(ld3(r), ld3(r + 3), &t, &st, &su, &sv);
+        float* o = out + (size_t)i * 4;
+        o[0] = hit ? 1.0f : 0.0f; o[1] = st; o[2] = su; o[3] = sv;
+    }
+}
+
+void aeo_shade_intersect_aabb(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + (size_t)i * 14;
+        float dist;
+        int hit = box_glsl(ld3(r), ld3(r + 3), r[12], r[13], r + 6, r + 9, &dist);
+        out[(size_t)i * 2] = hit ? 1.0f : 0.0f;
+        out[(size_t)i * 2 + 1] = dist;
+    }
+}
+
 typedef struct {
     v3 v0, v1, v2, n0, n1, n2;
     int material;

@@ -69,6 +69,16 @@ void aeo_closest_glsl_ties(const aeo_node* nodes, uint32_t n_nodes, const aeo_tr
                            const float* rays, uint32_t n_rays, int threads,
                            int32_t* tri_ptr, float* tuv, uint32_t* flags, float* t_second);
 
+/* The restatement's shading and intersection functions on rows of inputs,
+ * in the layouts of the golden vectors the reference's GLSL writes when
+ * compiled on the host (oracle/glsl/glsl_capi.cpp). */
+void aeo_shade_eval(const float* in, int n, float* out);
+void aeo_shade_eval_terms(const float* in, int n, float* out);
+void aeo_shade_sample(const float* in, int n, int specular, float* out);
+void aeo_shade_triangle_light(const float* in, int n, float* out);
+void aeo_shade_intersect_triangle(const float* in, int n, float* out);
+void aeo_shade_intersect_aabb(const float* in, int n, float* out);
+
 /* Host any-hit query (BVH.cpp:176-217); occluded[i] = 0/1. */
 void aeo_any_cpu(const aeo_node* nodes, uint32_t n_nodes, const aeo_tri* tris, uint32_t n_tris,
                  const float* rays, uint32_t n_rays, int threads, uint8_t* occluded);

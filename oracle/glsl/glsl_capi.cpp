@@ -1,0 +1,131 @@
+// C entry points over the reference's GLSL shading helpers compiled on the
+// host (oracle/glsl/make_ref.py) -- TEST INFRASTRUCTURE ONLY: the golden
+// generator calls them; nothing on the product path links this.
+//
+// Each function takes n packed input rows and writes n packed output rows of
+// floats, evaluating the reference's own code:
+//   CreateSurface / UpdateSurface            brdf/surface.hsh:25-57
+//   EvaluateDiffuseBRDF / EvaluateSpecularBRDF  brdf/brdfEval.hsh:8-32
+//   SampleDiffuseBRDF / SampleSpecularBRDF   brdf/brdfSample.hsh:8-90
+//   SampleTriangleLight                      raytracer/lights.hsh:11-29
+//   IntersectAABB / IntersectTriangle        raytracer/intersections.hsh:18-57
+//   random(x, inout seed)                    common/random.hsh:5-54
+#include "glsl.hpp"
+#include "glsl_ref.inc"
+
+namespace {
+
+// Row layout of a surface: V(3) N(3) L(3) baseColor(3) roughness metalness reflectance
+constexpr int kSurfaceIn = 15;
+
+Material MakeMaterial(const float* r) {
+    Material m;
+    m.baseColor = vec3(r[9], r[10], r[11]);
+    m.roughness = r[12];
+    m.metalness = r[13];
+    m.reflectance = r[14];
+    m.opacity = 1.0f;
+    m.ao = 1.0f;
+    return m;
+}
+
+vec3 V3(const float* p) { return vec3(p[0], p[1], p[2]); }
+void Put(float* o, const vec3& v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+
+}  // namespace
+
+extern "C" {
+
+// in: kSurfaceIn floats per row.  out per row (16): diffuse(3) specular(3)
+// NdotL NdotV NdotH LdotH F0(3) F90 H.xy
+void aeglsl_eval(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + i * kSurfaceIn;
+        Surface s = CreateSurface(V3(r), V3(r + 3), V3(r + 6), MakeMaterial(r));
+        float* o = out + i * 16;
+        Put(o, EvaluateDiffuseBRDF(s));
+        Put(o + 3, EvaluateSpecularBRDF(s));
+        o[6] = s.NdotL; o[7] = s.NdotV; o[8] = s.NdotH; o[9] = s.LdotH;
+        Put(o + 10, s.F0);
+        o[13] = s.F90;
+        o[14] = s.H.x; o[15] = s.H.y;
+    }
+}
+
+// in: kSurfaceIn floats (L ignored) + u0 u1 per row.  out per row (8):
+// L(3) pdf reflectance(3) NdotL.  specular: SampleSpecularBRDF, else diffuse.
+void aeglsl_sample(const float* in, int n, int specular, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + i * (kSurfaceIn + 2);
+        Surface s = CreateSurface(V3(r), V3(r + 3), V3(r + 3), MakeMaterial(r));
+        const vec2 u(r[kSurfaceIn], r[kSurfaceIn + 1]);
+        BRDFSample b = specular ? SampleSpecularBRDF(s, u) : SampleDiffuseBRDF(s, u);
+        float* o = out + i * 8;
+        Put(o, s.L);
+        o[3] = b.pdf;
+        Put(o + 4, b.reflectance);
+        o[7] = s.NdotL;
+    }
+}
+
+// in per row (24): v0 v1 v2 n0 n1 n2 (18) area r0 r1 P(3, the shaded point,
+// unused by the sample).  out per row (7): P(3) N(3) pdf.
+void aeglsl_triangle_light(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + i * 24;
+        Triangle t;
+        t.v0 = V3(r); t.v1 = V3(r + 3); t.v2 = V3(r + 6);
+        t.n0 = V3(r + 9); t.n1 = V3(r + 12); t.n2 = V3(r + 15);
+        Light l;
+        l.area = r[18];
+        Surface s;
+        s.P = V3(r + 21);
+        LightSample ls = SampleTriangleLight(l, t, s, r[19], r[20]);
+        float* o = out + i * 7;
+        Put(o, ls.P);
+        Put(o + 3, ls.N);
+        o[6] = ls.pdf;
+    }
+}
+
+// in per row (15): origin(3) direction(3) v0(3) v1(3) v2(3); out (4): hit, t, u, v.
+void aeglsl_intersect_triangle(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + i * 15;
+        Ray ray;
+        ray.origin = V3(r);
+        ray.direction = V3(r + 3);
+        vec3 sol;
+        const bool hit = IntersectTriangle(ray, V3(r + 6), V3(r + 9), V3(r + 12), sol);
+        float* o = out + i * 4;
+        o[0] = hit ? 1.0f : 0.0f;
+        o[1] = sol.x; o[2] = sol.y; o[3] = sol.z;
+    }
+}
+
+// in per row (14): origin(3) direction(3) min(3) max(3) tmin tmax; out (2): hit, dist.
+void aeglsl_intersect_aabb(const float* in, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = in + i * 14;
+        Ray ray;
+        ray.origin = V3(r);
+        ray.direction = V3(r + 3);
+        AABB box;
+        box.min = V3(r + 6);
+        box.max = V3(r + 9);
+        float dist = 0.0f;
+        const bool hit = IntersectAABB(ray, box, r[12], r[13], dist);
+        out[i * 2] = hit ? 1.0f : 0.0f;
+        out[i * 2 + 1] = dist;
+    }
+}
+
+// count draws of random(x, seed) from the seed, per x; out: n * count floats.
+void aeglsl_random(const float* x, int n, float seed0, int count, float* out) {
+    for (int i = 0; i < n; i++) {
+        float seed = seed0;
+        for (int k = 0; k < count; k++) out[i * count + k] = random(x[i], seed);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+"""Builds oracle/_ref/libglslref.so from the reference's own GLSL helpers --
+TEST INFRASTRUCTURE ONLY (the recipe; run by tests/golden/gen_glsl_goldens.py).
+
+The engine's shading math lives in GLSL include files that need no graphics
+API: data/shader/brdf/{brdf,brdfEval,brdfSample,surface}.hsh,
+raytracer/{lights,intersections,structures}.hsh, common/{random,utility,PI,
+material,packing}.hsh.  This recipe reads them where they lie in the
+reference tree (unchanged on disk), flattens their `#include <...>` lines the
+way the engine's shader loader does (relative to the including file, each
+file once), and makes the GLSL parse as C++ with the vector types of
+glsl.hpp.  The text of every function is kept; only these mechanical,
+language-level adjustments are applied:
+
+  * `#extension` lines are dropped;
+  * `in T x` / `out T x` / `inout T x` parameters become `T x` / `T& x` /
+    `T& x` (GLSL's copy-out semantics, expressed as C++ references);
+  * float literals get an `f` suffix (a GLSL float literal is single
+    precision, a C++ one double);
+  * resource declarations (`layout(...)`, storage `buffer` blocks, `uniform`
+    blocks) become plain globals: a buffer block's runtime-sized arrays become
+    pointers, which the goldens never read;
+  * the engine's globals.hsh (uniform blocks and bindless textures) is
+    replaced by the one resource the helpers name, the DFG lookup texture.
+
+The flattened source goes to oracle/_ref/glsl_ref.inc and is compiled with
+oracle/glsl/glsl_capi.cpp (-O2 -ffp-contract=off) into
+oracle/_ref/libglslref.so.  Usage: python make_ref.py [REFERENCE_ROOT]
+"""
+from __future__ import annotations
+
+import re
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ORACLE = HERE.parent
+OUT_DIR = ORACLE / "_ref"
+ENTRY_FILES = ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh"]
+GLOBALS_STUB = "static glsl_sampler2D dfgTexture;\n"
+
+_INCLUDE = re.compile(r'^\s*#include\s*<([^>]+)>\s*$')
+_FLOAT = re.compile(r'(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])')
+_QUAL = re.compile(r'\b(inout|out|in)\s+([A-Za-z_]\w*)\s+([A-Za-z_]\w*)')
+_LAYOUT = re.compile(r'\blayout\s*\([^)]*\)\s*')
+_BUFFER = re.compile(r'\bbuffer\s+\w+\s*\{([^}]*)\}\s*;', re.S)
+_UNIFORM_BLOCK = re.compile(r'\buniform\s+(\w+)\s*\{')
+
+
+def _flatten(path: Path, seen: set, shader_root: Path) -> str:
+    path = path.resolve()
+    if path in seen:
+        return ""
+    seen.add(path)
+    if path == (shader_root / "globals.hsh").resolve():
+        return GLOBALS_STUB
+    out = []
+    for line in path.read_text().splitlines():
+        m = _INCLUDE.match(line)
+        if m:
+            out.append(_flatten(path.parent / m.group(1), seen, shader_root))
+        elif line.lstrip().startswith("#extension"):
+            continue
+        else:
+            out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def _buffer_to_globals(m: re.Match) -> str:
+    decls = []
+    for d in m.group(1).split(";"):
+        d = d.strip()
+        if not d:
+            continue
+        arr = re.match(r'(\w+)\s+(\w+)\s*\[\s*\]$', d)
+        decls.append(f"static {arr.group(1)}* {arr.group(2)} = nullptr;" if arr else f"static {d};")
+    return "\n".join(decls)
+
+
+def to_cpp(src: str) -> str:
+    def qual(m):
+        return f"{m.group(2)}& {m.group(3)}" if m.group(1) in ("inout", "out") else f"{m.group(2)} {m.group(3)}"
+    src = _QUAL.sub(qual, src)
+    src = _LAYOUT.sub("", src)
+    src = _BUFFER.sub(_buffer_to_globals, src)
+    src = _UNIFORM_BLOCK.sub(lambda m: f"struct {m.group(1)} {{", src)
+    src = _FLOAT.sub(lambda m: m.group(1) + "f", src)
+    return src
+
+
+def build(reference_root: Path) -> Path:
+    shader_root = reference_root / "data" / "shader"
+    seen: set = set()
+    body = "".join(_flatten(shader_root / f, seen, shader_root) for f in ENTRY_FILES)
+    OUT_DIR.mkdir(exist_ok=True)
+    inc = OUT_DIR / "glsl_ref.inc"
+    header = "// generated by oracle/glsl/make_ref.py from the reference's shader files; do not edit\n"
+    inc.write_text(header + to_cpp(body))
+    lib = OUT_DIR / "libglslref.so"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fno-builtin",
+           "-w", f"-I{HERE}", f"-I{OUT_DIR}", str(HERE / "glsl_capi.cpp"), "-o", str(lib)]
+    subprocess.run(cmd, check=True)
+    return lib
+
+
+if __name__ == "__main__":
+    root = Path(sys.argv[1]) if len(sys.argv) > 1 else None
+    if root is None:
+        sys.path.insert(0, str(ORACLE))
+        import pyoracle
+        root = pyoracle.REFERENCE_ROOT
+    print(build(root))

@@ -63,6 +63,21 @@ def build_ref(force: bool = False) -> Path | None:
     return REF_LIB
 
 
+def build_glsl_ref(force: bool = False) -> Path | None:
+    """The reference's GLSL shading helpers compiled on the host
+    (oracle/glsl/make_ref.py), if the reference tree exists here."""
+    if not (REFERENCE_ROOT / "data" / "shader" / "brdf" / "brdf.hsh").exists():
+        return None
+    lib = ORACLE_DIR / "_ref" / "libglslref.so"
+    if force or not lib.exists():
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("make_ref", ORACLE_DIR / "glsl" / "make_ref.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build(REFERENCE_ROOT)
+    return lib
+
+
 def port():
     global _port
     if _port is None:
