@@ -1,31 +1,52 @@
 """Autotuner of the traversal kernels' launch parameters.
 
-Searches, for one workload on the current GPU, over
-  * threads per CTA and the shared-memory share of each lane's traversal
-    stack (the kernel shapes the library ships: (128, 32), (64, 32),
-    (256, 16), (128, 16)),
-  * the refill interval: traversal steps a warp takes between two queue
-    refills (8 ... 128), i.e. the size of the per-warp ray tile,
-  * persistent CTAs per SM (the kernel's occupancy, or half of it),
-timing each candidate with CUDA events (median of a few repetitions after a
-warm-up) and returning the fastest.  Results can be saved as JSON and fed
-back as ae_rt_config fields.
+Searches, for one workload on the current GPU, the axes
+  * shape: threads per CTA and the shared-memory share of each lane's
+    traversal stack (the kernel shapes the library ships: (128, 32),
+    (64, 32), (256, 16), (128, 16));
+  * refill_steps: traversal steps a warp takes between two queue refills,
+    i.e. the size of the per-warp ray tile (8 ... 64);
+  * refill_below: refill as soon as fewer lanes than this still traverse
+    (never, 8, 16, 24);
+  * leaf_wait: closest-hit lanes at a leaf wait for this many leaf lanes
+    (0, 2, 4, 6);
+  * workload-specific axes (for the path tracer: the number of image tiles,
+    which sets the size of its wavefront queues);
+by coordinate descent: starting from the library's defaults, each axis in
+turn is swept with the others fixed and the fastest value kept, until a pass
+changes nothing (at most `passes` passes).  Each candidate is timed with CUDA
+events (median of a few repetitions after a warm-up).  The result is saved as
+JSON (atlas_rt/tuning.json) and fed back as ae_rt_config fields.
 """
 from __future__ import annotations
 
-import itertools
 import json
 from pathlib import Path
 
 SHAPES = [(128, 32), (64, 32), (256, 16), (128, 16)]
-REFILLS = [8, 16, 32, 64, 128]
-BLOCKS = [0, -2]        # 0: occupancy; negative: occupancy // -n (resolved by the caller's kernel)
+AXES = {
+    "shape": SHAPES,
+    "refill_steps": [8, 16, 32, 64],
+    "refill_below": [33, 8, 16, 24],      # 33: never refill early
+    "leaf_wait": [0, 2, 4, 6],
+}
+DEFAULTS = {"shape": (128, 32), "refill_steps": 32, "refill_below": 8, "leaf_wait": 0}
+CONFIG_KEYS = ("threads_per_block", "stack_entries_smem", "refill_steps", "refill_below", "leaf_wait",
+               "blocks_per_sm")
 
 
-def candidates(shapes=SHAPES, refills=REFILLS, blocks=(0,)):
-    for (threads, smem), refill, bps in itertools.product(shapes, refills, blocks):
-        yield {"threads_per_block": threads, "stack_entries_smem": smem, "refill_steps": refill,
-               "blocks_per_sm": bps}
+def to_config(point: dict) -> dict:
+    """A search point as Context keyword arguments (other axes are the
+    workload's own)."""
+    cfg = {k: v for k, v in point.items() if k != "shape"}
+    if "shape" in point:
+        cfg["threads_per_block"], cfg["stack_entries_smem"] = point["shape"]
+    return cfg
+
+
+def context_kwargs(cfg: dict | None) -> dict:
+    """The ae_rt_config fields of a tuned configuration."""
+    return {k: v for k, v in (cfg or {}).items() if k in CONFIG_KEYS}
 
 
 def time_workload(run, torch, reps: int = 5, warmup: int = 2) -> float:
@@ -45,23 +66,42 @@ def time_workload(run, torch, reps: int = 5, warmup: int = 2) -> float:
     return ts[len(ts) // 2]
 
 
-def tune(make_run, torch, space=None, reps: int = 5, log=None):
-    """make_run(config) -> (run, cleanup).  Returns (best_config, best_ms,
-    all results)."""
-    results = []
-    best, best_ms = None, float("inf")
-    for cfg in (space if space is not None else candidates()):
-        run, cleanup = make_run(cfg)
-        try:
-            ms = time_workload(run, torch, reps=reps)
-        finally:
-            cleanup()
-        results.append({**cfg, "ms": ms})
-        if log:
-            log(f"autotune {cfg} -> {ms:.3f} ms")
-        if ms < best_ms:
-            best, best_ms = cfg, ms
-    return best, best_ms, results
+def search(make_run, torch, axes=None, start=None, reps: int = 5, passes: int = 2, log=None):
+    """Coordinate descent.  make_run(config) -> (run, cleanup).  Returns
+    (best_config, best_ms, every timed point)."""
+    axes = dict(AXES if axes is None else axes)
+    point = dict(DEFAULTS if start is None else start)
+    point = {k: v for k, v in point.items() if k in axes}
+    results, cache = [], {}
+
+    def measure(p):
+        key = json.dumps(p, sort_keys=True, default=list)
+        if key not in cache:
+            cfg = to_config(p)
+            run, cleanup = make_run(cfg)
+            try:
+                cache[key] = time_workload(run, torch, reps=reps)
+            finally:
+                cleanup()
+            results.append({**cfg, "ms": cache[key]})
+            if log:
+                log(f"autotune {cfg} -> {cache[key]:.3f} ms")
+        return cache[key]
+
+    best_ms = measure(point)
+    for _ in range(passes):
+        changed = False
+        for axis, values in axes.items():
+            for v in values:
+                cand = {**point, axis: v}
+                if cand == point:
+                    continue
+                ms = measure(cand)
+                if ms < best_ms * 0.995:       # a change must win by more than the noise
+                    point, best_ms, changed = cand, ms, True
+        if not changed:
+            break
+    return to_config(point), best_ms, results
 
 
 def save(path: Path, workload: str, best: dict, best_ms: float, results: list, gpu: str):

@@ -381,7 +381,9 @@ def workload_random65536(torch, dev, stream, flush, steps, hbm_peak=None, l2_gbs
     o, d = scenes.sphere_rays()
     b = BVH(tris)
     gt = b.pack_triangles()
-    ctx = atlas_rt.Context(device=dev.index or 0)
+    from atlas_rt import autotune as at
+    tuned = at.load(TUNING, "random65536")
+    ctx = atlas_rt.Context(device=dev.index or 0, **at.context_kwargs(tuned))
     mid = ctx.upload_mesh(b.nodes, gt)
     n = len(o)
     packed = scenes.pack_rays(o, d)
@@ -430,6 +432,7 @@ def workload_random65536(torch, dev, stream, flush, steps, hbm_peak=None, l2_gbs
     ctx.close()
     out["rays"] = n
     out["triangles"] = len(tris)
+    out["tuning"] = {"source": "tuning.json" if tuned else "defaults", "config": tuned}
     return out
 
 
@@ -456,9 +459,7 @@ def workload_batched(torch, dev, stream, flush, steps, autotune=False, log=None,
     total = sum(sp["n_rays"] for sp in specs)
 
     def make_ctx(cfg):
-        ctx = atlas_rt.Context(device=dev.index or 0, threads_per_block=cfg["threads_per_block"],
-                               stack_entries_smem=cfg["stack_entries_smem"], refill_steps=cfg["refill_steps"],
-                               blocks_per_sm=max(cfg.get("blocks_per_sm", 0), 0))
+        ctx = atlas_rt.Context(device=dev.index or 0, **at.context_kwargs(cfg))
         mids = [ctx.upload_mesh(n, t) for n, t in meshes]
         batches = [{"mesh": mids[i], "any": sp["any"], "rays": rays[i], "out": outs[i], "n_rays": sp["n_rays"],
                     "tmin": 1e-4, "tmax": 10.0} for i, sp in enumerate(specs)]
@@ -471,8 +472,7 @@ def workload_batched(torch, dev, stream, flush, steps, autotune=False, log=None,
             ctx, batches = make_ctx(cfg)
             plan = ctx.batch_plan(batches)
             return (lambda: plan.launch(stream)), (lambda: (plan.close(), ctx.close()))
-        space = list(at.candidates(refills=[16, 32, 64, 128]))
-        tuned, best_ms, results = at.tune(make_run, torch, space=space, reps=3, log=log)
+        tuned, best_ms, results = at.search(make_run, torch, reps=3, log=log)
         at.save(TUNING, "batched64", tuned, best_ms, results, torch.cuda.get_device_name(dev))
         tuning_info["candidates"] = len(results)
     tuning_info["config"] = tuned
@@ -571,15 +571,32 @@ def workload_bvh_build(torch, dev, stream, flush, reps=5):
     return out
 
 
-def pt_context(dev):
-    """Context + uploaded path-tracing scene (terrain + boxes + 4x4 light);
-    sc["upload"] keeps (mesh id, shading triangles, lights, BVH triangles)."""
+def pt_context(dev, sc=None, cfg=None):
+    """Context (launch parameters from cfg) + uploaded path-tracing scene
+    (terrain + boxes + 4x4 light); sc["upload"] keeps (mesh id, shading
+    triangles, lights, BVH triangles)."""
     import atlas_rt
-    from atlas_rt import ptscene
-    ctx = atlas_rt.Context(device=dev.index or 0)
-    sc = ptscene.build()
+    from atlas_rt import autotune as at, ptscene
+    ctx = atlas_rt.Context(device=dev.index or 0, **at.context_kwargs(cfg))
+    sc = ptscene.build() if sc is None else sc
     sc["upload"] = ptscene.upload(ctx, sc)
     return ctx, sc
+
+
+def pt_tiles(k):
+    """k horizontal bands of the image, or the whole image: the path tracer's
+    wavefront queues hold the rays of one band (W * H / k)."""
+    if k <= 1:
+        return [None]
+    rows = [round(i * H / k) for i in range(k + 1)]
+    return [(0, rows[i], W, rows[i + 1] - rows[i]) for i in range(k)]
+
+
+def pt_render(ctx, cam, acc, acc64, spp, sample_offset, seed, tiles, stream):
+    """spp samples of every pixel, band after band (a pixel's samples do not
+    depend on the tiling)."""
+    for t in pt_tiles(tiles):
+        ctx.pathtrace(cam, acc, acc64, spp=spp, sample_offset=sample_offset, seed=seed, tile=t, stream=stream)
 
 
 def pt_cpu_seconds_per_spp(sc, threads):
@@ -701,8 +718,10 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     `ref_spp`-sample FP64-accumulated converged image; with cpu_threads, the
     oracle's seconds per sample at full resolution on that many host cores."""
     import atlas_rt
-    from atlas_rt import ptscene, scenes
-    ctx, sc = pt_context(dev)
+    from atlas_rt import autotune as at, ptscene, scenes
+    tuned = at.load(TUNING, "pathtrace") or {}
+    tiles = int(tuned.get("tiles", 1))
+    ctx, sc = pt_context(dev, cfg=tuned)
     cam = atlas_rt.make_camera(scenes.pinhole_camera(W, H))
     n = W * H
     acc = torch.zeros((n, 4), dtype=torch.float32, device=dev)
@@ -716,7 +735,7 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    ctx.pathtrace(cam, acc, spp=spp, sample_offset=0, seed=3, stream=stream)
+    pt_render(ctx, cam, acc, None, spp, 0, 3, tiles, stream)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     ms_total = e0.elapsed_time(e1)
@@ -740,6 +759,8 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     res = {"resolution": [W, H], "bounces": 3, "spp": spp, "ms_to_spp": final["ms_cum"],
            "ms_per_spp": final["ms_cum"] / spp, "rel_mse": final["rel_mse"], "rmse": final["rmse"],
            "reference_spp": ref_spp, "reference_seconds": t_ref, "rel_mse_eps": 1e-2,
+           "tuning": {"source": "tuning.json" if tuned else "defaults", "config": tuned or None,
+                      "queue_rays": W * H // max(tiles, 1)},
            "curve": [{k: c[k] for k in ("spp", "ms_cum", "rel_mse")} for c in curve]}
     if cpu_threads:
         cpu_s = pt_cpu_seconds_per_spp(sc, cpu_threads)
@@ -865,6 +886,76 @@ def _rc_run(torch, dev, stream, pt, scene, starts, max_frames, n_paths, steps, r
     return out
 
 
+def run_autotune(torch, dev, stream, log):
+    """--autotune: the launch-parameter search (atlas_rt/autotune.py) for the
+    camera pass, random 65,536 (closest + any) and the path tracer (8 spp;
+    with its tile-count axis, i.e. the size of its wavefront queues); results
+    go to atlas_rt/tuning.json.  The batched workload tunes itself."""
+    import atlas_rt
+    from atlas_rt import BVH, autotune as at, ptscene, scenes
+    gpu = torch.cuda.get_device_name(dev)
+    out = {}
+    # camera pass: raygen, primary, spawn, bounce, shadow
+    tris, bvh, gt = build_scene()
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(W, H))
+    bp = atlas_rt.make_bounce_params(LIGHT, EPSILON, seed=1)
+    n = W * H
+    bufs = [torch.empty((n, 12), dtype=torch.float32, device=dev) for _ in range(3)]
+    hits = [torch.empty((n, 8), dtype=torch.float32, device=dev) for _ in range(2)]
+    occ = torch.empty(n, dtype=torch.uint8, device=dev)
+    counts = torch.zeros(4, dtype=torch.int32, device=dev)
+
+    def make_cast(cfg):
+        ctx = atlas_rt.Context(device=dev.index or 0, **at.context_kwargs(cfg))
+        mid = ctx.upload_mesh(bvh.nodes, gt)
+
+        def run():
+            ctx.raygen(cam, bufs[0], stream)
+            ctx.trace_closest(mid, bufs[0], TMIN, TINF, out=hits[0], stream=stream, n_rays=n)
+            counts.zero_()
+            ctx.spawn_bounce(mid, bufs[0], hits[0], n, bp, bufs[1], bufs[2], counts, stream=stream)
+            ctx.trace_closest_queue(mid, bufs[1], counts[0:1], n, TMIN, TINF, hits[1], stream=stream)
+            ctx.trace_any_queue(mid, bufs[2], counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=stream)
+        return run, ctx.close
+    best, ms, res = at.search(make_cast, torch, reps=7, log=log)
+    at.save(TUNING, "cast_pass", best, ms, res, gpu)
+    out["cast_pass"] = (best, ms)
+    # random 65,536: closest and any over the same rays
+    ct = scenes.random_triangles()
+    o, d = scenes.sphere_rays()
+    cb = BVH(ct)
+    cgt = cb.pack_triangles()
+    crays = torch.from_numpy(scenes.pack_rays(o, d)).to(dev)
+    ch = torch.empty((len(o), 8), dtype=torch.float32, device=dev)
+    co = torch.empty(len(o), dtype=torch.uint8, device=dev)
+
+    def make_c0(cfg):
+        ctx = atlas_rt.Context(device=dev.index or 0, **at.context_kwargs(cfg))
+        mid = ctx.upload_mesh(cb.nodes, cgt)
+
+        def run():
+            ctx.trace_closest(mid, crays, 1e-4, 10.0, out=ch, stream=stream, n_rays=len(o))
+            ctx.trace_any(mid, crays, 1e-4, 10.0, out=co, stream=stream, n_rays=len(o))
+        return run, ctx.close
+    best, ms, res = at.search(make_c0, torch, reps=7, log=log)
+    at.save(TUNING, "random65536", best, ms, res, gpu)
+    out["random65536"] = (best, ms)
+    # path tracer: 8 samples per pixel, 3 bounces
+    sc = ptscene.build()
+    pcam = atlas_rt.make_camera(scenes.pinhole_camera(W, H))
+    acc = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+
+    def make_pt(cfg):
+        ctx, _ = pt_context(dev, sc=sc, cfg=cfg)
+        tiles = int(cfg.get("tiles", 1))
+        return (lambda: pt_render(ctx, pcam, acc, None, 8, 0, 3, tiles, stream)), ctx.close
+    axes = dict(at.AXES, tiles=[1, 2, 4, 8])
+    best, ms, res = at.search(make_pt, torch, axes=axes, start=dict(at.DEFAULTS, tiles=1), reps=3, log=log)
+    at.save(TUNING, "pathtrace", best, ms, res, gpu)
+    out["pathtrace"] = (best, ms)
+    return out
+
+
 def profile_case(args, torch, dev, stream):
     """--profile: set up one workload and launch its trace kernels for two
     steps (the short case that ncu captures; see profiles/)."""
@@ -920,8 +1011,14 @@ def main():
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream(dev)
 
+    from atlas_rt import autotune as at
+    if args.autotune:
+        tuned_all = run_autotune(torch, dev, stream, log=(lambda m: print(m, file=sys.stderr)))
+        print(json.dumps({"autotune": {k: {"best": b, "ms": m} for k, (b, m) in tuned_all.items()}}),
+              file=sys.stderr)
+    tuned_cast = at.load(TUNING, "cast_pass")
     tris, bvh, gt = build_scene()
-    ctx = atlas_rt.Context(device=local)
+    ctx = atlas_rt.Context(device=local, **at.context_kwargs(tuned_cast))
     mid = ctx.upload_mesh(bvh.nodes, gt)
     cam_d = scenes.pinhole_camera(W, H)
     cam = atlas_rt.make_camera(cam_d)
@@ -1093,6 +1190,7 @@ def main():
                 "api": "ae_rt_cast_pass, pinned host result buffers",
                 "definition": "closest-hit rays per second of the whole pass, results copied to the host"},
         "gpu_launches": launches_per_step * args.steps,
+        "tuning": {"source": "tuning.json" if tuned_cast else "defaults", "config": tuned_cast},
     }
     if not args.quick:
         wl = set(args.workloads.split(","))
