@@ -1,19 +1,27 @@
 // A subset of GLSL 4.60 for host C++ -- TEST INFRASTRUCTURE ONLY.
 //
-// oracle/glsl/make_ref.py compiles the reference's own GLSL helper files
-// (brdf/*.hsh, raytracer/lights.hsh, raytracer/intersections.hsh,
-// common/random.hsh, ...) unmodified on the host against this header, to
-// produce golden vectors of the engine's shading math.  Written from the
-// GLSL specification (OpenGL Shading Language 4.60, chapters 5 and 8):
+// oracle/glsl/make_ref.py compiles the reference's own GLSL (the BRDF,
+// light, intersection, traversal and path-tracer files) unmodified on the
+// host against this header, to produce golden vectors of the engine's
+// shading and traversal.  Written from the GLSL specification (OpenGL
+// Shading Language 4.60, chapters 5 and 8):
 //
-//  * vec2/3/4, ivec, uvec with the component names x y z w / r g b a, the
-//    two-component swizzles xy / rg (read, assign, *=), constructors from
-//    scalars and shorter vectors, component-wise arithmetic;
-//  * mat3 (column-major; mat3(c0, c1, c2), mat3 * vec3, vec3 * mat3);
-//  * the built-ins the helpers call, with the specification's definitions:
+//  * vec2/3/4, ivec2/3/4, uvec2/3/4 with the component names x y z w /
+//    r g b a and the swizzles the engine's files use (xy xz yz zw xyz rg rgb;
+//    read, assign, compound-assign), constructors from scalars and shorter
+//    vectors, component-wise arithmetic;
+//  * mat3, mat4 (column-major), mat3x4 (three vec4 columns, the engine's
+//    instance matrix) and mat4x3, with the products, transpose, the mat4
+//    constructor from a mat4x3 (the missing row taken from the identity) and
+//    inverse (by cofactors);
+//  * the built-ins, with the specification's definitions:
 //    min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x,
 //    clamp(x, a, b) = min(max(x, a), b), mix(x, y, a) = x * (1 - a) + y * a,
-//    dot as a left-to-right sum, normalize(x) = x / length(x).
+//    dot as a left-to-right sum, normalize(x) = x / length(x);
+//  * textures as arrays of RGBA float texels: texelFetch, textureSize, and
+//    textureLod with the engine's bindless sampler (linear filtering, repeat
+//    addressing) evaluated with exact weights; images and atomics as plain
+//    memory, for the one invocation the goldens run.
 //
 // All arithmetic is single precision (the recipe suffixes GLSL's float
 // literals with f) and is compiled with -ffp-contract=off, so every
@@ -27,126 +35,145 @@
 
 typedef unsigned int uint;
 
-inline float glsl_sqrt(float x) { return __builtin_sqrtf(x); }
+// ---- swizzles: N components of type T, read as V, written component-wise ----
+template <typename V, typename T, int N, int... I>
+struct Swz {
+    T v[N];
+    operator V() const { return V(v[I]...); }
+    Swz& operator=(const V& o) { int k = 0; ((v[I] = o.v[k++]), ...); return *this; }
+    Swz& operator*=(T s) { ((v[I] = v[I] * s), ...); return *this; }
+    Swz& operator/=(T s) { ((v[I] = v[I] / s), ...); return *this; }
+    Swz& operator*=(const V& o) { int k = 0; ((v[I] = v[I] * o.v[k++]), ...); return *this; }
+    Swz& operator+=(const V& o) { int k = 0; ((v[I] = v[I] + o.v[k++]), ...); return *this; }
+    Swz& operator-=(const V& o) { int k = 0; ((v[I] = v[I] - o.v[k++]), ...); return *this; }
+};
 
-template <int N, int A, int B>
-struct Swz2;
-
-struct vec2 {
-    union {
-        struct { float x, y; };
-        struct { float r, g; };
-        float v[2];
+#define GLSL_VEC2(V, T)                                                                   \
+    struct V {                                                                            \
+        union {                                                                           \
+            struct { T x, y; };                                                           \
+            struct { T r, g; };                                                           \
+            T v[2];                                                                       \
+        };                                                                                \
+        V() : x(0), y(0) {}                                                               \
+        explicit V(T s) : x(s), y(s) {}                                                   \
+        V(T a, T b) : x(a), y(b) {}                                                       \
+        template <typename U> explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])) {}      \
+        T& operator[](int i) { return v[i]; }                                             \
+        T operator[](int i) const { return v[i]; }                                        \
     };
-    vec2() : x(0.0f), y(0.0f) {}
-    explicit vec2(float s) : x(s), y(s) {}
-    vec2(float a, float b) : x(a), y(b) {}
-    float& operator[](int i) { return v[i]; }
-    float operator[](int i) const { return v[i]; }
-};
-
-// Two components of a vecN, read as a vec2 and assigned or scaled in place.
-template <int N, int A, int B>
-struct Swz2 {
-    float v[N];
-    operator vec2() const { return vec2(v[A], v[B]); }
-    Swz2& operator=(const vec2& o) { v[A] = o.x; v[B] = o.y; return *this; }
-    Swz2& operator*=(float s) { v[A] = v[A] * s; v[B] = v[B] * s; return *this; }
-    Swz2& operator*=(const vec2& o) { v[A] = v[A] * o.x; v[B] = v[B] * o.y; return *this; }
-};
-
-struct vec3 {
-    union {
-        struct { float x, y, z; };
-        struct { float r, g, b; };
-        Swz2<3, 0, 1> xy;
-        Swz2<3, 0, 1> rg;
-        float v[3];
+#define GLSL_VEC3(V, T, V2)                                                               \
+    struct V {                                                                            \
+        union {                                                                           \
+            struct { T x, y, z; };                                                        \
+            struct { T r, g, b; };                                                        \
+            Swz<V2, T, 3, 0, 1> xy;                                                       \
+            Swz<V2, T, 3, 0, 1> rg;                                                       \
+            Swz<V2, T, 3, 0, 2> xz;                                                       \
+            Swz<V2, T, 3, 1, 2> yz;                                                       \
+            Swz<V, T, 3, 0, 1, 2> xyz;                                                    \
+            Swz<V, T, 3, 0, 1, 2> rgb;                                                    \
+            T v[3];                                                                       \
+        };                                                                                \
+        V() : x(0), y(0), z(0) {}                                                         \
+        explicit V(T s) : x(s), y(s), z(s) {}                                             \
+        V(T a, T b, T c) : x(a), y(b), z(c) {}                                            \
+        V(const V2& a, T c) : x(a.x), y(a.y), z(c) {}                                     \
+        V(const V& o) : x(o.x), y(o.y), z(o.z) {}                                         \
+        template <typename U> explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])), z(T(o.v[2])) {} \
+        V& operator=(const V& o) { x = o.x; y = o.y; z = o.z; return *this; }            \
+        T& operator[](int i) { return v[i]; }                                             \
+        T operator[](int i) const { return v[i]; }                                        \
     };
-    vec3() : x(0.0f), y(0.0f), z(0.0f) {}
-    explicit vec3(float s) : x(s), y(s), z(s) {}
-    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
-    vec3(const vec2& a, float c) : x(a.x), y(a.y), z(c) {}
-    vec3(const vec3& o) : x(o.x), y(o.y), z(o.z) {}
-    explicit vec3(const struct vec4& o);
-    vec3& operator=(const vec3& o) { x = o.x; y = o.y; z = o.z; return *this; }
-    float& operator[](int i) { return v[i]; }
-    float operator[](int i) const { return v[i]; }
-};
-
-struct vec4 {
-    union {
-        struct { float x, y, z, w; };
-        struct { float r, g, b, a; };
-        Swz2<4, 0, 1> xy;
-        Swz2<4, 0, 1> rg;
-        float v[4];
+#define GLSL_VEC4(V, T, V2, V3)                                                           \
+    struct V {                                                                            \
+        union {                                                                           \
+            struct { T x, y, z, w; };                                                     \
+            struct { T r, g, b, a; };                                                     \
+            Swz<V2, T, 4, 0, 1> xy;                                                       \
+            Swz<V2, T, 4, 0, 1> rg;                                                       \
+            Swz<V2, T, 4, 2, 3> zw;                                                       \
+            Swz<V3, T, 4, 0, 1, 2> xyz;                                                   \
+            Swz<V3, T, 4, 0, 1, 2> rgb;                                                   \
+            T v[4];                                                                       \
+        };                                                                                \
+        V() : x(0), y(0), z(0), w(0) {}                                                   \
+        explicit V(T s) : x(s), y(s), z(s), w(s) {}                                       \
+        V(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}                                 \
+        template <typename A, typename B, typename C, typename D>                         \
+        V(A a, B b, C c, D d) : x(T(a)), y(T(b)), z(T(c)), w(T(d)) {}                     \
+        V(const V3& a, T d) : x(a.x), y(a.y), z(a.z), w(d) {}                             \
+        V(const V2& a, T c, T d) : x(a.x), y(a.y), z(c), w(d) {}                          \
+        V(const V2& a, const V2& b) : x(a.x), y(a.y), z(b.x), w(b.y) {}                   \
+        V(const V& o) : x(o.x), y(o.y), z(o.z), w(o.w) {}                                 \
+        V& operator=(const V& o) { x = o.x; y = o.y; z = o.z; w = o.w; return *this; }   \
+        T& operator[](int i) { return v[i]; }                                             \
+        T operator[](int i) const { return v[i]; }                                        \
     };
-    vec4() : x(0.0f), y(0.0f), z(0.0f), w(0.0f) {}
-    explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
-    vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
-    vec4(const vec3& a, float d) : x(a.x), y(a.y), z(a.z), w(d) {}
-    vec4(const vec2& a, float c, float d) : x(a.x), y(a.y), z(c), w(d) {}
-    vec4(const vec4& o) : x(o.x), y(o.y), z(o.z), w(o.w) {}
-    vec4& operator=(const vec4& o) { x = o.x; y = o.y; z = o.z; w = o.w; return *this; }
-    float& operator[](int i) { return v[i]; }
-    float operator[](int i) const { return v[i]; }
-};
-inline vec3::vec3(const vec4& o) : x(o.x), y(o.y), z(o.z) {}
 
-#define GLSL_VEC_OPS(T, N)                                                                          \
-    inline T operator+(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] + b.v[i]; return r; } \
-    inline T operator-(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] - b.v[i]; return r; } \
-    inline T operator*(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] * b.v[i]; return r; } \
-    inline T operator/(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] / b.v[i]; return r; } \
-    inline T operator*(const T& a, float s) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] * s; return r; }      \
-    inline T operator*(float s, const T& a) { T r; for (int i = 0; i < N; i++) r.v[i] = s * a.v[i]; return r; }      \
-    inline T operator/(const T& a, float s) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] / s; return r; }      \
-    inline T operator+(const T& a, float s) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] + s; return r; }      \
-    inline T operator-(const T& a, float s) { T r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] - s; return r; }      \
-    inline T operator-(float s, const T& a) { T r; for (int i = 0; i < N; i++) r.v[i] = s - a.v[i]; return r; }      \
-    inline T operator-(const T& a) { T r; for (int i = 0; i < N; i++) r.v[i] = -a.v[i]; return r; }                \
-    inline T& operator+=(T& a, const T& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] + b.v[i]; return a; }      \
-    inline T& operator-=(T& a, const T& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] - b.v[i]; return a; }      \
-    inline T& operator*=(T& a, const T& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] * b.v[i]; return a; }      \
-    inline T& operator*=(T& a, float s) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] * s; return a; }              \
-    inline T& operator/=(T& a, float s) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] / s; return a; }
-GLSL_VEC_OPS(vec2, 2)
-GLSL_VEC_OPS(vec3, 3)
-GLSL_VEC_OPS(vec4, 4)
+GLSL_VEC2(vec2, float)
+GLSL_VEC3(vec3, float, vec2)
+GLSL_VEC4(vec4, float, vec2, vec3)
+GLSL_VEC2(ivec2, int)
+GLSL_VEC3(ivec3, int, ivec2)
+GLSL_VEC4(ivec4, int, ivec2, ivec3)
+GLSL_VEC2(uvec2, uint)
+GLSL_VEC3(uvec3, uint, uvec2)
+GLSL_VEC4(uvec4, uint, uvec2, uvec3)
 
-// Integer vectors (the hash functions of common/random.hsh take uvec).
-struct uvec2 { uint x, y; uvec2(uint a, uint b) : x(a), y(b) {} };
-struct uvec3 { uint x, y, z; uvec3(uint a, uint b, uint c) : x(a), y(b), z(c) {} };
-struct uvec4 { uint x, y, z, w; uvec4(uint a, uint b, uint c, uint d) : x(a), y(b), z(c), w(d) {} };
-struct ivec2 { int x, y; };
-struct ivec3 { int x, y, z; };
-struct ivec4 { int x, y, z, w; };
-
-// mat3: three columns.
-struct mat3 {
-    vec3 c[3];
-    mat3(const vec3& a, const vec3& b, const vec3& d) { c[0] = a; c[1] = b; c[2] = d; }
-};
-inline vec3 operator*(const mat3& m, const vec3& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
-struct mat4 { vec4 c[4]; };
-struct mat3x4 { vec4 c[3]; };
+#define GLSL_VEC_OPS(V, T, N)                                                                              \
+    inline V operator+(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] + b.v[i]; return r; } \
+    inline V operator-(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] - b.v[i]; return r; } \
+    inline V operator*(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] * b.v[i]; return r; } \
+    inline V operator/(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] / b.v[i]; return r; } \
+    inline V operator*(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] * s; return r; }      \
+    inline V operator*(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s * a.v[i]; return r; }      \
+    inline V operator/(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] / s; return r; }      \
+    inline V operator+(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] + s; return r; }      \
+    inline V operator+(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s + a.v[i]; return r; }      \
+    inline V operator-(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] - s; return r; }      \
+    inline V operator-(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s - a.v[i]; return r; }      \
+    inline V operator-(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = -a.v[i]; return r; }                \
+    inline V& operator+=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] + b.v[i]; return a; }      \
+    inline V& operator-=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] - b.v[i]; return a; }      \
+    inline V& operator*=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] * b.v[i]; return a; }      \
+    inline V& operator/=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] / b.v[i]; return a; }      \
+    inline V& operator*=(V& a, T s) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] * s; return a; }              \
+    inline V& operator/=(V& a, T s) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] / s; return a; }              \
+    inline V& operator+=(V& a, T s) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] + s; return a; }
+GLSL_VEC_OPS(vec2, float, 2)
+GLSL_VEC_OPS(vec3, float, 3)
+GLSL_VEC_OPS(vec4, float, 4)
+GLSL_VEC_OPS(ivec2, int, 2)
+GLSL_VEC_OPS(ivec3, int, 3)
+GLSL_VEC_OPS(ivec4, int, 4)
+GLSL_VEC_OPS(uvec2, uint, 2)
+GLSL_VEC_OPS(uvec3, uint, 3)
+GLSL_VEC_OPS(uvec4, uint, 4)
+inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
+inline ivec2 operator%(const ivec2& a, int b) { return ivec2(a.x % b, a.y % b); }
 
 // ---- scalar built-ins (GLSL 4.60 section 8) ----
 inline float min(float x, float y) { return (y < x) ? y : x; }
 inline float max(float x, float y) { return (x < y) ? y : x; }
 inline int min(int x, int y) { return (y < x) ? y : x; }
 inline int max(int x, int y) { return (x < y) ? y : x; }
+inline uint min(uint x, uint y) { return (y < x) ? y : x; }
+inline uint max(uint x, uint y) { return (x < y) ? y : x; }
 inline float clamp(float x, float lo, float hi) { return min(max(x, lo), hi); }
+inline int clamp(int x, int lo, int hi) { return min(max(x, lo), hi); }
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 inline float abs(float x) { return __builtin_fabsf(x); }
+inline int abs(int x) { return x < 0 ? -x : x; }
 inline float sqrt(float x) { return __builtin_sqrtf(x); }
 inline float pow(float x, float y) { return __builtin_powf(x, y); }
+inline float exp(float x) { return __builtin_expf(x); }
 inline float sin(float x) { return __builtin_sinf(x); }
 inline float cos(float x) { return __builtin_cosf(x); }
 inline float atan(float y, float x) { return __builtin_atan2f(y, x); }
 inline float atan(float x) { return __builtin_atanf(x); }
 inline float floor(float x) { return __builtin_floorf(x); }
+inline float fract(float x) { return x - __builtin_floorf(x); }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 inline bool isnan(float x) { return __builtin_isnan(x); }
 inline bool isinf(float x) { return __builtin_isinf(x); }
@@ -163,28 +190,124 @@ inline uvec4 floatBitsToUint(const vec4& v) {
 }
 
 // ---- vector built-ins ----
-#define GLSL_VEC_FUNCS(T, N)                                                                                \
-    inline T min(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = min(a.v[i], b.v[i]); return r; } \
-    inline T max(const T& a, const T& b) { T r; for (int i = 0; i < N; i++) r.v[i] = max(a.v[i], b.v[i]); return r; } \
-    inline T clamp(const T& x, const T& a, const T& b) { return min(max(x, a), b); }                          \
-    inline T clamp(const T& x, float a, float b) { return min(max(x, T(a)), T(b)); }                          \
-    inline T mix(const T& x, const T& y, float a) { return x * (1.0f - a) + y * a; }                          \
-    inline T abs(const T& a) { T r; for (int i = 0; i < N; i++) r.v[i] = abs(a.v[i]); return r; }            \
-    inline T sqrt(const T& a) { T r; for (int i = 0; i < N; i++) r.v[i] = sqrt(a.v[i]); return r; }          \
-    inline float dot(const T& a, const T& b) { float s = a.v[0] * b.v[0]; for (int i = 1; i < N; i++) s = s + a.v[i] * b.v[i]; return s; } \
-    inline float length(const T& a) { return sqrt(dot(a, a)); }                                                \
-    inline T normalize(const T& a) { return a / length(a); }
+#define GLSL_VEC_FUNCS(V, N)                                                                                \
+    inline V min(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = min(a.v[i], b.v[i]); return r; } \
+    inline V max(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = max(a.v[i], b.v[i]); return r; } \
+    inline V clamp(const V& x, const V& a, const V& b) { return min(max(x, a), b); }                          \
+    inline V abs(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = abs(a.v[i]); return r; }
 GLSL_VEC_FUNCS(vec2, 2)
 GLSL_VEC_FUNCS(vec3, 3)
 GLSL_VEC_FUNCS(vec4, 4)
+GLSL_VEC_FUNCS(ivec2, 2)
+GLSL_VEC_FUNCS(ivec3, 3)
+#define GLSL_FVEC_FUNCS(V, N)                                                                               \
+    inline V clamp(const V& x, float a, float b) { return min(max(x, V(a)), V(b)); }                          \
+    inline V mix(const V& x, const V& y, float a) { return x * (1.0f - a) + y * a; }                          \
+    inline V mix(const V& x, const V& y, const V& a) { return x * (1.0f - a) + y * a; }                       \
+    inline V sqrt(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = sqrt(a.v[i]); return r; }          \
+    inline V floor(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = floor(a.v[i]); return r; }        \
+    inline V fract(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = fract(a.v[i]); return r; }        \
+    inline V pow(const V& a, const V& b) { V r; for (int i = 0; i < N; i++) r.v[i] = pow(a.v[i], b.v[i]); return r; } \
+    inline V exp(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = exp(a.v[i]); return r; }            \
+    inline float dot(const V& a, const V& b) { float s = a.v[0] * b.v[0]; for (int i = 1; i < N; i++) s = s + a.v[i] * b.v[i]; return s; } \
+    inline float length(const V& a) { return sqrt(dot(a, a)); }                                                \
+    inline float distance(const V& a, const V& b) { return length(a - b); }                                    \
+    inline V normalize(const V& a) { return a / length(a); }
+GLSL_FVEC_FUNCS(vec2, 2)
+GLSL_FVEC_FUNCS(vec3, 3)
+GLSL_FVEC_FUNCS(vec4, 4)
 
 inline vec3 cross(const vec3& a, const vec3& b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
-// row vector times matrix: the dot products with the columns
-inline vec3 operator*(const vec3& v, const mat3& m) { return vec3(dot(v, m.c[0]), dot(v, m.c[1]), dot(v, m.c[2])); }
 
-// half2 packing (GLSL 4.60 section 8.4), the IEEE binary16 conversions
+// ---- matrices (column-major) ----
+struct mat3 {
+    vec3 c[3];
+    mat3() {}
+    mat3(const vec3& a, const vec3& b, const vec3& d) { c[0] = a; c[1] = b; c[2] = d; }
+    vec3& operator[](int i) { return c[i]; }
+    const vec3& operator[](int i) const { return c[i]; }
+};
+struct mat4x3 { vec3 c[4]; };                  // four columns of three rows
+struct mat3x4 {                                // three columns of four rows
+    vec4 c[3];
+    vec4& operator[](int i) { return c[i]; }
+    const vec4& operator[](int i) const { return c[i]; }
+};
+struct mat4 {
+    vec4 c[4];
+    mat4() {}
+    explicit mat4(float s) { for (int i = 0; i < 4; i++) c[i] = vec4(0.0f); for (int i = 0; i < 4; i++) c[i].v[i] = s; }
+    mat4(const vec4& a, const vec4& b, const vec4& d, const vec4& e) { c[0] = a; c[1] = b; c[2] = d; c[3] = e; }
+    // from a mat4x3: the fourth row taken from the identity
+    explicit mat4(const mat4x3& m) { for (int i = 0; i < 4; i++) c[i] = vec4(m.c[i], i == 3 ? 1.0f : 0.0f); }
+    vec4& operator[](int i) { return c[i]; }
+    const vec4& operator[](int i) const { return c[i]; }
+};
+inline vec3 operator*(const mat3& m, const vec3& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+inline vec3 operator*(const vec3& v, const mat3& m) { return vec3(dot(v, m.c[0]), dot(v, m.c[1]), dot(v, m.c[2])); }
+inline vec4 operator*(const mat4& m, const vec4& v) {
+    return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z + m.c[3] * v.w;
+}
+// row vector times a 3-column matrix: the dot products with its columns
+inline vec3 operator*(const vec4& v, const mat3x4& m) { return vec3(dot(v, m.c[0]), dot(v, m.c[1]), dot(v, m.c[2])); }
+inline mat4x3 transpose(const mat3x4& m) {
+    mat4x3 r;
+    for (int i = 0; i < 4; i++) r.c[i] = vec3(m.c[0].v[i], m.c[1].v[i], m.c[2].v[i]);
+    return r;
+}
+inline mat4 transpose(const mat4& m) {
+    mat4 r;
+    for (int i = 0; i < 4; i++) r.c[i] = vec4(m.c[0].v[i], m.c[1].v[i], m.c[2].v[i], m.c[3].v[i]);
+    return r;
+}
+// The inverse by cofactors (adjugate over the determinant), in single
+// precision; the specification leaves the method to the implementation.
+inline mat4 inverse(const mat4& m) {
+    float a[16], inv[16];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) a[i * 4 + j] = m.c[i].v[j];
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] +
+             a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] -
+             a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] +
+             a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] -
+              a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] -
+             a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] +
+             a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] -
+             a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] +
+              a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] +
+             a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] -
+             a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] +
+              a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] -
+              a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] -
+             a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] +
+             a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] -
+              a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] +
+              a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    const float det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    mat4 r;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) r.c[i].v[j] = inv[i * 4 + j] / det;
+    return r;
+}
+
+// ---- packing (GLSL 4.60 section 8.4) ----
 inline vec2 unpackHalf2x16(uint u) {
     auto h2f = [](uint h) {
         const uint s = (h >> 15) & 1u, e = (h >> 10) & 31u, m = h & 1023u;
@@ -196,9 +319,95 @@ inline vec2 unpackHalf2x16(uint u) {
     };
     return vec2(h2f(u & 0xffffu), h2f(u >> 16));
 }
+// binary32 -> binary16, rounded to nearest even (the conversion rounds
+// half-way cases to even, as IEEE 754 does)
+inline uint glsl_float_to_half(float f) {
+    const uint u = floatBitsToUint(f);
+    const uint s = (u >> 16) & 0x8000u;
+    const uint e = (u >> 23) & 0xffu;
+    uint m = u & 0x7fffffu;
+    if (e == 0xffu) return s | 0x7c00u | (m ? 0x200u : 0u);
+    int he = int(e) - 127 + 15;
+    if (he >= 31) return s | 0x7c00u;
+    if (he <= 0) {
+        if (he < -10) return s;
+        m |= 0x800000u;
+        const uint shift = uint(14 - he);
+        uint h = m >> shift;
+        const uint rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1u))) h++;
+        return s | h;
+    }
+    uint h = (uint(he) << 10) | (m >> 13);
+    const uint rem = m & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return s | h;
+}
+inline uint packHalf2x16(const vec2& v) { return glsl_float_to_half(v.x) | (glsl_float_to_half(v.y) << 16); }
+inline vec4 unpackUnorm4x8(uint u) {
+    return vec4(float(u & 255u) / 255.0f, float((u >> 8) & 255u) / 255.0f, float((u >> 16) & 255u) / 255.0f,
+                float(u >> 24) / 255.0f);
+}
 
-// Resource access the helpers mention but the goldens never evaluate
-// (EvaluateIndirect*BRDF reads the DFG lookup texture).
-struct glsl_sampler2D {};
-inline vec4 texture(const glsl_sampler2D&, const vec2&) { return vec4(0.0f); }
+// ---- textures: RGBA float texels, row-major, one level per texture ----
+struct glsl_texture2D {
+    const float* texels = nullptr;   // width * height * 4
+    int width = 0, height = 0;
+};
+struct glsl_sampler {};
+struct glsl_sampler2D {
+    const glsl_texture2D* tex = nullptr;
+    glsl_sampler2D() {}
+    glsl_sampler2D(const glsl_texture2D& t, const glsl_sampler&) : tex(&t) {}
+};
+typedef glsl_texture2D texture2D;
+typedef glsl_sampler sampler;
+typedef glsl_sampler2D sampler2D;
+struct sampler2DArray { int width = 0, height = 0, layers = 0; };
+struct samplerCube {};
+inline ivec2 textureSize(const sampler2D& s, int) { return s.tex ? ivec2(s.tex->width, s.tex->height) : ivec2(0); }
+inline ivec3 textureSize(const sampler2DArray& s, int) { return ivec3(s.width, s.height, s.layers); }
+inline vec4 texelFetch(const sampler2D& s, const ivec2& p, int) {
+    const float* t = s.tex->texels + (size_t(p.y) * s.tex->width + p.x) * 4;
+    return vec4(t[0], t[1], t[2], t[3]);
+}
+inline vec4 texelFetch(const sampler2DArray&, const ivec3&, int) { return vec4(0.0f); }
+// The bindless sampler of the engine (linear filtering, repeat addressing,
+// MainRenderer.cpp:922-929) at one level: the specification's bilinear
+// filter (OpenGL 4.6 section 8.14.2) with exact weights.
+inline vec4 textureLod(const sampler2D& s, const vec2& uv, float) {
+    const int w = s.tex->width, h = s.tex->height;
+    const float x = uv.x * float(w) - 0.5f, y = uv.y * float(h) - 0.5f;
+    const float fx = floor(x), fy = floor(y);
+    const float ax = x - fx, ay = y - fy;
+    auto wrap = [](int i, int n) { int m = i % n; return m < 0 ? m + n : m; };
+    const int x0 = wrap(int(fx), w), x1 = wrap(int(fx) + 1, w), y0 = wrap(int(fy), h), y1 = wrap(int(fy) + 1, h);
+    const vec4 t00 = texelFetch(s, ivec2(x0, y0), 0), t10 = texelFetch(s, ivec2(x1, y0), 0);
+    const vec4 t01 = texelFetch(s, ivec2(x0, y1), 0), t11 = texelFetch(s, ivec2(x1, y1), 0);
+    return t00 * ((1.0f - ax) * (1.0f - ay)) + t10 * (ax * (1.0f - ay)) + t01 * ((1.0f - ax) * ay) + t11 * (ax * ay);
+}
+inline vec4 textureLod(const samplerCube&, const vec3&, float) { return vec4(0.0f); }
+inline vec4 texture(const sampler2D& s, const vec2& uv) { return s.tex ? textureLod(s, uv, 0.0f) : vec4(0.0f); }
+
+// ---- images, atomics and invocation ids, for one invocation ----
+struct image2D { vec4* texels = nullptr; int width = 0; };
+struct uimage2D { uvec4* texels = nullptr; int width = 0; };
+struct uimage2DArray { uint* texels = nullptr; int width = 0, height = 0; };
+inline void imageStore(image2D& im, const ivec2& p, const vec4& v) { if (im.texels) im.texels[p.y * im.width + p.x] = v; }
+inline vec4 imageLoad(const image2D& im, const ivec2& p) { return im.texels ? im.texels[p.y * im.width + p.x] : vec4(0.0f); }
+inline void imageStore(uimage2D& im, const ivec2& p, const uvec4& v) { if (im.texels) im.texels[p.y * im.width + p.x] = v; }
+inline void imageStore(uimage2DArray& im, const ivec3& p, const uvec4& v) {
+    if (im.texels) im.texels[(size_t(p.z) * im.height + p.y) * im.width + p.x] = v.x;
+}
+inline uint imageAtomicAdd(uimage2DArray& im, const ivec3& p, uint v) {
+    if (!im.texels) return 0u;
+    uint& t = im.texels[(size_t(p.z) * im.height + p.y) * im.width + p.x];
+    const uint old = t;
+    t += v;
+    return old;
+}
+inline uint atomicAdd(uint& mem, uint v) { const uint old = mem; mem += v; return old; }
+inline int atomicAdd(int& mem, int v) { const int old = mem; mem += v; return old; }
+static uvec3 gl_GlobalInvocationID;
+static uint gl_LocalInvocationIndex = 0;
 #define nonuniformEXT(x) (x)

@@ -10,8 +10,13 @@
 //   SampleTriangleLight                      raytracer/lights.hsh:11-29
 //   IntersectAABB / IntersectTriangle        raytracer/intersections.hsh:18-57
 //   random(x, inout seed)                    common/random.hsh:5-54
+//   HitClosest / HitAny / HitClosestTransparency / HitAnyTransparency over a
+//   two-level scene (TLAS, instances, per-mesh BLAS, materials, opacity
+//   textures)                                raytracer/bvh.hsh:44-524
 #include "glsl.hpp"
 #include "glsl_ref.inc"
+
+#include <vector>
 
 namespace {
 
@@ -117,6 +122,63 @@ void aeglsl_intersect_aabb(const float* in, int n, float* out) {
         const bool hit = IntersectAABB(ray, box, r[12], r[13], dist);
         out[i * 2] = hit ? 1.0f : 0.0f;
         out[i * 2 + 1] = dist;
+    }
+}
+
+// The scene the traversals read, in the engine's GPU layouts (64-byte
+// nodes and instances, 48-byte BVH triangles, 96-byte triangles, 92-byte
+// materials), and its opacity textures as RGBA float texels (width, height
+// per texture in wh).  The arrays stay owned by the caller.
+static std::vector<glsl_texture2D> g_textures;
+
+void aeglsl_scene(const void* tlas, const void* instances, int n_meshes, const void* const* nodes,
+                  const void* const* bvh_tris, const void* const* tris, const void* mats, int n_textures,
+                  const float* const* texels, const int* wh) {
+    tlasNodes = (PackedBVHNode*)tlas;
+    bvhInstances = (Instance*)instances;
+    for (int m = 0; m < n_meshes; m++) {
+        blasNodes[m].data = (PackedBVHNode*)nodes[m];
+        bvhTriangles[m].data = (PackedBVHTriangle*)bvh_tris[m];
+        triangles[m].data = (PackedTriangle*)tris[m];
+    }
+    materials = (RaytraceMaterial*)mats;
+    g_textures.assign(size_t(n_textures), glsl_texture2D());
+    for (int i = 0; i < n_textures; i++) {
+        g_textures[i].texels = texels[i];
+        g_textures[i].width = wh[2 * i];
+        g_textures[i].height = wh[2 * i + 1];
+    }
+    bindlessTextures = g_textures.data();
+}
+
+// kind 0 HitClosest, 1 HitAny, 2 HitClosestTransparency, 3 HitAnyTransparency
+// over rows origin(3) direction(3) tmin tmax; out per row (4): hitID and
+// hitInstanceID (int bits), hitDistance, and HitAny's result (0 / 1) or
+// HitAnyTransparency's transparency.  A ray starts with hitID and
+// hitInstanceID -1, as the engine's ray queue writes them (tracing.hsh).
+void aeglsl_scene_trace(int kind, const float* rays, int n, uint cull, float* out) {
+    for (int i = 0; i < n; i++) {
+        const float* r = rays + i * 8;
+        Ray ray;
+        ray.ID = i;
+        ray.origin = V3(r);
+        ray.direction = V3(r + 3);
+        ray.hitID = -1;
+        ray.hitInstanceID = -1;
+        ray.currentInstanceID = -1;
+        ray.hitDistance = 0.0f;
+        float value = 0.0f;
+        switch (kind) {
+        case 0: HitClosest(ray, cull, r[6], r[7]); break;
+        case 1: value = HitAny(ray, cull, r[6], r[7]) ? 1.0f : 0.0f; break;
+        case 2: HitClosestTransparency(ray, cull, r[6], r[7]); break;
+        default: value = HitAnyTransparency(ray, cull, r[6], r[7]); break;
+        }
+        float* o = out + i * 4;
+        o[0] = intBitsToFloat(ray.hitID);
+        o[1] = intBitsToFloat(ray.hitInstanceID);
+        o[2] = ray.hitDistance;
+        o[3] = value;
     }
 }
 

@@ -1,10 +1,11 @@
 """Builds oracle/_ref/libglslref.so from the reference's own GLSL helpers --
 TEST INFRASTRUCTURE ONLY (the recipe; run by tests/golden/gen_glsl_goldens.py).
 
-The engine's shading math lives in GLSL include files that need no graphics
-API: data/shader/brdf/{brdf,brdfEval,brdfSample,surface}.hsh,
-raytracer/{lights,intersections,structures}.hsh, common/{random,utility,PI,
-material,packing}.hsh.  This recipe reads them where they lie in the
+The engine's shading math and its software scene traversal live in GLSL
+include files that need no graphics API: data/shader/brdf/{brdf,brdfEval,
+brdfSample,surface}.hsh, raytracer/{lights,intersections,structures,bvh,
+direct,buffers,texture}.hsh, common/{random,utility,PI,material,packing}.hsh.
+This recipe reads them where they lie in the
 reference tree (unchanged on disk), flattens their `#include <...>` lines the
 way the engine's shader loader does (relative to the including file, each
 file once), and makes the GLSL parse as C++ with the vector types of
@@ -17,10 +18,13 @@ language-level adjustments are applied:
   * float literals get an `f` suffix (a GLSL float literal is single
     precision, a C++ one double);
   * resource declarations (`layout(...)`, storage `buffer` blocks, `uniform`
-    blocks) become plain globals: a buffer block's runtime-sized arrays become
-    pointers, which the goldens never read;
+    blocks and variables, `shared` arrays) become plain globals: a buffer
+    block's runtime-sized arrays become pointers, an array of buffer blocks
+    (one per mesh under bindless resources) a table of such pointers, which
+    glsl_capi.cpp points at the caller's scene;
   * the engine's globals.hsh (uniform blocks and bindless textures) is
-    replaced by the one resource the helpers name, the DFG lookup texture.
+    replaced by the resources the helpers name: the DFG lookup texture and
+    the bindless texture table with its sampler.
 
 The flattened source goes to oracle/_ref/glsl_ref.inc and is compiled with
 oracle/glsl/glsl_capi.cpp (-O2 -ffp-contract=off) into
@@ -36,15 +40,26 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
 OUT_DIR = ORACLE / "_ref"
-ENTRY_FILES = ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh"]
-GLOBALS_STUB = "static glsl_sampler2D dfgTexture;\n"
+ENTRY_FILES = ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh", "raytracer/bvh.hsh",
+               "raytracer/direct.hsh"]
+# The engine compiles its shaders with bindless resources (AE_BINDLESS: one
+# buffer per mesh) and, where registers allow, the traversal stack in local
+# memory (LOCAL_STACK, bvh.hsh:39-42); compute shaders see one invocation.
+PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
+GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
+                "static glsl_texture2D* bindlessTextures = nullptr;\n"
+                "static glsl_sampler bindlessSampler;\n")
 
 _INCLUDE = re.compile(r'^\s*#include\s*<([^>]+)>\s*$')
 _FLOAT = re.compile(r'(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])')
 _QUAL = re.compile(r'\b(inout|out|in)\s+([A-Za-z_]\w*)\s+([A-Za-z_]\w*)')
 _LAYOUT = re.compile(r'\blayout\s*\([^)]*\)\s*')
 _BUFFER = re.compile(r'\bbuffer\s+\w+\s*\{([^}]*)\}\s*;', re.S)
+_BUFFER_ARRAY = re.compile(r'\bbuffer\s+(\w+)\s*\{([^}]*)\}\s*(\w+)\s*\[([^\]]*)\]\s*;', re.S)
 _UNIFORM_BLOCK = re.compile(r'\buniform\s+(\w+)\s*\{')
+_UNIFORM_VAR = re.compile(r'^(\s*)(?:readonly\s+|writeonly\s+)*uniform\s+(\w+\s+\w+(?:\s*\[[^\]]*\])?\s*;)', re.M)
+_SHARED = re.compile(r'^(\s*)shared\s+', re.M)
+_LAYOUT_IN = re.compile(r'^\s*in\s*;\s*$', re.M)
 
 
 def _flatten(path: Path, seen: set, shader_root: Path) -> str:
@@ -77,13 +92,28 @@ def _buffer_to_globals(m: re.Match) -> str:
     return "\n".join(decls)
 
 
+def _buffer_array(m: re.Match) -> str:
+    # one block per mesh (bindless): a table of per-mesh pointers
+    fields = []
+    for d in m.group(2).split(";"):
+        d = d.strip()
+        if d:
+            arr = re.match(r'(\w+)\s+(\w+)\s*\[\s*\]$', d)
+            fields.append(f"{arr.group(1)}* {arr.group(2)} = nullptr;" if arr else f"{d};")
+    return f"struct {m.group(1)} {{ {' '.join(fields)} }};\nstatic {m.group(1)} {m.group(3)}[{m.group(4)}];"
+
+
 def to_cpp(src: str) -> str:
     def qual(m):
         return f"{m.group(2)}& {m.group(3)}" if m.group(1) in ("inout", "out") else f"{m.group(2)} {m.group(3)}"
     src = _QUAL.sub(qual, src)
     src = _LAYOUT.sub("", src)
+    src = _LAYOUT_IN.sub("", src)
+    src = _BUFFER_ARRAY.sub(_buffer_array, src)
     src = _BUFFER.sub(_buffer_to_globals, src)
     src = _UNIFORM_BLOCK.sub(lambda m: f"struct {m.group(1)} {{", src)
+    src = _UNIFORM_VAR.sub(lambda m: f"{m.group(1)}static {m.group(2)}", src)
+    src = _SHARED.sub(lambda m: f"{m.group(1)}static ", src)
     src = _FLOAT.sub(lambda m: m.group(1) + "f", src)
     return src
 
@@ -95,7 +125,7 @@ def build(reference_root: Path) -> Path:
     OUT_DIR.mkdir(exist_ok=True)
     inc = OUT_DIR / "glsl_ref.inc"
     header = "// generated by oracle/glsl/make_ref.py from the reference's shader files; do not edit\n"
-    inc.write_text(header + to_cpp(body))
+    inc.write_text(header + PREAMBLE + to_cpp(body))
     lib = OUT_DIR / "libglslref.so"
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fno-builtin",
            "-w", f"-I{HERE}", f"-I{OUT_DIR}", str(HERE / "glsl_capi.cpp"), "-o", str(lib)]

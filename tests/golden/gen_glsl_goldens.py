@@ -1,7 +1,10 @@
 """Writes tests/golden/glsl_shading.npz: golden vectors of the engine's shading
-math, produced by the reference's own GLSL (data/shader/brdf/*.hsh,
-raytracer/lights.hsh, raytracer/intersections.hsh, common/random.hsh)
-compiled on the host by the recipe oracle/glsl/make_ref.py.
+math and scene traversal, produced by the reference's own GLSL
+(data/shader/brdf/*.hsh, raytracer/lights.hsh, raytracer/intersections.hsh,
+raytracer/bvh.hsh, common/random.hsh) compiled on the host by the recipe
+oracle/glsl/make_ref.py.  The traversal goldens (trav_*) are traced over
+traversal_scene(), a seeded scene in the engine's buffer layouts, whose
+digest the fixture keeps so that the tests can rebuild the same scene.
 
 Needs the reference tree (this container); the fixture it writes is what the
 tests compare the oracle's restatement and the GPU's device functions with.
@@ -89,6 +92,136 @@ def inputs(seed=20261204, n=512):
             "random_x": xs}
 
 
+def _rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def traversal_scene(seed=20261205, n_inst=12, n_rays=4096):
+    """A seeded two-level scene in the engine's layouts: three meshes (random
+    triangles, a terrain patch with boxes, a box) with per-triangle opacities
+    (opaque, clear, partial, or the material's through a negative value),
+    twelve instances with rotations, scales, translations, the three cull
+    masks and material offsets, twelve materials of random opacity (some
+    with an opacity texture, some with inverted UVs), three opacity textures
+    (R8, RGBA8, R32F), and rays aimed into it.
+    Built with the library's BVH builder (byte-identical to the reference's)
+    and packers; deterministic, so the tests rebuild it."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    import atlas_rt
+    from atlas_rt import BVH, MATERIAL_DTYPE, scenes
+    rng = np.random.default_rng(seed)
+    srcs = [scenes.random_triangles(600, seed=seed + 1),
+            scenes.terrain_boxes(seed=seed + 2, grid=10, extent=4.0, n_boxes=2)[0],
+            scenes._box_triangles(np.array([-0.5, -0.5, -0.5], F32), np.array([0.5, 0.5, 0.5], F32))]
+    meshes, bvhs = [], []
+    for t in srcs:
+        b = BVH(t)
+        n = len(t)
+        op = rng.uniform(0.0, 1.0, n).astype(F32)
+        kind = rng.integers(0, 4, n)
+        op[kind == 0] = -1.0                  # the material's opacity (and texture)
+        op[kind == 1] = 0.0                   # clear
+        op[kind == 2] = 1.0                   # opaque
+        mat = rng.integers(0, 4, n).astype(np.int32)
+        gt = b.pack_triangles(mat, op)
+        sh = b.pack_shading(None, mat, op)
+        b.pack_uvs(sh, rng.uniform(-1.5, 2.5, (n, 6)).astype(F32))
+        meshes.append((b.nodes_f32.copy(), gt, sh))
+        bvhs.append(b)
+    insts, boxes, centres = [], [], []
+    masks = [atlas_rt.MASK_ALL, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW, atlas_rt.MASK_SHADOW]
+    for i in range(n_inst):
+        k = int(rng.integers(len(meshes)))
+        M = np.eye(4)
+        M[:3, :3] = _rotation(rng) @ np.diag(rng.uniform(0.5, 2.0, 3))
+        M[:3, 3] = rng.uniform(-6, 6, 3)
+        centres.append(M[:3, 3].copy())
+        insts.append(atlas_rt.make_instance(M, k, masks[i % 3], material_offset=4 * k))
+        lo, hi = atlas_rt.mesh_bounds(bvhs[k])
+        boxes.append(atlas_rt.transform_aabb(lo, hi, M))
+    insts = np.array(insts, atlas_rt.INSTANCE_DTYPE)
+    boxes = np.array(boxes, F32)
+    top = BVH(boxes_only=boxes)
+    ordered = insts[top.order].copy()
+    ordered["nextInstance"] = np.where(top.end_of_node > 0, -1, np.arange(len(ordered)) + 1)
+    mats = np.zeros(12, MATERIAL_DTYPE)
+    mats["opacity"] = rng.uniform(0.0, 1.0, 12)
+    for t in ("baseColorTexture", "normalTexture", "roughnessTexture", "metalnessTexture", "aoTexture"):
+        mats[t] = -1
+    # -1: none; an index past the table is undefined in the engine (a
+    # bindless read out of bounds), so the goldens stay within it
+    mats["opacityTexture"] = rng.integers(-1, 3, 12)
+    mats["invertUVs"] = rng.integers(0, 2, 12)
+    tex = [rng.integers(0, 256, (16, 32), dtype=np.uint8),
+           rng.integers(0, 256, (8, 5, 4), dtype=np.uint8),
+           rng.uniform(-0.2, 1.2, (33, 7)).astype(F32)]
+    o, d = scenes.sphere_rays(n_rays, seed=seed + 3, radius=20.0, center=(0.0, 0.0, 0.0))
+    # three in four rays aimed at an instance, the rest anywhere in the scene
+    tgt = rng.uniform(-6, 6, (n_rays, 3))
+    aim = rng.random(n_rays) < 0.75
+    tgt[aim] = np.array(centres)[rng.integers(0, n_inst, aim.sum())] + rng.normal(0, 0.8, (aim.sum(), 3))
+    d = scenes._normalize((tgt - o).astype(F32))
+    rays8 = scenes.rays8(o, d, 1e-4, 1e3)
+    return {"top": top.nodes_f32.copy(), "instances": ordered, "meshes": meshes, "materials": mats,
+            "textures": tex, "rays8": rays8}
+
+
+def texture_rgba(t):
+    """A texel array of the library's formats as RGBA float texels, as a
+    sampler returns them: R8 / RGBA8 unorm c / 255, R32F as stored, absent
+    channels (0, 0, 1)."""
+    h, w = t.shape[:2]
+    out = np.zeros((h, w, 4), F32)
+    out[..., 3] = 1.0
+    if t.dtype == np.uint8 and t.ndim == 2:
+        out[..., 0] = t.astype(F32) / F32(255.0)
+    elif t.dtype == np.uint8:
+        out[...] = t.astype(F32) / F32(255.0)
+    else:
+        out[..., 0] = t
+    return np.ascontiguousarray(out)
+
+
+def scene_digest(sc):
+    import hashlib
+    h = hashlib.sha256()
+    for a in [sc["top"], sc["instances"], sc["materials"], sc["rays8"], *sc["textures"],
+              *[x for m in sc["meshes"] for x in m]]:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def trace_scene(lib: C.CDLL, sc: dict) -> dict:
+    """The reference's HitClosest / HitAny (cull mask: all) and
+    HitClosestTransparency / HitAnyTransparency (all and shadow) over sc."""
+    P = C.c_void_p
+    keep = [sc["top"], sc["instances"], sc["materials"]]
+    nodes = (P * 3)(*[m[0].ctypes.data for m in sc["meshes"]])
+    bt = (P * 3)(*[m[1].ctypes.data for m in sc["meshes"]])
+    tr = (P * 3)(*[m[2].ctypes.data for m in sc["meshes"]])
+    rgba = [texture_rgba(t) for t in sc["textures"]]
+    tp = (P * len(rgba))(*[t.ctypes.data for t in rgba])
+    wh = np.array([[t.shape[1], t.shape[0]] for t in rgba], np.int32).reshape(-1)
+    lib.aeglsl_scene(P(keep[0].ctypes.data), P(keep[1].ctypes.data), C.c_int(3), nodes, bt, tr,
+                     P(keep[2].ctypes.data), C.c_int(len(rgba)), tp, P(wh.ctypes.data))
+    rays = np.ascontiguousarray(sc["rays8"], F32)
+    out = {}
+    for name, kind, cull in (("closest", 0, 0xFFFFFFFF), ("any", 1, 0xFFFFFFFF),
+                             ("closest_transparency", 2, 0xFFFFFFFF), ("any_transparency", 3, 0xFFFFFFFF),
+                             ("closest_shadow", 0, 1 << 6), ("closest_transparency_shadow", 2, 1 << 6),
+                             ("any_transparency_shadow", 3, 1 << 6)):
+        o = np.zeros((len(rays), 4), F32)
+        lib.aeglsl_scene_trace(C.c_int(kind), P(rays.ctypes.data), C.c_int(len(rays)), C.c_uint(cull),
+                               P(o.ctypes.data))
+        out["trav_" + name] = o
+    return out
+
+
 def evaluate(lib: C.CDLL, ins: dict) -> dict:
     P = C.c_void_p
 
@@ -127,7 +260,10 @@ def main():
     if lib is None:
         raise SystemExit("the reference tree is needed to generate the GLSL goldens")
     ins = inputs()
-    np.savez_compressed(OUT, **ins, **evaluate(lib, ins))
+    sc = traversal_scene()
+    trav = trace_scene(lib, sc)
+    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav,
+                        trav_scene_digest=np.frombuffer(scene_digest(sc).encode(), np.uint8))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 
 

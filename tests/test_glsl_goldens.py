@@ -3,8 +3,10 @@
 tests/golden/glsl_shading.npz holds golden vectors written by the reference's
 GLSL helpers -- UpdateSurface, EvaluateDiffuseBRDF / EvaluateSpecularBRDF,
 SampleDiffuseBRDF / SampleSpecularBRDF (GGX VNDF), SampleTriangleLight,
-IntersectTriangle / IntersectAABB and the engine's random() -- compiled
-unmodified on the host by oracle/glsl/make_ref.py.  Here the oracle's
+IntersectTriangle / IntersectAABB, the engine's random(), and the software
+scene traversals HitClosest / HitAny / HitClosestTransparency /
+HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene --
+compiled unmodified on the host by oracle/glsl/make_ref.py.  Here the oracle's
 restatement (CPU) and the path tracer's and traversal's own device functions
 (GPU, through ae_rt_selftest_shading) are held to them: the intersections bit
 for bit, the BRDF from the reference's own surface terms to a few ulps, and
@@ -32,6 +34,10 @@ def test_fixture_is_what_the_reference_writes():
     for k, v in ins.items():
         assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
     for k, v in G.evaluate(lib, ins).items():
+        assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
+    sc = G.traversal_scene()
+    assert G.scene_digest(sc) == bytes(g["trav_scene_digest"]).decode()
+    for k, v in G.trace_scene(lib, sc).items():
         assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
 
 
@@ -107,3 +113,126 @@ def test_gpu_brdf_from_reference_terms():
     finally:
         ctx.close()
     np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-30)
+
+
+# ---- scene traversal: HitClosest / HitAny / HitClosestTransparency /
+# HitAnyTransparency (raytracer/bvh.hsh) compiled from the reference's GLSL ----
+
+# golden name -> (traversal, cull mask)
+TRAVERSALS = {"closest": ("closest", 0xFFFFFFFF), "any": ("any", 0xFFFFFFFF),
+              "closest_transparency": ("closest_transparency", 0xFFFFFFFF),
+              "any_transparency": ("any_transparency", 0xFFFFFFFF),
+              "closest_shadow": ("closest", 1 << 6),
+              "closest_transparency_shadow": ("closest_transparency", 1 << 6),
+              "any_transparency_shadow": ("any_transparency", 1 << 6)}
+
+
+def _generator():
+    import sys
+    from pathlib import Path
+    p = str(Path(__file__).resolve().parent / "golden")
+    if p not in sys.path:
+        sys.path.insert(0, p)
+    import gen_glsl_goldens as G
+    return G
+
+
+_SCENE = {}
+
+
+def traversal_scene():
+    """The seeded scene the trav_* goldens were traced over, rebuilt (the
+    library's builder and packers are deterministic) and checked against the
+    fixture's digest of every array."""
+    if "sc" not in _SCENE:
+        G = _generator()
+        sc = G.traversal_scene()
+        assert G.scene_digest(sc) == bytes(S.golden()["trav_scene_digest"]).decode()
+        _SCENE["sc"] = sc
+    return _SCENE["sc"]
+
+
+def check_traversal(name, ptr, inst, t, value):
+    """ptr / inst / t: triangle, instance and distance of a closest-hit
+    traversal (None for the any-hit ones), value: occlusion or transparency;
+    all held to the reference's bit for bit.  A miss leaves hitID and
+    hitInstanceID at -1 and hitDistance at tmax."""
+    g = S.golden()["trav_" + name]
+    gid, ginst = g[:, 0].view(np.int32), g[:, 1].view(np.int32)
+    if ptr is not None:
+        np.testing.assert_array_equal(ptr, gid)
+        hit = gid >= 0
+        np.testing.assert_array_equal(inst[hit], ginst[hit])
+        assert (ginst[~hit] == -1).all()
+        np.testing.assert_array_equal(t[hit].view(np.uint32), g[hit, 2].view(np.uint32))
+        assert 0.05 < hit.mean() < 0.95
+    else:
+        np.testing.assert_array_equal(np.asarray(value, np.float32).view(np.uint32), g[:, 3].view(np.uint32))
+        if name.startswith("any_transparency"):
+            assert ((value > 0) & (value < 1)).mean() > 0.02    # partial opacities were crossed
+
+
+def test_traversal_scene_is_the_golden_scene():
+    traversal_scene()
+
+
+@pytest.mark.parametrize("name", sorted(TRAVERSALS))
+def test_oracle_scene_traversal_matches_reference_glsl(name):
+    """The oracle's restated traversals give the reference's own HitClosest /
+    HitAny / HitClosestTransparency / HitAnyTransparency results bit for bit:
+    triangle, instance and distance, occlusion, and the product of the
+    opacities crossed (per-triangle, material and texture opacity)."""
+    import pyoracle
+    sc = traversal_scene()
+    kind, cull = TRAVERSALS[name]
+    args = (sc["top"], sc["instances"], sc["meshes"])
+    if kind == "closest":
+        ptr, ino, tuv = pyoracle.scene_closest_glsl(*args, sc["rays8"], cull)
+        check_traversal(name, ptr, ino, tuv[:, 0], None)
+    elif kind == "any":
+        check_traversal(name, None, None, None, pyoracle.scene_any_glsl(*args, sc["rays8"], cull).astype(np.float32))
+    elif kind == "closest_transparency":
+        ptr, ino, tuv = pyoracle.scene_closest_transparency_glsl(*args, sc["materials"], sc["rays8"], cull,
+                                                                 textures=sc["textures"])
+        check_traversal(name, ptr, ino, tuv[:, 0], None)
+    else:
+        tr = pyoracle.scene_any_transparency_glsl(*args, sc["materials"], sc["rays8"], cull, textures=sc["textures"])
+        check_traversal(name, None, None, None, tr)
+
+
+@pytest.mark.gpu
+def test_gpu_scene_traversal_matches_reference_glsl():
+    """The GPU's scene traversals (ae_rt_trace_scene_closest / _any /
+    _closest_transparency / _any_transparency) over the reference-layout
+    scene the goldens were traced on give the reference's results bit for
+    bit."""
+    import atlas_rt
+    from atlas_rt import scenes
+    sc = traversal_scene()
+    r8 = sc["rays8"]
+    tmin, tmax = float(r8[0, 6]), float(r8[0, 7])
+    assert (r8[:, 6] == r8[0, 6]).all() and (r8[:, 7] == r8[0, 7]).all()
+    packed = scenes.pack_rays(r8[:, 0:3], r8[:, 3:6])
+    ctx = atlas_rt.Context(device=0)
+    try:
+        for k, (nodes, gt, sh) in enumerate(sc["meshes"]):
+            assert ctx.upload_mesh(nodes, gt, sh) == k       # instances name meshes 0, 1, 2
+        ctx.scene_set(sc["top"], sc["instances"])
+        ctx.set_materials(sc["materials"])
+        ctx.set_textures(sc["textures"])
+        for name, (kind, cull) in sorted(TRAVERSALS.items()):
+            if kind == "closest":
+                h = ctx.trace_scene_closest(packed, tmin, tmax, cull)
+            elif kind == "closest_transparency":
+                h = ctx.trace_scene_closest_transparency(packed, tmin, tmax, cull)
+            elif kind == "any":
+                v = ctx.trace_scene_any(packed, tmin, tmax, cull)
+            else:
+                v = ctx.trace_scene_any_transparency(packed, tmin, tmax, cull)
+            ctx.synchronize()
+            if kind.startswith("closest"):
+                check_traversal(name, h["triPtr"], h["instance"], h["t"], None)
+            else:
+                check_traversal(name, None, None, None, v.astype(np.float32))
+    finally:
+        ctx.close()
