@@ -56,6 +56,7 @@ PT_CENTERED = 0x2
 MASK_ALL = 1 << 7
 MASK_SHADOW = 1 << 6
 CFG_COUNT_FETCHES = 0x1
+CFG_NO_NEAR_TIES = 0x2
 
 
 def _check(status: int, ctx=None):
@@ -202,14 +203,15 @@ class Context:
 
     def __init__(self, device: int = 0, count_fetches: bool = False, blocks_per_sm: int = 0,
                  max_steps: int = 0, refill_steps: int = 0, threads_per_block: int = 0,
-                 stack_entries_smem: int = 0, refill_below: int = 0, leaf_wait: int = 0):
+                 stack_entries_smem: int = 0, refill_below: int = 0, leaf_wait: int = 0,
+                 near_ties: bool = True):
         cfg = Config()
         cfg.device = device
         cfg.blocks_per_sm = blocks_per_sm
         cfg.threads_per_block = threads_per_block
         cfg.stack_entries_smem = stack_entries_smem
         cfg.max_steps = max_steps
-        cfg.flags = CFG_COUNT_FETCHES if count_fetches else 0
+        cfg.flags = (CFG_COUNT_FETCHES if count_fetches else 0) | (0 if near_ties else CFG_NO_NEAR_TIES)
         cfg.refill_steps = refill_steps
         cfg.refill_below = refill_below
         cfg.leaf_wait = leaf_wait
@@ -283,16 +285,17 @@ class Context:
         return nodes, tris
 
     def retest_near_ties(self, mesh: int, rays, hits, tmin: float, tmax: float, out, n_rays: int | None = None,
-                         stream=None) -> int:
+                         stream=None, count: bool = True):
         """FP64 re-test of the rays flagged HIT_FLAG_NEAR_TIE (device buffers:
         rays (n, 12) float32, hits (n, 8) float32, out (n, 8) float32 viewed
-        as HIT64_DTYPE).  Returns the number of flagged rays."""
+        as HIT64_DTYPE).  Returns the number of flagged rays (which waits for
+        the stream), or None with count=False (asynchronous)."""
         if n_rays is None:
             n_rays = rays.numel() * rays.element_size() // 48
         cnt = C.c_uint32()
         _check(lib().ae_rt_retest_near_ties(self._h, mesh, _ptr(rays), _ptr(hits), n_rays, tmin, tmax, _ptr(out),
-                                            C.byref(cnt), _stream_handle(stream)), self._h)
-        return cnt.value
+                                            C.byref(cnt) if count else None, _stream_handle(stream)), self._h)
+        return cnt.value if count else None
 
     def trace_any(self, mesh: int, rays, tmin: float, tmax: float, out=None, stream=None,
                   n_rays: int | None = None):

@@ -50,10 +50,15 @@ void* KernelFor() {
 }
 
 // ties = false: the caller discards the near-tie flag (the library's path
-// tracer, passes and radiance cache), so the scene kernels skip its detection.
+// tracer, passes and radiance cache) or the context was created with
+// AE_RT_CFG_NO_NEAR_TIES, so the kernel skips its detection.
 template <int W, int S>
 void* PickShape(bool any, bool count, int mode, bool ties) {
-    if (mode == MODE_BATCH) return count ? KernelFor<false, true, MODE_BATCH, W, S>() : KernelFor<false, false, MODE_BATCH, W, S>();
+    if (mode == MODE_BATCH) {
+        if (!ties)
+            return count ? KernelFor<false, true, MODE_BATCH, W, S, false>() : KernelFor<false, false, MODE_BATCH, W, S, false>();
+        return count ? KernelFor<false, true, MODE_BATCH, W, S>() : KernelFor<false, false, MODE_BATCH, W, S>();
+    }
     if (mode == MODE_SCENE) {
         if (any) return count ? KernelFor<true, true, MODE_SCENE, W, S>() : KernelFor<true, false, MODE_SCENE, W, S>();
         if (!ties)
@@ -61,6 +66,8 @@ void* PickShape(bool any, bool count, int mode, bool ties) {
         return count ? KernelFor<false, true, MODE_SCENE, W, S>() : KernelFor<false, false, MODE_SCENE, W, S>();
     }
     if (any) return count ? KernelFor<true, true, MODE_MESH, W, S>() : KernelFor<true, false, MODE_MESH, W, S>();
+    if (!ties)
+        return count ? KernelFor<false, true, MODE_MESH, W, S, false>() : KernelFor<false, false, MODE_MESH, W, S, false>();
     return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
 }
 
@@ -171,7 +178,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
-    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties);
+    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -339,6 +346,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     ctx->device = c.device;
     ctx->max_steps_cfg = c.max_steps;
     ctx->count_fetches = (c.flags & AE_RT_CFG_COUNT_FETCHES) != 0;
+    ctx->near_ties = (c.flags & AE_RT_CFG_NO_NEAR_TIES) == 0;
     ctx->refill_steps = c.refill_steps;
     ctx->refill_below = c.refill_below == 0 ? atlas::rt::dev::kDefaultRefillBelow
                                             : (c.refill_below > 32 ? 0u : c.refill_below);
@@ -709,7 +717,7 @@ ae_rt_status ae_rt_batch_plan_create(ae_rt_ctx* ctx, const ae_batch_desc* batche
         TraceParams p = BatchParams(ctx, plan->d_batches, n_batches, total, plan->d_counter);
         cudaError_t le = cudaMemsetAsync(plan->d_counter, 0, sizeof(uint32_t), cap);
         void* args[] = { &p };
-        void* fn = PickKernelShape(ctx->shape, false, false, MODE_BATCH);
+        void* fn = PickKernelShape(ctx->shape, false, false, MODE_BATCH, ctx->near_ties);
         if (le == cudaSuccess)
             le = cudaLaunchKernel(fn, dim3(GridFor(ctx, fn, total)), dim3(ctx->threads), args, 0, cap);
         e = cudaStreamEndCapture(cap, &plan->graph);

@@ -356,7 +356,7 @@ typedef struct ae_rt_config {
     uint32_t blocks_per_sm;       /* persistent CTAs per SM (0 = the kernel's occupancy) */
     uint32_t threads_per_block;   /* 0 = 128 */
     uint32_t max_steps;           /* traversal step cap per ray (0 = 4 x nodes + 64) */
-    uint32_t flags;               /* AE_RT_CFG_* */
+    uint32_t flags;               /* AE_RT_CFG_COUNT_FETCHES, AE_RT_CFG_NO_NEAR_TIES */
     uint32_t refill_steps;        /* traversal steps between warp refills (0 = 32) */
     uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
     uint32_t refill_below;        /* also refill as soon as fewer than this many lanes of a warp
@@ -1054,6 +1054,13 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
  * ae_rt_config.flags): inner-node fetches and triangle fetches summed over
  * rays. */
 #define AE_RT_CFG_COUNT_FETCHES 0x1u
+/* Closest-hit traces of the context skip the complete near-tie detection
+ * (AE_HIT_NEAR_TIE): the flag then marks only rays whose second accepted
+ * triangle lies within 1e-6 relative t of the nearest, a subset of the near
+ * ties, and ae_rt_retest_near_ties re-tests only those.  Hits are unchanged;
+ * the detection costs about a tenth of the closest-hit time of the terrain
+ * camera pass. */
+#define AE_RT_CFG_NO_NEAR_TIES  0x2u
 ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
 
 /* Device self-test of the traversal kernel's divide-free slab arithmetic:

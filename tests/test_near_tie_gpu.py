@@ -141,3 +141,37 @@ def test_flag_complete_and_equal_to_oracle(ctx):
     np.testing.assert_array_equal(order[h64["triPtr"][f][hit]], order[ptr[f][hit]])
     np.testing.assert_array_equal(h64["t"][f][hit], t1[f][hit])
     np.testing.assert_array_equal(h64["t_second"][f][hit], t2[f][hit])
+
+
+def test_no_near_ties_switch_keeps_hits():
+    """A context created with AE_RT_CFG_NO_NEAR_TIES returns the same hits
+    (triangle, t, u, v, second distance) as the default one; its near-tie
+    flags are the ones the second accepted distance alone shows, a subset of
+    the complete flags."""
+    import near_tie_util as U
+    import torch
+    tris, obj = U.near_tie_scene()
+    r8, lab = U.near_tie_rays(tris, obj)
+    b = BVH(tris)
+    gt = b.pack_triangles()
+    rays = torch.from_numpy(scenes.pack_rays(r8[:, 0:3], r8[:, 3:6])).cuda()
+    n = len(r8)
+    res = []
+    for near in (True, False):
+        c = atlas_rt.Context(device=0, near_ties=near)
+        try:
+            mid = c.upload_mesh(b.nodes, gt)
+            hits = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+            c.trace_closest(mid, rays, 1e-4, 1e4, out=hits, n_rays=n)
+            c.synchronize()
+            res.append(hits.cpu().numpy().view(atlas_rt.HIT_DTYPE).reshape(-1))
+        finally:
+            c.close()
+    full, off = res
+    for k in ("triPtr", "t", "u", "v", "tSecond"):
+        assert np.array_equal(full[k].view(np.uint32), off[k].view(np.uint32)), k
+    hit = full["triPtr"] >= 0
+    legacy = hit & (off["tSecond"] - off["t"] <= np.float32(1e-6) * off["t"])
+    np.testing.assert_array_equal((off["flags"] & HIT_FLAG_NEAR_TIE) != 0, legacy)
+    assert not np.any(((off["flags"] & HIT_FLAG_NEAR_TIE) != 0) & ((full["flags"] & HIT_FLAG_NEAR_TIE) == 0))
+    assert ((full["flags"] & HIT_FLAG_NEAR_TIE) != 0).sum() > ((off["flags"] & HIT_FLAG_NEAR_TIE) != 0).sum()
