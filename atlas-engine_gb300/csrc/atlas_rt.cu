@@ -40,20 +40,34 @@ using atlas::rt::dev::MODE_BATCH;
 using atlas::rt::dev::MODE_MESH;
 using atlas::rt::dev::MODE_SCENE;
 
-template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true>
+template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0>
 void* KernelFor() {
     // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
     // more per-lane state and get ~73
     constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks, false, TIES && !ANY>);
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks, false, TIES && !ANY,
+                                      STAGE>);
 }
 
 // ties = false: the caller discards the near-tie flag (the library's path
 // tracer, passes and radiance cache) or the context was created with
 // AE_RT_CFG_NO_NEAR_TIES, so the kernel skips its detection.
+// staged: the ray tiles go through shared memory by bulk copy
+// (AE_RT_CFG_STAGED_RAYS; single-mesh and scene launches without counters).
 template <int W, int S>
-void* PickShape(bool any, bool count, int mode, bool ties) {
+void* PickShape(bool any, bool count, int mode, bool ties, bool staged) {
+    constexpr int T = atlas::rt::dev::kStageRays;
+    if (staged && !count && mode != MODE_BATCH) {
+        if (mode == MODE_SCENE) {
+            if (any) return KernelFor<true, false, MODE_SCENE, W, S, true, T>();
+            return ties ? KernelFor<false, false, MODE_SCENE, W, S, true, T>()
+                        : KernelFor<false, false, MODE_SCENE, W, S, false, T>();
+        }
+        if (any) return KernelFor<true, false, MODE_MESH, W, S, true, T>();
+        return ties ? KernelFor<false, false, MODE_MESH, W, S, true, T>()
+                    : KernelFor<false, false, MODE_MESH, W, S, false, T>();
+    }
     if (mode == MODE_BATCH) {
         if (!ties)
             return count ? KernelFor<false, true, MODE_BATCH, W, S, false>() : KernelFor<false, false, MODE_BATCH, W, S, false>();
@@ -71,12 +85,12 @@ void* PickShape(bool any, bool count, int mode, bool ties) {
     return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
 }
 
-void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true) {
+void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true, bool staged = false) {
     switch (shape) {
-    case 1: return PickShape<2, 32>(any, count, mode, ties);
-    case 2: return PickShape<8, 16>(any, count, mode, ties);
-    case 3: return PickShape<4, 16>(any, count, mode, ties);
-    default: return PickShape<4, 32>(any, count, mode, ties);
+    case 1: return PickShape<2, 32>(any, count, mode, ties, staged);
+    case 2: return PickShape<8, 16>(any, count, mode, ties, staged);
+    case 3: return PickShape<4, 16>(any, count, mode, ties, staged);
+    default: return PickShape<4, 32>(any, count, mode, ties, staged);
     }
 }
 
@@ -178,7 +192,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
-    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties);
+    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -347,6 +361,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     ctx->max_steps_cfg = c.max_steps;
     ctx->count_fetches = (c.flags & AE_RT_CFG_COUNT_FETCHES) != 0;
     ctx->near_ties = (c.flags & AE_RT_CFG_NO_NEAR_TIES) == 0;
+    ctx->staged_rays = (c.flags & AE_RT_CFG_STAGED_RAYS) != 0;
     ctx->refill_steps = c.refill_steps;
     ctx->refill_below = c.refill_below == 0 ? atlas::rt::dev::kDefaultRefillBelow
                                             : (c.refill_below > 32 ? 0u : c.refill_below);

@@ -38,15 +38,18 @@ struct RetestParams {
     double tmin, tmax;
     uint32_t max_steps;
     ae_hit_f64* out;
-    uint32_t* n_retested;
+    uint32_t* n_retested;    // flagged rays found by the compaction pass
+    uint32_t* list;          // their indices, in no particular order
     uint32_t* error_word;
 };
 
 // Conservative slab test in double: [tn, tf] of the ray inside the box,
 // widened by 1e-9 relative; an axis with zero direction constrains only by
-// whether the origin lies in the (equally widened) slab.
-__device__ __forceinline__ bool box64(const double o[3], const double d[3], float lx, float ly, float lz, float hx,
-                                      float hy, float hz, double tmin, double tmax) {
+// whether the origin lies in the (equally widened) slab.  The slab distances
+// are products with the direction's reciprocal inv (one division per ray):
+// their relative error, a few units of 2^-53, is far inside the widening.
+__device__ __forceinline__ bool box64(const double o[3], const double d[3], const double inv[3], float lx, float ly,
+                                      float lz, float hx, float hy, float hz, double tmin, double tmax) {
     const double lo[3] = { lx, ly, lz }, hi[3] = { hx, hy, hz };
     double tn = tmin, tf = tmax;
     for (int k = 0; k < 3; k++) {
@@ -55,7 +58,7 @@ __device__ __forceinline__ bool box64(const double o[3], const double d[3], floa
             if (o[k] < lo[k] - w || o[k] > hi[k] + w) return false;
             continue;
         }
-        double a = (lo[k] - o[k]) / d[k], b = (hi[k] - o[k]) / d[k];
+        double a = (lo[k] - o[k]) * inv[k], b = (hi[k] - o[k]) * inv[k];
         if (a > b) { const double t = a; a = b; b = t; }
         const double w = 1e-9 * (fabs(a) + fabs(b)) + 1e-300;
         tn = fmax(tn, a - w);
@@ -75,9 +78,14 @@ __device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
 // intersections.hsh:36-57 in double, every operation rounded separately in
 // the formula's order (no contraction), so that exactly equal distances are
 // decided as the double-precision restatement decides them.  Returns the
-// accept test; t out.
+// accept test; t out.  A triangle whose quotients would fall clearly outside
+// the accept test, or beyond `bound` (a distance past which no candidate
+// changes the result), is rejected from the signs and sizes of the
+// numerators and the denominator, without the three divisions: the margins
+// (1e-12 of |den|) dwarf the rounding of a quotient (2^-53 relative), so
+// such a triangle fails the exact test too.
 __device__ __forceinline__ bool tri64(const double o[3], const double d[3], const float4& A, const float4& B,
-                                      const float4& C, double& t) {
+                                      const float4& C, double bound, double& t) {
     const double v0[3] = { A.x, A.y, A.z };
     const double e0[3] = { ds(B.x, v0[0]), ds(B.y, v0[1]), ds(B.z, v0[2]) };
     const double e1[3] = { ds(C.x, v0[0]), ds(C.y, v0[1]), ds(C.z, v0[2]) };
@@ -85,9 +93,18 @@ __device__ __forceinline__ bool tri64(const double o[3], const double d[3], cons
     const double p[3] = { cr(s[1], e0[2], e0[1], s[2]), cr(s[2], e0[0], e0[2], s[0]), cr(s[0], e0[1], e0[0], s[1]) };
     const double q[3] = { cr(d[1], e1[2], e1[1], d[2]), cr(d[2], e1[0], e1[2], d[0]), cr(d[0], e1[1], e1[0], d[1]) };
     const double den = dot3(q, e0);
-    t = __ddiv_rn(dot3(p, e1), den);
-    const double u = __ddiv_rn(dot3(q, s), den);
-    const double v = __ddiv_rn(dot3(p, d), den);
+    const double nt = dot3(p, e1), nu = dot3(q, s), nv = dot3(p, d);
+    const double ad = fabs(den);
+    if (ad > 1e-200 && ad < 1e200) {
+        const double sg = den < 0.0 ? -1.0 : 1.0;
+        const double wt = nt * sg, wu = nu * sg, wv = nv * sg;      // exact: sign flips
+        const double m = 1e-12 * ad;
+        if (wu < -m || wv < -m || wt < -m || (wu >= 0.0 && wv >= 0.0 && wu + wv > ad + m) || wt > bound * (ad + m))
+            return false;
+    }
+    t = __ddiv_rn(nt, den);
+    const double u = __ddiv_rn(nu, den);
+    const double v = __ddiv_rn(nv, den);
     return t >= 0.0 && u >= 0.0 && v >= 0.0 && da(u, v) <= 1.0;
 }
 
@@ -100,23 +117,49 @@ __device__ __forceinline__ bool same_triangle(const float4* q, const float4& A, 
            c.y == C.y && c.z == C.z;
 }
 
-__global__ void retest_kernel(RetestParams p) {
+// Pass 1: every ray's result as the FP32 trace left it, and the list of the
+// flagged rays (warp-aggregated appends), so that the double-precision pass
+// runs one flagged ray per thread with full warps.
+__global__ void retest_compact_kernel(RetestParams p) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
-        const float4 h0 = p.hits[i * 2], h1 = p.hits[i * 2 + 1];
-        const uint32_t flags = __float_as_uint(h0.w);
-        ae_hit_f64 r;
-        r.t = double(h0.x);
-        r.t_second = double(h1.z);
-        r.triPtr = __float_as_int(h0.y);
-        r.flags = flags & AE_HIT_HIT;
-        if (!(flags & AE_HIT_NEAR_TIE) || p.n_nodes == 0) {
+    const size_t n_iter = (size_t(p.n) + stride - 1) / stride * stride;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_iter; i += stride) {
+        bool flagged = false;
+        if (i < p.n) {
+            const float4 h0 = p.hits[i * 2], h1 = p.hits[i * 2 + 1];
+            const uint32_t flags = __float_as_uint(h0.w);
+            ae_hit_f64 r;
+            r.t = double(h0.x);
+            r.t_second = double(h1.z);
+            r.triPtr = __float_as_int(h0.y);
+            r.flags = flags & AE_HIT_HIT;
+            r.reserved[0] = r.reserved[1] = 0;
             p.out[i] = r;
-            continue;
+            flagged = (flags & AE_HIT_NEAR_TIE) && p.n_nodes != 0;
         }
-        atomicAdd(p.n_retested, 1u);
-        const float4 o4 = p.rays[i * 3], d4 = p.rays[i * 3 + 1];
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t want = __ballot_sync(0xffffffffu, flagged);
+        uint32_t base = 0;
+        if (want) {
+            const uint32_t leader = __ffs(want) - 1;
+            if (lane == leader) base = atomicAdd(p.n_retested, __popc(want));
+            base = __shfl_sync(0xffffffffu, base, leader);
+        }
+        if (flagged) p.list[base + __popc(want & ((1u << lane) - 1u))] = uint32_t(i);
+    }
+}
+
+// Pass 2: the double-precision search for every listed ray.
+__global__ void retest_kernel(RetestParams p) {
+    const uint32_t count = *p.n_retested;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+        const uint32_t i = p.list[j];
+        ae_hit_f64 r;
+        r.reserved[0] = r.reserved[1] = 0;
+        const float4 o4 = p.rays[size_t(i) * 3], d4 = p.rays[size_t(i) * 3 + 1];
         const double o[3] = { o4.x, o4.y, o4.z }, d[3] = { d4.x, d4.y, d4.z };
+        const double inv[3] = { 1.0 / d[0], 1.0 / d[1], 1.0 / d[2] };
         double best = INFINITY, second = INFINITY;
         int32_t bi = -1;
         int32_t stack[kRetestStack];
@@ -134,7 +177,7 @@ __global__ void retest_kernel(RetestParams p) {
                                  C = __ldg(p.tris + size_t(tp) * 3 + 2);
                     end = A.w > 0.0f;
                     double t;
-                    if (tri64(o, d, A, B, C, t) && t > p.tmin && t < p.tmax &&
+                    if (tri64(o, d, A, B, C, fmin(p.tmax, second), t) && t > p.tmin && t < p.tmax &&
                         !(bi >= 0 && t == best && same_triangle(p.tris + size_t(bi) * 3, A, B, C))) {
                         if (t < best || (t == best && tp < bi)) {
                             if (tp != bi) second = best;
@@ -155,8 +198,8 @@ __global__ void retest_kernel(RetestParams p) {
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
             // prune by the second distance so that t_second is exact as well
             const double bound = fmin(p.tmax, second);
-            const bool il = box64(o, d, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, p.tmin, bound);
-            const bool ir = box64(o, d, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, p.tmin, bound);
+            const bool il = box64(o, d, inv, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, p.tmin, bound);
+            const bool ir = box64(o, d, inv, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, p.tmin, bound);
             const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
             if (il && ir) {
                 if (sp >= kRetestStack) { bad = true; atomicOr(p.error_word, atlas::rt::dev::kErrStackOverflow); break; }
@@ -208,13 +251,20 @@ extern "C" ae_rt_status ae_rt_retest_near_ties(ae_rt_ctx* ctx, int32_t mesh_id, 
     p.tmax = tmax;
     p.max_steps = atlas::rt::dev::default_step_cap(m.n_nodes);
     p.out = out;
-    AE_CUDA(ctx, ctx->retest_count.ensure(sizeof(uint32_t)));
+    // word 0: the count of flagged rays; then their indices
+    AE_CUDA(ctx, ctx->retest_count.ensure(sizeof(uint32_t) * (size_t(n_rays) + 1)));
     p.n_retested = static_cast<uint32_t*>(ctx->retest_count.ptr);
+    p.list = p.n_retested + 1;
     p.error_word = ctx->d_counter + 1;
     AE_CUDA(ctx, cudaMemsetAsync(p.n_retested, 0, sizeof(uint32_t), s));
-    const uint32_t blocks = (n_rays + 255) / 256 < uint32_t(ctx->sm_count) * 8u ? (n_rays + 255) / 256
-                                                                                 : uint32_t(ctx->sm_count) * 8u;
-    retest_kernel<<<blocks, 256, 0, s>>>(p);
+    const uint32_t cap = uint32_t(ctx->sm_count) * 8u;
+    const uint32_t blocks = (n_rays + 255) / 256 < cap ? (n_rays + 255) / 256 : cap;
+    retest_compact_kernel<<<blocks, 256, 0, s>>>(p);
+    AE_CUDA(ctx, cudaGetLastError());
+    // one listed ray per thread: enough threads for every ray being flagged
+    const uint32_t cap2 = uint32_t(ctx->sm_count) * 16u;
+    const uint32_t blocks2 = (n_rays + 127) / 128 < cap2 ? (n_rays + 127) / 128 : cap2;
+    retest_kernel<<<blocks2, 128, 0, s>>>(p);
     AE_CUDA(ctx, cudaGetLastError());
     if (n_retested) {
         AE_CUDA(ctx, cudaMemcpyAsync(n_retested, p.n_retested, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -203,7 +203,7 @@ ae_rt_status GeneratePaths(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint
     pp.scale = rc->scale;
     pp.samples = static_cast<float4*>(rc->samples.ptr);
     pp.n_samples = rc->d_counts;
-    rc_paths_kernel<<<(n_paths + 127) / 128, 128, 0, s>>>(pp);
+    rc_paths_kernel<<<(n_paths + RC_PATH_THREADS - 1) / RC_PATH_THREADS, RC_PATH_THREADS, 0, s>>>(pp);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
 }

@@ -63,13 +63,6 @@ struct RcGrid {
     uint32_t dense[RC_LEVELS];           // 0: hashed, else the dense stride (res + 1)
 };
 
-__device__ __forceinline__ uint32_t rc_index(const RcGrid& g, int l, uint32_t x, uint32_t y, uint32_t z) {
-    const uint32_t st = g.dense[l];
-    if (st) return x + y * st + z * st * st;
-    // spatial hash of the Instant-NGP paper: xor of coordinates times primes
-    return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (g.T - 1u);
-}
-
 // Real spherical harmonics of degree < 4 (16 coefficients).
 __device__ __forceinline__ void sh16(float x, float y, float z, float* o) {
     const float xx = x * x, yy = y * y, zz = z * z;
@@ -91,34 +84,68 @@ __device__ __forceinline__ void sh16(float x, float y, float z, float* o) {
     o[15] = 0.59004358992664352f * x * (-xx + 3.0f * yy);
 }
 
-__device__ __forceinline__ void rc_cell(const RcGrid& g, const float4& q0, int l, uint32_t c[3], float f[3]) {
-    const float x[3] = { fminf(fmaxf((q0.x - g.lox) * g.sx, 0.0f), 0.999999f),
-                         fminf(fmaxf((q0.y - g.loy) * g.sy, 0.0f), 0.999999f),
-                         fminf(fmaxf((q0.z - g.loz) * g.sz, 0.0f), 0.999999f) };
+// Position in the grid's unit cube, clamped below 1.
+__device__ __forceinline__ void rc_unit(const RcGrid& g, const float4& q0, float x[3]) {
+    x[0] = fminf(fmaxf((q0.x - g.lox) * g.sx, 0.0f), 0.999999f);
+    x[1] = fminf(fmaxf((q0.y - g.loy) * g.sy, 0.0f), 0.999999f);
+    x[2] = fminf(fmaxf((q0.z - g.loz) * g.sz, 0.0f), 0.999999f);
+}
+
+// The eight corners of the level-l cell around x: table indices and
+// trilinear weights, corner k = (dx, dy, dz) = (k & 1, (k >> 1) & 1, k >> 2).
+// A corner (X, Y, Z) has index X + Y st + Z st^2 on a dense level (stride st
+// = res + 1) and (X ^ Y p1 ^ Z p2) mod T on a hashed one (the spatial hash of
+// the Instant-NGP paper, primes p1, p2), all arithmetic mod 2^32; the
+// per-axis terms are formed once and summed or xored per corner.  Weights
+// are (wx wy) wz.
+__device__ __forceinline__ void rc_corners(const RcGrid& g, int l, const float x[3], uint32_t idx[8], float w[8]) {
+    uint32_t c[3];
+    float f[3];
+#pragma unroll
     for (int a = 0; a < 3; a++) {
         const float p = x[a] * g.res[l];
         const float fl = floorf(p);
         c[a] = uint32_t(fl);
         f[a] = p - fl;
     }
+    const uint32_t st = g.dense[l];
+    uint32_t ax[2] = { c[0], c[0] + 1u }, ay[2], az[2];
+    if (st) {
+        ay[0] = c[1] * st; ay[1] = ay[0] + st;
+        az[0] = c[2] * st * st; az[1] = az[0] + st * st;
+#pragma unroll
+        for (int k = 0; k < 8; k++) idx[k] = ax[k & 1] + ay[(k >> 1) & 1] + az[k >> 2];
+    } else {
+        // spatial hash of the Instant-NGP paper: xor of coordinates times primes
+        ay[0] = c[1] * 2654435761u; ay[1] = ay[0] + 2654435761u;
+        az[0] = c[2] * 805459861u; az[1] = az[0] + 805459861u;
+#pragma unroll
+        for (int k = 0; k < 8; k++) idx[k] = (ax[k & 1] ^ ay[(k >> 1) & 1] ^ az[k >> 2]) & (g.T - 1u);
+    }
+    const float wx[2] = { 1.0f - f[0], f[0] }, wy[2] = { 1.0f - f[1], f[1] }, wz[2] = { 1.0f - f[2], f[2] };
+    float wxy[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) wxy[k] = wx[k & 1] * wy[k >> 1];
+#pragma unroll
+    for (int k = 0; k < 8; k++) w[k] = wxy[k & 3] * wz[k >> 2];
 }
 
 // Encodes one query into the 64 BF16 network inputs (32 pairs).
 __device__ __forceinline__ void rc_encode_values(const RcGrid& g, const float4& q0, const float4& q1,
                                                  const float4& q2, __nv_bfloat162 v[32]) {
+    float x[3];
+    rc_unit(g, q0, x);
     for (int l = 0; l < RC_LEVELS; l++) {
-        uint32_t c[3];
-        float f[3];
-        rc_cell(g, q0, l, c, f);
+        uint32_t idx[8];
+        float w[8];
+        rc_corners(g, l, x, idx, w);
         float a0 = 0.0f, a1 = 0.0f;
         const __half2* tab = g.table + size_t(l) * g.T;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-            const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-            const float2 e = __half22float2(tab[rc_index(g, l, c[0] + dx, c[1] + dy, c[2] + dz)]);
-            a0 += w * e.x;
-            a1 += w * e.y;
+            const float2 e = __half22float2(tab[idx[k]]);
+            a0 += w[k] * e.x;
+            a1 += w[k] * e.y;
         }
         v[l] = __floats2bfloat162_rn(a0, a1);
     }
@@ -144,19 +171,17 @@ __device__ __forceinline__ void rc_encode(const RcGrid& g, const float4& q0, con
 
 // Gradient of the hash-grid part of the input row, scattered to the table.
 __device__ __forceinline__ void rc_encode_backward(const RcGrid& g, const float4& q0, const __nv_bfloat16* drow) {
+    float x[3];
+    rc_unit(g, q0, x);
     for (int l = 0; l < RC_LEVELS; l++) {
         const float2 gr = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(drow)[l]);
         if (gr.x == 0.0f && gr.y == 0.0f) continue;
-        uint32_t c[3];
-        float f[3];
-        rc_cell(g, q0, l, c, f);
+        uint32_t idx[8];
+        float w[8];
+        rc_corners(g, l, x, idx, w);
         float2* gt = g.grad + size_t(l) * g.T;
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-            const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-            atomicAdd(&gt[rc_index(g, l, c[0] + dx, c[1] + dy, c[2] + dz)], make_float2(w * gr.x, w * gr.y));
-        }
+        for (int k = 0; k < 8; k++) atomicAdd(&gt[idx[k]], make_float2(w[k] * gr.x, w[k] * gr.y));
     }
 }
 
@@ -651,11 +676,17 @@ __device__ __forceinline__ float safe_div(float a, float b) { return b > 1e-30f 
 // indirect radiance estimate -- the next-event contributions of the later
 // vertices divided by the path throughput that arrived at k -- divided by
 // the base colour and scaled.
-static __global__ void rc_paths_kernel(RcPathParams p) {
+// A vertex's record, arriving throughput and base colour wait in shared
+// memory (one column per thread) until the path ends, so that the kernel
+// fits 128 registers and 65,536 paths run in one wave of 4 CTAs per SM.
+constexpr uint32_t RC_PATH_THREADS = 128;
+static __global__ void __launch_bounds__(RC_PATH_THREADS, 4) rc_paths_kernel(RcPathParams p) {
+    __shared__ float4 s_rec[RC_MAX_DEPTH * 3][RC_PATH_THREADS];
+    __shared__ float s_ab[RC_MAX_DEPTH * 6][RC_PATH_THREADS];    // arrive xyz, base xyz per vertex
+    const uint32_t tid = threadIdx.x;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    float4 rec[RC_MAX_DEPTH][3] = {};
-    V3 arrive[RC_MAX_DEPTH] = {}, base[RC_MAX_DEPTH] = {}, acc[RC_MAX_DEPTH] = {};
+    V3 acc[RC_MAX_DEPTH] = {};
     uint32_t nv = 0;
     if (i < p.n_paths) {
         const uint32_t npix = p.cam.width * p.cam.height;
@@ -689,16 +720,15 @@ static __global__ void rc_paths_kernel(RcPathParams p) {
                     if (k + 1 < int(b) && k < int(nv)) acc[k] = acc[k] + e;
             }
             if (b < p.max_bounces && b < uint32_t(RC_MAX_DEPTH)) {
+                s_rec[b * 3 + 0][tid] = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
+                s_rec[b * 3 + 1][tid] = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(pix));
+                s_rec[b * 3 + 2][tid] = make_float4(sf.N.x, sf.N.y, sf.N.z, float(b));
+                s_ab[b * 6 + 0][tid] = thr.x; s_ab[b * 6 + 1][tid] = thr.y; s_ab[b * 6 + 2][tid] = thr.z;
+                s_ab[b * 6 + 3][tid] = sf.mat.base.x; s_ab[b * 6 + 4][tid] = sf.mat.base.y;
+                s_ab[b * 6 + 5][tid] = sf.mat.base.z;
 #pragma unroll
                 for (int k = 0; k < RC_MAX_DEPTH; k++)
-                    if (k == int(b)) {
-                        rec[k][0] = make_float4(sf.P.x, sf.P.y, sf.P.z, sf.mat.roughness);
-                        rec[k][1] = make_float4(sf.V.x, sf.V.y, sf.V.z, __uint_as_float(pix));
-                        rec[k][2] = make_float4(sf.N.x, sf.N.y, sf.N.z, float(b));
-                        arrive[k] = thr;
-                        base[k] = sf.mat.base;
-                        acc[k] = v3(0, 0, 0);
-                    }
+                    if (k == int(b)) acc[k] = v3(0, 0, 0);
                 nv = b + 1;
             }
             const bool cont = b < p.max_bounces;
@@ -726,15 +756,18 @@ static __global__ void rc_paths_kernel(RcPathParams p) {
     }
 #pragma unroll
     for (int k = 0; k < RC_MAX_DEPTH; k++) {
-        const bool emit = k < int(nv) && base[k].x + base[k].y + base[k].z > 0.0f;
+        const bool has = k < int(nv);
+        const V3 base = has ? v3(s_ab[k * 6 + 3][tid], s_ab[k * 6 + 4][tid], s_ab[k * 6 + 5][tid]) : v3(0, 0, 0);
+        const bool emit = has && base.x + base.y + base.z > 0.0f;
         const uint32_t si = warp_append(p.n_samples, emit, lane);
         if (emit) {
-            const V3 tg = v3(safe_div(acc[k].x, arrive[k].x * base[k].x), safe_div(acc[k].y, arrive[k].y * base[k].y),
-                             safe_div(acc[k].z, arrive[k].z * base[k].z)) * p.scale;
+            const V3 arrive = v3(s_ab[k * 6 + 0][tid], s_ab[k * 6 + 1][tid], s_ab[k * 6 + 2][tid]);
+            const V3 tg = v3(safe_div(acc[k].x, arrive.x * base.x), safe_div(acc[k].y, arrive.y * base.y),
+                             safe_div(acc[k].z, arrive.z * base.z)) * p.scale;
             float4* o = p.samples + size_t(si) * 4;
-            o[0] = rec[k][0];
-            o[1] = rec[k][1];
-            o[2] = rec[k][2];
+            o[0] = s_rec[k * 3 + 0][tid];
+            o[1] = s_rec[k * 3 + 1][tid];
+            o[2] = s_rec[k * 3 + 2][tid];
             o[3] = make_float4(tg.x, tg.y, tg.z, 1.0f);
         }
     }

@@ -110,20 +110,20 @@ __device__ __forceinline__ void group_sync(uint32_t g) {
 // rc_encode_values with four levels' table reads in flight at once.
 __device__ __forceinline__ void rc_encode_values_wide(const RcGrid& g, const float4& q0, const float4& q1,
                                                       const float4& q2, __nv_bfloat162 v[32]) {
+    float x[3];
+    rc_unit(g, q0, x);
 #pragma unroll 4
     for (int l = 0; l < RC_LEVELS; l++) {
-        uint32_t c[3];
-        float f[3];
-        rc_cell(g, q0, l, c, f);
+        uint32_t idx[8];
+        float w[8];
+        rc_corners(g, l, x, idx, w);
         float a0 = 0.0f, a1 = 0.0f;
         const __half2* tab = g.table + size_t(l) * g.T;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-            const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-            const float2 e = __half22float2(tab[rc_index(g, l, c[0] + dx, c[1] + dy, c[2] + dz)]);
-            a0 += w * e.x;
-            a1 += w * e.y;
+            const float2 e = __half22float2(tab[idx[k]]);
+            a0 += w[k] * e.x;
+            a1 += w[k] * e.y;
         }
         v[l] = __floats2bfloat162_rn(a0, a1);
     }

@@ -268,6 +268,51 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// ---- staged ray queue: 1-D bulk copies (TMA) of ray tiles into shared memory ----
+constexpr uint32_t kErrWaitTimeout = 0x4u;     // a bounded device wait gave up
+constexpr int kStageRays = 16;                 // rays per staged tile (768 bytes)
+
+__device__ __forceinline__ uint32_t shared_addr(const void* ptr) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ void stage_barrier_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
+}
+
+// One bulk copy of `bytes` (a multiple of 16, both addresses 16-byte
+// aligned) from global into this CTA's shared memory; the barrier's phase
+// completes when the bytes have landed.  The proxy fence orders the warp's
+// earlier reads of the buffer before the copy's writes.
+__device__ __forceinline__ void stage_bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint64_t stage_clock_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the completion of the barrier phase of parity `parity`; false
+// after ~200 ms of the global timer, or after 2^25 polls whatever it says.
+__device__ __forceinline__ bool stage_wait(uint32_t bar, uint32_t parity) {
+    const uint64_t start = stage_clock_ns();
+    for (uint32_t it = 0; it < (1u << 25); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+        if ((it & 63u) == 63u && stage_clock_ns() - start > 200000000ull) return false;
+    }
+    return false;
+}
+
 // Per-lane traversal stack: SMEM entries in shared memory (lane-interleaved),
 // then SPILL entries in local memory.
 template <int SMEM, int SPILL>
@@ -352,12 +397,22 @@ __device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, u
 // TIES: closest-hit rays get the complete near-tie flag (kTieWindow); the
 // library's own consumers that discard the flag (path tracer, passes,
 // radiance cache) launch TIES = false.
+//
+// STAGE > 0: each warp claims its rays in tiles of STAGE consecutive rays and
+// copies every tile into shared memory with one bulk copy (TMA, 1-D) on an
+// mbarrier, the next tile in flight while the current one is handed out
+// (double-buffered); refills then read rays from shared memory.  Single-mesh
+// and scene launches only.  A copy that does not complete within the bounded
+// wait sets kErrWaitTimeout and ends the warp's refills.
 template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
-          bool BOUNDS = false, bool TIES = true>
+          bool BOUNDS = false, bool TIES = true, int STAGE = 0>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     constexpr bool TLAS = MODE == MODE_SCENE;
     constexpr bool BATCH = MODE == MODE_BATCH;
+    static_assert(STAGE == 0 || (!BATCH && !BOUNDS), "staged rays: single-mesh and scene launches only");
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
+    __shared__ __align__(128) float4 s_rays[STAGE > 0 ? WARPS : 1][2][STAGE > 0 ? STAGE * 3 : 1];
+    __shared__ __align__(8) uint64_t s_rbar[STAGE > 0 ? WARPS : 1][2];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = threadIdx.x >> 5;
     constexpr unsigned kFull = 0xffffffffu;
@@ -389,11 +444,110 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
     const uint32_t refillBelow = p.refill_below;
     const uint32_t leafWait = ANY ? 0u : p.leaf_wait;
 
+    // a ray's traversal state from its origin and direction (tmax already set)
+    auto beginRay = [&](const float4& o4, const float4& d4, uint32_t nodesHere) {
+        r.ox = o4.x; r.oy = o4.y; r.oz = o4.z;
+        r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
+        r.prepare();
+        if (TLAS) wr = r;
+        hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
+        hitID = -1; hitInst = -1; curInst = -1;
+        node = 0; sp = 0; steps = 0; flags = 0; occl = false; tieSuspect = false;
+        tlasIndex = kTlasInvalid;
+        if (MODE == MODE_MESH) { blasNodes = p.nodes; blasTris = p.tris; }
+        live = true;
+        // NaN direction or an empty BVH: miss (bvh.hsh:204, BVH.cpp:107)
+        if (isnan(r.dx) || isnan(r.dy) || isnan(r.dz) || nodesHere == 0) node = INT32_MIN;
+    };
+
+    // staged queue of the warp, kept in shared memory between refills (no
+    // registers during traversal): word 0 the current tile's first ray,
+    // word 1 the next tile's (in flight while kStPending), word 2 the rays of
+    // the current tile handed out (bits 0-7) and the flags below; the current
+    // tile sits in buffer kStCur's value, the next in the other one
+    constexpr uint32_t kStUsed = 0xffu, kStCur = 1u << 8, kStPhase0 = 1u << 9, kStPending = 1u << 11,
+                       kStDry = 1u << 12, kStFault = 1u << 13, kStEmpty = 1u << 14;
+    __shared__ uint32_t s_rstate[STAGE > 0 ? WARPS : 1][3];
+    if constexpr (STAGE > 0) {
+        if (lane == 0) {
+            stage_barrier_init(shared_addr(&s_rbar[warp][0]));
+            stage_barrier_init(shared_addr(&s_rbar[warp][1]));
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            s_rstate[warp][0] = 0;
+            s_rstate[warp][1] = 0;
+            s_rstate[warp][2] = kStEmpty;     // no current tile yet
+        }
+        __syncwarp();
+    }
+
     for (;;) {
         // ---- refill idle lanes (one atomic per warp) ----
         if (!queueDry) {
             const uint32_t idle = __ballot_sync(kFull, !live);
-            if (idle) {
+            if (STAGE > 0 && idle) {
+                uint32_t base = s_rstate[warp][0], nxt = s_rstate[warp][1], bits = s_rstate[warp][2];
+                // the rays of a tile starting at b
+                auto tileRays = [&](uint32_t b) { return min(uint32_t(STAGE), nRays - b); };
+                // claims the next tile and starts its copy into the free buffer
+                auto issue = [&]() {
+                    __syncwarp();
+                    uint32_t b = 0;
+                    if (lane == 0) b = atomicAdd(p.work_counter, uint32_t(STAGE));
+                    b = __shfl_sync(kFull, b, 0);
+                    if (b >= nRays) { bits |= kStDry; return; }
+                    if (b + uint32_t(STAGE) >= nRays) bits |= kStDry;
+                    const uint32_t nb = (bits & kStCur) ? 0u : 1u;
+                    if (lane == 0)
+                        stage_bulk_load(shared_addr(&s_rays[warp][nb][0]), p.rays + size_t(b) * 3,
+                                        tileRays(b) * 48u, shared_addr(&s_rbar[warp][nb]));
+                    nxt = b;
+                    bits |= kStPending;
+                };
+                uint32_t need = idle;
+                while (need && !(bits & kStFault)) {
+                    if ((bits & kStEmpty) || (bits & kStUsed) == tileRays(base)) {
+                        if (!(bits & kStPending)) {
+                            if (bits & kStDry) break;
+                            issue();
+                            if (!(bits & kStPending)) break;
+                        }
+                        const uint32_t nb = (bits & kStCur) ? 0u : 1u;
+                        const uint32_t parity = (bits >> (9 + nb)) & 1u;
+                        if (!__all_sync(kFull, stage_wait(shared_addr(&s_rbar[warp][nb]), parity))) {
+                            if (lane == 0) atomicOr(p.error_word, kErrWaitTimeout);
+                            bits |= kStFault;      // the copy stays pending: waited for again at exit
+                            break;
+                        }
+                        bits ^= kStPhase0 << nb;
+                        bits = (bits & ~(kStUsed | kStPending | kStEmpty | kStCur)) | (nb ? kStCur : 0u);
+                        base = nxt;
+                        if (!(bits & kStDry)) issue();
+                    }
+                    const uint32_t used = bits & kStUsed;
+                    const uint32_t rank = __popc(need & lanemask_lt());
+                    const uint32_t k = min(uint32_t(__popc(need)), tileRays(base) - used);
+                    const bool mine = ((need >> lane) & 1u) && rank < k;
+                    if (mine) {
+                        const float4* src = &s_rays[warp][(bits & kStCur) ? 1 : 0][(used + rank) * 3];
+                        rid = base + used + rank;
+                        if (p.per_ray_tmax) tmax = src[2].x;
+                        beginRay(src[0], src[1], nTop);
+                    }
+                    need &= ~__ballot_sync(kFull, mine);
+                    bits += k;
+                }
+                if ((bits & kStFault) ||
+                    ((bits & kStDry) && !(bits & kStPending) &&
+                     ((bits & kStEmpty) || (bits & kStUsed) == tileRays(base))))
+                    queueDry = true;
+                __syncwarp();
+                if (lane == 0) {
+                    s_rstate[warp][0] = base;
+                    s_rstate[warp][1] = nxt;
+                    s_rstate[warp][2] = bits;
+                }
+                __syncwarp();
+            } else if (idle) {
                 const uint32_t leader = __ffs(idle) - 1;
                 uint32_t base = 0;
                 if (lane == leader) base = atomicAdd(p.work_counter, __popc(idle));
@@ -421,19 +575,8 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         rid = ri;
                         const float4 o4 = ldg4(raySrc + size_t(ri) * 3);
                         const float4 d4 = ldg4(raySrc + size_t(ri) * 3 + 1);
-                        r.ox = o4.x; r.oy = o4.y; r.oz = o4.z;
-                        r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
-                        r.prepare();
-                        if (TLAS) wr = r;
                         if (p.per_ray_tmax) tmax = ldg4(raySrc + size_t(ri) * 3 + 2).x;
-                        hitDist = tmax; second = tmax; hu = 0.0f; hv = 0.0f;
-                        hitID = -1; hitInst = -1; curInst = -1;
-                        node = 0; sp = 0; steps = 0; flags = 0; occl = false; tieSuspect = false;
-                        tlasIndex = kTlasInvalid;
-                        if (MODE == MODE_MESH) { blasNodes = p.nodes; blasTris = p.tris; }
-                        live = true;
-                        // NaN direction or an empty BVH: miss (bvh.hsh:204, BVH.cpp:107)
-                        if (isnan(r.dx) || isnan(r.dy) || isnan(r.dz) || nodesHere == 0) node = INT32_MIN;
+                        beginRay(o4, d4, nodesHere);
                     }
                 }
             }
@@ -602,6 +745,15 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                 }
                 live = false;
             }
+        }
+    }
+
+    if constexpr (STAGE > 0) {
+        // a copy left in flight by a timed-out wait must land before the CTA exits
+        const uint32_t bits = s_rstate[warp][2];
+        if (bits & kStPending) {
+            const uint32_t nb = (bits & kStCur) ? 0u : 1u;
+            (void)__all_sync(kFull, stage_wait(shared_addr(&s_rbar[warp][nb]), (bits >> (9 + nb)) & 1u));
         }
     }
 

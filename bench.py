@@ -412,6 +412,19 @@ def workload_random65536(torch, dev, stream, flush, steps, hbm_peak=None, l2_gbs
             out[f"{name}_roofline"] = class_roofline(n * io + nf * 64 + tf * 48, ms, hbm_peak, l2_gbs,
                                                      TRAFFIC_BYTES[f"random65536_{name}"])
     cctx.close()
+    # staged ray queue A/B (same launch parameters)
+    sctx = atlas_rt.Context(device=dev.index or 0, staged_rays=True, **at.context_kwargs(tuned))
+    try:
+        smid = sctx.upload_mesh(b.nodes, gt)
+        st = {}
+        for name, fn in (("closest", lambda: sctx.trace_closest(smid, rays, 1e-4, 10.0, out=hits, stream=stream,
+                                                                 n_rays=n)),
+                         ("any", lambda: sctx.trace_any(smid, rays, 1e-4, 10.0, out=occ, stream=stream, n_rays=n))):
+            fn()
+            st[f"{name}_ms"] = float(np.mean(timed_steps(torch, dev, stream, fn, steps, flush)))
+        out["staged_rays"] = st
+    finally:
+        sctx.close()
     # end to end: pinned host rays in, pinned host hits out, one synchronous call each
     h_rays = torch.from_numpy(packed).pin_memory()
     h_hits = torch.empty((n, 8), dtype=torch.float32).pin_memory()
@@ -959,6 +972,37 @@ def near_tie_record(torch, dev, stream, flush, ctx, mid, bvh, gt, tuned, prim, p
                     "for every ray -- and value_with_retest adds it to the step time"}
 
 
+def staged_rays_record(torch, dev, stream, flush, bvh, gt, tuned, prim, sec, shd, n, n_sec, n_shd, steps):
+    """A/B of the staged ray queue (AE_RT_CFG_STAGED_RAYS: ray tiles copied
+    into shared memory by TMA bulk copies) on the camera pass's three ray
+    classes: each trace timed alone (L2 flushed before each) on a plain
+    context and on a staged one with the same launch parameters."""
+    import atlas_rt
+    from atlas_rt import autotune as at
+    hits = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    occ = torch.empty(n, dtype=torch.uint8, device=dev)
+
+    def timed(fn):
+        fn()
+        return float(np.mean(timed_steps(torch, dev, stream, fn, steps, flush)))
+    res = {}
+    for name, staged in (("plain", False), ("staged", True)):
+        c = atlas_rt.Context(device=dev.index, staged_rays=staged, **at.context_kwargs(tuned))
+        try:
+            m = c.upload_mesh(bvh.nodes, gt)
+            res[name] = {
+                "primary_ms": timed(lambda: c.trace_closest(m, prim, TMIN, TINF, out=hits, stream=stream, n_rays=n)),
+                "bounce_ms": timed(lambda: c.trace_closest(m, sec, TMIN, TINF, out=hits, stream=stream,
+                                                           n_rays=n_sec)),
+                "shadow_ms": timed(lambda: c.trace_any(m, shd, TMIN, TINF - 2 * EPSILON, out=occ, stream=stream,
+                                                       n_rays=n_shd))}
+        finally:
+            c.close()
+    tot = {k: sum(v.values()) for k, v in res.items()}
+    return dict(res, speedup=tot["plain"] / tot["staged"],
+                kept="staged" if tot["staged"] < tot["plain"] * 0.99 else "plain loads")
+
+
 def run_autotune(torch, dev, stream, log):
     """--autotune: the launch-parameter search (atlas_rt/autotune.py) for the
     camera pass, random 65,536 (closest + any) and the path tracer (8 spp;
@@ -1202,6 +1246,8 @@ def main():
 
     near = near_tie_record(torch, dev, stream, flush, ctx, mid, bvh, gt, tuned_cast, prim, prim_hits, sec, sec_hits,
                            n, n_sec, max(args.steps // 2, 3))
+    staged = staged_rays_record(torch, dev, stream, flush, bvh, gt, tuned_cast, prim, sec, shd, n, n_sec, n_shd,
+                                max(args.steps // 2, 3))
 
     ms = float(np.mean(step_ms))
     e2e = float(np.mean(e2e_ms))
@@ -1268,6 +1314,7 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "tuning": {"source": "tuning.json" if tuned_cast else "defaults", "config": tuned_cast},
         "near_ties": dict(near, value_with_retest=world * closest_rays / ((ms + near["retest_ms"]) * 1e-3) / 1e6),
+        "staged_rays": staged,
     }
     if not args.quick:
         wl = set(args.workloads.split(","))

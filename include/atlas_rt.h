@@ -356,7 +356,7 @@ typedef struct ae_rt_config {
     uint32_t blocks_per_sm;       /* persistent CTAs per SM (0 = the kernel's occupancy) */
     uint32_t threads_per_block;   /* 0 = 128 */
     uint32_t max_steps;           /* traversal step cap per ray (0 = 4 x nodes + 64) */
-    uint32_t flags;               /* AE_RT_CFG_COUNT_FETCHES, AE_RT_CFG_NO_NEAR_TIES */
+    uint32_t flags;               /* AE_RT_CFG_COUNT_FETCHES, _NO_NEAR_TIES, _STAGED_RAYS */
     uint32_t refill_steps;        /* traversal steps between warp refills (0 = 32) */
     uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
     uint32_t refill_below;        /* also refill as soon as fewer than this many lanes of a warp
@@ -1061,6 +1061,12 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
  * the detection costs about a tenth of the closest-hit time of the terrain
  * camera pass. */
 #define AE_RT_CFG_NO_NEAR_TIES  0x2u
+/* Single-mesh and scene traces of the context hand out rays in tiles of 16
+ * consecutive rays that each warp copies into shared memory with one bulk
+ * copy (TMA), the next tile in flight while the current one is used.  Ray
+ * buffers must be 16-byte aligned (as for the plain loads).  Results are
+ * unchanged. */
+#define AE_RT_CFG_STAGED_RAYS   0x4u
 ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
 
 /* Device self-test of the traversal kernel's divide-free slab arithmetic:
