@@ -613,8 +613,9 @@ class RadianceCache:
 
     def __init__(self, ctx: Context, aabb_min, aabb_max, log2_table=19, base_resolution=16, max_resolution=2048,
                  learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-15, seed=1, radiance_scale=1.0,
-                 rough_cut=0.35, glossy_split=4):
+                 rough_cut=0.35, glossy_split=4, warp_mma_training=False):
         cfg = RcConfig()
+        cfg.flags = 0x1 if warp_mma_training else 0
         cfg.radiance_scale = float(radiance_scale)
         cfg.rough_cut = float(rough_cut)
         cfg.glossy_split = int(glossy_split)

@@ -78,7 +78,7 @@ class RcConfig(C.Structure):
     _fields_ = [("log2_table", U32), ("base_resolution", U32), ("max_resolution", U32),
                 ("learning_rate", F32), ("beta1", F32), ("beta2", F32), ("epsilon", F32), ("seed", U32),
                 ("aabb_min", F32 * 3), ("aabb_max", F32 * 3), ("radiance_scale", F32), ("rough_cut", F32),
-                ("glossy_split", U32), ("reserved", U32)]
+                ("glossy_split", U32), ("flags", U32)]
 
 
 class GBuffer(C.Structure):

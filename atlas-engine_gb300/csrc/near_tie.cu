@@ -11,7 +11,10 @@
 // accepting tmin < t < tmax.  Exactly equal double distances resolve to the
 // lower BVH-order triangle index, and t_second is the second smallest
 // accepted distance over distinct triangles (two triangles at the same
-// distance make t_second equal to t).  An entry with the winner's vertices
+// distance make t_second equal to t) when it lies within kSecondWindow
+// relative of t, else +inf: the traversal prunes at that window once it has
+// a hit, so it visits about what the FP32 closest-hit traversal visits
+// instead of every box up to a far second surface.  An entry with the winner's vertices
 // is the winner itself (the root's spatial split stores a straddling
 // triangle twice), so the reported entry is one of its copies; the oracle's
 // brute-force pass over every entry gives the same triangle and pair.
@@ -26,6 +29,13 @@ using namespace atlas::rt::host;
 namespace {
 
 constexpr uint32_t kRetestStack = 128;
+constexpr double kSecondWindow = 1e-5;     // ten times the 1e-6 of a near tie
+
+// The farthest distance that can still matter: best + |best| kSecondWindow
+// (each operation rounded separately), or +inf before the first hit.
+__device__ __forceinline__ double second_limit(double best) {
+    return isinf(best) ? best : __dadd_rn(best, __dmul_rn(fabs(best), kSecondWindow));
+}
 
 struct RetestParams {
     const float4* nodes;
@@ -177,7 +187,8 @@ __global__ void retest_kernel(RetestParams p) {
                                  C = __ldg(p.tris + size_t(tp) * 3 + 2);
                     end = A.w > 0.0f;
                     double t;
-                    if (tri64(o, d, A, B, C, fmin(p.tmax, second), t) && t > p.tmin && t < p.tmax &&
+                    if (tri64(o, d, A, B, C, fmin(fmin(p.tmax, second), second_limit(best)), t) && t > p.tmin &&
+                        t < p.tmax &&
                         !(bi >= 0 && t == best && same_triangle(p.tris + size_t(bi) * 3, A, B, C))) {
                         if (t < best || (t == best && tp < bi)) {
                             if (tp != bi) second = best;
@@ -196,8 +207,9 @@ __global__ void retest_kernel(RetestParams p) {
             if (uint32_t(node) >= p.n_nodes) { bad = true; break; }
             const float4* np = p.nodes + size_t(node) * 4;
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-            // prune by the second distance so that t_second is exact as well
-            const double bound = fmin(p.tmax, second);
+            // prune by the second distance, and by the window past the nearest
+            // beyond which a second distance is not reported
+            const double bound = fmin(fmin(p.tmax, second), second_limit(best));
             const bool il = box64(o, d, inv, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, p.tmin, bound);
             const bool ir = box64(o, d, inv, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, p.tmin, bound);
             const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
@@ -217,7 +229,7 @@ __global__ void retest_kernel(RetestParams p) {
         r.flags = AE_HIT_RETESTED | (bi >= 0 ? AE_HIT_HIT : 0u) | (bad ? AE_HIT_OVERFLOW : 0u);
         r.triPtr = bi;
         r.t = best;
-        r.t_second = second;
+        r.t_second = second <= second_limit(best) ? second : INFINITY;
         p.out[i] = r;
     }
 }

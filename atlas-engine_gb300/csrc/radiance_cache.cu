@@ -88,7 +88,10 @@ ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t*
     p.slice = slice;
     p.slices = slices;
     const uint32_t count = slices ? (n + slices - 1) / slices : n;
-    rc_mlp_kernel<RC_TRAIN><<<GridBlocks(rc, count), RC_THREADS, kTrainSmem, s>>>(p);
+    if (rc->cfg.flags & AE_RC_TRAIN_WARP_MMA)
+        rc_mlp_kernel<RC_TRAIN><<<GridBlocks(rc, count), RC_THREADS, kTrainSmem, s>>>(p);
+    else
+        rc_train_tc_kernel<<<GridBlocks(rc, count), RC_TILE, RCTT_SMEM, s>>>(p);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
 }
@@ -429,6 +432,8 @@ ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out) 
     alloc((void**)&rc->d_counts, 4 * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(rc_mlp_kernel<RC_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rc_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(RCTT_SMEM));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(rc_infer_tc_kernel<RC_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(RCT_SMEM));

@@ -275,4 +275,274 @@ static __global__ void __launch_bounds__(RCT_THREADS) rc_infer_tc_kernel(RcMlpPa
                      : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Training on the tensor cores: encode + forward + relative-L2 loss +
+// backward, every GEMM a tcgen05.mma with FP32 accumulators in tensor memory.
+//
+// One group of 128 threads per CTA (one training record per thread, tile M =
+// 128), one CTA per SM (shared memory), persistent over the tiles of its
+// slice.  All operands stay in the blocked no-swizzle layout of the forward
+// pass: a core matrix is 8 rows x 16 bytes (8 BF16 along the row's inner
+// dimension), core matrices 128 bytes apart along that dimension and 1024
+// bytes apart along the rows.  Read K-major (rows = M or N, inner = K) the
+// leading byte offset is 128 and the stride byte offset 1024; read MN-major
+// (inner = M or N, rows = K) the same bytes have stride byte offset 128 and
+// leading byte offset 1024, with the instruction's transpose bit for that
+// operand.  So no operand is copied transposed:
+//  * forward      Z_l   = A_l  W_l^T   A = A_l  (K-major), B = W_l (K-major)
+//  * input grad   dA_l  = dZ_l W_l     A = dZ_l (K-major), B = W_l (MN-major)
+//  * weight grad  dW_l += dZ_l^T A_l   A = dZ_l (MN-major), B = A_l (MN-major)
+// The weight-gradient GEMM has M = 64 outputs (16 for the output layer); it
+// runs as M = 128, whose rows past the layer's outputs read the following
+// records' bytes of the dZ tile (a 2 KB margin after it keeps those reads
+// inside shared memory) and are never read back.  Tensor memory holds the
+// forward / input-gradient accumulator (columns 0-63) and the six weight
+// gradients (64 columns each from column 64), which accumulate over every
+// tile of the CTA and are added to the global FP32 gradient once, at the end.
+// Every wait is bounded (kErrTimeout); a CTA that gave up still frees its
+// tensor memory.
+constexpr uint32_t RCTT_ACT0 = 44032;                                        // 1 KB aligned, after the weights
+constexpr uint32_t RCTT_DZ = RCTT_ACT0 + (RC_HIDDEN + 1) * RCT_ABYTES;      // dP / dZ tile
+constexpr uint32_t RCTT_TAIL = RCTT_DZ + RCT_ABYTES + 2048;                 // + margin of the M = 128 reads
+constexpr uint32_t RCTT_SMEM = RCTT_TAIL + 64;
+constexpr uint32_t RCTT_TMEM_COLS = 512;
+constexpr uint32_t RCTT_DW = 64;                                             // first weight-gradient column
+
+// MN-major reading of the blocked layout (see above).
+__device__ __forceinline__ uint64_t rct_desc_mn(uint32_t saddr) {
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(1024u >> 4) << 16) | (uint64_t(128u >> 4) << 32) |
+           (uint64_t(1) << 46);
+}
+
+// kind::f16 instruction descriptor with A (bit 15) / B (bit 16) read MN-major.
+__host__ __device__ constexpr uint32_t rct_idesc_t(uint32_t m, uint32_t n, bool a_mn, bool b_mn) {
+    return rct_idesc(m, n) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
+static __global__ void __launch_bounds__(RC_TILE, 1) rc_train_tc_kernel(RcMlpParams p) {
+    extern __shared__ __align__(1024) unsigned char rctt_smem[];
+    unsigned char* wsm = rctt_smem;
+    unsigned char* acts = rctt_smem + RCTT_ACT0;
+    unsigned char* dzt = rctt_smem + RCTT_DZ;
+    unsigned char* tail = rctt_smem + RCTT_TAIL;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tail);
+    uint32_t* fail = reinterpret_cast<uint32_t*>(tail + 8);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tail + 16);
+    const uint32_t row = threadIdx.x, warp = row >> 5, lane = row & 31u;
+
+    for (uint32_t i = row; i < uint32_t(RC_WROWS) * 8u; i += blockDim.x) {
+        const uint32_t r = i >> 3, kb = i & 7u;
+        const uint32_t layer = r < uint32_t(RC_HIDDEN * RC_W) ? r / RC_W : uint32_t(RC_HIDDEN);
+        const uint32_t n = r - layer * RC_W;
+        *reinterpret_cast<uint4*>(wsm + layer * RCT_WLAYER + rct_off(n, kb)) =
+            reinterpret_cast<const uint4*>(p.weights + size_t(r) * RC_W)[kb];
+    }
+    // the dZ tile and its margin start as zeros (the M = 128 reads see no stale NaNs)
+    for (uint32_t i = row; i < (RCT_ABYTES + 2048u) / 16u; i += blockDim.x)
+        reinterpret_cast<uint4*>(dzt)[i] = make_uint4(0, 0, 0, 0);
+    if (row == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *fail = 0u;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(tslot)), "r"(RCTT_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_base = tmem + ((warp * 32u) << 16);
+    const uint32_t w_addr = smem_u32(wsm), a_addr = smem_u32(acts), dz_addr = smem_u32(dzt), mb = smem_u32(mbar);
+
+    const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
+    uint32_t first = p.offset, count = n > p.offset ? n - p.offset : 0u;
+    if (p.slices) {
+        first = uint32_t(uint64_t(n) * p.slice / p.slices);
+        count = uint32_t(uint64_t(n) * (p.slice + 1) / p.slices) - first;
+    }
+    const float inv_norm = count ? 1.0f / (3.0f * float(count)) : 0.0f;
+    const uint32_t tiles = (count + RC_TILE - 1) / RC_TILE;
+    uint32_t parity = 0;
+    bool ok = true;
+    uint32_t accw = 0;                      // weight gradients accumulate after the CTA's first tile
+
+    // thread 0 issues, commits; everyone waits and takes the same decision
+    auto wait_mma = [&]() {
+        if (!mbar_wait(mb, parity)) *fail = 1u;
+        parity ^= 1u;
+        __syncthreads();
+        ok = *fail == 0u;
+        tc_fence_after();
+    };
+    // a row of BF16 values into a tile (8 chunks of 16 bytes)
+    auto put_row = [&](unsigned char* tile, const uint32_t (&pk)[32]) {
+#pragma unroll
+        for (uint32_t kb = 0; kb < 8; kb++)
+            *reinterpret_cast<uint4*>(tile + rct_off(row, kb)) =
+                make_uint4(pk[4 * kb], pk[4 * kb + 1], pk[4 * kb + 2], pk[4 * kb + 3]);
+    };
+    auto handoff = [&]() {                  // smem writes of every thread -> the tensor core
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    };
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const uint32_t gi = tile * RC_TILE + row;
+        const bool valid = gi < count;
+        float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
+        {
+            __nv_bfloat162 v[32];
+            if (valid) {
+                const float4* rec = p.recs + size_t(first + gi) * 4;
+                q0 = rec[0]; q1 = rec[1]; q2 = rec[2]; q3 = rec[3];
+                rc_encode_values_wide(p.grid, q0, q1, q2, v);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 32; k++) v[k] = __floats2bfloat162_rn(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (uint32_t kb = 0; kb < 8; kb++)
+                *reinterpret_cast<uint4*>(acts + rct_off(row, kb)) = reinterpret_cast<const uint4*>(v)[kb];
+        }
+        handoff();
+        // ---- forward: A_{l+1} = relu(A_l W_l^T); the output layer's 16 columns ----
+#pragma unroll 1
+        for (int l = 0; l <= RC_HIDDEN && ok; l++) {
+            const uint32_t nn = l < RC_HIDDEN ? uint32_t(RC_W) : uint32_t(RC_OUT);
+            if (row == 0) {
+                const uint32_t idesc = rct_idesc(RC_TILE, nn);
+#pragma unroll
+                for (uint32_t s = 0; s < 4; s++)
+                    tc_mma(tmem, rct_desc(a_addr + uint32_t(l) * RCT_ABYTES + s * 2u * RCT_LBO),
+                           rct_desc(w_addr + uint32_t(l) * RCT_WLAYER + s * 2u * RCT_LBO), idesc, s);
+                tc_commit(mb);
+            }
+            wait_mma();
+            if (!ok) break;
+            if (l < RC_HIDDEN) {
+                uint32_t pk[32];
+#pragma unroll
+                for (uint32_t c = 0; c < 4; c++) {
+                    float x[16];
+                    tc_ld16(lane_base + c * 16u, x);
+#pragma unroll
+                    for (int k = 0; k < 8; k++) pk[c * 8 + k] = pack_bf16(fmaxf(x[2 * k], 0.0f), fmaxf(x[2 * k + 1], 0.0f));
+                }
+                put_row(acts + uint32_t(l + 1) * RCT_ABYTES, pk);
+            } else {
+                // relative L2 loss over the 3 colour outputs and its gradient dP
+                float x[16];
+                tc_ld16(lane_base, x);
+                const float tg[3] = { q3.x, q3.y, q3.z };
+                float lsum = 0.0f;
+                uint32_t pk[32];
+#pragma unroll
+                for (int k = 0; k < 32; k++) pk[k] = 0u;
+                float d[3] = { 0.0f, 0.0f, 0.0f };
+                if (valid) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float den = x[c] * x[c] + 0.01f;
+                        const float diff = x[c] - tg[c];
+                        lsum += diff * diff / den;
+                        d[c] = 2.0f * diff / den * inv_norm;
+                    }
+                }
+                pk[0] = pack_bf16(d[0], d[1]);
+                pk[1] = pack_bf16(d[2], 0.0f);
+                put_row(dzt, pk);
+                for (int off = 16; off > 0; off >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, off);
+                if (lane == 0) atomicAdd(p.loss, lsum * inv_norm);
+            }
+            handoff();
+        }
+        if (!ok) break;
+        // ---- backward: layer l's weight gradient and the gradient of its input ----
+#pragma unroll 1
+        for (int l = RC_HIDDEN; l >= 0 && ok; l--) {
+            if (row == 0) {
+                const uint32_t kout = l < RC_HIDDEN ? 4u : 1u;    // K = outputs of the layer, 16 per step
+                // dW_l (+)= dZ_l^T A_l: M = 128 (outputs, padded), N = 64 inputs, K = 128 records
+                const uint32_t idw = rct_idesc_t(RC_TILE, RC_W, true, true);
+#pragma unroll 1
+                for (uint32_t s = 0; s < RC_TILE / 16u; s++)
+                    tc_mma(tmem + RCTT_DW + uint32_t(l) * 64u, rct_desc_mn(dz_addr + s * 2u * 1024u),
+                           rct_desc_mn(a_addr + uint32_t(l) * RCT_ABYTES + s * 2u * 1024u), idw, (accw | s) ? 1u : 0u);
+                // dA_l = dZ_l W_l: M = 128 records, N = 64 inputs, K = outputs
+                const uint32_t idx = rct_idesc_t(RC_TILE, RC_W, false, true);
+#pragma unroll 1
+                for (uint32_t s = 0; s < kout; s++)
+                    tc_mma(tmem, rct_desc(dz_addr + s * 2u * RCT_LBO),
+                           rct_desc_mn(w_addr + uint32_t(l) * RCT_WLAYER + s * 2u * 1024u), idx, s);
+                tc_commit(mb);
+            }
+            wait_mma();
+            if (!ok) break;
+            float g[64];
+#pragma unroll
+            for (uint32_t c = 0; c < 4; c++) tc_ld16(lane_base + c * 16u, g + c * 16);
+            if (l > 0) {
+                // dZ_{l-1} = dA_l * relu'(A_l), A_l = relu(Z_{l-1}) read back from the tile
+                const unsigned char* al = acts + uint32_t(l) * RCT_ABYTES;
+                uint32_t pk[32];
+#pragma unroll
+                for (uint32_t kb = 0; kb < 8; kb++) {
+                    const uint4 a4 = *reinterpret_cast<const uint4*>(al + rct_off(row, kb));
+                    const uint32_t aw[4] = { a4.x, a4.y, a4.z, a4.w };
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        __nv_bfloat162 a2;
+                        *reinterpret_cast<uint32_t*>(&a2) = aw[h];
+                        const float2 af = __bfloat1622float2(a2);
+                        const int k = int(kb) * 8 + h * 2;
+                        pk[kb * 4 + h] = pack_bf16(af.x > 0.0f ? g[k] : 0.0f, af.y > 0.0f ? g[k + 1] : 0.0f);
+                    }
+                }
+                put_row(dzt, pk);
+                handoff();
+            } else if (valid) {
+                // dA_0: the hash-grid part of the input gradient, BF16 like the inputs
+                __nv_bfloat16 drow[RC_IN];
+#pragma unroll
+                for (int k = 0; k < RC_IN; k += 2)
+                    *reinterpret_cast<uint32_t*>(&drow[k]) = pack_bf16(g[k], g[k + 1]);
+                rc_encode_backward(p.grid, q0, drow);
+            }
+        }
+        accw = 1u;
+        // the next tile's encode overwrites A_0 and dZ: every MMA has completed (waited)
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    // ---- the CTA's weight gradients into the global FP32 sums (lanes = outputs) ----
+    if (ok && accw && warp < 2) {
+        const uint32_t out = row;           // warps 0 and 1: lanes 0-63
+#pragma unroll 1
+        for (int l = 0; l <= RC_HIDDEN; l++) {
+            float g[64];
+#pragma unroll
+            for (uint32_t c = 0; c < 4; c++) tc_ld16(lane_base + RCTT_DW + uint32_t(l) * 64u + c * 16u, g + c * 16);
+            const uint32_t nout = l < RC_HIDDEN ? uint32_t(RC_W) : uint32_t(RC_OUT);
+            if (out < nout) {
+                float* gw = p.grad_w + size_t(l) * RC_W * RC_W + size_t(out) * RC_W;
+#pragma unroll
+                for (int k = 0; k < 64; k += 2) atomicAdd(reinterpret_cast<float2*>(gw + k), make_float2(g[k], g[k + 1]));
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (!ok && row == 0 && p.error_word) atomicOr(p.error_word, kErrTimeout);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(RCTT_TMEM_COLS)
+                     : "memory");
+}
+
 }  // namespace atlas::rt::dev

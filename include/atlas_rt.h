@@ -930,8 +930,13 @@ typedef struct ae_rc_config {
     float radiance_scale;       /* stored value = radiance x scale (0: 1) */
     float rough_cut;            /* rendering: metals at least this rough end in the cache (0: 0.35) */
     uint32_t glossy_split;      /* rendering: paths per glossier metal at the first vertex (0: 4; max 4) */
-    uint32_t reserved;
+    uint32_t flags;             /* AE_RC_TRAIN_WARP_MMA */
 } ae_rc_config;
+
+/* Training runs on the warp-level mma.sync kernel instead of the default
+ * tensor-memory (tcgen05) kernel; both compute the same gradients up to the
+ * order of FP32 additions. */
+#define AE_RC_TRAIN_WARP_MMA 0x1u
 
 ae_rt_status ae_rc_create(ae_rt_ctx* ctx, const ae_rc_config* cfg, ae_rc** out);
 void ae_rc_destroy(ae_rc* rc);
@@ -1029,14 +1034,15 @@ ae_rt_status ae_rt_mesh_get_bvh(ae_rt_ctx* ctx, int32_t mesh, ae_bvh_node* nodes
  * tests and the double form of the shader's triangle test (tmin < t < tmax);
  * equal double distances resolve to the lower BVH-order index (entries with
  * the same vertices, the copies a spatial split makes, count as one triangle:
- * triPtr is one of them), t_second is
- * the second smallest accepted distance.  Other rays are passed through (t,
+ * triPtr is one of them), t_second is the second smallest accepted distance
+ * when it is at most t + |t| 1e-5 (each operation rounded separately), else
+ * +inf: the search prunes at that window.  Other rays are passed through (t,
  * triPtr, tSecond, AE_HIT_HIT).  Device buffers; n_retested (optional, host)
  * receives the number of flagged rays and synchronises.  The engine has no
  * counterpart: its shader keeps the FP32 winner (bvh.hsh:62-63). */
 typedef struct ae_hit_f64 {
     double t;             /* +inf: no hit */
-    double t_second;
+    double t_second;      /* within t + |t| 1e-5, else +inf (re-tested rays) */
     int32_t triPtr;       /* BVH order, -1: miss */
     uint32_t flags;       /* AE_HIT_HIT, AE_HIT_RETESTED, AE_HIT_OVERFLOW */
     int32_t reserved[2];

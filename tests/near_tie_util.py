@@ -99,3 +99,10 @@ def brute_gaps(gt, rays8):
     with np.errstate(invalid="ignore", divide="ignore"):
         gap = np.where(np.isfinite(t2) & (ptr >= 0), (t2 - t1) / t1, np.inf)
     return ptr, t1, t2, gap
+
+
+def windowed_second(t1, t2):
+    """The re-test's t_second: t2 when it is at most t1 + |t1| 1e-5 (float64,
+    each operation rounded), else +inf."""
+    lim = t1 + np.abs(t1) * 1e-5
+    return np.where(t2 <= lim, t2, np.inf)

@@ -13,6 +13,7 @@ import pytest
 
 import atlas_rt
 import pyoracle
+import near_tie_util as U
 from atlas_rt import BVH, HIT64_DTYPE, HIT_FLAG_HIT, HIT_FLAG_NEAR_TIE, HIT_FLAG_RETESTED, scenes
 
 pytestmark = pytest.mark.gpu
@@ -64,7 +65,7 @@ def check_against_brute(gt, rays8, h32, h64, cnt, limit=600, order=None):
     # the same triangle (a spatial split may store it twice: compare original indices)
     np.testing.assert_array_equal(order[h64["triPtr"][sel][hit]], order[ptr[hit]])
     np.testing.assert_array_equal(h64["t"][sel][hit], t[hit])
-    np.testing.assert_array_equal(h64["t_second"][sel][hit], t2[hit])
+    np.testing.assert_array_equal(h64["t_second"][sel][hit], U.windowed_second(t, t2)[hit])
     return len(flagged)
 
 
@@ -140,7 +141,8 @@ def test_flag_complete_and_equal_to_oracle(ctx):
     np.testing.assert_array_equal(h64["triPtr"][f] >= 0, hit)
     np.testing.assert_array_equal(order[h64["triPtr"][f][hit]], order[ptr[f][hit]])
     np.testing.assert_array_equal(h64["t"][f][hit], t1[f][hit])
-    np.testing.assert_array_equal(h64["t_second"][f][hit], t2[f][hit])
+    np.testing.assert_array_equal(h64["t_second"][f][hit], U.windowed_second(t1[f], t2[f])[hit])
+    assert (np.isfinite(h64["t_second"][f][hit]) == (gap[f][hit] <= 1e-5)).mean() > 0.99
 
 
 def test_no_near_ties_switch_keeps_hits():

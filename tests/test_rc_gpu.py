@@ -133,6 +133,42 @@ def test_gradients_match_fp64_oracle(cache):
         assert cosine(gm[a:b], gm_ref[a:b]) > 0.998, l
 
 
+@pytest.mark.parametrize("n", [512, 58_445])
+def test_tensor_memory_training_equals_warp_mma(n):
+    """The default training kernel (tcgen05, weight gradients accumulated in
+    tensor memory over every tile of a CTA and added to the global sums once)
+    and the warp-level mma.sync kernel give the same loss and gradients up to
+    the order of FP32 additions (and the BF16 roundings that order can
+    flip).  58,445 records give each CTA several tiles and a ragged last
+    one."""
+    import torch
+    ctx = atlas_rt.Context(device=0)
+    rcs = [atlas_rt.RadianceCache(ctx, LO, HI, log2_table=14, seed=3, warp_mma_training=w) for w in (False, True)]
+    try:
+        mlp, grid = scaled_params(rcs[0], 4)
+        rec = random_records(n, 6)
+        q = torch.from_numpy(rec).cuda()
+        res = []
+        for rc in rcs:
+            rc.set_params(mlp, grid)
+            gm = np.zeros(rc.n_mlp, np.float32)
+            gg = np.zeros(rc.n_grid, np.float32)
+            loss = rc.gradients(q, gm, gg)
+            res.append((loss, gm, gg))
+        (l0, gm0, gg0), (l1, gm1, gg1) = res
+        assert abs(l0 - l1) / l1 < 1e-3, (l0, l1)
+        assert rel(gm0, gm1) < 0.01 and cosine(gm0, gm1) > 0.9999, (rel(gm0, gm1), cosine(gm0, gm1))
+        assert rel(gg0, gg1) < 0.01 and cosine(gg0, gg1) > 0.9999, (rel(gg0, gg1), cosine(gg0, gg1))
+        for l in range(6):
+            a = l * 4096
+            b = a + (4096 if l < 5 else 16 * 64)
+            assert rel(gm0[a:b], gm1[a:b]) < 0.02, l
+    finally:
+        for rc in rcs:
+            rc.close()
+        ctx.close()
+
+
 def test_training_fits_a_smooth_field(cache):
     """Adam on a fixed batch drives the relative L2 loss down by 20x."""
     import torch

@@ -104,11 +104,18 @@ def test_cast_pass_and_path_tracer_equal_plain_loads():
         ph = np.zeros((W * H, 8), np.float32)
         sh = np.zeros((W * H, 8), np.float32)
         occ = np.zeros(W * H, np.uint8)
-        counts = ctx.cast_pass(mid, cam, bp, primary_hits=ph, secondary_hits=sh, shadow_occluded=occ)
+        sr = np.zeros((W * H, 12), np.float32)
+        dr = np.zeros((W * H, 12), np.float32)
+        counts = ctx.cast_pass(mid, cam, bp, primary_hits=ph, secondary_rays=sr, secondary_hits=sh,
+                               shadow_rays=dr, shadow_occluded=occ)
         acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
         ctx.pathtrace(cam, acc, spp=4, seed=9)
         ctx.synchronize()
-        return counts, ph, sh[:counts[1]], occ[:counts[2]], acc.cpu().numpy()
+        # the spawn's appends order the queues differently from run to run:
+        # compare each queue's results by ray (pixel) ID
+        o_sec = np.argsort(sr[:counts[1], 3].view(np.int32), kind="stable")
+        o_shd = np.argsort(dr[:counts[2], 3].view(np.int32), kind="stable")
+        return counts, ph, sh[:counts[1]][o_sec], occ[:counts[2]][o_shd], acc.cpu().numpy()
     r0, r1 = both(run)
     assert r0[0] == r1[0]
     for a, b in zip(r0[1:4], r1[1:4]):
