@@ -67,6 +67,9 @@ def parse():
                     help="comma-separated extra workloads (radiance_cache needs pathtrace)")
     ap.add_argument("--pt-ref-spp", type=int, default=4096, help="samples of the converged image")
     ap.add_argument("--rc-max-frames", type=int, default=320, help="frame cap of the radiance-cache run")
+    ap.add_argument("--pt-curve-spp", type=int, default=1024,
+                    help="last spp of the plain path tracer's error curve (short profiling runs use less)")
+    ap.add_argument("--pt-seeds", type=int, default=len(PT_SEEDS), help="seeds of the 64-spp target (1-4)")
     ap.add_argument("--profile", default=None, choices=["cast", "random65536", "batched64"],
                     help="set up one workload, launch its trace kernels for two steps and exit (a short case for "
                          "ncu captures; prints no bench line)")
@@ -742,7 +745,7 @@ def image_eps(ref):
     return 1e-2 * float(np.mean(ref)) ** 2
 
 
-def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
+def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0, curve_spp=1024, n_seeds=4):
     """Plain GPU path tracer on the terrain + boxes scene at 1920x1080, 3
     bounces.  The 64-spp target is averaged over the four seeds PT_SEEDS:
     each seed's `spp` samples are timed (CUDA events on the stream, and host
@@ -768,7 +771,7 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     t_ref = time.perf_counter() - t_ref0
     eps_img = image_eps(ref)
     runs = []
-    for seed in PT_SEEDS:
+    for seed in PT_SEEDS[:max(1, min(n_seeds, len(PT_SEEDS)))]:
         acc.zero_()
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -789,14 +792,14 @@ def workload_pathtrace(torch, dev, stream, ref_spp=4096, spp=64, cpu_threads=0):
     acc.zero_()
     done = 0
     ms_per_spp = mean["ms"] / spp
-    for mark in PT_CURVE:
+    for mark in [m for m in PT_CURVE if m <= curve_spp]:
         pt_render(ctx, cam, acc, None, mark - done, done, PT_SEEDS[0], tiles, stream)
         done = mark
         ctx.synchronize(stream)
         im = (acc[:, :3] / done).cpu().numpy().reshape(H, W, 3)
         curve.append({"spp": done, "ms_cum": ms_per_spp * done, "rel_mse": ptscene.rel_mse(im, ref),
                       "rel_mse_scaled_eps": ptscene.rel_mse(im, ref, eps_img)})
-    res = {"resolution": [W, H], "bounces": 3, "spp": spp, "seeds": list(PT_SEEDS),
+    res = {"resolution": [W, H], "bounces": 3, "spp": spp, "seeds": [r["seed"] for r in runs],
            "ms_to_spp": mean["ms"], "wall_ms_to_spp": mean["wall_ms"], "ms_per_spp": ms_per_spp,
            "rel_mse": mean["rel_mse"], "rel_mse_scaled_eps": mean["rel_mse_scaled_eps"], "rmse": mean["rmse"],
            "per_seed": runs, "reference_spp": ref_spp, "reference_seconds": t_ref, "rel_mse_eps": 1e-2,
@@ -1333,7 +1336,8 @@ def main():
             line["workloads"]["passes"] = workload_passes(torch, dev, stream, flush, max(args.steps // 2, 3),
                                                           0 if args.no_cpu_baseline else (os.cpu_count() or 1))
         if "pathtrace" in wl:
-            pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp,
+            pt, scene = workload_pathtrace(torch, dev, stream, ref_spp=args.pt_ref_spp, curve_spp=args.pt_curve_spp,
+                                           n_seeds=args.pt_seeds,
                                            cpu_threads=0 if args.no_cpu_baseline else (os.cpu_count() or 1))
             line["workloads"]["pathtrace"] = pt
             if "radiance_cache" in wl:
