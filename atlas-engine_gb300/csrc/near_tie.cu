@@ -5,8 +5,9 @@
 // nearest (AE_HIT_NEAR_TIE): for those rays the FP32 winner is decided by
 // rounding and traversal order.  This kernel finds, for each flagged ray, the
 // nearest triangle in double precision: a closest-hit traversal of the same
-// BVH with conservative double slab tests (every box is widened by a relative
-// 1e-9 so that no triangle the double test accepts is culled by rounding) and
+// BVH with conservative slab tests (single precision, every box widened by a
+// relative 1e-5 so that no triangle the double test accepts is culled by
+// rounding) and
 // the double form of the shader's triangle test (intersections.hsh:36-57),
 // accepting tmin < t < tmax.  Exactly equal double distances resolve to the
 // lower BVH-order triangle index, and t_second is the second smallest
@@ -53,26 +54,33 @@ struct RetestParams {
     uint32_t* error_word;
 };
 
-// Conservative slab test in double: [tn, tf] of the ray inside the box,
-// widened by 1e-9 relative; an axis with zero direction constrains only by
-// whether the origin lies in the (equally widened) slab.  The slab distances
-// are products with the direction's reciprocal inv (one division per ray):
-// their relative error, a few units of 2^-53, is far inside the widening.
-__device__ __forceinline__ bool box64(const double o[3], const double d[3], const double inv[3], float lx, float ly,
-                                      float lz, float hx, float hy, float hz, double tmin, double tmax) {
-    const double lo[3] = { lx, ly, lz }, hi[3] = { hx, hy, hz };
-    double tn = tmin, tf = tmax;
+// Conservative slab test in single precision: [tn, tf] of the ray inside the
+// box, widened by 1e-5 relative (+1e-30): each slab distance fl(fl(c - o) y)
+// with y = RN(1/d) is within 3 units of 2^-24 of (c - o) / d unless it
+// under- or overflows; an underflow stays inside the absolute term, and an
+// overflowed distance lies beyond every float tmax (entry) or below every
+// tmin (exit), where culling is right anyway; a NaN (0 times an infinite
+// reciprocal) is dropped by fminf / fmaxf, which only widens.  An axis with
+// zero direction constrains only by whether the origin lies in the (equally
+// widened) slab.  tmin / tmax are rounded outwards to float.  Double
+// precision is kept for the triangle test, which decides the result; the
+// boxes only have to keep every triangle that test can accept.
+__device__ __forceinline__ bool box32(const float o[3], const float d[3], const float y[3], float lx, float ly,
+                                      float lz, float hx, float hy, float hz, float tmin, float tmax) {
+    const float lo[3] = { lx, ly, lz }, hi[3] = { hx, hy, hz };
+    float tn = tmin, tf = tmax;
+#pragma unroll
     for (int k = 0; k < 3; k++) {
-        if (d[k] == 0.0) {
-            const double w = 1e-9 * (fabs(lo[k]) + fabs(hi[k])) + 1e-300;
+        if (d[k] == 0.0f) {
+            const float w = 1e-5f * (fabsf(lo[k]) + fabsf(hi[k])) + 1e-30f;
             if (o[k] < lo[k] - w || o[k] > hi[k] + w) return false;
             continue;
         }
-        double a = (lo[k] - o[k]) * inv[k], b = (hi[k] - o[k]) * inv[k];
-        if (a > b) { const double t = a; a = b; b = t; }
-        const double w = 1e-9 * (fabs(a) + fabs(b)) + 1e-300;
-        tn = fmax(tn, a - w);
-        tf = fmin(tf, b + w);
+        float a = (lo[k] - o[k]) * y[k], b = (hi[k] - o[k]) * y[k];
+        if (a > b) { const float t = a; a = b; b = t; }
+        const float w = 1e-5f * (fabsf(a) + fabsf(b)) + 1e-30f;
+        tn = fmaxf(tn, a - w);
+        tf = fminf(tf, b + w);
     }
     return tn <= tf;
 }
@@ -169,7 +177,9 @@ __global__ void retest_kernel(RetestParams p) {
         r.reserved[0] = r.reserved[1] = 0;
         const float4 o4 = p.rays[size_t(i) * 3], d4 = p.rays[size_t(i) * 3 + 1];
         const double o[3] = { o4.x, o4.y, o4.z }, d[3] = { d4.x, d4.y, d4.z };
-        const double inv[3] = { 1.0 / d[0], 1.0 / d[1], 1.0 / d[2] };
+        const float of[3] = { o4.x, o4.y, o4.z }, df[3] = { d4.x, d4.y, d4.z };
+        const float yf[3] = { __frcp_rn(d4.x), __frcp_rn(d4.y), __frcp_rn(d4.z) };
+        const float tminf = __double2float_rd(p.tmin);
         double best = INFINITY, second = INFINITY;
         int32_t bi = -1;
         int32_t stack[kRetestStack];
@@ -206,12 +216,14 @@ __global__ void retest_kernel(RetestParams p) {
             }
             if (uint32_t(node) >= p.n_nodes) { bad = true; break; }
             const float4* np = p.nodes + size_t(node) * 4;
-            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            float4 n0, n1, n2, n3;
+            atlas::rt::dev::ldg_node(np, n0, n1, n2, n3);
             // prune by the second distance, and by the window past the nearest
             // beyond which a second distance is not reported
             const double bound = fmin(fmin(p.tmax, second), second_limit(best));
-            const bool il = box64(o, d, inv, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, p.tmin, bound);
-            const bool ir = box64(o, d, inv, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, p.tmin, bound);
+            const float boundf = __double2float_ru(bound);
+            const bool il = box32(of, df, yf, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tminf, boundf);
+            const bool ir = box32(of, df, yf, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tminf, boundf);
             const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
             if (il && ir) {
                 if (sp >= kRetestStack) { bad = true; atomicOr(p.error_word, atlas::rt::dev::kErrStackOverflow); break; }

@@ -24,6 +24,7 @@ struct ae_rc {
     float* mlp_m = nullptr;
     float* mlp_v = nullptr;
     float* mlp_grad = nullptr;
+    bool grads_zero = false;       // the gradient buffers hold zeros (Adam leaves them so)
     __nv_bfloat16* mlp_bf16 = nullptr;
     float* grid_master = nullptr;
     float* grid_m = nullptr;
@@ -78,8 +79,11 @@ uint32_t GridBlocks(ae_rc* rc, uint32_t n) {
 // mlp_grad / grid_grad (zeroed first); loss sum into d_loss.
 ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t* n_dev, uint32_t slice,
                       uint32_t slices, cudaStream_t s) {
-    RC_CUDA(rc, cudaMemsetAsync(rc->mlp_grad, 0, RC_NPARAM * sizeof(float), s));
-    RC_CUDA(rc, cudaMemsetAsync(rc->grid_grad, 0, rc->grid_params * sizeof(float), s));
+    if (!rc->grads_zero) {
+        RC_CUDA(rc, cudaMemsetAsync(rc->mlp_grad, 0, RC_NPARAM * sizeof(float), s));
+        RC_CUDA(rc, cudaMemsetAsync(rc->grid_grad, 0, rc->grid_params * sizeof(float), s));
+    }
+    rc->grads_zero = false;
     RC_CUDA(rc, cudaMemsetAsync(rc->d_loss, 0, sizeof(float), s));
     RcMlpParams p = MlpParams(rc);
     p.recs = recs;
@@ -91,7 +95,7 @@ ae_rt_status Backprop(ae_rc* rc, const float4* recs, uint32_t n, const uint32_t*
     if (rc->cfg.flags & AE_RC_TRAIN_WARP_MMA)
         rc_mlp_kernel<RC_TRAIN><<<GridBlocks(rc, count), RC_THREADS, kTrainSmem, s>>>(p);
     else
-        rc_train_tc_kernel<<<GridBlocks(rc, count), RC_TILE, RCTT_SMEM, s>>>(p);
+        rc_train_tc_kernel<<<GridBlocks(rc, count), RCTT_THREADS, RCTT_SMEM, s>>>(p);
     RC_CUDA(rc, cudaGetLastError());
     return AE_RT_OK;
 }
@@ -108,6 +112,7 @@ ae_rt_status AdamStep(ae_rc* rc, cudaStream_t s) {
     a.step_scale = scale;
     a.master = rc->mlp_master; a.m = rc->mlp_m; a.v = rc->mlp_v; a.grad = rc->mlp_grad;
     a.out_bf16 = rc->mlp_bf16; a.out_f16 = nullptr; a.n = RC_NPARAM;
+    a.zero_grad = 1;
     rc_adam_kernel<<<(RC_NPARAM / 4 + 255) / 256, 256, 0, s>>>(a);
     RC_CUDA(rc, cudaGetLastError());
     a.master = rc->grid_master; a.m = rc->grid_m; a.v = rc->grid_v; a.grad = rc->grid_grad;
@@ -115,6 +120,7 @@ ae_rt_status AdamStep(ae_rc* rc, cudaStream_t s) {
     a.skip_zero = 1;
     rc_adam_kernel<<<uint32_t(rc->sm_count) * 8u, 256, 0, s>>>(a);
     RC_CUDA(rc, cudaGetLastError());
+    rc->grads_zero = true;
     return AE_RT_OK;
 }
 

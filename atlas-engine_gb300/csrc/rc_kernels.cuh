@@ -496,13 +496,14 @@ struct RcAdamParams {
     float* master;
     float* m;
     float* v;
-    const float* grad;
+    float* grad;
     __nv_bfloat16* out_bf16;
     __half* out_f16;
     size_t n;
     float lr, beta1, beta2, eps;
     float step_scale;     // sqrt(1 - beta2^t) / (1 - beta1^t)
     uint32_t skip_zero;
+    uint32_t zero_grad;   // leave the gradient zero behind (the next step's accumulation needs no clear)
 };
 
 __device__ __forceinline__ void adam1(const RcAdamParams& a, float gr, float& w, float& m, float& v) {
@@ -530,6 +531,7 @@ static __global__ void rc_adam_kernel(RcAdamParams a) {
         reinterpret_cast<float4*>(a.master)[i] = w;
         reinterpret_cast<float4*>(a.m)[i] = m;
         reinterpret_cast<float4*>(a.v)[i] = v;
+        if (a.zero_grad) reinterpret_cast<float4*>(a.grad)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (a.out_bf16) {
             __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(a.out_bf16) + 2 * i;
             o[0] = __floats2bfloat162_rn(w.x, w.y);
@@ -620,7 +622,8 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
             node = stack[--sp];
         } else {
             const float4* np = (top ? p.tlas : blasNodes) + size_t(node) * 4;
-            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            float4 n0, n1, n2, n3;
+            ldg_node(np, n0, n1, n2, n3);
             float hl, hr;
             bool il, ir;
             bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone

@@ -46,8 +46,8 @@ sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
 
 W, H = 1920, 1080
 # DRAM bytes (read + write) of the primary closest-hit launch of this workload,
-# from ncu (131,451,904 + 38,706,432)
-TRAFFIC_PRIMARY_BYTES = 170_158_336
+# from ncu (131,451,648 + 38,613,248)
+TRAFFIC_PRIMARY_BYTES = 170_064_896
 TMIN, TINF = 0.0, 1e12
 EPSILON = 0.1
 LIGHT = (0.4, 1.0, 0.3)
@@ -354,10 +354,10 @@ def timed_steps(torch, dev, stream, step, steps, flush):
 # DRAM bytes (read + write) per launch from one ncu capture per ray class
 # (bench.py --profile cast / random65536 / batched64; profiles/trace_kernel_ray_classes.md)
 TRAFFIC_BYTES = {"primary": TRAFFIC_PRIMARY_BYTES,
-                 "bounce": 92_541_184 + 10_687_232,
-                 "shadow": 53_865_216 + 99_072,
-                 "random65536_closest": 57_691_648 + 4_169_472,
-                 "random65536_any": 57_688_576 + 143_104,
+                 "bounce": 92_501_248 + 11_122_176,
+                 "shadow": 53_865_216 + 85_760,
+                 "random65536_closest": 57_699_072 + 4_891_392,
+                 "random65536_any": 57_689_088 + 346_624,
                  "batched64": 1_200_891_136 + 263_677_952}
 
 
