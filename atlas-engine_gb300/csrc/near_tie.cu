@@ -196,8 +196,20 @@ __global__ void retest_kernel(RetestParams p) {
                     const float4 A = __ldg(p.tris + size_t(tp) * 3), B = __ldg(p.tris + size_t(tp) * 3 + 1),
                                  C = __ldg(p.tris + size_t(tp) * 3 + 2);
                     end = A.w > 0.0f;
+                    // single-precision screen: the FP32 barycentrics are within m / |den|
+                    // of the exact ones (the near-tie slack), so a triangle outside its
+                    // bounds by twice that, with |den| well above m, fails the exact test
+                    // by more than m / |den| -- far more than the double test's rounding
+                    float t32, u32, v32, sl[2];
+                    bool near32 = true;
+                    (void)atlas::rt::dev::tri_test<true>(of[0], of[1], of[2], df[0], df[1], df[2], A, B, C, t32, u32,
+                                                         v32, &near32, sl);
+                    const float ad = sl[0], m2 = 2.0f * sl[1];
+                    const bool outside = ad > 2.0f * m2 && isfinite(u32) && isfinite(v32) &&
+                                         !(__fmaf_rn(u32, ad, m2) >= 0.0f && __fmaf_rn(v32, ad, m2) >= 0.0f &&
+                                           __fmaf_rn(1.0f - (u32 + v32), ad, 2.0f * m2) >= 0.0f);
                     double t;
-                    if (tri64(o, d, A, B, C, fmin(fmin(p.tmax, second), second_limit(best)), t) && t > p.tmin &&
+                    if (!outside && tri64(o, d, A, B, C, fmin(fmin(p.tmax, second), second_limit(best)), t) && t > p.tmin &&
                         t < p.tmax &&
                         !(bi >= 0 && t == best && same_triangle(p.tris + size_t(bi) * 3, A, B, C))) {
                         if (t < best || (t == best && tp < bi)) {

@@ -226,11 +226,12 @@ __device__ __forceinline__ bool box_test(float ox, float oy, float oz, float dx,
 // |error(u)|, |error(v)| < beta = m / |den| with
 // m = 2^-20 Sd (S0+S1) (Ss+S0+S1) (2^-20 = 16 ulps of 1).  The tests are
 // taken multiplied by |den| (u |den| + m >= 0, ...), one correctly rounded
-// FMA each, so the oracle reproduces them.
+// FMA each, so the oracle reproduces them.  slack (optional) receives |den| and m.
 template <bool NEAR = false>
 __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
                                          const float4& a, const float4& b, const float4& c,
-                                         float& t, float& u, float& v, bool* nearMiss = nullptr) {
+                                         float& t, float& u, float& v, bool* nearMiss = nullptr,
+                                         float* slack = nullptr) {
     const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
     const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
     const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
@@ -258,6 +259,7 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
         const float ad = fabsf(den);
         *nearMiss = __fmaf_rn(u, ad, m) >= 0.0f && __fmaf_rn(v, ad, m) >= 0.0f &&
                     __fmaf_rn(fsub(1.0f, fadd(u, v)), ad, fadd(m, m)) >= 0.0f;
+        if (slack) { slack[0] = ad; slack[1] = m; }
     }
     return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
 }

@@ -53,6 +53,7 @@ struct Swz {
         union {                                                                           \
             struct { T x, y; };                                                           \
             struct { T r, g; };                                                           \
+            Swz<V, T, 2, 1, 0> yx;                                                        \
             T v[2];                                                                       \
         };                                                                                \
         V() : x(0), y(0) {}                                                               \
@@ -152,6 +153,12 @@ GLSL_VEC_OPS(uvec3, uint, 3)
 GLSL_VEC_OPS(uvec4, uint, 4)
 inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
 inline ivec2 operator%(const ivec2& a, int b) { return ivec2(a.x % b, a.y % b); }
+
+// ---- boolean vectors and the component-wise relations (section 8.7) ----
+struct bvec2 { bool x, y; };
+inline bvec2 lessThan(const ivec2& a, const ivec2& b) { return bvec2{ a.x < b.x, a.y < b.y }; }
+inline bool all(const bvec2& b) { return b.x && b.y; }
+inline bool any(const bvec2& b) { return b.x || b.y; }
 
 // ---- scalar built-ins (GLSL 4.60 section 8) ----
 inline float min(float x, float y) { return (y < x) ? y : x; }
@@ -408,6 +415,10 @@ inline uint imageAtomicAdd(uimage2DArray& im, const ivec3& p, uint v) {
 }
 inline uint atomicAdd(uint& mem, uint v) { const uint old = mem; mem += v; return old; }
 inline int atomicAdd(int& mem, int v) { const int old = mem; mem += v; return old; }
+// compute-shader built-ins, set per invocation by the caller (section 7.1.3)
 static uvec3 gl_GlobalInvocationID;
+static uvec3 gl_WorkGroupID;
+static uvec3 gl_NumWorkGroups;
+static uvec3 gl_LocalInvocationID;
 static uint gl_LocalInvocationIndex = 0;
 #define nonuniformEXT(x) (x)

@@ -13,6 +13,8 @@
 //   HitClosest / HitAny / HitClosestTransparency / HitAnyTransparency over a
 //   two-level scene (TLAS, instances, per-mesh BLAS, materials, opacity
 //   textures)                                raytracer/bvh.hsh:44-524
+//   the path tracer's ray generation, every invocation of one dispatch
+//                                            pathtracer/rayGen.csh:25-91
 #include "glsl.hpp"
 #include "glsl_ref.inc"
 
@@ -181,6 +183,47 @@ void aeglsl_scene_trace(int kind, const float* rays, int n, uint cull, float* ou
         o[3] = value;
     }
 }
+
+// One dispatch of rayGen.csh (not REALTIME) over a tile of the image, the
+// engine's 8 x 8 work groups run invocation by invocation.  cam: origin(4)
+// right(4) bottom(4) location(4); ints: resolution(2) pixelOffset(2)
+// tileSize(2) sampleCount.  out: capacity PackedRays (12 floats each),
+// written where the shader writes them; returns the rays written (the
+// shader's write counter).
+int aeglsl_raygen(const float* cam, const int* ints, float* out, int capacity) {
+    Uniforms.origin = vec4(cam[0], cam[1], cam[2], cam[3]);
+    Uniforms.right = vec4(cam[4], cam[5], cam[6], cam[7]);
+    Uniforms.bottom = vec4(cam[8], cam[9], cam[10], cam[11]);
+    globalData.cameraLocation = vec4(cam[12], cam[13], cam[14], cam[15]);
+    Uniforms.resolution = ivec2(ints[0], ints[1]);
+    Uniforms.pixelOffset = ivec2(ints[2], ints[3]);
+    Uniforms.tileSize = ivec2(ints[4], ints[5]);
+    Uniforms.sampleCount = ints[6];
+    PushConstants.rayBufferOffset = 0;
+    PushConstants.rayBufferSize = uint(capacity);
+    PushConstants.useRayBinning = 0;
+    rays = reinterpret_cast<PackedRay*>(out);
+    static uint counter[1];
+    counter[0] = 0u;
+    writeAtomic = counter;
+    const uint gx = uint((ints[4] + 7) / 8), gy = uint((ints[5] + 7) / 8);
+    gl_NumWorkGroups = uvec3(gx, gy, 1u);
+    for (uint wy = 0; wy < gy; wy++)
+        for (uint wx = 0; wx < gx; wx++)
+            for (uint ly = 0; ly < 8u; ly++)
+                for (uint lx = 0; lx < 8u; lx++) {
+                    gl_WorkGroupID = uvec3(wx, wy, 0u);
+                    gl_LocalInvocationID = uvec3(lx, ly, 0u);
+                    gl_GlobalInvocationID = uvec3(wx * 8u + lx, wy * 8u + ly, 0u);
+                    gl_LocalInvocationIndex = ly * 8u + lx;
+                    aeglsl_raygen_main();
+                }
+    return int(counter[0]);
+}
+
+// random(vec2(x, y)) of common/random.hsh: the per-frame sub-pixel jitter of
+// rayGen.csh is random(vec2(sampleCount, 0)), random(vec2(sampleCount, 1)).
+float aeglsl_random2(float x, float y) { return random(vec2(x, y)); }
 
 // count draws of random(x, seed) from the seed, per x; out: n * count floats.
 void aeglsl_random(const float* x, int n, float seed0, int count, float* out) {

@@ -41,14 +41,20 @@ HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
 OUT_DIR = ORACLE / "_ref"
 ENTRY_FILES = ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh", "raytracer/bvh.hsh",
-               "raytracer/direct.hsh"]
+               "raytracer/direct.hsh", "pathtracer/rayGen.csh"]
 # The engine compiles its shaders with bindless resources (AE_BINDLESS: one
 # buffer per mesh) and, where registers allow, the traversal stack in local
 # memory (LOCAL_STACK, bvh.hsh:39-42); compute shaders see one invocation.
-PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
+PREAMBLE = ("#define AE_BINDLESS\n#define LOCAL_STACK\n"
+            # rayGen.csh's entry point, called per invocation by glsl_capi.cpp
+            "#define main aeglsl_raygen_main\n"
+            "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n")
 GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
                 "static glsl_texture2D* bindlessTextures = nullptr;\n"
-                "static glsl_sampler bindlessSampler;\n")
+                "static glsl_sampler bindlessSampler;\n"
+                # the members of globals.hsh's GlobalBuffer that rayGen.csh reads
+                "struct GlobalBufferStub { vec2 jitterCurrent; vec4 cameraLocation; };\n"
+                "static GlobalBufferStub globalData;\n")
 
 _INCLUDE = re.compile(r'^\s*#include\s*<([^>]+)>\s*$')
 _FLOAT = re.compile(r'(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])')

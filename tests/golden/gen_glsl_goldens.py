@@ -1,8 +1,10 @@
 """Writes tests/golden/glsl_shading.npz: golden vectors of the engine's shading
 math and scene traversal, produced by the reference's own GLSL
 (data/shader/brdf/*.hsh, raytracer/lights.hsh, raytracer/intersections.hsh,
-raytracer/bvh.hsh, common/random.hsh) compiled on the host by the recipe
-oracle/glsl/make_ref.py.  The traversal goldens (trav_*) are traced over
+raytracer/bvh.hsh, common/random.hsh, pathtracer/rayGen.csh) compiled on the
+host by the recipe oracle/glsl/make_ref.py.  The ray-generation goldens
+(raygen_*) are whole dispatches of rayGen.csh.  The traversal goldens
+(trav_*) are traced over
 traversal_scene(), a seeded scene in the engine's buffer layouts, whose
 digest the fixture keeps so that the tests can rebuild the same scene.
 
@@ -222,6 +224,43 @@ def trace_scene(lib: C.CDLL, sc: dict) -> dict:
     return out
 
 
+# (width, height, sampleCount): one dispatch of rayGen.csh over the whole
+# image each; 30 x 17 has partial work groups on the right and at the bottom
+RAYGEN_CASES = ((64, 40, 3), (30, 17, 7), (101, 67, 12))
+
+
+def raygen_camera(w, h):
+    """The camera the raygen goldens use (scenes.pinhole_camera): origin,
+    right, bottom, location as 4 floats each."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    from atlas_rt import scenes
+    c = scenes.pinhole_camera(w, h)
+    return np.concatenate([np.append(c[k], 0.0) for k in ("origin", "right", "bottom", "location")]).astype(F32)
+
+
+def trace_raygen(lib: C.CDLL) -> dict:
+    """rayGen.csh (not REALTIME) dispatched over whole images: the packed rays
+    in the order the shader writes them, and the frame's jitter."""
+    P = C.c_void_p
+    lib.aeglsl_random2.restype = C.c_float
+    lib.aeglsl_random2.argtypes = [C.c_float, C.c_float]
+    out = {}
+    for w, h, s in RAYGEN_CASES:
+        cam = raygen_camera(w, h)
+        ints = np.array([w, h, 0, 0, w, h, s], np.int32)
+        rays = np.zeros((w * h, 12), F32)
+        n = lib.aeglsl_raygen(P(cam.ctypes.data), P(ints.ctypes.data), P(rays.ctypes.data), C.c_int(w * h))
+        assert n == w * h
+        # the shader leaves the ray's hit distance and hit instance unset
+        # (rayGen.csh:46-55), so PackRay copies whatever they held: not kept
+        rays[:, 8] = 0.0
+        rays[:, 10] = 0.0
+        out[f"raygen_{w}x{h}"] = rays
+        out[f"raygen_{w}x{h}_jitter"] = np.array([lib.aeglsl_random2(float(s), 0.0), lib.aeglsl_random2(float(s), 1.0)],
+                                                 F32)
+    return out
+
+
 def evaluate(lib: C.CDLL, ins: dict) -> dict:
     P = C.c_void_p
 
@@ -262,7 +301,7 @@ def main():
     ins = inputs()
     sc = traversal_scene()
     trav = trace_scene(lib, sc)
-    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav,
+    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib),
                         trav_scene_digest=np.frombuffer(scene_digest(sc).encode(), np.uint8))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

@@ -3,9 +3,10 @@
 tests/golden/glsl_shading.npz holds golden vectors written by the reference's
 GLSL helpers -- UpdateSurface, EvaluateDiffuseBRDF / EvaluateSpecularBRDF,
 SampleDiffuseBRDF / SampleSpecularBRDF (GGX VNDF), SampleTriangleLight,
-IntersectTriangle / IntersectAABB, the engine's random(), and the software
+IntersectTriangle / IntersectAABB, the engine's random(), the software
 scene traversals HitClosest / HitAny / HitClosestTransparency /
-HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene --
+HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene, and
+the path tracer's ray generation (pathtracer/rayGen.csh, whole dispatches) --
 compiled unmodified on the host by oracle/glsl/make_ref.py.  Here the oracle's
 restatement (CPU) and the path tracer's and traversal's own device functions
 (GPU, through ae_rt_selftest_shading) are held to them: the intersections bit
@@ -38,6 +39,8 @@ def test_fixture_is_what_the_reference_writes():
     sc = G.traversal_scene()
     assert G.scene_digest(sc) == bytes(g["trav_scene_digest"]).decode()
     for k, v in G.trace_scene(lib, sc).items():
+        assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
+    for k, v in G.trace_raygen(lib).items():
         assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
 
 
@@ -236,3 +239,63 @@ def test_gpu_scene_traversal_matches_reference_glsl():
                 check_traversal(name, None, None, None, v.astype(np.float32))
     finally:
         ctx.close()
+
+
+# ---- ray generation: pathtracer/rayGen.csh dispatched over whole images ----
+
+def _raygen_case(w, h):
+    G = _generator()
+    g = S.golden()
+    rays = g[f"raygen_{w}x{h}"]
+    jitter = g[f"raygen_{w}x{h}_jitter"]
+    return G, rays, jitter
+
+
+@pytest.mark.parametrize("w,h", [(64, 40), (30, 17), (101, 67)])
+def test_host_camera_rays_match_reference_raygen(w, h):
+    """The host formula the oracle and the bench use (scenes.pinhole_rays:
+    normalize(origin + right u + bottom v - location), (u, v) = (pixel +
+    jitter) / resolution) gives the reference shader's rays, pixel by pixel,
+    with the shader's per-frame jitter: origins bit for bit, directions to
+    one unit in the last place -- the shim's normalize is the specification's
+    x / length(x), the library's x * (1 / length(x)); a GPU driver's is an
+    approximate reciprocal square root, so the last bit is not the engine's
+    to fix.  The shader writes every pixel once."""
+    from atlas_rt import scenes
+    G, rays, jitter = _raygen_case(w, h)
+    ids = rays[:, 3].view(np.int32)
+    assert np.array_equal(np.sort(ids), np.arange(w * h))
+    cam = scenes.pinhole_camera(w, h)
+    o, d = scenes.pinhole_rays(cam, jitter=(float(jitter[0]), float(jitter[1])))
+    assert np.array_equal(rays[:, 0:3], o[ids])
+    ulps = np.abs(rays[:, 4:7].view(np.int32).astype(np.int64) - d[ids].view(np.int32))
+    assert ulps.max() <= 1, ulps.max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("w,h", [(64, 40), (30, 17), (101, 67)])
+def test_gpu_raygen_matches_reference_raygen(w, h):
+    """ae_rt_raygen with the frame's jitter writes the reference shader's rays
+    slot for slot: the same pixel (ray ID) in every queue position -- the
+    8 x 8 work-group order, then the partial groups on the right, then
+    those at the bottom -- with the same origin bits and directions to one
+    unit in the last place (normalize; see the host test)."""
+    import atlas_rt
+    import torch
+    from atlas_rt import scenes
+    G, rays, jitter = _raygen_case(w, h)
+    camd = scenes.pinhole_camera(w, h)
+    camd["jitter"] = (float(jitter[0]), float(jitter[1]))
+    cam = atlas_rt.make_camera(camd)
+    ctx = atlas_rt.Context(device=0)
+    try:
+        out = torch.zeros((w * h, 12), dtype=torch.float32, device="cuda")
+        ctx.raygen(cam, out)
+        ctx.synchronize()
+        got = out.cpu().numpy()
+    finally:
+        ctx.close()
+    np.testing.assert_array_equal(got[:, 3].view(np.int32), rays[:, 3].view(np.int32))
+    np.testing.assert_array_equal(got[:, 0:3].view(np.uint32), rays[:, 0:3].view(np.uint32))
+    ulps = np.abs(got[:, 4:7].view(np.int32).astype(np.int64) - rays[:, 4:7].view(np.int32))
+    assert ulps.max() <= 1, ulps.max()
