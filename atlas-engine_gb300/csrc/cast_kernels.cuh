@@ -5,8 +5,9 @@
 //    engine's ray-gen pass (data/shader/pathtracer/rayGen.csh:25-91,
 //    PathTracingRenderer.cpp:157-160): dir = normalize(origin + right*u +
 //    bottom*v - location), u,v = (pixel + jitter) / resolution.  Rays are
-//    written in 8x8 tile order (as rayGen.csh:53-80 orders its queue) so that
-//    neighbouring lanes trace neighbouring pixels; ray.ID = pixel index.
+//    written in rayGen.csh's queue order (8 x 8 work groups, then the
+//    partial groups; :53-80) so that neighbouring lanes trace neighbouring
+//    pixels; ray.ID = pixel index.
 //    Arithmetic is explicitly rounded in a fixed order, so a host can
 //    regenerate the same rays bit for bit.
 //  * spawn_kernel: for every hit, one cosine-weighted diffuse bounce ray
@@ -46,15 +47,29 @@ struct SpawnParams {
     uint32_t seed;
 };
 
-// Pixel index of queue slot i.
+// Pixel index (within a w x h tile) of queue slot i, in rayGen.csh's order
+// (:57-80): the complete 8 x 8 work groups first, row-major, each row-major
+// inside; then the columns of the partial groups on the right (w % 8 wide,
+// as tall as the complete groups), row-major; then the partial rows at the
+// bottom (h % 8 tall, the full width), column-major.
 __device__ __forceinline__ uint32_t slot_to_pixel(uint32_t i, uint32_t w, uint32_t h) {
-    if ((w & 7u) == 0 && (h & 7u) == 0) {
+    const uint32_t px = w >> 3, py = h >> 3, ox = w & 7u, oy = h & 7u;
+    const uint32_t a = px * py * 64u, b = a + ox * py * 8u;
+    uint32_t x, y;
+    if (i < a) {
         const uint32_t tile = i >> 6, local = i & 63u;
-        const uint32_t tilesX = w >> 3;
-        const uint32_t tx = tile % tilesX, ty = tile / tilesX;
-        return (ty * 8u + (local >> 3)) * w + tx * 8u + (local & 7u);
+        x = (tile % px) * 8u + (local & 7u);
+        y = (tile / px) * 8u + (local >> 3);
+    } else if (i < b) {
+        const uint32_t j = i - a;
+        x = px * 8u + j % ox;
+        y = j / ox;
+    } else {
+        const uint32_t j = i - b;
+        x = j / oy;
+        y = py * 8u + j % oy;
     }
-    return i;
+    return y * w + x;
 }
 
 static __global__ void raygen_kernel(CameraParams c, float4* rays) {

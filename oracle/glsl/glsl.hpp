@@ -175,6 +175,7 @@ inline int abs(int x) { return x < 0 ? -x : x; }
 inline float sqrt(float x) { return __builtin_sqrtf(x); }
 inline float pow(float x, float y) { return __builtin_powf(x, y); }
 inline float exp(float x) { return __builtin_expf(x); }
+inline float acos(float x) { return __builtin_acosf(x); }
 inline float sin(float x) { return __builtin_sinf(x); }
 inline float cos(float x) { return __builtin_cosf(x); }
 inline float atan(float y, float x) { return __builtin_atan2f(y, x); }

@@ -17,6 +17,10 @@
 //                                            pathtracer/rayGen.csh:25-91
 #include "glsl.hpp"
 #include "glsl_ref.inc"
+#include "glsl_raygen.inc"
+#include "glsl_pt.inc"
+
+using namespace aeg_glsl;
 
 #include <vector>
 
@@ -191,21 +195,22 @@ void aeglsl_scene_trace(int kind, const float* rays, int n, uint cull, float* ou
 // written where the shader writes them; returns the rays written (the
 // shader's write counter).
 int aeglsl_raygen(const float* cam, const int* ints, float* out, int capacity) {
-    Uniforms.origin = vec4(cam[0], cam[1], cam[2], cam[3]);
-    Uniforms.right = vec4(cam[4], cam[5], cam[6], cam[7]);
-    Uniforms.bottom = vec4(cam[8], cam[9], cam[10], cam[11]);
-    globalData.cameraLocation = vec4(cam[12], cam[13], cam[14], cam[15]);
-    Uniforms.resolution = ivec2(ints[0], ints[1]);
-    Uniforms.pixelOffset = ivec2(ints[2], ints[3]);
-    Uniforms.tileSize = ivec2(ints[4], ints[5]);
-    Uniforms.sampleCount = ints[6];
-    PushConstants.rayBufferOffset = 0;
-    PushConstants.rayBufferSize = uint(capacity);
-    PushConstants.useRayBinning = 0;
-    rays = reinterpret_cast<PackedRay*>(out);
+    namespace R = aeg_raygen;
+    R::Uniforms.origin = vec4(cam[0], cam[1], cam[2], cam[3]);
+    R::Uniforms.right = vec4(cam[4], cam[5], cam[6], cam[7]);
+    R::Uniforms.bottom = vec4(cam[8], cam[9], cam[10], cam[11]);
+    R::globalData.cameraLocation = vec4(cam[12], cam[13], cam[14], cam[15]);
+    R::Uniforms.resolution = ivec2(ints[0], ints[1]);
+    R::Uniforms.pixelOffset = ivec2(ints[2], ints[3]);
+    R::Uniforms.tileSize = ivec2(ints[4], ints[5]);
+    R::Uniforms.sampleCount = ints[6];
+    R::PushConstants.rayBufferOffset = 0;
+    R::PushConstants.rayBufferSize = uint(capacity);
+    R::PushConstants.useRayBinning = 0;
+    R::rays = reinterpret_cast<R::PackedRay*>(out);
     static uint counter[1];
     counter[0] = 0u;
-    writeAtomic = counter;
+    R::writeAtomic = counter;
     const uint gx = uint((ints[4] + 7) / 8), gy = uint((ints[5] + 7) / 8);
     gl_NumWorkGroups = uvec3(gx, gy, 1u);
     for (uint wy = 0; wy < gy; wy++)
@@ -216,7 +221,7 @@ int aeglsl_raygen(const float* cam, const int* ints, float* out, int capacity) {
                     gl_LocalInvocationID = uvec3(lx, ly, 0u);
                     gl_GlobalInvocationID = uvec3(wx * 8u + lx, wy * 8u + ly, 0u);
                     gl_LocalInvocationIndex = ly * 8u + lx;
-                    aeglsl_raygen_main();
+                    R::aeg_raygen_main();
                 }
     return int(counter[0]);
 }

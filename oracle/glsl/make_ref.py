@@ -26,9 +26,10 @@ language-level adjustments are applied:
     replaced by the resources the helpers name: the DFG lookup texture and
     the bindless texture table with its sampler.
 
-The flattened source goes to oracle/_ref/glsl_ref.inc and is compiled with
-oracle/glsl/glsl_capi.cpp (-O2 -ffp-contract=off) into
-oracle/_ref/libglslref.so.  Usage: python make_ref.py [REFERENCE_ROOT]
+Each program's flattened source goes to oracle/_ref/<program>.inc (the
+compute shaders rayGen.csh and rayHit.csh each in a namespace of its own, their
+`main` renamed <namespace>_main), and glsl_capi.cpp includes them all; it is
+compiled (-O2 -ffp-contract=off) into oracle/_ref/libglslref.so.  Usage: python make_ref.py [REFERENCE_ROOT]
 """
 from __future__ import annotations
 
@@ -40,15 +41,22 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
 OUT_DIR = ORACLE / "_ref"
-ENTRY_FILES = ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh", "raytracer/bvh.hsh",
-               "raytracer/direct.hsh", "pathtracer/rayGen.csh"]
+# Programs, each in a namespace of its own (a compute shader brings its own
+# `main`, uniform block and buffers; and the shim's types live in the global
+# namespace, so argument-dependent lookup must not see two programs'
+# functions): the helpers, the path tracer's ray generation and its hit shader.
+PROGRAMS = {
+    "glsl_ref": ("aeg_glsl", ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh",
+                        "raytracer/bvh.hsh", "raytracer/direct.hsh"]),
+    "glsl_raygen": ("aeg_raygen", ["pathtracer/rayGen.csh"]),
+    "glsl_pt": ("aeg_pt", ["pathtracer/rayHit.csh"]),
+}
 # The engine compiles its shaders with bindless resources (AE_BINDLESS: one
 # buffer per mesh) and, where registers allow, the traversal stack in local
 # memory (LOCAL_STACK, bvh.hsh:39-42); compute shaders see one invocation.
-PREAMBLE = ("#define AE_BINDLESS\n#define LOCAL_STACK\n"
-            # rayGen.csh's entry point, called per invocation by glsl_capi.cpp
-            "#define main aeglsl_raygen_main\n"
-            "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n")
+PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
+# rayGen.csh's work-group size (layout(local_size_x = 8, local_size_y = 8))
+WORKGROUP = {"aeg_raygen": "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n"}
 GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
                 "static glsl_texture2D* bindlessTextures = nullptr;\n"
                 "static glsl_sampler bindlessSampler;\n"
@@ -126,12 +134,16 @@ def to_cpp(src: str) -> str:
 
 def build(reference_root: Path) -> Path:
     shader_root = reference_root / "data" / "shader"
-    seen: set = set()
-    body = "".join(_flatten(shader_root / f, seen, shader_root) for f in ENTRY_FILES)
     OUT_DIR.mkdir(exist_ok=True)
-    inc = OUT_DIR / "glsl_ref.inc"
     header = "// generated by oracle/glsl/make_ref.py from the reference's shader files; do not edit\n"
-    inc.write_text(header + PREAMBLE + to_cpp(body))
+    for name, (ns, files) in PROGRAMS.items():
+        seen: set = set()
+        body = to_cpp("".join(_flatten(shader_root / f, seen, shader_root) for f in files))
+        if ns:
+            # the program's entry point becomes <namespace>_main
+            body = (f"namespace {ns} {{\n#define main {ns}_main\n" + WORKGROUP.get(ns, "") + body +
+                    f"\n#undef main\n}}  // namespace {ns}\n")
+        (OUT_DIR / f"{name}.inc").write_text(header + PREAMBLE + body)
     lib = OUT_DIR / "libglslref.so"
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fno-builtin",
            "-w", f"-I{HERE}", f"-I{OUT_DIR}", str(HERE / "glsl_capi.cpp"), "-o", str(lib)]
