@@ -15,6 +15,9 @@
 //   textures)                                raytracer/bvh.hsh:44-524
 //   the path tracer's ray generation, every invocation of one dispatch
 //                                            pathtracer/rayGen.csh:25-91
+//   the engine's path tracer, sample by sample: rayGen.csh, the trace
+//   dispatch (traceClosest.csh:12-36) and the hit shader, bounce by bounce
+//                                            pathtracer/rayHit.csh:54-338
 #include "glsl.hpp"
 #include "glsl_ref.inc"
 #include "glsl_raygen.inc"
@@ -229,6 +232,93 @@ int aeglsl_raygen(const float* cam, const int* ints, float* out, int capacity) {
 // random(vec2(x, y)) of common/random.hsh: the per-frame sub-pixel jitter of
 // rayGen.csh is random(vec2(sampleCount, 0)), random(vec2(sampleCount, 1)).
 float aeglsl_random2(float x, float y) { return random(vec2(x, y)); }
+
+// The scene of the reference's hit shader (rayHit.csh's program): the same
+// layouts as aeglsl_scene, plus the light list (GPULight, 64 bytes each).
+// No textures (every material's texture indices must be -1) and a black
+// environment.  The arrays stay owned by the caller.
+void aeglsl_pt_scene(const void* tlas, const void* instances, int n_meshes, const void* const* nodes,
+                     const void* const* bvh_tris, const void* const* tris, const void* mats, const void* lights,
+                     int n_lights) {
+    namespace T = aeg_pt;
+    T::tlasNodes = (T::PackedBVHNode*)tlas;
+    T::bvhInstances = (T::Instance*)instances;
+    for (int m = 0; m < n_meshes; m++) {
+        T::blasNodes[m].data = (T::PackedBVHNode*)nodes[m];
+        T::bvhTriangles[m].data = (T::PackedBVHTriangle*)bvh_tris[m];
+        T::triangles[m].data = (T::PackedTriangle*)tris[m];
+    }
+    T::materials = (T::RaytraceMaterial*)mats;
+    T::lights = (T::PackedLight*)lights;
+    T::PushConstants.lightCount = n_lights;
+}
+
+// `spp` samples of the engine's path tracer (not REALTIME) over a w x h image:
+// per sample, rayGen.csh (sampleCount = first_sample + s), then per bounce the
+// trace dispatch (traceClosest.csh: hitID = -1, HitClosest -- or
+// HitClosestTransparency with opacity_check -- from 0 to INF) and the hit
+// shader over the queue, the two ray / payload halves swapping as the
+// engine's buffers do.  seeds: the hit shader's Uniforms.seed per sample and
+// bounce ((max_bounces + 1) per sample; the engine draws them uniformly).
+// accum: w * h float4, the radiance sums and sample counts (outAccumImage);
+// it must hold the previous samples' sums when first_sample > 0.
+void aeglsl_pt_render(const float* cam, int w, int h, int spp, int first_sample, int max_bounces,
+                      int opacity_check, const float* seeds, float* accum) {
+    namespace T = aeg_pt;
+    const int n_pix = w * h;
+    std::vector<T::PackedRay> ray_buf(size_t(2) * n_pix);
+    std::vector<T::PackedRayPayload> pay_buf(size_t(2) * n_pix);
+    std::vector<vec4> out_image(static_cast<size_t>(n_pix));
+    static uint read_count[1], write_count[1];
+    T::rays = ray_buf.data();
+    T::rayPayloads = pay_buf.data();
+    T::readAtomic = read_count;
+    T::writeAtomic = write_count;
+    T::inAccumImage.texels = reinterpret_cast<vec4*>(accum);
+    T::inAccumImage.width = w;
+    T::outAccumImage = T::inAccumImage;
+    T::outputImage.texels = out_image.data();
+    T::outputImage.width = w;
+    for (int s = 0; s < spp; s++) {
+        const int sample = first_sample + s;
+        const int ints[7] = { w, h, 0, 0, w, h, sample };
+        aeglsl_raygen(cam, ints, reinterpret_cast<float*>(ray_buf.data()), n_pix);
+        int cur = 0;
+        uint n = uint(n_pix);
+        for (int b = 0; b <= max_bounces && n > 0; b++) {
+            for (uint i = 0; i < n; i++) {
+                T::Ray r = T::UnpackRay(ray_buf[size_t(cur) * n_pix + i]);
+                r.hitID = -1;
+                r.hitDistance = 0.0f;
+                if (r.ID >= 0) {
+                    if (opacity_check) T::HitClosestTransparency(r, INSTANCE_MASK_ALL, 0.0f, INF);
+                    else T::HitClosest(r, INSTANCE_MASK_ALL, 0.0f, INF);
+                }
+                ray_buf[size_t(cur) * n_pix + i] = T::PackRay(r);
+            }
+            T::Uniforms.resolution = ivec2(w, h);
+            T::Uniforms.maxBounces = max_bounces;
+            T::Uniforms.sampleCount = sample;
+            T::Uniforms.bounceCount = b;
+            T::Uniforms.seed = seeds[s * (max_bounces + 1) + b];
+            T::Uniforms.exposure = 1.0f;
+            T::Uniforms.samplesPerFrame = 1;
+            T::Uniforms.maxRadiance = 1.0f;
+            T::PushConstants.rayBufferOffset = uint(1 - cur);
+            T::PushConstants.rayPayloadBufferOffset = uint(1 - cur);
+            T::PushConstants.rayBufferSize = uint(n_pix);
+            T::PushConstants.useRayBinning = 0;
+            read_count[0] = n;
+            write_count[0] = 0u;
+            for (uint i = 0; i < n; i++) {
+                gl_GlobalInvocationID = uvec3(i, 0u, 0u);
+                T::aeg_pt_main();
+            }
+            n = write_count[0];
+            cur = 1 - cur;
+        }
+    }
+}
 
 // count draws of random(x, seed) from the seed, per x; out: n * count floats.
 void aeglsl_random(const float* x, int n, float seed0, int count, float* out) {

@@ -261,6 +261,100 @@ def trace_raygen(lib: C.CDLL) -> dict:
     return out
 
 
+# ---- the engine's own path tracer: rayGen.csh, the trace dispatch and
+# rayHit.csh run invocation by invocation (glsl_capi.cpp: aeglsl_pt_render) ----
+
+def single_light(sc):
+    """The scene with one emissive triangle: the others of the emitter are
+    dropped.  The engine's light selection and light sampling draw the same
+    random numbers (direct.hsh: GetLight and SampleLight take the seed by
+    value), which biases its estimator once a scene has two lights; with one
+    light the choice is certain and the estimator is unbiased."""
+    from atlas_rt import BVH
+    emissive = np.any(sc["materials"]["emissiveColor"][sc["obj"]] > 0, axis=1)
+    keep = ~emissive
+    keep[np.nonzero(emissive)[0][0]] = True
+    out = dict(sc, tris=sc["tris"][keep], obj=sc["obj"][keep], normals=sc["normals"][keep])
+    if sc.get("opacity") is not None:
+        out["opacity"] = sc["opacity"][keep]
+    out["bvh"] = BVH(out["tris"])
+    return out
+
+
+def pt_cases():
+    """name -> (scene in ptscene.build's layout, camera dict, width, height,
+    samples, bounces, block): a small terrain + boxes scene under one
+    triangle of the area light (3 bounces), a half-opaque sheet over a floor
+    under one emitter triangle (1 bounce: the transmission branch), and the
+    diffuse floor under its two-triangle emitter (1 bounce), where the
+    engine's correlated light sampling shows."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    sys.path.insert(0, str(REPO / "tests"))
+    from atlas_rt import ptscene, scenes
+    import test_pt_quadrature as Q
+    return {"terrain": (single_light(ptscene.build(grid=48, n_boxes=12)), scenes.pinhole_camera(80, 45), 80, 45,
+                        2048, 3, 5),
+            "sheet": (single_light(Q.pass_through_scene()), Q.camera(), Q.W, Q.H, 8192, 1, 4),
+            "two_lights": (Q.furnace_scene("diffuse"), Q.camera(), Q.W, Q.H, 8192, 1, 4)}
+
+
+def pt_arrays(sc):
+    """The one-instance scene of a ptscene-layout dict in the engine's buffers:
+    (TLAS nodes, instances, model matrices, meshes [(nodes, BVH triangles,
+    shading triangles)], materials, lights) -- what the oracle's path tracer
+    takes too."""
+    import atlas_rt
+    from atlas_rt import BVH, ptscene
+    b = sc["bvh"]
+    gt = b.pack_triangles(sc["obj"], sc.get("opacity"))
+    sh = b.pack_shading(sc["normals"], sc["obj"], sc.get("opacity"))
+    lights = ptscene.lights_for(sc, sh)
+    lo, hi = atlas_rt.mesh_bounds(b)
+    top = BVH(boxes_only=np.concatenate([lo, hi])[None, :])
+    inst = np.array([atlas_rt.make_instance(np.eye(4), 0, atlas_rt.MASK_ALL | atlas_rt.MASK_SHADOW)],
+                    atlas_rt.INSTANCE_DTYPE)
+    ordered = inst[top.order].copy()
+    ordered["nextInstance"] = np.where(top.end_of_node > 0, -1, np.arange(len(ordered)) + 1)
+    model = np.tile(np.eye(3, 4, dtype=F32).reshape(-1), (len(ordered), 1))
+    return (top.nodes_f32.copy(), ordered, model, [(b.nodes_f32.copy(), gt, sh)],
+            np.ascontiguousarray(sc["materials"]), np.ascontiguousarray(lights, F32))
+
+
+def trace_pt(lib: C.CDLL, name: str) -> dict:
+    """The engine's path tracer over one case, one sample per call (the
+    hit shader's seeds drawn uniformly per sample and bounce, as the engine
+    does): the mean image, and per block of pixels the mean and the
+    per-sample variance of the block mean (what a statistical comparison
+    needs)."""
+    sc, camd, w, h, spp, mb, blk = pt_cases()[name]
+    tl, inst, model, meshes, mats, lights = pt_arrays(sc)
+    P = C.c_void_p
+    (nodes, gt, sh), = meshes
+    lib.aeglsl_pt_scene(P(tl.ctypes.data), P(inst.ctypes.data), C.c_int(1), (P * 1)(nodes.ctypes.data),
+                        (P * 1)(gt.ctypes.data), (P * 1)(sh.ctypes.data), P(mats.ctypes.data),
+                        P(lights.ctypes.data), C.c_int(len(lights)))
+    cam = np.concatenate([np.append(camd[k], 0.0) for k in ("origin", "right", "bottom", "location")]).astype(F32)
+    seeds = np.random.default_rng(sum(map(ord, name)) + 20261206).random((spp, mb + 1)).astype(F32)
+    total = np.zeros((h, w, 3))
+    bsum = np.zeros((h // blk, w // blk, 3))
+    bsq = np.zeros_like(bsum)
+    acc = np.zeros((h, w, 4), F32)
+    for s in range(spp):
+        acc[...] = 0.0
+        sd = np.ascontiguousarray(seeds[s])
+        lib.aeglsl_pt_render(P(cam.ctypes.data), C.c_int(w), C.c_int(h), C.c_int(1), C.c_int(s), C.c_int(mb),
+                             C.c_int(1), P(sd.ctypes.data), P(acc.ctypes.data))
+        img = acc[..., :3].astype(np.float64)
+        total += img
+        bm = img[:h // blk * blk, :w // blk * blk].reshape(h // blk, blk, w // blk, blk, 3).mean(axis=(1, 3))
+        bsum += bm
+        bsq += bm * bm
+    bmean = bsum / spp
+    return {f"pt_{name}_mean": (total / spp).astype(F32), f"pt_{name}_block_mean": bmean,
+            f"pt_{name}_block_var": np.maximum(bsq / spp - bmean * bmean, 0.0),
+            f"pt_{name}_spp": np.array([spp, mb, blk], np.int32)}
+
+
 def evaluate(lib: C.CDLL, ins: dict) -> dict:
     P = C.c_void_p
 
@@ -301,7 +395,10 @@ def main():
     ins = inputs()
     sc = traversal_scene()
     trav = trace_scene(lib, sc)
-    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib),
+    pt = {}
+    for name in pt_cases():
+        pt.update(trace_pt(lib, name))
+    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib), **pt,
                         trav_scene_digest=np.frombuffer(scene_digest(sc).encode(), np.uint8))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

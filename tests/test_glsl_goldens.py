@@ -5,8 +5,11 @@ GLSL helpers -- UpdateSurface, EvaluateDiffuseBRDF / EvaluateSpecularBRDF,
 SampleDiffuseBRDF / SampleSpecularBRDF (GGX VNDF), SampleTriangleLight,
 IntersectTriangle / IntersectAABB, the engine's random(), the software
 scene traversals HitClosest / HitAny / HitClosestTransparency /
-HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene, and
-the path tracer's ray generation (pathtracer/rayGen.csh, whole dispatches) --
+HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene, the
+path tracer's ray generation (pathtracer/rayGen.csh, whole dispatches), and
+the engine's whole path tracer (rayGen.csh, the trace dispatch and
+pathtracer/rayHit.csh, bounce by bounce; block statistics of thousands of its
+samples) --
 compiled unmodified on the host by oracle/glsl/make_ref.py.  Here the oracle's
 restatement (CPU) and the path tracer's and traversal's own device functions
 (GPU, through ae_rt_selftest_shading) are held to them: the intersections bit
@@ -42,6 +45,9 @@ def test_fixture_is_what_the_reference_writes():
         assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
     for k, v in G.trace_raygen(lib).items():
         assert np.array_equal(v.view(np.uint32), g[k].view(np.uint32)), k
+    for name in G.pt_cases():
+        for k, v in G.trace_pt(lib, name).items():
+            assert np.array_equal(np.asarray(v, g[k].dtype), g[k]), k
 
 
 def test_reference_random_is_the_documented_hash():
@@ -299,3 +305,87 @@ def test_gpu_raygen_matches_reference_raygen(w, h):
     np.testing.assert_array_equal(got[:, 0:3].view(np.uint32), rays[:, 0:3].view(np.uint32))
     ulps = np.abs(got[:, 4:7].view(np.int32).astype(np.int64) - rays[:, 4:7].view(np.int32))
     assert ulps.max() <= 1, ulps.max()
+
+
+# ---- the engine's own path tracer: rayGen.csh, the trace dispatch and
+# rayHit.csh compiled on the host, run invocation by invocation ----
+
+def pt_case(name):
+    G = _generator()
+    g = S.golden()
+    sc, camd, w, h, _, _, _ = G.pt_cases()[name]
+    spp, mb, blk = (int(x) for x in g[f"pt_{name}_spp"])
+    return G, sc, camd, w, h, spp, mb, blk, g[f"pt_{name}_block_mean"], g[f"pt_{name}_block_var"]
+
+
+def check_against_engine(name, img, n):
+    """img: an image averaged over n samples of another estimator of the same
+    expectation.  Per block of pixels, its mean against the engine's (the
+    golden), in units of the standard error of the difference (the engine's
+    per-sample block variance over both sample counts): the z values of an
+    unbiased match are standard normal."""
+    G, sc, camd, w, h, spp, mb, blk, bm, bv = pt_case(name)
+    ob = img[:h // blk * blk, :w // blk * blk].reshape(h // blk, blk, w // blk, blk, 3).mean(axis=(1, 3))
+    sig = np.sqrt(bv / spp + bv / n)
+    live = sig > 0
+    assert np.allclose(ob[~live], bm[~live], atol=1e-9)       # blocks that only ever see the black sky
+    z = (ob[live] - bm[live]) / sig[live]
+    assert z.size > 40
+    assert (z ** 2).mean() < 1.6 and np.abs(z).max() < 5.0, ((z ** 2).mean(), np.abs(z).max())
+
+
+@pytest.mark.parametrize("name", ["terrain", "sheet"])
+def test_oracle_path_tracer_matches_the_engines_estimator(name):
+    """The oracle's path tracer against the engine's own (rayGen.csh + the
+    trace dispatch + rayHit.csh, compiled unmodified on the host; the golden
+    holds 2,048 / 8,192 of its samples): the same expectation per block of
+    pixels, within the noise -- 3 bounces over terrain and boxes with glossy
+    and diffuse materials, and the transmission branch through a half-opaque
+    sheet.  The scenes have one light triangle (see the two-light test)."""
+    import pyoracle
+    G, sc, camd, w, h, spp, mb, blk, bm, bv = pt_case(name)
+    tl, inst, model, meshes, mats, lights = G.pt_arrays(sc)
+    camv = np.concatenate([camd["location"], camd["origin"], camd["right"], camd["bottom"]]).astype(np.float32)
+    n = 8192 if name == "terrain" else 65536
+    img = pyoracle.pathtrace(tl, inst, model, meshes, mats, lights, camv, w, h, n, max_bounces=mb) / n
+    check_against_engine(name, img, n)
+
+
+def test_engine_estimator_is_biased_with_two_lights():
+    """A documented deviation.  The engine's GetLight and SampleLight
+    (direct.hsh:12-86) take the random seed by value, so the light choice
+    and the point sampled on the chosen light draw the same numbers; with two
+    lights each light triangle is sampled over part of itself only.  Over the
+    diffuse floor under its two-triangle emitter the engine's own estimator
+    (golden) sits 12 % below the quadrature of the direct light, while the
+    library's estimator, whose draws are independent, meets it (the
+    quadrature tests); with one light triangle the two agree (above)."""
+    import test_pt_quadrature as Q
+    g = S.golden()
+    ref = g["pt_two_lights_block_mean"][..., 0].mean()
+    expected = Q.expected_for("diffuse").mean()
+    assert 0.86 < ref / expected < 0.90, ref / expected
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["terrain", "sheet"])
+def test_gpu_path_tracer_matches_the_engines_estimator(name):
+    """The GPU path tracer against the engine's own estimator, as the oracle
+    above: same scenes, same block statistics."""
+    import atlas_rt
+    import torch
+    from atlas_rt import ptscene
+    G, sc, camd, w, h, spp, mb, blk, bm, bv = pt_case(name)
+    n = 32768 if name == "terrain" else 65536
+    ctx = atlas_rt.Context(device=0)
+    try:
+        ptscene.upload(ctx, sc)
+        cam = atlas_rt.make_camera(camd)
+        acc = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+        acc64 = torch.zeros((w * h, 3), dtype=torch.float64, device="cuda")
+        ctx.pathtrace(cam, acc, acc64, spp=n, max_bounces=mb)
+        ctx.synchronize()
+        img = acc64.cpu().numpy().reshape(h, w, 3) / n
+    finally:
+        ctx.close()
+    check_against_engine(name, img, n)
