@@ -521,8 +521,9 @@ class Context:
     def _gbuffer(gb: dict):
         """ae_gbuffer from a dict of device tensors: depth (h, w), normal
         (h, w, 2), optional offset (h, w) uint8, roughness (h, w), samples
-        (h, w, 2); ip_matrix / iv_matrix as 4x4 row-major arrays (stored
-        column-major, like GLSL); half_res."""
+        (h, w, 2), the blue-noise textures scrambling_ranking (128, 128, 4)
+        and sobol_sequence (256, 4) uint8; ip_matrix / iv_matrix as 4x4
+        row-major arrays (stored column-major, like GLSL); half_res."""
         g = GBuffer()
         depth = gb["depth"]
         g.height, g.width = int(depth.shape[0]), int(depth.shape[1])
@@ -532,6 +533,11 @@ class Context:
         for name in ("ip_matrix", "iv_matrix"):
             m = np.asarray(gb[name], np.float32).reshape(4, 4)
             getattr(g, name)[:] = list(m.T.reshape(-1))
+        for name, shape in (("scrambling_ranking", (128, 128, 4)), ("sobol_sequence", (256, 4))):
+            t = gb.get(name)
+            if t is not None and tuple(t.shape) != shape:
+                raise ValueError(f"{name} must have shape {shape}")
+            setattr(g, name, _ptr(t))
         return g
 
     @staticmethod

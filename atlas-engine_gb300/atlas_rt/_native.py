@@ -84,7 +84,7 @@ class RcConfig(C.Structure):
 class GBuffer(C.Structure):
     _fields_ = [("depth", P), ("normal", P), ("offset", P), ("roughness", P), ("samples", P), ("width", U32),
                 ("height", U32), ("half_res", U32), ("reserved", U32), ("ip_matrix", F32 * 16),
-                ("iv_matrix", F32 * 16)]
+                ("iv_matrix", F32 * 16), ("scrambling_ranking", P), ("sobol_sequence", P)]
 
 
 class PassParams(C.Structure):

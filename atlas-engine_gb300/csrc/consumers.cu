@@ -43,9 +43,25 @@ struct GbParams {
     const uint8_t* offset;
     const float* rough;
     const float2* samples;
+    const uchar4* ranking;   // blue-noise scrambling / ranking texture, 128 x 128
+    const uchar4* sobol;     // blue-noise Sobol sequence, 256 x 1
     uint32_t w, h, half_res;
     float ip[16], iv[16];
 };
+
+// SampleBlueNoise of common/bluenoise.hsh:9-32 (Heitz, Belcour, Ostromoukhov,
+// Coeurjolly, Iehl 2019) for dimensions 0 and 1 of one pixel.  The shader
+// reads the RGBA8 texels as unorm floats c / 255 and takes
+// int(clamp(c / 255 * 256, 0, 255)); c / 255 * 256 = c + c / 255 lies in
+// [c, c + 1) for c <= 254 and clamps to 255 for c = 255, so that integer is
+// the byte itself, which is what this reads.
+__device__ __forceinline__ void blue_noise(const GbParams& g, uint32_t px, uint32_t py, uint32_t index,
+                                           float& u0, float& u1) {
+    const uchar4 r = g.ranking[(py & 127u) * 128u + (px & 127u)];
+    const uchar4 s = g.sobol[(index & 255u) ^ r.z];
+    u0 = (0.5f + float(uint32_t(s.x) ^ r.x)) / 256.0f;
+    u1 = (0.5f + float(uint32_t(s.y) ^ r.y)) / 256.0f;
+}
 
 struct PassP {
     float radius, bias, cutoff, limit;
@@ -149,6 +165,8 @@ __global__ void gb_raygen_kernel(GbParams g, PassP pp, Queue q, float* ao_out, f
                     const float2 s = g.samples[pix];
                     u0 = s.x;
                     u1 = s.y;
+                } else if (g.ranking) {
+                    blue_noise(g, px, py, pp.frame_seed, u0, u1);
                 } else {
                     u0 = rng(pix, pp.frame_seed, kSampleSlot, 0, pp.seed);
                     u1 = rng(pix, pp.frame_seed, kSampleSlot, 1, pp.seed);
@@ -411,8 +429,13 @@ ae_rt_status CheckGBuffer(ae_rt_ctx* ctx, const ae_gbuffer* gb, bool need_rough)
         return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^26 pixels");
     for (const void* ptr : { static_cast<const void*>(gb->depth), static_cast<const void*>(gb->normal),
                              static_cast<const void*>(gb->offset), static_cast<const void*>(gb->roughness),
-                             static_cast<const void*>(gb->samples) })
+                             static_cast<const void*>(gb->samples), static_cast<const void*>(gb->scrambling_ranking),
+                             static_cast<const void*>(gb->sobol_sequence) })
         if (ptr && !IsDevicePointer(ptr)) return Fail(ctx, AE_RT_INVALID_ARG, "G-buffer planes must be device memory");
+    if (!gb->scrambling_ranking != !gb->sobol_sequence)
+        return Fail(ctx, AE_RT_INVALID_ARG, "the blue-noise ranking and Sobol textures come together");
+    if ((reinterpret_cast<uintptr_t>(gb->scrambling_ranking) | reinterpret_cast<uintptr_t>(gb->sobol_sequence)) & 3u)
+        return Fail(ctx, AE_RT_INVALID_ARG, "the blue-noise textures must be 4-byte aligned");
     return AE_RT_OK;
 }
 
@@ -436,6 +459,8 @@ GbParams GBuffer(const ae_gbuffer* gb) {
     g.offset = gb->offset;
     g.rough = gb->roughness;
     g.samples = reinterpret_cast<const float2*>(gb->samples);
+    g.ranking = reinterpret_cast<const uchar4*>(gb->scrambling_ranking);
+    g.sobol = reinterpret_cast<const uchar4*>(gb->sobol_sequence);
     g.w = gb->width;
     g.h = gb->height;
     g.half_res = gb->half_res ? 1u : 0u;

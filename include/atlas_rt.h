@@ -803,13 +803,23 @@ ae_rt_status ae_rt_pt_tonemap_tile(ae_rt_ctx* ctx, const float* accum, uint32_t 
  *   roughness  one float per pixel, the material roughness after its map
  *              (reflections only; rtreflection.csh:92-96);
  *   samples    optional two floats per pixel in [0, 1): the shader's
- *              blue-noise vector; NULL = the library's PCG hash of (pixel,
- *              frame_seed);
+ *              blue-noise vector; NULL = drawn as below;
  *   ip_matrix, iv_matrix  inverse projection and inverse view, column-major
  *              like GLSL's mat4 (globalData.ipMatrix / ivMatrix);
  *   half_res   1: this buffer has half the depth buffer's resolution, and
  *              positions are reconstructed at 2*pixel + offset + 0.5 of the
  *              full one (ao/rtao.csh:66, rtreflection.csh:75-79).
+ *   scrambling_ranking, sobol_sequence  optional, both or neither: the
+ *              engine's blue-noise textures as RGBA8 texels, 128 x 128 and
+ *              256 x 1 (the scramblingRankingTexture / sobolSequenceTexture
+ *              that rtao.csh, rtreflection.csh and rtgi.csh bind).  When
+ *              `samples` is NULL and these are given, the pixel's vector is
+ *              (SampleBlueNoise(pixel, frame_seed, 0), SampleBlueNoise(pixel,
+ *              frame_seed, 1)) of common/bluenoise.hsh:9-32 (Heitz et al.
+ *              2019): pixel mod 128, sample index mod 256, ranked index =
+ *              index ^ ranking.b, value = sobol[ranked][dim] ^
+ *              ranking[dim], (value + 0.5) / 256; without them, the
+ *              library's PCG hash of (pixel, frame_seed).
  * World position = iv * (ConvertDepthToViewSpace: ip * (2*tc - 1, depth, 1),
  * divided by w); world normal = normalize(iv * (DecodeNormal(normal), 0)). */
 typedef struct ae_gbuffer {
@@ -824,6 +834,8 @@ typedef struct ae_gbuffer {
     uint32_t reserved;
     float ip_matrix[16];
     float iv_matrix[16];
+    const uint8_t* scrambling_ranking;
+    const uint8_t* sobol_sequence;
 } ae_gbuffer;
 
 #define AE_PASS_OPACITY_CHECK 0x1u   /* trace with the transparency variants (OPACITY_CHECK) */

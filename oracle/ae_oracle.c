@@ -1617,6 +1617,24 @@ static v3 decode_oct(float cx, float cy) {
     return vnorm(mk(cx, y, cy));
 }
 
+/* SampleBlueNoise, common/bluenoise.hsh:9-32 (Heitz, Belcour, Ostromoukhov,
+ * Coeurjolly, Iehl 2019), with the RGBA8 textures read as unorm floats
+ * (c / 255) the way the shader's sampler returns them. */
+static int blue_noise_texel(const uint8_t* t, int index, int channel) {
+    float v = (float)t[(size_t)index * 4 + channel] / 255.0f * 256.0f;
+    return (int)(v < 0.0f ? 0.0f : (v > 255.0f ? 255.0f : v));
+}
+
+static float blue_noise(const aeo_gbuffer* g, uint32_t px, uint32_t py, int sample_index, int dim) {
+    int pixel = (int)((py % 128u) * 128u + (px % 128u));
+    sample_index = sample_index % 256;
+    dim = dim % 4;
+    int ranked = sample_index ^ blue_noise_texel(g->scrambling_ranking, pixel, 2);
+    int value = blue_noise_texel(g->sobol_sequence, ranked, dim);
+    value = value ^ blue_noise_texel(g->scrambling_ranking, pixel, dim % 2);
+    return (0.5f + (float)value) / 256.0f;
+}
+
 static void frame_of(v3 N, v3* t, v3* b, int normalize_b) {
     v3 up = fabsf(N.z) < 0.999f ? mk(0, 0, 1) : mk(1, 0, 0);
     *t = vnorm(vcross(up, N));
@@ -1737,6 +1755,11 @@ static void pass_pixel(const pass_job_t* p, uint32_t pix, int32_t* stack) {
         if (g->samples) {
             u0 = g->samples[(size_t)pix * 2];
             u1 = g->samples[(size_t)pix * 2 + 1];
+        } else if (g->scrambling_ranking) {
+            /* int(frameSeed) % 256 for seeds below 2^31; above, the shader's
+             * index is negative (a texel fetch out of range) */
+            u0 = blue_noise(g, px, py, (int)(pp->frame_seed % 256u), 0);
+            u1 = blue_noise(g, px, py, (int)(pp->frame_seed % 256u), 1);
         } else {
             u0 = prng(pix, pp->frame_seed, PASS_SAMPLE_SLOT, 0, pp->seed);
             u1 = prng(pix, pp->frame_seed, PASS_SAMPLE_SLOT, 1, pp->seed);

@@ -199,8 +199,9 @@ void aeo_scene_any_transparency_glsl(const aeo_node* tlas, uint32_t n_tlas, cons
 
 /* The traversal's other consumers -- ao/rtao.csh, reflection/rtreflection.csh,
  * rtgi/rtgi.csh, ddgi/rayGen.csh + rayHit.csh -- restated per pixel / probe
- * ray with the library's random streams (pixel samples: PCG hash slot 13 of
- * (pixel, frame_seed) unless `samples` is given; light choices: slot 14 keyed
+ * ray with the library's random streams (pixel samples: `samples` if given,
+ * else the engine's SampleBlueNoise over the two blue-noise textures if
+ * given, else PCG hash slot 13 of (pixel, frame_seed); light choices: slot 14 keyed
  * by the pixel or probe-ray index).  Structs mirror the library's
  * ae_gbuffer, ae_rt_pass_params and ae_ddgi_probes (host memory here). */
 typedef struct aeo_gbuffer {
@@ -211,6 +212,8 @@ typedef struct aeo_gbuffer {
     const float* samples;
     uint32_t width, height, half_res, reserved;
     float ip_matrix[16], iv_matrix[16];
+    const uint8_t* scrambling_ranking;   /* blue-noise textures, RGBA8: 128 x 128 */
+    const uint8_t* sobol_sequence;       /* and 256 x 1 (used when samples is NULL) */
 } aeo_gbuffer;
 
 typedef struct aeo_pass_params {

@@ -20,8 +20,10 @@
 //    dot as a left-to-right sum, normalize(x) = x / length(x);
 //  * textures as arrays of RGBA float texels: texelFetch, textureSize, and
 //    textureLod with the engine's bindless sampler (linear filtering, repeat
-//    addressing) evaluated with exact weights; images and atomics as plain
-//    memory, for the one invocation the goldens run.
+//    addressing) evaluated with exact weights, or a render target's sampler
+//    (clamp to edge, weights rounded to the filter's sub-texel precision);
+//    integer textures (isampler2D); images and atomics as plain memory, for
+//    the one invocation the goldens run.
 //
 // All arithmetic is single precision (the recipe suffixes GLSL's float
 // literals with f) and is compiled with -ffp-contract=off, so every
@@ -151,6 +153,8 @@ GLSL_VEC_OPS(ivec4, int, 4)
 GLSL_VEC_OPS(uvec2, uint, 2)
 GLSL_VEC_OPS(uvec3, uint, 3)
 GLSL_VEC_OPS(uvec4, uint, 4)
+// GLSL's implicit int -> float conversion of an operand (section 4.1.10)
+inline vec2 operator+(const vec2& a, const ivec2& b) { return a + vec2(b); }
 inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
 inline ivec2 operator%(const ivec2& a, int b) { return ivec2(a.x % b, a.y % b); }
 
@@ -365,6 +369,11 @@ struct glsl_texture2D {
 struct glsl_sampler {};
 struct glsl_sampler2D {
     const glsl_texture2D* tex = nullptr;
+    // addressing and filter precision of a bound sampler: repeat and exact
+    // weights by default; a render target's sampler clamps to the edge, and
+    // filtering hardware weighs neighbours with subtexel_bits of fraction
+    bool clamp_to_edge = false;
+    int subtexel_bits = 0;
     glsl_sampler2D() {}
     glsl_sampler2D(const glsl_texture2D& t, const glsl_sampler&) : tex(&t) {}
 };
@@ -387,18 +396,35 @@ inline vec4 textureLod(const sampler2D& s, const vec2& uv, float) {
     const int w = s.tex->width, h = s.tex->height;
     const float x = uv.x * float(w) - 0.5f, y = uv.y * float(h) - 0.5f;
     const float fx = floor(x), fy = floor(y);
-    const float ax = x - fx, ay = y - fy;
-    auto wrap = [](int i, int n) { int m = i % n; return m < 0 ? m + n : m; };
+    float ax = x - fx, ay = y - fy;
+    if (s.subtexel_bits > 0) {
+        const float q = float(1 << s.subtexel_bits);
+        ax = __builtin_nearbyintf(ax * q) / q;
+        ay = __builtin_nearbyintf(ay * q) / q;
+    }
+    const bool clamp_edge = s.clamp_to_edge;
+    auto wrap = [clamp_edge](int i, int n) {
+        if (clamp_edge) return i < 0 ? 0 : (i >= n ? n - 1 : i);
+        int m = i % n;
+        return m < 0 ? m + n : m;
+    };
     const int x0 = wrap(int(fx), w), x1 = wrap(int(fx) + 1, w), y0 = wrap(int(fy), h), y1 = wrap(int(fy) + 1, h);
     const vec4 t00 = texelFetch(s, ivec2(x0, y0), 0), t10 = texelFetch(s, ivec2(x1, y0), 0);
     const vec4 t01 = texelFetch(s, ivec2(x0, y1), 0), t11 = texelFetch(s, ivec2(x1, y1), 0);
     return t00 * ((1.0f - ax) * (1.0f - ay)) + t10 * (ax * (1.0f - ay)) + t01 * ((1.0f - ax) * ay) + t11 * (ax * ay);
 }
 inline vec4 textureLod(const samplerCube&, const vec3&, float) { return vec4(0.0f); }
+// an integer texture, one channel per texel (r; g, b = 0, a = 1)
+struct isampler2D {
+    const int* texels = nullptr;
+    int width = 0, height = 0;
+};
+inline ivec4 texelFetch(const isampler2D& s, const ivec2& p, int) { return ivec4(s.texels[p.y * s.width + p.x], 0, 0, 1); }
 inline vec4 texture(const sampler2D& s, const vec2& uv) { return s.tex ? textureLod(s, uv, 0.0f) : vec4(0.0f); }
 
 // ---- images, atomics and invocation ids, for one invocation ----
-struct image2D { vec4* texels = nullptr; int width = 0; };
+struct image2D { vec4* texels = nullptr; int width = 0, height = 0; };
+inline ivec2 imageSize(const image2D& im) { return ivec2(im.width, im.height); }
 struct uimage2D { uvec4* texels = nullptr; int width = 0; };
 struct uimage2DArray { uint* texels = nullptr; int width = 0, height = 0; };
 inline void imageStore(image2D& im, const ivec2& p, const vec4& v) { if (im.texels) im.texels[p.y * im.width + p.x] = v; }

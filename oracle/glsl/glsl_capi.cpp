@@ -18,10 +18,16 @@
 //   the engine's path tracer, sample by sample: rayGen.csh, the trace
 //   dispatch (traceClosest.csh:12-36) and the hit shader, bounce by bounce
 //                                            pathtracer/rayHit.csh:54-338
+//   the ambient-occlusion pass, one dispatch over a G-buffer (with and
+//   without OPACITY_CHECK), and its blue-noise sampler
+//                                            ao/rtao.csh:40-112,
+//                                            common/bluenoise.hsh:9-32
 #include "glsl.hpp"
 #include "glsl_ref.inc"
 #include "glsl_raygen.inc"
 #include "glsl_pt.inc"
+#include "glsl_rtao.inc"
+#include "glsl_rtao_opacity.inc"
 
 using namespace aeg_glsl;
 
@@ -158,6 +164,20 @@ void aeglsl_scene(const void* tlas, const void* instances, int n_meshes, const v
         g_textures[i].height = wh[2 * i + 1];
     }
     bindlessTextures = g_textures.data();
+    // the ambient-occlusion programs trace the same scene
+#define AEG_SCENE_INTO(T)                                                  \
+    T::tlasNodes = (T::PackedBVHNode*)tlas;                                \
+    T::bvhInstances = (T::Instance*)instances;                             \
+    for (int m = 0; m < n_meshes; m++) {                                   \
+        T::blasNodes[m].data = (T::PackedBVHNode*)nodes[m];                \
+        T::bvhTriangles[m].data = (T::PackedBVHTriangle*)bvh_tris[m];      \
+        T::triangles[m].data = (T::PackedTriangle*)tris[m];                \
+    }                                                                      \
+    T::materials = (T::RaytraceMaterial*)mats;                             \
+    T::bindlessTextures = g_textures.data();
+    AEG_SCENE_INTO(aeg_rtao)
+    AEG_SCENE_INTO(aeg_rtao_opacity)
+#undef AEG_SCENE_INTO
 }
 
 // kind 0 HitClosest, 1 HitAny, 2 HitClosestTransparency, 3 HitAnyTransparency
@@ -318,6 +338,111 @@ void aeglsl_pt_render(const float* cam, int w, int h, int spp, int first_sample,
             cur = 1 - cur;
         }
     }
+}
+
+namespace {
+
+// A texture of RGBA float texels holding one or two channels per pixel.
+glsl_texture2D Plane(std::vector<float>& texels, const float* src, int channels, int w, int h) {
+    texels.assign(size_t(w) * h * 4, 0.0f);
+    for (size_t i = 0; i < size_t(w) * h; i++) {
+        for (int c = 0; c < channels; c++) texels[i * 4 + c] = src[i * channels + c];
+        texels[i * 4 + 3] = 1.0f;
+    }
+    glsl_texture2D t;
+    t.texels = texels.data();
+    t.width = w;
+    t.height = h;
+    return t;
+}
+
+glsl_texture2D Rgba(const float* texels, int w, int h) {
+    glsl_texture2D t;
+    t.texels = texels;
+    t.width = w;
+    t.height = h;
+    return t;
+}
+
+mat4 ColumnMajor(const float* m) {
+    mat4 r(1.0f);
+    for (int c = 0; c < 4; c++) r.c[c] = vec4(m[4 * c], m[4 * c + 1], m[4 * c + 2], m[4 * c + 3]);
+    return r;
+}
+
+}  // namespace
+
+// One dispatch of ao/rtao.csh over a w x h G-buffer, as AORenderer.cpp:85-114
+// issues it: ceil(w / 8) * ceil(h / 4) work groups of 8 x 4 invocations in a
+// row, which the shader lays onto tiles four groups wide; pixels that no
+// invocation reaches keep their value in `ao`.  Over the scene aeglsl_scene
+// set (HitAny, or HitAnyTransparency with opacity_check).
+//   depth   w * h floats (the depth texture's r; read with texelFetch)
+//   normal  w * h * 2 floats, octahedral (the normal texture's rg; read with
+//           textureLod at the texel's centre through the render target's
+//           sampler: clamp to edge, 8-bit sub-texel filter weights)
+//   offset  w * h ints, 0..3 (the offset texture; texelFetch)
+//   ranking 128 * 128 and sobol 256 RGBA float texels (c / 255 of the
+//           engine's RGBA8 blue-noise textures)
+//   ip, iv  column-major inverse projection and inverse view
+//   ao      w * h floats, in / out
+void aeglsl_rtao(int opacity_check, int w, int h, const float* depth, const float* normal, const int* offset,
+                 const float* ranking, const float* sobol, const float* ip, const float* iv, float radius,
+                 int frame_seed, float* ao) {
+    std::vector<float> depth_texels, normal_texels;
+    const glsl_texture2D depth_tex = Plane(depth_texels, depth, 1, w, h);
+    const glsl_texture2D normal_tex = Plane(normal_texels, normal, 2, w, h);
+    const glsl_texture2D rank_tex = Rgba(ranking, 128, 128), sobol_tex = Rgba(sobol, 256, 1);
+    std::vector<vec4> image(size_t(w) * h);
+    for (size_t i = 0; i < image.size(); i++) image[i] = vec4(ao[i], 0.0f, 0.0f, 0.0f);
+    const int gx = (w + 7) / 8, gy = (h + 3) / 4;
+#define AEG_RTAO_RUN(T)                                                                    \
+    T::rtaoImage.texels = image.data();                                                    \
+    T::rtaoImage.width = w;                                                                \
+    T::rtaoImage.height = h;                                                               \
+    T::normalTexture.tex = &normal_tex;                                                    \
+    T::normalTexture.clamp_to_edge = true;                                                 \
+    T::normalTexture.subtexel_bits = 8;                                                    \
+    T::shadowMap.tex = &depth_tex;                                                         \
+    T::offsetTexture.texels = offset;                                                      \
+    T::offsetTexture.width = w;                                                            \
+    T::offsetTexture.height = h;                                                           \
+    T::scramblingRankingTexture.tex = &rank_tex;                                           \
+    T::sobolSequenceTexture.tex = &sobol_tex;                                              \
+    T::uniforms.radius = radius;                                                           \
+    T::uniforms.frameSeed = frame_seed;                                                    \
+    T::globalData.ipMatrix = ColumnMajor(ip);                                              \
+    T::globalData.ivMatrix = ColumnMajor(iv);                                              \
+    gl_NumWorkGroups = uvec3(uint(gx * gy), 1u, 1u);                                       \
+    for (int g = 0; g < gx * gy; g++)                                                      \
+        for (uint ly = 0; ly < 4u; ly++)                                                   \
+            for (uint lx = 0; lx < 8u; lx++) {                                             \
+                gl_WorkGroupID = uvec3(uint(g), 0u, 0u);                                   \
+                gl_LocalInvocationID = uvec3(lx, ly, 0u);                                  \
+                gl_LocalInvocationIndex = ly * 8u + lx;                                    \
+                gl_GlobalInvocationID = uvec3(uint(g) * 8u + lx, ly, 0u);                  \
+                T::T##_main();                                                             \
+            }
+    if (opacity_check) {
+        AEG_RTAO_RUN(aeg_rtao_opacity)
+    } else {
+        AEG_RTAO_RUN(aeg_rtao)
+    }
+#undef AEG_RTAO_RUN
+    for (size_t i = 0; i < image.size(); i++) ao[i] = image[i].x;
+}
+
+// SampleBlueNoise(pixel, sample_index, 0 and 1) for every pixel of a w x h
+// image: out w * h * 2 floats (the blueNoiseVec of rtao.csh:82-86).
+void aeglsl_blue_noise(int w, int h, const float* ranking, const float* sobol, int sample_index, float* out) {
+    const glsl_texture2D rank_tex = Rgba(ranking, 128, 128), sobol_tex = Rgba(sobol, 256, 1);
+    sampler2D rank_s, sobol_s;
+    rank_s.tex = &rank_tex;
+    sobol_s.tex = &sobol_tex;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            for (int d = 0; d < 2; d++)
+                out[(size_t(y) * w + x) * 2 + d] = aeg_rtao::SampleBlueNoise(ivec2(x, y), sample_index, d, rank_s, sobol_s);
 }
 
 // count draws of random(x, seed) from the seed, per x; out: n * count floats.

@@ -17,6 +17,7 @@ language-level adjustments are applied:
     `T& x` (GLSL's copy-out semantics, expressed as C++ references);
   * float literals get an `f` suffix (a GLSL float literal is single
     precision, a C++ one double);
+  * an array constructor `T[N](a, b, ...)` becomes the brace list `{a, b, ...}`;
   * resource declarations (`layout(...)`, storage `buffer` blocks, `uniform`
     blocks and variables, `shared` arrays) become plain globals: a buffer
     block's runtime-sized arrays become pointers, an array of buffer blocks
@@ -26,9 +27,10 @@ language-level adjustments are applied:
     replaced by the resources the helpers name: the DFG lookup texture and
     the bindless texture table with its sampler.
 
-Each program's flattened source goes to oracle/_ref/<program>.inc (the
-compute shaders rayGen.csh and rayHit.csh each in a namespace of its own, their
-`main` renamed <namespace>_main), and glsl_capi.cpp includes them all; it is
+Each program's flattened source goes to oracle/_ref/<program>.inc (every
+program in a namespace of its own, the compute shaders' `main` renamed
+<namespace>_main; rayGen.csh, rayHit.csh and rtao.csh, the last twice: with
+and without OPACITY_CHECK), and glsl_capi.cpp includes them all; it is
 compiled (-O2 -ffp-contract=off) into oracle/_ref/libglslref.so.  Usage: python make_ref.py [REFERENCE_ROOT]
 """
 from __future__ import annotations
@@ -44,29 +46,39 @@ OUT_DIR = ORACLE / "_ref"
 # Programs, each in a namespace of its own (a compute shader brings its own
 # `main`, uniform block and buffers; and the shim's types live in the global
 # namespace, so argument-dependent lookup must not see two programs'
-# functions): the helpers, the path tracer's ray generation and its hit shader.
+# functions): the helpers, the path tracer's ray generation and its hit
+# shader, and the ambient-occlusion pass in its two variants (the engine
+# compiles rtao.csh with or without OPACITY_CHECK, AORenderer.cpp:89).
+# Entries: namespace, files, macros defined for the program alone.
 PROGRAMS = {
     "glsl_ref": ("aeg_glsl", ["brdf/brdfSample.hsh", "raytracer/lights.hsh", "raytracer/intersections.hsh",
-                        "raytracer/bvh.hsh", "raytracer/direct.hsh"]),
-    "glsl_raygen": ("aeg_raygen", ["pathtracer/rayGen.csh"]),
-    "glsl_pt": ("aeg_pt", ["pathtracer/rayHit.csh"]),
+                        "raytracer/bvh.hsh", "raytracer/direct.hsh"], []),
+    "glsl_raygen": ("aeg_raygen", ["pathtracer/rayGen.csh"], []),
+    "glsl_pt": ("aeg_pt", ["pathtracer/rayHit.csh"], []),
+    "glsl_rtao": ("aeg_rtao", ["ao/rtao.csh"], []),
+    "glsl_rtao_opacity": ("aeg_rtao_opacity", ["ao/rtao.csh"], ["OPACITY_CHECK"]),
 }
 # The engine compiles its shaders with bindless resources (AE_BINDLESS: one
 # buffer per mesh) and, where registers allow, the traversal stack in local
 # memory (LOCAL_STACK, bvh.hsh:39-42); compute shaders see one invocation.
 PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
-# rayGen.csh's work-group size (layout(local_size_x = 8, local_size_y = 8))
-WORKGROUP = {"aeg_raygen": "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n"}
+# the compute shaders' work-group sizes (rayGen.csh: local_size 8 x 8;
+# rtao.csh: 8 x 4)
+WORKGROUP = {"aeg_raygen": "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n",
+             "aeg_rtao": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_rtao_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n"}
 GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
                 "static glsl_texture2D* bindlessTextures = nullptr;\n"
                 "static glsl_sampler bindlessSampler;\n"
-                # the members of globals.hsh's GlobalBuffer that rayGen.csh reads
-                "struct GlobalBufferStub { vec2 jitterCurrent; vec4 cameraLocation; };\n"
+                # the members of globals.hsh's GlobalBuffer that rayGen.csh,
+                # rtao.csh and convert.hsh read
+                "struct GlobalBufferStub { vec2 jitterCurrent; vec4 cameraLocation; mat4 ivMatrix; "
+                "mat4 ipMatrix; };\n"
                 "static GlobalBufferStub globalData;\n")
 
 _INCLUDE = re.compile(r'^\s*#include\s*<([^>]+)>\s*$')
 _FLOAT = re.compile(r'(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])')
-_QUAL = re.compile(r'\b(inout|out|in)\s+([A-Za-z_]\w*)\s+([A-Za-z_]\w*)')
+_QUAL = re.compile(r'\b(inout|out|in)[ \t]+([A-Za-z_]\w*)[ \t]+([A-Za-z_]\w*)')
 _LAYOUT = re.compile(r'\blayout\s*\([^)]*\)\s*')
 _BUFFER = re.compile(r'\bbuffer\s+\w+\s*\{([^}]*)\}\s*;', re.S)
 _BUFFER_ARRAY = re.compile(r'\bbuffer\s+(\w+)\s*\{([^}]*)\}\s*(\w+)\s*\[([^\]]*)\]\s*;', re.S)
@@ -74,6 +86,7 @@ _UNIFORM_BLOCK = re.compile(r'\buniform\s+(\w+)\s*\{')
 _UNIFORM_VAR = re.compile(r'^(\s*)(?:readonly\s+|writeonly\s+)*uniform\s+(\w+\s+\w+(?:\s*\[[^\]]*\])?\s*;)', re.M)
 _SHARED = re.compile(r'^(\s*)shared\s+', re.M)
 _LAYOUT_IN = re.compile(r'^\s*in\s*;\s*$', re.M)
+_ARRAY_CTOR = re.compile(r'=\s*\w+\s*\[\s*\d*\s*\]\s*\((.*?)\);', re.S)
 
 
 def _flatten(path: Path, seen: set, shader_root: Path) -> str:
@@ -128,6 +141,8 @@ def to_cpp(src: str) -> str:
     src = _UNIFORM_BLOCK.sub(lambda m: f"struct {m.group(1)} {{", src)
     src = _UNIFORM_VAR.sub(lambda m: f"{m.group(1)}static {m.group(2)}", src)
     src = _SHARED.sub(lambda m: f"{m.group(1)}static ", src)
+    # an array constructor `T[N](a, b, ...)` initialises like a brace list
+    src = _ARRAY_CTOR.sub(lambda m: "= {" + m.group(1) + "};", src)
     src = _FLOAT.sub(lambda m: m.group(1) + "f", src)
     return src
 
@@ -136,13 +151,13 @@ def build(reference_root: Path) -> Path:
     shader_root = reference_root / "data" / "shader"
     OUT_DIR.mkdir(exist_ok=True)
     header = "// generated by oracle/glsl/make_ref.py from the reference's shader files; do not edit\n"
-    for name, (ns, files) in PROGRAMS.items():
+    for name, (ns, files, macros) in PROGRAMS.items():
         seen: set = set()
         body = to_cpp("".join(_flatten(shader_root / f, seen, shader_root) for f in files))
-        if ns:
-            # the program's entry point becomes <namespace>_main
-            body = (f"namespace {ns} {{\n#define main {ns}_main\n" + WORKGROUP.get(ns, "") + body +
-                    f"\n#undef main\n}}  // namespace {ns}\n")
+        # the program's entry point becomes <namespace>_main
+        body = (f"namespace {ns} {{\n#define main {ns}_main\n" + "".join(f"#define {m}\n" for m in macros) +
+                WORKGROUP.get(ns, "") + body + "".join(f"\n#undef {m}" for m in macros) +
+                f"\n#undef main\n}}  // namespace {ns}\n")
         (OUT_DIR / f"{name}.inc").write_text(header + PREAMBLE + body)
     lib = OUT_DIR / "libglslref.so"
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fno-builtin",

@@ -593,7 +593,7 @@ def ref_build_aabbs(boxes, parallel=True):
 class _GBuffer(C.Structure):
     _fields_ = [("depth", P), ("normal", P), ("offset", P), ("roughness", P), ("samples", P), ("width", U32),
                 ("height", U32), ("half_res", U32), ("reserved", U32), ("ip_matrix", C.c_float * 16),
-                ("iv_matrix", C.c_float * 16)]
+                ("iv_matrix", C.c_float * 16), ("scrambling_ranking", P), ("sobol_sequence", P)]
 
 
 class _PassParams(C.Structure):
@@ -655,7 +655,8 @@ def _gbuffer(gb):
     g = _GBuffer()
     g.height, g.width = depth.shape[0], depth.shape[1]
     g.depth, g.normal = depth.ctypes.data, normal.ctypes.data
-    for name, dt in (("offset", np.uint8), ("roughness", np.float32), ("samples", np.float32)):
+    for name, dt in (("offset", np.uint8), ("roughness", np.float32), ("samples", np.float32),
+                     ("scrambling_ranking", np.uint8), ("sobol_sequence", np.uint8)):
         if gb.get(name) is not None:
             a = np.ascontiguousarray(gb[name], dt)
             keep.append(a)
@@ -664,6 +665,21 @@ def _gbuffer(gb):
     for name in ("ip_matrix", "iv_matrix"):
         getattr(g, name)[:] = list(np.asarray(gb[name], np.float32).reshape(4, 4).T.reshape(-1))
     return g, keep
+
+
+def blue_noise(ranking, sobol, width, height, sample_index):
+    """SampleBlueNoise (common/bluenoise.hsh:9-32) for dimensions 0 and 1 of
+    every pixel of a width x height image -> (height, width, 2) float32.
+    ranking: (128, 128, 4) and sobol: (256, 4) uint8 RGBA texels, read as the
+    shader's sampler returns them (c / 255) and scaled by 256 as it does."""
+    def texel(t):
+        v = np.asarray(t, np.uint8).astype(np.float32) / np.float32(255.0) * np.float32(256.0)
+        return np.clip(v, np.float32(0.0), np.float32(255.0)).astype(np.int32)
+    y, x = np.mgrid[0:height, 0:width]
+    r = texel(ranking)[y % 128, x % 128]
+    s = texel(sobol)[(int(sample_index) % 256) ^ r[..., 2]]
+    v = s[..., :2] ^ r[..., :2]
+    return ((np.float32(0.5) + v.astype(np.float32)) / np.float32(256.0)).astype(np.float32)
 
 
 def pass_screen(kind, scene, gbuffer, threads=os.cpu_count(), **params):

@@ -376,6 +376,207 @@ def evaluate(lib: C.CDLL, ins: dict) -> dict:
     return out
 
 
+# rtao.csh over half-resolution G-buffers of the traversal scene: (width,
+# height).  96 x 64 is a whole number of the shader's tiles (four work groups
+# of 8 pixels across); 44 x 20 is not, and the engine's dispatch of
+# ceil(w / 8) * ceil(h / 4) groups (AORenderer.cpp:85-88) then reaches only
+# part of the last tile column.
+RTAO_CASES = ((96, 64), (44, 20))
+RTAO_RADIUS = 8.0
+RTAO_FRAMES = (5, 300)          # uniforms.frameSeed; 300 wraps the sample index
+
+
+def rtao_scene(seed=20261207):
+    """A seeded two-level scene for the ambient-occlusion goldens: a terrain
+    patch with boxes (mesh 0, one identity instance), a box with
+    per-triangle opacities (mesh 1) standing on it four times, and a sheet
+    of sixteen quads with per-triangle opacities (mesh 2) hovering over it
+    three times (tilted; one visible to the shadow mask only); twelve
+    materials of random opacity, some with an opacity texture.  Laid out
+    like traversal_scene (the library's builder and packers; deterministic,
+    so the tests rebuild it)."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    import atlas_rt
+    from atlas_rt import BVH, MATERIAL_DTYPE, scenes
+    rng = np.random.default_rng(seed)
+    extent = 16.0
+    terrain = scenes.terrain_boxes(seed=seed + 1, grid=32, extent=extent, n_boxes=16)[0]
+    box = scenes._box_triangles(np.array([-0.5, 0.0, -0.5], F32), np.array([0.5, 1.0, 0.5], F32))
+    q = np.linspace(-1.0, 1.0, 5, dtype=F32)
+    sheet = []
+    for i in range(4):
+        for j in range(4):
+            a, b = [q[i], 0.0, q[j]], [q[i + 1], 0.0, q[j]]
+            c, d = [q[i + 1], 0.0, q[j + 1]], [q[i], 0.0, q[j + 1]]
+            sheet += [[a, c, b], [a, d, c]]
+    sheet = np.array(sheet, F32)
+    meshes, bvhs = [], []
+    for k, t in enumerate((terrain, box, sheet)):
+        b = BVH(t)
+        n = len(t)
+        op = rng.uniform(0.0, 1.0, n).astype(F32)
+        kind = rng.integers(0, 4, n)
+        if k == 0:
+            kind = np.where(rng.random(n) < 0.9, 2, 0)   # the ground: mostly opaque
+        op[kind == 0] = -1.0
+        op[kind == 1] = 0.0
+        op[kind == 2] = 1.0
+        mat = rng.integers(0, 4, n).astype(np.int32)
+        gt = b.pack_triangles(mat, op)
+        sh = b.pack_shading(None, mat, op)
+        b.pack_uvs(sh, rng.uniform(-1.5, 2.5, (n, 6)).astype(F32))
+        meshes.append((b.nodes_f32.copy(), gt, sh))
+        bvhs.append(b)
+    insts, boxes = [], []
+    MA, MS = atlas_rt.MASK_ALL, atlas_rt.MASK_SHADOW
+
+    def add(M, k, mask):
+        insts.append(atlas_rt.make_instance(M, k, mask, material_offset=4 * k))
+        lo, hi = atlas_rt.mesh_bounds(bvhs[k])
+        boxes.append(atlas_rt.transform_aabb(lo, hi, M))
+
+    add(np.eye(4), 0, MA)
+    for i in range(7):
+        x, z = rng.uniform(2.0, extent - 2.0, 2)
+        ground = float(scenes.terrain_height(seed + 1, np.array([x], F32), np.array([z], F32))[0])
+        a = rng.uniform(0.0, 2.0 * np.pi)
+        R = np.array([[np.cos(a), 0.0, np.sin(a)], [0.0, 1.0, 0.0], [-np.sin(a), 0.0, np.cos(a)]])
+        M = np.eye(4)
+        if i < 4:
+            M[:3, :3] = R @ np.diag(rng.uniform(0.8, 2.5, 3))
+            M[:3, 3] = (x, ground - 0.3, z)
+            add(M, 1, (MA, MA | MS)[i % 2])
+        else:
+            M[:3, :3] = _rotation(rng) @ np.diag([rng.uniform(2.0, 3.5), 1.0, rng.uniform(2.0, 3.5)])
+            M[:3, :3] = 0.35 * M[:3, :3] + 0.65 * R @ np.diag([2.5, 1.0, 2.5])
+            M[:3, 3] = (x, ground + rng.uniform(0.6, 1.5), z)
+            add(M, 2, (MA | MS, MA, MS)[i - 4])
+    insts = np.array(insts, atlas_rt.INSTANCE_DTYPE)
+    top = BVH(boxes_only=np.array(boxes, F32))
+    ordered = insts[top.order].copy()
+    ordered["nextInstance"] = np.where(top.end_of_node > 0, -1, np.arange(len(ordered)) + 1)
+    mats = np.zeros(12, MATERIAL_DTYPE)
+    mats["opacity"] = rng.uniform(0.0, 1.0, 12)
+    mats["opacity"][0] = 1.0
+    for t in ("baseColorTexture", "normalTexture", "roughnessTexture", "metalnessTexture", "aoTexture"):
+        mats[t] = -1
+    mats["opacityTexture"] = rng.integers(-1, 3, 12)
+    mats["invertUVs"] = rng.integers(0, 2, 12)
+    tex = [rng.integers(0, 256, (16, 32), dtype=np.uint8),
+           rng.integers(0, 256, (8, 5, 4), dtype=np.uint8),
+           rng.uniform(-0.2, 1.2, (33, 7)).astype(F32)]
+    return {"top": top.nodes_f32.copy(), "instances": ordered, "meshes": meshes, "materials": mats,
+            "textures": tex, "rays8": np.zeros((0, 8), F32)}
+
+
+def set_scene(lib: C.CDLL, sc: dict, keep: list):
+    """Points the reference programs' scene buffers at sc (kept alive in keep)."""
+    P = C.c_void_p
+    nodes = (P * 3)(*[m[0].ctypes.data for m in sc["meshes"]])
+    bt = (P * 3)(*[m[1].ctypes.data for m in sc["meshes"]])
+    tr = (P * 3)(*[m[2].ctypes.data for m in sc["meshes"]])
+    rgba = [texture_rgba(t) for t in sc["textures"]]
+    tp = (P * len(rgba))(*[t.ctypes.data for t in rgba])
+    wh = np.array([[t.shape[1], t.shape[0]] for t in rgba], np.int32).reshape(-1)
+    keep += [rgba, tp, wh, nodes, bt, tr]
+    lib.aeglsl_scene(P(sc["top"].ctypes.data), P(sc["instances"].ctypes.data), C.c_int(3), nodes, bt, tr,
+                     P(sc["materials"].ctypes.data), C.c_int(len(rgba)), tp, P(wh.ctypes.data))
+
+
+def blue_noise_textures(seed=20261206):
+    """Stand-ins for the engine's blue-noise textures (RGBA8, 128 x 128
+    scrambling / ranking and 256 x 1 Sobol sequence): seeded bytes, since
+    what is pinned is the sampler's arithmetic over whatever they hold."""
+    rng = np.random.default_rng(seed)
+    return (rng.integers(0, 256, (128, 128, 4), dtype=np.uint8), rng.integers(0, 256, (256, 4), dtype=np.uint8))
+
+
+def rtao_camera(w: int, h: int):
+    """View and projection matrices of the ambient-occlusion goldens."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    from atlas_rt import gbuffer as G
+    return G.look_at((8.0, 16.0, -5.0), (8.0, 4.0, 9.0)), G.perspective(60.0, w / h, 0.5, 400.0)
+
+
+def rtao_gbuffer(lib: C.CDLL, sc: dict, w: int, h: int, seed: int = 7):
+    """A half-resolution G-buffer of the traversal scene (the lib's scene
+    must be sc): the eye ray of each pixel through 2 * pixel + offset + 0.5
+    of the full resolution, traced by the reference's HitClosest; depth =
+    the hit's NDC depth (1 where nothing is hit), normal = the encoded
+    view-space face normal of the hit triangle, turned towards the eye."""
+    sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
+    from atlas_rt import gbuffer as G
+    from atlas_rt import scenes
+    rng = np.random.default_rng(seed)
+    V, P = rtao_camera(w, h)
+    offset = rng.integers(0, 4, w * h).astype(np.uint8)
+    o, d = G.view_rays(V, P, w, h, offset)
+    rays8 = np.ascontiguousarray(scenes.rays8(o.astype(F32), d.astype(F32), 0.0, 1e12), F32)
+    hits = np.zeros((w * h, 4), F32)
+    lib.aeglsl_scene_trace(C.c_int(0), C.c_void_p(rays8.ctypes.data), C.c_int(w * h), C.c_uint(0xFFFFFFFF),
+                           C.c_void_p(hits.ctypes.data))
+    tri, inst = hits[:, 0].view(np.int32), hits[:, 1].view(np.int32)
+    hit = tri >= 0
+    od, dd = rays8[:, 0:3].astype(np.float64), rays8[:, 3:6].astype(np.float64)
+    pos = od + dd * hits[:, 2:3].astype(np.float64)
+    clip = np.concatenate([pos, np.ones((len(pos), 1))], axis=1) @ (P @ V).T
+    depth = np.where(hit, clip[:, 2] / clip[:, 3], 1.0)
+    n = np.zeros((w * h, 3))
+    for i in np.flatnonzero(hit):
+        ins = sc["instances"][inst[i]]
+        t = sc["meshes"][ins["meshOffset"]][2][tri[i], :12].astype(np.float64)
+        no = np.cross(t[4:7] - t[0:3], t[8:11] - t[0:3])
+        n[i] = np.asarray(ins["inverseMatrix"], np.float64).reshape(3, 4)[:, :3].T @ no
+    n /= np.linalg.norm(n, axis=1, keepdims=True) + 1e-30
+    n *= np.where((n * dd).sum(axis=1, keepdims=True) > 0, -1.0, 1.0)
+    nv = n @ V[:3, :3].T
+    nv /= np.linalg.norm(nv, axis=1, keepdims=True) + 1e-30
+    enc = np.zeros((w * h, 2))
+    enc[hit] = G.encode_normal(nv[hit])
+    return {"depth": depth.astype(F32).reshape(h, w), "normal": enc.astype(F32).reshape(h, w, 2),
+            "offset": offset.reshape(h, w), "ip_matrix": np.linalg.inv(P), "iv_matrix": np.linalg.inv(V)}
+
+
+def column_major(m):
+    return np.ascontiguousarray(np.asarray(m, np.float64).astype(F32).T.reshape(-1))
+
+
+def trace_rtao(lib: C.CDLL) -> dict:
+    """One dispatch of the reference's rtao.csh (HitAny and, with
+    OPACITY_CHECK, HitAnyTransparency) per case, frame seed and variant over
+    rtao_scene; unwritten pixels stay -1.  Also the blue-noise vectors of one
+    128 x 128 period per frame seed, stored as the integers v * 256 - 0.5."""
+    P = C.c_void_p
+    sc, keep = rtao_scene(), []
+    set_scene(lib, sc, keep)
+    out = {"rtao_scene_digest": np.frombuffer(scene_digest(sc).encode(), np.uint8)}
+    rank, sobol = blue_noise_textures()
+    rank_f, sobol_f = texture_rgba(rank), texture_rgba(sobol[None])
+    for f in RTAO_FRAMES:
+        bn = np.zeros((128, 128, 2), F32)
+        lib.aeglsl_blue_noise(C.c_int(128), C.c_int(128), P(rank_f.ctypes.data), P(sobol_f.ctypes.data), C.c_int(f),
+                              P(bn.ctypes.data))
+        q = bn * F32(256.0) - F32(0.5)
+        assert np.array_equal(q, np.round(q)) and q.min() >= 0 and q.max() <= 255
+        out[f"rtao_blue_noise_{f}"] = q.astype(np.uint8)
+    for w, h in RTAO_CASES:
+        gb = rtao_gbuffer(lib, sc, w, h)
+        key = f"rtao_{w}x{h}"
+        for k in ("depth", "normal", "offset"):
+            out[f"{key}_{k}"] = gb[k]
+        off = np.ascontiguousarray(gb["offset"], np.int32)
+        ip, iv = column_major(gb["ip_matrix"]), column_major(gb["iv_matrix"])
+        for f in RTAO_FRAMES:
+            for opacity in (0, 1):
+                ao = np.full((h, w), -1.0, F32)
+                lib.aeglsl_rtao(C.c_int(opacity), C.c_int(w), C.c_int(h), P(gb["depth"].ctypes.data),
+                                P(gb["normal"].ctypes.data), P(off.ctypes.data), P(rank_f.ctypes.data),
+                                P(sobol_f.ctypes.data), P(ip.ctypes.data), P(iv.ctypes.data), C.c_float(RTAO_RADIUS),
+                                C.c_int(f), P(ao.ctypes.data))
+                out[f"{key}_ao_{f}_{opacity}"] = ao
+    return out
+
+
 def reference_lib():
     """Builds (if needed) and loads the reference's GLSL compiled on the host;
     None where the reference tree is absent."""
@@ -398,7 +599,7 @@ def main():
     pt = {}
     for name in pt_cases():
         pt.update(trace_pt(lib, name))
-    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib), **pt,
+    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib), **pt, **trace_rtao(lib),
                         trav_scene_digest=np.frombuffer(scene_digest(sc).encode(), np.uint8))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

@@ -9,7 +9,8 @@ HitAnyTransparency of raytracer/bvh.hsh over a seeded two-level scene, the
 path tracer's ray generation (pathtracer/rayGen.csh, whole dispatches), and
 the engine's whole path tracer (rayGen.csh, the trace dispatch and
 pathtracer/rayHit.csh, bounce by bounce; block statistics of thousands of its
-samples) --
+samples), and the ambient-occlusion pass (ao/rtao.csh with and without
+OPACITY_CHECK, whole dispatches over G-buffers, with its blue-noise sampler) --
 compiled unmodified on the host by oracle/glsl/make_ref.py.  Here the oracle's
 restatement (CPU) and the path tracer's and traversal's own device functions
 (GPU, through ae_rt_selftest_shading) are held to them: the intersections bit
@@ -48,6 +49,8 @@ def test_fixture_is_what_the_reference_writes():
     for name in G.pt_cases():
         for k, v in G.trace_pt(lib, name).items():
             assert np.array_equal(np.asarray(v, g[k].dtype), g[k]), k
+    for k, v in G.trace_rtao(lib).items():
+        assert np.array_equal(np.asarray(v).view(np.uint8), np.asarray(g[k]).view(np.uint8)), k
 
 
 def test_reference_random_is_the_documented_hash():
@@ -389,3 +392,172 @@ def test_gpu_path_tracer_matches_the_engines_estimator(name):
     finally:
         ctx.close()
     check_against_engine(name, img, n)
+
+
+# ---- the ambient-occlusion pass: ao/rtao.csh dispatched over G-buffers ----
+
+_RTAO = {}
+
+
+def rtao_scene():
+    """The seeded scene of the rtao_* goldens, rebuilt and checked against
+    the fixture's digest, with the oracle's scene tuple (instance model
+    matrices inverted from the instances' inverse ones)."""
+    if "sc" not in _RTAO:
+        G = _generator()
+        sc = G.rtao_scene()
+        assert G.scene_digest(sc) == bytes(S.golden()["rtao_scene_digest"]).decode()
+        model = np.zeros((len(sc["instances"]), 12), np.float32)
+        for i, ins in enumerate(sc["instances"]):
+            a = np.eye(4)
+            a[:3] = np.asarray(ins["inverseMatrix"], np.float64).reshape(3, 4)
+            model[i] = np.linalg.inv(a)[:3].reshape(-1)
+        oracle = (sc["top"], sc["instances"], model, sc["meshes"], sc["materials"], np.zeros((0, 16), np.float32),
+                  sc["textures"])
+        _RTAO["sc"] = (sc, oracle)
+    return _RTAO["sc"]
+
+
+def rtao_gbuffer(w, h):
+    """The golden G-buffer of one case as Context.rtao / pyoracle.pass_screen
+    take it (numpy), with the blue-noise textures."""
+    G = _generator()
+    g = S.golden()
+    key = f"rtao_{w}x{h}"
+    V, P = G.rtao_camera(w, h)
+    rank, sobol = G.blue_noise_textures()
+    return {"depth": g[key + "_depth"], "normal": g[key + "_normal"], "offset": g[key + "_offset"], "half_res": 1,
+            "ip_matrix": np.linalg.inv(P), "iv_matrix": np.linalg.inv(V), "scrambling_ranking": rank,
+            "sobol_sequence": sobol}
+
+
+def assert_ao_equal(got, ref):
+    """Occlusion by HitAny is 0 or 1 and must match exactly.  With the
+    opacity check, a ray that crossed only partly transparent surfaces
+    carries the product of their opacities, which varies continuously with
+    where the ray meets them: the opacity textures of the scene change by
+    up to ~256 per world unit (random texels, 8 UV units per world unit),
+    and a direction that differs from the shader's in its last bits (sin,
+    cos and normalize round differently on the host and on the device)
+    moves a hit 8 units away by ~5e-7, so those values agree to rtol 1e-3."""
+    binary = (ref == 0.0) | (ref == 1.0)
+    np.testing.assert_array_equal(got[binary], ref[binary])
+    np.testing.assert_allclose(got[~binary], ref[~binary], rtol=1e-3, atol=1e-6)
+    return binary
+
+
+def check_rtao(got, ref, opacity):
+    """got against the reference's rtao.csh where its dispatch wrote (ref !=
+    -1), as assert_ao_equal states.  Returns the number of pixels the
+    dispatch left unwritten."""
+    wr = ref != -1.0
+    r = ref[wr]
+    binary = assert_ao_equal(got[wr], r)
+    if opacity:
+        assert (~binary).sum() > 0                      # partial opacities were crossed
+    else:
+        assert binary.all()
+    drawn = rtao_gbuffer(*ref.shape[::-1])["depth"][wr] < 1.0
+    assert 0.1 < (r[drawn] == 0.0).mean() < 0.5         # occluded and open pixels both occur
+    return int((~wr).sum())
+
+
+def _rtao_cases():
+    G = _generator()
+    return [(w, h, f, op) for (w, h) in G.RTAO_CASES for f in G.RTAO_FRAMES for op in (0, 1)]
+
+
+def test_oracle_blue_noise_matches_reference():
+    """The oracle's SampleBlueNoise gives the reference's bluenoise.hsh
+    values bit for bit over a whole 128 x 128 period, for a sample index
+    below 256 and one that wraps."""
+    import pyoracle
+    G = _generator()
+    rank, sobol = G.blue_noise_textures()
+    g = S.golden()
+    for f in G.RTAO_FRAMES:
+        ref = (g[f"rtao_blue_noise_{f}"].astype(np.float32) + np.float32(0.5)) / np.float32(256.0)
+        got = pyoracle.blue_noise(rank, sobol, 128, 128, f)
+        np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+        # the pattern repeats every 128 pixels
+        big = pyoracle.blue_noise(rank, sobol, 300, 260, f)
+        np.testing.assert_array_equal(big[128:256, 256:300], ref[:, :44])
+
+
+@pytest.mark.parametrize("w,h,frame,opacity", _rtao_cases())
+def test_oracle_rtao_matches_reference_rtao(w, h, frame, opacity):
+    """The oracle's RTAO pass (blue-noise samples from the G-buffer's
+    textures) against the reference's rtao.csh compiled on the host: one
+    whole dispatch each, with and without OPACITY_CHECK."""
+    import pyoracle
+    sc, oracle = rtao_scene()
+    G = _generator()
+    ref = S.golden()[f"rtao_{w}x{h}_ao_{frame}_{opacity}"]
+    got = pyoracle.pass_screen("rtao", oracle, rtao_gbuffer(w, h), radius=G.RTAO_RADIUS, opacity_check=bool(opacity),
+                               frame_seed=frame)
+    unwritten = check_rtao(got, ref, opacity)
+    assert unwritten == (0 if w % 32 == 0 else unwritten) and (unwritten > 0) == (w % 32 != 0)
+
+
+def test_engine_rtao_dispatch_leaves_part_of_the_last_tile_column():
+    """rtao.csh lays its one-dimensional dispatch onto tiles four work groups
+    (32 pixels) wide, but AORenderer.cpp:85-88 dispatches only
+    ceil(w / 8) * ceil(h / 4) groups: when ceil(w / 8) is not a multiple of
+    4, the last tile gets fewer groups than it spans and pixels of its
+    columns are never written (the engine's image keeps older values
+    there).  The library writes every pixel."""
+    g = S.golden()
+    ref = g["rtao_44x20_ao_5_0"]
+    gx, gy = (44 + 7) // 8, (20 + 3) // 4
+    covered = np.zeros((20, 44), bool)
+    for grp in range(gx * gy):
+        tile, idx = divmod(grp, 4 * gy)
+        x0, y0 = (tile * 4 + idx % 4) * 8, (idx // 4) * 4
+        covered[y0:y0 + 4, x0:x0 + 8] = True
+    np.testing.assert_array_equal(ref != -1.0, covered)
+    assert not covered[:, 32:].all() and covered[:, :32].all()
+
+
+@pytest.mark.gpu
+def test_gpu_rtao_matches_reference_rtao():
+    """The GPU's RTAO (ae_rt_rtao, blue-noise vectors drawn on the device
+    from the G-buffer's textures) against the reference's rtao.csh over the
+    same scene and G-buffers: every case, frame seed and variant; pixels
+    the engine's dispatch leaves unwritten are held to the oracle."""
+    import torch
+    import atlas_rt
+    import pyoracle
+    sc, oracle = rtao_scene()
+    G = _generator()
+    ctx = atlas_rt.Context(device=0)
+    try:
+        for k, (nodes, gt, sh) in enumerate(sc["meshes"]):
+            assert ctx.upload_mesh(nodes, gt, sh) == k
+        ctx.scene_set(sc["top"], sc["instances"])
+        ctx.set_materials(sc["materials"])
+        ctx.set_textures(sc["textures"])
+        for w, h, frame, opacity in _rtao_cases():
+            gb = rtao_gbuffer(w, h)
+            dev = {k: (torch.from_numpy(np.ascontiguousarray(v)).cuda() if isinstance(v, np.ndarray) and k not in
+                       ("ip_matrix", "iv_matrix") else v) for k, v in gb.items()}
+            out = torch.full((h, w), -5.0, dtype=torch.float32, device="cuda")
+            params = dict(radius=G.RTAO_RADIUS, opacity_check=bool(opacity), frame_seed=frame)
+            ctx.rtao(dev, out, **params)
+            ctx.synchronize()
+            got = out.cpu().numpy()
+            ref = S.golden()[f"rtao_{w}x{h}_ao_{frame}_{opacity}"]
+            check_rtao(got, ref, opacity)
+            gap = ref == -1.0
+            if gap.any():
+                orc = pyoracle.pass_screen("rtao", oracle, gb, **params)
+                assert_ao_equal(got[gap], orc[gap])
+            # the same vectors handed over as samples give the same image
+            samples = pyoracle.blue_noise(gb["scrambling_ranking"], gb["sobol_sequence"], w, h, frame)
+            dev2 = {k: v for k, v in dev.items() if k not in ("scrambling_ranking", "sobol_sequence")}
+            dev2["samples"] = torch.from_numpy(samples).cuda()
+            out2 = torch.full((h, w), -5.0, dtype=torch.float32, device="cuda")
+            ctx.rtao(dev2, out2, **params)
+            ctx.synchronize()
+            np.testing.assert_array_equal(out2.cpu().numpy(), got)
+    finally:
+        ctx.close()
