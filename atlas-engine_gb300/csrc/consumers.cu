@@ -322,7 +322,10 @@ __global__ void pass_shade_kernel(ShadeP p) {
                         V3 refl = KIND == kPassDDGI ? eval_diffuse(sf) : eval_diffuse(sf) + eval_specular(sf);
                         refl = refl * sf.mat.opacity;
                         const V3 c = refl * (ls.radiance * ls.solidAngle) * (sf.NdotL / ls.pdf);
-                        if (sf.NdotL > 0.0f && c.x + c.y + c.z > 0.0f) {
+                        // CheckVisibility traces whenever NdotL > 0; the light term can be
+                        // negative (a one-sided back face seen from behind gives NdotV < 0),
+                        // and the shaders add it as it is
+                        if (sf.NdotL > 0.0f && (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f)) {
                             const V3 so = sf.P + sf.N * kEps;
                             sr0 = make_float4(so.x, so.y, so.z, 0.0f);
                             sr1 = make_float4(sf.L.x, sf.L.y, sf.L.z, 0.0f);

@@ -1690,7 +1690,10 @@ static void pass_eval_hit(const pass_job_t* p, v3 ro, v3 rd, uint32_t key, int32
                                                : vadd(pt_eval_diffuse(&sf), pt_eval_specular(&sf));
                 refl = vmul(refl, sf.m.opacity);
                 v3 c = vmul(vmulv(refl, vmul(lrad, solidAngle)), sf.NdotL / lightPdf);
-                if (sf.NdotL > 0.0f && c.x + c.y + c.z > 0.0f) {
+                /* CheckVisibility traces whenever NdotL > 0; the light term can
+                 * be negative (a one-sided back face seen from behind gives
+                 * NdotV < 0), and the shaders add it as it is */
+                if (sf.NdotL > 0.0f && (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f)) {
                     v3 so = vadd(sf.P, vmul(sf.N, PASS_EPS));
                     float s8[8] = { so.x, so.y, so.z, sf.L.x, sf.L.y, sf.L.z, 0.0f, ldist - 2.0f * PASS_EPS };
                     float vis;

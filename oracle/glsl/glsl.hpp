@@ -34,6 +34,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 typedef unsigned int uint;
 
@@ -61,7 +62,11 @@ struct Swz {
         V() : x(0), y(0) {}                                                               \
         explicit V(T s) : x(s), y(s) {}                                                   \
         V(T a, T b) : x(a), y(b) {}                                                       \
-        template <typename U> explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])) {}      \
+        template <typename U, typename = decltype(static_cast<const U*>(nullptr)->v)>        \
+        explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])) {}                            \
+        template <typename U, typename = typename std::enable_if<std::is_arithmetic<U>::value>::type, \
+                  typename = void>                                                        \
+        explicit V(U s) : x(T(s)), y(T(s)) {}                                             \
         T& operator[](int i) { return v[i]; }                                             \
         T operator[](int i) const { return v[i]; }                                        \
     };
@@ -75,6 +80,7 @@ struct Swz {
             Swz<V2, T, 3, 0, 2> xz;                                                       \
             Swz<V2, T, 3, 1, 2> yz;                                                       \
             Swz<V, T, 3, 0, 1, 2> xyz;                                                    \
+            Swz<V, T, 3, 0, 2, 1> xzy;                                                    \
             Swz<V, T, 3, 0, 1, 2> rgb;                                                    \
             T v[3];                                                                       \
         };                                                                                \
@@ -83,7 +89,11 @@ struct Swz {
         V(T a, T b, T c) : x(a), y(b), z(c) {}                                            \
         V(const V2& a, T c) : x(a.x), y(a.y), z(c) {}                                     \
         V(const V& o) : x(o.x), y(o.y), z(o.z) {}                                         \
-        template <typename U> explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])), z(T(o.v[2])) {} \
+        template <typename U, typename = decltype(static_cast<const U*>(nullptr)->v)>        \
+        explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])), z(T(o.v[2])) {}              \
+        template <typename U, typename = typename std::enable_if<std::is_arithmetic<U>::value>::type, \
+                  typename = void>                                                        \
+        explicit V(U s) : x(T(s)), y(T(s)), z(T(s)) {}                                    \
         V& operator=(const V& o) { x = o.x; y = o.y; z = o.z; return *this; }            \
         T& operator[](int i) { return v[i]; }                                             \
         T operator[](int i) const { return v[i]; }                                        \
@@ -96,7 +106,9 @@ struct Swz {
             Swz<V2, T, 4, 0, 1> xy;                                                       \
             Swz<V2, T, 4, 0, 1> rg;                                                       \
             Swz<V2, T, 4, 2, 3> zw;                                                       \
+            Swz<V2, T, 4, 0, 2> xz;                                                       \
             Swz<V3, T, 4, 0, 1, 2> xyz;                                                   \
+            Swz<V3, T, 4, 0, 2, 1> xzy;                                                   \
             Swz<V3, T, 4, 0, 1, 2> rgb;                                                   \
             T v[4];                                                                       \
         };                                                                                \
@@ -136,6 +148,7 @@ GLSL_VEC4(uvec4, uint, uvec2, uvec3)
     inline V operator+(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s + a.v[i]; return r; }      \
     inline V operator-(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = a.v[i] - s; return r; }      \
     inline V operator-(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s - a.v[i]; return r; }      \
+    inline V operator/(T s, const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = s / a.v[i]; return r; }      \
     inline V operator-(const V& a) { V r; for (int i = 0; i < N; i++) r.v[i] = -a.v[i]; return r; }                \
     inline V& operator+=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] + b.v[i]; return a; }      \
     inline V& operator-=(V& a, const V& b) { for (int i = 0; i < N; i++) a.v[i] = a.v[i] - b.v[i]; return a; }      \
@@ -157,12 +170,22 @@ GLSL_VEC_OPS(uvec4, uint, 4)
 inline vec2 operator+(const vec2& a, const ivec2& b) { return a + vec2(b); }
 inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
 inline ivec2 operator%(const ivec2& a, int b) { return ivec2(a.x % b, a.y % b); }
+inline ivec3 operator&(const ivec3& a, const ivec3& b) { return ivec3(a.x & b.x, a.y & b.y, a.z & b.z); }
 
 // ---- boolean vectors and the component-wise relations (section 8.7) ----
 struct bvec2 { bool x, y; };
+struct bvec3 { bool x, y, z; };
 inline bvec2 lessThan(const ivec2& a, const ivec2& b) { return bvec2{ a.x < b.x, a.y < b.y }; }
+#define GLSL_REL3(V)                                                                                       \
+    inline bvec3 lessThan(const V& a, const V& b) { return bvec3{ a.x < b.x, a.y < b.y, a.z < b.z }; }      \
+    inline bvec3 greaterThan(const V& a, const V& b) { return bvec3{ a.x > b.x, a.y > b.y, a.z > b.z }; }   \
+    inline bvec3 greaterThanEqual(const V& a, const V& b) { return bvec3{ a.x >= b.x, a.y >= b.y, a.z >= b.z }; }
+GLSL_REL3(vec3)
+GLSL_REL3(ivec3)
 inline bool all(const bvec2& b) { return b.x && b.y; }
 inline bool any(const bvec2& b) { return b.x || b.y; }
+inline bool all(const bvec3& b) { return b.x && b.y && b.z; }
+inline bool any(const bvec3& b) { return b.x || b.y || b.z; }
 
 // ---- scalar built-ins (GLSL 4.60 section 8) ----
 inline float min(float x, float y) { return (y < x) ? y : x; }
@@ -212,6 +235,13 @@ GLSL_VEC_FUNCS(vec3, 3)
 GLSL_VEC_FUNCS(vec4, 4)
 GLSL_VEC_FUNCS(ivec2, 2)
 GLSL_VEC_FUNCS(ivec3, 3)
+// min / max of a vector and a scalar (genType min(genType, float))
+#define GLSL_VEC_SCALAR(V, T, N)                                                                            \
+    inline V min(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = min(a.v[i], s); return r; }   \
+    inline V max(const V& a, T s) { V r; for (int i = 0; i < N; i++) r.v[i] = max(a.v[i], s); return r; }
+GLSL_VEC_SCALAR(vec2, float, 2)
+GLSL_VEC_SCALAR(vec3, float, 3)
+GLSL_VEC_SCALAR(vec4, float, 4)
 #define GLSL_FVEC_FUNCS(V, N)                                                                               \
     inline V clamp(const V& x, float a, float b) { return min(max(x, V(a)), V(b)); }                          \
     inline V mix(const V& x, const V& y, float a) { return x * (1.0f - a) + y * a; }                          \
@@ -228,6 +258,9 @@ GLSL_VEC_FUNCS(ivec3, 3)
 GLSL_FVEC_FUNCS(vec2, 2)
 GLSL_FVEC_FUNCS(vec3, 3)
 GLSL_FVEC_FUNCS(vec4, 4)
+
+// reflect(I, N) = I - 2 * dot(N, I) * N (section 8.5)
+inline vec3 reflect(const vec3& i, const vec3& n) { return i - 2.0f * dot(n, i) * n; }
 
 inline vec3 cross(const vec3& a, const vec3& b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
@@ -381,7 +414,7 @@ typedef glsl_texture2D texture2D;
 typedef glsl_sampler sampler;
 typedef glsl_sampler2D sampler2D;
 struct sampler2DArray { int width = 0, height = 0, layers = 0; };
-struct samplerCube {};
+struct samplerCube { vec4 constant; };   // a constant environment (the goldens' sky)
 inline ivec2 textureSize(const sampler2D& s, int) { return s.tex ? ivec2(s.tex->width, s.tex->height) : ivec2(0); }
 inline ivec3 textureSize(const sampler2DArray& s, int) { return ivec3(s.width, s.height, s.layers); }
 inline vec4 texelFetch(const sampler2D& s, const ivec2& p, int) {
@@ -389,6 +422,14 @@ inline vec4 texelFetch(const sampler2D& s, const ivec2& p, int) {
     return vec4(t[0], t[1], t[2], t[3]);
 }
 inline vec4 texelFetch(const sampler2DArray&, const ivec3&, int) { return vec4(0.0f); }
+// layered and shadow samplers of the DDGI volume and the shadow cascades, which
+// the goldens leave unbound (the programs are compiled without DDGI and
+// without USE_SHADOW_MAP): they sample as zero
+inline vec4 textureLod(const sampler2DArray&, const vec3&, float) { return vec4(0.0f); }
+inline vec4 texture(const sampler2DArray&, const vec3&) { return vec4(0.0f); }
+struct sampler2DArrayShadow { int width = 0, height = 0, layers = 0; };
+inline float texture(const sampler2DArrayShadow&, const vec4&) { return 0.0f; }
+inline ivec3 textureSize(const sampler2DArrayShadow& s, int) { return ivec3(s.width, s.height, s.layers); }
 // The bindless sampler of the engine (linear filtering, repeat addressing,
 // MainRenderer.cpp:922-929) at one level: the specification's bilinear
 // filter (OpenGL 4.6 section 8.14.2) with exact weights.
@@ -413,13 +454,18 @@ inline vec4 textureLod(const sampler2D& s, const vec2& uv, float) {
     const vec4 t01 = texelFetch(s, ivec2(x0, y1), 0), t11 = texelFetch(s, ivec2(x1, y1), 0);
     return t00 * ((1.0f - ax) * (1.0f - ay)) + t10 * (ax * (1.0f - ay)) + t01 * ((1.0f - ax) * ay) + t11 * (ax * ay);
 }
-inline vec4 textureLod(const samplerCube&, const vec3&, float) { return vec4(0.0f); }
+inline vec4 textureLod(const samplerCube& s, const vec3&, float) { return s.constant; }
 // an integer texture, one channel per texel (r; g, b = 0, a = 1)
 struct isampler2D {
     const int* texels = nullptr;
     int width = 0, height = 0;
 };
 inline ivec4 texelFetch(const isampler2D& s, const ivec2& p, int) { return ivec4(s.texels[p.y * s.width + p.x], 0, 0, 1); }
+struct usampler2D {
+    const uint* texels = nullptr;
+    int width = 0, height = 0;
+};
+inline uvec4 texelFetch(const usampler2D& s, const ivec2& p, int) { return uvec4(s.texels[p.y * s.width + p.x], 0u, 0u, 1u); }
 inline vec4 texture(const sampler2D& s, const vec2& uv) { return s.tex ? textureLod(s, uv, 0.0f) : vec4(0.0f); }
 
 // ---- images, atomics and invocation ids, for one invocation ----

@@ -22,12 +22,19 @@
 //   without OPACITY_CHECK), and its blue-noise sampler
 //                                            ao/rtao.csh:40-112,
 //                                            common/bluenoise.hsh:9-32
+//   the reflection and diffuse GI passes, one dispatch each (with and
+//   without OPACITY_CHECK)              reflection/rtreflection.csh:60-245,
+//                                            rtgi/rtgi.csh:60-234
 #include "glsl.hpp"
 #include "glsl_ref.inc"
 #include "glsl_raygen.inc"
 #include "glsl_pt.inc"
 #include "glsl_rtao.inc"
 #include "glsl_rtao_opacity.inc"
+#include "glsl_rtr.inc"
+#include "glsl_rtr_opacity.inc"
+#include "glsl_rtgi.inc"
+#include "glsl_rtgi_opacity.inc"
 
 using namespace aeg_glsl;
 
@@ -177,7 +184,23 @@ void aeglsl_scene(const void* tlas, const void* instances, int n_meshes, const v
     T::bindlessTextures = g_textures.data();
     AEG_SCENE_INTO(aeg_rtao)
     AEG_SCENE_INTO(aeg_rtao_opacity)
+    AEG_SCENE_INTO(aeg_rtr)
+    AEG_SCENE_INTO(aeg_rtr_opacity)
+    AEG_SCENE_INTO(aeg_rtgi)
+    AEG_SCENE_INTO(aeg_rtgi_opacity)
 #undef AEG_SCENE_INTO
+}
+
+// The light list (GPULight, 64 bytes each) of the shading passes' programs.
+void aeglsl_scene_lights(const void* lights, int n_lights) {
+#define AEG_LIGHTS_INTO(T)                                                 \
+    T::lights = (T::PackedLight*)lights;                                   \
+    T::PushConstants.lightCount = n_lights;
+    AEG_LIGHTS_INTO(aeg_rtr)
+    AEG_LIGHTS_INTO(aeg_rtr_opacity)
+    AEG_LIGHTS_INTO(aeg_rtgi)
+    AEG_LIGHTS_INTO(aeg_rtgi_opacity)
+#undef AEG_LIGHTS_INTO
 }
 
 // kind 0 HitClosest, 1 HitAny, 2 HitClosestTransparency, 3 HitAnyTransparency
@@ -430,6 +453,84 @@ void aeglsl_rtao(int opacity_check, int w, int h, const float* depth, const floa
     }
 #undef AEG_RTAO_RUN
     for (size_t i = 0; i < image.size(); i++) ao[i] = image[i].x;
+}
+
+// One dispatch of reflection/rtreflection.csh (kind 0) or rtgi/rtgi.csh
+// (kind 1) over a w x h G-buffer, as RTReflectionRenderer.cpp:107-135 issues
+// it: ceil(w / 8) x ceil(h / 4) work groups of 8 x 4 over the pixels; over the
+// scene and lights of aeglsl_scene / aeglsl_scene_lights (HitClosest, or
+// HitClosestTransparency with opacity_check; shadows by HitAnyTransparency).
+// The G-buffer planes as in aeglsl_rtao, plus roughness (w * h floats: the
+// r channel of roughnessMetallicAoTexture); the pixel's material is a packed
+// material of roughness 1 with a roughness map, so its roughness is the
+// plane's (rtreflection.csh:92-96).  params: radianceLimit, bias,
+// roughnessCutoff and the environment's colour (r, g, b).  out: w * h * 4
+// floats (rtrImage), in / out.
+void aeglsl_screen_pass(int kind, int opacity_check, int w, int h, int half_res, const float* depth,
+                        const float* normal, const int* offset, const float* roughness, const float* ranking,
+                        const float* sobol, const float* ip, const float* iv, const float* params, uint frame_seed,
+                        float* out) {
+    std::vector<float> depth_texels, normal_texels, rough_texels;
+    const glsl_texture2D depth_tex = Plane(depth_texels, depth, 1, w, h);
+    const glsl_texture2D normal_tex = Plane(normal_texels, normal, 2, w, h);
+    const glsl_texture2D rough_tex = Plane(rough_texels, roughness, 1, w, h);
+    const glsl_texture2D rank_tex = Rgba(ranking, 128, 128), sobol_tex = Rgba(sobol, 256, 1);
+    std::vector<uint> material_idx(size_t(w) * h, 0u);
+    // packUnorm 10:10:10:2 of (opacity 0, roughness 1, metalness 0) and the
+    // roughness-map feature bit (common/material.hsh:52-92)
+    static uint packed_material[8];
+    packed_material[4] = 1023u << 10;
+    packed_material[7] = 1u << 4;
+    std::vector<vec4> image(size_t(w) * h);
+    for (size_t i = 0; i < image.size(); i++) image[i] = vec4(out[4 * i], out[4 * i + 1], out[4 * i + 2], out[4 * i + 3]);
+    const int gx = (w + 7) / 8, gy = (h + 3) / 4;
+#define AEG_SCREEN_RUN(T)                                                                  \
+    T::rtrImage.texels = image.data();                                                     \
+    T::rtrImage.width = w;                                                                 \
+    T::rtrImage.height = h;                                                                \
+    T::normalTexture.tex = &normal_tex;                                                    \
+    T::normalTexture.clamp_to_edge = true;                                                 \
+    T::normalTexture.subtexel_bits = 8;                                                    \
+    T::depthTexture.tex = &depth_tex;                                                      \
+    T::roughnessMetallicAoTexture.tex = &rough_tex;                                        \
+    T::offsetTexture.texels = offset;                                                      \
+    T::offsetTexture.width = w;                                                            \
+    T::offsetTexture.height = h;                                                           \
+    T::materialIdxTexture.texels = material_idx.data();                                    \
+    T::materialIdxTexture.width = w;                                                       \
+    T::materialIdxTexture.height = h;                                                      \
+    T::packedMaterials = reinterpret_cast<T::PackedMaterial*>(packed_material);            \
+    T::scramblingRankingTexture.tex = &rank_tex;                                           \
+    T::sobolSequenceTexture.tex = &sobol_tex;                                              \
+    T::environmentMap.constant = vec4(params[3], params[4], params[5], 1.0f);              \
+    T::uniforms.radianceLimit = params[0];                                                 \
+    T::uniforms.bias = params[1];                                                          \
+    T::uniforms.roughnessCutoff = params[2];                                               \
+    T::uniforms.frameSeed = frame_seed;                                                    \
+    T::uniforms.textureLevel = 0;                                                          \
+    T::uniforms.halfRes = half_res;                                                        \
+    T::uniforms.resolution = ivec2(w, h);                                                  \
+    T::globalData.ipMatrix = ColumnMajor(ip);                                              \
+    T::globalData.ivMatrix = ColumnMajor(iv);                                              \
+    gl_NumWorkGroups = uvec3(uint(gx), uint(gy), 1u);                                      \
+    for (int by = 0; by < gy; by++)                                                        \
+        for (int bx = 0; bx < gx; bx++)                                                    \
+            for (uint ly = 0; ly < 4u; ly++)                                               \
+                for (uint lx = 0; lx < 8u; lx++) {                                         \
+                    gl_WorkGroupID = uvec3(uint(bx), uint(by), 0u);                        \
+                    gl_LocalInvocationID = uvec3(lx, ly, 0u);                              \
+                    gl_LocalInvocationIndex = ly * 8u + lx;                                \
+                    gl_GlobalInvocationID = uvec3(uint(bx) * 8u + lx, uint(by) * 4u + ly, 0u); \
+                    T::T##_main();                                                         \
+                }
+    if (kind == 0) {
+        if (opacity_check) { AEG_SCREEN_RUN(aeg_rtr_opacity) } else { AEG_SCREEN_RUN(aeg_rtr) }
+    } else {
+        if (opacity_check) { AEG_SCREEN_RUN(aeg_rtgi_opacity) } else { AEG_SCREEN_RUN(aeg_rtgi) }
+    }
+#undef AEG_SCREEN_RUN
+    for (size_t i = 0; i < image.size(); i++)
+        for (int c = 0; c < 4; c++) out[4 * i + c] = image[i].v[c];
 }
 
 // SampleBlueNoise(pixel, sample_index, 0 and 1) for every pixel of a w x h

@@ -57,6 +57,10 @@ PROGRAMS = {
     "glsl_pt": ("aeg_pt", ["pathtracer/rayHit.csh"], []),
     "glsl_rtao": ("aeg_rtao", ["ao/rtao.csh"], []),
     "glsl_rtao_opacity": ("aeg_rtao_opacity", ["ao/rtao.csh"], ["OPACITY_CHECK"]),
+    "glsl_rtr": ("aeg_rtr", ["reflection/rtreflection.csh"], []),
+    "glsl_rtr_opacity": ("aeg_rtr_opacity", ["reflection/rtreflection.csh"], ["OPACITY_CHECK"]),
+    "glsl_rtgi": ("aeg_rtgi", ["rtgi/rtgi.csh"], []),
+    "glsl_rtgi_opacity": ("aeg_rtgi_opacity", ["rtgi/rtgi.csh"], ["OPACITY_CHECK"]),
 }
 # The engine compiles its shaders with bindless resources (AE_BINDLESS: one
 # buffer per mesh) and, where registers allow, the traversal stack in local
@@ -66,14 +70,18 @@ PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
 # rtao.csh: 8 x 4)
 WORKGROUP = {"aeg_raygen": "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n",
              "aeg_rtao": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
-             "aeg_rtao_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n"}
+             "aeg_rtao_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_rtr": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_rtr_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_rtgi": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_rtgi_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n"}
 GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
                 "static glsl_texture2D* bindlessTextures = nullptr;\n"
                 "static glsl_sampler bindlessSampler;\n"
                 # the members of globals.hsh's GlobalBuffer that rayGen.csh,
                 # rtao.csh and convert.hsh read
                 "struct GlobalBufferStub { vec2 jitterCurrent; vec4 cameraLocation; mat4 ivMatrix; "
-                "mat4 ipMatrix; };\n"
+                "mat4 ipMatrix; uint frameCount; };\n"
                 "static GlobalBufferStub globalData;\n")
 
 _INCLUDE = re.compile(r'^\s*#include\s*<([^>]+)>\s*$')

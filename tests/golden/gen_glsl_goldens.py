@@ -386,8 +386,8 @@ RTAO_RADIUS = 8.0
 RTAO_FRAMES = (5, 300)          # uniforms.frameSeed; 300 wraps the sample index
 
 
-def rtao_scene(seed=20261207):
-    """A seeded two-level scene for the ambient-occlusion goldens: a terrain
+def pass_scene(seed=20261207):
+    """A seeded two-level scene for the screen-space pass goldens: a terrain
     patch with boxes (mesh 0, one identity instance), a box with
     per-triangle opacities (mesh 1) standing on it four times, and a sheet
     of sixteen quads with per-triangle opacities (mesh 2) hovering over it
@@ -462,11 +462,23 @@ def rtao_scene(seed=20261207):
         mats[t] = -1
     mats["opacityTexture"] = rng.integers(-1, 3, 12)
     mats["invertUVs"] = rng.integers(0, 2, 12)
+    mats["baseColor"] = rng.uniform(0.2, 0.9, (12, 3))
+    mats["roughness"] = rng.uniform(0.05, 1.0, 12)
+    mats["metalness"] = np.where(rng.random(12) < 0.3, 1.0, 0.0)
+    mats["reflectance"] = rng.uniform(0.2, 0.8, 12)
+    mats["ao"] = 1.0
+    mats["emissiveColor"][[5, 9]] = [[2.0, 1.5, 1.0], [0.5, 1.0, 2.0]]
     tex = [rng.integers(0, 256, (16, 32), dtype=np.uint8),
            rng.integers(0, 256, (8, 5, 4), dtype=np.uint8),
            rng.uniform(-0.2, 1.2, (33, 7)).astype(F32)]
+    # one directional light (GPULight: N is the light's direction; type 0 in
+    # the top bits of data.x; selection pdf 1)
+    light = np.zeros((1, 16), F32)
+    light[0, 4:7] = np.array([-0.35, -1.0, 0.45]) / np.linalg.norm([-0.35, -1.0, 0.45])
+    light[0, 8:11] = (2.5, 2.3, 2.0)
+    light[0, 13] = 1.0
     return {"top": top.nodes_f32.copy(), "instances": ordered, "meshes": meshes, "materials": mats,
-            "textures": tex, "rays8": np.zeros((0, 8), F32)}
+            "textures": tex, "lights": light, "rays8": np.zeros((0, 8), F32)}
 
 
 def set_scene(lib: C.CDLL, sc: dict, keep: list):
@@ -491,26 +503,27 @@ def blue_noise_textures(seed=20261206):
     return (rng.integers(0, 256, (128, 128, 4), dtype=np.uint8), rng.integers(0, 256, (256, 4), dtype=np.uint8))
 
 
-def rtao_camera(w: int, h: int):
-    """View and projection matrices of the ambient-occlusion goldens."""
+def pass_camera(w: int, h: int):
+    """View and projection matrices of the screen-space pass goldens."""
     sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
     from atlas_rt import gbuffer as G
     return G.look_at((8.0, 16.0, -5.0), (8.0, 4.0, 9.0)), G.perspective(60.0, w / h, 0.5, 400.0)
 
 
-def rtao_gbuffer(lib: C.CDLL, sc: dict, w: int, h: int, seed: int = 7):
-    """A half-resolution G-buffer of the traversal scene (the lib's scene
-    must be sc): the eye ray of each pixel through 2 * pixel + offset + 0.5
-    of the full resolution, traced by the reference's HitClosest; depth =
-    the hit's NDC depth (1 where nothing is hit), normal = the encoded
-    view-space face normal of the hit triangle, turned towards the eye."""
+def pass_gbuffer(lib: C.CDLL, sc: dict, w: int, h: int, half_res: bool = True, seed: int = 7):
+    """A G-buffer of pass_scene (the lib's scene must be sc): the eye ray of
+    each pixel (at half resolution through 2 * pixel + offset + 0.5 of the
+    full one) traced by the reference's HitClosest; depth = the hit's NDC
+    depth (1 where nothing is hit), normal = the encoded view-space face
+    normal of the hit triangle, turned towards the eye; a roughness plane
+    with mirror (0, <= 0.01), glossy, rough and untraced (> 1) pixels."""
     sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
     from atlas_rt import gbuffer as G
     from atlas_rt import scenes
     rng = np.random.default_rng(seed)
-    V, P = rtao_camera(w, h)
-    offset = rng.integers(0, 4, w * h).astype(np.uint8)
-    o, d = G.view_rays(V, P, w, h, offset)
+    V, P = pass_camera(w, h)
+    offset = rng.integers(0, 4, w * h).astype(np.uint8) if half_res else np.zeros(w * h, np.uint8)
+    o, d = G.view_rays(V, P, w, h, offset if half_res else None)
     rays8 = np.ascontiguousarray(scenes.rays8(o.astype(F32), d.astype(F32), 0.0, 1e12), F32)
     hits = np.zeros((w * h, 4), F32)
     lib.aeglsl_scene_trace(C.c_int(0), C.c_void_p(rays8.ctypes.data), C.c_int(w * h), C.c_uint(0xFFFFFFFF),
@@ -533,23 +546,37 @@ def rtao_gbuffer(lib: C.CDLL, sc: dict, w: int, h: int, seed: int = 7):
     nv /= np.linalg.norm(nv, axis=1, keepdims=True) + 1e-30
     enc = np.zeros((w * h, 2))
     enc[hit] = G.encode_normal(nv[hit])
+    rough = rng.uniform(0.0, 1.1, w * h)
+    rough[rng.random(w * h) < 0.15] = 0.0
+    rough[rng.random(w * h) < 0.05] = 0.008
     return {"depth": depth.astype(F32).reshape(h, w), "normal": enc.astype(F32).reshape(h, w, 2),
-            "offset": offset.reshape(h, w), "ip_matrix": np.linalg.inv(P), "iv_matrix": np.linalg.inv(V)}
+            "offset": offset.reshape(h, w), "roughness": rough.astype(F32).reshape(h, w), "half_res": int(half_res),
+            "ip_matrix": np.linalg.inv(P), "iv_matrix": np.linalg.inv(V)}
 
 
 def column_major(m):
     return np.ascontiguousarray(np.asarray(m, np.float64).astype(F32).T.reshape(-1))
 
 
-def trace_rtao(lib: C.CDLL) -> dict:
-    """One dispatch of the reference's rtao.csh (HitAny and, with
-    OPACITY_CHECK, HitAnyTransparency) per case, frame seed and variant over
-    rtao_scene; unwritten pixels stay -1.  Also the blue-noise vectors of one
-    128 x 128 period per frame seed, stored as the integers v * 256 - 0.5."""
+# rtreflection.csh / rtgi.csh: (width, height, half resolution), their
+# uniforms (radianceLimit, bias, roughnessCutoff, the environment's colour)
+# and frame seed
+SHADE_CASES = ((64, 40, False), (48, 30, True))
+SHADE_PARAMS = (4.0, 0.1, 0.8, 0.05, 0.1, 0.2)
+SHADE_FRAME = 7
+
+
+def trace_passes(lib: C.CDLL) -> dict:
+    """Over pass_scene: one dispatch of the reference's rtao.csh (HitAny and,
+    with OPACITY_CHECK, HitAnyTransparency) per case, frame seed and variant,
+    unwritten pixels staying -1, and the blue-noise vectors of one 128 x 128
+    period per frame seed, stored as the integers v * 256 - 0.5; one
+    dispatch of rtreflection.csh and of rtgi.csh per case and variant."""
     P = C.c_void_p
-    sc, keep = rtao_scene(), []
+    sc, keep = pass_scene(), []
     set_scene(lib, sc, keep)
-    out = {"rtao_scene_digest": np.frombuffer(scene_digest(sc).encode(), np.uint8)}
+    lib.aeglsl_scene_lights(P(sc["lights"].ctypes.data), C.c_int(len(sc["lights"])))
+    out = {"pass_scene_digest": np.frombuffer(scene_digest(sc).encode(), np.uint8)}
     rank, sobol = blue_noise_textures()
     rank_f, sobol_f = texture_rgba(rank), texture_rgba(sobol[None])
     for f in RTAO_FRAMES:
@@ -560,7 +587,7 @@ def trace_rtao(lib: C.CDLL) -> dict:
         assert np.array_equal(q, np.round(q)) and q.min() >= 0 and q.max() <= 255
         out[f"rtao_blue_noise_{f}"] = q.astype(np.uint8)
     for w, h in RTAO_CASES:
-        gb = rtao_gbuffer(lib, sc, w, h)
+        gb = pass_gbuffer(lib, sc, w, h)
         key = f"rtao_{w}x{h}"
         for k in ("depth", "normal", "offset"):
             out[f"{key}_{k}"] = gb[k]
@@ -574,6 +601,23 @@ def trace_rtao(lib: C.CDLL) -> dict:
                                 P(sobol_f.ctypes.data), P(ip.ctypes.data), P(iv.ctypes.data), C.c_float(RTAO_RADIUS),
                                 C.c_int(f), P(ao.ctypes.data))
                 out[f"{key}_ao_{f}_{opacity}"] = ao
+    params = np.array(SHADE_PARAMS, F32)
+    for w, h, half in SHADE_CASES:
+        gb = pass_gbuffer(lib, sc, w, h, half_res=half, seed=11)
+        key = f"shade_{w}x{h}"
+        for k in ("depth", "normal", "offset", "roughness"):
+            out[f"{key}_{k}"] = gb[k]
+        off = np.ascontiguousarray(gb["offset"], np.int32)
+        ip, iv = column_major(gb["ip_matrix"]), column_major(gb["iv_matrix"])
+        for kind, name in ((0, "reflections"), (1, "rtgi")):
+            for opacity in (0, 1):
+                img = np.full((h, w, 4), -1.0, F32)
+                lib.aeglsl_screen_pass(C.c_int(kind), C.c_int(opacity), C.c_int(w), C.c_int(h), C.c_int(int(half)),
+                                       P(gb["depth"].ctypes.data), P(gb["normal"].ctypes.data), P(off.ctypes.data),
+                                       P(gb["roughness"].ctypes.data), P(rank_f.ctypes.data), P(sobol_f.ctypes.data),
+                                       P(ip.ctypes.data), P(iv.ctypes.data), P(params.ctypes.data),
+                                       C.c_uint(SHADE_FRAME), P(img.ctypes.data))
+                out[f"{key}_{name}_{opacity}"] = img
     return out
 
 
@@ -599,7 +643,7 @@ def main():
     pt = {}
     for name in pt_cases():
         pt.update(trace_pt(lib, name))
-    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib), **pt, **trace_rtao(lib),
+    np.savez_compressed(OUT, **ins, **evaluate(lib, ins), **trav, **trace_raygen(lib), **pt, **trace_passes(lib),
                         trav_scene_digest=np.frombuffer(scene_digest(sc).encode(), np.uint8))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
 

@@ -49,7 +49,7 @@ def test_fixture_is_what_the_reference_writes():
     for name in G.pt_cases():
         for k, v in G.trace_pt(lib, name).items():
             assert np.array_equal(np.asarray(v, g[k].dtype), g[k]), k
-    for k, v in G.trace_rtao(lib).items():
+    for k, v in G.trace_passes(lib).items():
         assert np.array_equal(np.asarray(v).view(np.uint8), np.asarray(g[k]).view(np.uint8)), k
 
 
@@ -399,23 +399,42 @@ def test_gpu_path_tracer_matches_the_engines_estimator(name):
 _RTAO = {}
 
 
-def rtao_scene():
-    """The seeded scene of the rtao_* goldens, rebuilt and checked against
-    the fixture's digest, with the oracle's scene tuple (instance model
-    matrices inverted from the instances' inverse ones)."""
+def pass_scene():
+    """The seeded scene of the rtao_* and shade_* goldens, rebuilt and
+    checked against the fixture's digest, with the oracle's scene tuple
+    (instance model matrices inverted from the instances' inverse ones)."""
     if "sc" not in _RTAO:
         G = _generator()
-        sc = G.rtao_scene()
-        assert G.scene_digest(sc) == bytes(S.golden()["rtao_scene_digest"]).decode()
+        sc = G.pass_scene()
+        assert G.scene_digest(sc) == bytes(S.golden()["pass_scene_digest"]).decode()
         model = np.zeros((len(sc["instances"]), 12), np.float32)
         for i, ins in enumerate(sc["instances"]):
             a = np.eye(4)
             a[:3] = np.asarray(ins["inverseMatrix"], np.float64).reshape(3, 4)
             model[i] = np.linalg.inv(a)[:3].reshape(-1)
-        oracle = (sc["top"], sc["instances"], model, sc["meshes"], sc["materials"], np.zeros((0, 16), np.float32),
-                  sc["textures"])
+        oracle = (sc["top"], sc["instances"], model, sc["meshes"], sc["materials"], sc["lights"], sc["textures"])
         _RTAO["sc"] = (sc, oracle)
     return _RTAO["sc"]
+
+
+def upload_pass_scene(sc):
+    """A context holding pass_scene: its three meshes, instances, materials,
+    opacity textures and light."""
+    import atlas_rt
+    ctx = atlas_rt.Context(device=0)
+    for k, (nodes, gt, sh) in enumerate(sc["meshes"]):
+        assert ctx.upload_mesh(nodes, gt, sh) == k
+    ctx.scene_set(sc["top"], sc["instances"])
+    ctx.set_materials(sc["materials"])
+    ctx.set_textures(sc["textures"])
+    ctx.set_lights(sc["lights"])
+    return ctx
+
+
+def to_device(gb):
+    import torch
+    return {k: (torch.from_numpy(np.ascontiguousarray(v)).cuda() if isinstance(v, np.ndarray) and k not in
+                ("ip_matrix", "iv_matrix") else v) for k, v in gb.items()}
 
 
 def rtao_gbuffer(w, h):
@@ -424,7 +443,7 @@ def rtao_gbuffer(w, h):
     G = _generator()
     g = S.golden()
     key = f"rtao_{w}x{h}"
-    V, P = G.rtao_camera(w, h)
+    V, P = G.pass_camera(w, h)
     rank, sobol = G.blue_noise_textures()
     return {"depth": g[key + "_depth"], "normal": g[key + "_normal"], "offset": g[key + "_offset"], "half_res": 1,
             "ip_matrix": np.linalg.inv(P), "iv_matrix": np.linalg.inv(V), "scrambling_ranking": rank,
@@ -490,7 +509,7 @@ def test_oracle_rtao_matches_reference_rtao(w, h, frame, opacity):
     textures) against the reference's rtao.csh compiled on the host: one
     whole dispatch each, with and without OPACITY_CHECK."""
     import pyoracle
-    sc, oracle = rtao_scene()
+    sc, oracle = pass_scene()
     G = _generator()
     ref = S.golden()[f"rtao_{w}x{h}_ao_{frame}_{opacity}"]
     got = pyoracle.pass_screen("rtao", oracle, rtao_gbuffer(w, h), radius=G.RTAO_RADIUS, opacity_check=bool(opacity),
@@ -527,19 +546,13 @@ def test_gpu_rtao_matches_reference_rtao():
     import torch
     import atlas_rt
     import pyoracle
-    sc, oracle = rtao_scene()
+    sc, oracle = pass_scene()
     G = _generator()
-    ctx = atlas_rt.Context(device=0)
+    ctx = upload_pass_scene(sc)
     try:
-        for k, (nodes, gt, sh) in enumerate(sc["meshes"]):
-            assert ctx.upload_mesh(nodes, gt, sh) == k
-        ctx.scene_set(sc["top"], sc["instances"])
-        ctx.set_materials(sc["materials"])
-        ctx.set_textures(sc["textures"])
         for w, h, frame, opacity in _rtao_cases():
             gb = rtao_gbuffer(w, h)
-            dev = {k: (torch.from_numpy(np.ascontiguousarray(v)).cuda() if isinstance(v, np.ndarray) and k not in
-                       ("ip_matrix", "iv_matrix") else v) for k, v in gb.items()}
+            dev = to_device(gb)
             out = torch.full((h, w), -5.0, dtype=torch.float32, device="cuda")
             params = dict(radius=G.RTAO_RADIUS, opacity_check=bool(opacity), frame_seed=frame)
             ctx.rtao(dev, out, **params)
@@ -559,5 +572,92 @@ def test_gpu_rtao_matches_reference_rtao():
             ctx.rtao(dev2, out2, **params)
             ctx.synchronize()
             np.testing.assert_array_equal(out2.cpu().numpy(), got)
+    finally:
+        ctx.close()
+
+
+# ---- the reflection and GI passes: rtreflection.csh and rtgi.csh ----
+
+SHADE_KINDS = ("reflections", "rtgi")
+
+
+def shade_gbuffer(w, h, half):
+    G = _generator()
+    g = S.golden()
+    key = f"shade_{w}x{h}"
+    V, P = G.pass_camera(w, h)
+    rank, sobol = G.blue_noise_textures()
+    return {"depth": g[key + "_depth"], "normal": g[key + "_normal"], "offset": g[key + "_offset"],
+            "roughness": g[key + "_roughness"], "half_res": int(half), "ip_matrix": np.linalg.inv(P),
+            "iv_matrix": np.linalg.inv(V), "scrambling_ranking": rank, "sobol_sequence": sobol}
+
+
+def shade_params(opacity):
+    G = _generator()
+    lim, bias, cut, r, g, b = G.SHADE_PARAMS
+    return dict(radiance_limit=lim, bias=bias, roughness_cutoff=cut, environment=(r, g, b),
+                opacity_check=bool(opacity), frame_seed=G.SHADE_FRAME)
+
+
+def shade_error(got, ref, atol):
+    """Per pixel: the largest channel difference over atol + the pixel's
+    largest channel (a radiance bound of atol absolute plus 1 relative)."""
+    d = np.abs(got[..., :3] - ref[..., :3]).max(-1)
+    return d / (atol + np.abs(ref[..., :3]).max(-1))
+
+
+def _shade_cases():
+    G = _generator()
+    return [(w, h, half, kind, op) for (w, h, half) in G.SHADE_CASES for kind in SHADE_KINDS for op in (0, 1)]
+
+
+@pytest.mark.parametrize("w,h,half,kind,opacity", _shade_cases())
+def test_oracle_shading_passes_match_reference(w, h, half, kind, opacity):
+    """The oracle's reflection and GI passes against the reference's
+    rtreflection.csh / rtgi.csh compiled on the host: one whole dispatch each
+    over a full- and a half-resolution G-buffer (mirror, glossy, rough,
+    cut-off and untraced pixels), with and without OPACITY_CHECK, one
+    directional light (shadows by HitAnyTransparency), emissive and
+    partly transparent surfaces, the radiance limit and a constant
+    environment.  Most pixels agree bit for bit; every pixel to 1e-5 + 1e-3
+    of its largest channel (the rest differ by the rounding of the ray
+    setup and the BRDF, which a dim pixel's cancellations magnify), alpha is
+    1 everywhere, and pixels whose light term is negative (a one-sided back
+    face lit from its front side) keep it as the shaders do."""
+    import pyoracle
+    sc, oracle = pass_scene()
+    ref = S.golden()[f"shade_{w}x{h}_{kind}_{opacity}"]
+    got = pyoracle.pass_screen(kind, oracle, shade_gbuffer(w, h, half), **shade_params(opacity))
+    assert (got[..., 3] == 1.0).all() and (ref[..., 3] == 1.0).all()
+    err = shade_error(got, ref, 1e-2)
+    assert err.max() < 1e-3, err.max()
+    assert (err == 0).mean() > 0.8
+    assert (ref[..., :3] < 0).any(axis=-1).sum() > 0 and (ref[..., :3] > 0.5).any(axis=-1).sum() > 0
+
+
+@pytest.mark.gpu
+def test_gpu_shading_passes_match_reference():
+    """The GPU's reflection and GI passes (ae_rt_reflections / ae_rt_rtgi,
+    blue-noise vectors drawn on the device) against the reference's
+    rtreflection.csh / rtgi.csh over the same scene and G-buffers.  Most
+    pixels agree bit for bit and 99 % to 1e-4 of (1e-2 + the pixel's largest
+    channel); the device's ray setup and BRDF use fast single-precision sin /
+    cos / pow / rsqrt, which a dim pixel's cancellations magnify, so every
+    pixel is held to 5e-3 of that bound."""
+    import torch
+    sc, oracle = pass_scene()
+    ctx = upload_pass_scene(sc)
+    try:
+        for w, h, half, kind, opacity in _shade_cases():
+            gb = shade_gbuffer(w, h, half)
+            out = torch.full((h, w, 4), -5.0, dtype=torch.float32, device="cuda")
+            getattr(ctx, kind)(to_device(gb), out, **shade_params(opacity))
+            ctx.synchronize()
+            got = out.cpu().numpy()
+            ref = S.golden()[f"shade_{w}x{h}_{kind}_{opacity}"]
+            assert (got[..., 3] == 1.0).all()
+            err = shade_error(got, ref, 1e-2)
+            assert err.max() < 5e-3 and (err < 1e-4).mean() > 0.99, (kind, opacity, w, err.max())
+            assert (err == 0).mean() > 0.8
     finally:
         ctx.close()
