@@ -39,6 +39,8 @@
 typedef unsigned int uint;
 
 // ---- swizzles: N components of type T, read as V, written component-wise ----
+// (a vector constructed from a swizzle, such as ivec3(v.xzy), converts the
+// swizzled vector, not the storage under it)
 template <typename V, typename T, int N, int... I>
 struct Swz {
     T v[N];
@@ -64,6 +66,8 @@ struct Swz {
         V(T a, T b) : x(a), y(b) {}                                                       \
         template <typename U, typename = decltype(static_cast<const U*>(nullptr)->v)>        \
         explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])) {}                            \
+        template <typename SV, typename ST, int SN, int... SI>                            \
+        explicit V(const Swz<SV, ST, SN, SI...>& s) : V(s.operator SV()) {}               \
         template <typename U, typename = typename std::enable_if<std::is_arithmetic<U>::value>::type, \
                   typename = void>                                                        \
         explicit V(U s) : x(T(s)), y(T(s)) {}                                             \
@@ -91,6 +95,8 @@ struct Swz {
         V(const V& o) : x(o.x), y(o.y), z(o.z) {}                                         \
         template <typename U, typename = decltype(static_cast<const U*>(nullptr)->v)>        \
         explicit V(const U& o) : x(T(o.v[0])), y(T(o.v[1])), z(T(o.v[2])) {}              \
+        template <typename SV, typename ST, int SN, int... SI>                            \
+        explicit V(const Swz<SV, ST, SN, SI...>& s) : V(s.operator SV()) {}               \
         template <typename U, typename = typename std::enable_if<std::is_arithmetic<U>::value>::type, \
                   typename = void>                                                        \
         explicit V(U s) : x(T(s)), y(T(s)), z(T(s)) {}                                    \
@@ -121,6 +127,8 @@ struct Swz {
         V(const V2& a, T c, T d) : x(a.x), y(a.y), z(c), w(d) {}                          \
         V(const V2& a, const V2& b) : x(a.x), y(a.y), z(b.x), w(b.y) {}                   \
         V(const V& o) : x(o.x), y(o.y), z(o.z), w(o.w) {}                                 \
+        template <typename SV, typename ST, int SN, int... SI>                            \
+        explicit V(const Swz<SV, ST, SN, SI...>& s) : V(s.operator SV()) {}               \
         V& operator=(const V& o) { x = o.x; y = o.y; z = o.z; w = o.w; return *this; }   \
         T& operator[](int i) { return v[i]; }                                             \
         T operator[](int i) const { return v[i]; }                                        \
@@ -271,6 +279,7 @@ struct mat3 {
     vec3 c[3];
     mat3() {}
     mat3(const vec3& a, const vec3& b, const vec3& d) { c[0] = a; c[1] = b; c[2] = d; }
+    explicit mat3(const struct mat4& m);   // the upper-left 3 x 3 (section 5.4.2)
     vec3& operator[](int i) { return c[i]; }
     const vec3& operator[](int i) const { return c[i]; }
 };
@@ -290,6 +299,7 @@ struct mat4 {
     vec4& operator[](int i) { return c[i]; }
     const vec4& operator[](int i) const { return c[i]; }
 };
+inline mat3::mat3(const mat4& m) { for (int i = 0; i < 3; i++) c[i] = vec3(m.c[i].x, m.c[i].y, m.c[i].z); }
 inline vec3 operator*(const mat3& m, const vec3& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
 inline vec3 operator*(const vec3& v, const mat3& m) { return vec3(dot(v, m.c[0]), dot(v, m.c[1]), dot(v, m.c[2])); }
 inline vec4 operator*(const mat4& m, const vec4& v) {
@@ -495,3 +505,7 @@ static uvec3 gl_NumWorkGroups;
 static uvec3 gl_LocalInvocationID;
 static uint gl_LocalInvocationIndex = 0;
 #define nonuniformEXT(x) (x)
+// one invocation runs at a time, each to its end, in invocation order: a
+// barrier() after which the group reads only what invocation 0 wrote before
+// it (ddgi/rayGen.csh) holds without waiting
+inline void barrier() {}

@@ -25,6 +25,9 @@
 //   the reflection and diffuse GI passes, one dispatch each (with and
 //   without OPACITY_CHECK)              reflection/rtreflection.csh:60-245,
 //                                            rtgi/rtgi.csh:60-234
+//   the DDGI probe rays: ray generation, the trace dispatch and the hit
+//   shader                               ddgi/rayGen.csh:39-81,
+//                                            ddgi/rayHit.csh:37-151
 #include "glsl.hpp"
 #include "glsl_ref.inc"
 #include "glsl_raygen.inc"
@@ -35,6 +38,8 @@
 #include "glsl_rtr_opacity.inc"
 #include "glsl_rtgi.inc"
 #include "glsl_rtgi_opacity.inc"
+#include "glsl_ddgi_raygen.inc"
+#include "glsl_ddgi.inc"
 
 using namespace aeg_glsl;
 
@@ -188,6 +193,7 @@ void aeglsl_scene(const void* tlas, const void* instances, int n_meshes, const v
     AEG_SCENE_INTO(aeg_rtr_opacity)
     AEG_SCENE_INTO(aeg_rtgi)
     AEG_SCENE_INTO(aeg_rtgi_opacity)
+    AEG_SCENE_INTO(aeg_ddgi)
 #undef AEG_SCENE_INTO
 }
 
@@ -200,6 +206,7 @@ void aeglsl_scene_lights(const void* lights, int n_lights) {
     AEG_LIGHTS_INTO(aeg_rtr_opacity)
     AEG_LIGHTS_INTO(aeg_rtgi)
     AEG_LIGHTS_INTO(aeg_rtgi_opacity)
+    AEG_LIGHTS_INTO(aeg_ddgi)
 #undef AEG_LIGHTS_INTO
 }
 
@@ -531,6 +538,114 @@ void aeglsl_screen_pass(int kind, int opacity_check, int w, int h, int half_res,
 #undef AEG_SCREEN_RUN
     for (size_t i = 0; i < image.size(); i++)
         for (int c = 0; c < 4; c++) out[4 * i + c] = image[i].v[c];
+}
+
+// One DDGI probe-ray pass as DDGIRenderer.cpp:93-175 issues it, one cascade:
+// ddgi/rayGen.csh over grid[0] x grid[1] x grid[2] work groups of 32, the
+// trace dispatch (traceClosest.csh:12-36: HitClosest, or HitClosestTransparency
+// with opacity_check, from 0 to INF) and ddgi/rayHit.csh over every ray slot,
+// over the scene and lights of aeglsl_scene / aeglsl_scene_lights.  The
+// hit shader's irradiance volume is given an empty box (volumeMax below
+// volumeMin), so IsInsideVolume is false and no indirect term is added.
+//   volume_min, cell_size  3 floats each (cascade 0)
+//   states     one PROBE_STATE_* per probe, offsets 4 floats per probe (the
+//              history buffers; probes in the engine's order,
+//              Flatten3D(probe.xzy))
+//   dirs / dirs_inactive  ray_count / inactive_count x 4 floats
+//   rotation   16 floats, column-major (Uniforms.randomRotation)
+//   env        the environment's colour; seed: the hit shader's Uniforms.seed
+//   origins    out: 4 floats per probe, the origin of its rays
+//   hits       n_probes * ray_count x 4 floats (PackedRayHit), in / out;
+//              slots past a probe's ray count keep their value
+void aeglsl_ddgi(const int* grid, const float* volume_min, const float* cell_size, uint ray_count,
+                 uint inactive_count, const uint* states, const float* offsets, const float* dirs,
+                 const float* dirs_inactive, const float* rotation, int opacity_check, const float* env, float seed,
+                 float* origins, float* hits) {
+    namespace R = aeg_ddgi_rg;
+    namespace H = aeg_ddgi;
+    const int nx = grid[0], ny = grid[1], nz = grid[2], n = nx * ny * nz;
+    const uint total = uint(n) * ray_count;
+    std::vector<R::PackedRay> rays(size_t(2) * total);
+    std::vector<vec4> history_states(static_cast<size_t>(n)), zeros(static_cast<size_t>(n), vec4(0.0f));
+    for (int p = 0; p < n; p++) history_states[p] = vec4(uintBitsToFloat(states[p]), 0.0f, 0.0f, 0.0f);
+    static uint read_count[1], write_count[1];
+    auto volume = [&](auto& d, bool empty) {
+        d.cascades[0].volumeMin = vec4(volume_min[0], volume_min[1], volume_min[2], 0.0f);
+        d.cascades[0].cellSize = vec4(cell_size[0], cell_size[1], cell_size[2], 0.0f);
+        d.cascades[0].volumeMax = empty ? vec4(volume_min[0] - 1.0f, volume_min[1] - 1.0f, volume_min[2] - 1.0f, 0.0f)
+                                        : vec4(volume_min[0] + cell_size[0] * float(nx - 1),
+                                               volume_min[1] + cell_size[1] * float(ny - 1),
+                                               volume_min[2] + cell_size[2] * float(nz - 1), 0.0f);
+        d.cascades[0].offsetDifference = ivec4(0, 0, 0, 0);
+        d.volumeProbeCount = ivec4(nx, ny, nz, n);
+        d.cascadeCount = 1;
+        d.rayCount = ray_count;
+        d.inactiveRayCount = inactive_count;
+    };
+    // ray generation into the first half of the ray buffer
+    volume(R::ddgiData, false);
+    R::rayDirs = reinterpret_cast<vec4*>(const_cast<float*>(dirs));
+    R::rayDirsInactiveProbes = reinterpret_cast<vec4*>(const_cast<float*>(dirs_inactive));
+    R::historyProbeStates = history_states.data();
+    R::historyProbeOffsets = reinterpret_cast<vec4*>(const_cast<float*>(offsets));
+    R::Uniforms.randomRotation = ColumnMajor(rotation);
+    R::rays = rays.data();
+    R::readAtomic = read_count;
+    R::writeAtomic = write_count;
+    R::PushConstants.rayBufferOffset = 0u;
+    R::PushConstants.rayBufferSize = total;
+    R::PushConstants.useRayBinning = 0;
+    write_count[0] = 0u;
+    gl_NumWorkGroups = uvec3(uint(nx), uint(ny), uint(nz));
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++)
+                for (uint l = 0; l < 32u; l++) {
+                    gl_WorkGroupID = uvec3(uint(x), uint(y), uint(z));
+                    gl_LocalInvocationID = uvec3(l, 0u, 0u);
+                    gl_LocalInvocationIndex = l;
+                    gl_GlobalInvocationID = uvec3(uint(x) * 32u + l, uint(y), uint(z));
+                    R::aeg_ddgi_rg_main();
+                }
+    for (int p = 0; p < n; p++) {
+        const R::Ray r = R::UnpackRay(rays[size_t(p) * ray_count]);
+        origins[4 * p] = r.origin.x;
+        origins[4 * p + 1] = r.origin.y;
+        origins[4 * p + 2] = r.origin.z;
+        origins[4 * p + 3] = 0.0f;
+    }
+    // the trace dispatch, then the hit shader over every slot
+    H::PackedRay* hr = reinterpret_cast<H::PackedRay*>(rays.data());
+    for (uint i = 0; i < total; i++) {
+        H::Ray r = H::UnpackRay(hr[i]);
+        r.hitID = -1;
+        r.hitDistance = 0.0f;
+        if (r.ID >= 0) {
+            if (opacity_check) H::HitClosestTransparency(r, INSTANCE_MASK_ALL, 0.0f, INF);
+            else H::HitClosest(r, INSTANCE_MASK_ALL, 0.0f, INF);
+        }
+        hr[i] = H::PackRay(r);
+    }
+    volume(H::ddgiData, true);
+    H::probeStates = zeros.data();
+    H::probeOffsets = zeros.data();
+    H::rays = hr;
+    H::readAtomic = read_count;
+    H::writeAtomic = write_count;
+    H::hits = reinterpret_cast<H::PackedRayHit*>(hits);
+    H::Uniforms.seed = seed;
+    H::environmentMap.constant = vec4(env[0], env[1], env[2], 1.0f);
+    H::PushConstants.rayBufferOffset = 1u;
+    H::PushConstants.rayBufferSize = total;
+    H::PushConstants.useRayBinning = 0;
+    read_count[0] = total;
+    for (uint i = 0; i < total; i++) {
+        gl_GlobalInvocationID = uvec3(i, 0u, 0u);
+        gl_LocalInvocationID = uvec3(i % 32u, 0u, 0u);
+        gl_LocalInvocationIndex = i % 32u;
+        gl_WorkGroupID = uvec3(i / 32u, 0u, 0u);
+        H::aeg_ddgi_main();
+    }
 }
 
 // SampleBlueNoise(pixel, sample_index, 0 and 1) for every pixel of a w x h

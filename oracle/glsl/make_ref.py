@@ -61,20 +61,25 @@ PROGRAMS = {
     "glsl_rtr_opacity": ("aeg_rtr_opacity", ["reflection/rtreflection.csh"], ["OPACITY_CHECK"]),
     "glsl_rtgi": ("aeg_rtgi", ["rtgi/rtgi.csh"], []),
     "glsl_rtgi_opacity": ("aeg_rtgi_opacity", ["rtgi/rtgi.csh"], ["OPACITY_CHECK"]),
+    "glsl_ddgi_raygen": ("aeg_ddgi_rg", ["ddgi/rayGen.csh"], []),
+    "glsl_ddgi": ("aeg_ddgi", ["ddgi/rayHit.csh"], []),
 }
 # The engine compiles its shaders with bindless resources (AE_BINDLESS: one
 # buffer per mesh) and, where registers allow, the traversal stack in local
 # memory (LOCAL_STACK, bvh.hsh:39-42); compute shaders see one invocation.
 PREAMBLE = "#define AE_BINDLESS\n#define LOCAL_STACK\n"
-# the compute shaders' work-group sizes (rayGen.csh: local_size 8 x 8;
-# rtao.csh: 8 x 4)
+# the compute shaders' work-group sizes (pathtracer/rayGen.csh: local_size
+# 8 x 8; rtao.csh, rtreflection.csh, rtgi.csh: 8 x 4; ddgi/rayGen.csh and
+# ddgi/rayHit.csh: 32)
 WORKGROUP = {"aeg_raygen": "static const uvec3 gl_WorkGroupSize(8u, 8u, 1u);\n",
              "aeg_rtao": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
              "aeg_rtao_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
              "aeg_rtr": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
              "aeg_rtr_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
              "aeg_rtgi": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
-             "aeg_rtgi_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n"}
+             "aeg_rtgi_opacity": "static const uvec3 gl_WorkGroupSize(8u, 4u, 1u);\n",
+             "aeg_ddgi_rg": "static const uvec3 gl_WorkGroupSize(32u, 1u, 1u);\n",
+             "aeg_ddgi": "static const uvec3 gl_WorkGroupSize(32u, 1u, 1u);\n"}
 GLOBALS_STUB = ("static glsl_sampler2D dfgTexture;\n"
                 "static glsl_texture2D* bindlessTextures = nullptr;\n"
                 "static glsl_sampler bindlessSampler;\n"

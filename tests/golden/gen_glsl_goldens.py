@@ -566,6 +566,48 @@ SHADE_PARAMS = (4.0, 0.1, 0.8, 0.05, 0.1, 0.2)
 SHADE_FRAME = 7
 
 
+# DDGI probe rays: a 4 x 3 x 4 grid over pass_scene (some probes under the
+# ground or inside boxes, so back faces are met), 32 rays per probe and 8 for
+# inactive ones, the environment's colour and the hit shader's seed
+DDGI_GRID = (4, 3, 4)
+DDGI_VOLUME = ((1.0, 8.5, 1.0), (4.5, 1.6, 4.5))
+DDGI_RAYS = (32, 8)
+DDGI_ENV = (0.25, 0.5, 0.75)
+DDGI_SEED = 0.37
+
+
+def fibonacci_dirs(n):
+    """n unit directions on a Fibonacci sphere as vec4 (w = 0)."""
+    i = np.arange(n) + 0.5
+    z = 1.0 - 2.0 * i / n
+    r = np.sqrt(1.0 - z * z)
+    phi = np.pi * (3.0 - np.sqrt(5.0)) * i
+    return np.stack([r * np.cos(phi), z, r * np.sin(phi), np.zeros(n)], axis=1).astype(F32)
+
+
+def ddgi_inputs(seed=20261209):
+    """Probe states (new, active, inactive), history offsets, the two
+    direction sets and the frame's rotation (4 x 4, row-major) of the DDGI
+    goldens; and pass_scene's materials without opacity textures (the hit
+    shader reads textures at mip level 4, and the harness's textures have
+    level 0 only)."""
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(DDGI_GRID))
+    states = rng.integers(0, 3, n).astype(np.uint32)
+    offsets = np.zeros((n, 4), F32)
+    offsets[:, :3] = rng.uniform(-0.3, 0.3, (n, 3))
+    rot = np.eye(4)
+    rot[:3, :3] = _rotation(rng)
+    return states, offsets, fibonacci_dirs(DDGI_RAYS[0]), fibonacci_dirs(DDGI_RAYS[1]), rot
+
+
+def ddgi_materials(sc):
+    m = sc["materials"].copy()
+    m["opacityTexture"] = -1
+    m["cullBackFaces"][::2] = 1        # back faces of these are reported (negative distance)
+    return m
+
+
 def trace_passes(lib: C.CDLL) -> dict:
     """Over pass_scene: one dispatch of the reference's rtao.csh (HitAny and,
     with OPACITY_CHECK, HitAnyTransparency) per case, frame seed and variant,
@@ -618,6 +660,24 @@ def trace_passes(lib: C.CDLL) -> dict:
                                        P(ip.ctypes.data), P(iv.ctypes.data), P(params.ctypes.data),
                                        C.c_uint(SHADE_FRAME), P(img.ctypes.data))
                 out[f"{key}_{name}_{opacity}"] = img
+    # DDGI: the scene again with the materials of ddgi_materials
+    dsc = dict(sc, materials=ddgi_materials(sc))
+    set_scene(lib, dsc, keep)
+    states, offsets, dirs, dirs_in, rot = ddgi_inputs()
+    n = len(states)
+    grid = np.array(DDGI_GRID, np.int32)
+    vmin, cell = (np.array(v, F32) for v in DDGI_VOLUME)
+    env = np.array(DDGI_ENV, F32)
+    rotc = column_major(rot)
+    for opacity in (0, 1):
+        origins = np.zeros((n, 4), F32)
+        hits = np.full((n * DDGI_RAYS[0], 4), -7.0, F32)
+        lib.aeglsl_ddgi(P(grid.ctypes.data), P(vmin.ctypes.data), P(cell.ctypes.data), C.c_uint(DDGI_RAYS[0]),
+                        C.c_uint(DDGI_RAYS[1]), P(states.ctypes.data), P(offsets.ctypes.data), P(dirs.ctypes.data),
+                        P(dirs_in.ctypes.data), P(rotc.ctypes.data), C.c_int(opacity), P(env.ctypes.data),
+                        C.c_float(DDGI_SEED), P(origins.ctypes.data), P(hits.ctypes.data))
+        out[f"ddgi_origins_{opacity}"] = origins
+        out[f"ddgi_hits_{opacity}"] = hits
     return out
 
 

@@ -661,3 +661,84 @@ def test_gpu_shading_passes_match_reference():
             assert (err == 0).mean() > 0.8
     finally:
         ctx.close()
+
+
+# ---- DDGI probe rays: ddgi/rayGen.csh, the trace dispatch, ddgi/rayHit.csh ----
+
+def ddgi_case(opacity):
+    """The golden DDGI pass: the probes as the library takes them (the
+    engine's ray origins, probe state bits in w), the direction sets, the
+    rotation and the reference's PackedRayHit buffer (-7 where untouched)."""
+    G = _generator()
+    g = S.golden()
+    states, offsets, dirs, dirs_in, rot = G.ddgi_inputs()
+    probes = g[f"ddgi_origins_{opacity}"].copy()
+    probes[:, 3] = states.view(np.float32)
+    return probes, dirs, dirs_in, rot, g[f"ddgi_hits_{opacity}"]
+
+
+def unpack_ray_hits(h):
+    """PackedRayHit (ddgi/ddgi.hsh:70-98) -> direction, radiance, distance."""
+    u = np.ascontiguousarray(h[:, :3]).view(np.uint32)
+    lo = (u & 0xFFFF).astype(np.uint16).view(np.float16).astype(np.float32)
+    hi = (u >> 16).astype(np.uint16).view(np.float16).astype(np.float32)
+    d = np.stack([lo[:, 0], hi[:, 0], lo[:, 2]], 1)
+    r = np.stack([lo[:, 1], hi[:, 1], hi[:, 2]], 1)
+    return d, r, h[:, 3]
+
+
+def check_ddgi(got, ref, dir_tol, rad_tol, dist_tol):
+    untouched = np.all(ref == -7.0, axis=1)
+    np.testing.assert_array_equal(untouched, np.all(got == -7.0, axis=1))
+    gd, gr, gt = unpack_ray_hits(got[~untouched])
+    rd, rr, rt = unpack_ray_hits(ref[~untouched])
+    np.testing.assert_array_equal(np.signbit(gt), np.signbit(rt))       # back faces: negative distance
+    assert (rt < 0).mean() > 0.05 and 0.2 < untouched.mean() < 0.5
+    np.testing.assert_allclose(gd, rd, rtol=0, atol=dir_tol)
+    np.testing.assert_allclose(gr, rr, rtol=rad_tol, atol=rad_tol * 0.1)
+    np.testing.assert_allclose(gt, rt, rtol=dist_tol)
+
+
+@pytest.mark.parametrize("opacity", [0, 1])
+def test_oracle_ddgi_matches_reference(opacity):
+    """The oracle's DDGI probe rays against the reference's ddgi/rayGen.csh,
+    trace dispatch and ddgi/rayHit.csh compiled on the host over a 4 x 3 x 4
+    probe grid (new, active and inactive probes; 32 and 8 rays; some probes
+    under the ground or inside boxes, so one-sided back faces report a
+    negative distance), one directional light and emitters: the packed
+    directions and radiance bit for bit, distances to 1e-5."""
+    import pyoracle
+    sc, oracle = pass_scene()
+    G = _generator()
+    probes, dirs, dirs_in, rot, ref = ddgi_case(opacity)
+    oracle = oracle[:4] + (G.ddgi_materials(sc),) + oracle[5:]
+    got = np.full(ref.shape, -7.0, np.float32)
+    pyoracle.pass_ddgi(oracle, probes, dirs, rot, got, ray_dirs_inactive=dirs_in, inactive_ray_count=len(dirs_in),
+                       environment=G.DDGI_ENV, opacity_check=bool(opacity))
+    np.testing.assert_array_equal(got[:, :3].view(np.uint32), ref[:, :3].view(np.uint32))
+    check_ddgi(got, ref, 0.0, 0.0, 1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_ddgi_matches_reference():
+    """The GPU's DDGI probe rays (ae_rt_ddgi_trace) against the reference's
+    rayGen.csh, trace dispatch and rayHit.csh: the same slots written, the
+    back faces the same, directions to one half-precision step, radiance to
+    2e-3 (fast sin / cos / pow in the BRDF, then half precision) and
+    distances to 1e-4."""
+    import torch
+    sc, oracle = pass_scene()
+    G = _generator()
+    ctx = upload_pass_scene(sc)
+    try:
+        ctx.set_materials(G.ddgi_materials(sc))
+        for opacity in (0, 1):
+            probes, dirs, dirs_in, rot, ref = ddgi_case(opacity)
+            out = torch.full(ref.shape, -7.0, dtype=torch.float32, device="cuda")
+            dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            ctx.ddgi_trace(dev(probes), dev(dirs), rot, out, ray_dirs_inactive=dev(dirs_in),
+                           inactive_ray_count=len(dirs_in), environment=G.DDGI_ENV, opacity_check=bool(opacity))
+            ctx.synchronize()
+            check_ddgi(out.cpu().numpy(), ref, 2.0 ** -10, 2e-3, 1e-4)
+    finally:
+        ctx.close()
