@@ -624,17 +624,16 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
             const float4* np = (top ? p.tlas : blasNodes) + size_t(node) * 4;
             float4 n0, n1, n2, n3;
             ldg_node(np, n0, n1, n2, n3);
-            float hl, hr;
-            bool il, ir;
+            bool il, ir, leftFirst;
             bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
-            test_children<false>(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, hl, hr, nearCullUnused);
+            test_children<false>(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, !ANY, false, il, ir,
+                                 leftFirst, nearCullUnused);
             const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
             int32_t next, far;
             if (ANY) {
                 next = il ? lptr : rptr;
                 far = rptr;
             } else {
-                const bool leftFirst = hl <= hr;
                 next = leftFirst ? lptr : rptr;
                 far = leftFirst ? rptr : lptr;
             }

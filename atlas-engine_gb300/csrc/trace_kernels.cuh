@@ -343,18 +343,63 @@ struct TRay {
     }
 };
 
-// Both child boxes of a node (IntersectAABB x 2, bvh.hsh:229-232 / :253-256).
-// node.padding0 != 0 marks a node holding a coordinate outside the fast window
-// (set by the upload); such nodes, out-of-window rays and the BOUNDS variant
-// (whose nodes did not go through the upload) divide with div.rn.
-// nearCull: either box was rejected with its entry within kTieWindow of the
-// bound (see kTieWindow); only closest-hit callers read it.
+// Approximate IntersectAABB for the screening below: the six quotients as
+// RN(RN(c - o) * RN(1/d)) instead of the shader's RN((c - o) / d).  Each
+// lies within 3 units of 2^-24 (relative) of the shader's quotient and has
+// its sign (zero exactly when c == o), and min / max carry that bound over
+// to the entry lo and exit hi.
+__device__ __forceinline__ void box_approx(const TRay& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                           float tmin, float tmax, float& lo, float& hi) {
+    const float t0x = fmul(fsub(lx, r.ox), r.yx), t0y = fmul(fsub(ly, r.oy), r.yy), t0z = fmul(fsub(lz, r.oz), r.yz);
+    const float t1x = fmul(fsub(hx, r.ox), r.yx), t1y = fmul(fsub(hy, r.oy), r.yy), t1z = fmul(fsub(hz, r.oz), r.yz);
+    lo = fmaxf(fmaxf(tmin, fminf(t0x, t1x)), fmaxf(fminf(t0y, t1y), fminf(t0z, t1z)));
+    hi = fminf(fminf(tmax, fmaxf(t0x, t1x)), fminf(fmaxf(t0y, t1y), fmaxf(t0z, t1z)));
+}
+
+// x <= y decided from approximations x', y' >= 0 that are each within 8 units
+// of 2^-24 (relative) of x and y: x' <= y' * kSure proves x <= y, and
+// x' * kSure > y' proves x > y (kSure = 1 - 2^-20 leaves room for the rounding
+// of the product); anything between is a close call.
+constexpr float kSure = 0.99999904632568359375f;
+
+// Both child boxes of a node (IntersectAABB x 2, bvh.hsh:229-232 / :253-256)
+// as the traversal uses them: il / ir whether each box is hit;
+// leftFirst = (distL <= distR) for the descent order (only read when
+// `ordered`), with a missed box reporting the bound as the shader's does;
+// nearCull (only when `ties`): a box was rejected with its entry within
+// kTieWindow of the bound (see kTieWindow).
+// Inside the fast-division window (node.padding0 == 0 marks a node whose
+// coordinates are in it, set by the upload; the ray's own flag; tmin >= 0)
+// the quotients are correctly rounded from the reciprocal (div_rn_from_rcp);
+// outside it and for the BOUNDS variant (whose nodes did not go through the
+// upload) they divide with div.rn.  A traversal that needs only il / ir (any
+// hit: neither ordered nor ties) first screens the boxes with box_approx:
+// every hit decision that the approximations settle with a margin of 16
+// units of 2^-24 is the shader's, and only a lane with a close call (a
+// grazing ray) computes the quotients exactly.  Closest-hit traversals
+// compare entry distances, which are often exactly equal (sibling boxes
+// with a common face), so they take the exact quotients at once.
 template <bool BOUNDS>
 __device__ __forceinline__ void test_children(const TRay& r, const float4& n0, const float4& n1, const float4& n2,
-                                              const float4& n3, float tmin, float bound, bool& il, bool& ir,
-                                              float& hl, float& hr, bool& nearCull) {
+                                              const float4& n3, float tmin, float bound, bool ordered, bool ties,
+                                              bool& il, bool& ir, bool& leftFirst, bool& nearCull) {
+    const bool fast = !BOUNDS && r.fast && __float_as_int(n3.z) == 0;
+    if (fast && !ordered && !ties && tmin >= 0.0f) {
+        float lol, hil, lor, hir;
+        box_approx(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, bound, lol, hil);
+        box_approx(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, bound, lor, hir);
+        // lo >= tmin >= 0, so a negative exit is a sure miss
+        il = hil >= 0.0f && lol <= fmul(hil, kSure);
+        ir = hir >= 0.0f && lor <= fmul(hir, kSure);
+        const bool close = (!il && hil >= 0.0f && !(fmul(lol, kSure) > hil)) ||
+                           (!ir && hir >= 0.0f && !(fmul(lor, kSure) > hir));
+        leftFirst = true;
+        nearCull = false;
+        if (!close) return;
+    }
     bool nl, nr;
-    if (!BOUNDS && r.fast && __float_as_int(n3.z) == 0) {
+    float hl, hr;
+    if (fast) {
         il = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y,
                             tmin, bound, hl, nl);
         ir = box_test<true>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w,
@@ -365,6 +410,7 @@ __device__ __forceinline__ void test_children(const TRay& r, const float4& n0, c
         ir = box_test<false>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.yx, r.yy, r.yz, n1.z, n1.w, n2.x, n2.y, n2.z,
                              n2.w, tmin, bound, hr, nr);
     }
+    leftFirst = hl <= hr;
     nearCull = nl || nr;
 }
 
@@ -698,16 +744,15 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     }
                     if (COUNT) nodeCount++;
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
-                    float hl, hr;
-                    bool il, ir, nearCull;
-                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, hl, hr, nearCull);
+                    bool il, ir, leftFirst, nearCull;
+                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, !anyQ, TIES && !anyQ, il, ir,
+                                          leftFirst, nearCull);
                     if (TIES && !anyQ) tieSuspect = tieSuspect || nearCull;
                     int32_t next, far;
                     if (anyQ) {
                         next = il ? lptr : rptr;
                         far = rptr;
                     } else {
-                        const bool leftFirst = hl <= hr;
                         next = leftFirst ? lptr : rptr;
                         far = leftFirst ? rptr : lptr;
                         // bvh.hsh:234-236: with only the right box hit and its

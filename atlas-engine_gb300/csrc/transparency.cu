@@ -118,10 +118,10 @@ __global__ void transparency_kernel(TransParams p) {
                     } else {
                         const float4* np = p.tlas + size_t(nodePtr) * 4;
                         const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-                        bool il, ir;
-                        float hl, hr;
+                        bool il, ir, leftFirst;
                         bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
-                        test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr, nearCullUnused);
+                        test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, !ANY, false, il, ir,
+                                             leftFirst, nearCullUnused);
                         const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
                         if (ANY) {
                             next = il ? l : rr;
@@ -130,10 +130,10 @@ __global__ void transparency_kernel(TransParams p) {
                                 stack[sp++] = rr;
                             }
                         } else {
-                            next = hl <= hr ? l : rr;
+                            next = leftFirst ? l : rr;
                             if (il && ir) {
                                 if (sp >= kTransStack) { flags |= kHitFlagOverflow; atomicOr(p.error_word, kErrStackOverflow); break; }
-                                stack[sp++] = hl <= hr ? rr : l;
+                                stack[sp++] = leftFirst ? rr : l;
                             }
                         }
                         pop = !il && !ir;
@@ -165,10 +165,10 @@ __global__ void transparency_kernel(TransParams p) {
                 } else {
                     const float4* np = blasNodes + size_t(nodePtr) * 4;
                     const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-                    bool il, ir;
-                    float hl, hr;
+                    bool il, ir, leftFirst;
                     bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
-                    test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, il, ir, hl, hr, nearCullUnused);
+                    test_children<false>(r, n0, n1, n2, n3, tMin, ANY ? tMax : hitDist, !ANY, false, il, ir, leftFirst,
+                                         nearCullUnused);
                     const int32_t l = __float_as_int(n3.x), rr = __float_as_int(n3.y);
                     if (ANY) {
                         next = il ? l : rr;
@@ -177,10 +177,10 @@ __global__ void transparency_kernel(TransParams p) {
                             stack[sp++] = rr;
                         }
                     } else {
-                        next = hl <= hr ? l : rr;
+                        next = leftFirst ? l : rr;
                         if (il && ir) {
                             if (sp >= kTransStack) { flags |= kHitFlagOverflow; atomicOr(p.error_word, kErrStackOverflow); break; }
-                            stack[sp++] = hl <= hr ? rr : l;
+                            stack[sp++] = leftFirst ? rr : l;
                         }
                     }
                     pop = !il && !ir;
