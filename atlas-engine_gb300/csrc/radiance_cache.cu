@@ -110,15 +110,15 @@ ae_rt_status AdamStep(ae_rc* rc, cudaStream_t s) {
     a.beta2 = rc->cfg.beta2;
     a.eps = rc->cfg.epsilon;
     a.step_scale = scale;
+    a.zero_grad = 1;
+    RcAdamParams g = a;
     a.master = rc->mlp_master; a.m = rc->mlp_m; a.v = rc->mlp_v; a.grad = rc->mlp_grad;
     a.out_bf16 = rc->mlp_bf16; a.out_f16 = nullptr; a.n = RC_NPARAM;
-    a.zero_grad = 1;
-    rc_adam_kernel<<<(RC_NPARAM / 4 + 255) / 256, 256, 0, s>>>(a);
-    RC_CUDA(rc, cudaGetLastError());
-    a.master = rc->grid_master; a.m = rc->grid_m; a.v = rc->grid_v; a.grad = rc->grid_grad;
-    a.out_bf16 = nullptr; a.out_f16 = rc->grid_f16; a.n = rc->grid_params;
-    a.skip_zero = 1;
-    rc_adam_kernel<<<uint32_t(rc->sm_count) * 8u, 256, 0, s>>>(a);
+    g.master = rc->grid_master; g.m = rc->grid_m; g.v = rc->grid_v; g.grad = rc->grid_grad;
+    g.out_bf16 = nullptr; g.out_f16 = rc->grid_f16; g.n = rc->grid_params;
+    g.skip_zero = 1;
+    const uint32_t mlp_blocks = (RC_NPARAM / 4 + 255) / 256;
+    rc_adam_kernel<<<mlp_blocks + uint32_t(rc->sm_count) * 8u, 256, 0, s>>>(a, g, mlp_blocks);
     RC_CUDA(rc, cudaGetLastError());
     rc->grads_zero = true;
     return AE_RT_OK;

@@ -512,10 +512,12 @@ __device__ __forceinline__ void adam1(const RcAdamParams& a, float gr, float& w,
     w = w - a.lr * a.step_scale * m / (sqrtf(v) + a.eps);
 }
 
-static __global__ void rc_adam_kernel(RcAdamParams a) {
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
+// One Adam step over the parameter set `a` by `blocks` blocks of the grid,
+// the first of them `block`.
+__device__ __forceinline__ void rc_adam_range(const RcAdamParams& a, uint32_t block, uint32_t blocks) {
+    const size_t stride = size_t(blocks) * blockDim.x;
     const size_t n4 = a.n / 4;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    for (size_t i = size_t(block) * blockDim.x + threadIdx.x; i < n4; i += stride) {
         const float4 g = reinterpret_cast<const float4*>(a.grad)[i];
         const bool z[4] = { g.x == 0.0f, g.y == 0.0f, g.z == 0.0f, g.w == 0.0f };
         if (a.skip_zero && z[0] && z[1] && z[2] && z[3]) continue;
@@ -545,9 +547,19 @@ static __global__ void rc_adam_kernel(RcAdamParams a) {
     }
 }
 
+// The MLP's and the hash grid's Adam steps in one launch: the first
+// `mlp_blocks` blocks update the MLP, the rest the grid.
+static __global__ void rc_adam_kernel(RcAdamParams mlp, RcAdamParams grid, uint32_t mlp_blocks) {
+    if (blockIdx.x < mlp_blocks) rc_adam_range(mlp, blockIdx.x, mlp_blocks);
+    else rc_adam_range(grid, blockIdx.x - mlp_blocks, gridDim.x - mlp_blocks);
+}
+
 // ---- inline two-level traversal for the training-path kernel ----
-// HitClosest / HitAny over the scene with a per-thread local stack (the same
-// arithmetic and visiting order as trace_kernel<MODE_SCENE>).
+// HitClosest / HitAny over the scene with a per-thread local stack: the
+// structure of trace_kernel<MODE_SCENE>, with the conservative approximate
+// box test (test_children_loose) and tri_test_fast.  The training
+// targets are Monte Carlo estimates, so the nearest hit may break exact
+// distance ties in another order than the shader's traversal.
 template <bool ANY>
 __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, float oz, float dx, float dy, float dz,
                                    float tmin, float tmax, float& tOut, int32_t& triOut, int32_t& instOut,
@@ -609,7 +621,7 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
                              c = __ldg(blasTris + size_t(tp) * 3 + 2);
                 end = a.w > 0.0f;
                 float t, u, v;
-                const bool hit = tri_test(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
+                const bool hit = tri_test_fast(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v);
                 if (ANY) {
                     if (hit && t > tmin && t < tmax) { occl = true; end = true; }
                 } else if (hit && t > tmin && t < tmax && t < hitDist) {
@@ -625,9 +637,7 @@ __device__ bool scene_trace_inline(const TraceParams& p, float ox, float oy, flo
             float4 n0, n1, n2, n3;
             ldg_node(np, n0, n1, n2, n3);
             bool il, ir, leftFirst;
-            bool nearCullUnused;   // near-tie detection is the closest-hit trace's alone
-            test_children<false>(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, !ANY, false, il, ir,
-                                 leftFirst, nearCullUnused);
+            test_children_loose(top ? wr : r, n0, n1, n2, n3, tmin, ANY ? tmax : hitDist, il, ir, leftFirst);
             const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
             int32_t next, far;
             if (ANY) {

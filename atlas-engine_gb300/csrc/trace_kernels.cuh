@@ -264,6 +264,25 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
     return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
 }
 
+// IntersectTriangle with one reciprocal of the denominator instead of three
+// divisions, for traversals whose results are statistical (the radiance
+// cache's training paths): t, u, v within a few units of 2^-24 of the
+// shader's; the same accept test.
+__device__ __forceinline__ bool tri_test_fast(float ox, float oy, float oz, float dx, float dy, float dz,
+                                              const float4& a, const float4& b, const float4& c,
+                                              float& t, float& u, float& v) {
+    const float e0x = b.x - a.x, e0y = b.y - a.y, e0z = b.z - a.z;
+    const float e1x = c.x - a.x, e1y = c.y - a.y, e1z = c.z - a.z;
+    const float sx = ox - a.x, sy = oy - a.y, sz = oz - a.z;
+    const float px = sy * e0z - e0y * sz, py = sz * e0x - e0z * sx, pz = sx * e0y - e0x * sy;
+    const float qx = dy * e1z - e1y * dz, qy = dz * e1x - e1z * dx, qz = dx * e1y - e1x * dy;
+    const float inv = __frcp_rn(qx * e0x + qy * e0y + qz * e0z);
+    t = (px * e1x + py * e1y + pz * e1z) * inv;
+    u = (qx * sx + qy * sy + qz * sz) * inv;
+    v = (px * dx + py * dy + pz * dz) * inv;
+    return t >= 0.0f && u >= 0.0f && v >= 0.0f && u + v <= 1.0f;
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -412,6 +431,31 @@ __device__ __forceinline__ void test_children(const TRay& r, const float4& n0, c
     }
     leftFirst = hl <= hr;
     nearCull = nl || nr;
+}
+
+// Both child boxes for traversals whose results are statistical rather than
+// the shader's bit for bit (the radiance cache's training paths): the
+// approximate quotients of box_approx with no exact re-test.  A box counts
+// as hit when its entry is at most its exit times 1 + 2^-20, so the test
+// never rejects a box that the exact test accepts (it may accept a grazed
+// one); the order follows the approximate entries.  Outside the
+// fast-division window it is test_children.
+constexpr float kLoose = 1.00000095367431640625f;   // 1 + 2^-20
+
+__device__ __forceinline__ void test_children_loose(const TRay& r, const float4& n0, const float4& n1,
+                                                    const float4& n2, const float4& n3, float tmin, float bound,
+                                                    bool& il, bool& ir, bool& leftFirst) {
+    if (r.fast && __float_as_int(n3.z) == 0 && tmin >= 0.0f) {
+        float lol, hil, lor, hir;
+        box_approx(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, bound, lol, hil);
+        box_approx(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, bound, lor, hir);
+        il = lol <= fmul(hil, kLoose);
+        ir = lor <= fmul(hir, kLoose);
+        leftFirst = (il ? lol : bound) <= (ir ? lor : bound);
+        return;
+    }
+    bool unused;
+    test_children<false>(r, n0, n1, n2, n3, tmin, bound, true, false, il, ir, leftFirst, unused);
 }
 
 // vec4(v, w) * inverseMatrix (bvh.hsh:179-180): component i = dot(vec4(v, w),
