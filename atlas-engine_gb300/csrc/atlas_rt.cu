@@ -40,14 +40,14 @@ using atlas::rt::dev::MODE_BATCH;
 using atlas::rt::dev::MODE_MESH;
 using atlas::rt::dev::MODE_SCENE;
 
-template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0>
+template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0, bool LOOSE = false>
 void* KernelFor() {
     // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
     // more per-lane state and get ~73
     constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
         &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks, false, TIES && !ANY,
-                                      STAGE>);
+                                      STAGE, LOOSE>);
 }
 
 // ties = false: the caller discards the near-tie flag (the library's path
@@ -55,9 +55,14 @@ void* KernelFor() {
 // AE_RT_CFG_NO_NEAR_TIES, so the kernel skips its detection.
 // staged: the ray tiles go through shared memory by bulk copy
 // (AE_RT_CFG_STAGED_RAYS; single-mesh and scene launches without counters).
+// loose: the approximate traversal of the radiance cache's render (scene
+// launches without the near-tie flag or counters).
 template <int W, int S>
-void* PickShape(bool any, bool count, int mode, bool ties, bool staged) {
+void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loose) {
     constexpr int T = atlas::rt::dev::kStageRays;
+    if (loose && mode == MODE_SCENE && !ties && !count && !staged)
+        return any ? KernelFor<true, false, MODE_SCENE, W, S, false, 0, true>()
+                   : KernelFor<false, false, MODE_SCENE, W, S, false, 0, true>();
     if (staged && !count && mode != MODE_BATCH) {
         if (mode == MODE_SCENE) {
             if (any) return KernelFor<true, false, MODE_SCENE, W, S, true, T>();
@@ -85,12 +90,13 @@ void* PickShape(bool any, bool count, int mode, bool ties, bool staged) {
     return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
 }
 
-void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true, bool staged = false) {
+void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true, bool staged = false,
+                      bool loose = false) {
     switch (shape) {
-    case 1: return PickShape<2, 32>(any, count, mode, ties, staged);
-    case 2: return PickShape<8, 16>(any, count, mode, ties, staged);
-    case 3: return PickShape<4, 16>(any, count, mode, ties, staged);
-    default: return PickShape<4, 32>(any, count, mode, ties, staged);
+    case 1: return PickShape<2, 32>(any, count, mode, ties, staged, loose);
+    case 2: return PickShape<8, 16>(any, count, mode, ties, staged, loose);
+    case 3: return PickShape<4, 16>(any, count, mode, ties, staged, loose);
+    default: return PickShape<4, 32>(any, count, mode, ties, staged, loose);
     }
 }
 
@@ -185,14 +191,16 @@ uint32_t* WorkCounter(ae_rt_ctx* ctx) {
     return ctx->d_counter + (k == 0 ? 0u : k + 1u);          // word 1 is the error word
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true) {
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true,
+                    bool loose = false) {
     if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
     AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
-    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays);
+    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays,
+                               loose);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -203,7 +211,8 @@ constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
 
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                    float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
-                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true) {
+                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true,
+                   bool loose = false) {
     if (!ctx) return AE_RT_INVALID_ARG;
     const bool scene = mesh_id == kSceneTarget;
     if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
@@ -260,7 +269,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.cull_mask = cull_mask;
     }
     p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
-    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties);
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties, loose);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -293,9 +302,10 @@ ae_rt_status atlas::rt::host::EnsureBounceQueues(ae_rt_ctx* ctx, uint32_t capaci
 
 ae_rt_status atlas::rt::host::TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity,
                                              float tmin, float tmax, void* out, void* stream,
-                                             const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax) {
+                                             const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax,
+                                             bool loose) {
     return Trace(ctx, any, kSceneTarget, rays, capacity, tmin, tmax, out, stream, count_dev, cull_mask, per_ray_tmax,
-                 false);
+                 false, loose);
 }
 
 namespace {

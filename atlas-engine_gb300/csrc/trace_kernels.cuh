@@ -496,12 +496,17 @@ __device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, u
 // (double-buffered); refills then read rays from shared memory.  Single-mesh
 // and scene launches only.  A copy that does not complete within the bounded
 // wait sets kErrWaitTimeout and ends the warp's refills.
+//
+// LOOSE: the conservative approximate box test (test_children_loose) and
+// tri_test_fast, for consumers whose results are Monte Carlo estimates (the
+// radiance cache's render), not the shader's bit for bit.
 template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
-          bool BOUNDS = false, bool TIES = true, int STAGE = 0>
+          bool BOUNDS = false, bool TIES = true, int STAGE = 0, bool LOOSE = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     constexpr bool TLAS = MODE == MODE_SCENE;
     constexpr bool BATCH = MODE == MODE_BATCH;
     static_assert(STAGE == 0 || (!BATCH && !BOUNDS), "staged rays: single-mesh and scene launches only");
+    static_assert(!LOOSE || (!TIES && !BOUNDS), "loose traversal: no near-tie flag, uploaded nodes");
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
     __shared__ __align__(128) float4 s_rays[STAGE > 0 ? WARPS : 1][2][STAGE > 0 ? STAGE * 3 : 1];
     __shared__ __align__(8) uint64_t s_rbar[STAGE > 0 ? WARPS : 1][2];
@@ -758,8 +763,9 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                         if (COUNT) triCount++;
                         float t, u, v;
                         bool nearMiss = false;
-                        const bool hit = tri_test<TIES && !ANY>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v,
-                                                                &nearMiss);
+                        const bool hit = LOOSE ? tri_test_fast(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t, u, v)
+                                               : tri_test<TIES && !ANY>(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c, t,
+                                                                        u, v, &nearMiss);
                         if (anyQ) {
                             if (hit && t > tmin && t < tmax) { occl = true; end = true; }
                         } else if (hit && t > tmin && t < tmax) {
@@ -788,9 +794,12 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                     }
                     if (COUNT) nodeCount++;
                     const int32_t lptr = __float_as_int(n3.x), rptr = __float_as_int(n3.y);
-                    bool il, ir, leftFirst, nearCull;
-                    test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, !anyQ, TIES && !anyQ, il, ir,
-                                          leftFirst, nearCull);
+                    bool il, ir, leftFirst, nearCull = false;
+                    if (LOOSE)
+                        test_children_loose(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, il, ir, leftFirst);
+                    else
+                        test_children<BOUNDS>(cr, n0, n1, n2, n3, tmin, anyQ ? tmax : hitDist, !anyQ, TIES && !anyQ,
+                                              il, ir, leftFirst, nearCull);
                     if (TIES && !anyQ) tieSuspect = tieSuspect || nearCull;
                     int32_t next, far;
                     if (anyQ) {
