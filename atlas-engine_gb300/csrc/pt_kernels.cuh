@@ -19,7 +19,7 @@
 //   * a constant environment radiance on a miss (the engine samples its sky cubemap there), and -- deliberately --
 //     without the engine's clamp of indirect radiance at 10 (rayHit.csh:
 //     196-201), which biases the estimate; this renderer is the unbiased
-//     reference the radiance cache is judged against.
+//     reference the radiance cache is compared against.
 // Shadow rays are not traced inline: the shade kernel appends them, with the
 // contribution they would add, to a shadow queue that the any-hit kernel
 // traces and the resolve kernel adds into the accumulation buffers (FP32,
