@@ -58,6 +58,7 @@ MASK_SHADOW = 1 << 6
 CFG_COUNT_FETCHES = 0x1
 CFG_NO_NEAR_TIES = 0x2
 CFG_STAGED_RAYS = 0x4
+CFG_APPROXIMATE = 0x8
 
 
 def _check(status: int, ctx=None):
@@ -205,7 +206,7 @@ class Context:
     def __init__(self, device: int = 0, count_fetches: bool = False, blocks_per_sm: int = 0,
                  max_steps: int = 0, refill_steps: int = 0, threads_per_block: int = 0,
                  stack_entries_smem: int = 0, refill_below: int = 0, leaf_wait: int = 0,
-                 near_ties: bool = True, staged_rays: bool = False):
+                 near_ties: bool = True, staged_rays: bool = False, approximate: bool = False):
         cfg = Config()
         cfg.device = device
         cfg.blocks_per_sm = blocks_per_sm
@@ -213,7 +214,7 @@ class Context:
         cfg.stack_entries_smem = stack_entries_smem
         cfg.max_steps = max_steps
         cfg.flags = ((CFG_COUNT_FETCHES if count_fetches else 0) | (0 if near_ties else CFG_NO_NEAR_TIES)
-                     | (CFG_STAGED_RAYS if staged_rays else 0))
+                     | (CFG_STAGED_RAYS if staged_rays else 0) | (CFG_APPROXIMATE if approximate else 0))
         cfg.refill_steps = refill_steps
         cfg.refill_below = refill_below
         cfg.leaf_wait = leaf_wait

@@ -55,14 +55,18 @@ void* KernelFor() {
 // AE_RT_CFG_NO_NEAR_TIES, so the kernel skips its detection.
 // staged: the ray tiles go through shared memory by bulk copy
 // (AE_RT_CFG_STAGED_RAYS; single-mesh and scene launches without counters).
-// loose: the approximate traversal of the radiance cache's render (scene
-// launches without the near-tie flag or counters).
+// loose: the approximate traversal (AE_RT_CFG_APPROXIMATE, the radiance
+// cache's render): single-mesh and scene launches without counters or staged
+// rays, no near-tie flag.
 template <int W, int S>
 void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loose) {
     constexpr int T = atlas::rt::dev::kStageRays;
-    if (loose && mode == MODE_SCENE && !ties && !count && !staged)
+    if (loose && mode == MODE_SCENE && !count && !staged)
         return any ? KernelFor<true, false, MODE_SCENE, W, S, false, 0, true>()
                    : KernelFor<false, false, MODE_SCENE, W, S, false, 0, true>();
+    if (loose && mode == MODE_MESH && !count && !staged)
+        return any ? KernelFor<true, false, MODE_MESH, W, S, false, 0, true>()
+                   : KernelFor<false, false, MODE_MESH, W, S, false, 0, true>();
     if (staged && !count && mode != MODE_BATCH) {
         if (mode == MODE_SCENE) {
             if (any) return KernelFor<true, false, MODE_SCENE, W, S, true, T>();
@@ -200,7 +204,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
     void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays,
-                               loose);
+                               loose || ctx->approximate);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -372,6 +376,7 @@ ae_rt_status ae_rt_ctx_create(const ae_rt_config* cfg, ae_rt_ctx** out) {
     ctx->count_fetches = (c.flags & AE_RT_CFG_COUNT_FETCHES) != 0;
     ctx->near_ties = (c.flags & AE_RT_CFG_NO_NEAR_TIES) == 0;
     ctx->staged_rays = (c.flags & AE_RT_CFG_STAGED_RAYS) != 0;
+    ctx->approximate = (c.flags & AE_RT_CFG_APPROXIMATE) != 0;
     ctx->refill_steps = c.refill_steps;
     ctx->refill_below = c.refill_below == 0 ? atlas::rt::dev::kDefaultRefillBelow
                                             : (c.refill_below > 32 ? 0u : c.refill_below);

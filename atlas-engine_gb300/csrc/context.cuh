@@ -58,7 +58,8 @@ struct ae_rt_ctx {
     uint32_t leaf_wait = 0;
     bool count_fetches = false;
     bool near_ties = true;            // complete near-tie detection on closest-hit traces
-    bool staged_rays = false;         // ray tiles through shared memory by bulk copy
+    bool staged_rays = false;
+    bool approximate = false;   // AE_RT_CFG_APPROXIMATE         // ray tiles through shared memory by bulk copy
     std::vector<atlas::rt::host::DeviceMesh> meshes;
     // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot
     float4* d_tlas = nullptr;

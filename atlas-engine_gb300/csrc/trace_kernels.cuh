@@ -266,21 +266,28 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
 
 // IntersectTriangle with one reciprocal of the denominator instead of three
 // divisions, for traversals whose results are statistical (the radiance
-// cache's training paths): t, u, v within a few units of 2^-24 of the
-// shader's; the same accept test.
+// cache, AE_RT_CFG_APPROXIMATE): the numerators and the denominator are the
+// shader's, operation by operation (no contraction: the dot products of
+// nearly edge-on triangles cancel), and each of t, u, v is RN(RN(n) *
+// RN(1/den)), within 1.5 units of 2^-24 (relative) of the shader's RN(n / den);
+// the same accept test.
 __device__ __forceinline__ bool tri_test_fast(float ox, float oy, float oz, float dx, float dy, float dz,
                                               const float4& a, const float4& b, const float4& c,
                                               float& t, float& u, float& v) {
-    const float e0x = b.x - a.x, e0y = b.y - a.y, e0z = b.z - a.z;
-    const float e1x = c.x - a.x, e1y = c.y - a.y, e1z = c.z - a.z;
-    const float sx = ox - a.x, sy = oy - a.y, sz = oz - a.z;
-    const float px = sy * e0z - e0y * sz, py = sz * e0x - e0z * sx, pz = sx * e0y - e0x * sy;
-    const float qx = dy * e1z - e1y * dz, qy = dz * e1x - e1z * dx, qz = dx * e1y - e1x * dy;
-    const float inv = __frcp_rn(qx * e0x + qy * e0y + qz * e0z);
-    t = (px * e1x + py * e1y + pz * e1z) * inv;
-    u = (qx * sx + qy * sy + qz * sz) * inv;
-    v = (px * dx + py * dy + pz * dz) * inv;
-    return t >= 0.0f && u >= 0.0f && v >= 0.0f && u + v <= 1.0f;
+    const float e0x = fsub(b.x, a.x), e0y = fsub(b.y, a.y), e0z = fsub(b.z, a.z);
+    const float e1x = fsub(c.x, a.x), e1y = fsub(c.y, a.y), e1z = fsub(c.z, a.z);
+    const float sx = fsub(ox, a.x), sy = fsub(oy, a.y), sz = fsub(oz, a.z);
+    const float px = fsub(fmul(sy, e0z), fmul(e0y, sz));
+    const float py = fsub(fmul(sz, e0x), fmul(e0z, sx));
+    const float pz = fsub(fmul(sx, e0y), fmul(e0x, sy));
+    const float qx = fsub(fmul(dy, e1z), fmul(e1y, dz));
+    const float qy = fsub(fmul(dz, e1x), fmul(e1z, dx));
+    const float qz = fsub(fmul(dx, e1y), fmul(e1x, dy));
+    const float inv = __frcp_rn(fadd(fadd(fmul(qx, e0x), fmul(qy, e0y)), fmul(qz, e0z)));
+    t = fmul(fadd(fadd(fmul(px, e1x), fmul(py, e1y)), fmul(pz, e1z)), inv);
+    u = fmul(fadd(fadd(fmul(qx, sx), fmul(qy, sy)), fmul(qz, sz)), inv);
+    v = fmul(fadd(fadd(fmul(px, dx), fmul(py, dy)), fmul(pz, dz)), inv);
+    return t >= 0.0f && u >= 0.0f && v >= 0.0f && fadd(u, v) <= 1.0f;
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

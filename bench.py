@@ -1014,6 +1014,45 @@ def staged_rays_record(torch, dev, stream, flush, bvh, gt, tuned, prim, sec, shd
                 kept="staged" if tot["staged"] < tot["plain"] * 0.99 else "plain loads")
 
 
+def approximate_record(torch, dev, stream, flush, bvh, gt, tuned, prim, sec, shd, n, n_sec, n_shd, steps):
+    """The approximate traversal (AE_RT_CFG_APPROXIMATE, for Monte Carlo
+    consumers; not the headline, which is the shader's traversal bit for bit)
+    on the camera pass's three ray classes: each trace timed alone (L2
+    flushed before each) on an exact and an approximate context with the same
+    launch parameters, and how many closest hits name the same triangle."""
+    import atlas_rt
+    from atlas_rt import autotune as at
+    occ = torch.empty(n, dtype=torch.uint8, device=dev)
+
+    def timed(fn):
+        fn()
+        return float(np.mean(timed_steps(torch, dev, stream, fn, steps, flush)))
+    res, tri = {}, {}
+    for name, approx in (("exact", False), ("approximate", True)):
+        c = atlas_rt.Context(device=dev.index, near_ties=False, approximate=approx, **at.context_kwargs(tuned))
+        hp = torch.empty((n, 8), dtype=torch.float32, device=dev)
+        hs = torch.empty((max(n_sec, 1), 8), dtype=torch.float32, device=dev)
+        try:
+            m = c.upload_mesh(bvh.nodes, gt)
+            res[name] = {
+                "primary_ms": timed(lambda: c.trace_closest(m, prim, TMIN, TINF, out=hp, stream=stream, n_rays=n)),
+                "bounce_ms": timed(lambda: c.trace_closest(m, sec, TMIN, TINF, out=hs, stream=stream,
+                                                           n_rays=n_sec)),
+                "shadow_ms": timed(lambda: c.trace_any(m, shd, TMIN, TINF - 2 * EPSILON, out=occ, stream=stream,
+                                                       n_rays=n_shd))}
+            c.synchronize(stream)
+            tri[name] = (hp[:, 1].contiguous().view(torch.int32).clone(),
+                         hs[:n_sec, 1].contiguous().view(torch.int32).clone())
+        finally:
+            c.close()
+    tot = {k: sum(v.values()) for k, v in res.items()}
+    same = [float((a == b).float().mean()) for a, b in zip(tri["exact"], tri["approximate"])]
+    return dict(res, speedup=tot["exact"] / tot["approximate"],
+                same_triangle={"primary": same[0], "bounce": same[1]},
+                note="exact = the shader's traversal without the near-tie detection; approximate = "
+                     "AE_RT_CFG_APPROXIMATE (conservative approximate box tests, one-reciprocal triangles)")
+
+
 def run_autotune(torch, dev, stream, log):
     """--autotune: the launch-parameter search (atlas_rt/autotune.py) for the
     camera pass, random 65,536 (closest + any) and the path tracer (8 spp;
@@ -1259,6 +1298,8 @@ def main():
                            n, n_sec, max(args.steps // 2, 3))
     staged = staged_rays_record(torch, dev, stream, flush, bvh, gt, tuned_cast, prim, sec, shd, n, n_sec, n_shd,
                                 max(args.steps // 2, 3))
+    approximate = approximate_record(torch, dev, stream, flush, bvh, gt, tuned_cast, prim, sec, shd, n, n_sec, n_shd,
+                                     max(args.steps // 2, 3))
 
     ms = float(np.mean(step_ms))
     e2e = float(np.mean(e2e_ms))
@@ -1326,6 +1367,7 @@ def main():
         "tuning": {"source": "tuning.json" if tuned_cast else "defaults", "config": tuned_cast},
         "near_ties": dict(near, value_with_retest=world * closest_rays / ((ms + near["retest_ms"]) * 1e-3) / 1e6),
         "staged_rays": staged,
+        "approximate_traversal": approximate,
     }
     if not args.quick:
         wl = set(args.workloads.split(","))

@@ -356,7 +356,7 @@ typedef struct ae_rt_config {
     uint32_t blocks_per_sm;       /* persistent CTAs per SM (0 = the kernel's occupancy) */
     uint32_t threads_per_block;   /* 0 = 128 */
     uint32_t max_steps;           /* traversal step cap per ray (0 = 4 x nodes + 64) */
-    uint32_t flags;               /* AE_RT_CFG_COUNT_FETCHES, _NO_NEAR_TIES, _STAGED_RAYS */
+    uint32_t flags;               /* AE_RT_CFG_COUNT_FETCHES, _NO_NEAR_TIES, _STAGED_RAYS, _APPROXIMATE */
     uint32_t refill_steps;        /* traversal steps between warp refills (0 = 32) */
     uint32_t stack_entries_smem;  /* shared-memory stack entries per lane (0 = 32) */
     uint32_t refill_below;        /* also refill as soon as fewer than this many lanes of a warp
@@ -1085,6 +1085,23 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
  * buffers must be 16-byte aligned (as for the plain loads).  Results are
  * unchanged. */
 #define AE_RT_CFG_STAGED_RAYS   0x4u
+/* Every closest- and any-hit trace of the context over one mesh or the scene
+ * (also those of the library's path tracer and passes on it) uses the
+ * approximate traversal, for consumers whose results are Monte Carlo
+ * estimates rather than the shader's bit for bit: child boxes are tested with
+ * RN(RN(c - o) * RN(1/d)) instead of the correctly rounded quotient, with a
+ * margin of 2^-20 relative that never rejects a box the exact test accepts,
+ * and triangles with one reciprocal of the denominator.  The nearest
+ * triangle is the exact traversal's except where two triangles tie in t or
+ * a ray grazes a triangle edge within a few units in the last place of its
+ * barycentrics; for the same triangle t, u and v are within 1.5 units of
+ * 2^-24 (relative) of the exact ones; the near-tie flag marks only rays whose
+ * second accepted triangle lies within 1e-6 relative t (as with
+ * AE_RT_CFG_NO_NEAR_TIES).  The library's radiance cache traces its render
+ * this way.  The transparency variants, the batched launch and the FP64
+ * re-test stay exact, and so do launches with AE_RT_CFG_STAGED_RAYS or
+ * AE_RT_CFG_COUNT_FETCHES. */
+#define AE_RT_CFG_APPROXIMATE   0x8u
 ae_rt_status ae_rt_get_fetch_counts(ae_rt_ctx* ctx, uint64_t* node_fetches, uint64_t* tri_fetches);
 
 /* Device self-test of the traversal kernel's divide-free slab arithmetic:
