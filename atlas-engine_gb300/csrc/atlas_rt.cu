@@ -55,9 +55,8 @@ void* KernelFor() {
 // AE_RT_CFG_NO_NEAR_TIES, so the kernel skips its detection.
 // staged: the ray tiles go through shared memory by bulk copy
 // (AE_RT_CFG_STAGED_RAYS; single-mesh and scene launches without counters).
-// loose: the approximate traversal (AE_RT_CFG_APPROXIMATE, the radiance
-// cache's render): single-mesh and scene launches without counters or staged
-// rays, no near-tie flag.
+// loose: the approximate traversal (AE_RT_CFG_APPROXIMATE): single-mesh and
+// scene launches without counters or staged rays, no near-tie flag.
 template <int W, int S>
 void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loose) {
     constexpr int T = atlas::rt::dev::kStageRays;
@@ -195,8 +194,7 @@ uint32_t* WorkCounter(ae_rt_ctx* ctx) {
     return ctx->d_counter + (k == 0 ? 0u : k + 1u);          // word 1 is the error word
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true,
-                    bool loose = false) {
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true) {
     if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
     AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
@@ -204,7 +202,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
     void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays,
-                               loose || ctx->approximate);
+                               ctx->approximate);
     const uint32_t grid = GridFor(ctx, fn, p.n_rays);
     void* args[] = { &p };
     AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
@@ -215,8 +213,7 @@ constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
 
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                    float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
-                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true,
-                   bool loose = false) {
+                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true) {
     if (!ctx) return AE_RT_INVALID_ARG;
     const bool scene = mesh_id == kSceneTarget;
     if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
@@ -273,7 +270,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.cull_mask = cull_mask;
     }
     p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
-    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties, loose);
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -306,10 +303,9 @@ ae_rt_status atlas::rt::host::EnsureBounceQueues(ae_rt_ctx* ctx, uint32_t capaci
 
 ae_rt_status atlas::rt::host::TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity,
                                              float tmin, float tmax, void* out, void* stream,
-                                             const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax,
-                                             bool loose) {
+                                             const uint32_t* count_dev, uint32_t cull_mask, bool per_ray_tmax) {
     return Trace(ctx, any, kSceneTarget, rays, capacity, tmin, tmax, out, stream, count_dev, cull_mask, per_ray_tmax,
-                 false, loose);
+                 false);
 }
 
 namespace {

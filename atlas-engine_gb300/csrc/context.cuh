@@ -142,12 +142,10 @@ inline bool IsDevicePointer(const void* p) {
 // Queue-driven trace over the context's two-level scene (rays, out and count
 // in device memory), for the other translation units.
 // Closest / any-hit trace of a scene queue for the library's own consumers
-// (passes, radiance cache): the near-tie detection is skipped.  loose: the
-// approximate traversal (conservative boxes, one-reciprocal triangles) for
-// Monte Carlo consumers that need no bit-exact match with the shader.
+// (passes, radiance cache): the near-tie detection is skipped.
 ae_rt_status TraceSceneQueue(ae_rt_ctx* ctx, bool any, const ae_packed_ray* rays, uint32_t capacity, float tmin,
                              float tmax, void* out, void* stream, const uint32_t* count_dev, uint32_t cull_mask,
-                             bool per_ray_tmax, bool loose = false);
+                             bool per_ray_tmax);
 
 // The transparency traversal variants over the scene (transparency.cu); with
 // count_dev, `n` is the queue capacity and the count lives on the device;

@@ -341,7 +341,7 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
         p.n_shadow = ctx->d_pt_counts + 2 + q;
         p.shadow_occ = static_cast<const uint8_t*>(shadowOcc[q]->ptr);
         st = TraceSceneQueue(ctx, false, static_cast<const ae_packed_ray*>(ctx->pt_rays[in].ptr), cap, 0.0f, 1e12f,
-                             ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false, true);
+                             ctx->pt_hits.ptr, stream, ctx->d_pt_counts + in, AE_RT_MASK_ALL, false);
         if (st != AE_RT_OK) return st;
         if (pending[q]) RC_CUDA(rc, cudaStreamWaitEvent(s, ctx->pt_events[2 + q], 0));
         RC_CUDA(rc, cudaMemsetAsync(ctx->d_pt_counts + out, 0, sizeof(uint32_t), s));
@@ -351,7 +351,7 @@ ae_rt_status RenderFrame(ae_rc* rc, const ae_camera* cam, uint32_t frame, uint32
         RC_CUDA(rc, cudaEventRecord(ctx->pt_events[q], s));
         RC_CUDA(rc, cudaStreamWaitEvent(side, ctx->pt_events[q], 0));
         st = TraceSceneQueue(ctx, true, static_cast<const ae_packed_ray*>(shadowRays[q]->ptr), cap, 0.0f, 1e12f,
-                             shadowOcc[q]->ptr, sideStream, p.n_shadow, AE_RT_MASK_SHADOW, true, true);
+                             shadowOcc[q]->ptr, sideStream, p.n_shadow, AE_RT_MASK_SHADOW, true);
         if (st != AE_RT_OK) return st;
         pt_resolve_kernel<<<blocks, 256, 0, side>>>(p);
         RC_CUDA(rc, cudaGetLastError());

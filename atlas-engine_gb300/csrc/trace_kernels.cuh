@@ -505,8 +505,8 @@ __device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, u
 // wait sets kErrWaitTimeout and ends the warp's refills.
 //
 // LOOSE: the conservative approximate box test (test_children_loose) and
-// tri_test_fast, for consumers whose results are Monte Carlo estimates (the
-// radiance cache's render), not the shader's bit for bit.
+// tri_test_fast, for consumers whose results are Monte Carlo estimates
+// (AE_RT_CFG_APPROXIMATE), not the shader's bit for bit.
 template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
           bool BOUNDS = false, bool TIES = true, int STAGE = 0, bool LOOSE = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {

@@ -1097,8 +1097,9 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream);
  * barycentrics; for the same triangle t, u and v are within 1.5 units of
  * 2^-24 (relative) of the exact ones; the near-tie flag marks only rays whose
  * second accepted triangle lies within 1e-6 relative t (as with
- * AE_RT_CFG_NO_NEAR_TIES).  The library's radiance cache traces its render
- * this way.  The transparency variants, the batched launch and the FP64
+ * AE_RT_CFG_NO_NEAR_TIES).  (The radiance cache's training paths always
+ * trace this way; its render follows the context.)  The transparency
+ * variants, the batched launch and the FP64
  * re-test stay exact, and so do launches with AE_RT_CFG_STAGED_RAYS or
  * AE_RT_CFG_COUNT_FETCHES. */
 #define AE_RT_CFG_APPROXIMATE   0x8u
