@@ -913,6 +913,8 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, max_frames=320, n_pat
         return next((c["spp"] for c in pt["curve"] if c[pk] < floor), None)
     head = reached.get("eps_1e-2")
     out = {"resolution": [W, H], "n_paths": n_paths, "adam_steps_per_frame": steps, "radiance_scale": scale,
+           "traversal": "the render and the plain path tracer both on the exact traversal (the context's default); "
+                        "the training paths on the approximate one (no counterpart in the plain path tracer)",
            "rough_cut": rough_cut, "last_bounce": last_bounce,
            "schedule": {"start_frame": RC_START, "samples_per_frame": 1, "declared": "fixed before the run; "
                         "no other schedule is tried"},
