@@ -29,6 +29,9 @@ using atlas::rt::dev::TraceParams;
 // lane's 128-entry traversal stack (the rest spills to local memory).  The
 // register budget follows from the minimum resident CTAs per SM.
 constexpr int kStackEntries = 128;
+// Stack entries of the deep variants, launched for meshes and scenes whose
+// trees can need more than kStackEntries (local memory, 4 KB per lane).
+constexpr int kDeepStackEntries = 1024;
 struct Shape {
     int warps;
     int smem;
@@ -40,14 +43,15 @@ using atlas::rt::dev::MODE_BATCH;
 using atlas::rt::dev::MODE_MESH;
 using atlas::rt::dev::MODE_SCENE;
 
-template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0, bool LOOSE = false>
+template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0, bool LOOSE = false,
+          bool DEEP = false>
 void* KernelFor() {
     // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
     // more per-lane state and get ~73
     constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
-        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, kStackEntries - S, minBlocks, false, TIES && !ANY,
-                                      STAGE, LOOSE>);
+        &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, (DEEP ? kDeepStackEntries : kStackEntries) - S,
+                                      minBlocks, false, TIES && !ANY, STAGE, LOOSE>);
 }
 
 // ties = false: the caller discards the near-tie flag (the library's path
@@ -91,6 +95,20 @@ void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loo
     if (!ties)
         return count ? KernelFor<false, true, MODE_MESH, W, S, false>() : KernelFor<false, false, MODE_MESH, W, S, false>();
     return count ? KernelFor<false, true, MODE_MESH, W, S>() : KernelFor<false, false, MODE_MESH, W, S>();
+}
+
+// The deep variants (kDeepStackEntries, exact traversal, the default shape)
+// for single-mesh and scene launches whose tree can need more than
+// kStackEntries entries.
+void* PickDeep(bool any, int mode, bool ties) {
+    if (mode == MODE_SCENE) {
+        if (any) return KernelFor<true, false, MODE_SCENE, 4, 32, true, 0, false, true>();
+        return ties ? KernelFor<false, false, MODE_SCENE, 4, 32, true, 0, false, true>()
+                    : KernelFor<false, false, MODE_SCENE, 4, 32, false, 0, false, true>();
+    }
+    if (any) return KernelFor<true, false, MODE_MESH, 4, 32, true, 0, false, true>();
+    return ties ? KernelFor<false, false, MODE_MESH, 4, 32, true, 0, false, true>()
+                : KernelFor<false, false, MODE_MESH, 4, 32, false, 0, false, true>();
 }
 
 void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true, bool staged = false,
@@ -163,6 +181,21 @@ ae_rt_status ValidateBlas(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_t n_n
     return AE_RT_OK;
 }
 
+// Inner-node levels on the longest root-to-leaf path of a validated tree
+// (children after their parents, so one pass from the back): the most stack
+// entries its traversal can hold.
+uint32_t TreeDepth(const ae_bvh_node* nodes, uint32_t n_nodes) {
+    if (n_nodes == 0) return 0;
+    std::vector<uint32_t> d(n_nodes, 1);
+    for (int64_t i = int64_t(n_nodes) - 1; i >= 0; i--) {
+        uint32_t below = 0;
+        for (int32_t ptr : { nodes[i].leftPtr, nodes[i].rightPtr })
+            if (ptr >= 0) below = std::max(below, d[size_t(ptr)]);
+        d[size_t(i)] = 1 + below;
+    }
+    return d[0];
+}
+
 uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
     if (ctx->max_steps_cfg) return ctx->max_steps_cfg;
     return atlas::rt::dev::default_step_cap(m.n_nodes);
@@ -170,18 +203,21 @@ uint32_t MaxSteps(const ae_rt_ctx* ctx, const DeviceMesh& m) {
 
 // Persistent grid for `fn`: SMs x resident CTAs (the configured count, or the
 // kernel's occupancy), never more warps than rays.
-uint32_t GridFor(const ae_rt_ctx* ctx, const void* fn, uint32_t n_rays) {
-    uint32_t per_sm = ctx->blocks_per_sm;
+// threads: the block size when it is not the context's (the deep variants,
+// sized by their occupancy alone).
+uint32_t GridFor(const ae_rt_ctx* ctx, const void* fn, uint32_t n_rays, uint32_t threads = 0) {
+    uint32_t per_sm = threads ? 0u : ctx->blocks_per_sm;
+    if (threads == 0) threads = ctx->threads;
     if (per_sm == 0) {
         int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, int(ctx->threads), 0) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, int(threads), 0) != cudaSuccess) {
             cudaGetLastError();
             occ = 1;
         }
         per_sm = uint32_t(occ > 0 ? occ : 1);
     }
     uint32_t grid = uint32_t(ctx->sm_count) * per_sm;
-    const uint32_t needed = (n_rays + ctx->threads - 1) / ctx->threads;
+    const uint32_t needed = (n_rays + threads - 1) / threads;
     if (needed < grid) grid = needed;
     return grid == 0 ? 1 : grid;
 }
@@ -194,18 +230,24 @@ uint32_t* WorkCounter(ae_rt_ctx* ctx) {
     return ctx->d_counter + (k == 0 ? 0u : k + 1u);          // word 1 is the error word
 }
 
-ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true) {
+// depth: stack entries the launch's tree can need (0: the batched launch,
+// whose meshes keep to kStackEntries or report overflow).
+ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true,
+                    uint32_t depth = 0) {
     if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
     AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
     p.refill_steps = ctx->refill_steps;
     p.refill_below = ctx->refill_below;
     p.leaf_wait = ctx->leaf_wait;
-    void* fn = PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties, ctx->staged_rays,
-                               ctx->approximate);
-    const uint32_t grid = GridFor(ctx, fn, p.n_rays);
+    const bool deep = depth > uint32_t(kStackEntries) && mode != MODE_BATCH;
+    void* fn = deep ? PickDeep(any, mode, ties && ctx->near_ties)
+                    : PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties,
+                                      ctx->staged_rays, ctx->approximate);
+    const uint32_t threads = deep ? 128u : ctx->threads;
+    const uint32_t grid = GridFor(ctx, fn, p.n_rays, threads);
     void* args[] = { &p };
-    AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->threads), args, 0, s));
+    AE_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, 0, s));
     return AE_RT_OK;
 }
 
@@ -270,7 +312,7 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.cull_mask = cull_mask;
     }
     p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
-    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties);
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties, scene ? ctx->scene_depth : m.depth);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -453,6 +495,7 @@ ae_rt_status ae_rt_mesh_upload(ae_rt_ctx* ctx, const ae_bvh_node* nodes, uint32_
     DeviceMesh m;
     m.n_nodes = n_nodes;
     m.n_tris = n_tris;
+    m.depth = TreeDepth(nodes, n_nodes);
     if (shading)
         for (uint32_t i = 0; i < n_tris && !m.transparent; i++) m.transparent = shading[i].d2[3] != 1.0f;
     auto upload = [&](float4** dst, const void* src, size_t bytes) -> cudaError_t {
@@ -501,13 +544,16 @@ ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n
         }
     }
     uint64_t steps = uint64_t(n_tlas) + n_instances;
+    uint32_t blas_depth = 0;
     for (uint32_t i = 0; i < n_instances; i++) {
         const int32_t m = instances[i].meshOffset;
         if (m < 0 || size_t(m) >= ctx->meshes.size())
             return Fail(ctx, AE_RT_INVALID_ARG, "instance " + std::to_string(i) + " names unknown mesh " +
                                                 std::to_string(m));
         steps += ctx->meshes[size_t(m)].n_nodes + ctx->meshes[size_t(m)].n_tris;
+        blas_depth = std::max(blas_depth, ctx->meshes[size_t(m)].depth);
     }
+    const uint32_t scene_depth = TreeDepth(tlas, n_tlas) + blas_depth;
     std::lock_guard<std::mutex> g(ctx->upload_mutex);
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     std::vector<atlas::rt::dev::MeshDesc> table(ctx->meshes.size());
@@ -576,6 +622,7 @@ ae_rt_status ae_rt_scene_set(ae_rt_ctx* ctx, const ae_bvh_node* tlas, uint32_t n
     if (e != cudaSuccess) return CudaFail(ctx, e, "scene upload");
     ctx->n_tlas = n_tlas;
     ctx->n_instances = n_instances;
+    ctx->scene_depth = scene_depth;
     ctx->n_mesh_table = uint32_t(table.size());
     steps = 4 * steps + 64;
     ctx->scene_steps = steps > 0xffffffffull ? 0xffffffffu : uint32_t(steps);

@@ -276,6 +276,11 @@ void OneTriangle(const float* v, int32_t material, float opacity, ae_bvh_node& n
 
 }  // namespace
 
+// Stack entries a traversal of the linear BVH can need: along any
+// root-to-leaf path the split bit of the 64-bit keys (30-bit Morton code,
+// triangle index) strictly advances, so the tree is at most 64 levels deep.
+static uint32_t LbvhDepthBound(uint32_t n_nodes) { return n_nodes > 64u ? 64u : n_nodes; }
+
 extern "C" ae_rt_status ae_rt_mesh_build(ae_rt_ctx* ctx, const float* verts, uint32_t n, const int32_t* material,
                                          const float* opacity, int32_t* mesh_id, uint32_t* order_out, void* stream) {
     if (!ctx || !mesh_id) return AE_RT_INVALID_ARG;
@@ -287,6 +292,7 @@ extern "C" ae_rt_status ae_rt_mesh_build(ae_rt_ctx* ctx, const float* verts, uin
     std::lock_guard<std::mutex> lock(ctx->upload_mutex);
     DeviceMesh m;
     if (n == 0) {
+        m.depth = LbvhDepthBound(m.n_nodes);
         ctx->meshes.push_back(m);
         *mesh_id = int32_t(ctx->meshes.size() - 1);
         return AE_RT_OK;
@@ -333,6 +339,7 @@ extern "C" ae_rt_status ae_rt_mesh_build(ae_rt_ctx* ctx, const float* verts, uin
         }
         m.n_nodes = 1;
         m.n_tris = 2;
+        m.depth = LbvhDepthBound(m.n_nodes);
         ctx->meshes.push_back(m);
         *mesh_id = int32_t(ctx->meshes.size() - 1);
         if (order_out) {
@@ -429,7 +436,8 @@ extern "C" ae_rt_status ae_rt_mesh_build(ae_rt_ctx* ctx, const float* verts, uin
 #undef BUILD_CUDA
     m.n_nodes = n - 1;
     m.n_tris = n;
-    ctx->meshes.push_back(m);
+    m.depth = LbvhDepthBound(m.n_nodes);
+        ctx->meshes.push_back(m);
     *mesh_id = int32_t(ctx->meshes.size() - 1);
     return AE_RT_OK;
 }

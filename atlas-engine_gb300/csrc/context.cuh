@@ -21,6 +21,7 @@ struct DeviceMesh {
     uint32_t n_nodes = 0;
     uint32_t n_tris = 0;
     bool transparent = false;   // a shading triangle's opacity (d2.w) is not 1: opacity texture or partial
+    uint32_t depth = 0;         // inner-node levels on the longest root-to-leaf path (stack entries it can need)
 };
 
 // Grow-only device scratch buffer.
@@ -59,7 +60,8 @@ struct ae_rt_ctx {
     bool count_fetches = false;
     bool near_ties = true;            // complete near-tie detection on closest-hit traces
     bool staged_rays = false;
-    bool approximate = false;   // AE_RT_CFG_APPROXIMATE         // ray tiles through shared memory by bulk copy
+    bool approximate = false;   // AE_RT_CFG_APPROXIMATE
+    uint32_t scene_depth = 0;   // top-level depth + the deepest mesh's: stack entries a scene ray can need         // ray tiles through shared memory by bulk copy
     std::vector<atlas::rt::host::DeviceMesh> meshes;
     // two-level scene: TLAS nodes, instances (TLAS order), mesh table snapshot
     float4* d_tlas = nullptr;

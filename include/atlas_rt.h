@@ -39,7 +39,8 @@ typedef enum ae_rt_status {
     AE_RT_OUT_OF_MEMORY = 3,
     AE_RT_CUDA_ERROR = 4,       /* a CUDA call failed; see ae_rt_last_error */
     AE_RT_TIMEOUT = 5,          /* a bounded device wait gave up */
-    AE_RT_STACK_OVERFLOW = 6,   /* a ray needed more traversal stack than configured */
+    AE_RT_STACK_OVERFLOW = 6,   /* a ray needed more traversal stack than its launch holds
+                                   (trees deeper than 1,024 levels; batched launches: 128) */
     AE_RT_ITERATION_LIMIT = 7,  /* a ray exceeded the traversal step cap (cyclic BVH?) */
     AE_RT_NO_DEVICE = 8,
     AE_RT_NOT_BUILT = 9         /* the library was built without the requested feature */
@@ -350,7 +351,9 @@ typedef struct ae_rt_ctx ae_rt_ctx;
  * (atlas_rt.autotune) picks these per workload.  Supported
  * (threads_per_block, stack_entries_smem) pairs: (128, 32) default, (64, 32),
  * (256, 16), (128, 16); each lane has 128 stack entries in total, the rest in
- * local memory. */
+ * local memory.  Meshes and scenes whose trees can need more (the upload
+ * measures each tree's depth) are traced by a variant with 1,024 entries
+ * per lane (128 threads, 32 in shared memory). */
 typedef struct ae_rt_config {
     int32_t device;               /* CUDA device ordinal */
     uint32_t blocks_per_sm;       /* persistent CTAs per SM (0 = the kernel's occupancy) */

@@ -231,22 +231,68 @@ def comb_bvh(depth):
     return nodes, tris
 
 
-def test_stack_overflow_is_reported(ctx):
-    nodes, tris = comb_bvh(200)
-    mid = ctx.upload_mesh(nodes, tris)
+def chain_bvh(n):
+    """A chain-shaped BVH whose traversal needs n - 1 stack entries: triangle
+    i lies in the plane z = n - i, node i has the inner node i + 1 (the boxes
+    of triangles i+1 .. n-1, nearer to a +z ray from z = -1) on the left and
+    the leaf of triangle i (farther) on the right, so every level pushes its
+    leaf and descends; the nearest triangle is the last."""
+    nodes = np.zeros(n - 1, atlas_rt.NODE_DTYPE)
+    tris = np.zeros((n, 12), np.float32)
+    for i in range(n):
+        z = float(n - i)
+        tris[i, 0:4] = (-1.0, -1.0, z, 1.0)
+        tris[i, 4:7] = (3.0, -1.0, z)
+        tris[i, 8:11] = (-1.0, 3.0, z)
+    for i in range(n - 1):
+        nodes[i]["leftMin"], nodes[i]["leftMax"] = (-1.0, -1.0, 1.0), (3.0, 3.0, float(n - i - 1))
+        nodes[i]["rightMin"], nodes[i]["rightMax"] = (-1.0, -1.0, float(n - i)), (3.0, 3.0, float(n - i))
+        nodes[i]["leftPtr"] = i + 1 if i + 1 < n - 1 else ~(n - 1)
+        nodes[i]["rightPtr"] = ~i
+    return nodes, tris
+
+
+def test_deep_trees_complete_and_deeper_than_1024_report_overflow(ctx):
+    """Meshes whose traversal can need more than the usual kernels' 128 stack
+    entries (the upload measures the tree's depth) are traced by the deep
+    variants, 1,024 entries per lane in local memory: 200- and 1,000-level
+    combs traverse and miss, and a 400-triangle chain (399 entries) returns
+    the nearest triangle bit for bit as the oracle's unbounded traversal.
+    Beyond 1,024 levels the overflow is still reported (status 6)."""
     rays8 = scenes.rays8(np.array([[0.5, 0.5, -1.0]], np.float32), np.array([[0, 0, 1]], np.float32), 0.0, 10.0)
-    with pytest.raises(atlas_rt.AeRtError) as e:
-        ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
-    assert e.value.status == 6
-    # shallower combs traverse fine and miss: 100 levels need more than 64
-    # entries, which a 65-deep top level (100,000 clustered boxes) over a
-    # 32-deep bottom level (the builder's depth cap, BVH.cpp:253) can need
-    for depth in (20, 100):
+    for depth in (20, 100, 200, 1000):
         nodes, tris = comb_bvh(depth)
         mid = ctx.upload_mesh(nodes, tris)
         hits = ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
-        assert hits["triPtr"][0] == -1
+        assert hits["triPtr"][0] == -1 and (hits["flags"][0] & 0x4) == 0
         assert not ctx.trace_any(mid, packed(rays8), 0.0, 10.0)[0]
+    nodes, tris = comb_bvh(1100)
+    mid = ctx.upload_mesh(nodes, tris)
+    with pytest.raises(atlas_rt.AeRtError) as e:
+        ctx.trace_closest(mid, packed(rays8), 0.0, 10.0)
+    assert e.value.status == 6
+    n = 400
+    nodes, tris = chain_bvh(n)
+    mid = ctx.upload_mesh(nodes, tris)
+    rays8 = scenes.rays8(np.array([[0.5, 0.5, -1.0], [0.2, 0.7, -3.0]], np.float32),
+                         np.array([[0, 0, 1], [0.01, -0.02, 1.0]], np.float32), 0.0, 1e4)
+    hits = ctx.trace_closest(mid, packed(rays8), 0.0, 1e4)
+    ptr, tuv = pyoracle.closest_glsl(nodes.view(np.float32).reshape(-1, 16), tris, rays8)
+    assert np.array_equal(hits["triPtr"], ptr) and (ptr == n - 1).all()
+    assert np.array_equal(hits["t"].view(np.uint32), tuv[:, 0].view(np.uint32))
+    assert ctx.trace_any(mid, packed(rays8), 0.0, 1e4).all()
+    # the same chain as the one instance of a scene (top level + bottom level)
+    sc = atlas_rt.Context(device=0)
+    try:
+        m2 = sc.upload_mesh(nodes, tris)
+        inst = np.array([atlas_rt.make_instance(np.eye(4), m2, atlas_rt.MASK_ALL)])
+        sc.scene_build(inst, np.array([[-1.0, -1.0, 1.0, 3.0, 3.0, float(n)]], np.float32))
+        sh = sc.trace_scene_closest(packed(rays8), 0.0, 1e4)
+        sc.synchronize()
+        assert np.array_equal(sh["triPtr"], ptr)
+        assert np.array_equal(sh["t"].view(np.uint32), tuv[:, 0].view(np.uint32))
+    finally:
+        sc.close()
 
 
 def test_step_cap_is_reported():
