@@ -862,6 +862,7 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, max_frames=320, n_pat
     reached, curve, plateau = {}, [], {}
     train_ms = frame_ms = 0.0
     train_frames = []
+    prev = None          # the previous rendered frame's (time, errors)
     rendered = 0
     f = -1
     try:
@@ -894,6 +895,12 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, max_frames=320, n_pat
                 if k not in reached and e <= targets[k]:
                     reached[k] = {"frame": f, "rendered_frames": rendered, "ms": t_cum, "wall_ms": wall_cum,
                                   "rel_mse": e}
+                    if prev is not None and prev[1][k] > targets[k] > 0 and e > 0:
+                        # where the error falls to the target between the two frames,
+                        # log-linear in the error: less tied to the frame grid
+                        a = np.log(prev[1][k] / targets[k]) / np.log(prev[1][k] / e)
+                        reached[k]["ms_interpolated"] = prev[0] + a * (t_cum - prev[0])
+            prev = (t_cum, errs)
             if rendered in (1, 2, 4, 8, 16, 32, 64, 128, 256):
                 curve.append({"rendered_frames": rendered, "ms_cum": t_cum, "wall_ms_cum": wall_cum, **errs})
             if rendered in RC_PLATEAU_FRAMES:
@@ -933,6 +940,9 @@ def workload_radiance_cache(torch, dev, stream, pt, scene, max_frames=320, n_pat
                           "plain_pt_spp_below_floor": {k: pt_spp_below(k) for k in ("eps_1e-2", "eps_scaled")}},
            "ms_to_equal_rel_mse": head["ms"] if head else None,
            "speedup_vs_plain_pt": pt["ms_to_spp"] / head["ms"] if head else None,
+           "ms_to_equal_rel_mse_interpolated": head.get("ms_interpolated") if head else None,
+           "speedup_vs_plain_pt_interpolated": (pt["ms_to_spp"] / head["ms_interpolated"]
+                                                if head and head.get("ms_interpolated") else None),
            "wall_speedup_vs_plain_pt": pt["wall_ms_to_spp"] / head["wall_ms"] if head else None}
     sc_ = reached.get("eps_scaled")
     out["speedup_vs_plain_pt_scaled_eps"] = pt["ms_to_spp"] / sc_["ms"] if sc_ else None
