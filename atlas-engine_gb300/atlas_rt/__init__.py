@@ -421,6 +421,18 @@ class Context:
                                         _ptr(secondary), _ptr(shadow), _ptr(counts), _stream_handle(stream)),
                self._h)
 
+    def trace_camera_closest(self, mesh, cam: "Camera", hits, tmin=0.0, tmax=float("inf"), stream=None):
+        """raygen + trace_closest of the camera's rays without a ray buffer."""
+        _check(lib().ae_rt_trace_camera_closest(self._h, mesh, C.byref(cam), tmin, tmax, _ptr(hits),
+                                                _stream_handle(stream)), self._h)
+
+    def spawn_bounce_camera(self, mesh, cam: "Camera", hits, params: "BounceParams", secondary, shadow, counts,
+                            stream=None):
+        """spawn_bounce over the camera's width*height rays."""
+        _check(lib().ae_rt_spawn_bounce_camera(self._h, mesh, C.byref(cam), _ptr(hits), C.byref(params),
+                                               _ptr(secondary), _ptr(shadow), _ptr(counts),
+                                               _stream_handle(stream)), self._h)
+
     def cast_pass(self, mesh, cam: "Camera", params: "BounceParams", primary_hits=None, secondary_rays=None,
                   secondary_hits=None, shadow_rays=None, shadow_occluded=None, stream=None):
         """One camera pass (primary, bounce and shadow rays).  Returns counts

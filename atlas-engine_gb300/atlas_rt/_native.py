@@ -184,6 +184,8 @@ _SIGNATURES = [
     ("ae_rt_trace_closest_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),
     ("ae_rt_trace_any_queue", C.c_int, [P, I32, P, P, U32, F32, F32, P, P]),
     ("ae_rt_spawn_bounce", C.c_int, [P, I32, P, P, P, U32, C.POINTER(BounceParams), P, P, P, P]),
+    ("ae_rt_trace_camera_closest", C.c_int, [P, I32, C.POINTER(Camera), F32, F32, P, P]),
+    ("ae_rt_spawn_bounce_camera", C.c_int, [P, I32, C.POINTER(Camera), P, C.POINTER(BounceParams), P, P, P, P]),
     ("ae_rt_cast_pass", C.c_int, [P, I32, C.POINTER(Camera), C.POINTER(BounceParams), C.POINTER(CastOutputs), P]),
     ("ae_rt_synchronize", C.c_int, [P, P]),
     ("ae_rt_selftest_division", C.c_int, [P, C.c_uint64, U32, C.POINTER(C.c_uint64)]),

@@ -44,14 +44,14 @@ using atlas::rt::dev::MODE_MESH;
 using atlas::rt::dev::MODE_SCENE;
 
 template <bool ANY, bool COUNT, int MODE, int W, int S, bool TIES = true, int STAGE = 0, bool LOOSE = false,
-          bool DEEP = false>
+          bool DEEP = false, bool CAMERA = false>
 void* KernelFor() {
     // single-mesh kernels keep <= 64 registers; scene / batched kernels carry
     // more per-lane state and get ~73
     constexpr int minBlocks = MODE == MODE_MESH ? 32 / W : (28 / W > 0 ? 28 / W : 1);
     return reinterpret_cast<void*>(
         &atlas::rt::dev::trace_kernel<ANY, COUNT, MODE, W, S, (DEEP ? kDeepStackEntries : kStackEntries) - S,
-                                      minBlocks, false, TIES && !ANY, STAGE, LOOSE>);
+                                      minBlocks, false, TIES && !ANY, STAGE, LOOSE, CAMERA>);
 }
 
 // ties = false: the caller discards the near-tie flag (the library's path
@@ -62,8 +62,11 @@ void* KernelFor() {
 // loose: the approximate traversal (AE_RT_CFG_APPROXIMATE): single-mesh and
 // scene launches without counters or staged rays, no near-tie flag.
 template <int W, int S>
-void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loose) {
+void* PickShape(bool any, bool count, int mode, bool ties, bool staged, bool loose, bool camera) {
     constexpr int T = atlas::rt::dev::kStageRays;
+    if (camera)
+        return ties ? KernelFor<false, false, MODE_MESH, W, S, true, 0, false, false, true>()
+                    : KernelFor<false, false, MODE_MESH, W, S, false, 0, false, false, true>();
     if (loose && mode == MODE_SCENE && !count && !staged)
         return any ? KernelFor<true, false, MODE_SCENE, W, S, false, 0, true>()
                    : KernelFor<false, false, MODE_SCENE, W, S, false, 0, true>();
@@ -112,12 +115,12 @@ void* PickDeep(bool any, int mode, bool ties) {
 }
 
 void* PickKernelShape(int shape, bool any, bool count, int mode, bool ties = true, bool staged = false,
-                      bool loose = false) {
+                      bool loose = false, bool camera = false) {
     switch (shape) {
-    case 1: return PickShape<2, 32>(any, count, mode, ties, staged, loose);
-    case 2: return PickShape<8, 16>(any, count, mode, ties, staged, loose);
-    case 3: return PickShape<4, 16>(any, count, mode, ties, staged, loose);
-    default: return PickShape<4, 32>(any, count, mode, ties, staged, loose);
+    case 1: return PickShape<2, 32>(any, count, mode, ties, staged, loose, camera);
+    case 2: return PickShape<8, 16>(any, count, mode, ties, staged, loose, camera);
+    case 3: return PickShape<4, 16>(any, count, mode, ties, staged, loose, camera);
+    default: return PickShape<4, 32>(any, count, mode, ties, staged, loose, camera);
     }
 }
 
@@ -232,8 +235,10 @@ uint32_t* WorkCounter(ae_rt_ctx* ctx) {
 
 // depth: stack entries the launch's tree can need (0: the batched launch,
 // whose meshes keep to kStackEntries or report overflow).
+// camera: the rays are p.cam's camera rays (single mesh, closest hit, a tree
+// within kStackEntries, exact, no counters: Trace checks this).
 ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStream_t s, bool ties = true,
-                    uint32_t depth = 0) {
+                    uint32_t depth = 0, bool camera = false) {
     if (p.work_counter == ctx->d_counter) p.work_counter = WorkCounter(ctx);
     AE_CUDA(ctx, cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s));
     if (ctx->count_fetches) AE_CUDA(ctx, cudaMemsetAsync(ctx->d_fetch, 0, 2 * sizeof(unsigned long long), s));
@@ -243,7 +248,7 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
     const bool deep = depth > uint32_t(kStackEntries) && mode != MODE_BATCH;
     void* fn = deep ? PickDeep(any, mode, ties && ctx->near_ties)
                     : PickKernelShape(ctx->shape, any, ctx->count_fetches, mode, ties && ctx->near_ties,
-                                      ctx->staged_rays, ctx->approximate);
+                                      ctx->staged_rays, ctx->approximate, camera);
     const uint32_t threads = deep ? 128u : ctx->threads;
     const uint32_t grid = GridFor(ctx, fn, p.n_rays, threads);
     void* args[] = { &p };
@@ -253,16 +258,33 @@ ae_rt_status Launch(ae_rt_ctx* ctx, bool any, int mode, TraceParams& p, cudaStre
 
 constexpr int32_t kSceneTarget = -1;   // Trace() target: the two-level scene
 
+// The camera of ae_rt_raygen and the camera traces.
+atlas::rt::dev::CameraParams CameraFrom(const ae_camera* cam) {
+    atlas::rt::dev::CameraParams c{};
+    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
+    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
+    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
+    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
+    c.width = cam->width; c.height = cam->height;
+    c.jx = cam->jitter[0]; c.jy = cam->jitter[1];
+    return c;
+}
+
+// cam: trace the camera rays of `cam` (rays null, n_rays = its pixel
+// count), made in the traversal kernel where it can (one mesh, closest hit,
+// a tree within kStackEntries, and none of the approximate, counting or
+// staged launches), else written by raygen_kernel into scratch first.
 ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ray* rays, uint32_t n_rays,
                    float tmin, float tmax, void* out, void* stream, const uint32_t* count_dev = nullptr,
-                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true) {
+                   uint32_t cull_mask = 0xffffffffu, bool per_ray_tmax = false, bool ties = true,
+                   const atlas::rt::dev::CameraParams* cam = nullptr) {
     if (!ctx) return AE_RT_INVALID_ARG;
     const bool scene = mesh_id == kSceneTarget;
     if (scene && !ctx->scene_ready) return Fail(ctx, AE_RT_INVALID_ARG, "no scene has been set");
     if (!scene && (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size()))
         return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
     if (n_rays == 0) return AE_RT_OK;
-    if (!rays || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray or result buffer");
+    if ((!rays && !cam) || !out) return Fail(ctx, AE_RT_INVALID_ARG, "null ray or result buffer");
     if (n_rays > (1u << 30)) return Fail(ctx, AE_RT_INVALID_ARG, "more than 2^30 rays in one call");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -271,10 +293,20 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
 
     const size_t ray_bytes = size_t(n_rays) * sizeof(ae_packed_ray);
     const size_t out_bytes = size_t(n_rays) * (any ? 1 : sizeof(ae_hit));
-    const bool rays_dev = IsDevicePointer(rays);
+    const bool camera = cam && !scene && !any && count_dev == nullptr && m.depth <= uint32_t(kStackEntries) &&
+                        !ctx->approximate && !ctx->count_fetches && !ctx->staged_rays;
+    if (cam && !camera) {
+        // the general path: the camera's rays into scratch, then a plain trace
+        AE_CUDA(ctx, ctx->rays_in.ensure(ray_bytes));
+        atlas::rt::dev::raygen_kernel<<<(n_rays + 255) / 256, 256, 0, s>>>(*cam,
+                                                                        static_cast<float4*>(ctx->rays_in.ptr));
+        AE_CUDA(ctx, cudaGetLastError());
+        rays = static_cast<const ae_packed_ray*>(ctx->rays_in.ptr);
+    }
+    const bool rays_dev = camera || IsDevicePointer(rays);
     const bool out_dev = IsDevicePointer(out);
 
-    const void* d_rays = rays;
+    const void* d_rays = camera ? nullptr : rays;
     void* d_out = out;
     if (!rays_dev) {
         AE_CUDA(ctx, ctx->rays_in.ensure(ray_bytes));
@@ -312,7 +344,9 @@ ae_rt_status Trace(ae_rt_ctx* ctx, bool any, int32_t mesh_id, const ae_packed_ra
         p.cull_mask = cull_mask;
     }
     p.per_ray_tmax = per_ray_tmax ? 1u : 0u;
-    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties, scene ? ctx->scene_depth : m.depth);
+    if (camera) p.cam = *cam;
+    ae_rt_status st = Launch(ctx, any, scene ? MODE_SCENE : MODE_MESH, p, s, ties, scene ? ctx->scene_depth : m.depth,
+                             camera);
     if (st != AE_RT_OK) return st;
 
     if (!out_dev) {
@@ -1257,13 +1291,7 @@ ae_rt_status ae_rt_raygen(ae_rt_ctx* ctx, const ae_camera* cam, ae_packed_ray* r
         return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
     if (!IsDevicePointer(rays)) return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_raygen writes device memory only");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
-    atlas::rt::dev::CameraParams c{};
-    c.lx = cam->location[0]; c.ly = cam->location[1]; c.lz = cam->location[2];
-    c.ox = cam->origin[0]; c.oy = cam->origin[1]; c.oz = cam->origin[2];
-    c.rx = cam->right[0]; c.ry = cam->right[1]; c.rz = cam->right[2];
-    c.bx = cam->bottom[0]; c.by = cam->bottom[1]; c.bz = cam->bottom[2];
-    c.width = cam->width; c.height = cam->height;
-    c.jx = cam->jitter[0]; c.jy = cam->jitter[1];
+    const atlas::rt::dev::CameraParams c = CameraFrom(cam);
     const uint32_t n = cam->width * cam->height;
     atlas::rt::dev::raygen_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
         c, reinterpret_cast<float4*>(rays));
@@ -1289,21 +1317,24 @@ ae_rt_status ae_rt_trace_any_queue(ae_rt_ctx* ctx, int32_t mesh_id, const ae_pac
     return Trace(ctx, true, mesh_id, rays, capacity, tmin, tmax, occluded, stream, count);
 }
 
-ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, const ae_hit* hits,
-                                const uint32_t* count, uint32_t n, const ae_bounce_params* params,
-                                ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts,
-                                void* stream) {
+namespace {
+// The bounce spawn over primary rays in a buffer, or (rays null) over the
+// camera rays of `cam`.
+ae_rt_status Spawn(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, const ae_camera* cam,
+                   const ae_hit* hits, const uint32_t* count, uint32_t n, const ae_bounce_params* params,
+                   ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts, void* stream) {
     if (!ctx) return AE_RT_INVALID_ARG;
     if (mesh_id < 0 || size_t(mesh_id) >= ctx->meshes.size())
         return Fail(ctx, AE_RT_INVALID_ARG, "unknown mesh id " + std::to_string(mesh_id));
     if (!params || !counts) return Fail(ctx, AE_RT_INVALID_ARG, "null parameters");
     if (n == 0) return AE_RT_OK;
-    if (!IsDevicePointer(rays) || !IsDevicePointer(hits) || !IsDevicePointer(secondary) ||
+    if ((rays && !IsDevicePointer(rays)) || !IsDevicePointer(hits) || !IsDevicePointer(secondary) ||
         !IsDevicePointer(shadow) || !IsDevicePointer(counts) || (count && !IsDevicePointer(count)))
-        return Fail(ctx, AE_RT_INVALID_ARG, "ae_rt_spawn_bounce takes device buffers");
+        return Fail(ctx, AE_RT_INVALID_ARG, "the bounce spawn takes device buffers");
     AE_CUDA(ctx, cudaSetDevice(ctx->device));
     atlas::rt::dev::SpawnParams sp{};
     sp.rays = reinterpret_cast<const float4*>(rays);
+    if (!rays) sp.cam = CameraFrom(cam);
     sp.hits = reinterpret_cast<const float4*>(hits);
     sp.n_dev = count;
     sp.n = n;
@@ -1317,6 +1348,37 @@ ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed
     atlas::rt::dev::spawn_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(sp);
     AE_CUDA(ctx, cudaGetLastError());
     return AE_RT_OK;
+}
+}  // namespace
+
+ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed_ray* rays, const ae_hit* hits,
+                                const uint32_t* count, uint32_t n, const ae_bounce_params* params,
+                                ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts,
+                                void* stream) {
+    if (ctx && !rays) return Fail(ctx, AE_RT_INVALID_ARG, "null ray buffer");
+    return Spawn(ctx, mesh_id, rays, nullptr, hits, count, n, params, secondary, shadow, counts, stream);
+}
+
+ae_rt_status ae_rt_trace_camera_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam, float tmin,
+                                        float tmax, ae_hit* hits, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!cam) return Fail(ctx, AE_RT_INVALID_ARG, "null camera");
+    if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 30))
+        return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
+    const atlas::rt::dev::CameraParams c = CameraFrom(cam);
+    return Trace(ctx, false, mesh_id, nullptr, cam->width * cam->height, tmin, tmax, hits, stream, nullptr,
+                 0xffffffffu, false, true, &c);
+}
+
+ae_rt_status ae_rt_spawn_bounce_camera(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam, const ae_hit* hits,
+                                       const ae_bounce_params* params, ae_packed_ray* secondary,
+                                       ae_packed_ray* shadow, uint32_t* counts, void* stream) {
+    if (!ctx) return AE_RT_INVALID_ARG;
+    if (!cam) return Fail(ctx, AE_RT_INVALID_ARG, "null camera");
+    if (cam->width == 0 || cam->height == 0 || uint64_t(cam->width) * cam->height > (1ull << 30))
+        return Fail(ctx, AE_RT_INVALID_ARG, "camera resolution out of range");
+    return Spawn(ctx, mesh_id, nullptr, cam, hits, nullptr, cam->width * cam->height, params, secondary, shadow,
+                 counts, stream);
 }
 
 namespace {
@@ -1345,13 +1407,11 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t n = cam->width * cam->height;
     const size_t rb = size_t(n) * sizeof(ae_packed_ray), hb = size_t(n) * sizeof(ae_hit);
-    AE_CUDA(ctx, ctx->cast_primary.ensure(rb));
     AE_CUDA(ctx, ctx->cast_primary_hits.ensure(hb));
     AE_CUDA(ctx, ctx->cast_secondary.ensure(rb));
     AE_CUDA(ctx, ctx->cast_secondary_hits.ensure(hb));
     AE_CUDA(ctx, ctx->cast_shadow.ensure(rb));
     AE_CUDA(ctx, ctx->cast_occluded.ensure(n));
-    auto* prim = static_cast<ae_packed_ray*>(ctx->cast_primary.ptr);
     auto* primHits = static_cast<ae_hit*>(ctx->cast_primary_hits.ptr);
     auto* sec = static_cast<ae_packed_ray*>(ctx->cast_secondary.ptr);
     auto* secHits = static_cast<ae_hit*>(ctx->cast_secondary_hits.ptr);
@@ -1380,13 +1440,13 @@ ae_rt_status ae_rt_cast_pass(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* c
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, cs);
     };
     ae_rt_status st;
-    if ((st = ae_rt_raygen(ctx, cam, prim, stream)) != AE_RT_OK) return st;
-    if ((st = Trace(ctx, false, mesh_id, prim, n, 0.0f, kInf, primHits, stream)) != AE_RT_OK) return st;
+    // the primary rays are made in the traversal kernel (no ray buffer)
+    if ((st = ae_rt_trace_camera_closest(ctx, mesh_id, cam, 0.0f, kInf, primHits, stream)) != AE_RT_OK) return st;
     AE_CUDA(ctx, cudaEventRecord(evPrim, s));
     AE_CUDA(ctx, cudaStreamWaitEvent(cs, evPrim, 0));
     AE_CUDA(ctx, copy(out->primary_hits, primHits, hb));
     AE_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s));
-    if ((st = ae_rt_spawn_bounce(ctx, mesh_id, prim, primHits, nullptr, n, params, sec, shd, counts, stream)) != AE_RT_OK)
+    if ((st = ae_rt_spawn_bounce_camera(ctx, mesh_id, cam, primHits, params, sec, shd, counts, stream)) != AE_RT_OK)
         return st;
     // the queue lengths reach the host through mapped memory, written by a
     // kernel: a copy here would queue on the copy engine behind the primary
@@ -1453,8 +1513,10 @@ ae_rt_status ae_rt_synchronize(ae_rt_ctx* ctx, void* stream) {
         if (err & atlas::rt::dev::kErrQueueOverflow)
             return Fail(ctx, AE_RT_OUT_OF_MEMORY, "a wavefront queue was full; rays were dropped");
         if (err & atlas::rt::dev::kErrStackOverflow)
-            return Fail(ctx, AE_RT_STACK_OVERFLOW, "a ray needed more than " +
-                                                   std::to_string(kStackEntries) + " stack entries");
+            return Fail(ctx, AE_RT_STACK_OVERFLOW,
+                        "a ray needed more stack entries than its kernel holds (" + std::to_string(kStackEntries) +
+                            "; " + std::to_string(kDeepStackEntries) + " for trees deeper than " +
+                            std::to_string(kStackEntries) + " levels)");
         return Fail(ctx, AE_RT_ITERATION_LIMIT, "a ray exceeded the traversal step cap");
     }
     return AE_RT_OK;

@@ -22,19 +22,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "camera.cuh"
+
 namespace atlas::rt::dev {
 
-struct CameraParams {
-    float lx, ly, lz;       // location
-    float ox, oy, oz;       // top-left corner of the image plane
-    float rx, ry, rz;       // right span
-    float bx, by, bz;       // bottom span
-    uint32_t width, height;
-    float jx, jy;           // sub-pixel jitter
-};
-
 struct SpawnParams {
-    const float4* rays;
+    const float4* rays;        // primary rays, or null: made from `cam` (the camera trace)
+    CameraParams cam;
     const float4* hits;        // 2 float4 per ae_hit
     const uint32_t* n_dev;     // optional device count
     uint32_t n;
@@ -47,47 +41,15 @@ struct SpawnParams {
     uint32_t seed;
 };
 
-// Pixel index (within a w x h tile) of queue slot i, in rayGen.csh's order
-// (:57-80): the complete 8 x 8 work groups first, row-major, each row-major
-// inside; then the columns of the partial groups on the right (w % 8 wide,
-// as tall as the complete groups), row-major; then the partial rows at the
-// bottom (h % 8 tall, the full width), column-major.
-__device__ __forceinline__ uint32_t slot_to_pixel(uint32_t i, uint32_t w, uint32_t h) {
-    const uint32_t px = w >> 3, py = h >> 3, ox = w & 7u, oy = h & 7u;
-    const uint32_t a = px * py * 64u, b = a + ox * py * 8u;
-    uint32_t x, y;
-    if (i < a) {
-        const uint32_t tile = i >> 6, local = i & 63u;
-        x = (tile % px) * 8u + (local & 7u);
-        y = (tile / px) * 8u + (local >> 3);
-    } else if (i < b) {
-        const uint32_t j = i - a;
-        x = px * 8u + j % ox;
-        y = j / ox;
-    } else {
-        const uint32_t j = i - b;
-        x = j / oy;
-        y = py * 8u + j % oy;
-    }
-    return y * w + x;
-}
-
 static __global__ void raygen_kernel(CameraParams c, float4* rays) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = c.width * c.height;
     if (i >= n) return;
-    const uint32_t pix = slot_to_pixel(i, c.width, c.height);
-    const float px = float(pix % c.width), py = float(pix / c.width);
-    const float u = __fdiv_rn(__fadd_rn(px, c.jx), float(c.width));
-    const float v = __fdiv_rn(__fadd_rn(py, c.jy), float(c.height));
-    const float qx = __fsub_rn(__fadd_rn(__fadd_rn(c.ox, __fmul_rn(c.rx, u)), __fmul_rn(c.bx, v)), c.lx);
-    const float qy = __fsub_rn(__fadd_rn(__fadd_rn(c.oy, __fmul_rn(c.ry, u)), __fmul_rn(c.by, v)), c.ly);
-    const float qz = __fsub_rn(__fadd_rn(__fadd_rn(c.oz, __fmul_rn(c.rz, u)), __fmul_rn(c.bz, v)), c.lz);
-    const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
-    const float inv = __frcp_rn(__fsqrt_rn(len2));
+    float4 o, d;
+    camera_ray(c, i, o, d);
     float4* r = rays + size_t(i) * 3;
-    r[0] = make_float4(c.lx, c.ly, c.lz, __int_as_float(int32_t(pix)));
-    r[1] = make_float4(__fmul_rn(qx, inv), __fmul_rn(qy, inv), __fmul_rn(qz, inv), 0.0f);
+    r[0] = o;
+    r[1] = d;
     r[2] = make_float4(0.0f, __int_as_float(-1), __int_as_float(-1), 0.0f);
 }
 
@@ -198,8 +160,13 @@ static __global__ void spawn_kernel(SpawnParams p) {
         const float4 h0 = p.hits[size_t(i) * 2];
         const int32_t tp = __float_as_int(h0.y);
         if (tp >= 0) {
-            const float4 o4 = p.rays[size_t(i) * 3];
-            const float4 d4 = p.rays[size_t(i) * 3 + 1];
+            float4 o4, d4;
+            if (p.rays) {
+                o4 = p.rays[size_t(i) * 3];
+                d4 = p.rays[size_t(i) * 3 + 1];
+            } else {
+                camera_ray(p.cam, i, o4, d4);
+            }
             id = __float_as_int(o4.w);
             const float t = h0.x;
             P = make_float3(o4.x + t * d4.x, o4.y + t * d4.y, o4.z + t * d4.z);

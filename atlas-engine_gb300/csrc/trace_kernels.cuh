@@ -26,6 +26,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "camera.cuh"
+
 namespace atlas::rt::dev {
 
 constexpr uint32_t kErrStackOverflow = 0x1u;
@@ -78,6 +80,7 @@ struct TraceParams {
     uint32_t refill_below;       // refill early when fewer lanes than this still traverse (0: never)
     uint32_t per_ray_tmax;       // nonzero: a ray's tmax is its PackedRay hit.x (shadow queues)
     uint32_t leaf_wait;          // closest hit: a lane at a leaf waits for this many leaf lanes (0: never)
+    CameraParams cam;            // the camera variant: ray i is camera_ray(cam, i), `rays` unused
 };
 
 // One ray batch of a batched launch: its mesh, its rays and results, its
@@ -507,13 +510,18 @@ __device__ __forceinline__ uint32_t find_batch(const BatchDesc* b, uint32_t n, u
 // LOOSE: the conservative approximate box test (test_children_loose) and
 // tri_test_fast, for consumers whose results are Monte Carlo estimates
 // (AE_RT_CFG_APPROXIMATE), not the shader's bit for bit.
+//
+// CAMERA: ray i is the camera ray of queue slot i (camera_ray), made by the
+// lane that takes it, instead of a load from a ray buffer written by a
+// separate ray-generation launch.
 template <bool ANY, bool COUNT, int MODE, int WARPS, int SMEM_STACK, int SPILL_STACK, int MIN_BLOCKS,
-          bool BOUNDS = false, bool TIES = true, int STAGE = 0, bool LOOSE = false>
+          bool BOUNDS = false, bool TIES = true, int STAGE = 0, bool LOOSE = false, bool CAMERA = false>
 __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TraceParams p) {
     constexpr bool TLAS = MODE == MODE_SCENE;
     constexpr bool BATCH = MODE == MODE_BATCH;
     static_assert(STAGE == 0 || (!BATCH && !BOUNDS), "staged rays: single-mesh and scene launches only");
     static_assert(!LOOSE || (!TIES && !BOUNDS), "loose traversal: no near-tie flag, uploaded nodes");
+    static_assert(!CAMERA || (MODE == MODE_MESH && STAGE == 0 && !ANY), "camera rays: single-mesh closest hits");
     __shared__ int32_t s_stack[WARPS][SMEM_STACK][32];
     __shared__ __align__(128) float4 s_rays[STAGE > 0 ? WARPS : 1][2][STAGE > 0 ? STAGE * 3 : 1];
     __shared__ __align__(8) uint64_t s_rbar[STAGE > 0 ? WARPS : 1][2];
@@ -677,9 +685,15 @@ __global__ void __launch_bounds__(WARPS * 32, MIN_BLOCKS) trace_kernel(TracePara
                             out = bd.out;
                         }
                         rid = ri;
-                        const float4 o4 = ldg4(raySrc + size_t(ri) * 3);
-                        const float4 d4 = ldg4(raySrc + size_t(ri) * 3 + 1);
-                        if (p.per_ray_tmax) tmax = ldg4(raySrc + size_t(ri) * 3 + 2).x;
+                        float4 o4, d4;
+                        if (CAMERA) {
+                            // the ray made where it is traced (no ray buffer)
+                            camera_ray(p.cam, ri, o4, d4);
+                        } else {
+                            o4 = ldg4(raySrc + size_t(ri) * 3);
+                            d4 = ldg4(raySrc + size_t(ri) * 3 + 1);
+                            if (p.per_ray_tmax) tmax = ldg4(raySrc + size_t(ri) * 3 + 2).x;
+                        }
                         beginRay(o4, d4, nodesHere);
                     }
                 }

@@ -6,15 +6,17 @@ the terrain + boxes scene (512x512 value-noise heightfield over [0,100]^2,
 rays, then per hit one cosine-weighted bounce ray (closest hit) and one
 shadow ray to a directional light (any hit).  The scene and BVH are built
 once (host builder, byte-identical to the reference builder) and stay in
-HBM; each step regenerates the camera rays on the device.
+HBM; each step makes the camera rays again, inside the primary traversal
+kernel and the bounce spawn (no primary ray buffer).
 
 value   = rays traced per second over the whole pass (primary + bounce +
           shadow), CUDA events on the launching stream, L2 flushed between
           steps (a 256 MiB write), max over ranks.
 e2e     = the same pass through the C ABI call ae_rt_cast_pass with pinned
           host result buffers (results copied back inside the timed region).
-roofline: the primary closest-hit trace kernel; algorithmic bytes = per ray
-          (32 B ray read + 32 B hit write) + node fetches x 64 B + triangle
+roofline: the longest trace launch of the step; algorithmic bytes = per ray
+          (32 B ray read, none for the primary rays made in the kernel, +
+          32 B hit write) + node fetches x 64 B + triangle
           fetches x 48 B (fetch counts from the counting build of the same
           kernel); bound = L2 (the 59 MB BVH is L2-resident), peak = an L2
           copy bandwidth measured live on this GPU; the HBM fraction against
@@ -45,9 +47,9 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "atlas-engine_gb300"))
 
 W, H = 1920, 1080
-# DRAM bytes (read + write) of the primary closest-hit launch of this workload,
-# from ncu (131,451,648 + 38,613,248)
-TRAFFIC_PRIMARY_BYTES = 170_064_896
+# DRAM bytes (read + write) of the primary closest-hit launch of this workload
+# (camera rays made in the kernel), from ncu (31,899,392 + 18,045,952)
+TRAFFIC_PRIMARY_BYTES = 49_945_344
 TMIN, TINF = 0.0, 1e12
 EPSILON = 0.1
 LIGHT = (0.4, 1.0, 0.3)
@@ -1089,10 +1091,9 @@ def run_autotune(torch, dev, stream, log):
         mid = ctx.upload_mesh(bvh.nodes, gt)
 
         def run():
-            ctx.raygen(cam, bufs[0], stream)
-            ctx.trace_closest(mid, bufs[0], TMIN, TINF, out=hits[0], stream=stream, n_rays=n)
+            ctx.trace_camera_closest(mid, cam, hits[0], TMIN, TINF, stream=stream)
             counts.zero_()
-            ctx.spawn_bounce(mid, bufs[0], hits[0], n, bp, bufs[1], bufs[2], counts, stream=stream)
+            ctx.spawn_bounce_camera(mid, cam, hits[0], bp, bufs[1], bufs[2], counts, stream=stream)
             ctx.trace_closest_queue(mid, bufs[1], counts[0:1], n, TMIN, TINF, hits[1], stream=stream)
             ctx.trace_any_queue(mid, bufs[2], counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=stream)
         return run, ctx.close
@@ -1152,10 +1153,9 @@ def profile_case(args, torch, dev, stream):
         occ = torch.empty(n, dtype=torch.uint8, device=dev)
         counts = torch.zeros(4, dtype=torch.int32, device=dev)
         for _ in range(2):
-            ctx.raygen(cam, bufs[0], stream)
-            ctx.trace_closest(mid, bufs[0], TMIN, TINF, out=hits[0], stream=stream, n_rays=n)
+            ctx.trace_camera_closest(mid, cam, hits[0], TMIN, TINF, stream=stream)
             counts.zero_()
-            ctx.spawn_bounce(mid, bufs[0], hits[0], n, bp, bufs[1], bufs[2], counts, stream=stream)
+            ctx.spawn_bounce_camera(mid, cam, hits[0], bp, bufs[1], bufs[2], counts, stream=stream)
             ctx.trace_closest_queue(mid, bufs[1], counts[0:1], n, TMIN, TINF, hits[1], stream=stream)
             ctx.trace_any_queue(mid, bufs[2], counts[1:2], n, TMIN, TINF - 2 * EPSILON, occ, stream=stream)
         ctx.synchronize(stream)
@@ -1212,7 +1212,7 @@ def main():
     occ = torch.empty(n, dtype=torch.uint8, device=dev)
     counts = torch.zeros(4, dtype=torch.int32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    launches_per_step = 5
+    launches_per_step = 4
 
     side = torch.cuda.Stream(dev)
     ev_spawn, ev_shadow = torch.cuda.Event(), torch.cuda.Event()
@@ -1222,12 +1222,12 @@ def main():
             ev[cls][k].record(s)
 
     def step(ev=None):
-        ctx.raygen(cam, prim, stream)
+        # the primary rays are made inside the traversal kernel (no ray buffer)
         rec(ev, "primary", 0, stream)
-        ctx.trace_closest(mid, prim, TMIN, TINF, out=prim_hits, stream=stream, n_rays=n)
+        ctx.trace_camera_closest(mid, cam, prim_hits, TMIN, TINF, stream=stream)
         rec(ev, "primary", 1, stream)
         counts.zero_()
-        ctx.spawn_bounce(mid, prim, prim_hits, n, bp, sec, shd, counts, stream=stream)
+        ctx.spawn_bounce_camera(mid, cam, prim_hits, bp, sec, shd, counts, stream=stream)
         # the shadow trace beside the bounce trace, joined before the step ends
         ev_spawn.record(stream)
         side.wait_event(ev_spawn)
@@ -1249,6 +1249,8 @@ def main():
     n_sec, n_shd = (int(x) for x in counts[:2].cpu())
     closest_rays = n + n_sec
     rays_per_step = closest_rays + n_shd
+    # the stored primary rays for the records below that trace them from a buffer
+    ctx.raygen(cam, prim, stream)
 
     # fetch counts per ray class (counting build, outside the timed region)
     cctx = atlas_rt.Context(device=local, count_fetches=True)
@@ -1322,7 +1324,8 @@ def main():
     value = world * closest_rays / (ms * 1e-3) / 1e6
     e2e_value = world * closest_rays / (e2e * 1e-3) / 1e6
 
-    io = {"primary": 32 + 32, "bounce": 32 + 32, "shadow": 48 + 1}     # ray read + result write per ray
+    # ray read + result write per ray (the primary rays are made in the kernel)
+    io = {"primary": 32, "bounce": 32 + 32, "shadow": 48 + 1}
     nrays = {"primary": n, "bounce": n_sec, "shadow": n_shd}
     by_class = {}
     for cls in ("primary", "bounce", "shadow"):

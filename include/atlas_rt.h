@@ -571,6 +571,23 @@ ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed
                                 ae_packed_ray* secondary, ae_packed_ray* shadow, uint32_t* counts,
                                 void* stream);
 
+/* ae_rt_raygen followed by ae_rt_trace_closest of its width*height rays,
+ * with the same hits, but the rays are made inside the traversal kernel
+ * and never stored (16 B of HBM writes and reads per ray saved).  `hits`
+ * is a device buffer.  Meshes deeper than 128 levels, and contexts with
+ * AE_RT_CFG_APPROXIMATE or fetch counting, run raygen and the plain trace
+ * on context scratch instead.  Replaces the rayGen.csh dispatch of
+ * RayTracingHelper::DispatchRayGen (RayTracingHelper.cpp:147-221) and the
+ * closest-hit trace of its rays. */
+ae_rt_status ae_rt_trace_camera_closest(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam, float tmin,
+                                        float tmax, ae_hit* hits, void* stream);
+
+/* ae_rt_spawn_bounce over the width*height camera rays of `cam` (as
+ * ae_rt_raygen makes them) and their hits, without a primary ray buffer. */
+ae_rt_status ae_rt_spawn_bounce_camera(ae_rt_ctx* ctx, int32_t mesh_id, const ae_camera* cam, const ae_hit* hits,
+                                       const ae_bounce_params* params, ae_packed_ray* secondary,
+                                       ae_packed_ray* shadow, uint32_t* counts, void* stream);
+
 /* One ray-cast pass of a camera over a mesh: primary closest-hit, bounce and
  * shadow spawn, secondary closest-hit, shadow any-hit.  Output buffers may be
  * host or device memory (any may be NULL); counts receives the number of

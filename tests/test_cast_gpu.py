@@ -116,3 +116,74 @@ def test_cast_pass_cosine_distribution(ctx):
     cy = sr[:n1, 5]
     assert np.all(cy > 0)
     assert abs(cy.mean() - 2.0 / 3.0) < 0.01
+
+
+def _by_id(rows):
+    rows = rows.view(np.uint32)
+    return rows[np.argsort(rows[:, 3].view(np.int32), kind="stable")]
+
+
+@pytest.mark.parametrize("w,h", [(64, 40), (30, 17), (1920, 1080)])
+def test_camera_trace_equals_raygen_then_trace(ctx, terrain, w, h):
+    """trace_camera_closest makes each lane's ray in the traversal kernel:
+    its hits equal raygen + trace_closest word for word (partial 8x8 tiles
+    included), and spawn_bounce_camera appends the same bounce and shadow
+    rays as spawn_bounce over the stored rays (queue order differs: the
+    appends are atomics)."""
+    import torch
+    b, gt, mid = terrain
+    n = w * h
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h))
+    cam.jitter[0], cam.jitter[1] = 0.3, -0.7
+    bp = atlas_rt.make_bounce_params((0.4, 1.0, 0.3), 0.1, seed=5)
+    dev = "cuda"
+    prim = torch.zeros((n, 12), dtype=torch.float32, device=dev)
+    ref = torch.zeros((n, 8), dtype=torch.float32, device=dev)
+    got = torch.full((n, 8), -7.0, dtype=torch.float32, device=dev)
+    ctx.raygen(cam, prim)
+    ctx.trace_closest(mid, prim, 0.0, float("inf"), out=ref, n_rays=n)
+    ctx.trace_camera_closest(mid, cam, got)
+    ctx.synchronize()
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), ref.cpu().numpy().view(np.uint32))
+    qs = []
+    for camera in (False, True):
+        sec = torch.zeros((n, 12), dtype=torch.float32, device=dev)
+        shd = torch.zeros((n, 12), dtype=torch.float32, device=dev)
+        counts = torch.zeros(4, dtype=torch.int32, device=dev)
+        if camera:
+            ctx.spawn_bounce_camera(mid, cam, got, bp, sec, shd, counts)
+        else:
+            ctx.spawn_bounce(mid, prim, ref, n, bp, sec, shd, counts)
+        ctx.synchronize()
+        c = counts.cpu().numpy()
+        qs.append((c[:2].tolist(), _by_id(sec[:c[0]].cpu().numpy()), _by_id(shd[:c[1]].cpu().numpy())))
+    assert qs[0][0] == qs[1][0] and qs[0][0][0] > 0
+    assert np.array_equal(qs[0][1], qs[1][1]) and np.array_equal(qs[0][2], qs[1][2])
+
+
+def test_camera_trace_general_paths(terrain):
+    """Where the traversal kernel cannot make the rays (a tree deeper than
+    128 levels, or the approximate traversal) the camera trace writes them to
+    scratch first; the hits still equal raygen + trace_closest."""
+    import torch
+    from test_trace_gpu import chain_bvh
+    w, h = 48, 24
+    n = w * h
+    cam = atlas_rt.make_camera(scenes.pinhole_camera(w, h, eye=(0.5, 0.5, -2.0), target=(0.5, 0.5, 1.0)))
+    b, gt, _ = terrain
+    for kwargs, mesh in (({}, chain_bvh(300)), ({"approximate": True}, (b.nodes, gt))):
+        c = atlas_rt.Context(device=0, **kwargs)
+        try:
+            mid = c.upload_mesh(*mesh)
+            prim = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
+            ref = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+            got = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+            c.raygen(cam, prim)
+            c.trace_closest(mid, prim, 0.0, float("inf"), out=ref, n_rays=n)
+            c.trace_camera_closest(mid, cam, got)
+            c.synchronize()
+            r = ref.cpu().numpy()
+            assert np.array_equal(got.cpu().numpy().view(np.uint32), r.view(np.uint32))
+            assert (r[:, 0].view(np.int32) >= 0).any()
+        finally:
+            c.close()
