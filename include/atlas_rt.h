@@ -499,8 +499,11 @@ void ae_rt_batch_plan_destroy(ae_rt_batch_plan* plan);
  *    need not have passed the upload validator: node and triangle indices are
  *    range-checked on the device, and a bad one ends that ray with
  *    AE_HIT_OVERFLOW in its flags.
- *  - Results and semantics are those of ae_rt_trace_closest, with the same
- *    128-entry traversal stack per ray.  The call is
+ *  - Results and semantics are those of ae_rt_trace_closest for trees of up
+ *    to 128 levels, with the same 128-entry traversal stack per ray.  The
+ *    call does not measure the tree, so a ray that needs more entries ends
+ *    with AE_HIT_OVERFLOW (ae_rt_trace_closest, which knows each uploaded
+ *    mesh's depth, runs 1,024-entry kernels for deeper trees).  The call is
  *    asynchronous on `stream` (NULL = legacy default stream) and reports
  *    device-side failures per ray in ae_hit.flags (AE_HIT_OVERFLOW,
  *    AE_HIT_ITER_CAP) rather than through a status.
