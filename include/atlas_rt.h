@@ -576,8 +576,8 @@ ae_rt_status ae_rt_spawn_bounce(ae_rt_ctx* ctx, int32_t mesh_id, const ae_packed
 
 /* ae_rt_raygen followed by ae_rt_trace_closest of its width*height rays,
  * with the same hits, but the rays are made inside the traversal kernel
- * and never stored (16 B of HBM writes and reads per ray saved).  `hits`
- * is a device buffer.  Meshes deeper than 128 levels, and contexts with
+ * and never stored (the 32-byte ray write and read per ray saved).  `hits`
+ * is host or device memory, as for ae_rt_trace_closest.  Meshes deeper than 128 levels, and contexts with
  * AE_RT_CFG_APPROXIMATE or fetch counting, run raygen and the plain trace
  * on context scratch instead.  Replaces the rayGen.csh dispatch of
  * RayTracingHelper::DispatchRayGen (RayTracingHelper.cpp:147-221) and the

@@ -143,8 +143,11 @@ def test_camera_trace_equals_raygen_then_trace(ctx, terrain, w, h):
     ctx.raygen(cam, prim)
     ctx.trace_closest(mid, prim, 0.0, float("inf"), out=ref, n_rays=n)
     ctx.trace_camera_closest(mid, cam, got)
+    host = np.zeros((n, 8), np.float32)
+    ctx.trace_camera_closest(mid, cam, host)   # pageable host hits: through scratch and a copy
     ctx.synchronize()
     assert np.array_equal(got.cpu().numpy().view(np.uint32), ref.cpu().numpy().view(np.uint32))
+    assert np.array_equal(host.view(np.uint32), ref.cpu().numpy().view(np.uint32))
     qs = []
     for camera in (False, True):
         sec = torch.zeros((n, 12), dtype=torch.float32, device=dev)
